@@ -1,0 +1,224 @@
+/*
+ * dml.h - C ABI of the GB300 (sm_103a) implementation of din-mol-Li's
+ * per-step hot path.
+ *
+ * The reference exposes no library interface: its hot path is a set of
+ * internal procedures of `program dana` (src/dana.F90) that read
+ * host-associated globals and walk linked lists of `atom` objects.  Each entry
+ * point below replaces one of those procedures, so a driver written like
+ * dana.F90 calls `dml_ermak_a` where dana.F90 calls `ermak_a`, and so on.
+ * The replaced procedure is cited beside each declaration.
+ *
+ * Conventions
+ *  - Every call returns 0 on success or a positive `dml_status` code; the
+ *    codes mirror the reference's `werr` / `stop` sites.  `dml_strerror`
+ *    gives the message.  A failed call leaves the context usable only for
+ *    `dml_get_*`, `dml_last_error` and `dml_destroy`.
+ *  - The context owns all device memory.  Host arrays passed in are read
+ *    during the call only.
+ *  - Atom arrays are given in the order of the reference's `sys%alist`
+ *    (attachment order).  Membership of `hs%ref` is a flag per atom; the
+ *    iteration order of `hs%ref` is `sys%alist` order restricted to members,
+ *    exactly as in the reference (both lists only ever append and remove).
+ *  - A context is used from one host thread.  All work is queued on the
+ *    context's own CUDA stream; calls return after the stream is idle.
+ *  - Coordinates are Å, masses amu, time ps, energies ui = amu Å^2 ps^-2.
+ */
+#ifndef DML_H
+#define DML_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DML_ABI_VERSION 1
+
+typedef enum dml_status {
+  DML_OK = 0,
+  DML_E_ARG = 1,                 /* invalid argument */
+  DML_E_CUDA = 2,                /* CUDA runtime error (message via dml_last_error) */
+  DML_E_NOMEM = 3,               /* device or host allocation failed */
+  DML_E_OUT_OF_TESSELLATION = 4, /* src/Cells.F90:293-294 "Particle out of tessellation" */
+  DML_E_UNSORT = 5,              /* src/Cells.F90:350 "Unsort cgroup particle fail" */
+  DML_E_INDEX = 6,               /* src/Groups.F90:1088 "Index inconsistency" */
+  DML_E_NO_PARTICLES = 7,        /* src/dana.F90:624 "No more particles" */
+  DML_E_CHOSEN_MISSING = 8,      /* src/dana.F90:701 "Chosen particle does not exists" */
+  DML_E_RESERVOIR = 9,           /* src/dana.F90:423 "Unknown reservoir type" */
+  DML_E_DENDRITE = 10,           /* src/dana.F90:905-908 deposit above z0 ("supero z0", stop) */
+  DML_E_RSA = 11,                /* src/dana.F90:386-389 placement tries exhausted */
+  DML_E_OVERLAP_PASSES = 12,     /* overlap_moveback recursion exceeded the pass cap */
+  DML_E_NEIGH_OVERFLOW = 13,     /* more than mnb neighbours (src/Neighbor.F90:44) */
+  DML_E_EVENT_OVERFLOW = 14,     /* per-atom interaction bucket overflow (force path) */
+  DML_E_FIXEDPOINT_OVERFLOW = 15,/* mixed form: force beyond the int64 fixed-point range */
+  DML_E_CAPACITY = 16,           /* atom capacity exceeded */
+  DML_E_UNSUPPORTED = 17,        /* option not implemented on the device */
+  DML_E_NEAR_OVERFLOW = 18,      /* overlap near-contact bucket overflow */
+  DML_E_STATE = 19               /* call out of order (e.g. step before set_atoms) */
+} dml_status;
+
+enum { DML_INTEGRATOR_BROWNIAN = 0, DML_INTEGRATOR_ERMAK = 1 };
+enum { DML_RESERVOIR_NONE = 0, DML_RESERVOIR_PISTON = 1, DML_RESERVOIR_CHUNKS = 2, DML_RESERVOIR_GCMC = 3 };
+enum { DML_PRECISION_FP64 = 0, DML_PRECISION_MIXED = 1 };
+enum { DML_Z_LI = 1, DML_Z_CG = 2, DML_Z_F = 3 };
+
+/* Run parameters.  The reference reads them from entrada.ini / movedor.ini
+ * (src/dana.F90:309-327, 399-427) or hard-codes them (src/dana.F90:12-25,
+ * 81-100, 113).  dml_params_default fills the hard-coded values. */
+typedef struct dml_params {
+  double box[3];          /* tbox diagonal: xi, yi, box height (src/dana.F90:342-346) */
+  double z0;              /* reservoir bottom */
+  double zmax;            /* reservoir top (moves with the piston) */
+  double z1;              /* chunk-reservoir sensor top (chunks only) */
+  double h;               /* time step [ps] */
+  double gamma;           /* friction [1/ps] (src/dana.F90:15) */
+  double temp;            /* temperature [K] (src/dana.F90:17) */
+  double kb_driver;       /* kB [ui/K] of program dana, used by set_ermak (src/dana.F90:22-24) */
+  double kb_module;       /* kB [ui/K] of gems_constants, used by gcmc_run (src/Constants.F90:165-167) */
+  double eps[3][3];       /* pair epsilon [ui], index [z-1][z-1] (src/dana.F90:86-100) */
+  double r0[3][3];        /* pair r0 [Å] */
+  double mass[3];         /* masses of Li, CG, F (src/dana.F90:82-84) */
+  double rc;              /* hard-core radius = list cut radius (src/dana.F90:113) */
+  double skin;            /* nb_dcut, Verlet shell (src/Neighbor.F90:109) */
+  double prob;            /* capture probability */
+  double dif_sc;          /* Brownian diffusion above dif_switch_z */
+  double dif_sei;         /* Brownian diffusion at or below dif_switch_z */
+  double dif_switch_z;    /* 80 Å (src/dana.F90:817) */
+  double tau;             /* piston relaxation time (src/dana.F90:12) */
+  double act;             /* GCMC activity */
+  int32_t nadj;           /* GCMC trials per step */
+  int32_t integrator;     /* DML_INTEGRATOR_* */
+  int32_t reservoir;      /* DML_RESERVOIR_* */
+  int32_t precision;      /* DML_PRECISION_* */
+  int32_t mnb;            /* max neighbours per atom (reference: 10000) */
+  int32_t capacity;       /* max atoms the context can hold (0: 2 x initial count) */
+  int32_t max_passes;     /* overlap_moveback pass cap (0: 64) */
+  int32_t event_cap;      /* interacting entries per atom per step, force path (0: 64) */
+  uint64_t seed;          /* Philox key */
+} dml_params;
+
+/* Atom state in sys%alist order.  Arrays are [n] or [n][3] (x,y,z innermost).
+ * Output pointers that are NULL are skipped by dml_get_atoms. */
+typedef struct dml_atoms {
+  int32_t n;
+  double* pos;      /* [n][3] */
+  double* vel;      /* [n][3] */
+  double* acel;     /* [n][3] */
+  double* force;    /* [n][3] */
+  double* pos_old;  /* [n][3] position at the last neighbour-list build */
+  double* old_cg;   /* [n][3] position at the start of the step */
+  double* epot;     /* [n] */
+  int32_t* z;       /* DML_Z_* */
+  int8_t* skip;     /* overlap_moveback flag */
+  int8_t* in_ref;   /* member of hs%ref (mobile) */
+  int8_t* in_gcmc;  /* member of the gcmc group */
+  int64_t* id;      /* persistent atom id (Philox key) */
+} dml_atoms;
+
+/* Run counters (src/dana.F90:30-33, 50; src/Neighbor.F90:110-111). */
+typedef struct dml_counters {
+  int64_t try_;       /* capture attempts since the last reset (try) */
+  int64_t depo;       /* captures since the last reset (depo) */
+  int64_t choques;    /* ion-ion move-backs */
+  int64_t choques3;   /* unresolved piston overlaps */
+  int64_t nupd;       /* neighbour-list rebuilds (nupd_vlist) */
+  int64_t step;       /* steps done */
+  int64_t gcmc_ins;   /* accepted insertions */
+  int64_t gcmc_del;   /* accepted deletions */
+  int32_t n_atoms;    /* sys%nat */
+  int32_t n_ref;      /* hs%ref%nat */
+  int32_t max_nn;     /* largest neighbour count of the last build */
+  int32_t passes;     /* overlap passes in the last overlap_moveback */
+  double zmax;        /* current zmax */
+  double z0;          /* current z0 */
+  double rho;         /* last calc_rho */
+  double rho0;        /* initial rho */
+} dml_counters;
+
+typedef struct dml_ctx dml_ctx;
+
+/* Fills the reference's hard-coded constants (src/dana.F90:12-25,81-100,113;
+ * src/Constants.F90:165-167) and the tests/ermak run values. */
+void dml_params_default(dml_params* p);
+
+/* Creates a context on the current CUDA device.  Allocates device memory
+ * for `capacity` atoms and their neighbour lists. */
+int dml_create(const dml_params* p, dml_ctx** out);
+
+/* Loads atoms (replaces config_inic, src/dana.F90:430-517, and the gcmc
+ * attach loop :130-137).  Marks the neighbour list as not built. */
+int dml_set_atoms(dml_ctx* c, const dml_atoms* a);
+
+/* set_ermak (src/dana.F90:947-971) + test_update (:140) + fuerza (:142) +
+ * calc_rho (:145, sets rho0): the start-up sequence before the step loop. */
+int dml_setup(dml_ctx* c);
+
+/* test_update (src/Neighbor.F90:668-713): do_pbc, cell sort and the
+ * displacement test; rebuilds the Verlet list when needed.  *rebuilt is set
+ * to 1 when the list was rebuilt (may be NULL). */
+int dml_test_update(dml_ctx* c, int32_t* rebuilt);
+
+/* fuerza (src/dana.F90:1055-1139): pair forces and energies over the list. */
+int dml_force(dml_ctx* c);
+
+/* ermak_a (src/dana.F90:974-1028) with atom_pbc (:1187-1250) for step `step`. */
+int dml_ermak_a(dml_ctx* c, int64_t step);
+
+/* ermak_b (src/dana.F90:1031-1052). */
+int dml_ermak_b(dml_ctx* c);
+
+/* cbrownian_hs (src/dana.F90:798-846) with atom_pbc for step `step`. */
+int dml_brownian(dml_ctx* c, int64_t step);
+
+/* overlap_moveback (src/dana.F90:849-943) for step `step`. */
+int dml_overlap_moveback(dml_ctx* c, int64_t step);
+
+/* Capture commit loop (src/dana.F90:226-236): F -> CG, detach from hs%ref
+ * and gcmc.  *n_new may be NULL. */
+int dml_capture_commit(dml_ctx* c, int32_t* n_new);
+
+/* gcmc_run (src/dana.F90:590-713) for step `step`. */
+int dml_gcmc(dml_ctx* c, int64_t step);
+
+/* calc_rho (src/dana.F90:521-549).  *rho may be NULL. */
+int dml_calc_rho(dml_ctx* c, double* rho);
+
+/* maxz (src/dana.F90:776-794): piston compression using the last rho. */
+int dml_piston(dml_ctx* c);
+
+/* One or more iterations of the step loop body (src/dana.F90:173-265,
+ * without the output and timer lines), starting at step counter+1.  The
+ * steps are queued as one CUDA graph per call shape and replayed. */
+int dml_step(dml_ctx* c, int64_t nsteps);
+
+/* Queues nsteps like dml_step and returns without waiting. dml_sync waits. */
+int dml_step_async(dml_ctx* c, int64_t nsteps);
+int dml_sync(dml_ctx* c);
+
+/* Copies atom state to host arrays (sys%alist order).  a->n must be the
+ * array capacity on entry; it is set to the atom count on return. */
+int dml_get_atoms(dml_ctx* c, dml_atoms* a);
+
+/* Neighbour lists of hs%ref members in hs%ref order: nn[k] entries for the
+ * k-th member, written to list[k*ld ...] as sys%alist positions (0-based).
+ * Limbo entries are written as -1.  n_ref is set to the member count. */
+int dml_get_neighbors(dml_ctx* c, int32_t* n_ref, int32_t* nn, int32_t* list, int32_t ld);
+
+int dml_get_counters(dml_ctx* c, dml_counters* out);
+
+/* Resets try and depo (salida, src/dana.F90:1171-1174). */
+int dml_reset_counters(dml_ctx* c);
+
+const char* dml_strerror(int code);
+
+/* Text of the last CUDA or argument error of this context. */
+const char* dml_last_error(dml_ctx* c);
+
+void dml_destroy(dml_ctx* c);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DML_H */
