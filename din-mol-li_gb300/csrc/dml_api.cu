@@ -1,0 +1,689 @@
+// dml_api.cu - the C ABI of include/dml.h: context, device memory, the
+// host-side constants of the reference (computed in its evaluation order),
+// and the step sequence of src/dana.F90:173-265 queued on one stream and
+// replayed as a CUDA graph.
+//
+// Host floating-point code in this file is compiled with
+// -ffp-contract=off: the Ermak constants (set_ermak) and pair-table
+// products are evaluated exactly as the reference evaluates them.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/dml.h"
+#include "dml_internal.h"
+
+using namespace dml;
+
+struct dml_ctx {
+  dml_params P;
+  KParams K;
+  Dev D;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  bool loaded = false, setup_done = false;
+  int n_slots = 0, n_b = 0, n_rank = 0, n_atoms = 0;
+  std::vector<int> alist;  // hs slots in sys%alist order
+  cudaGraphExec_t step_graph = nullptr;
+  std::string last_error;
+  Scalars* h_sc = nullptr;  // pinned mirror
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+int cuda_fail(dml_ctx* c, cudaError_t e, const char* what) {
+  c->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return DML_E_CUDA;
+}
+
+#define CK(call)                                              \
+  do {                                                        \
+    cudaError_t _e = (call);                                  \
+    if (_e != cudaSuccess) return cuda_fail(c, _e, #call);    \
+  } while (0)
+
+template <class T>
+int dalloc(dml_ctx* c, T** p, size_t n) {
+  size_t bytes = sizeof(T) * (n > 0 ? n : 1);
+  cudaError_t e = cudaMalloc((void**)p, bytes);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMalloc");
+  c->allocs.push_back(*p);
+  e = cudaMemsetAsync(*p, 0, bytes, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaMemset");
+  return 0;
+}
+
+double pow6h(double x) {
+  double x2 = x * x;
+  double x4 = x2 * x2;
+  return x2 * x4;
+}
+
+// Host-side constants (see KParams).
+void make_kparams(const dml_params& P, KParams& K) {
+  std::memset(&K, 0, sizeof K);
+  double maxc = 0;
+  for (int k = 0; k < 3; ++k) {
+    K.box[k] = P.box[k];
+    K.one_box[k] = 1.0 / P.box[k];
+    K.halfbox[k] = P.box[k] * .5;
+    K.boxf[k] = (float)P.box[k];
+    K.halfboxf[k] = (float)(P.box[k] * .5);
+    K.one_boxf[k] = (float)(1.0 / P.box[k]);
+    maxc = std::max(maxc, P.box[k]);
+  }
+  maxc = 2.0 * std::max(maxc, P.zmax) + 100.0;
+  // FP32 coordinates carry at most 2^-24 relative rounding; a difference of
+  // two of them and its square stay well inside 64 ulps of maxc.
+  double margin = std::max(1e-3, 64.0 * std::ldexp(maxc, -24));
+  K.margin = (float)margin;
+  // cgroup_tessellate (Cells.F90:227-242): ncells = int(box/(rc+skin)).
+  double rcut_b = P.rc + P.skin;
+  for (int k = 0; k < 3; ++k) K.ncells[k] = (int)(P.box[k] / rcut_b);
+  K.use_cells = !(K.ncells[0] < 4 && K.ncells[1] < 4 && K.ncells[2] < 4);
+  for (int k = 0; k < 3; ++k) {
+    if (K.ncells[k] < 1) K.ncells[k] = 1;
+    K.cell[k] = P.box[k] / (double)K.ncells[k];
+    K.head_dim[k] = K.ncells[k] + 2;
+  }
+  K.rc2 = P.rc * P.rc;
+  double rl = P.rc + P.skin;
+  K.rlist2 = rl * rl;
+  K.skin = P.skin;
+  K.rlist_lo2 = (float)((rl - margin) * (rl - margin));
+  K.rlist_hi2 = (float)((rl + margin) * (rl + margin));
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double r0 = P.r0[i][j], eps = P.eps[i][j];
+      K.eps[i][j] = eps;
+      K.r0sq[i][j] = r0 * r0;
+      K.b0[i][j] = pow6h(r0);
+      K.c0[i][j] = eps * 12.0 * K.b0[i][j];
+      K.r0f_pref2[i][j] = (float)((r0 + margin) * (r0 + margin));
+    }
+  for (int t = 0; t < 3; ++t) K.mass[t] = P.mass[t];
+  // set_ermak (dana.F90:947-971)
+  const double h = P.h, gama = P.gamma;
+  double cc0 = std::exp(-h * gama);
+  double cc1 = (1.0 - cc0) / gama;
+  double cc2 = (1.0 - cc1 / h) / gama;
+  double sdr = std::sqrt(h / gama * (2.0 - (3.0 - 4.0 * cc0 + cc0 * cc0) / (h * gama)));
+  double sdv = std::sqrt(1.0 - cc0 * cc0);
+  double crv1 = (1.0 - cc0) * (1.0 - cc0) / (gama * sdr * sdv);
+  double crv2 = std::sqrt(1.0 - (crv1 * crv1));
+  double skt = std::sqrt(P.kb_driver * P.temp);
+  K.cc0 = cc0;
+  K.cc1 = cc1;
+  K.cc2 = cc2;
+  K.cc2h = cc2 * h;
+  K.cc1mcc2 = cc1 - cc2;
+  K.crv1 = crv1;
+  K.crv2 = crv2;
+  for (int t = 0; t < 3; ++t) {
+    K.rfac[t] = skt / std::sqrt(P.mass[t]) * sdr;
+    K.vfac[t] = skt / std::sqrt(P.mass[t]) * sdv;
+  }
+  // cbrownian_hs (dana.F90:817-823)
+  K.fac_sc = std::sqrt(2.0 * P.dif_sc * P.h);
+  K.fac_sei = std::sqrt(2.0 * P.dif_sei * P.h);
+  K.dif_switch_z = P.dif_switch_z;
+  K.h = P.h;
+  K.prob = P.prob;
+  K.h_over_tau = P.h / P.tau;
+  K.ztop_is_z1 = P.reservoir == DML_RESERVOIR_CHUNKS ? 1.0 : 0.0;
+  K.integrator = P.integrator;
+  K.reservoir = P.reservoir;
+  K.mnb = P.mnb;
+  K.ev_cap = P.event_cap;
+  K.max_passes = P.max_passes;
+  K.seed = P.seed;
+}
+
+int read_scalars(dml_ctx* c) {
+  CK(cudaMemcpyAsync(c->h_sc, c->D.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int finish(dml_ctx* c) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, "kernel launch");
+  int rc = read_scalars(c);
+  if (rc) return rc;
+  if (c->h_sc->error) {
+    char buf[128];
+    std::snprintf(buf, sizeof buf, "device error %d (%s), info %d", c->h_sc->error,
+                  dml_strerror(c->h_sc->error), c->h_sc->err_info);
+    c->last_error = buf;
+    return c->h_sc->error;
+  }
+  return 0;
+}
+
+int set_step(dml_ctx* c, int64_t step) {
+  long long v = step;
+  CK(cudaMemcpyAsync(&c->D.sc->step, &v, sizeof v, cudaMemcpyHostToDevice, c->stream));
+  return 0;
+}
+
+// One iteration of the loop body of dana.F90:173-265 (without salida,
+// timer_dump and the chunk reservoir), queued on the context stream.
+void enqueue_step(dml_ctx* c) {
+  const Dev& d = c->D;
+  const KParams& k = c->K;
+  cudaStream_t s = c->stream;
+  k_step_begin(d, s);
+  if (c->P.integrator == DML_INTEGRATOR_ERMAK) {
+    k_ermak_a(d, k, c->n_rank, s);
+    k_force(d, k, c->n_rank, c->n_slots, true, s);  // fuerza + ermak_b
+  } else {
+    k_brownian(d, k, c->n_rank, s);
+  }
+  k_test_update(d, k, c->n_slots, c->n_b, c->n_rank, s);
+  k_overlap(d, k, c->n_rank, c->n_slots, s);
+  k_test_update(d, k, c->n_slots, c->n_b, c->n_rank, s);
+  k_capture_commit(d, k, c->n_rank, s);
+  k_calc_rho(d, k, c->n_slots, s);
+  if (c->P.reservoir == DML_RESERVOIR_PISTON) k_piston(d, k, c->n_slots, s);
+}
+
+int build_step_graph(dml_ctx* c) {
+  if (c->step_graph) return 0;
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_step(c);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&c->step_graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void dml_params_default(dml_params* p) {
+  std::memset(p, 0, sizeof *p);
+  // program dana (dana.F90:22-24): kB_ui = kB_eVK * eV_ui, eV_ui = 96.485 * 100.
+  const double eV_ui = 96.485 * 100.0;
+  // gems_constants (Constants.F90:105-167): kB_ui = kB_ev / (axps_mxs^2 uma_kg joule_ev).
+  const double joule_ev = 1.0 / 1.60219e-19;
+  const double ui_ev = 1.0e2 * 1.0e2 * 1.6605402e-27 * joule_ev;
+  const double ev_ui = 1.0 / ui_ev;
+  p->box[0] = 100.0;
+  p->box[1] = 100.0;
+  p->box[2] = 200.0;
+  p->z0 = 100.0;
+  p->zmax = 200.0;
+  p->h = 1.e-2;
+  p->gamma = 1.0;
+  p->temp = 300.0;
+  p->kb_driver = 8.617330350e-5 * eV_ui;
+  p->kb_module = 8.617385e-05 * ev_ui;
+  // Pair tables (dana.F90:86-100), index [z-1][z-1]: 1 Li, 2 CG, 3 F.
+  p->r0[1][0] = p->r0[0][1] = 3.5;
+  p->eps[0][0] = 2313.6;
+  p->r0[0][0] = 3.2;
+  p->eps[2][2] = 121.0;
+  p->r0[2][2] = 3.61;
+  p->eps[0][2] = p->eps[2][0] = 529.1;
+  p->r0[0][2] = p->r0[2][0] = 1.564;
+  p->mass[0] = p->mass[1] = p->mass[2] = 6.94;
+  p->rc = 3.2;
+  p->skin = 10.0;
+  p->prob = 1.0;
+  p->dif_sc = 250.0;
+  p->dif_sei = 250.0;
+  p->dif_switch_z = 80.0;
+  p->tau = 0.1;
+  p->integrator = DML_INTEGRATOR_ERMAK;
+  p->reservoir = DML_RESERVOIR_PISTON;
+  p->precision = DML_PRECISION_FP64;
+  p->mnb = 1024;
+  p->max_passes = 64;
+  p->event_cap = 64;
+}
+
+const char* dml_strerror(int code) {
+  switch (code) {
+    case DML_OK: return "ok";
+    case DML_E_ARG: return "invalid argument";
+    case DML_E_CUDA: return "CUDA error";
+    case DML_E_NOMEM: return "out of memory";
+    case DML_E_OUT_OF_TESSELLATION: return "Particle out of tessellation";
+    case DML_E_UNSORT: return "Unsort cgroup particle fail";
+    case DML_E_INDEX: return "Index inconsistency";
+    case DML_E_NO_PARTICLES: return "No more particles";
+    case DML_E_CHOSEN_MISSING: return "Chosen particle does not exists";
+    case DML_E_RESERVOIR: return "Unknown reservoir type";
+    case DML_E_DENDRITE: return "deposit above z0 (dendrite reached the reservoir)";
+    case DML_E_RSA: return "maximum number of placement tries reached";
+    case DML_E_OVERLAP_PASSES: return "overlap_moveback exceeded the pass cap";
+    case DML_E_NEIGH_OVERFLOW: return "more neighbours than mnb";
+    case DML_E_EVENT_OVERFLOW: return "too many interacting entries for one atom";
+    case DML_E_FIXEDPOINT_OVERFLOW: return "force beyond the fixed-point range";
+    case DML_E_CAPACITY: return "atom capacity exceeded";
+    case DML_E_UNSUPPORTED: return "option not supported on the device";
+    case DML_E_NEAR_OVERFLOW: return "too many near contacts";
+    case DML_E_STATE: return "call out of order";
+    default: return "unknown error";
+  }
+}
+
+const char* dml_last_error(dml_ctx* c) { return c ? c->last_error.c_str() : "no context"; }
+
+int dml_create(const dml_params* p, dml_ctx** out) {
+  if (!p || !out) return DML_E_ARG;
+  *out = nullptr;
+  if (p->reservoir < 0 || p->reservoir > 3) return DML_E_RESERVOIR;
+  if (p->reservoir == DML_RESERVOIR_CHUNKS || p->reservoir == DML_RESERVOIR_GCMC)
+    return DML_E_UNSUPPORTED;
+  if (p->precision != DML_PRECISION_FP64) return DML_E_UNSUPPORTED;
+  if (!(p->box[0] > 0 && p->box[1] > 0 && p->box[2] > 0 && p->h > 0 && p->rc > 0)) return DML_E_ARG;
+  // The FP32 pre-filters assume the minimum image is unambiguous at every cut-off.
+  double rmax = p->rc + p->skin;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) rmax = std::max(rmax, p->r0[i][j]);
+  if (p->box[0] * 0.5 <= rmax + 0.01 || p->box[1] * 0.5 <= rmax + 0.01) return DML_E_ARG;
+  dml_ctx* c = new dml_ctx();
+  c->P = *p;
+  if (c->P.mnb <= 0) c->P.mnb = 1024;
+  if (c->P.max_passes <= 0) c->P.max_passes = 64;
+  if (c->P.event_cap <= 0) c->P.event_cap = 64;
+  if (c->P.event_cap > 128) c->P.event_cap = 128;
+  make_kparams(c->P, c->K);
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_sc, sizeof(Scalars));
+  if (e != cudaSuccess) {
+    delete c;
+    return DML_E_CUDA;
+  }
+  *out = c;
+  return 0;
+}
+
+void dml_destroy(dml_ctx* c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->h_sc) cudaFreeHost(c->h_sc);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
+  if (!c || !a || a->n <= 0 || !a->pos || !a->z) return DML_E_ARG;
+  if (c->loaded) return DML_E_STATE;
+  const int n = a->n;
+  const int cap = std::max(n, c->P.capacity);
+  c->P.capacity = cap;
+  Dev& d = c->D;
+  d.cap = cap;
+  const KParams& K = c->K;
+  int rc = 0;
+#define AL(ptr, cnt) \
+  if ((rc = dalloc(c, &(ptr), (cnt))) != 0) return rc;
+  AL(d.pos, cap);
+  AL(d.vel, cap);
+  AL(d.acel, cap);
+  AL(d.force, cap);
+  AL(d.old_cg, cap);
+  AL(d.pos_old, cap);
+  AL(d.ranv, cap);
+  AL(d.posf, cap);
+  AL(d.epot, cap);
+  AL(d.typ, cap);
+  AL(d.skip, cap);
+  AL(d.state, cap);
+  AL(d.active, cap);
+  AL(d.id, cap);
+  AL(d.rank, cap);
+  AL(d.bslot, cap);
+  AL(d.ref, cap);
+  AL(d.b2hs, cap);
+  AL(d.nn, cap);
+  AL(d.list, (size_t)cap * c->P.mnb);
+  d.ncell_tot = K.use_cells ? K.head_dim[0] * K.head_dim[1] * K.head_dim[2] : 1;
+  AL(d.cell_of, cap);
+  AL(d.cell_count, d.ncell_tot + 1);
+  AL(d.cell_start, d.ncell_tot + 1);
+  AL(d.cell_fill, d.ncell_tot + 1);
+  AL(d.cell_atoms, cap);
+  AL(d.ev_count, cap);
+  AL(d.ev, (size_t)cap * c->P.event_cap);
+  AL(d.near_count, cap);
+  AL(d.near, (size_t)cap * kNearCap);
+  AL(d.uf, cap);
+  AL(d.comp_size, cap);
+  AL(d.comp_id, cap);
+  AL(d.comp_off, cap);
+  AL(d.comp_fill, cap);
+  AL(d.comp_members, cap);
+  AL(d.comp_list, 2 * (size_t)cap);
+  d.nblk_part = (cap + kBlock - 1) / kBlock + 1;
+  AL(d.part, 2 * (size_t)d.nblk_part);
+  AL(d.sc, 1);
+#undef AL
+
+  // Host staging in slot order (slot = position in the array).
+  std::vector<double4> pos(n), vel(n), acel(n), force(n), pos_old(n), old_cg(n);
+  std::vector<float4> posf(n);
+  std::vector<double> epot(n);
+  std::vector<int8_t> typ(n), skip(n), state(n, ST_LIVE);
+  std::vector<long long> id(n);
+  std::vector<int> rank(n, -1), ref, slot(n);
+  int64_t max_id = -1;
+  for (int i = 0; i < n; ++i) {
+    auto v3 = [&](const double* src, double def) {
+      if (!src) return make_double4(def, def, def, 0.0);
+      return make_double4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.0);
+    };
+    int z = a->z[i];
+    if (z < 1 || z > 3) return DML_E_ARG;
+    pos[i] = v3(a->pos, 0.0);
+    vel[i] = v3(a->vel, 0.0);
+    acel[i] = v3(a->acel, 0.0);
+    force[i] = v3(a->force, 0.0);
+    pos_old[i] = a->pos_old ? v3(a->pos_old, 0.0) : pos[i];
+    old_cg[i] = v3(a->old_cg, 1e8);
+    epot[i] = a->epot ? a->epot[i] : 0.0;
+    typ[i] = (int8_t)z;
+    skip[i] = a->skip ? (a->skip[i] != 0) : 0;
+    id[i] = a->id ? a->id[i] : i;
+    max_id = std::max<int64_t>(max_id, id[i]);
+    posf[i] = make_float4((float)pos[i].x, (float)pos[i].y, (float)pos[i].z, (float)z);
+    bool in_ref = a->in_ref ? a->in_ref[i] != 0 : (z != DML_Z_CG);
+    if (in_ref) {
+      rank[i] = (int)ref.size();
+      ref.push_back(i);
+    }
+    slot[i] = i;
+  }
+  cudaStream_t s = c->stream;
+  CK(cudaMemcpyAsync(d.pos, pos.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.vel, vel.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.acel, acel.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.force, force.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.pos_old, pos_old.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.old_cg, old_cg.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.posf, posf.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.epot, epot.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.typ, typ.data(), n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.skip, skip.data(), n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.state, state.data(), n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.id, id.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.rank, rank.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.bslot, slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.b2hs, slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  if (!ref.empty())
+    CK(cudaMemcpyAsync(d.ref, ref.data(), sizeof(int) * ref.size(), cudaMemcpyHostToDevice, s));
+  Scalars sc;
+  std::memset(&sc, 0, sizeof sc);
+  sc.zmax = c->P.zmax;
+  sc.z0 = c->P.z0;
+  sc.z1 = c->P.z1;
+  sc.n_slots = n;
+  sc.n_b = n;
+  sc.n_rank = (int)ref.size();
+  sc.n_ref = (int)ref.size();
+  sc.n_atoms = n;
+  *c->h_sc = sc;
+  CK(cudaMemcpyAsync(d.sc, c->h_sc, sizeof sc, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  c->n_slots = n;
+  c->n_b = n;
+  c->n_rank = (int)ref.size();
+  c->n_atoms = n;
+  c->alist.resize(n);
+  for (int i = 0; i < n; ++i) c->alist[i] = i;
+  c->loaded = true;
+  return 0;
+}
+
+int dml_test_update(dml_ctx* c, int32_t* rebuilt) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  k_test_update(c->D, c->K, c->n_slots, c->n_b, c->n_rank, c->stream);
+  int rc = finish(c);
+  if (rc) return rc;
+  if (rebuilt) *rebuilt = c->h_sc->rebuild;
+  return 0;
+}
+
+int dml_force(dml_ctx* c) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  k_force(c->D, c->K, c->n_rank, c->n_slots, false, c->stream);
+  return finish(c);
+}
+
+int dml_ermak_a(dml_ctx* c, int64_t step) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  int rc = set_step(c, step);
+  if (rc) return rc;
+  k_ermak_a(c->D, c->K, c->n_rank, c->stream);
+  return finish(c);
+}
+
+int dml_ermak_b(dml_ctx* c) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  k_ermak_b(c->D, c->K, c->n_rank, c->stream);
+  return finish(c);
+}
+
+int dml_brownian(dml_ctx* c, int64_t step) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  int rc = set_step(c, step);
+  if (rc) return rc;
+  k_brownian(c->D, c->K, c->n_rank, c->stream);
+  return finish(c);
+}
+
+int dml_overlap_moveback(dml_ctx* c, int64_t step) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  int rc = set_step(c, step);
+  if (rc) return rc;
+  k_overlap(c->D, c->K, c->n_rank, c->n_slots, c->stream);
+  return finish(c);
+}
+
+int dml_capture_commit(dml_ctx* c, int32_t* n_new) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  int zero = 0;
+  CK(cudaMemcpyAsync(&c->D.sc->n_new_cg, &zero, sizeof zero, cudaMemcpyHostToDevice, c->stream));
+  k_capture_commit(c->D, c->K, c->n_rank, c->stream);
+  int rc = finish(c);
+  if (rc) return rc;
+  if (n_new) *n_new = c->h_sc->n_new_cg;
+  return 0;
+}
+
+int dml_gcmc(dml_ctx* c, int64_t step) {
+  (void)step;
+  if (!c || !c->loaded) return DML_E_STATE;
+  return DML_E_UNSUPPORTED;
+}
+
+int dml_calc_rho(dml_ctx* c, double* rho) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  k_calc_rho(c->D, c->K, c->n_slots, c->stream);
+  int rc = finish(c);
+  if (rc) return rc;
+  if (rho) *rho = c->h_sc->rho;
+  return 0;
+}
+
+int dml_piston(dml_ctx* c) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  k_piston(c->D, c->K, c->n_slots, c->stream);
+  return finish(c);
+}
+
+int dml_setup(dml_ctx* c) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  int rc = dml_test_update(c, nullptr);
+  if (rc) return rc;
+  if (c->P.integrator == DML_INTEGRATOR_ERMAK) {
+    rc = dml_force(c);
+    if (rc) return rc;
+  }
+  double rho = 0;
+  rc = dml_calc_rho(c, &rho);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(&c->D.sc->rho0, &rho, sizeof rho, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->setup_done = true;
+  return 0;
+}
+
+int dml_step_async(dml_ctx* c, int64_t nsteps) {
+  if (!c || !c->loaded || !c->setup_done) return DML_E_STATE;
+  int rc = build_step_graph(c);
+  if (rc) return rc;
+  for (int64_t i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(c->step_graph, c->stream));
+  return 0;
+}
+
+int dml_sync(dml_ctx* c) {
+  if (!c) return DML_E_ARG;
+  return finish(c);
+}
+
+int dml_step(dml_ctx* c, int64_t nsteps) {
+  int rc = dml_step_async(c, nsteps);
+  if (rc) return rc;
+  return finish(c);
+}
+
+int dml_get_counters(dml_ctx* c, dml_counters* o) {
+  if (!c || !o) return DML_E_ARG;
+  std::memset(o, 0, sizeof *o);
+  if (!c->loaded) return 0;
+  int rc = read_scalars(c);
+  if (rc) return rc;
+  const Scalars& s = *c->h_sc;
+  o->try_ = (int64_t)s.try_;
+  o->depo = (int64_t)s.depo;
+  o->choques = (int64_t)s.choques;
+  o->choques3 = (int64_t)s.choques3;
+  o->nupd = (int64_t)s.nupd;
+  o->step = s.step;
+  o->gcmc_ins = (int64_t)s.gcmc_ins;
+  o->gcmc_del = (int64_t)s.gcmc_del;
+  o->n_atoms = s.n_atoms;
+  o->n_ref = s.n_ref;
+  o->max_nn = s.max_nn;
+  o->passes = s.passes;
+  o->zmax = s.zmax;
+  o->z0 = s.z0;
+  o->rho = s.rho;
+  o->rho0 = s.rho0;
+  return 0;
+}
+
+int dml_reset_counters(dml_ctx* c) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  unsigned long long z[2] = {0, 0};
+  CK(cudaMemcpyAsync(&c->D.sc->try_, &z[0], sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                     c->stream));
+  CK(cudaMemcpyAsync(&c->D.sc->depo, &z[1], sizeof(unsigned long long), cudaMemcpyHostToDevice,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int dml_get_atoms(dml_ctx* c, dml_atoms* a) {
+  if (!c || !a) return DML_E_ARG;
+  if (!c->loaded) return DML_E_STATE;
+  const int n = (int)c->alist.size();
+  if (a->n < n) return DML_E_ARG;
+  const int ns = c->n_slots;
+  const Dev& d = c->D;
+  cudaStream_t s = c->stream;
+  std::vector<double4> pos(ns), vel(ns), acel(ns), force(ns), pos_old(ns), old_cg(ns);
+  std::vector<double> epot(ns);
+  std::vector<int8_t> typ(ns), skip(ns);
+  std::vector<long long> id(ns);
+  std::vector<int> rank(ns);
+  CK(cudaMemcpyAsync(pos.data(), d.pos, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
+  if (a->vel) CK(cudaMemcpyAsync(vel.data(), d.vel, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
+  if (a->acel) CK(cudaMemcpyAsync(acel.data(), d.acel, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
+  if (a->force) CK(cudaMemcpyAsync(force.data(), d.force, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
+  if (a->pos_old) CK(cudaMemcpyAsync(pos_old.data(), d.pos_old, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
+  if (a->old_cg) CK(cudaMemcpyAsync(old_cg.data(), d.old_cg, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
+  if (a->epot) CK(cudaMemcpyAsync(epot.data(), d.epot, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(typ.data(), d.typ, ns, cudaMemcpyDeviceToHost, s));
+  if (a->skip) CK(cudaMemcpyAsync(skip.data(), d.skip, ns, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(id.data(), d.id, sizeof(long long) * ns, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(rank.data(), d.rank, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  a->n = n;
+  for (int i = 0; i < n; ++i) {
+    int h = c->alist[i];
+    auto put = [&](double* dst, const double4& v) {
+      if (!dst) return;
+      dst[3 * i] = v.x;
+      dst[3 * i + 1] = v.y;
+      dst[3 * i + 2] = v.z;
+    };
+    put(a->pos, pos[h]);
+    put(a->vel, vel[h]);
+    put(a->acel, acel[h]);
+    put(a->force, force[h]);
+    put(a->pos_old, pos_old[h]);
+    put(a->old_cg, old_cg[h]);
+    if (a->epot) a->epot[i] = epot[h];
+    if (a->z) a->z[i] = typ[h];
+    if (a->skip) a->skip[i] = skip[h];
+    if (a->in_ref) a->in_ref[i] = rank[h] >= 0 ? 1 : 0;
+    if (a->in_gcmc) a->in_gcmc[i] = 0;
+    if (a->id) a->id[i] = id[h];
+  }
+  return 0;
+}
+
+int dml_get_neighbors(dml_ctx* c, int32_t* n_ref, int32_t* nn, int32_t* list, int32_t ld) {
+  if (!c || !n_ref || !nn || !list) return DML_E_ARG;
+  if (!c->loaded) return DML_E_STATE;
+  const Dev& d = c->D;
+  cudaStream_t s = c->stream;
+  const int ns = c->n_slots, mnb = c->P.mnb;
+  std::vector<int> ref(c->n_rank), hnn(ns), state8(ns);
+  std::vector<int8_t> st(ns);
+  if (c->n_rank)
+    CK(cudaMemcpyAsync(ref.data(), d.ref, sizeof(int) * c->n_rank, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(hnn.data(), d.nn, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(st.data(), d.state, ns, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  std::vector<int> pos_of(ns, -1);
+  for (size_t i = 0; i < c->alist.size(); ++i) pos_of[c->alist[i]] = (int)i;
+  std::vector<int> row(mnb);
+  int k = 0;
+  for (int r = 0; r < c->n_rank; ++r) {
+    int h = ref[r];
+    if (h < 0) continue;
+    int cnt = hnn[h];
+    if (cnt > ld) return DML_E_ARG;
+    if (cnt) {
+      CK(cudaMemcpy(row.data(), d.list + (size_t)h * mnb, sizeof(int) * cnt, cudaMemcpyDeviceToHost));
+    }
+    nn[k] = cnt;
+    for (int q = 0; q < cnt; ++q) {
+      int j = row[q];
+      list[(size_t)k * ld + q] = st[j] == ST_LIMBO ? -1 : pos_of[j];
+    }
+    ++k;
+  }
+  *n_ref = k;
+  return 0;
+}
+
+}  // extern "C"

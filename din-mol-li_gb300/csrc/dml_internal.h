@@ -1,0 +1,137 @@
+// dml_internal.h - device data layout and kernel launchers shared by the
+// C-ABI host code (dml_api.cu) and the kernels (dml_kernels.cu).
+//
+// Layout in HBM.  Atoms are addressed by their slot in the reference's
+// `hs` ngroup index (src/Neighbor.F90:32-79); the neighbour list stores hs
+// slots, so every per-atom array is indexed by hs slot:
+//   pos      double4 (x, y, z, 0)            32 B, one sector per gather
+//   posf     float4  (x, y, z, element)      16 B, the FP32 pre-filter copy
+//   vel, acel, force, old_cg, pos_old, ranv  double4
+//   epot double, typ/skip/state int8, id int64, rank/bslot int32
+// `ref` holds hs slots in hs%ref order (holes = -1 after captures); ranks
+// are positions in it.  The Verlet list is row-major [slot][mnb] int32.
+// Cells are a counting sort of hs%b slots into (n1+2)(n2+2)(n3+2) bins,
+// each bin ordered by descending b slot (the LIFO chains of
+// src/Cells.F90:299-300).
+#ifndef DML_INTERNAL_H
+#define DML_INTERNAL_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/dml.h"
+
+namespace dml {
+
+enum { ST_NULL = 0, ST_LIVE = 1, ST_LIMBO = 2 };
+
+constexpr int kNearCap = 32;   // near-contact entries per atom (overlap)
+constexpr int kBlock = 256;
+
+// Device scalars (one struct in device memory per context).
+struct Scalars {
+  double zmax, z0, z1, rho, rho0, lohi;
+  unsigned long long delta2_bits;   // max |pos - old_cg|^2 over hs%ref (as bits)
+  unsigned long long d1_bits, d2_bits; // unused slot (kept for alignment)
+  long long step;
+  unsigned long long try_, depo, choques, choques3, nupd, gcmc_ins, gcmc_del;
+  int n_slots;     // hs%amax
+  int n_b;         // hs%b%amax
+  int n_rank;      // rank slots in use (members + holes)
+  int n_ref;       // hs%ref%nat
+  int n_atoms;     // sys%nat
+  int listed;      // neighbour list built
+  int rebuild;     // set by the displacement test
+  int error;       // first dml_status raised on the device
+  int err_info;
+  int again;       // overlap pass produced a move-back
+  int passes;      // passes of the last overlap_moveback
+  int n_comp;      // overlap components
+  int comp_total;  // members over all components
+  int max_nn;
+  unsigned int ticket;   // last-block-done counters
+  unsigned int ticket2;
+  int rho_count;
+  int n_new_cg;
+};
+
+struct EvRec {            // one interacting list entry seen from one atom
+  unsigned long long key; // rank(o1) << 32 | jj : the reference's summation order
+  double fx, fy, fz;      // aux*vd/dr of the entry (o1 - o2 orientation)
+  double e;               // aux*0.5
+  int sign;               // +1 o1 side (force += t), -1 o2 side (force -= t)
+  int pad;
+};
+
+// Constants computed on the host with the reference's operation order and
+// passed by value to every kernel.
+struct KParams {
+  double box[3], one_box[3], halfbox[3];
+  double cell[3];
+  int ncells[3];
+  int head_dim[3];          // ncells + 2
+  int use_cells;
+  double rc2;               // rc*rc (hs%rcut2)
+  double rlist2;            // (rc+skin)^2
+  double skin;
+  double eps[3][3], r0sq[3][3], b0[3][3], c0[3][3];  // b0 = r0^6, c0 = eps*12*b0
+  float r0f_pref2[3][3];    // FP32 pre-filter thresholds (r0 + margin)^2
+  float rlist_lo2, rlist_hi2; // list shell bounds (FP32)
+  float margin;             // FP32 position error bound
+  float boxf[3], halfboxf[3], one_boxf[3];
+  double mass[3];
+  // Ermak (set_ermak, dana.F90:947-971)
+  double cc0, cc1, cc2, cc2h, cc1mcc2, crv1, crv2;
+  double rfac[3], vfac[3];  // (skt/sqrt(m))*sdr, (skt/sqrt(m))*sdv per element
+  // Brownian
+  double fac_sc, fac_sei, dif_switch_z, h;
+  double prob;
+  double h_over_tau;
+  double ztop_is_z1;        // chunks: calc_rho uses z1
+  int integrator, reservoir;
+  int mnb, ev_cap, max_passes;
+  unsigned long long seed;
+};
+
+// All device buffers of one context.
+struct Dev {
+  double4 *pos, *vel, *acel, *force, *old_cg, *pos_old, *ranv;
+  float4* posf;
+  double* epot;
+  int8_t *typ, *skip, *state, *active;
+  long long* id;
+  int *rank, *bslot, *ref, *b2hs;
+  int *nn, *list;
+  // cells
+  int *cell_of, *cell_count, *cell_start, *cell_fill, *cell_atoms;
+  int ncell_tot;
+  // force events
+  int* ev_count;
+  EvRec* ev;
+  // overlap
+  int *near_count, *near, *uf, *comp_size, *comp_id, *comp_off, *comp_fill, *comp_members, *comp_list;
+  // reductions
+  double* part;       // per-block partials (top-2)
+  int nblk_part;
+  Scalars* sc;
+  int cap;            // atom capacity (hs slots, b slots, ranks)
+};
+
+// ---- kernel launchers (dml_kernels.cu) ----
+void k_step_begin(const Dev& d, cudaStream_t s);
+void k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
+void k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
+void k_force(const Dev& d, const KParams& p, int n_rank, int n_slots, bool fuse_ermak_b,
+             cudaStream_t s);
+void k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
+void k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
+                   cudaStream_t s);
+void k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStream_t s);
+void k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
+void k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
+void k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
+void k_force_setup(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStream_t s);
+
+}  // namespace dml
+
+#endif

@@ -1,0 +1,1092 @@
+// dml_kernels.cu - sm_103a kernels of the plain FP64 form.
+//
+// Compiled with --fmad=false: no multiply-add is contracted, and every
+// expression is written in the reference's evaluation order, so each kernel
+// reproduces the serial reference bit for bit (double add, multiply, divide
+// and sqrt are IEEE round-to-nearest on the device as on the host).
+//
+// Where work can be skipped without changing a bit of the result it is
+// skipped: list entries are pre-filtered with FP32 distances carrying a
+// rigorous error margin (the FP64 test decides every entry near a cut-off),
+// and entries whose pair epsilon is zero add signed zeros, which leave a sum
+// started at +0 unchanged.
+#include <cuda_runtime.h>
+
+#include "../../include/dml_rng.h"
+#include "dml_internal.h"
+
+namespace dml {
+
+namespace {
+
+__constant__ int c_map[27][3] = {
+    {0, 0, 0},   {1, 0, 0},   {1, 1, 0},    {0, 1, 0},   {-1, 1, 0},  {1, 0, -1}, {1, 1, -1},
+    {0, 1, -1},  {-1, 1, -1}, {1, 0, 1},    {1, 1, 1},   {0, 1, 1},   {-1, 1, 1}, {0, 0, 1},
+    {-1, 0, 0},  {-1, -1, 0}, {0, -1, 0},   {1, -1, 0},  {-1, 0, 1},  {-1, -1, 1}, {0, -1, 1},
+    {1, -1, 1},  {-1, 0, -1}, {-1, -1, -1}, {0, -1, -1}, {1, -1, -1}, {0, 0, -1}};
+
+__device__ __forceinline__ void raise_error(Scalars* sc, int code, int info) {
+  if (atomicCAS(&sc->error, 0, code) == 0) sc->err_info = info;
+}
+
+__device__ __forceinline__ unsigned long long* u64(unsigned long long* p) { return p; }
+
+__device__ __forceinline__ void count_add(unsigned long long* c, unsigned long long v) {
+  atomicAdd(c, v);
+}
+
+__device__ __forceinline__ float4 to_f4(double4 p, int typ) {
+  return make_float4((float)p.x, (float)p.y, (float)p.z, (float)typ);
+}
+
+__device__ __forceinline__ double dot3(double x, double y, double z) {
+  // dot_product as the reference evaluates it: ((0 + x*x) + y*y) + z*z.
+  return (x * x + y * y) + z * z;
+}
+
+// x^6 = x^2 * x^4 and x^7 = (x * x^2) * x^4 (square-and-multiply), the
+// evaluation of dana.F90:1117-1120 pinned by the reference's Ermak golden.
+__device__ __forceinline__ double pow6(double x) {
+  double x2 = x * x;
+  double x4 = x2 * x2;
+  return x2 * x4;
+}
+__device__ __forceinline__ double pow7(double x) {
+  double x2 = x * x;
+  double x3 = x * x2;
+  double x4 = x2 * x2;
+  return x3 * x4;
+}
+
+// vdistance (Groups.F90:995-1016): a - b, minimum image by idnint (round half
+// away from zero) in x and y; z is not periodic.
+__device__ __forceinline__ void vdist_nint(const KParams& p, double4 a, double4 b, double& x,
+                                           double& y, double& z) {
+  x = a.x - b.x;
+  y = a.y - b.y;
+  z = a.z - b.z;
+  x = x - p.box[0] * round(x * p.one_box[0]);
+  y = y - p.box[1] * round(y * p.one_box[1]);
+}
+
+__device__ __forceinline__ void vdist_nint_f(const KParams& p, float4 a, float4 b, float& x,
+                                             float& y, float& z) {
+  x = a.x - b.x;
+  y = a.y - b.y;
+  z = a.z - b.z;
+  x = x - p.boxf[0] * rintf(x * p.one_boxf[0]);
+  y = y - p.boxf[1] * rintf(y * p.one_boxf[1]);
+}
+
+__device__ __forceinline__ int warp_id_global() {
+  return (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+}
+
+// ----------------------------------------------------------------- step
+__global__ void step_begin_kernel(Scalars* sc) { sc->step += 1; }
+
+// atom_pbc (dana.F90:1187-1250) on registers; returns true when deposited.
+__device__ __forceinline__ bool atom_pbc_dev(const KParams& p, Scalars* sc, long long step,
+                                             long long id, double* pp, double4& po, bool& po_changed,
+                                             double4& vv, bool& v_changed, const double4& oc,
+                                             int& typ, double zmax) {
+  bool depos = false;
+  double pox[2] = {po.x, po.y};
+  for (int j = 0; j < 2; ++j) {
+    if (pp[j] > p.box[j]) {
+      pp[j] = pp[j] - p.box[j];
+      pox[j] = pox[j] - p.box[j];
+      po_changed = true;
+    }
+    if (pp[j] < 0.0) {
+      pp[j] = pp[j] + p.box[j];
+      pox[j] = pox[j] + p.box[j];
+      po_changed = true;
+    }
+  }
+  po.x = pox[0];
+  po.y = pox[1];
+  if (pp[2] > zmax) {
+    if (p.integrator == DML_INTEGRATOR_ERMAK) {
+      pp[2] = pp[2] - 2.0 * (pp[2] - zmax);
+      vv.z = -vv.z;
+      v_changed = true;
+    } else {
+      pp[0] = oc.x;
+      pp[1] = oc.y;
+      pp[2] = oc.z;
+    }
+  }
+  if (pp[2] <= 0.0) {
+    count_add(&sc->try_, 1ull);
+    double ne = dml_uniform(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_CAPTURE, 0));
+    if (ne < p.prob) {
+      count_add(&sc->depo, 1ull);
+      typ = DML_Z_F;
+      depos = true;
+    }
+    pp[0] = oc.x;
+    pp[1] = oc.y;
+    pp[2] = oc.z;
+  }
+  return depos;
+}
+
+// ermak_a (dana.F90:974-1028): one thread per hs%ref member.
+__global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rank) return;
+  int h = d.ref[r];
+  if (h < 0) return;
+  Scalars* sc = d.sc;
+  long long step = sc->step;
+  double zmax = sc->zmax;
+  double4 P = d.pos[h];
+  double4 V = d.vel[h];
+  double4 A = d.acel[h];
+  int typ = d.typ[h];
+  long long id = d.id[h];
+  double rf = p.rfac[typ - 1], vf = p.vfac[typ - 1];
+  double pp[3] = {P.x, P.y, P.z};
+  double vv[3] = {V.x, V.y, V.z};
+  double aa[3] = {A.x, A.y, A.z};
+  double rv[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    double r1, r2;
+    dml_normal_pair(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_ERMAK, (uint32_t)j), &r1, &r2);
+    double ranr = rf * r1;
+    pp[j] = pp[j] + p.cc1 * vv[j] + p.cc2h * aa[j] + ranr;
+    rv[j] = vf * (p.crv1 * r1 + p.crv2 * r2);
+  }
+  double4 po = d.pos_old[h];
+  bool po_changed = false, v_changed = false;
+  int typ0 = typ;
+  bool depos = atom_pbc_dev(p, sc, step, id, pp, po, po_changed, V, v_changed, P, typ, zmax);
+  double4 np = make_double4(pp[0], pp[1], pp[2], 0.0);
+  d.old_cg[h] = P;
+  d.pos[h] = np;
+  d.posf[h] = to_f4(np, typ);
+  d.ranv[h] = make_double4(rv[0], rv[1], rv[2], 0.0);
+  if (po_changed) d.pos_old[h] = po;
+  if (v_changed) d.vel[h] = V;
+  if (typ != typ0) d.typ[h] = (int8_t)typ;
+  if (!depos) d.skip[h] = 0;
+}
+
+// cbrownian_hs (dana.F90:798-846): one thread per hs%ref member.
+__global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rank) return;
+  int h = d.ref[r];
+  if (h < 0) return;
+  Scalars* sc = d.sc;
+  long long step = sc->step;
+  double zmax = sc->zmax;
+  double4 P = d.pos[h];
+  int typ = d.typ[h];
+  long long id = d.id[h];
+  double fac = P.z > p.dif_switch_z ? p.fac_sc : p.fac_sei;
+  double nrm[4];
+  dml_normal_pair(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_BROWN, 0), &nrm[0], &nrm[1]);
+  dml_normal_pair(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_BROWN, 1), &nrm[2], &nrm[3]);
+  double pp[3] = {P.x, P.y, P.z};
+  double vv[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    double posold = pp[j];
+    pp[j] = posold + nrm[j] * fac;
+    vv[j] = (pp[j] - posold) / p.h;
+  }
+  double4 V = make_double4(vv[0], vv[1], vv[2], 0.0);
+  double4 po = d.pos_old[h];
+  bool po_changed = false, v_changed = false;
+  int typ0 = typ;
+  bool depos = atom_pbc_dev(p, sc, step, id, pp, po, po_changed, V, v_changed, P, typ, zmax);
+  double4 np = make_double4(pp[0], pp[1], pp[2], 0.0);
+  d.old_cg[h] = P;
+  d.pos[h] = np;
+  d.posf[h] = to_f4(np, typ);
+  d.vel[h] = V;
+  if (po_changed) d.pos_old[h] = po;
+  if (typ != typ0) d.typ[h] = (int8_t)typ;
+  if (!depos) d.skip[h] = 0;
+}
+
+// ---------------------------------------------------------------- fuerza
+// Pass 1: one warp per hs%ref member scans its list row; every interacting
+// entry (r <= r0, eps != 0) is computed in FP64 and recorded for both atoms
+// with the key (rank, jj) that orders the reference's accumulation.
+__global__ void force_pairs_kernel(Dev d, KParams p, int n_rank) {
+  int r = warp_id_global();
+  int lane = threadIdx.x & 31;
+  if (r >= n_rank) return;
+  int h = d.ref[r];
+  if (h < 0) return;
+  int k = d.typ[h];
+  double4 Pi = d.pos[h];
+  float4 Pf = d.posf[h];
+  int n = d.nn[h];
+  const int* row = d.list + (size_t)h * p.mnb;
+  for (int base = 0; base < n; base += 32) {
+    int jj = base + lane;
+    if (jj >= n) break;
+    int j = row[jj];
+    if (d.state[j] != ST_LIVE) continue;  // limbo (Neighbor.F90:1089-1092)
+    float4 Q = d.posf[j];
+    int m = (int)Q.w;
+    if (k == DML_Z_CG && m == DML_Z_CG) continue;
+    double eps = p.eps[k - 1][m - 1];
+    if (eps == 0.0) continue;  // contributes signed zeros only
+    float fx = Pf.x - Q.x, fy = Pf.y - Q.y, fz = Pf.z - Q.z;
+    if (fx > p.halfboxf[0]) fx -= p.boxf[0]; else if (fx < -p.halfboxf[0]) fx += p.boxf[0];
+    if (fy > p.halfboxf[1]) fy -= p.boxf[1]; else if (fy < -p.halfboxf[1]) fy += p.boxf[1];
+    float drf = fx * fx + fy * fy + fz * fz;
+    if (drf > p.r0f_pref2[k - 1][m - 1]) continue;
+    // exact FP64 (dana.F90:1095-1134)
+    double4 Pj = d.pos[j];
+    double vx = Pi.x - Pj.x, vy = Pi.y - Pj.y, vz = Pi.z - Pj.z;
+    if (vx > p.halfbox[0]) {
+      vx = vx - p.box[0];
+    } else if (vx < -p.halfbox[0]) {
+      vx = vx + p.box[0];
+    }
+    if (vy > p.halfbox[1]) {
+      vy = vy - p.box[1];
+    } else if (vy < -p.halfbox[1]) {
+      vy = vy + p.box[1];
+    }
+    double dr = dot3(vx, vy, vz);
+    if (dr > p.r0sq[k - 1][m - 1]) continue;
+    dr = sqrt(dr);
+    double c = p.c0[k - 1][m - 1] / pow7(dr);
+    double b = p.b0[k - 1][m - 1] / pow6(dr);
+    double aux = c * (b - 1.0);
+    EvRec e;
+    e.key = ((unsigned long long)(unsigned)r << 32) | (unsigned)jj;
+    e.fx = aux * vx / dr;
+    e.fy = aux * vy / dr;
+    e.fz = aux * vz / dr;
+    double ea = eps * b * (b - 2.0);
+    ea = ea + eps;
+    e.e = ea * .5;
+    e.pad = 0;
+    int si = atomicAdd(&d.ev_count[h], 1);
+    if (si < p.ev_cap) {
+      e.sign = 1;
+      d.ev[(size_t)h * p.ev_cap + si] = e;
+    } else {
+      raise_error(d.sc, DML_E_EVENT_OVERFLOW, h);
+    }
+    int sj = atomicAdd(&d.ev_count[j], 1);
+    if (sj < p.ev_cap) {
+      e.sign = -1;
+      d.ev[(size_t)j * p.ev_cap + sj] = e;
+    } else {
+      raise_error(d.sc, DML_E_EVENT_OVERFLOW, j);
+    }
+  }
+}
+
+// ermak_b (dana.F90:1031-1052) for one atom.
+__device__ __forceinline__ void ermak_b_atom(const Dev& d, const KParams& p, int h, int typ,
+                                             double4 F) {
+  if (typ == DML_Z_CG) return;
+  double m = p.mass[typ - 1];
+  double4 V = d.vel[h], A = d.acel[h], R = d.ranv[h];
+  V.x = p.cc0 * V.x + p.cc1mcc2 * A.x + p.cc2 * F.x / m + R.x;
+  V.y = p.cc0 * V.y + p.cc1mcc2 * A.y + p.cc2 * F.y / m + R.y;
+  V.z = p.cc0 * V.z + p.cc1mcc2 * A.z + p.cc2 * F.z / m + R.z;
+  A.x = F.x / m;
+  A.y = F.y / m;
+  A.z = F.z / m;
+  d.vel[h] = V;
+  d.acel[h] = A;
+}
+
+// Pass 2: one thread per hs slot sums its recorded entries in key order,
+// i.e. in the reference's global accumulation order (hs%ref order x list
+// order, with the Newton reaction applied to both atoms of every entry).
+template <bool FUSE_B>
+__global__ void force_sum_kernel(Dev d, KParams p, int n_slots) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_slots) return;
+  if (d.state[s] != ST_LIVE) return;
+  int cnt = d.ev_count[s];
+  bool inref = d.rank[s] >= 0;
+  if (!inref && cnt == 0) return;
+  if (cnt > p.ev_cap) cnt = p.ev_cap;  // overflow already raised
+  double4 F;
+  double ep;
+  if (inref) {
+    F = make_double4(0.0, 0.0, 0.0, 0.0);
+    ep = 0.0;
+  } else {
+    F = d.force[s];
+    ep = d.epot[s];
+  }
+  if (cnt > 0) {
+    const EvRec* ev = d.ev + (size_t)s * p.ev_cap;
+    // order of entries: insertion sort of the keys (few entries per atom)
+    unsigned char idx[128];
+    unsigned long long keys[128];
+    int c = cnt < 128 ? cnt : 128;
+    if (cnt > 128) raise_error(d.sc, DML_E_EVENT_OVERFLOW, s);
+    for (int i = 0; i < c; ++i) {
+      unsigned long long kk = ev[i].key;
+      int q = i;
+      while (q > 0 && keys[q - 1] > kk) {
+        keys[q] = keys[q - 1];
+        idx[q] = idx[q - 1];
+        --q;
+      }
+      keys[q] = kk;
+      idx[q] = (unsigned char)i;
+    }
+    for (int q = 0; q < c; ++q) {
+      const EvRec& e = ev[idx[q]];
+      if (e.sign > 0) {
+        F.x = F.x + e.fx;
+        F.y = F.y + e.fy;
+        F.z = F.z + e.fz;
+      } else {
+        F.x = F.x - e.fx;
+        F.y = F.y - e.fy;
+        F.z = F.z - e.fz;
+      }
+      ep = ep + e.e;
+    }
+    d.ev_count[s] = 0;
+  }
+  d.force[s] = F;
+  d.epot[s] = ep;
+  if (FUSE_B && inref) ermak_b_atom(d, p, s, d.typ[s], F);
+}
+
+__global__ void ermak_b_kernel(Dev d, KParams p, int n_rank) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rank) return;
+  int h = d.ref[r];
+  if (h < 0) return;
+  ermak_b_atom(d, p, h, d.typ[h], d.force[h]);
+}
+
+// ----------------------------------------------------------- test_update
+__device__ __forceinline__ void top2_merge(double& a1, double& a2, double b1, double b2) {
+  double hi = fmax(a1, b1);
+  double lo = fmax(fmin(a1, b1), fmax(a2, b2));
+  a1 = hi;
+  a2 = lo;
+}
+
+// do_pbc (Groups.F90:1440-1467) + inq_dispmax (Neighbor.F90:635-666) + the
+// update decision (Neighbor.F90:697-710).  The top-2 of squared
+// displacements is order independent, so a tree reduction is exact.
+__global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  double a1 = 1.e-16, a2 = 1.e-16;
+  if (s < n_slots && d.state[s] == ST_LIVE) {
+    double4 P = d.pos[s];
+    double4 O = d.pos_old[s];
+    bool ch = false;
+    if (P.x >= p.box[0]) {
+      P.x = P.x - p.box[0];
+      O.x = O.x - p.box[0];
+      ch = true;
+    } else if (P.x < 0.0) {
+      P.x = P.x + p.box[0];
+      O.x = O.x + p.box[0];
+      ch = true;
+    }
+    if (P.y >= p.box[1]) {
+      P.y = P.y - p.box[1];
+      O.y = O.y - p.box[1];
+      ch = true;
+    } else if (P.y < 0.0) {
+      P.y = P.y + p.box[1];
+      O.y = O.y + p.box[1];
+      ch = true;
+    }
+    if (ch) {
+      d.pos[s] = P;
+      d.pos_old[s] = O;
+      d.posf[s] = to_f4(P, d.typ[s]);
+    }
+    double rd = dot3(P.x - O.x, P.y - O.y, P.z - O.z);
+    top2_merge(a1, a2, rd, 1.e-16);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    double b1 = __shfl_down_sync(0xffffffffu, a1, off);
+    double b2 = __shfl_down_sync(0xffffffffu, a2, off);
+    top2_merge(a1, a2, b1, b2);
+  }
+  __shared__ double w1[32], w2[32];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    w1[wid] = a1;
+    w2[wid] = a2;
+  }
+  __syncthreads();
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    double b1 = 1.e-16, b2 = 1.e-16;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) top2_merge(b1, b2, w1[w], w2[w]);
+    d.part[2 * blockIdx.x] = b1;
+    d.part[2 * blockIdx.x + 1] = b2;
+    __threadfence();
+    unsigned t = atomicAdd(&d.sc->ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double b1 = 1.e-16, b2 = 1.e-16;
+    for (int b = 0; b < (int)gridDim.x; ++b) {
+      double c1 = ((volatile double*)d.part)[2 * b];
+      double c2 = ((volatile double*)d.part)[2 * b + 1];
+      top2_merge(b1, b2, c1, c2);
+    }
+    Scalars* sc = d.sc;
+    int rebuild = (!sc->listed) || (sqrt(b1) + sqrt(b2) > p.skin);
+    sc->rebuild = rebuild;
+    if (rebuild) {
+      sc->nupd += 1;
+      sc->max_nn = 0;
+    }
+    sc->ticket = 0;
+  }
+}
+
+// update() (Neighbor.F90:608-633) part 1: pos_old = pos, limbo cleaned
+// (igroup_clean, Groups.F90:1036-1053), cell index of every hs%b slot
+// (cgroup_sort_atom, Cells.F90:281-302) and the per-cell counts.
+__global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b) {
+  if (!d.sc->rebuild) return;
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n_slots) {
+    int st = d.state[s];
+    if (st == ST_LIVE) {
+      d.pos_old[s] = d.pos[s];
+    } else if (st == ST_LIMBO) {
+      d.state[s] = ST_NULL;
+    }
+  }
+  if (p.use_cells && s < n_b) {
+    int hs = d.b2hs[s];
+    if (hs < 0) {
+      d.cell_of[s] = -1;
+      return;
+    }
+    double4 P = d.pos[hs];
+    int c1 = (int)(P.x / p.cell[0]) + 1;
+    int c2 = (int)(P.y / p.cell[1]) + 1;
+    int c3 = (int)(P.z / p.cell[2]) + 1;
+    if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > p.ncells[0] + 1 || c2 > p.ncells[1] + 1 ||
+        c3 > p.ncells[2] + 1) {
+      raise_error(d.sc, DML_E_OUT_OF_TESSELLATION, hs);
+      d.cell_of[s] = -1;
+      return;
+    }
+    int lin = (c3 * p.head_dim[1] + c2) * p.head_dim[0] + c1;
+    d.cell_of[s] = lin;
+    atomicAdd(&d.cell_count[lin], 1);
+  }
+}
+
+// Exclusive scan of the cell counts (one block).
+__global__ void cell_scan_kernel(Dev d, int ncell) {
+  if (!d.sc->rebuild) return;
+  __shared__ int wsum[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int base = 0; base < ncell; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    int v = i < ncell ? d.cell_count[i] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int ws = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, ws, o);
+        if (lane >= o) ws += y;
+      }
+      wsum[lane] = ws;
+    }
+    __syncthreads();
+    int pre = (wid > 0 ? wsum[wid - 1] : 0) + x - v;
+    if (i < ncell) {
+      d.cell_start[i] = carry + pre;
+      d.cell_fill[i] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry += pre + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) d.cell_start[ncell] = carry;
+}
+
+__global__ void cell_scatter_kernel(Dev d, int n_b) {
+  if (!d.sc->rebuild) return;
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n_b) return;
+  int c = d.cell_of[b];
+  if (c < 0) return;
+  int idx = d.cell_start[c] + atomicAdd(&d.cell_fill[c], 1);
+  d.cell_atoms[idx] = b;
+}
+
+// Orders each cell by descending hs%b slot: the chain order of
+// cgroup_sort (Cells.F90:267-302), which prepends slots in increasing order.
+// One warp per cell; the sorted cell goes to comp_members (scratch) and is
+// copied back.
+__global__ void cell_order_kernel(Dev d, int ncell) {
+  if (!d.sc->rebuild) return;
+  int c = warp_id_global();
+  int lane = threadIdx.x & 31;
+  if (c >= ncell) return;
+  int start = d.cell_start[c];
+  int num = d.cell_start[c + 1] - start;
+  if (lane == 0) d.cell_count[c] = 0;
+  if (num <= 1) return;
+  const int* seg = d.cell_atoms + start;
+  int* tmp = d.comp_members + start;  // scratch of n_b entries
+  for (int i = lane; i < num; i += 32) {
+    int v = seg[i];
+    int rnk = 0;
+    for (int q = 0; q < num; ++q) rnk += seg[q] > v;
+    tmp[rnk] = v;
+  }
+  __syncwarp();
+  for (int i = lane; i < num; i += 32) ((int*)seg)[i] = tmp[i];
+}
+
+// ngroup_cells (Neighbor.F90:465-548): one warp per hs%ref member, the 27
+// stencil cells in map order (Cells.F90:28-36), each cell in chain order,
+// wrapped as cell_pbc with mic (Cells.F90:378-404), `rd < (rc+skin)^2`.
+__global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
+  if (!d.sc->rebuild) return;
+  int r = warp_id_global();
+  int lane = threadIdx.x & 31;
+  if (r >= n_rank) return;
+  int h = d.ref[r];
+  if (h < 0) return;
+  double4 P = d.pos[h];
+  float4 Pf = d.posf[h];
+  int rc[3] = {(int)(P.x / p.cell[0]) + 1, (int)(P.y / p.cell[1]) + 1, (int)(P.z / p.cell[2]) + 1};
+  int* row = d.list + (size_t)h * p.mnb;
+  int cnt = 0;
+  for (int nabor = 0; nabor < 27; ++nabor) {
+    int nc[3];
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      int t = c_map[nabor][k] + rc[k] - 1;
+      t = (t + p.ncells[k]) % p.ncells[k];
+      nc[k] = t + 1;
+      if (nc[k] < 0 || nc[k] > p.ncells[k] + 1) bad = true;
+    }
+    if (bad) {
+      if (lane == 0) raise_error(d.sc, DML_E_OUT_OF_TESSELLATION, h);
+      return;
+    }
+    int c = (nc[2] * p.head_dim[1] + nc[1]) * p.head_dim[0] + nc[0];
+    int start = d.cell_start[c];
+    int num = d.cell_start[c + 1] - start;
+    for (int base = 0; base < num; base += 32) {
+      int idx = base + lane;
+      bool inc = false;
+      int j = -1;
+      if (idx < num) {
+        int b = d.cell_atoms[start + idx];
+        j = d.b2hs[b];
+        if (j != h) {
+          float4 Q = d.posf[j];
+          float fx, fy, fz;
+          vdist_nint_f(p, Q, Pf, fx, fy, fz);
+          float drf = fx * fx + fy * fy + fz * fz;
+          if (drf < p.rlist_lo2) {
+            inc = true;
+          } else if (drf <= p.rlist_hi2) {
+            double vx, vy, vz;
+            vdist_nint(p, d.pos[j], P, vx, vy, vz);
+            double rd = dot3(vx, vy, vz);
+            inc = rd < p.rlist2;
+          }
+        }
+      }
+      unsigned bal = __ballot_sync(0xffffffffu, inc);
+      int pre = __popc(bal & ((1u << lane) - 1u));
+      if (inc && cnt + pre < p.mnb) row[cnt + pre] = j;
+      cnt += __popc(bal);
+    }
+  }
+  if (lane == 0) {
+    if (cnt > p.mnb) {
+      raise_error(d.sc, DML_E_NEIGH_OVERFLOW, h);
+      cnt = p.mnb;
+    }
+    d.nn[h] = cnt;
+    atomicMax(&d.sc->max_nn, cnt);
+  }
+}
+
+// ngroup_verlet (Neighbor.F90:358-424): all hs%b slots in index order,
+// `rd > (rc+skin)^2` rejected (so equality is kept), vdistance(ai, aj).
+__global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
+  if (!d.sc->rebuild) return;
+  int r = warp_id_global();
+  int lane = threadIdx.x & 31;
+  if (r >= n_rank) return;
+  int h = d.ref[r];
+  if (h < 0) return;
+  double4 P = d.pos[h];
+  float4 Pf = d.posf[h];
+  int* row = d.list + (size_t)h * p.mnb;
+  int cnt = 0;
+  for (int base = 0; base < n_b; base += 32) {
+    int b = base + lane;
+    bool inc = false;
+    int j = -1;
+    if (b < n_b) {
+      j = d.b2hs[b];
+      if (j >= 0 && j != h) {
+        float4 Q = d.posf[j];
+        float fx, fy, fz;
+        vdist_nint_f(p, Pf, Q, fx, fy, fz);
+        float drf = fx * fx + fy * fy + fz * fz;
+        if (drf < p.rlist_lo2) {
+          inc = true;
+        } else if (drf <= p.rlist_hi2) {
+          double vx, vy, vz;
+          vdist_nint(p, P, d.pos[j], vx, vy, vz);
+          double rd = dot3(vx, vy, vz);
+          inc = !(rd > p.rlist2);
+        }
+      }
+    }
+    unsigned bal = __ballot_sync(0xffffffffu, inc);
+    int pre = __popc(bal & ((1u << lane) - 1u));
+    if (inc && cnt + pre < p.mnb) row[cnt + pre] = j;
+    cnt += __popc(bal);
+  }
+  if (lane == 0) {
+    if (cnt > p.mnb) {
+      raise_error(d.sc, DML_E_NEIGH_OVERFLOW, h);
+      cnt = p.mnb;
+    }
+    d.nn[h] = cnt;
+    atomicMax(&d.sc->max_nn, cnt);
+  }
+}
+
+__global__ void rebuild_done_kernel(Dev d) {
+  if (d.sc->rebuild) d.sc->listed = 1;
+}
+
+// ------------------------------------------------------- overlap_moveback
+// The reference resolves hard-core overlaps sequentially in hs%ref order and
+// repeats while a pass moved an atom (dana.F90:849-943).  During this phase
+// every atom sits either at its integrated position or at old_cg, so any
+// pair that can touch during any pass was within rc + 2*delta at the start,
+// delta = max |pos - old_cg|.  Atoms linked by such near pairs form
+// components; events in different components touch disjoint atoms and
+// commute, so each component is replayed in rank order by one thread and
+// gives exactly the reference's result.
+
+__global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) {
+    d.sc->again = 0;
+    d.sc->n_comp = 0;
+    d.sc->comp_total = 0;
+  }
+  if (s >= n_slots) return;
+  d.uf[s] = s;
+  d.active[s] = 0;
+  d.comp_size[s] = 0;
+  d.comp_fill[s] = 0;
+  if (d.state[s] == ST_LIVE && d.rank[s] >= 0) {
+    double4 P = d.pos[s], O = d.old_cg[s];
+    double x, y, z;
+    vdist_nint(p, P, O, x, y, z);
+    double dd = dot3(x, y, z);
+    atomicMax(&d.sc->delta2_bits, (unsigned long long)__double_as_longlong(dd));
+  }
+}
+
+__device__ int uf_find(volatile int* uf, int x) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    int px = uf[x];
+    if (px == x) return x;
+    int ppx = uf[px];
+    if (ppx != px) atomicCAS((int*)&uf[x], px, ppx);
+    x = px;
+  }
+  return -1;
+}
+
+__device__ void uf_union(Scalars* sc, volatile int* uf, int a, int b) {
+  for (int it = 0; it < (1 << 20); ++it) {
+    a = uf_find(uf, a);
+    b = uf_find(uf, b);
+    if (a < 0 || b < 0) break;
+    if (a == b) return;
+    if (a < b) {
+      int t = a;
+      a = b;
+      b = t;
+    }
+    if (atomicCAS((int*)&uf[a], a, b) == a) return;
+  }
+  raise_error(sc, DML_E_OVERLAP_PASSES, -1);
+}
+
+// Near entries of every hs%ref member: list entries within rc + 2 delta
+// (FP32 with margin; a superset is harmless) in list order.
+__global__ void overlap_detect_kernel(Dev d, KParams p, int n_rank) {
+  int r = warp_id_global();
+  int lane = threadIdx.x & 31;
+  if (r >= n_rank) return;
+  int h = d.ref[r];
+  if (h < 0) return;
+  double delta = sqrt(__longlong_as_double((long long)d.sc->delta2_bits));
+  double rn = sqrt(p.rc2) + 2.0 * delta;
+  float rnf = (float)rn + 4.0f * p.margin + 1e-3f;
+  float rn2 = rnf * rnf;
+  float4 Pf = d.posf[h];
+  int n = d.nn[h];
+  const int* row = d.list + (size_t)h * p.mnb;
+  int* near = d.near + (size_t)h * kNearCap;
+  int cnt = 0;
+  bool any = false;
+  for (int base = 0; base < n; base += 32) {
+    int jj = base + lane;
+    bool inc = false;
+    int j = -1;
+    if (jj < n) {
+      j = row[jj];
+      if (d.state[j] == ST_LIVE) {
+        float4 Q = d.posf[j];
+        float fx, fy, fz;
+        vdist_nint_f(p, Pf, Q, fx, fy, fz);
+        inc = fx * fx + fy * fy + fz * fz <= rn2;
+      }
+    }
+    unsigned bal = __ballot_sync(0xffffffffu, inc);
+    int pre = __popc(bal & ((1u << lane) - 1u));
+    if (inc) {
+      if (cnt + pre < kNearCap) near[cnt + pre] = j;
+      if (d.typ[j] != DML_Z_CG) {
+        uf_union(d.sc, (volatile int*)d.uf, h, j);
+        d.active[j] = 1;
+      }
+    }
+    cnt += __popc(bal);
+    any = any || bal != 0;
+  }
+  if (lane == 0) {
+    d.near_count[h] = cnt > kNearCap ? -1 : cnt;
+    if (any) d.active[h] = 1;
+  }
+}
+
+// Atoms with no near entry are examined trivially in pass 1 (skip = true)
+// and can never be moved; the others are counted per component root.
+__global__ void overlap_count_kernel(Dev d, int n_rank) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r == 0) d.sc->delta2_bits = 0ull;
+  if (r >= n_rank) return;
+  int h = d.ref[r];
+  if (h < 0) return;
+  if (!d.active[h]) {
+    d.skip[h] = 1;
+    return;
+  }
+  int root = uf_find((volatile int*)d.uf, h);
+  d.uf[h] = root;
+  atomicAdd(&d.comp_size[root], 1);
+}
+
+__global__ void overlap_assign_kernel(Dev d, int n_slots) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_slots) return;
+  int sz = d.comp_size[s];
+  if (sz <= 0) return;
+  int cid = atomicAdd(&d.sc->n_comp, 1);
+  int off = atomicAdd(&d.sc->comp_total, sz);
+  d.comp_id[s] = cid;
+  d.comp_list[2 * cid] = off;
+  d.comp_list[2 * cid + 1] = sz;
+}
+
+__global__ void overlap_scatter_kernel(Dev d, int n_rank) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rank) return;
+  int h = d.ref[r];
+  if (h < 0 || !d.active[h]) return;
+  int root = d.uf[h];
+  int cid = d.comp_id[root];
+  int idx = d.comp_list[2 * cid] + atomicAdd(&d.comp_fill[root], 1);
+  d.comp_members[idx] = h;
+}
+
+// Examination of o1 = x in pass `pass` (dana.F90:871-935).
+__device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, int* again) {
+  Scalars* sc = d.sc;
+  int nc = d.near_count[x];
+  int n = nc >= 0 ? nc : d.nn[x];
+  const int* src = nc >= 0 ? d.near + (size_t)x * kNearCap : d.list + (size_t)x * p.mnb;
+  for (int q = 0; q < n; ++q) {
+    int j = src[q];
+    if (d.state[j] != ST_LIVE) continue;
+    double4 P = d.pos[x];
+    double4 Q = d.pos[j];
+    double vx, vy, vz;
+    vdist_nint(p, P, Q, vx, vy, vz);
+    double dr = dot3(vx, vy, vz);
+    if (dr > p.rc2) continue;
+    if (d.typ[j] == DML_Z_CG) {
+      count_add(&sc->try_, 1ull);
+      double ne = dml_uniform(dml_draw(p.seed, sc->step, (uint64_t)d.id[x], DML_RNG_OVERLAP,
+                                       (uint32_t)pass));
+      if (ne < p.prob) {
+        count_add(&sc->depo, 1ull);
+        d.typ[x] = DML_Z_F;
+        float4 f = d.posf[x];
+        f.w = (float)DML_Z_F;
+        d.posf[x] = f;
+        if (P.z > sc->z0) raise_error(sc, DML_E_DENDRITE, x);
+      } else {
+        double4 O = d.old_cg[x];
+        d.pos[x] = O;
+        d.posf[x] = to_f4(O, d.typ[x]);
+        d.skip[x] = 0;
+      }
+      break;
+    }
+    double4 Oj = d.old_cg[j];
+    if (p.reservoir == DML_RESERVOIR_PISTON) {
+      double4 Ox = d.old_cg[x];
+      bool j_old = Q.x == Oj.x && Q.y == Oj.y && Q.z == Oj.z;
+      bool x_old = P.x == Ox.x && P.y == Ox.y && P.z == Ox.z;
+      if (j_old && x_old) {
+        count_add(&sc->choques3, 1ull);
+        continue;
+      }
+    }
+    d.pos[j] = Oj;
+    d.posf[j] = to_f4(Oj, d.typ[j]);
+    d.acel[j] = make_double4(0.0, 0.0, 0.0, 0.0);
+    d.vel[j] = make_double4(0.0, 0.0, 0.0, 0.0);
+    d.skip[j] = 0;
+    count_add(&sc->choques, 1ull);
+    *again = 1;
+  }
+}
+
+// Pass 1: one thread per component; members sorted by rank first.
+__global__ void overlap_pass1_kernel(Dev d, KParams p) {
+  int cid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cid >= d.sc->n_comp) return;
+  int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
+  int* mem = d.comp_members + off;
+  for (int i = 1; i < sz; ++i) {
+    int v = mem[i];
+    int rv = d.rank[v];
+    int q = i;
+    while (q > 0 && d.rank[mem[q - 1]] > rv) {
+      mem[q] = mem[q - 1];
+      --q;
+    }
+    mem[q] = v;
+  }
+  int again = 0;
+  for (int i = 0; i < sz; ++i) {
+    int x = mem[i];
+    if (d.skip[x]) continue;
+    d.skip[x] = 1;
+    overlap_exam(d, p, x, 1, &again);
+  }
+  if (again) d.sc->again = 1;
+}
+
+// Passes 2.. (the recursion): one block, a barrier between passes.
+__global__ void overlap_passn_kernel(Dev d, KParams p) {
+  __shared__ int again_s;
+  __shared__ int go;
+  Scalars* sc = d.sc;
+  int ncomp = sc->n_comp;
+  int pass = 1;
+  if (threadIdx.x == 0) go = sc->again;
+  __syncthreads();
+  while (go) {
+    pass += 1;
+    if (pass > p.max_passes) {
+      if (threadIdx.x == 0) raise_error(sc, DML_E_OVERLAP_PASSES, pass);
+      break;
+    }
+    if (threadIdx.x == 0) again_s = 0;
+    __syncthreads();
+    int again = 0;
+    for (int cid = threadIdx.x; cid < ncomp; cid += blockDim.x) {
+      int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
+      const int* mem = d.comp_members + off;
+      for (int i = 0; i < sz; ++i) {
+        int x = mem[i];
+        if (d.skip[x]) continue;
+        d.skip[x] = 1;
+        overlap_exam(d, p, x, pass, &again);
+      }
+    }
+    if (again) atomicOr(&again_s, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) go = again_s;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sc->passes = pass;
+}
+
+// ------------------------------------------------- capture commit, rho, piston
+// dana.F90:228-236: every F member of hs%ref becomes CG and leaves hs%ref
+// (its rank becomes a hole; the order of the remaining members is kept).
+__global__ void commit_kernel(Dev d, int n_rank) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n_rank) return;
+  int h = d.ref[r];
+  if (h < 0) return;
+  if (d.typ[h] != DML_Z_F) return;
+  d.typ[h] = DML_Z_CG;
+  float4 f = d.posf[h];
+  f.w = (float)DML_Z_CG;
+  d.posf[h] = f;
+  d.rank[h] = -1;
+  d.ref[r] = -1;
+  atomicSub(&d.sc->n_ref, 1);
+  atomicAdd(&d.sc->n_new_cg, 1);
+}
+
+// calc_rho (dana.F90:521-549): integer count, so any reduction order is exact.
+__global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  Scalars* sc = d.sc;
+  double z0 = sc->z0;
+  double zt = p.ztop_is_z1 != 0.0 ? sc->z1 : sc->zmax;
+  int c = 0;
+  if (s < n_slots && d.state[s] == ST_LIVE) {
+    double z = d.pos[s].z;
+    c = (z > z0 && z < zt) ? 1 : 0;
+  }
+  c = __syncthreads_count(c);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    if (c) atomicAdd(&sc->rho_count, c);
+    __threadfence();
+    unsigned t = atomicAdd(&sc->ticket2, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    int g = atomicAdd(&sc->rho_count, 0);
+    double vol = p.box[0] * p.box[1] * (zt - z0);
+    sc->rho = (double)g / vol;
+    sc->rho_count = 0;
+    sc->ticket2 = 0;
+  }
+}
+
+// maxz (dana.F90:776-794)
+__global__ void piston_kernel(Dev d, KParams p, int n_slots) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  Scalars* sc = d.sc;
+  double z0 = sc->z0;
+  double lohi = (p.h_over_tau * ((sc->rho0 - sc->rho) / sc->rho));
+  if (s < n_slots && d.state[s] == ST_LIVE) {
+    double4 P = d.pos[s];
+    if (P.z > z0) {
+      P.z = P.z - lohi * (P.z - z0);
+      d.pos[s] = P;
+      d.posf[s] = to_f4(P, d.typ[s]);
+    }
+  }
+  if (s == 0) {
+    double zm = sc->zmax;
+    sc->lohi = lohi;
+    sc->zmax = zm - lohi * (zm - z0);
+  }
+}
+
+inline int nblk(int n, int b = kBlock) { return n > 0 ? (n + b - 1) / b : 1; }
+inline int nblk_warps(int n) { return n > 0 ? (n + (kBlock / 32) - 1) / (kBlock / 32) : 1; }
+
+}  // namespace
+
+void k_step_begin(const Dev& d, cudaStream_t s) { step_begin_kernel<<<1, 1, 0, s>>>(d.sc); }
+
+void k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
+  ermak_a_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+}
+
+void k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
+  brownian_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+}
+
+void k_force(const Dev& d, const KParams& p, int n_rank, int n_slots, bool fuse_b, cudaStream_t s) {
+  force_pairs_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  if (fuse_b)
+    force_sum_kernel<true><<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  else
+    force_sum_kernel<false><<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+}
+
+void k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
+  ermak_b_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+}
+
+void k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
+                   cudaStream_t s) {
+  pbc_dispmax_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  int nmax = n_slots > n_b ? n_slots : n_b;
+  rebuild_prep_kernel<<<nblk(nmax), kBlock, 0, s>>>(d, p, n_slots, n_b);
+  if (p.use_cells) {
+    cell_scan_kernel<<<1, 1024, 0, s>>>(d, d.ncell_tot);
+    cell_scatter_kernel<<<nblk(n_b), kBlock, 0, s>>>(d, n_b);
+    cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot);
+    list_cells_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  } else {
+    list_verlet_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank, n_b);
+  }
+  rebuild_done_kernel<<<1, 1, 0, s>>>(d);
+}
+
+void k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStream_t s) {
+  overlap_init_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  overlap_detect_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  overlap_count_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
+  overlap_assign_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, n_slots);
+  overlap_scatter_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
+  overlap_pass1_kernel<<<nblk(n_rank, 128), 128, 0, s>>>(d, p);
+  overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
+}
+
+void k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
+  (void)p;
+  commit_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
+}
+
+void k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
+  calc_rho_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+}
+
+void k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
+  piston_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+}
+
+}  // namespace dml

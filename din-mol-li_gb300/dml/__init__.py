@@ -1,2 +1,222 @@
-"""Host-side mirror of din-mol-Li's hot-path routines over the GB300 C ABI."""
+"""Host-side mirror of din-mol-Li's hot-path routines over the GB300 C ABI.
+
+`Simulation` wraps one `dml_ctx` of libdml.so (include/dml.h).  Its methods
+carry the names of the reference procedures they replace (src/dana.F90,
+src/Neighbor.F90): `test_update`, `fuerza`, `ermak_a`, `ermak_b`,
+`cbrownian_hs`, `overlap_moveback`, `capture_commit`, `calc_rho`, `maxz`,
+plus `step(n)`, the fused loop body of dana.F90:173-265.
+
+The CUDA library is the only implementation: if libdml.so is missing or
+cannot reach a GPU, every call raises.  There is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
 from ._abi import *  # noqa: F401,F403
+from . import _abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.dirname(_HERE)
+LIB_PATH = os.path.join(PKG_DIR, "_build", "libdml.so")
+
+_lib = None
+
+
+class DmlError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (_abi.STATUS.get(code, "?"), code, msg))
+        self.code = code
+
+
+def build(force=False, verbose=False):
+    """Compiles libdml.so for sm_103a (din-mol-li_gb300/build.py)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("_dml_build", os.path.join(PKG_DIR, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force, verbose=verbose)
+
+
+def lib():
+    """Loads libdml.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libdml.so not built: run din-mol-li_gb300/build.py (no CPU fallback)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+    P = ctypes.POINTER
+    L.dml_params_default.argtypes = [P(_abi.Params)]
+    L.dml_params_default.restype = None
+    L.dml_create.argtypes = [P(_abi.Params), P(vp)]
+    L.dml_destroy.argtypes = [vp]
+    L.dml_destroy.restype = None
+    L.dml_set_atoms.argtypes = [vp, P(_abi.Atoms)]
+    L.dml_get_atoms.argtypes = [vp, P(_abi.Atoms)]
+    for name in ["dml_setup", "dml_force", "dml_ermak_b", "dml_piston", "dml_sync",
+                 "dml_reset_counters"]:
+        getattr(L, name).argtypes = [vp]
+    for name in ["dml_ermak_a", "dml_brownian", "dml_overlap_moveback", "dml_gcmc", "dml_step",
+                 "dml_step_async"]:
+        getattr(L, name).argtypes = [vp, i64]
+    L.dml_test_update.argtypes = [vp, P(i32)]
+    L.dml_capture_commit.argtypes = [vp, P(i32)]
+    L.dml_calc_rho.argtypes = [vp, P(ctypes.c_double)]
+    L.dml_get_neighbors.argtypes = [vp, P(i32), vp, vp, i32]
+    L.dml_get_counters.argtypes = [vp, P(_abi.Counters)]
+    L.dml_strerror.restype = ctypes.c_char_p
+    L.dml_strerror.argtypes = [ctypes.c_int]
+    L.dml_last_error.restype = ctypes.c_char_p
+    L.dml_last_error.argtypes = [vp]
+    L.dml_gen_bcc_slab.argtypes = [i32, i32, i32, ctypes.c_double, vp, i32]
+    L.dml_gen_ions.argtypes = [ctypes.c_uint64, i32, ctypes.c_double, ctypes.c_double,
+                               ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
+    _lib = L
+    return L
+
+
+def default_params():
+    p = _abi.Params()
+    lib().dml_params_default(ctypes.byref(p))
+    return p
+
+
+def bcc_slab(nx, ny, nz, a=3.51):
+    """Frozen bcc Li electrode: 2*nx*ny*nz positions."""
+    n = 2 * nx * ny * nz
+    out = np.zeros((n, 3))
+    rc = lib().dml_gen_bcc_slab(nx, ny, nz, a, out.ctypes.data, n)
+    if rc < 0:
+        raise DmlError(-rc, "dml_gen_bcc_slab")
+    return out
+
+
+def random_ions(seed, n, box_x, box_y, zlo, zhi, dmin):
+    """RSA ions with minimum separation dmin (x,y periodic)."""
+    out = np.zeros((n, 3))
+    rc = lib().dml_gen_ions(seed, n, box_x, box_y, zlo, zhi, dmin, out.ctypes.data)
+    if rc < 0:
+        raise DmlError(-rc, "dml_gen_ions")
+    return out
+
+
+def slab_system(nx, ny, nz_slab, box_z, n_ion, zlo, zhi, seed, a=3.51, dmin=2.5):
+    """Electrode slab followed by ions, as sys%alist-ordered arrays."""
+    slab = bcc_slab(nx, ny, nz_slab, a)
+    ions = random_ions(seed, n_ion, nx * a, ny * a, zlo, zhi, dmin)
+    pos = np.concatenate([slab, ions])
+    z = np.concatenate([np.full(len(slab), Z_CG, np.int32), np.full(n_ion, Z_LI, np.int32)])
+    return {"pos": pos, "z": z}
+
+
+class Simulation:
+    """One device context (dml_ctx); methods mirror the reference routines."""
+
+    def __init__(self, params):
+        self.lib = lib()
+        self.params = params
+        h = ctypes.c_void_p()
+        rc = self.lib.dml_create(ctypes.byref(params), ctypes.byref(h))
+        if rc != 0:
+            raise DmlError(rc, "dml_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.dml_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc, what=""):
+        if rc != 0:
+            raise DmlError(rc, "%s: %s" % (what, self.lib.dml_last_error(self.h).decode()))
+
+    def set_atoms(self, arrays):
+        n = len(arrays["z"])
+        a = _abi.atoms_struct(dict(arrays), n)
+        self._check(self.lib.dml_set_atoms(self.h, ctypes.byref(a)), "dml_set_atoms")
+
+    def setup(self):
+        self._check(self.lib.dml_setup(self.h), "dml_setup")
+
+    def step(self, n=1):
+        self._check(self.lib.dml_step(self.h, n), "dml_step")
+
+    def step_async(self, n=1):
+        self._check(self.lib.dml_step_async(self.h, n), "dml_step_async")
+
+    def sync(self):
+        self._check(self.lib.dml_sync(self.h), "dml_sync")
+
+    def test_update(self):
+        r = ctypes.c_int32()
+        self._check(self.lib.dml_test_update(self.h, ctypes.byref(r)), "dml_test_update")
+        return r.value
+
+    def fuerza(self):
+        self._check(self.lib.dml_force(self.h), "dml_force")
+
+    def ermak_a(self, step):
+        self._check(self.lib.dml_ermak_a(self.h, step), "dml_ermak_a")
+
+    def ermak_b(self):
+        self._check(self.lib.dml_ermak_b(self.h), "dml_ermak_b")
+
+    def cbrownian_hs(self, step):
+        self._check(self.lib.dml_brownian(self.h, step), "dml_brownian")
+
+    def overlap_moveback(self, step):
+        self._check(self.lib.dml_overlap_moveback(self.h, step), "dml_overlap_moveback")
+
+    def capture_commit(self):
+        r = ctypes.c_int32()
+        self._check(self.lib.dml_capture_commit(self.h, ctypes.byref(r)), "dml_capture_commit")
+        return r.value
+
+    def gcmc_run(self, step):
+        self._check(self.lib.dml_gcmc(self.h, step), "dml_gcmc")
+
+    def calc_rho(self):
+        r = ctypes.c_double()
+        self._check(self.lib.dml_calc_rho(self.h, ctypes.byref(r)), "dml_calc_rho")
+        return r.value
+
+    def maxz(self):
+        self._check(self.lib.dml_piston(self.h), "dml_piston")
+
+    def reset_counters(self):
+        self._check(self.lib.dml_reset_counters(self.h), "dml_reset_counters")
+
+    def counters(self):
+        c = _abi.Counters()
+        self._check(self.lib.dml_get_counters(self.h, ctypes.byref(c)), "dml_get_counters")
+        return c.as_dict()
+
+    def get_atoms(self, n=None):
+        if n is None:
+            n = self.counters()["n_atoms"]
+        out = _abi.empty_atoms(n)
+        a = _abi.atoms_struct(out, n)
+        self._check(self.lib.dml_get_atoms(self.h, ctypes.byref(a)), "dml_get_atoms")
+        return out
+
+    def get_neighbors(self, ld):
+        n_ref = self.counters()["n_ref"]
+        nn = np.zeros(max(n_ref, 1), np.int32)
+        lst = np.zeros((max(n_ref, 1), ld), np.int32)
+        nr = ctypes.c_int32()
+        self._check(self.lib.dml_get_neighbors(self.h, ctypes.byref(nr), nn.ctypes.data,
+                                               lst.ctypes.data, ld), "dml_get_neighbors")
+        return nn[: nr.value], lst[: nr.value]

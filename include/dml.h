@@ -210,6 +210,18 @@ int dml_get_counters(dml_ctx* c, dml_counters* out);
 /* Resets try and depo (salida, src/dana.F90:1171-1174). */
 int dml_reset_counters(dml_ctx* c);
 
+/* Initial configurations (replaces pos_inic, src/dana.F90:330-396, which
+ * cannot load an electrode).  dml_gen_bcc_slab writes the 2*nx*ny*nz atoms
+ * of a bcc lattice with constant a (corner then body-centre atom per cell,
+ * x fastest) and returns the count, or -status.  dml_gen_ions places n ions
+ * uniformly in [0,box_x) x [0,box_y) x [zlo,zhi) by random sequential
+ * addition with minimum-image separation >= dmin (the rule of
+ * dana.F90:361-389), drawing from the seeded Philox stream; returns 0 or
+ * -status. */
+int dml_gen_bcc_slab(int32_t nx, int32_t ny, int32_t nz, double a, double* pos_out, int32_t cap);
+int dml_gen_ions(uint64_t seed, int32_t n, double box_x, double box_y, double zlo, double zhi,
+                 double dmin, double* pos_out);
+
 const char* dml_strerror(int code);
 
 /* Text of the last CUDA or argument error of this context. */

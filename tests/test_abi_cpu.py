@@ -1,0 +1,70 @@
+"""CPU checks of the product library: it builds, loads without a GPU and
+exports every entry point include/dml.h declares; host-side generators."""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+from tests import systems  # noqa: F401  (sets sys.path)
+import dml
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for hdr in ["dml.h"]:
+        text = open(os.path.join(ROOT, "include", hdr)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(dml_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_builds_and_exports_all_symbols():
+    path = dml.build()
+    assert os.path.exists(path)
+    lib = ctypes.CDLL(path)
+    names = declared_symbols()
+    assert "dml_create" in names and "dml_step" in names
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_default_params_match_reference_constants():
+    p = dml.default_params()
+    assert p.eps[0][0] == 2313.6 and p.r0[0][0] == 3.2
+    assert p.r0[0][1] == 3.5 and p.eps[0][1] == 0.0
+    assert p.eps[0][2] == 529.1 and p.r0[0][2] == 1.564
+    assert p.eps[2][2] == 121.0 and p.r0[2][2] == 3.61
+    assert p.kb_driver == 8.617330350e-5 * (96.485 * 100.0)
+    assert abs(p.kb_module / p.kb_driver - 1) < 1e-4
+    assert p.rc == 3.2 and p.tau == 0.1 and p.gamma == 1.0 and p.temp == 300.0
+
+
+def test_strerror_names_reference_messages():
+    lib = dml.lib()
+    assert lib.dml_strerror(4) == b"Particle out of tessellation"
+    assert lib.dml_strerror(7) == b"No more particles"
+
+
+def test_bcc_slab_and_ions():
+    slab = dml.bcc_slab(10, 10, 2)
+    assert slab.shape == (400, 3)
+    assert slab[:, 2].max() == 1.5 * 3.51
+    ions = dml.random_ions(7, 200, 35.1, 35.1, 10.0, 60.0, 2.5)
+    d = ions[:, None, :] - ions[None, :, :]
+    d[..., :2] -= 35.1 * np.round(d[..., :2] / 35.1)
+    r2 = (d ** 2).sum(-1) + np.eye(len(ions)) * 1e9
+    assert r2.min() >= 2.5 ** 2
+    assert ions[:, 2].min() >= 10.0 and ions[:, 2].max() < 60.0
+    # a pure function of the seed
+    assert np.array_equal(ions, dml.random_ions(7, 200, 35.1, 35.1, 10.0, 60.0, 2.5))
+
+
+def test_create_rejects_unsupported_options_without_gpu():
+    p = systems.c1_params()
+    p.box[0] = 10.0  # minimum image ambiguous at the list radius
+    h = ctypes.c_void_p()
+    assert dml.lib().dml_create(ctypes.byref(p), ctypes.byref(h)) == 1
