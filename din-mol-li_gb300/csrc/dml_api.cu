@@ -30,6 +30,8 @@ struct dml_ctx {
   int n_slots = 0, n_b = 0, n_rank = 0, n_atoms = 0;
   std::vector<int> alist;  // hs slots in sys%alist order
   cudaGraphExec_t step_graph = nullptr;
+  int launches_per_step = 0;
+  void* flush_buf = nullptr;
   std::string last_error;
   Scalars* h_sc = nullptr;  // pinned mirror
   std::vector<void*> allocs;
@@ -173,36 +175,63 @@ int set_step(dml_ctx* c, int64_t step) {
 }
 
 // One iteration of the loop body of dana.F90:173-265 (without salida,
-// timer_dump and the chunk reservoir), queued on the context stream.
-void enqueue_step(dml_ctx* c) {
+// timer_dump and the chunk reservoir), queued on the context stream.  With
+// `ev` (DML_NPHASE + 1 events) the phase boundaries are recorded.  Returns
+// the number of kernels queued.
+int enqueue_step(dml_ctx* c, cudaEvent_t* ev) {
   const Dev& d = c->D;
   const KParams& k = c->K;
   cudaStream_t s = c->stream;
-  k_step_begin(d, s);
+  int n = 0;
+  auto mark = [&](int i) {
+    if (ev) cudaEventRecord(ev[i], s);
+  };
+  mark(DML_PHASE_INTEGRATE);
+  n += k_step_begin(d, s);
   if (c->P.integrator == DML_INTEGRATOR_ERMAK) {
-    k_ermak_a(d, k, c->n_rank, s);
-    k_force(d, k, c->n_rank, c->n_slots, true, s);  // fuerza + ermak_b
+    n += k_ermak_a(d, k, c->n_rank, s);
+    mark(DML_PHASE_FORCE_PAIRS);
+    n += k_force_pairs(d, k, c->n_rank, s);
+    mark(DML_PHASE_FORCE_SUM);
+    n += k_force_sum(d, k, c->n_slots, true, s);  // fuerza + ermak_b
   } else {
-    k_brownian(d, k, c->n_rank, s);
+    n += k_brownian(d, k, c->n_rank, s);
+    mark(DML_PHASE_FORCE_PAIRS);
+    mark(DML_PHASE_FORCE_SUM);
   }
-  k_test_update(d, k, c->n_slots, c->n_b, c->n_rank, s);
-  k_overlap(d, k, c->n_rank, c->n_slots, s);
-  k_test_update(d, k, c->n_slots, c->n_b, c->n_rank, s);
-  k_capture_commit(d, k, c->n_rank, s);
-  k_calc_rho(d, k, c->n_slots, s);
-  if (c->P.reservoir == DML_RESERVOIR_PISTON) k_piston(d, k, c->n_slots, s);
+  mark(DML_PHASE_TEST_UPDATE1);
+  n += k_test_update(d, k, c->n_slots, c->n_b, c->n_rank, s);
+  mark(DML_PHASE_OVERLAP);
+  n += k_overlap(d, k, c->n_rank, c->n_slots, s);
+  mark(DML_PHASE_TEST_UPDATE2);
+  n += k_test_update(d, k, c->n_slots, c->n_b, c->n_rank, s);
+  mark(DML_PHASE_COMMIT);
+  n += k_capture_commit(d, k, c->n_rank, s);
+  mark(DML_PHASE_RHO_PISTON);
+  n += k_calc_rho(d, k, c->n_slots, s);
+  if (c->P.reservoir == DML_RESERVOIR_PISTON) n += k_piston(d, k, c->n_slots, s);
+  mark(DML_NPHASE);
+  return n;
 }
 
 int build_step_graph(dml_ctx* c) {
   if (c->step_graph) return 0;
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  enqueue_step(c);
+  c->launches_per_step = enqueue_step(c, nullptr);
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
   e = cudaGraphInstantiate(&c->step_graph, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+  return 0;
+}
+
+constexpr size_t kFlushBytes = 256ull << 20;  // > 2x the 129 MB L2
+
+int ensure_flush(dml_ctx* c) {
+  if (c->flush_buf) return 0;
+  CK(cudaMalloc(&c->flush_buf, kFlushBytes));
   return 0;
 }
 
@@ -316,6 +345,7 @@ void dml_destroy(dml_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
   for (void* p : c->allocs) cudaFree(p);
+  if (c->flush_buf) cudaFree(c->flush_buf);
   if (c->h_sc) cudaFreeHost(c->h_sc);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -461,7 +491,8 @@ int dml_test_update(dml_ctx* c, int32_t* rebuilt) {
 
 int dml_force(dml_ctx* c) {
   if (!c || !c->loaded) return DML_E_STATE;
-  k_force(c->D, c->K, c->n_rank, c->n_slots, false, c->stream);
+  k_force_pairs(c->D, c->K, c->n_rank, c->stream);
+  k_force_sum(c->D, c->K, c->n_slots, false, c->stream);
   return finish(c);
 }
 
@@ -561,6 +592,66 @@ int dml_step(dml_ctx* c, int64_t nsteps) {
   int rc = dml_step_async(c, nsteps);
   if (rc) return rc;
   return finish(c);
+}
+
+int dml_time_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* ms) {
+  if (!c || !ms || nsteps <= 0) return DML_E_ARG;
+  if (!c->loaded || !c->setup_done) return DML_E_STATE;
+  int rc = build_step_graph(c);
+  if (rc) return rc;
+  if (flush_l2 && (rc = ensure_flush(c)) != 0) return rc;
+  std::vector<cudaEvent_t> ev(2 * nsteps);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  for (int64_t i = 0; i < nsteps; ++i) {
+    if (flush_l2) k_flush(c->flush_buf, kFlushBytes, c->stream);
+    CK(cudaEventRecord(ev[2 * i], c->stream));
+    CK(cudaGraphLaunch(c->step_graph, c->stream));
+    CK(cudaEventRecord(ev[2 * i + 1], c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  double tot = 0;
+  for (int64_t i = 0; i < nsteps; ++i) {
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]));
+    tot += t;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  *ms = tot;
+  return finish(c);
+}
+
+int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phase_ms,
+                      int32_t nphase) {
+  if (!c || !phase_ms || nsteps <= 0 || nphase < DML_NPHASE) return DML_E_ARG;
+  if (!c->loaded || !c->setup_done) return DML_E_STATE;
+  int rc = 0;
+  if (flush_l2 && (rc = ensure_flush(c)) != 0) return rc;
+  const int ne = DML_NPHASE + 1;
+  std::vector<cudaEvent_t> ev(ne * nsteps);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  for (int64_t i = 0; i < nsteps; ++i) {
+    if (flush_l2) k_flush(c->flush_buf, kFlushBytes, c->stream);
+    c->launches_per_step = enqueue_step(c, &ev[ne * i]);
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < nphase; ++k) phase_ms[k] = 0;
+  for (int64_t i = 0; i < nsteps; ++i)
+    for (int k = 0; k < DML_NPHASE; ++k) {
+      float t = 0;
+      CK(cudaEventElapsedTime(&t, ev[ne * i + k], ev[ne * i + k + 1]));
+      phase_ms[k] += t;
+    }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return finish(c);
+}
+
+int dml_launches_per_step(dml_ctx* c) {
+  if (!c) return -DML_E_ARG;
+  if (!c->launches_per_step) {
+    int rc = build_step_graph(c);
+    if (rc) return -rc;
+  }
+  return c->launches_per_step;
 }
 
 int dml_get_counters(dml_ctx* c, dml_counters* o) {

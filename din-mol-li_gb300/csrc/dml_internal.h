@@ -117,20 +117,20 @@ struct Dev {
   int cap;            // atom capacity (hs slots, b slots, ranks)
 };
 
-// ---- kernel launchers (dml_kernels.cu) ----
-void k_step_begin(const Dev& d, cudaStream_t s);
-void k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
-void k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
-void k_force(const Dev& d, const KParams& p, int n_rank, int n_slots, bool fuse_ermak_b,
-             cudaStream_t s);
-void k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
-void k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
-                   cudaStream_t s);
-void k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStream_t s);
-void k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
-void k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
-void k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
-void k_force_setup(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStream_t s);
+// ---- kernel launchers (dml_kernels.cu); each returns the kernels it queued ----
+int k_step_begin(const Dev& d, cudaStream_t s);
+int k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
+int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
+int k_force_pairs(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
+int k_force_sum(const Dev& d, const KParams& p, int n_slots, bool fuse_ermak_b, cudaStream_t s);
+int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
+int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
+                  cudaStream_t s);
+int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStream_t s);
+int k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
+int k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
+int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
+int k_flush(void* buf, size_t bytes, cudaStream_t s);
 
 }  // namespace dml
 

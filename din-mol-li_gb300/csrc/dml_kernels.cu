@@ -12,6 +12,8 @@
 // started at +0 unchanged.
 #include <cuda_runtime.h>
 
+#include <climits>
+
 #include "../../include/dml_rng.h"
 #include "dml_internal.h"
 
@@ -76,6 +78,14 @@ __device__ __forceinline__ void vdist_nint_f(const KParams& p, float4 a, float4 
   z = a.z - b.z;
   x = x - p.boxf[0] * rintf(x * p.one_boxf[0]);
   y = y - p.boxf[1] * rintf(y * p.one_boxf[1]);
+}
+
+// int(x) + 1 for a cell index, with the x86-64 reference semantics: NaN or
+// out-of-range values give the integer indefinite, i.e. an invalid index.
+__device__ __forceinline__ int cell_index(double x, double cell) {
+  double q = x / cell;
+  if (!(q > -2147483649.0 && q < 2147483648.0)) return INT_MIN;
+  return (int)q + 1;
 }
 
 __device__ __forceinline__ int warp_id_global() {
@@ -478,9 +488,9 @@ __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b) {
       return;
     }
     double4 P = d.pos[hs];
-    int c1 = (int)(P.x / p.cell[0]) + 1;
-    int c2 = (int)(P.y / p.cell[1]) + 1;
-    int c3 = (int)(P.z / p.cell[2]) + 1;
+    int c1 = cell_index(P.x, p.cell[0]);
+    int c2 = cell_index(P.y, p.cell[1]);
+    int c3 = cell_index(P.z, p.cell[2]);
     if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > p.ncells[0] + 1 || c2 > p.ncells[1] + 1 ||
         c3 > p.ncells[2] + 1) {
       raise_error(d.sc, DML_E_OUT_OF_TESSELLATION, hs);
@@ -579,7 +589,11 @@ __global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
   if (h < 0) return;
   double4 P = d.pos[h];
   float4 Pf = d.posf[h];
-  int rc[3] = {(int)(P.x / p.cell[0]) + 1, (int)(P.y / p.cell[1]) + 1, (int)(P.z / p.cell[2]) + 1};
+  int rc[3] = {cell_index(P.x, p.cell[0]), cell_index(P.y, p.cell[1]), cell_index(P.z, p.cell[2])};
+  if (rc[0] == INT_MIN || rc[1] == INT_MIN || rc[2] == INT_MIN) {
+    if (lane == 0) raise_error(d.sc, DML_E_OUT_OF_TESSELLATION, h);
+    return;
+  }
   int* row = d.list + (size_t)h * p.mnb;
   int cnt = 0;
   for (int nabor = 0; nabor < 27; ++nabor) {
@@ -1026,47 +1040,69 @@ __global__ void piston_kernel(Dev d, KParams p, int n_slots) {
 inline int nblk(int n, int b = kBlock) { return n > 0 ? (n + b - 1) / b : 1; }
 inline int nblk_warps(int n) { return n > 0 ? (n + (kBlock / 32) - 1) / (kBlock / 32) : 1; }
 
+// Overwrites a buffer larger than L2 (benchmark L2 flush between steps).
+__global__ void flush_kernel(uint4* buf, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) buf[i] = make_uint4((unsigned)i, 0u, 0u, 0u);
+}
+
 }  // namespace
 
-void k_step_begin(const Dev& d, cudaStream_t s) { step_begin_kernel<<<1, 1, 0, s>>>(d.sc); }
+int k_step_begin(const Dev& d, cudaStream_t s) {
+  step_begin_kernel<<<1, 1, 0, s>>>(d.sc);
+  return 1;
+}
 
-void k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
+int k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   ermak_a_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  return 1;
 }
 
-void k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
+int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   brownian_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  return 1;
 }
 
-void k_force(const Dev& d, const KParams& p, int n_rank, int n_slots, bool fuse_b, cudaStream_t s) {
+int k_force_pairs(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   force_pairs_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  return 1;
+}
+
+int k_force_sum(const Dev& d, const KParams& p, int n_slots, bool fuse_b, cudaStream_t s) {
   if (fuse_b)
     force_sum_kernel<true><<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
   else
     force_sum_kernel<false><<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  return 1;
 }
 
-void k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
+int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   ermak_b_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  return 1;
 }
 
-void k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
-                   cudaStream_t s) {
+int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
+                  cudaStream_t s) {
   pbc_dispmax_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
   int nmax = n_slots > n_b ? n_slots : n_b;
   rebuild_prep_kernel<<<nblk(nmax), kBlock, 0, s>>>(d, p, n_slots, n_b);
+  int n = 2;
   if (p.use_cells) {
     cell_scan_kernel<<<1, 1024, 0, s>>>(d, d.ncell_tot);
     cell_scatter_kernel<<<nblk(n_b), kBlock, 0, s>>>(d, n_b);
     cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot);
     list_cells_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+    n += 4;
   } else {
     list_verlet_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank, n_b);
+    n += 1;
   }
   rebuild_done_kernel<<<1, 1, 0, s>>>(d);
+  return n + 1;
 }
 
-void k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStream_t s) {
+int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStream_t s) {
   overlap_init_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
   overlap_detect_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
   overlap_count_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
@@ -1074,19 +1110,29 @@ void k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStre
   overlap_scatter_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
   overlap_pass1_kernel<<<nblk(n_rank, 128), 128, 0, s>>>(d, p);
   overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
+  return 7;
 }
 
-void k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
+int k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   (void)p;
   commit_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
+  return 1;
 }
 
-void k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
+int k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
   calc_rho_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  return 1;
 }
 
-void k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
+int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
   piston_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  return 1;
+}
+
+int k_flush(void* buf, size_t bytes, cudaStream_t s) {
+  size_t n = bytes / sizeof(uint4);
+  flush_kernel<<<152 * 8, 512, 0, s>>>((uint4*)buf, n);
+  return 1;
 }
 
 }  // namespace dml

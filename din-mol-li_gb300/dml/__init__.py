@@ -72,6 +72,9 @@ def lib():
     L.dml_strerror.argtypes = [ctypes.c_int]
     L.dml_last_error.restype = ctypes.c_char_p
     L.dml_last_error.argtypes = [vp]
+    L.dml_time_steps.argtypes = [vp, i64, i32, P(ctypes.c_double)]
+    L.dml_profile_steps.argtypes = [vp, i64, i32, vp, i32]
+    L.dml_launches_per_step.argtypes = [vp]
     L.dml_gen_bcc_slab.argtypes = [i32, i32, i32, ctypes.c_double, vp, i32]
     L.dml_gen_ions.argtypes = [ctypes.c_uint64, i32, ctypes.c_double, ctypes.c_double,
                                ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
@@ -211,6 +214,29 @@ class Simulation:
         a = _abi.atoms_struct(out, n)
         self._check(self.lib.dml_get_atoms(self.h, ctypes.byref(a)), "dml_get_atoms")
         return out
+
+    def time_steps(self, n, flush_l2=True):
+        """Device time [ms] of n steps, each bracketed by CUDA events."""
+        ms = ctypes.c_double()
+        self._check(self.lib.dml_time_steps(self.h, n, 1 if flush_l2 else 0, ctypes.byref(ms)),
+                    "dml_time_steps")
+        return ms.value
+
+    PHASES = ["integrate", "force_pairs", "force_sum", "test_update1", "overlap",
+              "test_update2", "commit", "rho_piston"]
+
+    def profile_steps(self, n, flush_l2=True):
+        """Per-phase device time [ms] summed over n un-graphed steps."""
+        out = np.zeros(len(self.PHASES))
+        self._check(self.lib.dml_profile_steps(self.h, n, 1 if flush_l2 else 0, out.ctypes.data,
+                                               len(out)), "dml_profile_steps")
+        return dict(zip(self.PHASES, out.tolist()))
+
+    def launches_per_step(self):
+        n = self.lib.dml_launches_per_step(self.h)
+        if n < 0:
+            raise DmlError(-n, "dml_launches_per_step")
+        return n
 
     def get_neighbors(self, ld):
         n_ref = self.counters()["n_ref"]

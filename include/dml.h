@@ -196,6 +196,29 @@ int dml_step(dml_ctx* c, int64_t nsteps);
 int dml_step_async(dml_ctx* c, int64_t nsteps);
 int dml_sync(dml_ctx* c);
 
+/* Benchmark support.  dml_time_steps queues nsteps steps like dml_step,
+ * each bracketed by CUDA events on the context stream; with flush_l2 a
+ * 256 MiB buffer is overwritten between steps, outside the events.  *ms is
+ * the sum of the per-step device times.  dml_profile_steps runs nsteps steps
+ * without the graph, recording an event at every phase boundary, and adds
+ * the device time of phase k (DML_PHASE_*) to phase_ms[k].
+ * dml_launches_per_step returns the kernels one step queues (or -status). */
+enum {
+  DML_PHASE_INTEGRATE = 0,   /* ermak_a or cbrownian_hs (+ atom_pbc) */
+  DML_PHASE_FORCE_PAIRS = 1, /* fuerza: list scan, interacting entries */
+  DML_PHASE_FORCE_SUM = 2,   /* fuerza: ordered sums + ermak_b */
+  DML_PHASE_TEST_UPDATE1 = 3,/* test_update after the move (+ rebuild) */
+  DML_PHASE_OVERLAP = 4,     /* overlap_moveback */
+  DML_PHASE_TEST_UPDATE2 = 5,/* test_update after the overlaps */
+  DML_PHASE_COMMIT = 6,      /* F -> CG commit */
+  DML_PHASE_RHO_PISTON = 7,  /* calc_rho + maxz */
+  DML_NPHASE = 8
+};
+int dml_time_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* ms);
+int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phase_ms,
+                      int32_t nphase);
+int dml_launches_per_step(dml_ctx* c);
+
 /* Copies atom state to host arrays (sys%alist order).  a->n must be the
  * array capacity on entry; it is set to the atom count on return. */
 int dml_get_atoms(dml_ctx* c, dml_atoms* a);

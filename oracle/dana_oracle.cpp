@@ -31,6 +31,7 @@
 // -ffast-math: every expression is evaluated in the reference's order.
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -133,6 +134,14 @@ inline double pow7(double x) {
   double x3 = x * x2;
   double x4 = x2 * x2;
   return x3 * x4;
+}
+
+// int() of a real as the x86-64 reference build computes it: truncation,
+// and the integer indefinite (INT_MIN) for NaN or out-of-range values, which
+// makes cgroup_sort_atom stop with "Particle out of tessellation".
+inline int f2i(double x) {
+  if (!(x > -2147483649.0 && x < 2147483648.0)) return INT32_MIN;
+  return (int)x;
 }
 
 struct Frame {
@@ -292,7 +301,10 @@ struct Sim {
     tessellated = true;
   }
   bool cell_of(const Atom& a, int* ci) const {
-    for (int k = 0; k < 3; ++k) ci[k] = (int)(a.pos[k] / cell[k]) + 1;
+    for (int k = 0; k < 3; ++k) {
+      int t = f2i(a.pos[k] / cell[k]);
+      ci[k] = t == INT32_MIN ? INT32_MIN : t + 1;
+    }
     return true;
   }
   // cgroup_sort_atom (Cells.F90:281-302).  silent: attach path (errors
@@ -389,6 +401,10 @@ struct Sim {
     double rcut2 = list_rcut2();
     int rc[3];
     cell_of(ai, rc);
+    if (rc[0] == INT32_MIN || rc[1] == INT32_MIN || rc[2] == INT32_MIN) {
+      fail(DML_E_OUT_OF_TESSELLATION, "Particle out of tessellation");
+      return;
+    }
     for (int nabor = 0; nabor < 27; ++nabor) {
       int nc[3];
       for (int k = 0; k < 3; ++k) nc[k] = kMap[nabor][k] + rc[k];

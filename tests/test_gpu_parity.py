@@ -152,7 +152,7 @@ def test_verlet_path_small_box():
 
 def test_capture_events_happen_and_match():
     """Ions started next to the electrode are captured; counts match exactly."""
-    p = systems.c1_params(integrator=dml.INTEGRATOR_BROWNIAN)
+    p = systems.c1_params(integrator=dml.INTEGRATOR_BROWNIAN, reservoir=dml.RESERVOIR_NONE)
     p.h = 1e-2  # sqrt(2*250*0.01) = 2.2 Å per step: reaches the slab quickly
     atoms = dml.slab_system(10, 10, 2, 60.0, 150, 5.0, 20.0, 3, dmin=3.2)
     g, o = make_pair(p, atoms)
@@ -163,3 +163,30 @@ def test_capture_events_happen_and_match():
     assert_same_state(g, o, "capture run")
     assert_same_counters(g, o, "capture run")
     assert g.counters()["depo"] > 0
+
+
+def test_error_parity_empty_reservoir_piston():
+    """No ion above z0 at start: rho0 = 0, the piston factor is 0/0 and the
+    positions become NaN; both sides stop with 'Particle out of tessellation'
+    at the same step (the reference would stop in cgroup_sort, Cells.F90:293)."""
+    p = systems.c1_params(integrator=dml.INTEGRATOR_BROWNIAN)
+    p.h = 1e-2
+    atoms = dml.slab_system(10, 10, 2, 60.0, 150, 5.0, 20.0, 3, dmin=3.2)
+    g, o = make_pair(p, atoms)
+    g.setup()
+    o.setup()
+    fail_g = fail_o = None
+    for step in range(1, 30):
+        if fail_g is None:
+            try:
+                g.step(1)
+            except dml.DmlError as e:
+                fail_g = (step, e.code)
+        if fail_o is None:
+            try:
+                o.step(1)
+            except RuntimeError as e:
+                fail_o = (step, "OUT_OF_TESSELLATION" in str(e))
+        if fail_g and fail_o:
+            break
+    assert fail_g == (fail_o[0], 4) and fail_o[1]
