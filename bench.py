@@ -238,6 +238,7 @@ def run_gpu(args, ws, rank, local):
     clocks = Clocks(local)
     dist.barrier()
     clocks.start()
+    nupd0 = sim.counters()["nupd"]
     ms = sim.time_steps(args.steps, flush_l2=True)
     clk = clocks.stop()
     dist.barrier()
@@ -246,7 +247,8 @@ def run_gpu(args, ws, rank, local):
     ms_max = dist.reduce(ms, "max")
     ions_all = dist.reduce(n_ion, "sum")
     value = ions_all * args.steps / (ms_max / 1e3)
-    launches = sim.launches_per_step() * args.steps
+    per_step, per_rebuild = sim.launches_per_step()
+    launches = per_step * args.steps + per_rebuild * (c["nupd"] - nupd0)
 
     # Per-phase device times (same work, un-graphed) for the roofline.
     nprof = max(3, min(args.steps, 20))

@@ -25,12 +25,14 @@ struct dml_ctx {
   KParams K;
   Dev D;
   cudaStream_t stream = nullptr;
+  cudaStream_t aux = nullptr;  // captures conditional bodies
   int device = 0;
   bool loaded = false, setup_done = false;
   int n_slots = 0, n_b = 0, n_rank = 0, n_atoms = 0;
   std::vector<int> alist;  // hs slots in sys%alist order
   cudaGraphExec_t step_graph = nullptr;
-  int launches_per_step = 0;
+  int launches_per_step = 0;    // kernels of a step without a list rebuild
+  int launches_per_rebuild = 0; // extra kernels when the list is rebuilt
   void* flush_buf = nullptr;
   std::string last_error;
   Scalars* h_sc = nullptr;  // pinned mirror
@@ -174,17 +176,54 @@ int set_step(dml_ctx* c, int64_t step) {
   return 0;
 }
 
+// test_update inside a graph capture: the displacement-test kernel sets the
+// condition of an IF node whose body is the rebuild (update(), Neighbor.F90:
+// 608-633), so steps without a rebuild launch no rebuild kernel at all.
+int capture_test_update(dml_ctx* c, int* n_base, int* n_body) {
+  cudaStream_t s = c->stream;
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
+  cudaGraphConditionalHandle h;
+  CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+  *n_base += k_pbc_dispmax_cond(c->D, c->K, c->n_slots, h, s);
+  CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(c->aux, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  *n_body += k_rebuild(c->D, c->K, c->n_slots, c->n_b, c->n_rank, c->aux);
+  cudaGraph_t outg;
+  CK(cudaStreamEndCapture(c->aux, &outg));
+  CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return 0;
+}
+
 // One iteration of the loop body of dana.F90:173-265 (without salida,
 // timer_dump and the chunk reservoir), queued on the context stream.  With
-// `ev` (DML_NPHASE + 1 events) the phase boundaries are recorded.  Returns
-// the number of kernels queued.
-int enqueue_step(dml_ctx* c, cudaEvent_t* ev) {
+// `ev` (DML_NPHASE + 1 events) the phase boundaries are recorded.  With
+// `capture` the rebuilds become conditional graph nodes.  Returns 0 or a
+// status; the kernels queued are counted in *n_base (every step) and *n_body
+// (only when the list is rebuilt).
+int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_body) {
   const Dev& d = c->D;
   const KParams& k = c->K;
   cudaStream_t s = c->stream;
-  int n = 0;
+  int n = 0, nb = 0, rc = 0;
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], s);
+  };
+  auto test_update = [&]() -> int {
+    if (capture) return capture_test_update(c, &n, &nb);
+    n += k_test_update(d, k, c->n_slots, c->n_b, c->n_rank, s);
+    return 0;
   };
   mark(DML_PHASE_INTEGRATE);
   n += k_step_begin(d, s);
@@ -200,30 +239,36 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev) {
     mark(DML_PHASE_FORCE_SUM);
   }
   mark(DML_PHASE_TEST_UPDATE1);
-  n += k_test_update(d, k, c->n_slots, c->n_b, c->n_rank, s);
+  if ((rc = test_update()) != 0) return rc;
   mark(DML_PHASE_OVERLAP);
   n += k_overlap(d, k, c->n_rank, c->n_slots, s);
   mark(DML_PHASE_TEST_UPDATE2);
-  n += k_test_update(d, k, c->n_slots, c->n_b, c->n_rank, s);
+  if ((rc = test_update()) != 0) return rc;
   mark(DML_PHASE_COMMIT);
   n += k_capture_commit(d, k, c->n_rank, s);
   mark(DML_PHASE_RHO_PISTON);
   n += k_calc_rho(d, k, c->n_slots, s);
   if (c->P.reservoir == DML_RESERVOIR_PISTON) n += k_piston(d, k, c->n_slots, s);
   mark(DML_NPHASE);
-  return n;
+  if (n_base) *n_base = n;
+  if (n_body) *n_body = nb;
+  return 0;
 }
 
 int build_step_graph(dml_ctx* c) {
   if (c->step_graph) return 0;
   cudaGraph_t g;
-  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  c->launches_per_step = enqueue_step(c, nullptr);
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+  int nb = 0, nr = 0;
+  int rc = enqueue_step(c, nullptr, true, &nb, &nr);
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (rc) return rc;
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
   e = cudaGraphInstantiate(&c->step_graph, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate");
+  c->launches_per_step = nb;
+  c->launches_per_rebuild = nr / 2;
   return 0;
 }
 
@@ -331,6 +376,7 @@ int dml_create(const dml_params* p, dml_ctx** out) {
   make_kparams(c->P, c->K);
   cudaError_t e = cudaGetDevice(&c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_sc, sizeof(Scalars));
   if (e != cudaSuccess) {
     delete c;
@@ -348,6 +394,7 @@ void dml_destroy(dml_ctx* c) {
   if (c->flush_buf) cudaFree(c->flush_buf);
   if (c->h_sc) cudaFreeHost(c->h_sc);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->aux) cudaStreamDestroy(c->aux);
   delete c;
 }
 
@@ -631,7 +678,8 @@ int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phas
   for (auto& e : ev) CK(cudaEventCreate(&e));
   for (int64_t i = 0; i < nsteps; ++i) {
     if (flush_l2) k_flush(c->flush_buf, kFlushBytes, c->stream);
-    c->launches_per_step = enqueue_step(c, &ev[ne * i]);
+    rc = enqueue_step(c, &ev[ne * i], false, nullptr, nullptr);
+    if (rc) return rc;
   }
   CK(cudaStreamSynchronize(c->stream));
   for (int k = 0; k < nphase; ++k) phase_ms[k] = 0;
@@ -645,12 +693,13 @@ int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phas
   return finish(c);
 }
 
-int dml_launches_per_step(dml_ctx* c) {
+int dml_launches_per_step(dml_ctx* c, int32_t* per_rebuild) {
   if (!c) return -DML_E_ARG;
   if (!c->launches_per_step) {
     int rc = build_step_graph(c);
     if (rc) return -rc;
   }
+  if (per_rebuild) *per_rebuild = c->launches_per_rebuild;
   return c->launches_per_step;
 }
 

@@ -126,6 +126,9 @@ int k_force_sum(const Dev& d, const KParams& p, int n_slots, bool fuse_ermak_b, 
 int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
                   cudaStream_t s);
+int k_pbc_dispmax_cond(const Dev& d, const KParams& p, int n_slots,
+                       cudaGraphConditionalHandle h, cudaStream_t s);
+int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, cudaStream_t s);
 int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStream_t s);
 int k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);

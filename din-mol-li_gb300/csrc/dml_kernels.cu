@@ -392,7 +392,8 @@ __device__ __forceinline__ void top2_merge(double& a1, double& a2, double b1, do
 // do_pbc (Groups.F90:1440-1467) + inq_dispmax (Neighbor.F90:635-666) + the
 // update decision (Neighbor.F90:697-710).  The top-2 of squared
 // displacements is order independent, so a tree reduction is exact.
-__global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots) {
+__global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
+                                   cudaGraphConditionalHandle cond_handle) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   double a1 = 1.e-16, a2 = 1.e-16;
   if (s < n_slots && d.state[s] == ST_LIVE) {
@@ -448,22 +449,37 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots) {
     last = (t == gridDim.x - 1);
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    double b1 = 1.e-16, b2 = 1.e-16;
-    for (int b = 0; b < (int)gridDim.x; ++b) {
-      double c1 = ((volatile double*)d.part)[2 * b];
-      double c2 = ((volatile double*)d.part)[2 * b + 1];
-      top2_merge(b1, b2, c1, c2);
-    }
+  if (!last) return;
+  __threadfence();
+  // last block: parallel top-2 over the block partials
+  double b1 = 1.e-16, b2 = 1.e-16;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+    double c1 = __ldcg(d.part + 2 * b), c2 = __ldcg(d.part + 2 * b + 1);
+    top2_merge(b1, b2, c1, c2);
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    double c1 = __shfl_down_sync(0xffffffffu, b1, off);
+    double c2 = __shfl_down_sync(0xffffffffu, b2, off);
+    top2_merge(b1, b2, c1, c2);
+  }
+  __syncthreads();
+  if (lane == 0) {
+    w1[wid] = b1;
+    w2[wid] = b2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double e1 = 1.e-16, e2 = 1.e-16;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) top2_merge(e1, e2, w1[w], w2[w]);
     Scalars* sc = d.sc;
-    int rebuild = (!sc->listed) || (sqrt(b1) + sqrt(b2) > p.skin);
+    int rebuild = (!sc->listed) || (sqrt(e1) + sqrt(e2) > p.skin);
     sc->rebuild = rebuild;
     if (rebuild) {
       sc->nupd += 1;
       sc->max_nn = 0;
     }
     sc->ticket = 0;
+    if (cond) cudaGraphSetConditional(cond_handle, rebuild ? 1u : 0u);
   }
 }
 
@@ -720,19 +736,24 @@ __global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
     d.sc->again = 0;
     d.sc->n_comp = 0;
     d.sc->comp_total = 0;
+    d.sc->passes = 1;
   }
-  if (s >= n_slots) return;
-  d.uf[s] = s;
-  d.active[s] = 0;
-  d.comp_size[s] = 0;
-  d.comp_fill[s] = 0;
-  if (d.state[s] == ST_LIVE && d.rank[s] >= 0) {
-    double4 P = d.pos[s], O = d.old_cg[s];
-    double x, y, z;
-    vdist_nint(p, P, O, x, y, z);
-    double dd = dot3(x, y, z);
+  double dd = 0.0;
+  if (s < n_slots) {
+    d.uf[s] = s;
+    d.active[s] = 0;
+    d.comp_size[s] = 0;
+    d.comp_fill[s] = 0;
+    if (d.state[s] == ST_LIVE && d.rank[s] >= 0) {
+      double4 P = d.pos[s], O = d.old_cg[s];
+      double x, y, z;
+      vdist_nint(p, P, O, x, y, z);
+      dd = dot3(x, y, z);
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) dd = fmax(dd, __shfl_down_sync(0xffffffffu, dd, off));
+  if ((threadIdx.x & 31) == 0 && dd > 0.0)
     atomicMax(&d.sc->delta2_bits, (unsigned long long)__double_as_longlong(dd));
-  }
 }
 
 __device__ int uf_find(volatile int* uf, int x) {
@@ -905,8 +926,14 @@ __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, in
   }
 }
 
-// Pass 1: one thread per component; members sorted by rank first.
-__global__ void overlap_pass1_kernel(Dev d, KParams p) {
+// One thread per component; members sorted by rank first.  With
+// `all_passes` (prob >= 1: a contact capture never fails, so no atom is left
+// with skip = false unless an ion was moved back in its own component) the
+// component runs every pass itself: pass p of the reference examines exactly
+// the members with skip = false, in rank order, whatever the other
+// components do.  Otherwise only pass 1 runs here and the later passes run
+// in overlap_passn_kernel with a barrier per pass.
+__global__ void overlap_pass1_kernel(Dev d, KParams p, int all_passes) {
   int cid = blockIdx.x * blockDim.x + threadIdx.x;
   if (cid >= d.sc->n_comp) return;
   int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
@@ -921,14 +948,27 @@ __global__ void overlap_pass1_kernel(Dev d, KParams p) {
     }
     mem[q] = v;
   }
-  int again = 0;
-  for (int i = 0; i < sz; ++i) {
-    int x = mem[i];
-    if (d.skip[x]) continue;
-    d.skip[x] = 1;
-    overlap_exam(d, p, x, 1, &again);
+  int pass = 1;
+  for (;;) {
+    int again = 0;
+    for (int i = 0; i < sz; ++i) {
+      int x = mem[i];
+      if (d.skip[x]) continue;
+      d.skip[x] = 1;
+      overlap_exam(d, p, x, pass, &again);
+    }
+    if (!all_passes) {
+      if (again) d.sc->again = 1;
+      return;
+    }
+    if (!again) break;
+    if (pass >= p.max_passes) {
+      raise_error(d.sc, DML_E_OVERLAP_PASSES, pass + 1);
+      break;
+    }
+    pass += 1;
   }
-  if (again) d.sc->again = 1;
+  atomicMax(&d.sc->passes, pass);
 }
 
 // Passes 2.. (the recursion): one block, a barrier between passes.
@@ -1084,10 +1124,20 @@ int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
 
 int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
                   cudaStream_t s) {
-  pbc_dispmax_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  pbc_dispmax_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots, 0, 0);
+  return 1 + k_rebuild(d, p, n_slots, n_b, n_rank, s);
+}
+
+int k_pbc_dispmax_cond(const Dev& d, const KParams& p, int n_slots,
+                       cudaGraphConditionalHandle h, cudaStream_t s) {
+  pbc_dispmax_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots, 1, h);
+  return 1;
+}
+
+int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, cudaStream_t s) {
   int nmax = n_slots > n_b ? n_slots : n_b;
   rebuild_prep_kernel<<<nblk(nmax), kBlock, 0, s>>>(d, p, n_slots, n_b);
-  int n = 2;
+  int n = 1;
   if (p.use_cells) {
     cell_scan_kernel<<<1, 1024, 0, s>>>(d, d.ncell_tot);
     cell_scatter_kernel<<<nblk(n_b), kBlock, 0, s>>>(d, n_b);
@@ -1108,7 +1158,9 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStrea
   overlap_count_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
   overlap_assign_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, n_slots);
   overlap_scatter_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
-  overlap_pass1_kernel<<<nblk(n_rank, 128), 128, 0, s>>>(d, p);
+  int all_passes = p.prob >= 1.0;
+  overlap_pass1_kernel<<<nblk(n_rank, 128), 128, 0, s>>>(d, p, all_passes);
+  if (all_passes) return 6;
   overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
   return 7;
 }

@@ -74,7 +74,7 @@ def lib():
     L.dml_last_error.argtypes = [vp]
     L.dml_time_steps.argtypes = [vp, i64, i32, P(ctypes.c_double)]
     L.dml_profile_steps.argtypes = [vp, i64, i32, vp, i32]
-    L.dml_launches_per_step.argtypes = [vp]
+    L.dml_launches_per_step.argtypes = [vp, P(i32)]
     L.dml_gen_bcc_slab.argtypes = [i32, i32, i32, ctypes.c_double, vp, i32]
     L.dml_gen_ions.argtypes = [ctypes.c_uint64, i32, ctypes.c_double, ctypes.c_double,
                                ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
@@ -233,10 +233,12 @@ class Simulation:
         return dict(zip(self.PHASES, out.tolist()))
 
     def launches_per_step(self):
-        n = self.lib.dml_launches_per_step(self.h)
+        """(kernels per step without a rebuild, extra kernels per rebuild)."""
+        r = ctypes.c_int32()
+        n = self.lib.dml_launches_per_step(self.h, ctypes.byref(r))
         if n < 0:
             raise DmlError(-n, "dml_launches_per_step")
-        return n
+        return n, r.value
 
     def get_neighbors(self, ld):
         n_ref = self.counters()["n_ref"]

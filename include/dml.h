@@ -202,7 +202,9 @@ int dml_sync(dml_ctx* c);
  * the sum of the per-step device times.  dml_profile_steps runs nsteps steps
  * without the graph, recording an event at every phase boundary, and adds
  * the device time of phase k (DML_PHASE_*) to phase_ms[k].
- * dml_launches_per_step returns the kernels one step queues (or -status). */
+ * dml_launches_per_step returns the kernels a step launches when the list is
+ * not rebuilt (or -status); *per_rebuild (may be NULL) receives the kernels
+ * each list rebuild adds (the rebuild is a conditional graph node). */
 enum {
   DML_PHASE_INTEGRATE = 0,   /* ermak_a or cbrownian_hs (+ atom_pbc) */
   DML_PHASE_FORCE_PAIRS = 1, /* fuerza: list scan, interacting entries */
@@ -217,7 +219,7 @@ enum {
 int dml_time_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* ms);
 int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phase_ms,
                       int32_t nphase);
-int dml_launches_per_step(dml_ctx* c);
+int dml_launches_per_step(dml_ctx* c, int32_t* per_rebuild);
 
 /* Copies atom state to host arrays (sys%alist order).  a->n must be the
  * array capacity on entry; it is set to the atom count on return. */
