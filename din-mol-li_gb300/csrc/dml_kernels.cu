@@ -161,10 +161,12 @@ __global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
   double vv[3] = {V.x, V.y, V.z};
   double aa[3] = {A.x, A.y, A.z};
   double rv[3];
+  double nq[8];
+  dml_normal_quad(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_ERMAK, 0), &nq[0]);
+  dml_normal_quad(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_ERMAK, 1), &nq[4]);
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    double r1, r2;
-    dml_normal_pair(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_ERMAK, (uint32_t)j), &r1, &r2);
+    double r1 = nq[2 * j], r2 = nq[2 * j + 1];
     double ranr = rf * r1;
     pp[j] = pp[j] + p.cc1 * vv[j] + p.cc2h * aa[j] + ranr;
     rv[j] = vf * (p.crv1 * r1 + p.crv2 * r2);
@@ -198,8 +200,7 @@ __global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
   long long id = d.id[h];
   double fac = P.z > p.dif_switch_z ? p.fac_sc : p.fac_sei;
   double nrm[4];
-  dml_normal_pair(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_BROWN, 0), &nrm[0], &nrm[1]);
-  dml_normal_pair(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_BROWN, 1), &nrm[2], &nrm[3]);
+  dml_normal_quad(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_BROWN, 0), nrm);
   double pp[3] = {P.x, P.y, P.z};
   double vv[3];
 #pragma unroll
@@ -224,76 +225,97 @@ __global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
 }
 
 // ---------------------------------------------------------------- fuerza
-// Pass 1: one warp per hs%ref member scans its list row; every interacting
-// entry (r <= r0, eps != 0) is computed in FP64 and recorded for both atoms
-// with the key (rank, jj) that orders the reference's accumulation.
-__global__ void force_pairs_kernel(Dev d, KParams p, int n_rank) {
+// Exact FP64 evaluation of one list entry (dana.F90:1095-1134), kept out of
+// line so the scan loop stays small; records the entry for both atoms.
+__device__ __noinline__ void force_entry(const Dev& d, const KParams& p, int r, int jj, int h,
+                                         int j, int k, int m, double4 Pi) {
+  double4 Pj = d.pos[j];
+  double vx = Pi.x - Pj.x, vy = Pi.y - Pj.y, vz = Pi.z - Pj.z;
+  if (vx > p.halfbox[0]) {
+    vx = vx - p.box[0];
+  } else if (vx < -p.halfbox[0]) {
+    vx = vx + p.box[0];
+  }
+  if (vy > p.halfbox[1]) {
+    vy = vy - p.box[1];
+  } else if (vy < -p.halfbox[1]) {
+    vy = vy + p.box[1];
+  }
+  double dr = dot3(vx, vy, vz);
+  if (dr > p.r0sq[k - 1][m - 1]) return;
+  double eps = p.eps[k - 1][m - 1];
+  dr = sqrt(dr);
+  double c = p.c0[k - 1][m - 1] / pow7(dr);
+  double b = p.b0[k - 1][m - 1] / pow6(dr);
+  double aux = c * (b - 1.0);
+  EvRec e;
+  e.key = ((unsigned long long)(unsigned)r << 32) | (unsigned)jj;
+  e.fx = aux * vx / dr;
+  e.fy = aux * vy / dr;
+  e.fz = aux * vz / dr;
+  double ea = eps * b * (b - 2.0);
+  ea = ea + eps;
+  e.e = ea * .5;
+  e.pad = 0;
+  int si = atomicAdd(&d.ev_count[h], 1);
+  if (si < p.ev_cap) {
+    e.sign = 1;
+    d.ev[(size_t)h * p.ev_cap + si] = e;
+  } else {
+    raise_error(d.sc, DML_E_EVENT_OVERFLOW, h);
+  }
+  int sj = atomicAdd(&d.ev_count[j], 1);
+  if (sj < p.ev_cap) {
+    e.sign = -1;
+    d.ev[(size_t)j * p.ev_cap + sj] = e;
+  } else {
+    raise_error(d.sc, DML_E_EVENT_OVERFLOW, j);
+  }
+}
+
+// FP32 pre-filter of one entry: true when the entry may interact.  The
+// element of a non-live slot (limbo, Neighbor.F90:1089-1092) is 0 in posf.
+__device__ __forceinline__ bool force_candidate(const KParams& p, float4 Pf, int k, float4 Q,
+                                                int& m) {
+  m = (int)Q.w;
+  if (m == 0) return false;
+  if (k == DML_Z_CG && m == DML_Z_CG) return false;
+  if (p.eps[k - 1][m - 1] == 0.0) return false;  // contributes signed zeros only
+  float fx = Pf.x - Q.x, fy = Pf.y - Q.y, fz = Pf.z - Q.z;
+  if (fx > p.halfboxf[0]) fx -= p.boxf[0]; else if (fx < -p.halfboxf[0]) fx += p.boxf[0];
+  if (fy > p.halfboxf[1]) fy -= p.boxf[1]; else if (fy < -p.halfboxf[1]) fy += p.boxf[1];
+  float drf = fx * fx + fy * fy + fz * fz;
+  return drf <= p.r0f_pref2[k - 1][m - 1];
+}
+
+// Pass 1: one warp per hs%ref member scans its list row (two entries per
+// lane in flight); every interacting entry (r <= r0, eps != 0) is computed
+// in FP64 and recorded for both atoms with the key (rank, jj) that orders the
+// reference's accumulation.
+__global__ void __launch_bounds__(256, 4) force_pairs_kernel(Dev d, KParams p, int n_rank) {
   int r = warp_id_global();
   int lane = threadIdx.x & 31;
   if (r >= n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
   int k = d.typ[h];
-  double4 Pi = d.pos[h];
   float4 Pf = d.posf[h];
   int n = d.nn[h];
   const int* row = d.list + (size_t)h * p.mnb;
-  for (int base = 0; base < n; base += 32) {
-    int jj = base + lane;
-    if (jj >= n) break;
-    int j = row[jj];
-    if (d.state[j] != ST_LIVE) continue;  // limbo (Neighbor.F90:1089-1092)
-    float4 Q = d.posf[j];
-    int m = (int)Q.w;
-    if (k == DML_Z_CG && m == DML_Z_CG) continue;
-    double eps = p.eps[k - 1][m - 1];
-    if (eps == 0.0) continue;  // contributes signed zeros only
-    float fx = Pf.x - Q.x, fy = Pf.y - Q.y, fz = Pf.z - Q.z;
-    if (fx > p.halfboxf[0]) fx -= p.boxf[0]; else if (fx < -p.halfboxf[0]) fx += p.boxf[0];
-    if (fy > p.halfboxf[1]) fy -= p.boxf[1]; else if (fy < -p.halfboxf[1]) fy += p.boxf[1];
-    float drf = fx * fx + fy * fy + fz * fz;
-    if (drf > p.r0f_pref2[k - 1][m - 1]) continue;
-    // exact FP64 (dana.F90:1095-1134)
-    double4 Pj = d.pos[j];
-    double vx = Pi.x - Pj.x, vy = Pi.y - Pj.y, vz = Pi.z - Pj.z;
-    if (vx > p.halfbox[0]) {
-      vx = vx - p.box[0];
-    } else if (vx < -p.halfbox[0]) {
-      vx = vx + p.box[0];
-    }
-    if (vy > p.halfbox[1]) {
-      vy = vy - p.box[1];
-    } else if (vy < -p.halfbox[1]) {
-      vy = vy + p.box[1];
-    }
-    double dr = dot3(vx, vy, vz);
-    if (dr > p.r0sq[k - 1][m - 1]) continue;
-    dr = sqrt(dr);
-    double c = p.c0[k - 1][m - 1] / pow7(dr);
-    double b = p.b0[k - 1][m - 1] / pow6(dr);
-    double aux = c * (b - 1.0);
-    EvRec e;
-    e.key = ((unsigned long long)(unsigned)r << 32) | (unsigned)jj;
-    e.fx = aux * vx / dr;
-    e.fy = aux * vy / dr;
-    e.fz = aux * vz / dr;
-    double ea = eps * b * (b - 2.0);
-    ea = ea + eps;
-    e.e = ea * .5;
-    e.pad = 0;
-    int si = atomicAdd(&d.ev_count[h], 1);
-    if (si < p.ev_cap) {
-      e.sign = 1;
-      d.ev[(size_t)h * p.ev_cap + si] = e;
-    } else {
-      raise_error(d.sc, DML_E_EVENT_OVERFLOW, h);
-    }
-    int sj = atomicAdd(&d.ev_count[j], 1);
-    if (sj < p.ev_cap) {
-      e.sign = -1;
-      d.ev[(size_t)j * p.ev_cap + sj] = e;
-    } else {
-      raise_error(d.sc, DML_E_EVENT_OVERFLOW, j);
+  for (int base = 0; base < n; base += 64) {
+    int jj0 = base + lane, jj1 = jj0 + 32;
+    int j0 = jj0 < n ? __ldg(row + jj0) : -1;
+    int j1 = jj1 < n ? __ldg(row + jj1) : -1;
+    float4 Q0 = make_float4(0.f, 0.f, 0.f, 0.f), Q1 = Q0;
+    if (j0 >= 0) Q0 = d.posf[j0];
+    if (j1 >= 0) Q1 = d.posf[j1];
+    int m0, m1;
+    bool c0 = j0 >= 0 && force_candidate(p, Pf, k, Q0, m0);
+    bool c1 = j1 >= 0 && force_candidate(p, Pf, k, Q1, m1);
+    if (c0 | c1) {
+      double4 Pi = d.pos[h];
+      if (c0) force_entry(d, p, r, jj0, h, j0, k, m0, Pi);
+      if (c1) force_entry(d, p, r, jj1, h, j1, k, m1, Pi);
     }
   }
 }
@@ -571,7 +593,7 @@ __global__ void cell_scatter_kernel(Dev d, int n_b) {
 // Orders each cell by descending hs%b slot: the chain order of
 // cgroup_sort (Cells.F90:267-302), which prepends slots in increasing order.
 // One warp per cell; the sorted cell goes to comp_members (scratch) and is
-// copied back.
+// copied back as hs slots (what the list stores).
 __global__ void cell_order_kernel(Dev d, int ncell) {
   if (!d.sc->rebuild) return;
   int c = warp_id_global();
@@ -580,6 +602,7 @@ __global__ void cell_order_kernel(Dev d, int ncell) {
   int start = d.cell_start[c];
   int num = d.cell_start[c + 1] - start;
   if (lane == 0) d.cell_count[c] = 0;
+  if (num == 1 && lane == 0) d.cell_atoms[start] = d.b2hs[d.cell_atoms[start]];
   if (num <= 1) return;
   const int* seg = d.cell_atoms + start;
   int* tmp = d.comp_members + start;  // scratch of n_b entries
@@ -590,7 +613,7 @@ __global__ void cell_order_kernel(Dev d, int ncell) {
     tmp[rnk] = v;
   }
   __syncwarp();
-  for (int i = lane; i < num; i += 32) ((int*)seg)[i] = tmp[i];
+  for (int i = lane; i < num; i += 32) ((int*)seg)[i] = d.b2hs[tmp[i]];
 }
 
 // ngroup_cells (Neighbor.F90:465-548): one warp per hs%ref member, the 27
@@ -634,8 +657,7 @@ __global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
       bool inc = false;
       int j = -1;
       if (idx < num) {
-        int b = d.cell_atoms[start + idx];
-        j = d.b2hs[b];
+        j = d.cell_atoms[start + idx];  // hs slot, cells in descending b-slot order
         if (j != h) {
           float4 Q = d.posf[j];
           float fx, fy, fz;
@@ -785,7 +807,7 @@ __device__ void uf_union(Scalars* sc, volatile int* uf, int a, int b) {
 
 // Near entries of every hs%ref member: list entries within rc + 2 delta
 // (FP32 with margin; a superset is harmless) in list order.
-__global__ void overlap_detect_kernel(Dev d, KParams p, int n_rank) {
+__global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p, int n_rank) {
   int r = warp_id_global();
   int lane = threadIdx.x & 31;
   if (r >= n_rank) return;
@@ -801,30 +823,35 @@ __global__ void overlap_detect_kernel(Dev d, KParams p, int n_rank) {
   int* near = d.near + (size_t)h * kNearCap;
   int cnt = 0;
   bool any = false;
-  for (int base = 0; base < n; base += 32) {
-    int jj = base + lane;
-    bool inc = false;
-    int j = -1;
-    if (jj < n) {
-      j = row[jj];
-      if (d.state[j] == ST_LIVE) {
-        float4 Q = d.posf[j];
+  for (int base = 0; base < n; base += 64) {
+    int jj0 = base + lane, jj1 = jj0 + 32;
+    int j0 = jj0 < n ? __ldg(row + jj0) : -1;
+    int j1 = jj1 < n ? __ldg(row + jj1) : -1;
+    float4 Q0 = make_float4(0.f, 0.f, 0.f, 0.f), Q1 = Q0;
+    if (j0 >= 0) Q0 = d.posf[j0];
+    if (j1 >= 0) Q1 = d.posf[j1];
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      int j = half ? j1 : j0;
+      float4 Q = half ? Q1 : Q0;
+      bool inc = false;
+      if (j >= 0 && Q.w != 0.f) {
         float fx, fy, fz;
         vdist_nint_f(p, Pf, Q, fx, fy, fz);
         inc = fx * fx + fy * fy + fz * fz <= rn2;
       }
-    }
-    unsigned bal = __ballot_sync(0xffffffffu, inc);
-    int pre = __popc(bal & ((1u << lane) - 1u));
-    if (inc) {
-      if (cnt + pre < kNearCap) near[cnt + pre] = j;
-      if (d.typ[j] != DML_Z_CG) {
-        uf_union(d.sc, (volatile int*)d.uf, h, j);
-        d.active[j] = 1;
+      unsigned bal = __ballot_sync(0xffffffffu, inc);
+      int pre = __popc(bal & ((1u << lane) - 1u));
+      if (inc) {
+        if (cnt + pre < kNearCap) near[cnt + pre] = j;
+        if ((int)Q.w != DML_Z_CG) {
+          uf_union(d.sc, (volatile int*)d.uf, h, j);
+          d.active[j] = 1;
+        }
       }
+      cnt += __popc(bal);
+      any = any || bal != 0;
     }
-    cnt += __popc(bal);
-    any = any || bal != 0;
   }
   if (lane == 0) {
     d.near_count[h] = cnt > kNearCap ? -1 : cnt;

@@ -15,17 +15,21 @@
  * numbers: as easy as 1, 2, 3" (SC'11): ten rounds of two 32x32->64 bit
  * multiplications with the published multipliers and Weyl key increments.
  *
- * Normals come from the Box-Muller transform.  `log`, `sin` and `cos` are NOT
- * taken from libm or CUDA (their results differ between host and device);
- * they are written here from textbook series:
+ * Normals come from the Box-Muller transform evaluated in single precision
+ * (the reference's own gasdev also rounds its radius through a real(4)
+ * intermediate, dana.F90:1380-1381), returned as doubles.  `log`, `sin` and
+ * `cos` are NOT taken from libm or CUDA (their results differ between host
+ * and device); they are written here from textbook series:
  *   log(m) = 2 atanh(s) = 2 (s + s^3/3 + s^5/5 + ...),  s = (m-1)/(m+1),
  *            with m in [sqrt(1/2), sqrt(2)) after removing the binary exponent;
  *   sin, cos: Taylor series on [0, pi/4] after an exact quadrant reduction of
- *            the angle 2*pi*u (u is a multiple of 2^-53, so 4u is exact).
- * Every operation is an IEEE double add, subtract, multiply, divide or sqrt
+ *            the angle 2*pi*u (u is a multiple of 2^-24, so 4u is exact).
+ * Every operation is an IEEE single add, subtract, multiply, divide or sqrt
  * in a fixed order with no fused multiply-add, so host and device agree to
- * the last bit.  Accuracy: |error| < 4e-16 relative for log, < 3e-16 absolute
- * for sin/cos (checked against libm in the CPU test suite).
+ * the last bit.  Accuracy: |error| < 2e-7 relative for log, < 2e-7 absolute
+ * for sin/cos (checked against libm in the CPU test suite).  The radius uses
+ * a 32-bit uniform in (0,1], so the normal tail reaches 6.6 sigma.
+ * Uniforms are doubles with 53 random bits.
  */
 #ifndef DML_RNG_H
 #define DML_RNG_H
@@ -42,6 +46,11 @@
  * (never contracted into FMA); on the host the translation unit is compiled
  * with -ffp-contract=off. */
 #if defined(__CUDA_ARCH__)
+#define DMLF_MUL(a, b) __fmul_rn((a), (b))
+#define DMLF_ADD(a, b) __fadd_rn((a), (b))
+#define DMLF_SUB(a, b) __fsub_rn((a), (b))
+#define DMLF_DIV(a, b) __fdiv_rn((a), (b))
+#define DMLF_SQRT(a) __fsqrt_rn(a)
 #define DML_MUL(a, b) __dmul_rn((a), (b))
 #define DML_ADD(a, b) __dadd_rn((a), (b))
 #define DML_SUB(a, b) __dsub_rn((a), (b))
@@ -50,6 +59,11 @@
 #else
 #include <math.h>
 #include <string.h>
+#define DMLF_MUL(a, b) ((float)(a) * (float)(b))
+#define DMLF_ADD(a, b) ((float)(a) + (float)(b))
+#define DMLF_SUB(a, b) ((float)(a) - (float)(b))
+#define DMLF_DIV(a, b) ((float)(a) / (float)(b))
+#define DMLF_SQRT(a) sqrtf(a)
 #define DML_MUL(a, b) ((a) * (b))
 #define DML_ADD(a, b) ((a) + (b))
 #define DML_SUB(a, b) ((a) - (b))
@@ -142,77 +156,80 @@ DML_HD double dml_bits_f64(uint64_t u) {
 #endif
 }
 
+DML_HD uint32_t dml_f32_bits(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(x);
+#else
+  uint32_t u;
+  memcpy(&u, &x, sizeof u);
+  return u;
+#endif
+}
+
+DML_HD float dml_bits_f32(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float x;
+  memcpy(&x, &u, sizeof x);
+  return x;
+#endif
+}
+
 /* Natural logarithm for normal positive x (the Box-Muller argument lies in
- * [2^-53, 1]).  Exponent split + atanh series, see the header comment. */
-DML_HD double dml_log(double x) {
-  uint64_t bits = dml_f64_bits(x);
-  int e = (int)((bits >> 52) & 0x7FF) - 1023;
-  double m = dml_bits_f64((bits & 0x000FFFFFFFFFFFFFull) | 0x3FF0000000000000ull);
-  if (m > 0x1.6a09e667f3bcdp+0) { /* sqrt(2) */
-    m = DML_MUL(m, 0.5);
+ * [2^-32, 1]).  Exponent split + atanh series, see the header comment. */
+DML_HD float dml_logf(float x) {
+  uint32_t bits = dml_f32_bits(x);
+  int e = (int)((bits >> 23) & 0xFFu) - 127;
+  float m = dml_bits_f32((bits & 0x007FFFFFu) | 0x3F800000u);
+  if (m > 0x1.6a09e6p+0f) { /* sqrt(2) */
+    m = DMLF_MUL(m, 0.5f);
     e += 1;
   }
-  double f = DML_SUB(m, 1.0);          /* exact (Sterbenz) */
-  double s = DML_DIV(f, DML_ADD(2.0, f));
-  double s2 = DML_MUL(s, s);
-  /* r = s2/3 + s2^2/5 + ... + s2^11/23, Horner from the highest term. */
-  double p = 0x1.642c8590b2164p-5;                         /* 1/23 */
-  p = DML_ADD(DML_MUL(p, s2), 0x1.8618618618618p-5);      /* 1/21 */
-  p = DML_ADD(DML_MUL(p, s2), 0x1.af286bca1af28p-5);      /* 1/19 */
-  p = DML_ADD(DML_MUL(p, s2), 0x1.e1e1e1e1e1e1ep-5);      /* 1/17 */
-  p = DML_ADD(DML_MUL(p, s2), 0x1.1111111111111p-4);      /* 1/15 */
-  p = DML_ADD(DML_MUL(p, s2), 0x1.3b13b13b13b14p-4);      /* 1/13 */
-  p = DML_ADD(DML_MUL(p, s2), 0x1.745d1745d1746p-4);      /* 1/11 */
-  p = DML_ADD(DML_MUL(p, s2), 0x1.c71c71c71c71cp-4);      /* 1/9 */
-  p = DML_ADD(DML_MUL(p, s2), 0x1.2492492492492p-3);      /* 1/7 */
-  p = DML_ADD(DML_MUL(p, s2), 0x1.999999999999ap-3);      /* 1/5 */
-  p = DML_ADD(DML_MUL(p, s2), 0x1.5555555555555p-2);      /* 1/3 */
-  double r = DML_MUL(s2, p);
-  double two_s = DML_MUL(2.0, s);
-  double lm = DML_ADD(two_s, DML_MUL(two_s, r));
-  double de = (double)e;
-  /* ln2 split in a high part (exact products with |e| <= 1100) and a low part. */
-  return DML_ADD(DML_MUL(de, 0x1.62e42fefa39efp-1), DML_ADD(lm, DML_MUL(de, 0x1.abc9e3b39803fp-56)));
+  float f = DMLF_SUB(m, 1.0f); /* exact (Sterbenz) */
+  float s = DMLF_DIV(f, DMLF_ADD(2.0f, f));
+  float s2 = DMLF_MUL(s, s);
+  /* r = s2/3 + s2^2/5 + ... + s2^5/11, Horner from the highest term. */
+  float q = 0x1.745d18p-4f;                        /* 1/11 */
+  q = DMLF_ADD(DMLF_MUL(q, s2), 0x1.c71c72p-4f);   /* 1/9 */
+  q = DMLF_ADD(DMLF_MUL(q, s2), 0x1.24924ap-3f);   /* 1/7 */
+  q = DMLF_ADD(DMLF_MUL(q, s2), 0x1.99999ap-3f);   /* 1/5 */
+  q = DMLF_ADD(DMLF_MUL(q, s2), 0x1.555556p-2f);   /* 1/3 */
+  float r = DMLF_MUL(s2, q);
+  float two_s = DMLF_MUL(2.0f, s);
+  float lm = DMLF_ADD(two_s, DMLF_MUL(two_s, r));
+  return DMLF_ADD(DMLF_MUL((float)e, 0x1.62e430p-1f), lm); /* + e ln2 */
 }
 
-/* sin and cos of theta in [0, pi/4] by Taylor series (terms to theta^19 / theta^18). */
-DML_HD void dml_sincos_small(double th, double* s, double* c) {
-  double t2 = DML_MUL(th, th);
-  double ps = -0x1.2f49b46814157p-57;                    /* -1/19! */
-  ps = DML_ADD(DML_MUL(ps, t2), 0x1.952c77030ad4ap-49);  /* +1/17! */
-  ps = DML_ADD(DML_MUL(ps, t2), -0x1.ae7f3e733b81fp-41); /* -1/15! */
-  ps = DML_ADD(DML_MUL(ps, t2), 0x1.6124613a86d09p-33);  /* +1/13! */
-  ps = DML_ADD(DML_MUL(ps, t2), -0x1.ae64567f544e4p-26); /* -1/11! */
-  ps = DML_ADD(DML_MUL(ps, t2), 0x1.71de3a556c734p-19);  /* +1/9! */
-  ps = DML_ADD(DML_MUL(ps, t2), -0x1.a01a01a01a01ap-13); /* -1/7! */
-  ps = DML_ADD(DML_MUL(ps, t2), 0x1.1111111111111p-7);   /* +1/5! */
-  ps = DML_ADD(DML_MUL(ps, t2), -0x1.5555555555555p-3);  /* -1/3! */
-  *s = DML_ADD(th, DML_MUL(DML_MUL(ps, t2), th));
-  double pc = 0x1.6827863b97d97p-53;                     /* +1/18! */
-  pc = DML_ADD(DML_MUL(pc, t2), -0x1.ae7f3e733b81fp-45); /* -1/16! */
-  pc = DML_ADD(DML_MUL(pc, t2), 0x1.93974a8c07c9dp-37);  /* +1/14! */
-  pc = DML_ADD(DML_MUL(pc, t2), -0x1.1eed8eff8d898p-29); /* -1/12! */
-  pc = DML_ADD(DML_MUL(pc, t2), 0x1.27e4fb7789f5cp-22);  /* +1/10! */
-  pc = DML_ADD(DML_MUL(pc, t2), -0x1.a01a01a01a01ap-16); /* -1/8! */
-  pc = DML_ADD(DML_MUL(pc, t2), 0x1.6c16c16c16c17p-10);  /* +1/6! */
-  pc = DML_ADD(DML_MUL(pc, t2), -0x1.5555555555555p-5);  /* -1/4! */
-  pc = DML_ADD(DML_MUL(pc, t2), 0x1.0p-1);               /* +1/2! */
-  *c = DML_SUB(1.0, DML_MUL(pc, t2));
+/* sin and cos of theta in [0, pi/4] by Taylor series (to theta^9 / theta^10). */
+DML_HD void dml_sincosf_small(float th, float* s, float* c) {
+  float t2 = DMLF_MUL(th, th);
+  float ps = 0x1.71de3ap-19f;                        /* +1/9! */
+  ps = DMLF_ADD(DMLF_MUL(ps, t2), -0x1.a01a02p-13f); /* -1/7! */
+  ps = DMLF_ADD(DMLF_MUL(ps, t2), 0x1.111112p-7f);   /* +1/5! */
+  ps = DMLF_ADD(DMLF_MUL(ps, t2), -0x1.555556p-3f);  /* -1/3! */
+  *s = DMLF_ADD(th, DMLF_MUL(DMLF_MUL(ps, t2), th));
+  float pc = -0x1.27e4fcp-22f;                       /* -1/10! */
+  pc = DMLF_ADD(DMLF_MUL(pc, t2), 0x1.a01a02p-16f);  /* +1/8! */
+  pc = DMLF_ADD(DMLF_MUL(pc, t2), -0x1.6c16c2p-10f); /* -1/6! */
+  pc = DMLF_ADD(DMLF_MUL(pc, t2), 0x1.555556p-5f);   /* +1/4! */
+  pc = DMLF_ADD(DMLF_MUL(pc, t2), -0.5f);            /* -1/2! */
+  *c = DMLF_ADD(1.0f, DMLF_MUL(pc, t2));
 }
 
-/* sin(2 pi u) and cos(2 pi u) for u in [0,1) that is a multiple of 2^-53. */
-DML_HD void dml_sincos_2pi(double u, double* sn, double* cs) {
-  double t4 = DML_MUL(u, 4.0); /* exact */
-  double q = floor(t4);
-  double f = DML_SUB(t4, q);  /* exact, [0,1) */
+/* sin(2 pi u) and cos(2 pi u) for u in [0,1) that is a multiple of 2^-24. */
+DML_HD void dml_sincosf_2pi(float u, float* sn, float* cs) {
+  float t4 = DMLF_MUL(u, 4.0f); /* exact */
+  float q = floorf(t4);
+  float f = DMLF_SUB(t4, q);    /* exact, [0,1) */
   int qi = (int)q;
-  int swap = f > 0.5;
-  double g = swap ? DML_SUB(1.0, f) : f; /* exact */
-  double th = DML_MUL(g, 0x1.921fb54442d18p+0); /* g * pi/2, in [0, pi/4] */
-  double s0, c0;
-  dml_sincos_small(th, &s0, &c0);
-  double sa = swap ? c0 : s0; /* sin(f pi/2) */
-  double ca = swap ? s0 : c0; /* cos(f pi/2) */
+  int swap = f > 0.5f;
+  float g = swap ? DMLF_SUB(1.0f, f) : f; /* exact */
+  float th = DMLF_MUL(g, 0x1.921fb6p+0f); /* g * pi/2, in [0, pi/4] */
+  float s0, c0;
+  dml_sincosf_small(th, &s0, &c0);
+  float sa = swap ? c0 : s0; /* sin(f pi/2) */
+  float ca = swap ? s0 : c0; /* cos(f pi/2) */
   switch (qi & 3) {
     case 0: *sn = sa; *cs = ca; break;
     case 1: *sn = ca; *cs = -sa; break;
@@ -221,15 +238,27 @@ DML_HD void dml_sincos_2pi(double u, double* sn, double* cs) {
   }
 }
 
-/* Two independent standard normals from one 128-bit draw (Box-Muller). */
-DML_HD void dml_normal_pair(dml_u4 w, double* n0, double* n1) {
-  double u1 = DML_SUB(1.0, dml_u53(w.w[0], w.w[1])); /* (0,1] */
-  double u2 = dml_u53(w.w[2], w.w[3]);
-  double r = DML_SQRT(DML_MUL(-2.0, dml_log(u1)));
-  double s, c;
-  dml_sincos_2pi(u2, &s, &c);
-  *n0 = DML_MUL(r, c);
-  *n1 = DML_MUL(r, s);
+/* Two standard normals from two 32-bit words (Box-Muller): a uniform in
+ * (0,1] from the first word, an angle from the top 24 bits of the second. */
+DML_HD void dml_normal_pair32(uint32_t a, uint32_t b, double* n0, double* n1) {
+#if defined(__CUDA_ARCH__)
+  float u1 = __fmul_rn(__ull2float_rn((unsigned long long)a + 1ull), 0x1.0p-32f); /* (0,1] */
+  float u2 = __fmul_rn(__uint2float_rn(b >> 8), 0x1.0p-24f);
+#else
+  float u1 = (float)((uint64_t)a + 1ull) * 0x1.0p-32f;
+  float u2 = (float)(b >> 8) * 0x1.0p-24f;
+#endif
+  float r = DMLF_SQRT(DMLF_MUL(-2.0f, dml_logf(u1)));
+  float s, c;
+  dml_sincosf_2pi(u2, &s, &c);
+  *n0 = (double)DMLF_MUL(r, c);
+  *n1 = (double)DMLF_MUL(r, s);
+}
+
+/* Four standard normals from one 128-bit draw. */
+DML_HD void dml_normal_quad(dml_u4 w, double* n) {
+  dml_normal_pair32(w.w[0], w.w[1], &n[0], &n[1]);
+  dml_normal_pair32(w.w[2], w.w[3], &n[2], &n[3]);
 }
 
 /* Uniform on [0,1) from the first two words of a draw. */

@@ -577,14 +577,19 @@ struct Sim {
     for (size_t i = 0; i < ref_list.size(); ++i) {
       Atom& o1 = at[ref_list[i]];
       for (int k = 0; k < 3; ++k) o1.old_cg[k] = o1.pos[k];
+      // Philox: (r1, r2) of x, y from draw 0 and of z from draw 1.
+      double nq[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (rng_mode == RNG_PHILOX) {
+        dml_normal_quad(dml_draw(P.seed, step, (uint64_t)o1.id, DML_RNG_ERMAK, 0), &nq[0]);
+        dml_normal_quad(dml_draw(P.seed, step, (uint64_t)o1.id, DML_RNG_ERMAK, 1), &nq[4]);
+      }
       for (int j = 0; j < 3; ++j) {
         double r1, r2 = 0;
-        dml_u4 w{};
         if (rng_mode == RNG_NR) {
           r1 = gasdev();
         } else {
-          w = dml_draw(P.seed, step, (uint64_t)o1.id, DML_RNG_ERMAK, (uint32_t)j);
-          dml_normal_pair(w, &r1, &r2);
+          r1 = nq[2 * j];
+          r2 = nq[2 * j + 1];
         }
         double ranr = skt / std::sqrt(o1.mass) * sdr * r1;
         o1.pos[j] = o1.pos[j] + cc1 * o1.vel[j] + cc2 * P.h * o1.acel[j] + ranr;
@@ -614,10 +619,8 @@ struct Sim {
       double dif = o1.pos[2] > P.dif_switch_z ? P.dif_sc : P.dif_sei;
       double fac1 = std::sqrt(2.0 * dif * P.h);
       double nrm[4] = {0, 0, 0, 0};
-      if (rng_mode == RNG_PHILOX) {
-        dml_normal_pair(dml_draw(P.seed, step, (uint64_t)o1.id, DML_RNG_BROWN, 0), &nrm[0], &nrm[1]);
-        dml_normal_pair(dml_draw(P.seed, step, (uint64_t)o1.id, DML_RNG_BROWN, 1), &nrm[2], &nrm[3]);
-      }
+      if (rng_mode == RNG_PHILOX)
+        dml_normal_quad(dml_draw(P.seed, step, (uint64_t)o1.id, DML_RNG_BROWN, 0), nrm);
       for (int j = 0; j < 3; ++j) {
         double r1 = rng_mode == RNG_NR ? gasdev() : nrm[j];
         double posold = o1.pos[j];
@@ -941,8 +944,7 @@ struct Sim {
           for (int j = 0; j < 3; ++j) at[hlast].vel[j] = beta * gasdev();
         } else {
           double nv[4];
-          dml_normal_pair(dml_draw(P.seed, step, (uint64_t)t, DML_RNG_GCMC_VEL, 0), &nv[0], &nv[1]);
-          dml_normal_pair(dml_draw(P.seed, step, (uint64_t)t, DML_RNG_GCMC_VEL, 1), &nv[2], &nv[3]);
+          dml_normal_quad(dml_draw(P.seed, step, (uint64_t)t, DML_RNG_GCMC_VEL, 0), nv);
           for (int j = 0; j < 3; ++j) at[hlast].vel[j] = beta * nv[j];
         }
         // Same groups as the template, in group-id order: sys, ref, b, hs, gcmc.
@@ -1520,11 +1522,11 @@ void orc_rng_draw(uint64_t seed, int64_t step, uint64_t id, uint32_t stream, uin
   dml_u4 w = dml_draw(seed, step, id, stream, sub);
   for (int k = 0; k < 4; ++k) out4[k] = w.w[k];
 }
-double orc_rng_log(double x) { return dml_log(x); }
-void orc_rng_sincos_2pi(double u, double* s, double* c) { dml_sincos_2pi(u, s, c); }
-void orc_rng_normal_pair(const uint32_t* w4, double* n0, double* n1) {
+float orc_rng_logf(float x) { return dml_logf(x); }
+void orc_rng_sincosf_2pi(float u, float* s, float* c) { dml_sincosf_2pi(u, s, c); }
+void orc_rng_normal_quad(const uint32_t* w4, double* n4) {
   dml_u4 w;
   for (int k = 0; k < 4; ++k) w.w[k] = w4[k];
-  dml_normal_pair(w, n0, n1);
+  dml_normal_quad(w, n4);
 }
 }

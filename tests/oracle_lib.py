@@ -56,12 +56,11 @@ def load():
                                            ctypes.POINTER(ctypes.c_double), vp]
     lib.orc_rng_draw.argtypes = [ctypes.c_uint64, i64, ctypes.c_uint64, ctypes.c_uint32,
                                  ctypes.c_uint32, vp]
-    lib.orc_rng_log.restype = ctypes.c_double
-    lib.orc_rng_log.argtypes = [ctypes.c_double]
-    lib.orc_rng_sincos_2pi.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_double),
-                                       ctypes.POINTER(ctypes.c_double)]
-    lib.orc_rng_normal_pair.argtypes = [vp, ctypes.POINTER(ctypes.c_double),
-                                        ctypes.POINTER(ctypes.c_double)]
+    lib.orc_rng_logf.restype = ctypes.c_float
+    lib.orc_rng_logf.argtypes = [ctypes.c_float]
+    lib.orc_rng_sincosf_2pi.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_float),
+                                        ctypes.POINTER(ctypes.c_float)]
+    lib.orc_rng_normal_quad.argtypes = [vp, vp]
     _lib = lib
     return lib
 

@@ -49,44 +49,46 @@ def test_draw_matches_python_philox():
 def test_log_accuracy():
     lib = oracle_lib.load()
     rng = np.random.default_rng(1)
-    xs = np.concatenate([rng.random(20000), [2.0**-53, 0.5, 1.0, 0.70710678, 1.41421356 / 2]])
-    xs = xs[xs > 0]
+    xs = np.concatenate([(rng.integers(0, 2**32, 20000) + 1.0) * 2.0**-32,
+                         [2.0**-32, 0.5, 1.0, 0.70710678, 0.75]]).astype(np.float32)
     worst = 0.0
     for x in xs:
-        got = lib.orc_rng_log(float(x))
+        got = lib.orc_rng_logf(float(x))
         ref = math.log(float(x))
         if ref != 0.0:
             worst = max(worst, abs(got - ref) / abs(ref))
         else:
             assert got == 0.0
-    assert worst < 4e-16
+    assert worst < 2e-7
 
 
 def test_sincos_accuracy():
     lib = oracle_lib.load()
-    s, c = ctypes.c_double(), ctypes.c_double()
+    s, c = ctypes.c_float(), ctypes.c_float()
     rng = np.random.default_rng(2)
-    us = np.floor(rng.random(20000) * 2.0**53) / 2.0**53
-    us = np.concatenate([us, [0.0, 0.125, 0.25, 0.375, 0.5, 0.75, 1 - 2.0**-53]])
+    us = np.floor(rng.random(20000) * 2.0**24) / 2.0**24
+    us = np.concatenate([us, [0.0, 0.125, 0.25, 0.375, 0.5, 0.75, 1 - 2.0**-24]])
     worst = 0.0
     for u in us:
-        lib.orc_rng_sincos_2pi(float(u), ctypes.byref(s), ctypes.byref(c))
+        lib.orc_rng_sincosf_2pi(float(u), ctypes.byref(s), ctypes.byref(c))
         a = 2.0 * math.pi * float(u)
         worst = max(worst, abs(s.value - math.sin(a)), abs(c.value - math.cos(a)))
-    # math.sin(2*pi*u) itself carries the rounding of 2*pi*u (< 7e-16 * |a|).
-    assert worst < 5e-15
+    assert worst < 2e-7
 
 
 def test_normals_moments():
     lib = oracle_lib.load()
     w = np.zeros(4, np.uint32)
-    n0, n1 = ctypes.c_double(), ctypes.c_double()
+    n = np.zeros(4)
     vals = []
-    for i in range(20000):
+    for i in range(10000):
         lib.orc_rng_draw(7, i, 3, 1, 0, w.ctypes.data)
-        lib.orc_rng_normal_pair(w.ctypes.data, ctypes.byref(n0), ctypes.byref(n1))
-        vals += [n0.value, n1.value]
+        lib.orc_rng_normal_quad(w.ctypes.data, n.ctypes.data)
+        vals += list(n)
     v = np.array(vals)
     assert abs(v.mean()) < 0.02
     assert abs(v.var() - 1.0) < 0.03
     assert abs((v**4).mean() - 3.0) < 0.15
+    # independence of the two pairs of one draw
+    a = v.reshape(-1, 4)
+    assert abs(np.corrcoef(a[:, 0], a[:, 2])[0, 1]) < 0.03
