@@ -110,6 +110,7 @@ void make_kparams(const dml_params& P, KParams& K) {
       K.b0[i][j] = pow6h(r0);
       K.c0[i][j] = eps * 12.0 * K.b0[i][j];
       K.r0f_pref2[i][j] = (float)((r0 + margin) * (r0 + margin));
+      K.pair_on[i][j] = eps != 0.0;
     }
   for (int t = 0; t < 3; ++t) K.mass[t] = P.mass[t];
   // set_ermak (dana.F90:947-971)
@@ -147,6 +148,9 @@ void make_kparams(const dml_params& P, KParams& K) {
   K.ev_cap = P.event_cap;
   K.max_passes = P.max_passes;
   K.seed = P.seed;
+  K.act = P.act;
+  K.beta_num = P.kb_module * P.temp;
+  K.nadj = P.nadj;
 }
 
 int read_scalars(dml_ctx* c) {
@@ -188,7 +192,7 @@ int capture_test_update(dml_ctx* c, int* n_base, int* n_body) {
   CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
   cudaGraphConditionalHandle h;
   CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
-  *n_base += k_pbc_dispmax_cond(c->D, c->K, c->n_slots, h, s);
+  *n_base += k_pbc_dispmax_cond(c->D, c->K, c->D.cap, h, s);
   CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
   cudaGraphNodeParams cp = {};
   cp.type = cudaGraphNodeTypeConditional;
@@ -199,7 +203,7 @@ int capture_test_update(dml_ctx* c, int* n_base, int* n_body) {
   CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp));
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CK(cudaStreamBeginCaptureToGraph(c->aux, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  *n_body += k_rebuild(c->D, c->K, c->n_slots, c->n_b, c->n_rank, c->aux);
+  *n_body += k_rebuild(c->D, c->K, c->D.cap, c->D.cap, c->D.cap, c->aux);
   cudaGraph_t outg;
   CK(cudaStreamEndCapture(c->aux, &outg));
   CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
@@ -216,39 +220,41 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
   const Dev& d = c->D;
   const KParams& k = c->K;
   cudaStream_t s = c->stream;
+  const int cap = d.cap;  // kernels read the live counts from the device scalars
   int n = 0, nb = 0, rc = 0;
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], s);
   };
   auto test_update = [&]() -> int {
     if (capture) return capture_test_update(c, &n, &nb);
-    n += k_test_update(d, k, c->n_slots, c->n_b, c->n_rank, s);
+    n += k_test_update(d, k, cap, cap, cap, s);
     return 0;
   };
   mark(DML_PHASE_INTEGRATE);
   n += k_step_begin(d, s);
   if (c->P.integrator == DML_INTEGRATOR_ERMAK) {
-    n += k_ermak_a(d, k, c->n_rank, s);
+    n += k_ermak_a(d, k, cap, s);
     mark(DML_PHASE_FORCE_PAIRS);
-    n += k_force_pairs(d, k, c->n_rank, s);
+    n += k_force_pairs(d, k, cap, s);
     mark(DML_PHASE_FORCE_SUM);
-    n += k_force_sum(d, k, c->n_slots, true, s);  // fuerza + ermak_b
+    n += k_force_sum(d, k, cap, true, s);  // fuerza + ermak_b
   } else {
-    n += k_brownian(d, k, c->n_rank, s);
+    n += k_brownian(d, k, cap, s);
     mark(DML_PHASE_FORCE_PAIRS);
     mark(DML_PHASE_FORCE_SUM);
   }
   mark(DML_PHASE_TEST_UPDATE1);
   if ((rc = test_update()) != 0) return rc;
   mark(DML_PHASE_OVERLAP);
-  n += k_overlap(d, k, c->n_rank, c->n_slots, s);
+  n += k_overlap(d, k, cap, cap, s);
   mark(DML_PHASE_TEST_UPDATE2);
   if ((rc = test_update()) != 0) return rc;
   mark(DML_PHASE_COMMIT);
-  n += k_capture_commit(d, k, c->n_rank, s);
+  n += k_capture_commit(d, k, cap, s);
+  if (c->P.reservoir == DML_RESERVOIR_GCMC) n += k_gcmc(d, k, cap, s);
   mark(DML_PHASE_RHO_PISTON);
-  n += k_calc_rho(d, k, c->n_slots, s);
-  if (c->P.reservoir == DML_RESERVOIR_PISTON) n += k_piston(d, k, c->n_slots, s);
+  n += k_calc_rho(d, k, cap, s);
+  if (c->P.reservoir == DML_RESERVOIR_PISTON) n += k_piston(d, k, cap, s);
   mark(DML_NPHASE);
   if (n_base) *n_base = n;
   if (n_body) *n_body = nb;
@@ -358,8 +364,8 @@ int dml_create(const dml_params* p, dml_ctx** out) {
   if (!p || !out) return DML_E_ARG;
   *out = nullptr;
   if (p->reservoir < 0 || p->reservoir > 3) return DML_E_RESERVOIR;
-  if (p->reservoir == DML_RESERVOIR_CHUNKS || p->reservoir == DML_RESERVOIR_GCMC)
-    return DML_E_UNSUPPORTED;
+  if (p->reservoir == DML_RESERVOIR_CHUNKS) return DML_E_UNSUPPORTED;
+  if (p->reservoir == DML_RESERVOIR_GCMC && (p->nadj < 0 || !(p->act > 0))) return DML_E_ARG;
   if (p->precision != DML_PRECISION_FP64) return DML_E_UNSUPPORTED;
   if (!(p->box[0] > 0 && p->box[1] > 0 && p->box[2] > 0 && p->h > 0 && p->rc > 0)) return DML_E_ARG;
   // The FP32 pre-filters assume the minimum image is unambiguous at every cut-off.
@@ -402,7 +408,8 @@ int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
   if (!c || !a || a->n <= 0 || !a->pos || !a->z) return DML_E_ARG;
   if (c->loaded) return DML_E_STATE;
   const int n = a->n;
-  const int cap = std::max(n, c->P.capacity);
+  const int cap = std::max(n, c->P.capacity > 0 ? c->P.capacity
+                                                 : (c->P.reservoir == DML_RESERVOIR_GCMC ? 2 * n + 1024 : n));
   c->P.capacity = cap;
   Dev& d = c->D;
   d.cap = cap;
@@ -436,6 +443,13 @@ int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
   AL(d.cell_start, d.ncell_tot + 1);
   AL(d.cell_fill, d.ncell_tot + 1);
   AL(d.cell_atoms, cap);
+  AL(d.alist, cap);
+  AL(d.apos, cap);
+  AL(d.gorder, cap);
+  AL(d.gpos, cap);
+  AL(d.in_gcmc, cap);
+  AL(d.ins_head, d.ncell_tot + 1);
+  AL(d.ins_next, cap);
   AL(d.ev_count, cap);
   AL(d.ev, (size_t)cap * c->P.event_cap);
   AL(d.near_count, cap);
@@ -458,7 +472,8 @@ int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
   std::vector<double> epot(n);
   std::vector<int8_t> typ(n), skip(n), state(n, ST_LIVE);
   std::vector<long long> id(n);
-  std::vector<int> rank(n, -1), ref, slot(n);
+  std::vector<int> rank(n, -1), ref, slot(n), gorder, gpos(n, -1);
+  std::vector<int8_t> in_gcmc(n, 0);
   int64_t max_id = -1;
   for (int i = 0; i < n; ++i) {
     auto v3 = [&](const double* src, double def) {
@@ -478,13 +493,23 @@ int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
     skip[i] = a->skip ? (a->skip[i] != 0) : 0;
     id[i] = a->id ? a->id[i] : i;
     max_id = std::max<int64_t>(max_id, id[i]);
-    posf[i] = make_float4((float)pos[i].x, (float)pos[i].y, (float)pos[i].z, (float)z);
+    float zbits;
+    std::memcpy(&zbits, &z, sizeof zbits);  // element as integer bits in w
+    posf[i] = make_float4((float)pos[i].x, (float)pos[i].y, (float)pos[i].z, zbits);
     bool in_ref = a->in_ref ? a->in_ref[i] != 0 : (z != DML_Z_CG);
     if (in_ref) {
       rank[i] = (int)ref.size();
       ref.push_back(i);
     }
     slot[i] = i;
+    // gcmc attach loop (dana.F90:130-137): z == 1 atoms in sys order
+    bool g = c->P.reservoir == DML_RESERVOIR_GCMC &&
+             (a->in_gcmc ? a->in_gcmc[i] != 0 : z == DML_Z_LI);
+    if (g) {
+      gpos[i] = (int)gorder.size();
+      gorder.push_back(i);
+      in_gcmc[i] = 1;
+    }
   }
   cudaStream_t s = c->stream;
   CK(cudaMemcpyAsync(d.pos, pos.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
@@ -502,6 +527,12 @@ int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
   CK(cudaMemcpyAsync(d.rank, rank.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(d.bslot, slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(d.b2hs, slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.alist, slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.apos, slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.gpos, gpos.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d.in_gcmc, in_gcmc.data(), n, cudaMemcpyHostToDevice, s));
+  if (!gorder.empty())
+    CK(cudaMemcpyAsync(d.gorder, gorder.data(), sizeof(int) * gorder.size(), cudaMemcpyHostToDevice, s));
   if (!ref.empty())
     CK(cudaMemcpyAsync(d.ref, ref.data(), sizeof(int) * ref.size(), cudaMemcpyHostToDevice, s));
   Scalars sc;
@@ -514,6 +545,12 @@ int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
   sc.n_rank = (int)ref.size();
   sc.n_ref = (int)ref.size();
   sc.n_atoms = n;
+  sc.n_alist = n;
+  sc.n_gorder = (int)gorder.size();
+  sc.n_gcmc = (int)gorder.size();
+  sc.b_nat = n;
+  sc.nlimbo = 0;
+  sc.next_id = max_id + 1;
   *c->h_sc = sc;
   CK(cudaMemcpyAsync(d.sc, c->h_sc, sizeof sc, cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));
@@ -529,7 +566,7 @@ int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
 
 int dml_test_update(dml_ctx* c, int32_t* rebuilt) {
   if (!c || !c->loaded) return DML_E_STATE;
-  k_test_update(c->D, c->K, c->n_slots, c->n_b, c->n_rank, c->stream);
+  k_test_update(c->D, c->K, c->D.cap, c->D.cap, c->D.cap, c->stream);
   int rc = finish(c);
   if (rc) return rc;
   if (rebuilt) *rebuilt = c->h_sc->rebuild;
@@ -538,8 +575,8 @@ int dml_test_update(dml_ctx* c, int32_t* rebuilt) {
 
 int dml_force(dml_ctx* c) {
   if (!c || !c->loaded) return DML_E_STATE;
-  k_force_pairs(c->D, c->K, c->n_rank, c->stream);
-  k_force_sum(c->D, c->K, c->n_slots, false, c->stream);
+  k_force_pairs(c->D, c->K, c->D.cap, c->stream);
+  k_force_sum(c->D, c->K, c->D.cap, false, c->stream);
   return finish(c);
 }
 
@@ -547,13 +584,13 @@ int dml_ermak_a(dml_ctx* c, int64_t step) {
   if (!c || !c->loaded) return DML_E_STATE;
   int rc = set_step(c, step);
   if (rc) return rc;
-  k_ermak_a(c->D, c->K, c->n_rank, c->stream);
+  k_ermak_a(c->D, c->K, c->D.cap, c->stream);
   return finish(c);
 }
 
 int dml_ermak_b(dml_ctx* c) {
   if (!c || !c->loaded) return DML_E_STATE;
-  k_ermak_b(c->D, c->K, c->n_rank, c->stream);
+  k_ermak_b(c->D, c->K, c->D.cap, c->stream);
   return finish(c);
 }
 
@@ -561,7 +598,7 @@ int dml_brownian(dml_ctx* c, int64_t step) {
   if (!c || !c->loaded) return DML_E_STATE;
   int rc = set_step(c, step);
   if (rc) return rc;
-  k_brownian(c->D, c->K, c->n_rank, c->stream);
+  k_brownian(c->D, c->K, c->D.cap, c->stream);
   return finish(c);
 }
 
@@ -569,7 +606,7 @@ int dml_overlap_moveback(dml_ctx* c, int64_t step) {
   if (!c || !c->loaded) return DML_E_STATE;
   int rc = set_step(c, step);
   if (rc) return rc;
-  k_overlap(c->D, c->K, c->n_rank, c->n_slots, c->stream);
+  k_overlap(c->D, c->K, c->D.cap, c->D.cap, c->stream);
   return finish(c);
 }
 
@@ -577,7 +614,7 @@ int dml_capture_commit(dml_ctx* c, int32_t* n_new) {
   if (!c || !c->loaded) return DML_E_STATE;
   int zero = 0;
   CK(cudaMemcpyAsync(&c->D.sc->n_new_cg, &zero, sizeof zero, cudaMemcpyHostToDevice, c->stream));
-  k_capture_commit(c->D, c->K, c->n_rank, c->stream);
+  k_capture_commit(c->D, c->K, c->D.cap, c->stream);
   int rc = finish(c);
   if (rc) return rc;
   if (n_new) *n_new = c->h_sc->n_new_cg;
@@ -585,14 +622,17 @@ int dml_capture_commit(dml_ctx* c, int32_t* n_new) {
 }
 
 int dml_gcmc(dml_ctx* c, int64_t step) {
-  (void)step;
   if (!c || !c->loaded) return DML_E_STATE;
-  return DML_E_UNSUPPORTED;
+  if (c->P.reservoir != DML_RESERVOIR_GCMC) return DML_E_RESERVOIR;
+  int rc = set_step(c, step);
+  if (rc) return rc;
+  k_gcmc(c->D, c->K, c->D.cap, c->stream);
+  return finish(c);
 }
 
 int dml_calc_rho(dml_ctx* c, double* rho) {
   if (!c || !c->loaded) return DML_E_STATE;
-  k_calc_rho(c->D, c->K, c->n_slots, c->stream);
+  k_calc_rho(c->D, c->K, c->D.cap, c->stream);
   int rc = finish(c);
   if (rc) return rc;
   if (rho) *rho = c->h_sc->rho;
@@ -601,7 +641,7 @@ int dml_calc_rho(dml_ctx* c, double* rho) {
 
 int dml_piston(dml_ctx* c) {
   if (!c || !c->loaded) return DML_E_STATE;
-  k_piston(c->D, c->K, c->n_slots, c->stream);
+  k_piston(c->D, c->K, c->D.cap, c->stream);
   return finish(c);
 }
 
@@ -743,14 +783,16 @@ int dml_reset_counters(dml_ctx* c) {
 int dml_get_atoms(dml_ctx* c, dml_atoms* a) {
   if (!c || !a) return DML_E_ARG;
   if (!c->loaded) return DML_E_STATE;
-  const int n = (int)c->alist.size();
-  if (a->n < n) return DML_E_ARG;
-  const int ns = c->n_slots;
+  int rc = read_scalars(c);
+  if (rc) return rc;
+  const int ns = c->h_sc->n_slots, nal = c->h_sc->n_alist;
   const Dev& d = c->D;
   cudaStream_t s = c->stream;
+  std::vector<int> alist(nal);
+  if (nal) CK(cudaMemcpyAsync(alist.data(), d.alist, sizeof(int) * nal, cudaMemcpyDeviceToHost, s));
   std::vector<double4> pos(ns), vel(ns), acel(ns), force(ns), pos_old(ns), old_cg(ns);
   std::vector<double> epot(ns);
-  std::vector<int8_t> typ(ns), skip(ns);
+  std::vector<int8_t> typ(ns), skip(ns), ing(ns);
   std::vector<long long> id(ns);
   std::vector<int> rank(ns);
   CK(cudaMemcpyAsync(pos.data(), d.pos, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
@@ -762,12 +804,19 @@ int dml_get_atoms(dml_ctx* c, dml_atoms* a) {
   if (a->epot) CK(cudaMemcpyAsync(epot.data(), d.epot, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(typ.data(), d.typ, ns, cudaMemcpyDeviceToHost, s));
   if (a->skip) CK(cudaMemcpyAsync(skip.data(), d.skip, ns, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(ing.data(), d.in_gcmc, ns, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(id.data(), d.id, sizeof(long long) * ns, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(rank.data(), d.rank, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  int n = 0;
+  for (int q = 0; q < nal; ++q)
+    if (alist[q] >= 0) ++n;
+  if (a->n < n) return DML_E_ARG;
   a->n = n;
-  for (int i = 0; i < n; ++i) {
-    int h = c->alist[i];
+  int i = 0;
+  for (int q = 0; q < nal; ++q) {
+    int h = alist[q];
+    if (h < 0) continue;
     auto put = [&](double* dst, const double4& v) {
       if (!dst) return;
       dst[3 * i] = v.x;
@@ -784,8 +833,9 @@ int dml_get_atoms(dml_ctx* c, dml_atoms* a) {
     if (a->z) a->z[i] = typ[h];
     if (a->skip) a->skip[i] = skip[h];
     if (a->in_ref) a->in_ref[i] = rank[h] >= 0 ? 1 : 0;
-    if (a->in_gcmc) a->in_gcmc[i] = 0;
+    if (a->in_gcmc) a->in_gcmc[i] = ing[h];
     if (a->id) a->id[i] = id[h];
+    ++i;
   }
   return 0;
 }
@@ -793,32 +843,37 @@ int dml_get_atoms(dml_ctx* c, dml_atoms* a) {
 int dml_get_neighbors(dml_ctx* c, int32_t* n_ref, int32_t* nn, int32_t* list, int32_t ld) {
   if (!c || !n_ref || !nn || !list) return DML_E_ARG;
   if (!c->loaded) return DML_E_STATE;
+  int rc = read_scalars(c);
+  if (rc) return rc;
   const Dev& d = c->D;
   cudaStream_t s = c->stream;
-  const int ns = c->n_slots, mnb = c->P.mnb;
-  std::vector<int> ref(c->n_rank), hnn(ns), state8(ns);
+  const int ns = c->h_sc->n_slots, nr = c->h_sc->n_rank, nal = c->h_sc->n_alist;
+  const int mnb = c->P.mnb;
+  std::vector<int> ref(nr), hnn(ns), alist(nal);
   std::vector<int8_t> st(ns);
-  if (c->n_rank)
-    CK(cudaMemcpyAsync(ref.data(), d.ref, sizeof(int) * c->n_rank, cudaMemcpyDeviceToHost, s));
+  if (nr) CK(cudaMemcpyAsync(ref.data(), d.ref, sizeof(int) * nr, cudaMemcpyDeviceToHost, s));
+  if (nal) CK(cudaMemcpyAsync(alist.data(), d.alist, sizeof(int) * nal, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(hnn.data(), d.nn, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(st.data(), d.state, ns, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  // hs slot -> sys%alist position
   std::vector<int> pos_of(ns, -1);
-  for (size_t i = 0; i < c->alist.size(); ++i) pos_of[c->alist[i]] = (int)i;
+  int q = 0;
+  for (int i = 0; i < nal; ++i)
+    if (alist[i] >= 0) pos_of[alist[i]] = q++;
   std::vector<int> row(mnb);
   int k = 0;
-  for (int r = 0; r < c->n_rank; ++r) {
+  for (int r = 0; r < nr; ++r) {
     int h = ref[r];
     if (h < 0) continue;
     int cnt = hnn[h];
     if (cnt > ld) return DML_E_ARG;
-    if (cnt) {
+    if (cnt)
       CK(cudaMemcpy(row.data(), d.list + (size_t)h * mnb, sizeof(int) * cnt, cudaMemcpyDeviceToHost));
-    }
     nn[k] = cnt;
-    for (int q = 0; q < cnt; ++q) {
-      int j = row[q];
-      list[(size_t)k * ld + q] = st[j] == ST_LIMBO ? -1 : pos_of[j];
+    for (int e = 0; e < cnt; ++e) {
+      int j = row[e];
+      list[(size_t)k * ld + e] = st[j] == ST_LIMBO ? -1 : pos_of[j];
     }
     ++k;
   }

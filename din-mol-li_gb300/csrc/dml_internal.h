@@ -5,7 +5,7 @@
 // `hs` ngroup index (src/Neighbor.F90:32-79); the neighbour list stores hs
 // slots, so every per-atom array is indexed by hs slot:
 //   pos      double4 (x, y, z, 0)            32 B, one sector per gather
-//   posf     float4  (x, y, z, element)      16 B, the FP32 pre-filter copy
+//   posf     float4  (x, y, z, element bits)  16 B, the FP32 pre-filter copy
 //   vel, acel, force, old_cg, pos_old, ranv  double4
 //   epot double, typ/skip/state int8, id int64, rank/bslot int32
 // `ref` holds hs slots in hs%ref order (holes = -1 after captures); ranks
@@ -53,6 +53,13 @@ struct Scalars {
   unsigned int ticket2;
   int rho_count;
   int n_new_cg;
+  // structure (GCMC insertions and deletions)
+  int n_alist;     // positions used in alist (members + holes)
+  int n_gorder;    // positions used in gorder (members + holes)
+  int n_gcmc;      // gcmc%nat
+  int nlimbo;      // hs%nlimbo
+  int b_nat;       // hs%b%nat
+  long long next_id;
 };
 
 struct EvRec {            // one interacting list entry seen from one atom
@@ -76,6 +83,7 @@ struct KParams {
   double skin;
   double eps[3][3], r0sq[3][3], b0[3][3], c0[3][3];  // b0 = r0^6, c0 = eps*12*b0
   float r0f_pref2[3][3];    // FP32 pre-filter thresholds (r0 + margin)^2
+  int pair_on[3][3];        // eps != 0 (other pairs add signed zeros only)
   float rlist_lo2, rlist_hi2; // list shell bounds (FP32)
   float margin;             // FP32 position error bound
   float boxf[3], halfboxf[3], one_boxf[3];
@@ -91,6 +99,9 @@ struct KParams {
   int integrator, reservoir;
   int mnb, ev_cap, max_passes;
   unsigned long long seed;
+  // gcmc_run (dana.F90:590-713)
+  double act, beta_num;     // beta = sqrt(beta_num / mass), beta_num = kB(module) * T
+  int nadj;
 };
 
 // All device buffers of one context.
@@ -108,6 +119,10 @@ struct Dev {
   // force events
   int* ev_count;
   EvRec* ev;
+  // structure: sys%alist and gcmc%alist orders (hs slots, holes = -1)
+  int *alist, *apos, *gorder, *gpos;
+  int8_t* in_gcmc;
+  int *ins_head, *ins_next;  // atoms inserted at cell-chain heads during gcmc_run
   // overlap
   int *near_count, *near, *uf, *comp_size, *comp_id, *comp_off, *comp_fill, *comp_members, *comp_list;
   // reductions
@@ -134,6 +149,7 @@ int k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s)
 int k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
 int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
 int k_flush(void* buf, size_t bytes, cudaStream_t s);
+int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s);
 
 }  // namespace dml
 

@@ -37,9 +37,13 @@ __device__ __forceinline__ void count_add(unsigned long long* c, unsigned long l
   atomicAdd(c, v);
 }
 
+// FP32 copy of a position; w carries the element as integer bits (0 for a
+// slot that is not live), so reading it needs no conversion instruction.
 __device__ __forceinline__ float4 to_f4(double4 p, int typ) {
-  return make_float4((float)p.x, (float)p.y, (float)p.z, (float)typ);
+  return make_float4((float)p.x, (float)p.y, (float)p.z, __int_as_float(typ));
 }
+
+__device__ __forceinline__ int elem_of(float4 q) { return __float_as_int(q.w); }
 
 __device__ __forceinline__ double dot3(double x, double y, double z) {
   // dot_product as the reference evaluates it: ((0 + x*x) + y*y) + z*z.
@@ -71,13 +75,17 @@ __device__ __forceinline__ void vdist_nint(const KParams& p, double4 a, double4 
   y = y - p.box[1] * round(y * p.one_box[1]);
 }
 
+// FP32 pre-filter distance: minimum image by compare and add (no rounding
+// or conversion instruction; on GB300 those issue on the narrow FP64 pipe).
+// Near half a box the chosen image may differ from the exact one, where both
+// images are farther than any cut-off.
 __device__ __forceinline__ void vdist_nint_f(const KParams& p, float4 a, float4 b, float& x,
                                              float& y, float& z) {
   x = a.x - b.x;
   y = a.y - b.y;
   z = a.z - b.z;
-  x = x - p.boxf[0] * rintf(x * p.one_boxf[0]);
-  y = y - p.boxf[1] * rintf(y * p.one_boxf[1]);
+  if (x > p.halfboxf[0]) x -= p.boxf[0]; else if (x < -p.halfboxf[0]) x += p.boxf[0];
+  if (y > p.halfboxf[1]) y -= p.boxf[1]; else if (y < -p.halfboxf[1]) y += p.boxf[1];
 }
 
 // int(x) + 1 for a cell index, with the x86-64 reference semantics: NaN or
@@ -144,6 +152,7 @@ __device__ __forceinline__ bool atom_pbc_dev(const KParams& p, Scalars* sc, long
 
 // ermak_a (dana.F90:974-1028): one thread per hs%ref member.
 __global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
+  n_rank = d.sc->n_rank;  // grids are sized by capacity
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rank) return;
   int h = d.ref[r];
@@ -188,6 +197,7 @@ __global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
 
 // cbrownian_hs (dana.F90:798-846): one thread per hs%ref member.
 __global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
+  n_rank = d.sc->n_rank;  // grids are sized by capacity
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rank) return;
   int h = d.ref[r];
@@ -277,10 +287,10 @@ __device__ __noinline__ void force_entry(const Dev& d, const KParams& p, int r, 
 // element of a non-live slot (limbo, Neighbor.F90:1089-1092) is 0 in posf.
 __device__ __forceinline__ bool force_candidate(const KParams& p, float4 Pf, int k, float4 Q,
                                                 int& m) {
-  m = (int)Q.w;
+  m = elem_of(Q);
   if (m == 0) return false;
   if (k == DML_Z_CG && m == DML_Z_CG) return false;
-  if (p.eps[k - 1][m - 1] == 0.0) return false;  // contributes signed zeros only
+  if (!p.pair_on[k - 1][m - 1]) return false;  // eps = 0: contributes signed zeros only
   float fx = Pf.x - Q.x, fy = Pf.y - Q.y, fz = Pf.z - Q.z;
   if (fx > p.halfboxf[0]) fx -= p.boxf[0]; else if (fx < -p.halfboxf[0]) fx += p.boxf[0];
   if (fy > p.halfboxf[1]) fy -= p.boxf[1]; else if (fy < -p.halfboxf[1]) fy += p.boxf[1];
@@ -293,6 +303,7 @@ __device__ __forceinline__ bool force_candidate(const KParams& p, float4 Pf, int
 // in FP64 and recorded for both atoms with the key (rank, jj) that orders the
 // reference's accumulation.
 __global__ void __launch_bounds__(256, 4) force_pairs_kernel(Dev d, KParams p, int n_rank) {
+  n_rank = d.sc->n_rank;  // grids are sized by capacity
   int r = warp_id_global();
   int lane = threadIdx.x & 31;
   if (r >= n_rank) return;
@@ -341,6 +352,7 @@ __device__ __forceinline__ void ermak_b_atom(const Dev& d, const KParams& p, int
 // order, with the Newton reaction applied to both atoms of every entry).
 template <bool FUSE_B>
 __global__ void force_sum_kernel(Dev d, KParams p, int n_slots) {
+  n_slots = d.sc->n_slots;  // grids are sized by capacity
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_slots) return;
   if (d.state[s] != ST_LIVE) return;
@@ -396,6 +408,7 @@ __global__ void force_sum_kernel(Dev d, KParams p, int n_slots) {
 }
 
 __global__ void ermak_b_kernel(Dev d, KParams p, int n_rank) {
+  n_rank = d.sc->n_rank;  // grids are sized by capacity
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rank) return;
   int h = d.ref[r];
@@ -416,6 +429,7 @@ __device__ __forceinline__ void top2_merge(double& a1, double& a2, double b1, do
 // displacements is order independent, so a tree reduction is exact.
 __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
                                    cudaGraphConditionalHandle cond_handle) {
+  n_slots = d.sc->n_slots;  // grids are sized by capacity
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   double a1 = 1.e-16, a2 = 1.e-16;
   if (s < n_slots && d.state[s] == ST_LIVE) {
@@ -508,10 +522,13 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
 // update() (Neighbor.F90:608-633) part 1: pos_old = pos, limbo cleaned
 // (igroup_clean, Groups.F90:1036-1053), cell index of every hs%b slot
 // (cgroup_sort_atom, Cells.F90:281-302) and the per-cell counts.
-__global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b) {
-  if (!d.sc->rebuild) return;
+__global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int cells_only) {
+  n_slots = d.sc->n_slots;
+  n_b = d.sc->n_b;
+  if (!cells_only && !d.sc->rebuild) return;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n_slots) {
+  if (!cells_only && s == 0) d.sc->nlimbo = 0;
+  if (!cells_only && s < n_slots) {
     int st = d.state[s];
     if (st == ST_LIVE) {
       d.pos_old[s] = d.pos[s];
@@ -542,8 +559,8 @@ __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b) {
 }
 
 // Exclusive scan of the cell counts (one block).
-__global__ void cell_scan_kernel(Dev d, int ncell) {
-  if (!d.sc->rebuild) return;
+__global__ void cell_scan_kernel(Dev d, int ncell, int force) {
+  if (!force && !d.sc->rebuild) return;
   __shared__ int wsum[32];
   __shared__ int carry;
   if (threadIdx.x == 0) carry = 0;
@@ -580,8 +597,9 @@ __global__ void cell_scan_kernel(Dev d, int ncell) {
   if (threadIdx.x == 0) d.cell_start[ncell] = carry;
 }
 
-__global__ void cell_scatter_kernel(Dev d, int n_b) {
-  if (!d.sc->rebuild) return;
+__global__ void cell_scatter_kernel(Dev d, int n_b, int force) {
+  n_b = d.sc->n_b;
+  if (!force && !d.sc->rebuild) return;
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= n_b) return;
   int c = d.cell_of[b];
@@ -594,8 +612,8 @@ __global__ void cell_scatter_kernel(Dev d, int n_b) {
 // cgroup_sort (Cells.F90:267-302), which prepends slots in increasing order.
 // One warp per cell; the sorted cell goes to comp_members (scratch) and is
 // copied back as hs slots (what the list stores).
-__global__ void cell_order_kernel(Dev d, int ncell) {
-  if (!d.sc->rebuild) return;
+__global__ void cell_order_kernel(Dev d, int ncell, int force) {
+  if (!force && !d.sc->rebuild) return;
   int c = warp_id_global();
   int lane = threadIdx.x & 31;
   if (c >= ncell) return;
@@ -620,6 +638,7 @@ __global__ void cell_order_kernel(Dev d, int ncell) {
 // stencil cells in map order (Cells.F90:28-36), each cell in chain order,
 // wrapped as cell_pbc with mic (Cells.F90:378-404), `rd < (rc+skin)^2`.
 __global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
+  n_rank = d.sc->n_rank;  // grids are sized by capacity
   if (!d.sc->rebuild) return;
   int r = warp_id_global();
   int lane = threadIdx.x & 31;
@@ -692,6 +711,8 @@ __global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
 // ngroup_verlet (Neighbor.F90:358-424): all hs%b slots in index order,
 // `rd > (rc+skin)^2` rejected (so equality is kept), vdistance(ai, aj).
 __global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
+  n_rank = d.sc->n_rank;
+  n_b = d.sc->n_b;
   if (!d.sc->rebuild) return;
   int r = warp_id_global();
   int lane = threadIdx.x & 31;
@@ -753,6 +774,7 @@ __global__ void rebuild_done_kernel(Dev d) {
 // gives exactly the reference's result.
 
 __global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
+  n_slots = d.sc->n_slots;  // grids are sized by capacity
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0) {
     d.sc->again = 0;
@@ -808,6 +830,7 @@ __device__ void uf_union(Scalars* sc, volatile int* uf, int a, int b) {
 // Near entries of every hs%ref member: list entries within rc + 2 delta
 // (FP32 with margin; a superset is harmless) in list order.
 __global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p, int n_rank) {
+  n_rank = d.sc->n_rank;  // grids are sized by capacity
   int r = warp_id_global();
   int lane = threadIdx.x & 31;
   if (r >= n_rank) return;
@@ -835,7 +858,7 @@ __global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p
       int j = half ? j1 : j0;
       float4 Q = half ? Q1 : Q0;
       bool inc = false;
-      if (j >= 0 && Q.w != 0.f) {
+      if (j >= 0 && elem_of(Q) != 0) {
         float fx, fy, fz;
         vdist_nint_f(p, Pf, Q, fx, fy, fz);
         inc = fx * fx + fy * fy + fz * fz <= rn2;
@@ -844,7 +867,7 @@ __global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p
       int pre = __popc(bal & ((1u << lane) - 1u));
       if (inc) {
         if (cnt + pre < kNearCap) near[cnt + pre] = j;
-        if ((int)Q.w != DML_Z_CG) {
+        if (elem_of(Q) != DML_Z_CG) {
           uf_union(d.sc, (volatile int*)d.uf, h, j);
           d.active[j] = 1;
         }
@@ -862,6 +885,7 @@ __global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p
 // Atoms with no near entry are examined trivially in pass 1 (skip = true)
 // and can never be moved; the others are counted per component root.
 __global__ void overlap_count_kernel(Dev d, int n_rank) {
+  n_rank = d.sc->n_rank;  // grids are sized by capacity
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r == 0) d.sc->delta2_bits = 0ull;
   if (r >= n_rank) return;
@@ -877,6 +901,7 @@ __global__ void overlap_count_kernel(Dev d, int n_rank) {
 }
 
 __global__ void overlap_assign_kernel(Dev d, int n_slots) {
+  n_slots = d.sc->n_slots;  // grids are sized by capacity
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_slots) return;
   int sz = d.comp_size[s];
@@ -889,6 +914,7 @@ __global__ void overlap_assign_kernel(Dev d, int n_slots) {
 }
 
 __global__ void overlap_scatter_kernel(Dev d, int n_rank) {
+  n_rank = d.sc->n_rank;  // grids are sized by capacity
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rank) return;
   int h = d.ref[r];
@@ -922,7 +948,7 @@ __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, in
         count_add(&sc->depo, 1ull);
         d.typ[x] = DML_Z_F;
         float4 f = d.posf[x];
-        f.w = (float)DML_Z_F;
+        f.w = __int_as_float(DML_Z_F);
         d.posf[x] = f;
         if (P.z > sc->z0) raise_error(sc, DML_E_DENDRITE, x);
       } else {
@@ -1038,6 +1064,7 @@ __global__ void overlap_passn_kernel(Dev d, KParams p) {
 // dana.F90:228-236: every F member of hs%ref becomes CG and leaves hs%ref
 // (its rank becomes a hole; the order of the remaining members is kept).
 __global__ void commit_kernel(Dev d, int n_rank) {
+  n_rank = d.sc->n_rank;  // grids are sized by capacity
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n_rank) return;
   int h = d.ref[r];
@@ -1045,16 +1072,22 @@ __global__ void commit_kernel(Dev d, int n_rank) {
   if (d.typ[h] != DML_Z_F) return;
   d.typ[h] = DML_Z_CG;
   float4 f = d.posf[h];
-  f.w = (float)DML_Z_CG;
+  f.w = __int_as_float(DML_Z_CG);
   d.posf[h] = f;
   d.rank[h] = -1;
   d.ref[r] = -1;
   atomicSub(&d.sc->n_ref, 1);
   atomicAdd(&d.sc->n_new_cg, 1);
+  if (d.in_gcmc[h]) {  // gcmc%detach (dana.F90:235)
+    d.in_gcmc[h] = 0;
+    d.gorder[d.gpos[h]] = -1;
+    atomicSub(&d.sc->n_gcmc, 1);
+  }
 }
 
 // calc_rho (dana.F90:521-549): integer count, so any reduction order is exact.
 __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
+  n_slots = d.sc->n_slots;  // grids are sized by capacity
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   Scalars* sc = d.sc;
   double z0 = sc->z0;
@@ -1085,6 +1118,7 @@ __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
 
 // maxz (dana.F90:776-794)
 __global__ void piston_kernel(Dev d, KParams p, int n_slots) {
+  n_slots = d.sc->n_slots;  // grids are sized by capacity
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   Scalars* sc = d.sc;
   double z0 = sc->z0;
@@ -1101,6 +1135,411 @@ __global__ void piston_kernel(Dev d, KParams p, int n_slots) {
     double zm = sc->zmax;
     sc->lohi = lohi;
     sc->zmax = zm - lohi * (zm - z0);
+  }
+}
+
+
+// ------------------------------------------------------------------ gcmc_run
+// gcmc_run (dana.F90:590-713): the trials are sequential (each sees the
+// previous one's insertion or deletion), so one block of 1024 threads runs
+// them in order and parallelises inside a trial: the hard-core test over the
+// gcmc group, the m-th in-slab selection, the first-free slot searches
+// (igroup_attach_atom, Groups.F90:1083-1093), the new atom's own list
+// (ngroup_cells_atom over chains that hold this run's insertions at their
+// heads, Cells.F90:299-300) and its appends to the other lists
+// (ngroup_sort_atom, Neighbor.F90:271-318).
+
+__device__ int blk_scan_excl(int v, int* total) {
+  // exclusive scan over a block of up to 1024 threads
+  __shared__ int ws[32];
+  __shared__ int tot;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    int w = lane < nw ? ws[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    ws[lane] = w;
+    if (lane == 31) tot = w;
+  }
+  __syncthreads();
+  int r = (wid > 0 ? ws[wid - 1] : 0) + x - v;
+  *total = tot;
+  __syncthreads();
+  return r;
+}
+
+// Stable in-place compaction of an order array (holes = -1); pos_of[h]
+// receives the new position of every member.
+__device__ int blk_compact(int* arr, int n, int* pos_of) {
+  int out = 0;
+  for (int base = 0; base < n; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    int h = i < n ? arr[i] : -1;
+    int tot;
+    int pre = blk_scan_excl(h >= 0 ? 1 : 0, &tot);
+    __syncthreads();
+    if (h >= 0) {
+      arr[out + pre] = h;
+      pos_of[h] = out + pre;
+    }
+    out += tot;
+    __syncthreads();
+  }
+  for (int i = out + threadIdx.x; i < n; i += blockDim.x) arr[i] = -1;
+  __syncthreads();
+  return out;
+}
+
+__device__ __forceinline__ bool list_entry_in(const KParams& p, double4 a, double4 b, bool strict) {
+  double vx, vy, vz;
+  vdist_nint(p, a, b, vx, vy, vz);
+  double rd = dot3(vx, vy, vz);
+  return strict ? rd < p.rlist2 : !(rd > p.rlist2);
+}
+
+// Own list of a newly attached atom i, one warp (ngroup_cells_atom,
+// Neighbor.F90:550-603, or ngroup_verlet_atom :426-463).
+__device__ void gcmc_own_list(const Dev& d, const KParams& p, int i) {
+  int lane = threadIdx.x & 31;
+  double4 P = d.pos[i];
+  int* row = d.list + (size_t)i * p.mnb;
+  int cnt = 0;
+  if (p.use_cells) {
+    int rc[3] = {cell_index(P.x, p.cell[0]), cell_index(P.y, p.cell[1]), cell_index(P.z, p.cell[2])};
+    for (int nabor = 0; nabor < 27; ++nabor) {
+      int nc[3];
+      for (int k = 0; k < 3; ++k) {
+        int t = c_map[nabor][k] + rc[k] - 1;
+        t = (t + p.ncells[k]) % p.ncells[k];
+        nc[k] = t + 1;
+      }
+      int c = (nc[2] * p.head_dim[1] + nc[1]) * p.head_dim[0] + nc[0];
+      // atoms inserted during this run, most recent first (chain heads)
+      if (lane == 0) {
+        for (int j = d.ins_head[c]; j >= 0; j = d.ins_next[j]) {
+          if (j == i || d.state[j] != ST_LIVE) continue;
+          if (list_entry_in(p, d.pos[j], P, true)) {
+            if (cnt < p.mnb) row[cnt] = j;
+            ++cnt;
+          }
+        }
+      }
+      cnt = __shfl_sync(0xffffffffu, cnt, 0);
+      int start = d.cell_start[c];
+      int num = d.cell_start[c + 1] - start;
+      for (int base = 0; base < num; base += 32) {
+        int idx = base + lane;
+        bool inc = false;
+        int j = -1;
+        if (idx < num) {
+          j = d.cell_atoms[start + idx];
+          if (j != i && d.state[j] == ST_LIVE) inc = list_entry_in(p, d.pos[j], P, true);
+        }
+        unsigned bal = __ballot_sync(0xffffffffu, inc);
+        int pre = __popc(bal & ((1u << lane) - 1u));
+        if (inc && cnt + pre < p.mnb) row[cnt + pre] = j;
+        cnt += __popc(bal);
+      }
+    }
+  } else {
+    int n_b = d.sc->n_b;
+    for (int base = 0; base < n_b; base += 32) {
+      int b = base + lane;
+      bool inc = false;
+      int j = -1;
+      if (b < n_b) {
+        j = d.b2hs[b];
+        if (j >= 0 && j != i) inc = list_entry_in(p, P, d.pos[j], false);
+      }
+      unsigned bal = __ballot_sync(0xffffffffu, inc);
+      int pre = __popc(bal & ((1u << lane) - 1u));
+      if (inc && cnt + pre < p.mnb) row[cnt + pre] = j;
+      cnt += __popc(bal);
+    }
+  }
+  if (lane == 0) {
+    if (cnt > p.mnb) raise_error(d.sc, DML_E_NEIGH_OVERFLOW, i);
+    d.nn[i] = cnt > p.mnb ? p.mnb : cnt;
+  }
+}
+
+__global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
+  Scalars* sc = d.sc;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  __shared__ int s_min, s_max, s_cnt, s_sel, s_go;
+  __shared__ int s_n;
+  const long long step = sc->step;
+  const double z0 = sc->z0, zmax = sc->zmax;
+  const double v = p.box[0] * p.box[1] * (zmax - z0);
+  if (!sc->listed) {
+    if (tid == 0) raise_error(sc, DML_E_STATE, 0);
+    return;
+  }
+  if (p.use_cells)
+    for (int c = tid; c < d.ncell_tot; c += nt) d.ins_head[c] = -1;
+  // order arrays grow by appends: compact them before they could overflow
+  if (sc->n_rank + p.nadj >= d.cap) {
+    int n = blk_compact(d.ref, sc->n_rank, d.rank);
+    if (tid == 0) sc->n_rank = n;
+  }
+  if (sc->n_alist + p.nadj >= d.cap) {
+    int n = blk_compact(d.alist, sc->n_alist, d.apos);
+    if (tid == 0) sc->n_alist = n;
+  }
+  if (sc->n_gorder + p.nadj >= d.cap) {
+    int n = blk_compact(d.gorder, sc->n_gorder, d.gpos);
+    if (tid == 0) sc->n_gorder = n;
+  }
+  if (tid == 0) s_cnt = 0;
+  __syncthreads();
+  {
+    int ng = sc->n_gorder, c = 0;
+    for (int i = tid; i < ng; i += nt) {
+      int h = d.gorder[i];
+      if (h < 0) continue;
+      double z = d.pos[h].z;
+      if (!(z < z0 || z > zmax)) ++c;
+    }
+    if (c) atomicAdd(&s_cnt, c);
+  }
+  __syncthreads();
+  if (tid == 0) s_n = s_cnt;
+  __syncthreads();
+  for (int t = 1; t <= p.nadj; ++t) {
+    int n = s_n;
+    int ng = sc->n_gorder;
+    if (tid == 0) {
+      s_min = INT_MAX;
+      s_max = -1;
+    }
+    __syncthreads();
+    for (int i = tid; i < ng; i += nt)
+      if (d.gorder[i] >= 0) {
+        atomicMin(&s_min, i);
+        atomicMax(&s_max, i);
+      }
+    __syncthreads();
+    if (s_min == INT_MAX) {
+      if (tid == 0) raise_error(sc, DML_E_NO_PARTICLES, t);
+      return;
+    }
+    const int href = d.gorder[s_min], hlast = d.gorder[s_max];
+    dml_u4 w0 = dml_draw(p.seed, step, (uint64_t)t, DML_RNG_GCMC, 0);
+    dml_u4 w1 = dml_draw(p.seed, step, (uint64_t)t, DML_RNG_GCMC, 1);
+    dml_u4 w2 = dml_draw(p.seed, step, (uint64_t)t, DML_RNG_GCMC, 2);
+    double coin = dml_u53(w0.w[0], w0.w[1]);
+    double uacc = dml_u53(w0.w[2], w0.w[3]);
+    if (coin < 0.5) {
+      // creation attempt (dana.F90:627-677)
+      if (p.act * v / (double)(n + 1) < uacc) continue;
+      double r0 = dml_u53(w1.w[0], w1.w[1]) * p.box[0];
+      double r1 = dml_u53(w1.w[2], w1.w[3]) * p.box[1];
+      double r2 = dml_u53(w2.w[0], w2.w[1]) * (zmax - z0) + z0;
+      double4 R = make_double4(r0, r1, r2, 0.0);
+      bool ov = false;
+      for (int i = tid; i < ng && !ov; i += nt) {
+        int h = d.gorder[i];
+        if (h < 0) continue;
+        double vx, vy, vz;  // distance(o%pos, r, o%pbc) = r - o%pos
+        vdist_nint(p, R, d.pos[h], vx, vy, vz);
+        if (dot3(vx, vy, vz) < p.rc2) ov = true;
+      }
+      if (__syncthreads_or(ov)) continue;
+      s_n = n + 1;  // every thread writes the same value
+      // first free hs slot (limbo slots are not free) and hs%b slot
+      int nat = sc->n_atoms + 1, bnat = sc->b_nat + 1;
+      int ns = sc->n_slots, nb = sc->n_b;
+      if (tid == 0) {
+        s_min = INT_MAX;
+        s_sel = INT_MAX;
+      }
+      __syncthreads();
+      if (ns >= nat + sc->nlimbo)
+        for (int i = tid; i < ns; i += nt)
+          if (d.state[i] == ST_NULL) atomicMin(&s_min, i);
+      if (nb >= bnat)
+        for (int b = tid; b < nb; b += nt)
+          if (d.b2hs[b] < 0) atomicMin(&s_sel, b);
+      __syncthreads();
+      int slot = ns >= nat + sc->nlimbo ? s_min : ns;
+      int bs = nb >= bnat ? s_sel : nb;
+      if (slot == INT_MAX || bs == INT_MAX) {
+        if (tid == 0) raise_error(sc, DML_E_INDEX, t);
+        return;
+      }
+      if (slot >= d.cap || bs >= d.cap || sc->n_rank >= d.cap || sc->n_alist >= d.cap ||
+          sc->n_gorder >= d.cap) {
+        if (tid == 0) raise_error(sc, DML_E_CAPACITY, t);
+        return;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        // atom_asign(o, ref) then pos, pos_old = r (dana.F90:659-663)
+        int typ = d.typ[href];
+        d.vel[slot] = d.vel[href];
+        d.force[slot] = d.force[href];
+        d.acel[slot] = d.acel[href];
+        d.epot[slot] = d.epot[href];
+        d.typ[slot] = (int8_t)typ;
+        d.pos[slot] = R;
+        d.pos_old[slot] = R;
+        d.old_cg[slot] = make_double4(1e8, 1e8, 1e8, 0.0);
+        d.posf[slot] = to_f4(R, typ);
+        d.skip[slot] = 0;
+        d.id[slot] = sc->next_id;
+        sc->next_id += 1;
+        d.ev_count[slot] = 0;
+        // Maxwell velocity to the last listed atom (dana.F90:666-668)
+        double beta = sqrt(p.beta_num / p.mass[d.typ[href] - 1]);
+        double nv[4];
+        dml_normal_quad(dml_draw(p.seed, step, (uint64_t)t, DML_RNG_GCMC_VEL, 0), nv);
+        d.vel[hlast] = make_double4(beta * nv[0], beta * nv[1], beta * nv[2], 0.0);
+        // sys
+        int ap = sc->n_alist;
+        d.alist[ap] = slot;
+        d.apos[slot] = ap;
+        sc->n_alist = ap + 1;
+        // hs%ref
+        int rk = sc->n_rank;
+        d.ref[rk] = slot;
+        d.rank[slot] = rk;
+        sc->n_rank = rk + 1;
+        sc->n_ref += 1;
+        // hs%b (cgroup_attach_atom, Cells.F90:105-144)
+        d.b2hs[bs] = slot;
+        d.bslot[slot] = bs;
+        if (bs == nb) sc->n_b = nb + 1;
+        sc->b_nat = bnat;
+        if (p.use_cells) {
+          int c1 = cell_index(R.x, p.cell[0]), c2 = cell_index(R.y, p.cell[1]),
+              c3 = cell_index(R.z, p.cell[2]);
+          if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > p.ncells[0] + 1 || c2 > p.ncells[1] + 1 ||
+              c3 > p.ncells[2] + 1) {
+            raise_error(sc, DML_E_OUT_OF_TESSELLATION, slot);
+          } else {
+            int c = (c3 * p.head_dim[1] + c2) * p.head_dim[0] + c1;
+            d.ins_next[slot] = d.ins_head[c];
+            d.ins_head[c] = slot;
+          }
+        }
+        // hs (igroup slot)
+        d.state[slot] = ST_LIVE;
+        if (slot == ns) sc->n_slots = ns + 1;
+        sc->n_atoms = nat;
+        // gcmc
+        int gp = sc->n_gorder;
+        d.gorder[gp] = slot;
+        d.gpos[slot] = gp;
+        d.in_gcmc[slot] = 1;
+        sc->n_gorder = gp + 1;
+        sc->n_gcmc += 1;
+        sc->gcmc_ins += 1;
+      }
+      __syncthreads();
+      // ngroup_sort_atom: own list, then append to every hs%ref list within reach
+      if (tid < 32) gcmc_own_list(d, p, slot);
+      {
+        int nr = sc->n_rank;
+        double4 A = d.pos[slot];
+        for (int q = tid; q < nr; q += nt) {
+          int j = d.ref[q];
+          if (j < 0 || j == slot) continue;
+          if (!list_entry_in(p, A, d.pos[j], false)) continue;
+          int m = d.nn[j];
+          if (m >= p.mnb) {
+            raise_error(sc, DML_E_NEIGH_OVERFLOW, j);
+            continue;
+          }
+          d.list[(size_t)j * p.mnb + m] = slot;
+          d.nn[j] = m + 1;
+        }
+      }
+      __syncthreads();
+    } else {
+      // destruction attempt (dana.F90:680-707)
+      if ((double)n / (v * p.act) < uacc) continue;
+      double upick = dml_u53(w2.w[2], w2.w[3]);
+      int m = (int)floor(upick * (double)n) + 1;
+      if (m > n) m = n;
+      int hsel = -1;
+      if (m <= 0) {
+        hsel = hlast;  // the walk never reaches m == 0 and ends on the last atom
+      } else {
+        if (tid == 0) {
+          s_cnt = 0;
+          s_go = 1;
+          s_sel = -1;
+        }
+        __syncthreads();
+        for (int base = 0; base < ng && s_go; base += nt) {
+          int i = base + tid;
+          int h = i < ng ? d.gorder[i] : -1;
+          bool in = false;
+          if (h >= 0) {
+            double z = d.pos[h].z;
+            in = !(z < z0) && !(z > zmax);
+          }
+          int tot;
+          int pre = blk_scan_excl(in ? 1 : 0, &tot);
+          if (in && s_cnt + pre + 1 == m) s_sel = h;
+          __syncthreads();
+          if (tid == 0) {
+            s_cnt += tot;
+            if (s_sel >= 0) s_go = 0;
+          }
+          __syncthreads();
+        }
+        hsel = s_sel;
+        if (hsel < 0) {
+          if (tid == 0) raise_error(sc, DML_E_CHOSEN_MISSING, t);
+          return;
+        }
+      }
+      s_n = n - 1;
+      __syncthreads();
+      if (tid == 0) {
+        // atom_destroy: gcmc, hs (nn, hs%ref, hs%b), sys (Groups.F90:433-467)
+        int h = hsel;
+        d.in_gcmc[h] = 0;
+        d.gorder[d.gpos[h]] = -1;
+        sc->n_gcmc -= 1;
+        d.nn[h] = 0;
+        if (d.rank[h] >= 0) {
+          d.ref[d.rank[h]] = -1;
+          d.rank[h] = -1;
+          sc->n_ref -= 1;
+        }
+        if (p.use_cells) {
+          double4 P = d.pos[h];
+          int c1 = cell_index(P.x, p.cell[0]), c2 = cell_index(P.y, p.cell[1]),
+              c3 = cell_index(P.z, p.cell[2]);
+          if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > p.ncells[0] || c2 > p.ncells[1] || c3 > p.ncells[2])
+            raise_error(sc, DML_E_UNSUPPORTED, h);  // tessellation dropped (Cells.F90:320-327)
+        }
+        d.b2hs[d.bslot[h]] = -1;
+        d.bslot[h] = -1;
+        sc->b_nat -= 1;
+        d.state[h] = ST_LIMBO;
+        sc->nlimbo += 1;
+        sc->n_atoms -= 1;
+        float4 f = d.posf[h];
+        f.w = __int_as_float(0);
+        d.posf[h] = f;
+        d.alist[d.apos[h]] = -1;
+        sc->gcmc_del += 1;
+      }
+      __syncthreads();
+    }
   }
 }
 
@@ -1163,12 +1602,12 @@ int k_pbc_dispmax_cond(const Dev& d, const KParams& p, int n_slots,
 
 int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, cudaStream_t s) {
   int nmax = n_slots > n_b ? n_slots : n_b;
-  rebuild_prep_kernel<<<nblk(nmax), kBlock, 0, s>>>(d, p, n_slots, n_b);
+  rebuild_prep_kernel<<<nblk(nmax), kBlock, 0, s>>>(d, p, n_slots, n_b, 0);
   int n = 1;
   if (p.use_cells) {
-    cell_scan_kernel<<<1, 1024, 0, s>>>(d, d.ncell_tot);
-    cell_scatter_kernel<<<nblk(n_b), kBlock, 0, s>>>(d, n_b);
-    cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot);
+    cell_scan_kernel<<<1, 1024, 0, s>>>(d, d.ncell_tot, 0);
+    cell_scatter_kernel<<<nblk(n_b), kBlock, 0, s>>>(d, n_b, 0);
+    cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot, 0);
     list_cells_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
     n += 4;
   } else {
@@ -1206,6 +1645,19 @@ int k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
 int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
   piston_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
   return 1;
+}
+
+int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
+  int n = 0;
+  if (p.use_cells) {
+    rebuild_prep_kernel<<<nblk(cap), kBlock, 0, s>>>(d, p, cap, cap, 1);
+    cell_scan_kernel<<<1, 1024, 0, s>>>(d, d.ncell_tot, 1);
+    cell_scatter_kernel<<<nblk(cap), kBlock, 0, s>>>(d, cap, 1);
+    cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot, 1);
+    n += 4;
+  }
+  gcmc_kernel<<<1, 1024, 0, s>>>(d, p);
+  return n + 1;
 }
 
 int k_flush(void* buf, size_t bytes, cudaStream_t s) {

@@ -61,3 +61,41 @@ def scaled_params(nx, box_z, z0, seed=1234):
     p.skin = 10.0
     p.seed = seed
     return p
+
+
+def gcmc_params(seed=99, integrator=dml.INTEGRATOR_BROWNIAN):
+    """The reference's tests/gcmc run: 100^3 Å box, reservoir z in [80, 100],
+    act 0.000627, 10 trials per step, dt = 5e-5 ps, skin 2 Å (Brownian)."""
+    p = dml.default_params()
+    p.box[:] = [100.0, 100.0, 100.0]
+    p.z0, p.zmax = 80.0, 100.0
+    p.h = 5e-5
+    p.skin = 2.0
+    p.integrator = integrator
+    p.reservoir = dml.RESERVOIR_GCMC
+    p.act = 0.000627
+    p.nadj = 10
+    p.seed = seed
+    p.mnb = 512
+    return p
+
+
+def gcmc_atoms(seed=5):
+    """602 Li+ (1 M in the 100^3 Å box, dana.F90:349-353) at >= 3.2 Å separation."""
+    import numpy as np
+
+    ions = dml.random_ions(seed, 602, 100.0, 100.0, 0.0, 100.0, 3.2)
+    return {"pos": ions, "z": np.full(len(ions), dml.Z_LI, np.int32)}
+
+
+def c5_small_params(seed=7, nadj=32):
+    """Config-5-like electrode system at test size: 35.1 x 35.1 x 60 Å, Ermak,
+    GCMC reservoir slab z in [40, 60]."""
+    p = c1_params(seed=seed)
+    p.reservoir = dml.RESERVOIR_GCMC
+    p.z0, p.zmax = 40.0, 60.0
+    p.act = 0.0045
+    p.nadj = nadj
+    # deleted atoms hold limbo slots until the next list rebuild
+    p.capacity = 16384
+    return p

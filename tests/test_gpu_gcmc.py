@@ -1,0 +1,78 @@
+"""Device gcmc_run vs the oracle, bit-exact (structure, slots, lists).
+
+Insertions reuse the first free slot, go to the head of their cell chain and
+are appended to the other atoms' lists; deletions leave limbo slots; captured
+atoms leave the gcmc group.  The device must reproduce all of it: every state
+array in sys%alist order, the gcmc membership, the neighbour lists (with
+limbo entries) and the insertion/deletion counters.
+"""
+import numpy as np
+import pytest
+
+from tests import oracle_lib, systems
+from tests.test_gpu_parity import (assert_same_counters, assert_same_lists, assert_same_state,
+                                   make_pair)
+import dml
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["pos", "vel", "acel", "force", "epot", "z", "skip", "old_cg", "pos_old", "in_ref",
+          "in_gcmc", "id"]
+COUNTERS = ["try_", "depo", "choques", "choques3", "nupd", "n_ref", "n_atoms", "zmax", "rho",
+            "gcmc_ins", "gcmc_del"]
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    dml.build()
+
+
+def test_gcmc_routine_after_setup():
+    p = systems.gcmc_params()
+    g, o = make_pair(p, systems.gcmc_atoms())
+    g.setup()
+    o.setup()
+    for step in range(1, 6):
+        g.gcmc_run(step)
+        o.gcmc_run(step)
+        assert_same_state(g, o, "gcmc_run %d" % step, FIELDS)
+        assert_same_counters(g, o, "gcmc_run %d" % step, COUNTERS)
+        assert_same_lists(g, o, "gcmc_run %d" % step, ld=1024)
+    c = g.counters()
+    assert c["gcmc_ins"] + c["gcmc_del"] > 0
+
+
+def test_reference_gcmc_case_fused_steps():
+    """tests/gcmc configuration (Brownian + GCMC), Philox streams, 400 steps."""
+    p = systems.gcmc_params()
+    g, o = make_pair(p, systems.gcmc_atoms())
+    g.setup()
+    o.setup()
+    done = 0
+    for chunk in [1, 19, 80, 300]:
+        g.step(chunk)
+        o.step(chunk)
+        done += chunk
+        assert_same_state(g, o, "gcmc after %d" % done, FIELDS)
+        assert_same_counters(g, o, "gcmc after %d" % done, COUNTERS)
+    assert_same_lists(g, o, "gcmc end", ld=1024)
+    c = g.counters()
+    assert c["gcmc_ins"] > 0 and c["gcmc_del"] > 0
+
+
+def test_ermak_gcmc_with_electrode():
+    """Electrode + Ermak forces + GCMC reservoir (config 5 at test size)."""
+    p = systems.c5_small_params()
+    g, o = make_pair(p, systems.c1_atoms(dmin=3.2))
+    g.setup()
+    o.setup()
+    done = 0
+    for chunk in [1, 29, 170]:
+        g.step(chunk)
+        o.step(chunk)
+        done += chunk
+        assert_same_state(g, o, "ermak+gcmc after %d" % done, FIELDS)
+        assert_same_counters(g, o, "ermak+gcmc after %d" % done, COUNTERS)
+    assert_same_lists(g, o, "ermak+gcmc end")
+    c = g.counters()
+    assert c["gcmc_ins"] > 0 and c["gcmc_del"] > 0

@@ -47,3 +47,25 @@ def test_duplicate_stencil_cells_in_c1():
         row = lst[k, : nn[k]]
         dup += len(row) - len(np.unique(row))
     assert dup > 0
+
+
+def test_gcmc_reference_case_runs():
+    p = systems.gcmc_params()
+    o = oracle_lib.Oracle(p)
+    o.set_atoms(systems.gcmc_atoms())
+    o.setup()
+    o.step(200)
+    c = o.counters()
+    assert c["gcmc_ins"] > 0 and c["gcmc_del"] > 0
+    a = o.get_atoms()
+    assert len(a["z"]) == c["n_atoms"]
+
+
+def test_c5_small_runs():
+    p = systems.c5_small_params()
+    o = oracle_lib.Oracle(p)
+    o.set_atoms(systems.c1_atoms(dmin=3.2))
+    o.setup()
+    o.step(200)
+    c = o.counters()
+    assert c["gcmc_ins"] > 0 and c["gcmc_del"] > 0
