@@ -111,6 +111,8 @@ void make_kparams(const dml_params& P, KParams& K) {
       K.c0[i][j] = eps * 12.0 * K.b0[i][j];
       K.r0f_pref2[i][j] = (float)((r0 + margin) * (r0 + margin));
       K.pair_on[i][j] = eps != 0.0;
+      K.r0sqf[i][j] = (float)(r0 * r0);
+      K.epsf[i][j] = (float)eps;
     }
   for (int t = 0; t < 3; ++t) K.mass[t] = P.mass[t];
   // set_ermak (dana.F90:947-971)
@@ -148,6 +150,11 @@ void make_kparams(const dml_params& P, KParams& K) {
   K.ev_cap = P.event_cap;
   K.max_passes = P.max_passes;
   K.seed = P.seed;
+  K.mixed = P.precision == DML_PRECISION_MIXED;
+  K.rcf = (float)P.rc;
+  // 2^32 per eV/Å; 1 eV = 96.485 * 100 ui (dana.F90:23)
+  K.fix_scale = std::ldexp(1.0, 32) / (96.485 * 100.0);
+  K.fix_inv = 1.0 / K.fix_scale;
   K.act = P.act;
   K.beta_num = P.kb_module * P.temp;
   K.nadj = P.nadj;
@@ -366,7 +373,7 @@ int dml_create(const dml_params* p, dml_ctx** out) {
   if (p->reservoir < 0 || p->reservoir > 3) return DML_E_RESERVOIR;
   if (p->reservoir == DML_RESERVOIR_CHUNKS) return DML_E_UNSUPPORTED;
   if (p->reservoir == DML_RESERVOIR_GCMC && (p->nadj < 0 || !(p->act > 0))) return DML_E_ARG;
-  if (p->precision != DML_PRECISION_FP64) return DML_E_UNSUPPORTED;
+  if (p->precision != DML_PRECISION_FP64 && p->precision != DML_PRECISION_MIXED) return DML_E_ARG;
   if (!(p->box[0] > 0 && p->box[1] > 0 && p->box[2] > 0 && p->h > 0 && p->rc > 0)) return DML_E_ARG;
   // The FP32 pre-filters assume the minimum image is unambiguous at every cut-off.
   double rmax = p->rc + p->skin;
@@ -450,6 +457,9 @@ int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
   AL(d.in_gcmc, cap);
   AL(d.ins_head, d.ncell_tot + 1);
   AL(d.ins_next, cap);
+  AL(d.facc, 4 * (size_t)cap);
+  c->K.cand_cap = 16 * cap;
+  AL(d.cand, (size_t)c->K.cand_cap);
   AL(d.ev_count, cap);
   AL(d.ev, (size_t)cap * c->P.event_cap);
   AL(d.near_count, cap);

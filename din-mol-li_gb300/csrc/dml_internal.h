@@ -54,6 +54,7 @@ struct Scalars {
   int rho_count;
   int n_new_cg;
   // structure (GCMC insertions and deletions)
+  int n_cand;      // entries in the force candidate queue
   int n_alist;     // positions used in alist (members + holes)
   int n_gorder;    // positions used in gorder (members + holes)
   int n_gcmc;      // gcmc%nat
@@ -84,6 +85,12 @@ struct KParams {
   double eps[3][3], r0sq[3][3], b0[3][3], c0[3][3];  // b0 = r0^6, c0 = eps*12*b0
   float r0f_pref2[3][3];    // FP32 pre-filter thresholds (r0 + margin)^2
   int pair_on[3][3];        // eps != 0 (other pairs add signed zeros only)
+  // mixed form: FP32 pair math, int64 fixed-point sums
+  int mixed;
+  int cand_cap;
+  float rcf;                // rc (FP32, pre-filters)
+  float r0sqf[3][3], epsf[3][3];
+  double fix_scale, fix_inv; // 2^32 per eV/Å in ui/Å, and its inverse
   float rlist_lo2, rlist_hi2; // list shell bounds (FP32)
   float margin;             // FP32 position error bound
   float boxf[3], halfboxf[3], one_boxf[3];
@@ -116,6 +123,10 @@ struct Dev {
   // cells
   int *cell_of, *cell_count, *cell_start, *cell_fill, *cell_atoms;
   int ncell_tot;
+  // force candidate queue (rank, jj, o1 slot, o2 slot)
+  int4* cand;
+  // mixed form: per-atom int64 fixed-point force (x, y, z) and energy
+  long long* facc;
   // force events
   int* ev_count;
   EvRec* ev;

@@ -235,54 +235,6 @@ __global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
 }
 
 // ---------------------------------------------------------------- fuerza
-// Exact FP64 evaluation of one list entry (dana.F90:1095-1134), kept out of
-// line so the scan loop stays small; records the entry for both atoms.
-__device__ __noinline__ void force_entry(const Dev& d, const KParams& p, int r, int jj, int h,
-                                         int j, int k, int m, double4 Pi) {
-  double4 Pj = d.pos[j];
-  double vx = Pi.x - Pj.x, vy = Pi.y - Pj.y, vz = Pi.z - Pj.z;
-  if (vx > p.halfbox[0]) {
-    vx = vx - p.box[0];
-  } else if (vx < -p.halfbox[0]) {
-    vx = vx + p.box[0];
-  }
-  if (vy > p.halfbox[1]) {
-    vy = vy - p.box[1];
-  } else if (vy < -p.halfbox[1]) {
-    vy = vy + p.box[1];
-  }
-  double dr = dot3(vx, vy, vz);
-  if (dr > p.r0sq[k - 1][m - 1]) return;
-  double eps = p.eps[k - 1][m - 1];
-  dr = sqrt(dr);
-  double c = p.c0[k - 1][m - 1] / pow7(dr);
-  double b = p.b0[k - 1][m - 1] / pow6(dr);
-  double aux = c * (b - 1.0);
-  EvRec e;
-  e.key = ((unsigned long long)(unsigned)r << 32) | (unsigned)jj;
-  e.fx = aux * vx / dr;
-  e.fy = aux * vy / dr;
-  e.fz = aux * vz / dr;
-  double ea = eps * b * (b - 2.0);
-  ea = ea + eps;
-  e.e = ea * .5;
-  e.pad = 0;
-  int si = atomicAdd(&d.ev_count[h], 1);
-  if (si < p.ev_cap) {
-    e.sign = 1;
-    d.ev[(size_t)h * p.ev_cap + si] = e;
-  } else {
-    raise_error(d.sc, DML_E_EVENT_OVERFLOW, h);
-  }
-  int sj = atomicAdd(&d.ev_count[j], 1);
-  if (sj < p.ev_cap) {
-    e.sign = -1;
-    d.ev[(size_t)j * p.ev_cap + sj] = e;
-  } else {
-    raise_error(d.sc, DML_E_EVENT_OVERFLOW, j);
-  }
-}
-
 // FP32 pre-filter of one entry: true when the entry may interact.  The
 // element of a non-live slot (limbo, Neighbor.F90:1089-1092) is 0 in posf.
 __device__ __forceinline__ bool force_candidate(const KParams& p, float4 Pf, int k, float4 Q,
@@ -299,10 +251,12 @@ __device__ __forceinline__ bool force_candidate(const KParams& p, float4 Pf, int
 }
 
 // Pass 1: one warp per hs%ref member scans its list row (two entries per
-// lane in flight); every interacting entry (r <= r0, eps != 0) is computed
-// in FP64 and recorded for both atoms with the key (rank, jj) that orders the
-// reference's accumulation.
-__global__ void __launch_bounds__(256, 4) force_pairs_kernel(Dev d, KParams p, int n_rank) {
+// lane in flight) with the FP32 pre-filter and appends every possibly
+// interacting entry (r <= r0 + margin, eps != 0) to a compact queue.
+// On GB300 an FP64 instruction occupies the narrow FP64 pipe for the whole
+// warp whatever its active lanes, so the exact FP64 work is done afterwards
+// on the dense queue (force_exact_kernel), 32 entries per instruction.
+__global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n_rank) {
   n_rank = d.sc->n_rank;  // grids are sized by capacity
   int r = warp_id_global();
   int lane = threadIdx.x & 31;
@@ -323,10 +277,78 @@ __global__ void __launch_bounds__(256, 4) force_pairs_kernel(Dev d, KParams p, i
     int m0, m1;
     bool c0 = j0 >= 0 && force_candidate(p, Pf, k, Q0, m0);
     bool c1 = j1 >= 0 && force_candidate(p, Pf, k, Q1, m1);
-    if (c0 | c1) {
-      double4 Pi = d.pos[h];
-      if (c0) force_entry(d, p, r, jj0, h, j0, k, m0, Pi);
-      if (c1) force_entry(d, p, r, jj1, h, j1, k, m1, Pi);
+    unsigned b0 = __ballot_sync(0xffffffffu, c0), b1 = __ballot_sync(0xffffffffu, c1);
+    int tot = __popc(b0) + __popc(b1);
+    if (tot == 0) continue;
+    int base_q = 0;
+    if (lane == 0) base_q = atomicAdd(&d.sc->n_cand, tot);
+    base_q = __shfl_sync(0xffffffffu, base_q, 0);
+    unsigned lt = (1u << lane) - 1u;
+    if (c0) {
+      int q = base_q + __popc(b0 & lt);
+      if (q < p.cand_cap) d.cand[q] = make_int4(r, jj0, h, j0);
+    }
+    if (c1) {
+      int q = base_q + __popc(b0) + __popc(b1 & lt);
+      if (q < p.cand_cap) d.cand[q] = make_int4(r, jj1, h, j1);
+    }
+  }
+}
+
+// Exact FP64 evaluation of the queued entries (dana.F90:1095-1134), one
+// thread per entry, recording each interacting entry for both atoms with the
+// key (rank, jj) that orders the reference's accumulation.
+__global__ void force_exact_kernel(Dev d, KParams p) {
+  int nc = d.sc->n_cand;
+  if (nc > p.cand_cap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(d.sc, DML_E_EVENT_OVERFLOW, nc);
+    nc = p.cand_cap;
+  }
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nc; q += gridDim.x * blockDim.x) {
+    int4 c = d.cand[q];
+    int r = c.x, jj = c.y, h = c.z, j = c.w;
+    int k = d.typ[h], m = d.typ[j];
+    double4 Pi = d.pos[h], Pj = d.pos[j];
+    double vx = Pi.x - Pj.x, vy = Pi.y - Pj.y, vz = Pi.z - Pj.z;
+    if (vx > p.halfbox[0]) {
+      vx = vx - p.box[0];
+    } else if (vx < -p.halfbox[0]) {
+      vx = vx + p.box[0];
+    }
+    if (vy > p.halfbox[1]) {
+      vy = vy - p.box[1];
+    } else if (vy < -p.halfbox[1]) {
+      vy = vy + p.box[1];
+    }
+    double dr = dot3(vx, vy, vz);
+    if (dr > p.r0sq[k - 1][m - 1]) continue;
+    double eps = p.eps[k - 1][m - 1];
+    dr = sqrt(dr);
+    double cc = p.c0[k - 1][m - 1] / pow7(dr);
+    double b = p.b0[k - 1][m - 1] / pow6(dr);
+    double aux = cc * (b - 1.0);
+    EvRec e;
+    e.key = ((unsigned long long)(unsigned)r << 32) | (unsigned)jj;
+    e.fx = aux * vx / dr;
+    e.fy = aux * vy / dr;
+    e.fz = aux * vz / dr;
+    double ea = eps * b * (b - 2.0);
+    ea = ea + eps;
+    e.e = ea * .5;
+    e.pad = 0;
+    int si = atomicAdd(&d.ev_count[h], 1);
+    if (si < p.ev_cap) {
+      e.sign = 1;
+      d.ev[(size_t)h * p.ev_cap + si] = e;
+    } else {
+      raise_error(d.sc, DML_E_EVENT_OVERFLOW, h);
+    }
+    int sj = atomicAdd(&d.ev_count[j], 1);
+    if (sj < p.ev_cap) {
+      e.sign = -1;
+      d.ev[(size_t)j * p.ev_cap + sj] = e;
+    } else {
+      raise_error(d.sc, DML_E_EVENT_OVERFLOW, j);
     }
   }
 }
@@ -354,6 +376,7 @@ template <bool FUSE_B>
 __global__ void force_sum_kernel(Dev d, KParams p, int n_slots) {
   n_slots = d.sc->n_slots;  // grids are sized by capacity
   int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) d.sc->n_cand = 0;
   if (s >= n_slots) return;
   if (d.state[s] != ST_LIVE) return;
   int cnt = d.ev_count[s];
@@ -414,6 +437,100 @@ __global__ void ermak_b_kernel(Dev d, KParams p, int n_rank) {
   int h = d.ref[r];
   if (h < 0) return;
   ermak_b_atom(d, p, h, d.typ[h], d.force[h]);
+}
+
+
+// ------------------------------------------------------- mixed-precision force
+// The chosen form of fuerza: the pair difference is taken in FP64 (positions
+// reach 350 Å, where an FP32 coordinate has a 3e-5 Å ulp), the pair force and
+// energy in FP32, and both are accumulated as int64 fixed point (2^32 per
+// eV/Å and per eV).  Integer addition is associative, so the sums do not
+// depend on the order of the atomics: deterministic without ordering.
+__device__ __forceinline__ long long to_fixed(const KParams& p, float v, double scale) {
+  double x = (double)v * scale;
+  if (!(fabs(x) < 4.0e18)) return LLONG_MIN;  // overflow marker
+  return __double2ll_rn(x);
+}
+
+__global__ void force_exact_mixed_kernel(Dev d, KParams p) {
+  int nc = d.sc->n_cand;
+  if (nc > p.cand_cap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(d.sc, DML_E_EVENT_OVERFLOW, nc);
+    nc = p.cand_cap;
+  }
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nc; q += gridDim.x * blockDim.x) {
+    int4 c = d.cand[q];
+    int h = c.z, j = c.w;
+    int k = d.typ[h], m = d.typ[j];
+    double4 Pi = d.pos[h], Pj = d.pos[j];
+    double dx = Pi.x - Pj.x, dy = Pi.y - Pj.y, dz = Pi.z - Pj.z;
+    if (dx > p.halfbox[0]) dx -= p.box[0]; else if (dx < -p.halfbox[0]) dx += p.box[0];
+    if (dy > p.halfbox[1]) dy -= p.box[1]; else if (dy < -p.halfbox[1]) dy += p.box[1];
+    float vx = (float)dx, vy = (float)dy, vz = (float)dz;
+    float r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 > p.r0sqf[k - 1][m - 1]) continue;
+    float inv_r2 = 1.0f / r2;
+    float qq = p.r0sqf[k - 1][m - 1] * inv_r2;
+    float b = qq * qq * qq;                               // (r0/r)^6
+    float eps = p.epsf[k - 1][m - 1];
+    float fr = 12.0f * eps * b * (b - 1.0f) * inv_r2;      // |F|/r
+    float e = 0.5f * (eps * b * (b - 2.0f) + eps);         // half the pair energy
+    long long fx = to_fixed(p, fr * vx, p.fix_scale);
+    long long fy = to_fixed(p, fr * vy, p.fix_scale);
+    long long fz = to_fixed(p, fr * vz, p.fix_scale);
+    long long fe = to_fixed(p, e, p.fix_scale);
+    if (fx == LLONG_MIN || fy == LLONG_MIN || fz == LLONG_MIN || fe == LLONG_MIN) {
+      raise_error(d.sc, DML_E_FIXEDPOINT_OVERFLOW, h);
+      continue;
+    }
+    unsigned long long* ai = (unsigned long long*)(d.facc + 4 * (size_t)h);
+    unsigned long long* aj = (unsigned long long*)(d.facc + 4 * (size_t)j);
+    atomicAdd(ai + 0, (unsigned long long)fx);
+    atomicAdd(ai + 1, (unsigned long long)fy);
+    atomicAdd(ai + 2, (unsigned long long)fz);
+    atomicAdd(ai + 3, (unsigned long long)fe);
+    atomicAdd(aj + 0, (unsigned long long)(-fx));
+    atomicAdd(aj + 1, (unsigned long long)(-fy));
+    atomicAdd(aj + 2, (unsigned long long)(-fz));
+    atomicAdd(aj + 3, (unsigned long long)fe);
+  }
+}
+
+// Fixed point -> double, accumulators cleared, ermak_b fused.
+template <bool FUSE_B>
+__global__ void force_fix_kernel(Dev d, KParams p, int n_slots) {
+  n_slots = d.sc->n_slots;
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0) d.sc->n_cand = 0;
+  if (s >= n_slots) return;
+  if (d.state[s] != ST_LIVE) return;
+  long long* a = d.facc + 4 * (size_t)s;
+  long long ax = a[0], ay = a[1], az = a[2], ae = a[3];
+  bool inref = d.rank[s] >= 0;
+  bool any = (ax | ay | az | ae) != 0;
+  if (!inref && !any) return;
+  double4 F;
+  double ep;
+  const double inv = p.fix_inv;
+  if (inref) {
+    F = make_double4((double)ax * inv, (double)ay * inv, (double)az * inv, 0.0);
+    ep = (double)ae * inv;
+  } else {
+    F = d.force[s];
+    F.x += (double)ax * inv;
+    F.y += (double)ay * inv;
+    F.z += (double)az * inv;
+    ep = d.epot[s] + (double)ae * inv;
+  }
+  if (any) {
+    a[0] = 0;
+    a[1] = 0;
+    a[2] = 0;
+    a[3] = 0;
+  }
+  d.force[s] = F;
+  d.epot[s] = ep;
+  if (FUSE_B && inref) ermak_b_atom(d, p, s, d.typ[s], F);
 }
 
 // ----------------------------------------------------------- test_update
@@ -836,9 +953,9 @@ __global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p
   if (r >= n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
-  double delta = sqrt(__longlong_as_double((long long)d.sc->delta2_bits));
-  double rn = sqrt(p.rc2) + 2.0 * delta;
-  float rnf = (float)rn + 4.0f * p.margin + 1e-3f;
+  // rc + 2 delta in FP32 (sqrtf is exact to an ulp; the margin covers it)
+  float delta = sqrtf(__double2float_ru(__longlong_as_double((long long)d.sc->delta2_bits)));
+  float rnf = (p.rcf + 2.0f * delta) * 1.000001f + 4.0f * p.margin + 1e-3f;
   float rn2 = rnf * rnf;
   float4 Pf = d.posf[h];
   int n = d.nn[h];
@@ -1571,11 +1688,22 @@ int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
 }
 
 int k_force_pairs(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
-  force_pairs_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
-  return 1;
+  force_scan_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  if (p.mixed)
+    force_exact_mixed_kernel<<<152 * 4, kBlock, 0, s>>>(d, p);
+  else
+    force_exact_kernel<<<152 * 4, kBlock, 0, s>>>(d, p);
+  return 2;
 }
 
 int k_force_sum(const Dev& d, const KParams& p, int n_slots, bool fuse_b, cudaStream_t s) {
+  if (p.mixed) {
+    if (fuse_b)
+      force_fix_kernel<true><<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+    else
+      force_fix_kernel<false><<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+    return 1;
+  }
   if (fuse_b)
     force_sum_kernel<true><<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
   else
