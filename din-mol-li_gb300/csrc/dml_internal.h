@@ -137,7 +137,7 @@ struct Dev {
   // overlap
   int *near_count, *near, *uf, *comp_size, *comp_id, *comp_off, *comp_fill, *comp_members, *comp_list;
   // reductions
-  double* part;       // per-block partials (top-2)
+  unsigned long long* part;  // per-block partials (top-2, as double bits)
   int nblk_part;
   Scalars* sc;
   int cap;            // atom capacity (hs slots, b slots, ranks)

@@ -441,10 +441,10 @@ __global__ void ermak_b_kernel(Dev d, KParams p, int n_rank) {
 
 
 // ------------------------------------------------------- mixed-precision force
-// The chosen form of fuerza: the pair difference is taken in FP64 (positions
-// reach 350 Å, where an FP32 coordinate has a 3e-5 Å ulp), the pair force and
-// energy in FP32, and both are accumulated as int64 fixed point (2^32 per
-// eV/Å and per eV).  Integer addition is associative, so the sums do not
+// The chosen form of fuerza: the pair difference and its square are taken in
+// FP64 (positions reach 350 Å, where an FP32 coordinate has a 3e-5 Å ulp),
+// the pair force and energy in FP32, and both are accumulated as int64 fixed
+// point (2^32 per eV/Å and per eV).  Integer addition is associative, so the sums do not
 // depend on the order of the atomics: deterministic without ordering.
 __device__ __forceinline__ long long to_fixed(const KParams& p, float v, double scale) {
   double x = (double)v * scale;
@@ -466,8 +466,11 @@ __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
     double dx = Pi.x - Pj.x, dy = Pi.y - Pj.y, dz = Pi.z - Pj.z;
     if (dx > p.halfbox[0]) dx -= p.box[0]; else if (dx < -p.halfbox[0]) dx += p.box[0];
     if (dy > p.halfbox[1]) dy -= p.box[1]; else if (dy < -p.halfbox[1]) dy += p.box[1];
+    // r^2 from the FP64 difference, rounded once to FP32: the force goes as
+    // r^-14 in the core, so an FP32 sum of squares (3 roundings) would be
+    // amplified about sevenfold.  The pair math below is FP32.
+    float r2 = (float)dot3(dx, dy, dz);
     float vx = (float)dx, vy = (float)dy, vz = (float)dz;
-    float r2 = vx * vx + vy * vy + vz * vz;
     if (r2 > p.r0sqf[k - 1][m - 1]) continue;
     float inv_r2 = 1.0f / r2;
     float qq = p.r0sqf[k - 1][m - 1] * inv_r2;
@@ -534,11 +537,15 @@ __global__ void force_fix_kernel(Dev d, KParams p, int n_slots) {
 }
 
 // ----------------------------------------------------------- test_update
-__device__ __forceinline__ void top2_merge(double& a1, double& a2, double b1, double b2) {
-  double hi = fmax(a1, b1);
-  double lo = fmax(fmin(a1, b1), fmax(a2, b2));
+// Top-2 merge on the bit patterns of non-negative doubles, which order like
+// unsigned integers: the integer pipe gives the FP64 maximum exactly.
+__device__ __forceinline__ void top2_merge(unsigned long long& a1, unsigned long long& a2,
+                                           unsigned long long b1, unsigned long long b2) {
+  unsigned long long hi = a1 > b1 ? a1 : b1;
+  unsigned long long lo1 = a1 > b1 ? b1 : a1;
+  unsigned long long lo2 = a2 > b2 ? a2 : b2;
   a1 = hi;
-  a2 = lo;
+  a2 = lo1 > lo2 ? lo1 : lo2;
 }
 
 // do_pbc (Groups.F90:1440-1467) + inq_dispmax (Neighbor.F90:635-666) + the
@@ -548,7 +555,8 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
                                    cudaGraphConditionalHandle cond_handle) {
   n_slots = d.sc->n_slots;  // grids are sized by capacity
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  double a1 = 1.e-16, a2 = 1.e-16;
+  const unsigned long long tiny = (unsigned long long)__double_as_longlong(1.e-16);
+  unsigned long long a1 = tiny, a2 = tiny;
   if (s < n_slots && d.state[s] == ST_LIVE) {
     double4 P = d.pos[s];
     double4 O = d.pos_old[s];
@@ -577,14 +585,14 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
       d.posf[s] = to_f4(P, d.typ[s]);
     }
     double rd = dot3(P.x - O.x, P.y - O.y, P.z - O.z);
-    top2_merge(a1, a2, rd, 1.e-16);
+    top2_merge(a1, a2, (unsigned long long)__double_as_longlong(rd), tiny);
   }
   for (int off = 16; off > 0; off >>= 1) {
-    double b1 = __shfl_down_sync(0xffffffffu, a1, off);
-    double b2 = __shfl_down_sync(0xffffffffu, a2, off);
+    unsigned long long b1 = __shfl_down_sync(0xffffffffu, a1, off);
+    unsigned long long b2 = __shfl_down_sync(0xffffffffu, a2, off);
     top2_merge(a1, a2, b1, b2);
   }
-  __shared__ double w1[32], w2[32];
+  __shared__ unsigned long long w1[32], w2[32];
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) {
     w1[wid] = a1;
@@ -593,7 +601,7 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
   __syncthreads();
   __shared__ bool last;
   if (threadIdx.x == 0) {
-    double b1 = 1.e-16, b2 = 1.e-16;
+    unsigned long long b1 = tiny, b2 = tiny;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) top2_merge(b1, b2, w1[w], w2[w]);
     d.part[2 * blockIdx.x] = b1;
     d.part[2 * blockIdx.x + 1] = b2;
@@ -605,14 +613,14 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
   if (!last) return;
   __threadfence();
   // last block: parallel top-2 over the block partials
-  double b1 = 1.e-16, b2 = 1.e-16;
+  unsigned long long b1 = tiny, b2 = tiny;
   for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
-    double c1 = __ldcg(d.part + 2 * b), c2 = __ldcg(d.part + 2 * b + 1);
+    unsigned long long c1 = __ldcg(d.part + 2 * b), c2 = __ldcg(d.part + 2 * b + 1);
     top2_merge(b1, b2, c1, c2);
   }
   for (int off = 16; off > 0; off >>= 1) {
-    double c1 = __shfl_down_sync(0xffffffffu, b1, off);
-    double c2 = __shfl_down_sync(0xffffffffu, b2, off);
+    unsigned long long c1 = __shfl_down_sync(0xffffffffu, b1, off);
+    unsigned long long c2 = __shfl_down_sync(0xffffffffu, b2, off);
     top2_merge(b1, b2, c1, c2);
   }
   __syncthreads();
@@ -622,10 +630,11 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double e1 = 1.e-16, e2 = 1.e-16;
+    unsigned long long e1 = tiny, e2 = tiny;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) top2_merge(e1, e2, w1[w], w2[w]);
     Scalars* sc = d.sc;
-    int rebuild = (!sc->listed) || (sqrt(e1) + sqrt(e2) > p.skin);
+    double d1 = __longlong_as_double((long long)e1), d2 = __longlong_as_double((long long)e2);
+    int rebuild = (!sc->listed) || (sqrt(d1) + sqrt(d2) > p.skin);
     sc->rebuild = rebuild;
     if (rebuild) {
       sc->nupd += 1;
