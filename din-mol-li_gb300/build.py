@@ -6,6 +6,7 @@ library in din-mol-li_gb300/_build/:
                        plain form is bit-exact to the reference order)
   csrc/dml_api.cu      C ABI and host orchestration (-ffp-contract=off)
   csrc/dml_config.cpp  initial-configuration generators (host)
+  csrc/dml_noalloc.cu  dml_force_noalloc, scratch in a static device array
 """
 import os
 import subprocess
@@ -27,6 +28,8 @@ HEADERS = [os.path.join(ROOT, "include", "dml.h"), os.path.join(ROOT, "include",
 UNITS = [
     ("dml_kernels.cu", [NVCC, "-std=c++17", "-O3", "-lineinfo", "--fmad=false"] + ARCH +
      ["-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v"]),
+    ("dml_noalloc.cu", [NVCC, "-std=c++17", "-O3", "-lineinfo", "--fmad=false"] + ARCH +
+     ["-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]),
     ("dml_api.cu", [NVCC, "-std=c++17", "-O2"] + ARCH +
      ["-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]),
     ("dml_config.cpp", ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off"]),

@@ -221,6 +221,27 @@ int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phas
                       int32_t nphase);
 int dml_launches_per_step(dml_ctx* c, int32_t* per_rebuild);
 
+/* Pair force and energy (the fuerza of dml_force) over caller-provided
+ * device-accessible arrays, allocating nothing.  This entry point has no
+ * counterpart in the reference.  It serves callers that cannot allocate
+ * device memory: code running while a stream is captured into a CUDA graph
+ * (cudaMalloc is not allowed there), drivers whose device buffers belong to
+ * another runtime, loops that must not allocate.  Its scratch lives in one
+ * static device array sized for at most 16384 atoms and 32 interacting list
+ * entries per atom: more atoms return DML_E_CAPACITY before any launch, more
+ * entries DML_E_EVENT_OVERFLOW.  Inputs: pos [n][3], z [n] (DML_Z_*), the
+ * hs%ref members ref [n_ref] (atom indices in hs%ref order) and their lists
+ * nn [n_ref], list [n_ref][ld] (atom indices, -1 for limbo).  force [n][3]
+ * and epot [n] are outputs for hs%ref members (zeroed, then summed) and are
+ * added to for the other atoms, as fuerza does.  Results equal dml_force's
+ * bit for bit.  The first call on a device sets up the array's address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  Calls
+ * share the array: calls that overlap on the GPU race.  The call queues on
+ * `stream` (a cudaStream_t, NULL = default) and returns when it is done. */
+int dml_force_noalloc(const dml_params* p, int32_t n_atoms, const double* pos, const int32_t* z,
+                      int32_t n_ref, const int32_t* ref, const int32_t* nn, const int32_t* list,
+                      int32_t ld, double* force, double* epot, void* stream);
+
 /* Copies atom state to host arrays (sys%alist order).  a->n must be the
  * array capacity on entry; it is set to the atom count on return. */
 int dml_get_atoms(dml_ctx* c, dml_atoms* a);
