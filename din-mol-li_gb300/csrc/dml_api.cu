@@ -113,6 +113,7 @@ void make_kparams(const dml_params& P, KParams& K) {
       K.pair_on[i][j] = eps != 0.0;
       K.r0sqf[i][j] = (float)(r0 * r0);
       K.epsf[i][j] = (float)eps;
+      K.c12f[i][j] = r0 > 0.0 ? (float)(12.0 * eps / (r0 * r0)) : 0.0f;
     }
   for (int t = 0; t < 3; ++t) K.mass[t] = P.mass[t];
   // set_ermak (dana.F90:947-971)

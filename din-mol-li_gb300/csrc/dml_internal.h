@@ -89,7 +89,7 @@ struct KParams {
   int mixed;
   int cand_cap;
   float rcf;                // rc (FP32, pre-filters)
-  float r0sqf[3][3], epsf[3][3];
+  float r0sqf[3][3], epsf[3][3], c12f[3][3];  // c12 = 12 eps / r0^2
   double fix_scale, fix_inv; // 2^32 per eV/Å in ui/Å, and its inverse
   float rlist_lo2, rlist_hi2; // list shell bounds (FP32)
   float margin;             // FP32 position error bound

@@ -96,6 +96,24 @@ __device__ __forceinline__ int cell_index(double x, double cell) {
   return (int)q + 1;
 }
 
+// cgroup_sort_atom's range test (Cells.F90:289-294): 0 <= int(x/cell)+1 <=
+// ncells+1 in every dimension, NaN out of range.  The quotient is formed only
+// for coordinates within 1e-9 relative of a bound; elsewhere the bounds
+// -2*cell < x < (ncells+1)*cell decide the same question.
+__device__ __forceinline__ bool coord_in_tess(double x, double cell, int n) {
+  double lo = -2.0 * cell, hi = (double)(n + 1) * cell;
+  double tol = 1e-9 * (hi - lo);
+  if (x > lo + tol && x < hi - tol) return true;
+  if (!(x > lo - tol && x < hi + tol)) return false;  // far out, or NaN
+  int c = cell_index(x, cell);
+  return c >= 0 && c <= n + 1;
+}
+
+__device__ __forceinline__ bool in_tessellation(const KParams& p, double4 P) {
+  return coord_in_tess(P.x, p.cell[0], p.ncells[0]) && coord_in_tess(P.y, p.cell[1], p.ncells[1]) &&
+         coord_in_tess(P.z, p.cell[2], p.ncells[2]);
+}
+
 __device__ __forceinline__ int warp_id_global() {
   return (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 }
@@ -441,10 +459,10 @@ __global__ void ermak_b_kernel(Dev d, KParams p, int n_rank) {
 
 
 // ------------------------------------------------------- mixed-precision force
-// The chosen form of fuerza: the pair difference and its square are taken in
-// FP64 (positions reach 350 Å, where an FP32 coordinate has a 3e-5 Å ulp),
-// the pair force and energy in FP32, and both are accumulated as int64 fixed
-// point (2^32 per eV/Å and per eV).  Integer addition is associative, so the sums do not
+// The chosen form of fuerza: the pair difference and the core (r0/r)^2,
+// (r0/r)^6 are taken in FP64 (positions reach 350 Å, where an FP32
+// coordinate has a 3e-5 Å ulp), the pair force and energy in FP32, and both
+// are accumulated as int64 fixed point (2^32 per eV/Å and per eV).  Integer addition is associative, so the sums do not
 // depend on the order of the atomics: deterministic without ordering.
 __device__ __forceinline__ long long to_fixed(const KParams& p, float v, double scale) {
   double x = (double)v * scale;
@@ -466,18 +484,19 @@ __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
     double dx = Pi.x - Pj.x, dy = Pi.y - Pj.y, dz = Pi.z - Pj.z;
     if (dx > p.halfbox[0]) dx -= p.box[0]; else if (dx < -p.halfbox[0]) dx += p.box[0];
     if (dy > p.halfbox[1]) dy -= p.box[1]; else if (dy < -p.halfbox[1]) dy += p.box[1];
-    // r^2 from the FP64 difference, rounded once to FP32: the force goes as
-    // r^-14 in the core, so an FP32 sum of squares (3 roundings) would be
-    // amplified about sevenfold.  The pair math below is FP32.
-    float r2 = (float)dot3(dx, dy, dz);
+    // The distance-dependent core, q = (r0/r)^2 and b = q^3, is formed in
+    // FP64 and rounded once to FP32: the force goes as r^-14 in the core, so
+    // FP32 roundings of r^2, 1/r^2 and q^3 would be amplified about sixfold.
+    // The force polynomial, the vector and the energy are FP32.
+    double r2d = dot3(dx, dy, dz);
+    if (r2d > p.r0sq[k - 1][m - 1]) continue;
+    double qd = p.r0sq[k - 1][m - 1] / r2d;
+    float b = (float)(qd * qd * qd);                      // (r0/r)^6
+    float qf = (float)qd;
     float vx = (float)dx, vy = (float)dy, vz = (float)dz;
-    if (r2 > p.r0sqf[k - 1][m - 1]) continue;
-    float inv_r2 = 1.0f / r2;
-    float qq = p.r0sqf[k - 1][m - 1] * inv_r2;
-    float b = qq * qq * qq;                               // (r0/r)^6
     float eps = p.epsf[k - 1][m - 1];
-    float fr = 12.0f * eps * b * (b - 1.0f) * inv_r2;      // |F|/r
-    float e = 0.5f * (eps * b * (b - 2.0f) + eps);         // half the pair energy
+    float fr = p.c12f[k - 1][m - 1] * (b * (b - 1.0f)) * qf;  // |F|/r = 12 eps b (b-1) / r^2
+    float e = 0.5f * (eps * b * (b - 2.0f) + eps);          // half the pair energy
     long long fx = to_fixed(p, fr * vx, p.fix_scale);
     long long fy = to_fixed(p, fr * vy, p.fix_scale);
     long long fz = to_fixed(p, fr * vz, p.fix_scale);
@@ -584,8 +603,12 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
       d.pos_old[s] = O;
       d.posf[s] = to_f4(P, d.typ[s]);
     }
+    // cgroup_sort runs at every test_update (Neighbor.F90:687-691) and stops
+    // on an atom outside the tessellation (Cells.F90:293-294), rebuild or not.
+    if (p.use_cells && !in_tessellation(p, P)) raise_error(d.sc, DML_E_OUT_OF_TESSELLATION, s);
     double rd = dot3(P.x - O.x, P.y - O.y, P.z - O.z);
-    top2_merge(a1, a2, (unsigned long long)__double_as_longlong(rd), tiny);
+    // a NaN displacement never passes `rd > dispmax` (Neighbor.F90:657-661)
+    if (rd == rd) top2_merge(a1, a2, (unsigned long long)__double_as_longlong(rd), tiny);
   }
   for (int off = 16; off > 0; off >>= 1) {
     unsigned long long b1 = __shfl_down_sync(0xffffffffu, a1, off);
