@@ -28,14 +28,15 @@ struct dml_ctx {
   cudaStream_t aux = nullptr;  // captures conditional bodies
   int device = 0;
   bool loaded = false, setup_done = false;
-  int n_slots = 0, n_b = 0, n_rank = 0, n_atoms = 0;
-  std::vector<int> alist;  // hs slots in sys%alist order
+  std::vector<dml_replica> reps;  // per-replica geometry and seeds
+  std::vector<RepConst> rc;       // per-replica device constants (host copy)
   cudaGraphExec_t step_graph = nullptr;
   int launches_per_step = 0;    // kernels of a step without a list rebuild
   int launches_per_rebuild = 0; // extra kernels when the list is rebuilt
   void* flush_buf = nullptr;
   std::string last_error;
-  Scalars* h_sc = nullptr;  // pinned mirror
+  Scalars* h_sc = nullptr;  // pinned mirror of the per-replica state
+  Global* h_g = nullptr;    // pinned mirror of the context-wide state
   std::vector<void*> allocs;
 };
 
@@ -69,33 +70,37 @@ double pow6h(double x) {
   return x2 * x4;
 }
 
-// Host-side constants (see KParams).
-void make_kparams(const dml_params& P, KParams& K) {
-  std::memset(&K, 0, sizeof K);
-  double maxc = 0;
+// Per-replica constants: box, cells (cgroup_tessellate, Cells.F90:227-242:
+// ncells = int(box/(rc+skin)), cells off when all three are below 4).
+void make_repconst(const dml_params& P, const dml_replica& r, RepConst& R) {
+  std::memset(&R, 0, sizeof R);
   for (int k = 0; k < 3; ++k) {
-    K.box[k] = P.box[k];
-    K.one_box[k] = 1.0 / P.box[k];
-    K.halfbox[k] = P.box[k] * .5;
-    K.boxf[k] = (float)P.box[k];
-    K.halfboxf[k] = (float)(P.box[k] * .5);
-    K.one_boxf[k] = (float)(1.0 / P.box[k]);
-    maxc = std::max(maxc, P.box[k]);
+    R.box[k] = r.box[k];
+    R.one_box[k] = 1.0 / r.box[k];
+    R.halfbox[k] = r.box[k] * .5;
+    R.boxf[k] = (float)r.box[k];
+    R.halfboxf[k] = (float)(r.box[k] * .5);
   }
-  maxc = 2.0 * std::max(maxc, P.zmax) + 100.0;
+  double rcut_b = P.rc + P.skin;
+  for (int k = 0; k < 3; ++k) R.ncells[k] = (int)(r.box[k] / rcut_b);
+  R.use_cells = !(R.ncells[0] < 4 && R.ncells[1] < 4 && R.ncells[2] < 4);
+  for (int k = 0; k < 3; ++k) {
+    if (R.ncells[k] < 1) R.ncells[k] = 1;
+    R.cell[k] = r.box[k] / (double)R.ncells[k];
+    R.head_dim[k] = R.ncells[k] + 2;
+  }
+  R.ncell = R.use_cells ? R.head_dim[0] * R.head_dim[1] * R.head_dim[2] : 0;
+  R.seed = r.seed;
+}
+
+// Context-wide constants (see KParams); maxc bounds every coordinate.
+void make_kparams(const dml_params& P, double maxc, KParams& K) {
+  std::memset(&K, 0, sizeof K);
+  maxc = 2.0 * maxc + 100.0;
   // FP32 coordinates carry at most 2^-24 relative rounding; a difference of
   // two of them and its square stay well inside 64 ulps of maxc.
   double margin = std::max(1e-3, 64.0 * std::ldexp(maxc, -24));
   K.margin = (float)margin;
-  // cgroup_tessellate (Cells.F90:227-242): ncells = int(box/(rc+skin)).
-  double rcut_b = P.rc + P.skin;
-  for (int k = 0; k < 3; ++k) K.ncells[k] = (int)(P.box[k] / rcut_b);
-  K.use_cells = !(K.ncells[0] < 4 && K.ncells[1] < 4 && K.ncells[2] < 4);
-  for (int k = 0; k < 3; ++k) {
-    if (K.ncells[k] < 1) K.ncells[k] = 1;
-    K.cell[k] = P.box[k] / (double)K.ncells[k];
-    K.head_dim[k] = K.ncells[k] + 2;
-  }
   K.rc2 = P.rc * P.rc;
   double rl = P.rc + P.skin;
   K.rlist2 = rl * rl;
@@ -150,7 +155,6 @@ void make_kparams(const dml_params& P, KParams& K) {
   K.mnb = P.mnb;
   K.ev_cap = P.event_cap;
   K.max_passes = P.max_passes;
-  K.seed = P.seed;
   K.mixed = P.precision == DML_PRECISION_MIXED;
   K.rcf = (float)P.rc;
   // 2^32 per eV/Å; 1 eV = 96.485 * 100 ui (dana.F90:23)
@@ -162,7 +166,18 @@ void make_kparams(const dml_params& P, KParams& K) {
 }
 
 int read_scalars(dml_ctx* c) {
-  CK(cudaMemcpyAsync(c->h_sc, c->D.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+  if (c->loaded) {
+    CK(cudaMemcpyAsync(c->h_g, c->D.g, sizeof(Global), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(c->h_sc, c->D.sc, sizeof(Scalars) * c->D.nrep, cudaMemcpyDeviceToHost,
+                       c->stream));
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int write_scalars(dml_ctx* c) {
+  CK(cudaMemcpyAsync(c->D.sc, c->h_sc, sizeof(Scalars) * c->D.nrep, cudaMemcpyHostToDevice,
+                     c->stream));
   CK(cudaStreamSynchronize(c->stream));
   return 0;
 }
@@ -172,19 +187,19 @@ int finish(dml_ctx* c) {
   if (e != cudaSuccess) return cuda_fail(c, e, "kernel launch");
   int rc = read_scalars(c);
   if (rc) return rc;
-  if (c->h_sc->error) {
+  if (c->h_g->error) {
     char buf[128];
-    std::snprintf(buf, sizeof buf, "device error %d (%s), info %d", c->h_sc->error,
-                  dml_strerror(c->h_sc->error), c->h_sc->err_info);
+    std::snprintf(buf, sizeof buf, "device error %d (%s), info %d", c->h_g->error,
+                  dml_strerror(c->h_g->error), c->h_g->err_info);
     c->last_error = buf;
-    return c->h_sc->error;
+    return c->h_g->error;
   }
   return 0;
 }
 
 int set_step(dml_ctx* c, int64_t step) {
   long long v = step;
-  CK(cudaMemcpyAsync(&c->D.sc->step, &v, sizeof v, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemcpyAsync(&c->D.g->step, &v, sizeof v, cudaMemcpyHostToDevice, c->stream));
   return 0;
 }
 
@@ -368,37 +383,65 @@ const char* dml_strerror(int code) {
 
 const char* dml_last_error(dml_ctx* c) { return c ? c->last_error.c_str() : "no context"; }
 
-int dml_create(const dml_params* p, dml_ctx** out) {
-  if (!p || !out) return DML_E_ARG;
+int dml_create_batch(const dml_params* p, int32_t n_rep, const dml_replica* reps,
+                     dml_ctx** out) {
+  if (!p || !out || n_rep <= 0 || !reps) return DML_E_ARG;
   *out = nullptr;
   if (p->reservoir < 0 || p->reservoir > 3) return DML_E_RESERVOIR;
   if (p->reservoir == DML_RESERVOIR_CHUNKS) return DML_E_UNSUPPORTED;
   if (p->reservoir == DML_RESERVOIR_GCMC && (p->nadj < 0 || !(p->act > 0))) return DML_E_ARG;
   if (p->precision != DML_PRECISION_FP64 && p->precision != DML_PRECISION_MIXED) return DML_E_ARG;
-  if (!(p->box[0] > 0 && p->box[1] > 0 && p->box[2] > 0 && p->h > 0 && p->rc > 0)) return DML_E_ARG;
+  if (!(p->h > 0 && p->rc > 0)) return DML_E_ARG;
   // The FP32 pre-filters assume the minimum image is unambiguous at every cut-off.
   double rmax = p->rc + p->skin;
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) rmax = std::max(rmax, p->r0[i][j]);
-  if (p->box[0] * 0.5 <= rmax + 0.01 || p->box[1] * 0.5 <= rmax + 0.01) return DML_E_ARG;
+  double maxc = 0.0;
+  for (int r = 0; r < n_rep; ++r) {
+    const dml_replica& q = reps[r];
+    if (!(q.box[0] > 0 && q.box[1] > 0 && q.box[2] > 0)) return DML_E_ARG;
+    if (q.box[0] * 0.5 <= rmax + 0.01 || q.box[1] * 0.5 <= rmax + 0.01) return DML_E_ARG;
+    maxc = std::max({maxc, q.box[0], q.box[1], q.box[2], q.zmax});
+  }
   dml_ctx* c = new dml_ctx();
   c->P = *p;
   if (c->P.mnb <= 0) c->P.mnb = 1024;
   if (c->P.max_passes <= 0) c->P.max_passes = 64;
   if (c->P.event_cap <= 0) c->P.event_cap = 64;
   if (c->P.event_cap > 128) c->P.event_cap = 128;
-  make_kparams(c->P, c->K);
+  c->reps.assign(reps, reps + n_rep);
+  make_kparams(c->P, maxc, c->K);
+  c->rc.resize(n_rep);
+  for (int r = 0; r < n_rep; ++r) make_repconst(c->P, reps[r], c->rc[r]);
   cudaError_t e = cudaGetDevice(&c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_sc, sizeof(Scalars));
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_sc, sizeof(Scalars) * n_rep);
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&c->h_g, sizeof(Global));
   if (e != cudaSuccess) {
-    delete c;
+    dml_destroy(c);
     return DML_E_CUDA;
   }
+  std::memset(c->h_g, 0, sizeof(Global));
+  std::memset(c->h_sc, 0, sizeof(Scalars) * n_rep);
+  c->D.nrep = n_rep;
   *out = c;
   return 0;
 }
+
+int dml_create(const dml_params* p, dml_ctx** out) {
+  if (!p) return DML_E_ARG;
+  dml_replica r;
+  std::memset(&r, 0, sizeof r);
+  for (int k = 0; k < 3; ++k) r.box[k] = p->box[k];
+  r.z0 = p->z0;
+  r.zmax = p->zmax;
+  r.z1 = p->z1;
+  r.seed = p->seed;
+  return dml_create_batch(p, 1, &r, out);
+}
+
+int dml_num_replicas(dml_ctx* c) { return c ? c->D.nrep : -DML_E_ARG; }
 
 void dml_destroy(dml_ctx* c) {
   if (!c) return;
@@ -407,21 +450,41 @@ void dml_destroy(dml_ctx* c) {
   for (void* p : c->allocs) cudaFree(p);
   if (c->flush_buf) cudaFree(c->flush_buf);
   if (c->h_sc) cudaFreeHost(c->h_sc);
+  if (c->h_g) cudaFreeHost(c->h_g);
   if (c->stream) cudaStreamDestroy(c->stream);
   if (c->aux) cudaStreamDestroy(c->aux);
   delete c;
 }
 
-int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
-  if (!c || !a || a->n <= 0 || !a->pos || !a->z) return DML_E_ARG;
+int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
+  if (!c || !atoms) return DML_E_ARG;
   if (c->loaded) return DML_E_STATE;
-  const int n = a->n;
-  const int cap = std::max(n, c->P.capacity > 0 ? c->P.capacity
-                                                 : (c->P.reservoir == DML_RESERVOIR_GCMC ? 2 * n + 1024 : n));
-  c->P.capacity = cap;
+  const int nrep = c->D.nrep;
   Dev& d = c->D;
-  d.cap = cap;
-  const KParams& K = c->K;
+  // capacities: positions per replica, a multiple of the block size
+  int total = 0, ncell = 0, any_cells = 0, any_verlet = 0;
+  for (int r = 0; r < nrep; ++r) {
+    const dml_atoms* a = atoms + r;
+    if (a->n <= 0 || !a->pos || !a->z) return DML_E_ARG;
+    int want = c->P.capacity > 0 ? c->P.capacity
+                                 : (c->P.reservoir == DML_RESERVOIR_GCMC ? 2 * a->n + 1024 : a->n);
+    int cap = std::max(a->n, want);
+    cap = (cap + kBlock - 1) / kBlock * kBlock;
+    RepConst& R = c->rc[r];
+    R.base = total;
+    R.cap = cap;
+    R.nblk = cap / kBlock;
+    R.cell_off = ncell;
+    ncell += R.ncell;
+    total += cap;
+    if (R.use_cells) any_cells = 1; else any_verlet = 1;
+  }
+  d.cap = total;
+  d.ncell_tot = ncell;
+  d.any_cells = any_cells;
+  d.any_verlet = any_verlet;
+  const int cap = total;
+  c->K.cand_cap = 16 * cap;
   int rc = 0;
 #define AL(ptr, cnt) \
   if ((rc = dalloc(c, &(ptr), (cnt))) != 0) return rc;
@@ -445,21 +508,19 @@ int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
   AL(d.b2hs, cap);
   AL(d.nn, cap);
   AL(d.list, (size_t)cap * c->P.mnb);
-  d.ncell_tot = K.use_cells ? K.head_dim[0] * K.head_dim[1] * K.head_dim[2] : 1;
   AL(d.cell_of, cap);
-  AL(d.cell_count, d.ncell_tot + 1);
-  AL(d.cell_start, d.ncell_tot + 1);
-  AL(d.cell_fill, d.ncell_tot + 1);
+  AL(d.cell_count, ncell + 1);
+  AL(d.cell_start, ncell + 1);
+  AL(d.cell_fill, ncell + 1);
   AL(d.cell_atoms, cap);
   AL(d.alist, cap);
   AL(d.apos, cap);
   AL(d.gorder, cap);
   AL(d.gpos, cap);
   AL(d.in_gcmc, cap);
-  AL(d.ins_head, d.ncell_tot + 1);
+  AL(d.ins_head, ncell + 1);
   AL(d.ins_next, cap);
   AL(d.facc, 4 * (size_t)cap);
-  c->K.cand_cap = 16 * cap;
   AL(d.cand, (size_t)c->K.cand_cap);
   AL(d.ev_count, cap);
   AL(d.ev, (size_t)cap * c->P.event_cap);
@@ -472,107 +533,124 @@ int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
   AL(d.comp_fill, cap);
   AL(d.comp_members, cap);
   AL(d.comp_list, 2 * (size_t)cap);
-  d.nblk_part = (cap + kBlock - 1) / kBlock + 1;
+  d.nblk_part = cap / kBlock + 1;
   AL(d.part, 2 * (size_t)d.nblk_part);
-  AL(d.sc, 1);
+  AL(d.sc, nrep);
+  AL(d.g, 1);
+  AL(d.rc, nrep);
+  AL(d.rep_of, cap);
 #undef AL
 
-  // Host staging in slot order (slot = position in the array).
-  std::vector<double4> pos(n), vel(n), acel(n), force(n), pos_old(n), old_cg(n);
-  std::vector<float4> posf(n);
-  std::vector<double> epot(n);
-  std::vector<int8_t> typ(n), skip(n), state(n, ST_LIVE);
-  std::vector<long long> id(n);
-  std::vector<int> rank(n, -1), ref, slot(n), gorder, gpos(n, -1);
-  std::vector<int8_t> in_gcmc(n, 0);
-  int64_t max_id = -1;
-  for (int i = 0; i < n; ++i) {
-    auto v3 = [&](const double* src, double def) {
-      if (!src) return make_double4(def, def, def, 0.0);
-      return make_double4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.0);
-    };
-    int z = a->z[i];
-    if (z < 1 || z > 3) return DML_E_ARG;
-    pos[i] = v3(a->pos, 0.0);
-    vel[i] = v3(a->vel, 0.0);
-    acel[i] = v3(a->acel, 0.0);
-    force[i] = v3(a->force, 0.0);
-    pos_old[i] = a->pos_old ? v3(a->pos_old, 0.0) : pos[i];
-    old_cg[i] = v3(a->old_cg, 1e8);
-    epot[i] = a->epot ? a->epot[i] : 0.0;
-    typ[i] = (int8_t)z;
-    skip[i] = a->skip ? (a->skip[i] != 0) : 0;
-    id[i] = a->id ? a->id[i] : i;
-    max_id = std::max<int64_t>(max_id, id[i]);
-    float zbits;
-    std::memcpy(&zbits, &z, sizeof zbits);  // element as integer bits in w
-    posf[i] = make_float4((float)pos[i].x, (float)pos[i].y, (float)pos[i].z, zbits);
-    bool in_ref = a->in_ref ? a->in_ref[i] != 0 : (z != DML_Z_CG);
-    if (in_ref) {
-      rank[i] = (int)ref.size();
-      ref.push_back(i);
+  // Host staging, position order (replica r at [base, base + cap)).
+  std::vector<double4> pos(cap), vel(cap), acel(cap), force(cap), pos_old(cap), old_cg(cap);
+  std::vector<float4> posf(cap, make_float4(0.f, 0.f, 0.f, 0.f));
+  std::vector<double> epot(cap, 0.0);
+  std::vector<int8_t> typ(cap, 0), skip(cap, 0), state(cap, ST_NULL), in_gcmc(cap, 0);
+  std::vector<long long> id(cap, 0);
+  std::vector<int> rank(cap, -1), ref(cap, -1), slot(cap, -1), alist(cap, -1), apos(cap, -1),
+      gorder(cap, -1), gpos(cap, -1), rep_of(cap, 0);
+  std::memset(c->h_sc, 0, sizeof(Scalars) * nrep);
+  for (int r = 0; r < nrep; ++r) {
+    const dml_atoms* a = atoms + r;
+    const RepConst& R = c->rc[r];
+    const int n = a->n, B = R.base;
+    for (int q = 0; q < R.cap; ++q) rep_of[B + q] = r;
+    int nref = 0, ng = 0;
+    int64_t max_id = -1;
+    for (int i = 0; i < n; ++i) {
+      auto v3 = [&](const double* src, double def) {
+        if (!src) return make_double4(def, def, def, 0.0);
+        return make_double4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.0);
+      };
+      int z = a->z[i];
+      if (z < 1 || z > 3) return DML_E_ARG;
+      const int h = B + i;  // hs slot = hs%b slot = sys%alist position
+      pos[h] = v3(a->pos, 0.0);
+      vel[h] = v3(a->vel, 0.0);
+      acel[h] = v3(a->acel, 0.0);
+      force[h] = v3(a->force, 0.0);
+      pos_old[h] = a->pos_old ? v3(a->pos_old, 0.0) : pos[h];
+      old_cg[h] = v3(a->old_cg, 1e8);
+      epot[h] = a->epot ? a->epot[i] : 0.0;
+      typ[h] = (int8_t)z;
+      skip[h] = a->skip ? (a->skip[i] != 0) : 0;
+      state[h] = ST_LIVE;
+      id[h] = a->id ? a->id[i] : i;
+      max_id = std::max<int64_t>(max_id, id[h]);
+      float zbits;
+      std::memcpy(&zbits, &z, sizeof zbits);  // element as integer bits in w
+      posf[h] = make_float4((float)pos[h].x, (float)pos[h].y, (float)pos[h].z, zbits);
+      bool in_ref = a->in_ref ? a->in_ref[i] != 0 : (z != DML_Z_CG);
+      if (in_ref) {
+        rank[h] = B + nref;
+        ref[B + nref] = h;
+        ++nref;
+      }
+      slot[h] = h;
+      alist[h] = h;
+      apos[h] = h;
+      // gcmc attach loop (dana.F90:130-137): z == 1 atoms in sys order
+      bool gm = c->P.reservoir == DML_RESERVOIR_GCMC &&
+                (a->in_gcmc ? a->in_gcmc[i] != 0 : z == DML_Z_LI);
+      if (gm) {
+        gpos[h] = B + ng;
+        gorder[B + ng] = h;
+        in_gcmc[h] = 1;
+        ++ng;
+      }
     }
-    slot[i] = i;
-    // gcmc attach loop (dana.F90:130-137): z == 1 atoms in sys order
-    bool g = c->P.reservoir == DML_RESERVOIR_GCMC &&
-             (a->in_gcmc ? a->in_gcmc[i] != 0 : z == DML_Z_LI);
-    if (g) {
-      gpos[i] = (int)gorder.size();
-      gorder.push_back(i);
-      in_gcmc[i] = 1;
-    }
+    Scalars& S = c->h_sc[r];
+    S.zmax = c->reps[r].zmax;
+    S.z0 = c->reps[r].z0;
+    S.z1 = c->reps[r].z1;
+    S.n_slots = n;
+    S.n_b = n;
+    S.n_rank = nref;
+    S.n_ref = nref;
+    S.n_atoms = n;
+    S.n_alist = n;
+    S.n_gorder = ng;
+    S.n_gcmc = ng;
+    S.b_nat = n;
+    S.nlimbo = 0;
+    S.next_id = max_id + 1;
   }
-  cudaStream_t s = c->stream;
-  CK(cudaMemcpyAsync(d.pos, pos.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.vel, vel.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.acel, acel.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.force, force.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.pos_old, pos_old.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.old_cg, old_cg.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.posf, posf.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.epot, epot.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.typ, typ.data(), n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.skip, skip.data(), n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.state, state.data(), n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.id, id.data(), sizeof(long long) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.rank, rank.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.bslot, slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.b2hs, slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.alist, slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.apos, slot.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.gpos, gpos.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(d.in_gcmc, in_gcmc.data(), n, cudaMemcpyHostToDevice, s));
-  if (!gorder.empty())
-    CK(cudaMemcpyAsync(d.gorder, gorder.data(), sizeof(int) * gorder.size(), cudaMemcpyHostToDevice, s));
-  if (!ref.empty())
-    CK(cudaMemcpyAsync(d.ref, ref.data(), sizeof(int) * ref.size(), cudaMemcpyHostToDevice, s));
-  Scalars sc;
-  std::memset(&sc, 0, sizeof sc);
-  sc.zmax = c->P.zmax;
-  sc.z0 = c->P.z0;
-  sc.z1 = c->P.z1;
-  sc.n_slots = n;
-  sc.n_b = n;
-  sc.n_rank = (int)ref.size();
-  sc.n_ref = (int)ref.size();
-  sc.n_atoms = n;
-  sc.n_alist = n;
-  sc.n_gorder = (int)gorder.size();
-  sc.n_gcmc = (int)gorder.size();
-  sc.b_nat = n;
-  sc.nlimbo = 0;
-  sc.next_id = max_id + 1;
-  *c->h_sc = sc;
-  CK(cudaMemcpyAsync(d.sc, c->h_sc, sizeof sc, cudaMemcpyHostToDevice, s));
-  CK(cudaStreamSynchronize(s));
-  c->n_slots = n;
-  c->n_b = n;
-  c->n_rank = (int)ref.size();
-  c->n_atoms = n;
-  c->alist.resize(n);
-  for (int i = 0; i < n; ++i) c->alist[i] = i;
+  cudaStream_t st = c->stream;
+  CK(cudaMemcpyAsync(d.pos, pos.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.vel, vel.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.acel, acel.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.force, force.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.pos_old, pos_old.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.old_cg, old_cg.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.posf, posf.data(), sizeof(float4) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.epot, epot.data(), sizeof(double) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.typ, typ.data(), cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.skip, skip.data(), cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.state, state.data(), cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.in_gcmc, in_gcmc.data(), cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.id, id.data(), sizeof(long long) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.rank, rank.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.ref, ref.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.bslot, slot.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.b2hs, slot.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.alist, alist.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.apos, apos.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.gorder, gorder.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.gpos, gpos.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.rep_of, rep_of.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.rc, c->rc.data(), sizeof(RepConst) * nrep, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.sc, c->h_sc, sizeof(Scalars) * nrep, cudaMemcpyHostToDevice, st));
+  std::memset(c->h_g, 0, sizeof(Global));
+  CK(cudaMemcpyAsync(d.g, c->h_g, sizeof(Global), cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));
   c->loaded = true;
   return 0;
+}
+
+int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
+  if (!c || !a) return DML_E_ARG;
+  if (c->D.nrep != 1) return DML_E_ARG;
+  return dml_set_atoms_batch(c, a);
 }
 
 int dml_test_update(dml_ctx* c, int32_t* rebuilt) {
@@ -580,7 +658,10 @@ int dml_test_update(dml_ctx* c, int32_t* rebuilt) {
   k_test_update(c->D, c->K, c->D.cap, c->D.cap, c->D.cap, c->stream);
   int rc = finish(c);
   if (rc) return rc;
-  if (rebuilt) *rebuilt = c->h_sc->rebuild;
+  if (rebuilt) {
+    *rebuilt = 0;
+    for (int r = 0; r < c->D.nrep; ++r) *rebuilt |= c->h_sc[r].rebuild;
+  }
   return 0;
 }
 
@@ -624,11 +705,16 @@ int dml_overlap_moveback(dml_ctx* c, int64_t step) {
 int dml_capture_commit(dml_ctx* c, int32_t* n_new) {
   if (!c || !c->loaded) return DML_E_STATE;
   int zero = 0;
-  CK(cudaMemcpyAsync(&c->D.sc->n_new_cg, &zero, sizeof zero, cudaMemcpyHostToDevice, c->stream));
+  for (int r = 0; r < c->D.nrep; ++r)
+    CK(cudaMemcpyAsync(&c->D.sc[r].n_new_cg, &zero, sizeof zero, cudaMemcpyHostToDevice,
+                       c->stream));
   k_capture_commit(c->D, c->K, c->D.cap, c->stream);
   int rc = finish(c);
   if (rc) return rc;
-  if (n_new) *n_new = c->h_sc->n_new_cg;
+  if (n_new) {
+    *n_new = 0;
+    for (int r = 0; r < c->D.nrep; ++r) *n_new += c->h_sc[r].n_new_cg;
+  }
   return 0;
 }
 
@@ -646,7 +732,7 @@ int dml_calc_rho(dml_ctx* c, double* rho) {
   k_calc_rho(c->D, c->K, c->D.cap, c->stream);
   int rc = finish(c);
   if (rc) return rc;
-  if (rho) *rho = c->h_sc->rho;
+  if (rho) *rho = c->h_sc[0].rho;  // replica 0; every replica's rho in dml_get_counters_replica
   return 0;
 }
 
@@ -664,11 +750,11 @@ int dml_setup(dml_ctx* c) {
     rc = dml_force(c);
     if (rc) return rc;
   }
-  double rho = 0;
-  rc = dml_calc_rho(c, &rho);
+  rc = dml_calc_rho(c, nullptr);
   if (rc) return rc;
-  CK(cudaMemcpyAsync(&c->D.sc->rho0, &rho, sizeof rho, cudaMemcpyHostToDevice, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
+  for (int r = 0; r < c->D.nrep; ++r) c->h_sc[r].rho0 = c->h_sc[r].rho;  // rho0 (dana.F90:146)
+  rc = write_scalars(c);
+  if (rc) return rc;
   c->setup_done = true;
   return 0;
 }
@@ -754,19 +840,19 @@ int dml_launches_per_step(dml_ctx* c, int32_t* per_rebuild) {
   return c->launches_per_step;
 }
 
-int dml_get_counters(dml_ctx* c, dml_counters* o) {
-  if (!c || !o) return DML_E_ARG;
+int dml_get_counters_replica(dml_ctx* c, int32_t rep, dml_counters* o) {
+  if (!c || !o || rep < 0 || rep >= c->D.nrep) return DML_E_ARG;
   std::memset(o, 0, sizeof *o);
   if (!c->loaded) return 0;
   int rc = read_scalars(c);
   if (rc) return rc;
-  const Scalars& s = *c->h_sc;
+  const Scalars& s = c->h_sc[rep];
   o->try_ = (int64_t)s.try_;
   o->depo = (int64_t)s.depo;
   o->choques = (int64_t)s.choques;
   o->choques3 = (int64_t)s.choques3;
   o->nupd = (int64_t)s.nupd;
-  o->step = s.step;
+  o->step = c->h_g->step;
   o->gcmc_ins = (int64_t)s.gcmc_ins;
   o->gcmc_del = (int64_t)s.gcmc_del;
   o->n_atoms = s.n_atoms;
@@ -780,44 +866,72 @@ int dml_get_counters(dml_ctx* c, dml_counters* o) {
   return 0;
 }
 
-int dml_reset_counters(dml_ctx* c) {
-  if (!c || !c->loaded) return DML_E_STATE;
-  unsigned long long z[2] = {0, 0};
-  CK(cudaMemcpyAsync(&c->D.sc->try_, &z[0], sizeof(unsigned long long), cudaMemcpyHostToDevice,
-                     c->stream));
-  CK(cudaMemcpyAsync(&c->D.sc->depo, &z[1], sizeof(unsigned long long), cudaMemcpyHostToDevice,
-                     c->stream));
-  CK(cudaStreamSynchronize(c->stream));
+// Sums over replicas for the event counters and atom counts; the geometry
+// (zmax, z0, rho, rho0) is replica 0's, max_nn and passes the maxima.
+int dml_get_counters(dml_ctx* c, dml_counters* o) {
+  if (!c || !o) return DML_E_ARG;
+  int rc = dml_get_counters_replica(c, 0, o);
+  if (rc || !c->loaded) return rc;
+  for (int r = 1; r < c->D.nrep; ++r) {
+    const Scalars& s = c->h_sc[r];
+    o->try_ += (int64_t)s.try_;
+    o->depo += (int64_t)s.depo;
+    o->choques += (int64_t)s.choques;
+    o->choques3 += (int64_t)s.choques3;
+    o->nupd += (int64_t)s.nupd;
+    o->gcmc_ins += (int64_t)s.gcmc_ins;
+    o->gcmc_del += (int64_t)s.gcmc_del;
+    o->n_atoms += s.n_atoms;
+    o->n_ref += s.n_ref;
+    o->max_nn = std::max(o->max_nn, s.max_nn);
+    o->passes = std::max(o->passes, s.passes);
+  }
   return 0;
 }
 
-int dml_get_atoms(dml_ctx* c, dml_atoms* a) {
-  if (!c || !a) return DML_E_ARG;
+// salida resets try and depo after each output (dana.F90:252-258).
+int dml_reset_counters(dml_ctx* c) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  int rc = read_scalars(c);
+  if (rc) return rc;
+  for (int r = 0; r < c->D.nrep; ++r) c->h_sc[r].try_ = c->h_sc[r].depo = 0;
+  return write_scalars(c);
+}
+
+// Replica `rep`'s atoms in sys%alist order (its slots are [base, base + cap)).
+int dml_get_atoms_replica(dml_ctx* c, int32_t rep, dml_atoms* a) {
+  if (!c || !a || rep < 0 || rep >= c->D.nrep) return DML_E_ARG;
   if (!c->loaded) return DML_E_STATE;
   int rc = read_scalars(c);
   if (rc) return rc;
-  const int ns = c->h_sc->n_slots, nal = c->h_sc->n_alist;
+  const int B = c->rc[rep].base;
+  const int ns = c->h_sc[rep].n_slots, nal = c->h_sc[rep].n_alist;
   const Dev& d = c->D;
   cudaStream_t s = c->stream;
   std::vector<int> alist(nal);
-  if (nal) CK(cudaMemcpyAsync(alist.data(), d.alist, sizeof(int) * nal, cudaMemcpyDeviceToHost, s));
+  if (nal)
+    CK(cudaMemcpyAsync(alist.data(), d.alist + B, sizeof(int) * nal, cudaMemcpyDeviceToHost, s));
   std::vector<double4> pos(ns), vel(ns), acel(ns), force(ns), pos_old(ns), old_cg(ns);
   std::vector<double> epot(ns);
   std::vector<int8_t> typ(ns), skip(ns), ing(ns);
   std::vector<long long> id(ns);
   std::vector<int> rank(ns);
-  CK(cudaMemcpyAsync(pos.data(), d.pos, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
-  if (a->vel) CK(cudaMemcpyAsync(vel.data(), d.vel, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
-  if (a->acel) CK(cudaMemcpyAsync(acel.data(), d.acel, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
-  if (a->force) CK(cudaMemcpyAsync(force.data(), d.force, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
-  if (a->pos_old) CK(cudaMemcpyAsync(pos_old.data(), d.pos_old, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
-  if (a->old_cg) CK(cudaMemcpyAsync(old_cg.data(), d.old_cg, sizeof(double4) * ns, cudaMemcpyDeviceToHost, s));
-  if (a->epot) CK(cudaMemcpyAsync(epot.data(), d.epot, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(typ.data(), d.typ, ns, cudaMemcpyDeviceToHost, s));
-  if (a->skip) CK(cudaMemcpyAsync(skip.data(), d.skip, ns, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(ing.data(), d.in_gcmc, ns, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(id.data(), d.id, sizeof(long long) * ns, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(rank.data(), d.rank, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
+  auto get = [&](void* dst, const void* src, size_t elem) -> cudaError_t {
+    if (!ns) return cudaSuccess;
+    return cudaMemcpyAsync(dst, (const char*)src + elem * B, elem * ns, cudaMemcpyDeviceToHost, s);
+  };
+  CK(get(pos.data(), d.pos, sizeof(double4)));
+  if (a->vel) CK(get(vel.data(), d.vel, sizeof(double4)));
+  if (a->acel) CK(get(acel.data(), d.acel, sizeof(double4)));
+  if (a->force) CK(get(force.data(), d.force, sizeof(double4)));
+  if (a->pos_old) CK(get(pos_old.data(), d.pos_old, sizeof(double4)));
+  if (a->old_cg) CK(get(old_cg.data(), d.old_cg, sizeof(double4)));
+  if (a->epot) CK(get(epot.data(), d.epot, sizeof(double)));
+  CK(get(typ.data(), d.typ, 1));
+  if (a->skip) CK(get(skip.data(), d.skip, 1));
+  CK(get(ing.data(), d.in_gcmc, 1));
+  CK(get(id.data(), d.id, sizeof(long long)));
+  CK(get(rank.data(), d.rank, sizeof(int)));
   CK(cudaStreamSynchronize(s));
   int n = 0;
   for (int q = 0; q < nal; ++q)
@@ -826,8 +940,9 @@ int dml_get_atoms(dml_ctx* c, dml_atoms* a) {
   a->n = n;
   int i = 0;
   for (int q = 0; q < nal; ++q) {
-    int h = alist[q];
-    if (h < 0) continue;
+    int h = alist[q] - B;
+    if (alist[q] < 0) continue;
+    if (h < 0 || h >= ns) return DML_E_STATE;
     auto put = [&](double* dst, const double4& v) {
       if (!dst) return;
       dst[3 * i] = v.x;
@@ -851,45 +966,71 @@ int dml_get_atoms(dml_ctx* c, dml_atoms* a) {
   return 0;
 }
 
-int dml_get_neighbors(dml_ctx* c, int32_t* n_ref, int32_t* nn, int32_t* list, int32_t ld) {
-  if (!c || !n_ref || !nn || !list) return DML_E_ARG;
+int dml_get_atoms(dml_ctx* c, dml_atoms* a) {
+  if (!c || !a) return DML_E_ARG;
+  if (c->D.nrep != 1) return DML_E_ARG;
+  return dml_get_atoms_replica(c, 0, a);
+}
+
+// Replica `rep`'s Verlet lists by hs%ref rank, entries as sys%alist positions
+// (-1 for an atom in limbo).
+int dml_get_neighbors_replica(dml_ctx* c, int32_t rep, int32_t* n_ref, int32_t* nn,
+                              int32_t* list, int32_t ld) {
+  if (!c || !n_ref || !nn || !list || rep < 0 || rep >= c->D.nrep) return DML_E_ARG;
   if (!c->loaded) return DML_E_STATE;
   int rc = read_scalars(c);
   if (rc) return rc;
   const Dev& d = c->D;
   cudaStream_t s = c->stream;
-  const int ns = c->h_sc->n_slots, nr = c->h_sc->n_rank, nal = c->h_sc->n_alist;
+  const int B = c->rc[rep].base;
+  const int ns = c->h_sc[rep].n_slots, nr = c->h_sc[rep].n_rank, nal = c->h_sc[rep].n_alist;
   const int mnb = c->P.mnb;
   std::vector<int> ref(nr), hnn(ns), alist(nal);
   std::vector<int8_t> st(ns);
-  if (nr) CK(cudaMemcpyAsync(ref.data(), d.ref, sizeof(int) * nr, cudaMemcpyDeviceToHost, s));
-  if (nal) CK(cudaMemcpyAsync(alist.data(), d.alist, sizeof(int) * nal, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(hnn.data(), d.nn, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(st.data(), d.state, ns, cudaMemcpyDeviceToHost, s));
+  if (nr) CK(cudaMemcpyAsync(ref.data(), d.ref + B, sizeof(int) * nr, cudaMemcpyDeviceToHost, s));
+  if (nal) CK(cudaMemcpyAsync(alist.data(), d.alist + B, sizeof(int) * nal, cudaMemcpyDeviceToHost, s));
+  if (ns) {
+    CK(cudaMemcpyAsync(hnn.data(), d.nn + B, sizeof(int) * ns, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(st.data(), d.state + B, ns, cudaMemcpyDeviceToHost, s));
+  }
   CK(cudaStreamSynchronize(s));
-  // hs slot -> sys%alist position
+  // local slot -> sys%alist position
   std::vector<int> pos_of(ns, -1);
   int q = 0;
   for (int i = 0; i < nal; ++i)
-    if (alist[i] >= 0) pos_of[alist[i]] = q++;
+    if (alist[i] >= 0) {
+      int h = alist[i] - B;
+      if (h < 0 || h >= ns) return DML_E_STATE;
+      pos_of[h] = q++;
+    }
   std::vector<int> row(mnb);
   int k = 0;
   for (int r = 0; r < nr; ++r) {
     int h = ref[r];
     if (h < 0) continue;
+    h -= B;
+    if (h < 0 || h >= ns) return DML_E_STATE;
     int cnt = hnn[h];
     if (cnt > ld) return DML_E_ARG;
     if (cnt)
-      CK(cudaMemcpy(row.data(), d.list + (size_t)h * mnb, sizeof(int) * cnt, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(row.data(), d.list + (size_t)(B + h) * mnb, sizeof(int) * cnt,
+                    cudaMemcpyDeviceToHost));
     nn[k] = cnt;
     for (int e = 0; e < cnt; ++e) {
-      int j = row[e];
+      int j = row[e] - B;
+      if (j < 0 || j >= ns) return DML_E_STATE;
       list[(size_t)k * ld + e] = st[j] == ST_LIMBO ? -1 : pos_of[j];
     }
     ++k;
   }
   *n_ref = k;
   return 0;
+}
+
+int dml_get_neighbors(dml_ctx* c, int32_t* n_ref, int32_t* nn, int32_t* list, int32_t ld) {
+  if (!c) return DML_E_ARG;
+  if (c->D.nrep != 1) return DML_E_ARG;
+  return dml_get_neighbors_replica(c, 0, n_ref, nn, list, ld);
 }
 
 }  // extern "C"

@@ -28,39 +28,67 @@ enum { ST_NULL = 0, ST_LIVE = 1, ST_LIMBO = 2 };
 constexpr int kNearCap = 32;   // near-contact entries per atom (overlap)
 constexpr int kBlock = 256;
 
-// Device scalars (one struct in device memory per context).
+// Replicas.  A context holds one or more independent systems ("replicas",
+// the batched form); a single system is a batch of one.  Replica r owns the
+// positions [base, base + cap) of every per-atom array (hs slots, hs%b
+// slots, hs%ref ranks, sys%alist and gcmc%alist positions), with cap a
+// multiple of kBlock, so every thread block lies inside one replica and
+// loads its replica's constants and state once.
+
+// Per-replica constants (read-only during steps).
+struct RepConst {
+  double box[3], one_box[3], halfbox[3];
+  double cell[3];
+  float boxf[3], halfboxf[3];
+  int ncells[3];
+  int head_dim[3];          // ncells + 2
+  int use_cells;
+  int cell_off, ncell;      // this replica's range of the cell arrays
+  int base, cap, nblk;      // positions [base, base + cap), cap / kBlock blocks
+  unsigned long long seed;  // Philox key of this replica
+};
+
+// Per-replica device state (mutable).
 struct Scalars {
   double zmax, z0, z1, rho, rho0, lohi;
-  unsigned long long delta2_bits;   // max |pos - old_cg|^2 over hs%ref (as bits)
-  unsigned long long d1_bits, d2_bits; // unused slot (kept for alignment)
-  long long step;
   unsigned long long try_, depo, choques, choques3, nupd, gcmc_ins, gcmc_del;
-  int n_slots;     // hs%amax
+  int n_slots;     // hs%amax (local slots in use)
   int n_b;         // hs%b%amax
-  int n_rank;      // rank slots in use (members + holes)
+  int n_rank;      // rank positions in use (members + holes)
   int n_ref;       // hs%ref%nat
   int n_atoms;     // sys%nat
   int listed;      // neighbour list built
   int rebuild;     // set by the displacement test
-  int error;       // first dml_status raised on the device
-  int err_info;
-  int again;       // overlap pass produced a move-back
-  int passes;      // passes of the last overlap_moveback
-  int n_comp;      // overlap components
-  int comp_total;  // members over all components
   int max_nn;
-  unsigned int ticket;   // last-block-done counters
+  int passes;      // passes of the last overlap_moveback
+  int again, again2;     // overlap pass flags (pass p-1, pass p) when captures can fail
+  unsigned int ticket;   // last-block-done counters of this replica
   unsigned int ticket2;
   int rho_count;
   int n_new_cg;
   // structure (GCMC insertions and deletions)
-  int n_cand;      // entries in the force candidate queue
   int n_alist;     // positions used in alist (members + holes)
   int n_gorder;    // positions used in gorder (members + holes)
   int n_gcmc;      // gcmc%nat
   int nlimbo;      // hs%nlimbo
   int b_nat;       // hs%b%nat
   long long next_id;
+};
+
+// Context-wide device state.
+struct Global {
+  long long step;
+  unsigned long long delta2_bits;  // max |pos - old_cg|^2 over all hs%ref (as bits)
+  int error;       // first dml_status raised on the device
+  int err_info;
+  int err_rep;
+  int again;       // overlap pass produced a move-back
+  int passes;      // passes of the last overlap_moveback (max over replicas)
+  int n_comp;      // overlap components
+  int comp_total;  // members over all components
+  int n_cand;      // entries in the force candidate queue
+  int any_rebuild; // some replica rebuilds its list this test_update
+  unsigned int ticket_rep;  // replicas finished with the displacement test
 };
 
 struct EvRec {            // one interacting list entry seen from one atom
@@ -74,11 +102,6 @@ struct EvRec {            // one interacting list entry seen from one atom
 // Constants computed on the host with the reference's operation order and
 // passed by value to every kernel.
 struct KParams {
-  double box[3], one_box[3], halfbox[3];
-  double cell[3];
-  int ncells[3];
-  int head_dim[3];          // ncells + 2
-  int use_cells;
   double rc2;               // rc*rc (hs%rcut2)
   double rlist2;            // (rc+skin)^2
   double skin;
@@ -93,7 +116,6 @@ struct KParams {
   double fix_scale, fix_inv; // 2^32 per eV/Å in ui/Å, and its inverse
   float rlist_lo2, rlist_hi2; // list shell bounds (FP32)
   float margin;             // FP32 position error bound
-  float boxf[3], halfboxf[3], one_boxf[3];
   double mass[3];
   // Ermak (set_ermak, dana.F90:947-971)
   double cc0, cc1, cc2, cc2h, cc1mcc2, crv1, crv2;
@@ -105,7 +127,6 @@ struct KParams {
   double ztop_is_z1;        // chunks: calc_rho uses z1
   int integrator, reservoir;
   int mnb, ev_cap, max_passes;
-  unsigned long long seed;
   // gcmc_run (dana.F90:590-713)
   double act, beta_num;     // beta = sqrt(beta_num / mass), beta_num = kB(module) * T
   int nadj;
@@ -139,8 +160,14 @@ struct Dev {
   // reductions
   unsigned long long* part;  // per-block partials (top-2, as double bits)
   int nblk_part;
-  Scalars* sc;
-  int cap;            // atom capacity (hs slots, b slots, ranks)
+  // replicas
+  Scalars* sc;        // [nrep] per-replica state
+  Global* g;          // context-wide state
+  RepConst* rc;       // [nrep] per-replica constants
+  int* rep_of;        // [cap] replica of every position
+  int nrep;
+  int cap;            // positions over all replicas (sum of the replica caps)
+  int any_cells, any_verlet;  // some replica uses linked cells / the all-pairs build
 };
 
 // ---- kernel launchers (dml_kernels.cu); each returns the kernels it queued ----

@@ -27,8 +27,8 @@ __constant__ int c_map[27][3] = {
     {-1, 0, 0},  {-1, -1, 0}, {0, -1, 0},   {1, -1, 0},  {-1, 0, 1},  {-1, -1, 1}, {0, -1, 1},
     {1, -1, 1},  {-1, 0, -1}, {-1, -1, -1}, {0, -1, -1}, {1, -1, -1}, {0, 0, -1}};
 
-__device__ __forceinline__ void raise_error(Scalars* sc, int code, int info) {
-  if (atomicCAS(&sc->error, 0, code) == 0) sc->err_info = info;
+__device__ __forceinline__ void raise_error(Global* g, int code, int info) {
+  if (atomicCAS(&g->error, 0, code) == 0) g->err_info = info;
 }
 
 __device__ __forceinline__ unsigned long long* u64(unsigned long long* p) { return p; }
@@ -66,26 +66,26 @@ __device__ __forceinline__ double pow7(double x) {
 
 // vdistance (Groups.F90:995-1016): a - b, minimum image by idnint (round half
 // away from zero) in x and y; z is not periodic.
-__device__ __forceinline__ void vdist_nint(const KParams& p, double4 a, double4 b, double& x,
+__device__ __forceinline__ void vdist_nint(const RepConst& R, double4 a, double4 b, double& x,
                                            double& y, double& z) {
   x = a.x - b.x;
   y = a.y - b.y;
   z = a.z - b.z;
-  x = x - p.box[0] * round(x * p.one_box[0]);
-  y = y - p.box[1] * round(y * p.one_box[1]);
+  x = x - R.box[0] * round(x * R.one_box[0]);
+  y = y - R.box[1] * round(y * R.one_box[1]);
 }
 
 // FP32 pre-filter distance: minimum image by compare and add (no rounding
 // or conversion instruction; on GB300 those issue on the narrow FP64 pipe).
 // Near half a box the chosen image may differ from the exact one, where both
 // images are farther than any cut-off.
-__device__ __forceinline__ void vdist_nint_f(const KParams& p, float4 a, float4 b, float& x,
+__device__ __forceinline__ void vdist_nint_f(const RepConst& R, float4 a, float4 b, float& x,
                                              float& y, float& z) {
   x = a.x - b.x;
   y = a.y - b.y;
   z = a.z - b.z;
-  if (x > p.halfboxf[0]) x -= p.boxf[0]; else if (x < -p.halfboxf[0]) x += p.boxf[0];
-  if (y > p.halfboxf[1]) y -= p.boxf[1]; else if (y < -p.halfboxf[1]) y += p.boxf[1];
+  if (x > R.halfboxf[0]) x -= R.boxf[0]; else if (x < -R.halfboxf[0]) x += R.boxf[0];
+  if (y > R.halfboxf[1]) y -= R.boxf[1]; else if (y < -R.halfboxf[1]) y += R.boxf[1];
 }
 
 // int(x) + 1 for a cell index, with the x86-64 reference semantics: NaN or
@@ -109,34 +109,38 @@ __device__ __forceinline__ bool coord_in_tess(double x, double cell, int n) {
   return c >= 0 && c <= n + 1;
 }
 
-__device__ __forceinline__ bool in_tessellation(const KParams& p, double4 P) {
-  return coord_in_tess(P.x, p.cell[0], p.ncells[0]) && coord_in_tess(P.y, p.cell[1], p.ncells[1]) &&
-         coord_in_tess(P.z, p.cell[2], p.ncells[2]);
+__device__ __forceinline__ bool in_tessellation(const RepConst& R, double4 P) {
+  return coord_in_tess(P.x, R.cell[0], R.ncells[0]) && coord_in_tess(P.y, R.cell[1], R.ncells[1]) &&
+         coord_in_tess(P.z, R.cell[2], R.ncells[2]);
 }
+
+// Replica of the block (replica capacities are multiples of the block size).
+__device__ __forceinline__ int block_rep(const Dev& d) { return d.rep_of[blockIdx.x * blockDim.x]; }
 
 __device__ __forceinline__ int warp_id_global() {
   return (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 }
 
 // ----------------------------------------------------------------- step
-__global__ void step_begin_kernel(Scalars* sc) { sc->step += 1; }
+__global__ void step_begin_kernel(Global* g) { g->step += 1; }
 
 // atom_pbc (dana.F90:1187-1250) on registers; returns true when deposited.
-__device__ __forceinline__ bool atom_pbc_dev(const KParams& p, Scalars* sc, long long step,
+__device__ __forceinline__ bool atom_pbc_dev(const KParams& p, const RepConst& R, Scalars* sc,
+                                             long long step,
                                              long long id, double* pp, double4& po, bool& po_changed,
                                              double4& vv, bool& v_changed, const double4& oc,
                                              int& typ, double zmax) {
   bool depos = false;
   double pox[2] = {po.x, po.y};
   for (int j = 0; j < 2; ++j) {
-    if (pp[j] > p.box[j]) {
-      pp[j] = pp[j] - p.box[j];
-      pox[j] = pox[j] - p.box[j];
+    if (pp[j] > R.box[j]) {
+      pp[j] = pp[j] - R.box[j];
+      pox[j] = pox[j] - R.box[j];
       po_changed = true;
     }
     if (pp[j] < 0.0) {
-      pp[j] = pp[j] + p.box[j];
-      pox[j] = pox[j] + p.box[j];
+      pp[j] = pp[j] + R.box[j];
+      pox[j] = pox[j] + R.box[j];
       po_changed = true;
     }
   }
@@ -155,7 +159,7 @@ __device__ __forceinline__ bool atom_pbc_dev(const KParams& p, Scalars* sc, long
   }
   if (pp[2] <= 0.0) {
     count_add(&sc->try_, 1ull);
-    double ne = dml_uniform(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_CAPTURE, 0));
+    double ne = dml_uniform(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_CAPTURE, 0));
     if (ne < p.prob) {
       count_add(&sc->depo, 1ull);
       typ = DML_Z_F;
@@ -170,13 +174,15 @@ __device__ __forceinline__ bool atom_pbc_dev(const KParams& p, Scalars* sc, long
 
 // ermak_a (dana.F90:974-1028): one thread per hs%ref member.
 __global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
-  n_rank = d.sc->n_rank;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
   int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_rank) return;
+  if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
-  Scalars* sc = d.sc;
-  long long step = sc->step;
+  long long step = d.g->step;
   double zmax = sc->zmax;
   double4 P = d.pos[h];
   double4 V = d.vel[h];
@@ -189,8 +195,8 @@ __global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
   double aa[3] = {A.x, A.y, A.z};
   double rv[3];
   double nq[8];
-  dml_normal_quad(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_ERMAK, 0), &nq[0]);
-  dml_normal_quad(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_ERMAK, 1), &nq[4]);
+  dml_normal_quad(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 0), &nq[0]);
+  dml_normal_quad(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 1), &nq[4]);
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
     double r1 = nq[2 * j], r2 = nq[2 * j + 1];
@@ -201,7 +207,7 @@ __global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
   double4 po = d.pos_old[h];
   bool po_changed = false, v_changed = false;
   int typ0 = typ;
-  bool depos = atom_pbc_dev(p, sc, step, id, pp, po, po_changed, V, v_changed, P, typ, zmax);
+  bool depos = atom_pbc_dev(p, R, sc, step, id, pp, po, po_changed, V, v_changed, P, typ, zmax);
   double4 np = make_double4(pp[0], pp[1], pp[2], 0.0);
   d.old_cg[h] = P;
   d.pos[h] = np;
@@ -215,20 +221,22 @@ __global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
 
 // cbrownian_hs (dana.F90:798-846): one thread per hs%ref member.
 __global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
-  n_rank = d.sc->n_rank;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
   int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_rank) return;
+  if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
-  Scalars* sc = d.sc;
-  long long step = sc->step;
+  long long step = d.g->step;
   double zmax = sc->zmax;
   double4 P = d.pos[h];
   int typ = d.typ[h];
   long long id = d.id[h];
   double fac = P.z > p.dif_switch_z ? p.fac_sc : p.fac_sei;
   double nrm[4];
-  dml_normal_quad(dml_draw(p.seed, step, (uint64_t)id, DML_RNG_BROWN, 0), nrm);
+  dml_normal_quad(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_BROWN, 0), nrm);
   double pp[3] = {P.x, P.y, P.z};
   double vv[3];
 #pragma unroll
@@ -241,7 +249,7 @@ __global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
   double4 po = d.pos_old[h];
   bool po_changed = false, v_changed = false;
   int typ0 = typ;
-  bool depos = atom_pbc_dev(p, sc, step, id, pp, po, po_changed, V, v_changed, P, typ, zmax);
+  bool depos = atom_pbc_dev(p, R, sc, step, id, pp, po, po_changed, V, v_changed, P, typ, zmax);
   double4 np = make_double4(pp[0], pp[1], pp[2], 0.0);
   d.old_cg[h] = P;
   d.pos[h] = np;
@@ -255,15 +263,15 @@ __global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
 // ---------------------------------------------------------------- fuerza
 // FP32 pre-filter of one entry: true when the entry may interact.  The
 // element of a non-live slot (limbo, Neighbor.F90:1089-1092) is 0 in posf.
-__device__ __forceinline__ bool force_candidate(const KParams& p, float4 Pf, int k, float4 Q,
-                                                int& m) {
+__device__ __forceinline__ bool force_candidate(const KParams& p, const RepConst& R, float4 Pf,
+                                                int k, float4 Q, int& m) {
   m = elem_of(Q);
   if (m == 0) return false;
   if (k == DML_Z_CG && m == DML_Z_CG) return false;
   if (!p.pair_on[k - 1][m - 1]) return false;  // eps = 0: contributes signed zeros only
   float fx = Pf.x - Q.x, fy = Pf.y - Q.y, fz = Pf.z - Q.z;
-  if (fx > p.halfboxf[0]) fx -= p.boxf[0]; else if (fx < -p.halfboxf[0]) fx += p.boxf[0];
-  if (fy > p.halfboxf[1]) fy -= p.boxf[1]; else if (fy < -p.halfboxf[1]) fy += p.boxf[1];
+  if (fx > R.halfboxf[0]) fx -= R.boxf[0]; else if (fx < -R.halfboxf[0]) fx += R.boxf[0];
+  if (fy > R.halfboxf[1]) fy -= R.boxf[1]; else if (fy < -R.halfboxf[1]) fy += R.boxf[1];
   float drf = fx * fx + fy * fy + fz * fz;
   return drf <= p.r0f_pref2[k - 1][m - 1];
 }
@@ -275,10 +283,12 @@ __device__ __forceinline__ bool force_candidate(const KParams& p, float4 Pf, int
 // warp whatever its active lanes, so the exact FP64 work is done afterwards
 // on the dense queue (force_exact_kernel), 32 entries per instruction.
 __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n_rank) {
-  n_rank = d.sc->n_rank;  // grids are sized by capacity
-  int r = warp_id_global();
+  int r = warp_id_global();  // grids are sized by capacity
   int lane = threadIdx.x & 31;
-  if (r >= n_rank) return;
+  const int rep = d.rep_of[r];
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
   int k = d.typ[h];
@@ -293,13 +303,13 @@ __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n
     if (j0 >= 0) Q0 = d.posf[j0];
     if (j1 >= 0) Q1 = d.posf[j1];
     int m0, m1;
-    bool c0 = j0 >= 0 && force_candidate(p, Pf, k, Q0, m0);
-    bool c1 = j1 >= 0 && force_candidate(p, Pf, k, Q1, m1);
+    bool c0 = j0 >= 0 && force_candidate(p, R, Pf, k, Q0, m0);
+    bool c1 = j1 >= 0 && force_candidate(p, R, Pf, k, Q1, m1);
     unsigned b0 = __ballot_sync(0xffffffffu, c0), b1 = __ballot_sync(0xffffffffu, c1);
     int tot = __popc(b0) + __popc(b1);
     if (tot == 0) continue;
     int base_q = 0;
-    if (lane == 0) base_q = atomicAdd(&d.sc->n_cand, tot);
+    if (lane == 0) base_q = atomicAdd(&d.g->n_cand, tot);
     base_q = __shfl_sync(0xffffffffu, base_q, 0);
     unsigned lt = (1u << lane) - 1u;
     if (c0) {
@@ -317,26 +327,27 @@ __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n
 // thread per entry, recording each interacting entry for both atoms with the
 // key (rank, jj) that orders the reference's accumulation.
 __global__ void force_exact_kernel(Dev d, KParams p) {
-  int nc = d.sc->n_cand;
+  int nc = d.g->n_cand;
   if (nc > p.cand_cap) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(d.sc, DML_E_EVENT_OVERFLOW, nc);
+    if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(d.g, DML_E_EVENT_OVERFLOW, nc);
     nc = p.cand_cap;
   }
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nc; q += gridDim.x * blockDim.x) {
     int4 c = d.cand[q];
     int r = c.x, jj = c.y, h = c.z, j = c.w;
+    const RepConst& R = d.rc[d.rep_of[h]];
     int k = d.typ[h], m = d.typ[j];
     double4 Pi = d.pos[h], Pj = d.pos[j];
     double vx = Pi.x - Pj.x, vy = Pi.y - Pj.y, vz = Pi.z - Pj.z;
-    if (vx > p.halfbox[0]) {
-      vx = vx - p.box[0];
-    } else if (vx < -p.halfbox[0]) {
-      vx = vx + p.box[0];
+    if (vx > R.halfbox[0]) {
+      vx = vx - R.box[0];
+    } else if (vx < -R.halfbox[0]) {
+      vx = vx + R.box[0];
     }
-    if (vy > p.halfbox[1]) {
-      vy = vy - p.box[1];
-    } else if (vy < -p.halfbox[1]) {
-      vy = vy + p.box[1];
+    if (vy > R.halfbox[1]) {
+      vy = vy - R.box[1];
+    } else if (vy < -R.halfbox[1]) {
+      vy = vy + R.box[1];
     }
     double dr = dot3(vx, vy, vz);
     if (dr > p.r0sq[k - 1][m - 1]) continue;
@@ -359,14 +370,14 @@ __global__ void force_exact_kernel(Dev d, KParams p) {
       e.sign = 1;
       d.ev[(size_t)h * p.ev_cap + si] = e;
     } else {
-      raise_error(d.sc, DML_E_EVENT_OVERFLOW, h);
+      raise_error(d.g, DML_E_EVENT_OVERFLOW, h);
     }
     int sj = atomicAdd(&d.ev_count[j], 1);
     if (sj < p.ev_cap) {
       e.sign = -1;
       d.ev[(size_t)j * p.ev_cap + sj] = e;
     } else {
-      raise_error(d.sc, DML_E_EVENT_OVERFLOW, j);
+      raise_error(d.g, DML_E_EVENT_OVERFLOW, j);
     }
   }
 }
@@ -392,9 +403,13 @@ __device__ __forceinline__ void ermak_b_atom(const Dev& d, const KParams& p, int
 // order, with the Newton reaction applied to both atoms of every entry).
 template <bool FUSE_B>
 __global__ void force_sum_kernel(Dev d, KParams p, int n_slots) {
-  n_slots = d.sc->n_slots;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  n_slots = R.base + sc->n_slots;  // positions in use end here
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s == 0) d.sc->n_cand = 0;
+  if (s == 0) d.g->n_cand = 0;
   if (s >= n_slots) return;
   if (d.state[s] != ST_LIVE) return;
   int cnt = d.ev_count[s];
@@ -416,7 +431,7 @@ __global__ void force_sum_kernel(Dev d, KParams p, int n_slots) {
     unsigned char idx[128];
     unsigned long long keys[128];
     int c = cnt < 128 ? cnt : 128;
-    if (cnt > 128) raise_error(d.sc, DML_E_EVENT_OVERFLOW, s);
+    if (cnt > 128) raise_error(d.g, DML_E_EVENT_OVERFLOW, s);
     for (int i = 0; i < c; ++i) {
       unsigned long long kk = ev[i].key;
       int q = i;
@@ -449,9 +464,12 @@ __global__ void force_sum_kernel(Dev d, KParams p, int n_slots) {
 }
 
 __global__ void ermak_b_kernel(Dev d, KParams p, int n_rank) {
-  n_rank = d.sc->n_rank;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
   int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_rank) return;
+  if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
   ermak_b_atom(d, p, h, d.typ[h], d.force[h]);
@@ -471,19 +489,20 @@ __device__ __forceinline__ long long to_fixed(const KParams& p, float v, double 
 }
 
 __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
-  int nc = d.sc->n_cand;
+  int nc = d.g->n_cand;
   if (nc > p.cand_cap) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(d.sc, DML_E_EVENT_OVERFLOW, nc);
+    if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(d.g, DML_E_EVENT_OVERFLOW, nc);
     nc = p.cand_cap;
   }
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nc; q += gridDim.x * blockDim.x) {
     int4 c = d.cand[q];
     int h = c.z, j = c.w;
+    const RepConst& R = d.rc[d.rep_of[h]];
     int k = d.typ[h], m = d.typ[j];
     double4 Pi = d.pos[h], Pj = d.pos[j];
     double dx = Pi.x - Pj.x, dy = Pi.y - Pj.y, dz = Pi.z - Pj.z;
-    if (dx > p.halfbox[0]) dx -= p.box[0]; else if (dx < -p.halfbox[0]) dx += p.box[0];
-    if (dy > p.halfbox[1]) dy -= p.box[1]; else if (dy < -p.halfbox[1]) dy += p.box[1];
+    if (dx > R.halfbox[0]) dx -= R.box[0]; else if (dx < -R.halfbox[0]) dx += R.box[0];
+    if (dy > R.halfbox[1]) dy -= R.box[1]; else if (dy < -R.halfbox[1]) dy += R.box[1];
     // The distance-dependent core, q = (r0/r)^2 and b = q^3, is formed in
     // FP64 and rounded once to FP32: the force goes as r^-14 in the core, so
     // FP32 roundings of r^2, 1/r^2 and q^3 would be amplified about sixfold.
@@ -502,7 +521,7 @@ __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
     long long fz = to_fixed(p, fr * vz, p.fix_scale);
     long long fe = to_fixed(p, e, p.fix_scale);
     if (fx == LLONG_MIN || fy == LLONG_MIN || fz == LLONG_MIN || fe == LLONG_MIN) {
-      raise_error(d.sc, DML_E_FIXEDPOINT_OVERFLOW, h);
+      raise_error(d.g, DML_E_FIXEDPOINT_OVERFLOW, h);
       continue;
     }
     unsigned long long* ai = (unsigned long long*)(d.facc + 4 * (size_t)h);
@@ -521,9 +540,11 @@ __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
 // Fixed point -> double, accumulators cleared, ermak_b fused.
 template <bool FUSE_B>
 __global__ void force_fix_kernel(Dev d, KParams p, int n_slots) {
-  n_slots = d.sc->n_slots;
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  n_slots = d.rc[rep].base + d.sc[rep].n_slots;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s == 0) d.sc->n_cand = 0;
+  if (s == 0) d.g->n_cand = 0;
   if (s >= n_slots) return;
   if (d.state[s] != ST_LIVE) return;
   long long* a = d.facc + 4 * (size_t)s;
@@ -572,7 +593,11 @@ __device__ __forceinline__ void top2_merge(unsigned long long& a1, unsigned long
 // displacements is order independent, so a tree reduction is exact.
 __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
                                    cudaGraphConditionalHandle cond_handle) {
-  n_slots = d.sc->n_slots;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  n_slots = R.base + sc->n_slots;  // positions in use end here
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned long long tiny = (unsigned long long)__double_as_longlong(1.e-16);
   unsigned long long a1 = tiny, a2 = tiny;
@@ -580,22 +605,22 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
     double4 P = d.pos[s];
     double4 O = d.pos_old[s];
     bool ch = false;
-    if (P.x >= p.box[0]) {
-      P.x = P.x - p.box[0];
-      O.x = O.x - p.box[0];
+    if (P.x >= R.box[0]) {
+      P.x = P.x - R.box[0];
+      O.x = O.x - R.box[0];
       ch = true;
     } else if (P.x < 0.0) {
-      P.x = P.x + p.box[0];
-      O.x = O.x + p.box[0];
+      P.x = P.x + R.box[0];
+      O.x = O.x + R.box[0];
       ch = true;
     }
-    if (P.y >= p.box[1]) {
-      P.y = P.y - p.box[1];
-      O.y = O.y - p.box[1];
+    if (P.y >= R.box[1]) {
+      P.y = P.y - R.box[1];
+      O.y = O.y - R.box[1];
       ch = true;
     } else if (P.y < 0.0) {
-      P.y = P.y + p.box[1];
-      O.y = O.y + p.box[1];
+      P.y = P.y + R.box[1];
+      O.y = O.y + R.box[1];
       ch = true;
     }
     if (ch) {
@@ -605,7 +630,7 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
     }
     // cgroup_sort runs at every test_update (Neighbor.F90:687-691) and stops
     // on an atom outside the tessellation (Cells.F90:293-294), rebuild or not.
-    if (p.use_cells && !in_tessellation(p, P)) raise_error(d.sc, DML_E_OUT_OF_TESSELLATION, s);
+    if (R.use_cells && !in_tessellation(R, P)) raise_error(d.g, DML_E_OUT_OF_TESSELLATION, s);
     double rd = dot3(P.x - O.x, P.y - O.y, P.z - O.z);
     // a NaN displacement never passes `rd > dispmax` (Neighbor.F90:657-661)
     if (rd == rd) top2_merge(a1, a2, (unsigned long long)__double_as_longlong(rd), tiny);
@@ -629,15 +654,16 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
     d.part[2 * blockIdx.x] = b1;
     d.part[2 * blockIdx.x + 1] = b2;
     __threadfence();
-    unsigned t = atomicAdd(&d.sc->ticket, 1u);
-    last = (t == gridDim.x - 1);
+    unsigned t = atomicAdd(&sc->ticket, 1u);
+    last = (t == (unsigned)R.nblk - 1u);
   }
   __syncthreads();
   if (!last) return;
   __threadfence();
-  // last block: parallel top-2 over the block partials
+  // last block of this replica: parallel top-2 over the replica's partials
   unsigned long long b1 = tiny, b2 = tiny;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+  const int b0 = R.base / kBlock;
+  for (int b = b0 + threadIdx.x; b < b0 + R.nblk; b += blockDim.x) {
     unsigned long long c1 = __ldcg(d.part + 2 * b), c2 = __ldcg(d.part + 2 * b + 1);
     top2_merge(b1, b2, c1, c2);
   }
@@ -655,16 +681,23 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
   if (threadIdx.x == 0) {
     unsigned long long e1 = tiny, e2 = tiny;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) top2_merge(e1, e2, w1[w], w2[w]);
-    Scalars* sc = d.sc;
     double d1 = __longlong_as_double((long long)e1), d2 = __longlong_as_double((long long)e2);
     int rebuild = (!sc->listed) || (sqrt(d1) + sqrt(d2) > p.skin);
     sc->rebuild = rebuild;
     if (rebuild) {
       sc->nupd += 1;
       sc->max_nn = 0;
+      atomicOr(&d.g->any_rebuild, 1);
     }
     sc->ticket = 0;
-    if (cond) cudaGraphSetConditional(cond_handle, rebuild ? 1u : 0u);
+    __threadfence();
+    // the last replica to decide opens the rebuild subgraph if any rebuilds
+    unsigned t2 = atomicAdd(&d.g->ticket_rep, 1u);
+    if (t2 == (unsigned)d.nrep - 1u) {
+      int any = atomicAdd(&d.g->any_rebuild, 0);
+      d.g->ticket_rep = 0;
+      if (cond) cudaGraphSetConditional(cond_handle, any ? 1u : 0u);
+    }
   }
 }
 
@@ -672,11 +705,14 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
 // (igroup_clean, Groups.F90:1036-1053), cell index of every hs%b slot
 // (cgroup_sort_atom, Cells.F90:281-302) and the per-cell counts.
 __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int cells_only) {
-  n_slots = d.sc->n_slots;
-  n_b = d.sc->n_b;
-  if (!cells_only && !d.sc->rebuild) return;
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  n_slots = R.base + sc->n_slots;
+  n_b = R.base + sc->n_b;
+  if (!cells_only && !sc->rebuild) return;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!cells_only && s == 0) d.sc->nlimbo = 0;
+  if (!cells_only && s == R.base) sc->nlimbo = 0;
   if (!cells_only && s < n_slots) {
     int st = d.state[s];
     if (st == ST_LIVE) {
@@ -685,23 +721,23 @@ __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int 
       d.state[s] = ST_NULL;
     }
   }
-  if (p.use_cells && s < n_b) {
+  if (R.use_cells && s < n_b) {
     int hs = d.b2hs[s];
     if (hs < 0) {
       d.cell_of[s] = -1;
       return;
     }
     double4 P = d.pos[hs];
-    int c1 = cell_index(P.x, p.cell[0]);
-    int c2 = cell_index(P.y, p.cell[1]);
-    int c3 = cell_index(P.z, p.cell[2]);
-    if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > p.ncells[0] + 1 || c2 > p.ncells[1] + 1 ||
-        c3 > p.ncells[2] + 1) {
-      raise_error(d.sc, DML_E_OUT_OF_TESSELLATION, hs);
+    int c1 = cell_index(P.x, R.cell[0]);
+    int c2 = cell_index(P.y, R.cell[1]);
+    int c3 = cell_index(P.z, R.cell[2]);
+    if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] + 1 || c2 > R.ncells[1] + 1 ||
+        c3 > R.ncells[2] + 1) {
+      raise_error(d.g, DML_E_OUT_OF_TESSELLATION, hs);
       d.cell_of[s] = -1;
       return;
     }
-    int lin = (c3 * p.head_dim[1] + c2) * p.head_dim[0] + c1;
+    int lin = R.cell_off + (c3 * R.head_dim[1] + c2) * R.head_dim[0] + c1;
     d.cell_of[s] = lin;
     atomicAdd(&d.cell_count[lin], 1);
   }
@@ -709,7 +745,7 @@ __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int 
 
 // Exclusive scan of the cell counts (one block).
 __global__ void cell_scan_kernel(Dev d, int ncell, int force) {
-  if (!force && !d.sc->rebuild) return;
+  if (!force && !d.g->any_rebuild) return;
   __shared__ int wsum[32];
   __shared__ int carry;
   if (threadIdx.x == 0) carry = 0;
@@ -747,8 +783,12 @@ __global__ void cell_scan_kernel(Dev d, int ncell, int force) {
 }
 
 __global__ void cell_scatter_kernel(Dev d, int n_b, int force) {
-  n_b = d.sc->n_b;
-  if (!force && !d.sc->rebuild) return;
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  n_b = R.base + sc->n_b;
+  if (!R.use_cells) return;            // no cells: cell_of is never written
+  if (!force && !sc->rebuild) return;  // its cell_of entries are from an older sort
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= n_b) return;
   int c = d.cell_of[b];
@@ -762,7 +802,7 @@ __global__ void cell_scatter_kernel(Dev d, int n_b, int force) {
 // One warp per cell; the sorted cell goes to comp_members (scratch) and is
 // copied back as hs slots (what the list stores).
 __global__ void cell_order_kernel(Dev d, int ncell, int force) {
-  if (!force && !d.sc->rebuild) return;
+  if (!force && !d.g->any_rebuild) return;
   int c = warp_id_global();
   int lane = threadIdx.x & 31;
   if (c >= ncell) return;
@@ -787,18 +827,20 @@ __global__ void cell_order_kernel(Dev d, int ncell, int force) {
 // stencil cells in map order (Cells.F90:28-36), each cell in chain order,
 // wrapped as cell_pbc with mic (Cells.F90:378-404), `rd < (rc+skin)^2`.
 __global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
-  n_rank = d.sc->n_rank;  // grids are sized by capacity
-  if (!d.sc->rebuild) return;
-  int r = warp_id_global();
+  int r = warp_id_global();  // grids are sized by capacity
   int lane = threadIdx.x & 31;
-  if (r >= n_rank) return;
+  const int rep = d.rep_of[r];
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  if (!sc->rebuild || !R.use_cells) return;
+  if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
   double4 P = d.pos[h];
   float4 Pf = d.posf[h];
-  int rc[3] = {cell_index(P.x, p.cell[0]), cell_index(P.y, p.cell[1]), cell_index(P.z, p.cell[2])};
+  int rc[3] = {cell_index(P.x, R.cell[0]), cell_index(P.y, R.cell[1]), cell_index(P.z, R.cell[2])};
   if (rc[0] == INT_MIN || rc[1] == INT_MIN || rc[2] == INT_MIN) {
-    if (lane == 0) raise_error(d.sc, DML_E_OUT_OF_TESSELLATION, h);
+    if (lane == 0) raise_error(d.g, DML_E_OUT_OF_TESSELLATION, h);
     return;
   }
   int* row = d.list + (size_t)h * p.mnb;
@@ -809,15 +851,15 @@ __global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       int t = c_map[nabor][k] + rc[k] - 1;
-      t = (t + p.ncells[k]) % p.ncells[k];
+      t = (t + R.ncells[k]) % R.ncells[k];
       nc[k] = t + 1;
-      if (nc[k] < 0 || nc[k] > p.ncells[k] + 1) bad = true;
+      if (nc[k] < 0 || nc[k] > R.ncells[k] + 1) bad = true;
     }
     if (bad) {
-      if (lane == 0) raise_error(d.sc, DML_E_OUT_OF_TESSELLATION, h);
+      if (lane == 0) raise_error(d.g, DML_E_OUT_OF_TESSELLATION, h);
       return;
     }
-    int c = (nc[2] * p.head_dim[1] + nc[1]) * p.head_dim[0] + nc[0];
+    int c = R.cell_off + (nc[2] * R.head_dim[1] + nc[1]) * R.head_dim[0] + nc[0];
     int start = d.cell_start[c];
     int num = d.cell_start[c + 1] - start;
     for (int base = 0; base < num; base += 32) {
@@ -829,13 +871,13 @@ __global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
         if (j != h) {
           float4 Q = d.posf[j];
           float fx, fy, fz;
-          vdist_nint_f(p, Q, Pf, fx, fy, fz);
+          vdist_nint_f(R, Q, Pf, fx, fy, fz);
           float drf = fx * fx + fy * fy + fz * fz;
           if (drf < p.rlist_lo2) {
             inc = true;
           } else if (drf <= p.rlist_hi2) {
             double vx, vy, vz;
-            vdist_nint(p, d.pos[j], P, vx, vy, vz);
+            vdist_nint(R, d.pos[j], P, vx, vy, vz);
             double rd = dot3(vx, vy, vz);
             inc = rd < p.rlist2;
           }
@@ -849,30 +891,32 @@ __global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
   }
   if (lane == 0) {
     if (cnt > p.mnb) {
-      raise_error(d.sc, DML_E_NEIGH_OVERFLOW, h);
+      raise_error(d.g, DML_E_NEIGH_OVERFLOW, h);
       cnt = p.mnb;
     }
     d.nn[h] = cnt;
-    atomicMax(&d.sc->max_nn, cnt);
+    atomicMax(&sc->max_nn, cnt);
   }
 }
 
 // ngroup_verlet (Neighbor.F90:358-424): all hs%b slots in index order,
 // `rd > (rc+skin)^2` rejected (so equality is kept), vdistance(ai, aj).
 __global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
-  n_rank = d.sc->n_rank;
-  n_b = d.sc->n_b;
-  if (!d.sc->rebuild) return;
-  int r = warp_id_global();
+  int r = warp_id_global();  // grids are sized by capacity
   int lane = threadIdx.x & 31;
-  if (r >= n_rank) return;
+  const int rep = d.rep_of[r];
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  if (!sc->rebuild || R.use_cells) return;
+  if (r - R.base >= sc->n_rank) return;
+  n_b = R.base + sc->n_b;
   int h = d.ref[r];
   if (h < 0) return;
   double4 P = d.pos[h];
   float4 Pf = d.posf[h];
   int* row = d.list + (size_t)h * p.mnb;
   int cnt = 0;
-  for (int base = 0; base < n_b; base += 32) {
+  for (int base = R.base; base < n_b; base += 32) {
     int b = base + lane;
     bool inc = false;
     int j = -1;
@@ -881,13 +925,13 @@ __global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
       if (j >= 0 && j != h) {
         float4 Q = d.posf[j];
         float fx, fy, fz;
-        vdist_nint_f(p, Pf, Q, fx, fy, fz);
+        vdist_nint_f(R, Pf, Q, fx, fy, fz);
         float drf = fx * fx + fy * fy + fz * fz;
         if (drf < p.rlist_lo2) {
           inc = true;
         } else if (drf <= p.rlist_hi2) {
           double vx, vy, vz;
-          vdist_nint(p, P, d.pos[j], vx, vy, vz);
+          vdist_nint(R, P, d.pos[j], vx, vy, vz);
           double rd = dot3(vx, vy, vz);
           inc = !(rd > p.rlist2);
         }
@@ -900,16 +944,19 @@ __global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
   }
   if (lane == 0) {
     if (cnt > p.mnb) {
-      raise_error(d.sc, DML_E_NEIGH_OVERFLOW, h);
+      raise_error(d.g, DML_E_NEIGH_OVERFLOW, h);
       cnt = p.mnb;
     }
     d.nn[h] = cnt;
-    atomicMax(&d.sc->max_nn, cnt);
+    atomicMax(&sc->max_nn, cnt);
   }
 }
 
 __global__ void rebuild_done_kernel(Dev d) {
-  if (d.sc->rebuild) d.sc->listed = 1;
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r == 0) d.g->any_rebuild = 0;
+  if (r >= d.nrep) return;
+  if (d.sc[r].rebuild) d.sc[r].listed = 1;
 }
 
 // ------------------------------------------------------- overlap_moveback
@@ -923,13 +970,21 @@ __global__ void rebuild_done_kernel(Dev d) {
 // gives exactly the reference's result.
 
 __global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
-  n_slots = d.sc->n_slots;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  n_slots = R.base + sc->n_slots;  // positions in use end here
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s == 0) {
-    d.sc->again = 0;
-    d.sc->n_comp = 0;
-    d.sc->comp_total = 0;
-    d.sc->passes = 1;
+    d.g->again = 0;
+    d.g->n_comp = 0;
+    d.g->comp_total = 0;
+    d.g->passes = 1;
+  }
+  if (s == R.base) {
+    sc->passes = 1;
+    sc->again2 = 0;
   }
   double dd = 0.0;
   if (s < n_slots) {
@@ -940,13 +995,13 @@ __global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
     if (d.state[s] == ST_LIVE && d.rank[s] >= 0) {
       double4 P = d.pos[s], O = d.old_cg[s];
       double x, y, z;
-      vdist_nint(p, P, O, x, y, z);
+      vdist_nint(R, P, O, x, y, z);
       dd = dot3(x, y, z);
     }
   }
   for (int off = 16; off > 0; off >>= 1) dd = fmax(dd, __shfl_down_sync(0xffffffffu, dd, off));
   if ((threadIdx.x & 31) == 0 && dd > 0.0)
-    atomicMax(&d.sc->delta2_bits, (unsigned long long)__double_as_longlong(dd));
+    atomicMax(&d.g->delta2_bits, (unsigned long long)__double_as_longlong(dd));
 }
 
 __device__ int uf_find(volatile int* uf, int x) {
@@ -960,7 +1015,7 @@ __device__ int uf_find(volatile int* uf, int x) {
   return -1;
 }
 
-__device__ void uf_union(Scalars* sc, volatile int* uf, int a, int b) {
+__device__ void uf_union(Global* g, volatile int* uf, int a, int b) {
   for (int it = 0; it < (1 << 20); ++it) {
     a = uf_find(uf, a);
     b = uf_find(uf, b);
@@ -973,20 +1028,22 @@ __device__ void uf_union(Scalars* sc, volatile int* uf, int a, int b) {
     }
     if (atomicCAS((int*)&uf[a], a, b) == a) return;
   }
-  raise_error(sc, DML_E_OVERLAP_PASSES, -1);
+  raise_error(g, DML_E_OVERLAP_PASSES, -1);
 }
 
 // Near entries of every hs%ref member: list entries within rc + 2 delta
 // (FP32 with margin; a superset is harmless) in list order.
 __global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p, int n_rank) {
-  n_rank = d.sc->n_rank;  // grids are sized by capacity
-  int r = warp_id_global();
+  int r = warp_id_global();  // grids are sized by capacity
   int lane = threadIdx.x & 31;
-  if (r >= n_rank) return;
+  const int rep = d.rep_of[r];
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
   // rc + 2 delta in FP32 (sqrtf is exact to an ulp; the margin covers it)
-  float delta = sqrtf(__double2float_ru(__longlong_as_double((long long)d.sc->delta2_bits)));
+  float delta = sqrtf(__double2float_ru(__longlong_as_double((long long)d.g->delta2_bits)));
   float rnf = (p.rcf + 2.0f * delta) * 1.000001f + 4.0f * p.margin + 1e-3f;
   float rn2 = rnf * rnf;
   float4 Pf = d.posf[h];
@@ -1009,7 +1066,7 @@ __global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p
       bool inc = false;
       if (j >= 0 && elem_of(Q) != 0) {
         float fx, fy, fz;
-        vdist_nint_f(p, Pf, Q, fx, fy, fz);
+        vdist_nint_f(R, Pf, Q, fx, fy, fz);
         inc = fx * fx + fy * fy + fz * fz <= rn2;
       }
       unsigned bal = __ballot_sync(0xffffffffu, inc);
@@ -1017,7 +1074,7 @@ __global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p
       if (inc) {
         if (cnt + pre < kNearCap) near[cnt + pre] = j;
         if (elem_of(Q) != DML_Z_CG) {
-          uf_union(d.sc, (volatile int*)d.uf, h, j);
+          uf_union(d.g, (volatile int*)d.uf, h, j);
           d.active[j] = 1;
         }
       }
@@ -1034,10 +1091,11 @@ __global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p
 // Atoms with no near entry are examined trivially in pass 1 (skip = true)
 // and can never be moved; the others are counted per component root.
 __global__ void overlap_count_kernel(Dev d, int n_rank) {
-  n_rank = d.sc->n_rank;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
   int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r == 0) d.sc->delta2_bits = 0ull;
-  if (r >= n_rank) return;
+  if (r == 0) d.g->delta2_bits = 0ull;
+  if (r - d.rc[rep].base >= d.sc[rep].n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
   if (!d.active[h]) {
@@ -1050,22 +1108,29 @@ __global__ void overlap_count_kernel(Dev d, int n_rank) {
 }
 
 __global__ void overlap_assign_kernel(Dev d, int n_slots) {
-  n_slots = d.sc->n_slots;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  n_slots = R.base + sc->n_slots;  // positions in use end here
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_slots) return;
   int sz = d.comp_size[s];
   if (sz <= 0) return;
-  int cid = atomicAdd(&d.sc->n_comp, 1);
-  int off = atomicAdd(&d.sc->comp_total, sz);
+  int cid = atomicAdd(&d.g->n_comp, 1);
+  int off = atomicAdd(&d.g->comp_total, sz);
   d.comp_id[s] = cid;
   d.comp_list[2 * cid] = off;
   d.comp_list[2 * cid + 1] = sz;
 }
 
 __global__ void overlap_scatter_kernel(Dev d, int n_rank) {
-  n_rank = d.sc->n_rank;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
   int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_rank) return;
+  if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0 || !d.active[h]) return;
   int root = d.uf[h];
@@ -1076,7 +1141,9 @@ __global__ void overlap_scatter_kernel(Dev d, int n_rank) {
 
 // Examination of o1 = x in pass `pass` (dana.F90:871-935).
 __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, int* again) {
-  Scalars* sc = d.sc;
+  const int rep = d.rep_of[x];
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
   int nc = d.near_count[x];
   int n = nc >= 0 ? nc : d.nn[x];
   const int* src = nc >= 0 ? d.near + (size_t)x * kNearCap : d.list + (size_t)x * p.mnb;
@@ -1086,12 +1153,12 @@ __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, in
     double4 P = d.pos[x];
     double4 Q = d.pos[j];
     double vx, vy, vz;
-    vdist_nint(p, P, Q, vx, vy, vz);
+    vdist_nint(R, P, Q, vx, vy, vz);
     double dr = dot3(vx, vy, vz);
     if (dr > p.rc2) continue;
     if (d.typ[j] == DML_Z_CG) {
       count_add(&sc->try_, 1ull);
-      double ne = dml_uniform(dml_draw(p.seed, sc->step, (uint64_t)d.id[x], DML_RNG_OVERLAP,
+      double ne = dml_uniform(dml_draw(R.seed, d.g->step, (uint64_t)d.id[x], DML_RNG_OVERLAP,
                                        (uint32_t)pass));
       if (ne < p.prob) {
         count_add(&sc->depo, 1ull);
@@ -1099,7 +1166,7 @@ __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, in
         float4 f = d.posf[x];
         f.w = __int_as_float(DML_Z_F);
         d.posf[x] = f;
-        if (P.z > sc->z0) raise_error(sc, DML_E_DENDRITE, x);
+        if (P.z > sc->z0) raise_error(d.g, DML_E_DENDRITE, x);
       } else {
         double4 O = d.old_cg[x];
         d.pos[x] = O;
@@ -1137,7 +1204,7 @@ __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, in
 // in overlap_passn_kernel with a barrier per pass.
 __global__ void overlap_pass1_kernel(Dev d, KParams p, int all_passes) {
   int cid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (cid >= d.sc->n_comp) return;
+  if (cid >= d.g->n_comp) return;
   int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
   int* mem = d.comp_members + off;
   for (int i = 1; i < sz; ++i) {
@@ -1160,62 +1227,84 @@ __global__ void overlap_pass1_kernel(Dev d, KParams p, int all_passes) {
       overlap_exam(d, p, x, pass, &again);
     }
     if (!all_passes) {
-      if (again) d.sc->again = 1;
+      if (again) {
+        d.sc[d.rep_of[mem[0]]].again2 = 1;
+        d.g->again = 1;
+      }
       return;
     }
     if (!again) break;
     if (pass >= p.max_passes) {
-      raise_error(d.sc, DML_E_OVERLAP_PASSES, pass + 1);
+      raise_error(d.g, DML_E_OVERLAP_PASSES, pass + 1);
       break;
     }
     pass += 1;
   }
-  atomicMax(&d.sc->passes, pass);
+  if (sz > 0) atomicMax(&d.sc[d.rep_of[mem[0]]].passes, pass);
+  atomicMax(&d.g->passes, pass);
 }
 
-// Passes 2.. (the recursion): one block, a barrier between passes.
+// Passes 2.. (the recursion, needed when a capture can fail): one block, a
+// barrier between passes.  Each replica recurses on its own flag, as it would
+// alone: a component is examined in pass p only if its replica's pass p-1
+// moved an atom.
 __global__ void overlap_passn_kernel(Dev d, KParams p) {
   __shared__ int again_s;
   __shared__ int go;
-  Scalars* sc = d.sc;
-  int ncomp = sc->n_comp;
+  int ncomp = d.g->n_comp;
   int pass = 1;
-  if (threadIdx.x == 0) go = sc->again;
+  if (threadIdx.x == 0) go = d.g->again;
   __syncthreads();
   while (go) {
     pass += 1;
+    for (int r = threadIdx.x; r < d.nrep; r += blockDim.x) {
+      d.sc[r].again = d.sc[r].again2;
+      d.sc[r].again2 = 0;
+      if (d.sc[r].again) d.sc[r].passes = pass;
+    }
     if (pass > p.max_passes) {
-      if (threadIdx.x == 0) raise_error(sc, DML_E_OVERLAP_PASSES, pass);
+      if (threadIdx.x == 0) raise_error(d.g, DML_E_OVERLAP_PASSES, pass);
       break;
     }
     if (threadIdx.x == 0) again_s = 0;
     __syncthreads();
-    int again = 0;
+    int again_any = 0;
     for (int cid = threadIdx.x; cid < ncomp; cid += blockDim.x) {
       int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
       const int* mem = d.comp_members + off;
+      if (sz == 0) continue;
+      Scalars* sc = d.sc + d.rep_of[mem[0]];
+      if (!sc->again) continue;
+      int again = 0;
       for (int i = 0; i < sz; ++i) {
         int x = mem[i];
         if (d.skip[x]) continue;
         d.skip[x] = 1;
         overlap_exam(d, p, x, pass, &again);
       }
+      if (again) {
+        sc->again2 = 1;
+        again_any = 1;
+      }
     }
-    if (again) atomicOr(&again_s, 1);
+    if (again_any) atomicOr(&again_s, 1);
     __syncthreads();
     if (threadIdx.x == 0) go = again_s;
     __syncthreads();
   }
-  if (threadIdx.x == 0) sc->passes = pass;
+  if (threadIdx.x == 0) d.g->passes = pass;
 }
 
 // ------------------------------------------------- capture commit, rho, piston
 // dana.F90:228-236: every F member of hs%ref becomes CG and leaves hs%ref
 // (its rank becomes a hole; the order of the remaining members is kept).
 __global__ void commit_kernel(Dev d, int n_rank) {
-  n_rank = d.sc->n_rank;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
   int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n_rank) return;
+  if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
   if (d.typ[h] != DML_Z_F) return;
@@ -1225,20 +1314,23 @@ __global__ void commit_kernel(Dev d, int n_rank) {
   d.posf[h] = f;
   d.rank[h] = -1;
   d.ref[r] = -1;
-  atomicSub(&d.sc->n_ref, 1);
-  atomicAdd(&d.sc->n_new_cg, 1);
+  atomicSub(&sc->n_ref, 1);
+  atomicAdd(&sc->n_new_cg, 1);
   if (d.in_gcmc[h]) {  // gcmc%detach (dana.F90:235)
     d.in_gcmc[h] = 0;
     d.gorder[d.gpos[h]] = -1;
-    atomicSub(&d.sc->n_gcmc, 1);
+    atomicSub(&sc->n_gcmc, 1);
   }
 }
 
 // calc_rho (dana.F90:521-549): integer count, so any reduction order is exact.
 __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
-  n_slots = d.sc->n_slots;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  n_slots = R.base + sc->n_slots;  // positions in use end here
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  Scalars* sc = d.sc;
   double z0 = sc->z0;
   double zt = p.ztop_is_z1 != 0.0 ? sc->z1 : sc->zmax;
   int c = 0;
@@ -1252,13 +1344,13 @@ __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
     if (c) atomicAdd(&sc->rho_count, c);
     __threadfence();
     unsigned t = atomicAdd(&sc->ticket2, 1u);
-    last = (t == gridDim.x - 1);
+    last = (t == (unsigned)R.nblk - 1u);  // the replica's last block
   }
   __syncthreads();
   if (last && threadIdx.x == 0) {
     __threadfence();
     int g = atomicAdd(&sc->rho_count, 0);
-    double vol = p.box[0] * p.box[1] * (zt - z0);
+    double vol = R.box[0] * R.box[1] * (zt - z0);
     sc->rho = (double)g / vol;
     sc->rho_count = 0;
     sc->ticket2 = 0;
@@ -1267,9 +1359,12 @@ __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
 
 // maxz (dana.F90:776-794)
 __global__ void piston_kernel(Dev d, KParams p, int n_slots) {
-  n_slots = d.sc->n_slots;  // grids are sized by capacity
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  n_slots = R.base + sc->n_slots;  // positions in use end here
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  Scalars* sc = d.sc;
   double z0 = sc->z0;
   double lohi = (p.h_over_tau * ((sc->rho0 - sc->rho) / sc->rho));
   if (s < n_slots && d.state[s] == ST_LIVE) {
@@ -1280,7 +1375,7 @@ __global__ void piston_kernel(Dev d, KParams p, int n_slots) {
       d.posf[s] = to_f4(P, d.typ[s]);
     }
   }
-  if (s == 0) {
+  if (s == R.base) {
     double zm = sc->zmax;
     sc->lohi = lohi;
     sc->zmax = zm - lohi * (zm - z0);
@@ -1329,55 +1424,56 @@ __device__ int blk_scan_excl(int v, int* total) {
 
 // Stable in-place compaction of an order array (holes = -1); pos_of[h]
 // receives the new position of every member.
-__device__ int blk_compact(int* arr, int n, int* pos_of) {
+__device__ int blk_compact(int* arr, int off, int n, int* pos_of) {
   int out = 0;
   for (int base = 0; base < n; base += blockDim.x) {
     int i = base + threadIdx.x;
-    int h = i < n ? arr[i] : -1;
+    int h = i < n ? arr[off + i] : -1;
     int tot;
     int pre = blk_scan_excl(h >= 0 ? 1 : 0, &tot);
     __syncthreads();
     if (h >= 0) {
-      arr[out + pre] = h;
-      pos_of[h] = out + pre;
+      arr[off + out + pre] = h;
+      pos_of[h] = off + out + pre;
     }
     out += tot;
     __syncthreads();
   }
-  for (int i = out + threadIdx.x; i < n; i += blockDim.x) arr[i] = -1;
+  for (int i = out + threadIdx.x; i < n; i += blockDim.x) arr[off + i] = -1;
   __syncthreads();
   return out;
 }
 
-__device__ __forceinline__ bool list_entry_in(const KParams& p, double4 a, double4 b, bool strict) {
+__device__ __forceinline__ bool list_entry_in(const KParams& p, const RepConst& R, double4 a,
+                                              double4 b, bool strict) {
   double vx, vy, vz;
-  vdist_nint(p, a, b, vx, vy, vz);
+  vdist_nint(R, a, b, vx, vy, vz);
   double rd = dot3(vx, vy, vz);
   return strict ? rd < p.rlist2 : !(rd > p.rlist2);
 }
 
 // Own list of a newly attached atom i, one warp (ngroup_cells_atom,
 // Neighbor.F90:550-603, or ngroup_verlet_atom :426-463).
-__device__ void gcmc_own_list(const Dev& d, const KParams& p, int i) {
+__device__ void gcmc_own_list(const Dev& d, const KParams& p, const RepConst& R, int i) {
   int lane = threadIdx.x & 31;
   double4 P = d.pos[i];
   int* row = d.list + (size_t)i * p.mnb;
   int cnt = 0;
-  if (p.use_cells) {
-    int rc[3] = {cell_index(P.x, p.cell[0]), cell_index(P.y, p.cell[1]), cell_index(P.z, p.cell[2])};
+  if (R.use_cells) {
+    int rc[3] = {cell_index(P.x, R.cell[0]), cell_index(P.y, R.cell[1]), cell_index(P.z, R.cell[2])};
     for (int nabor = 0; nabor < 27; ++nabor) {
       int nc[3];
       for (int k = 0; k < 3; ++k) {
         int t = c_map[nabor][k] + rc[k] - 1;
-        t = (t + p.ncells[k]) % p.ncells[k];
+        t = (t + R.ncells[k]) % R.ncells[k];
         nc[k] = t + 1;
       }
-      int c = (nc[2] * p.head_dim[1] + nc[1]) * p.head_dim[0] + nc[0];
+      int c = R.cell_off + (nc[2] * R.head_dim[1] + nc[1]) * R.head_dim[0] + nc[0];
       // atoms inserted during this run, most recent first (chain heads)
       if (lane == 0) {
         for (int j = d.ins_head[c]; j >= 0; j = d.ins_next[j]) {
           if (j == i || d.state[j] != ST_LIVE) continue;
-          if (list_entry_in(p, d.pos[j], P, true)) {
+          if (list_entry_in(p, R, d.pos[j], P, true)) {
             if (cnt < p.mnb) row[cnt] = j;
             ++cnt;
           }
@@ -1392,7 +1488,7 @@ __device__ void gcmc_own_list(const Dev& d, const KParams& p, int i) {
         int j = -1;
         if (idx < num) {
           j = d.cell_atoms[start + idx];
-          if (j != i && d.state[j] == ST_LIVE) inc = list_entry_in(p, d.pos[j], P, true);
+          if (j != i && d.state[j] == ST_LIVE) inc = list_entry_in(p, R, d.pos[j], P, true);
         }
         unsigned bal = __ballot_sync(0xffffffffu, inc);
         int pre = __popc(bal & ((1u << lane) - 1u));
@@ -1401,14 +1497,14 @@ __device__ void gcmc_own_list(const Dev& d, const KParams& p, int i) {
       }
     }
   } else {
-    int n_b = d.sc->n_b;
-    for (int base = 0; base < n_b; base += 32) {
+    int n_b = R.base + d.sc[d.rep_of[i]].n_b;
+    for (int base = R.base; base < n_b; base += 32) {
       int b = base + lane;
       bool inc = false;
       int j = -1;
       if (b < n_b) {
         j = d.b2hs[b];
-        if (j >= 0 && j != i) inc = list_entry_in(p, P, d.pos[j], false);
+        if (j >= 0 && j != i) inc = list_entry_in(p, R, P, d.pos[j], false);
       }
       unsigned bal = __ballot_sync(0xffffffffu, inc);
       int pre = __popc(bal & ((1u << lane) - 1u));
@@ -1417,36 +1513,40 @@ __device__ void gcmc_own_list(const Dev& d, const KParams& p, int i) {
     }
   }
   if (lane == 0) {
-    if (cnt > p.mnb) raise_error(d.sc, DML_E_NEIGH_OVERFLOW, i);
+    if (cnt > p.mnb) raise_error(d.g, DML_E_NEIGH_OVERFLOW, i);
     d.nn[i] = cnt > p.mnb ? p.mnb : cnt;
   }
 }
 
 __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
-  Scalars* sc = d.sc;
+  // one block per replica; its positions are [R.base, R.base + R.cap)
+  const int rep = blockIdx.x;
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  const int B = R.base;
   const int tid = threadIdx.x, nt = blockDim.x;
   __shared__ int s_min, s_max, s_cnt, s_sel, s_go;
   __shared__ int s_n;
-  const long long step = sc->step;
+  const long long step = d.g->step;
   const double z0 = sc->z0, zmax = sc->zmax;
-  const double v = p.box[0] * p.box[1] * (zmax - z0);
+  const double v = R.box[0] * R.box[1] * (zmax - z0);
   if (!sc->listed) {
-    if (tid == 0) raise_error(sc, DML_E_STATE, 0);
+    if (tid == 0) raise_error(d.g, DML_E_STATE, 0);
     return;
   }
-  if (p.use_cells)
-    for (int c = tid; c < d.ncell_tot; c += nt) d.ins_head[c] = -1;
+  if (R.use_cells)
+    for (int c = tid; c < R.ncell; c += nt) d.ins_head[R.cell_off + c] = -1;
   // order arrays grow by appends: compact them before they could overflow
-  if (sc->n_rank + p.nadj >= d.cap) {
-    int n = blk_compact(d.ref, sc->n_rank, d.rank);
+  if (sc->n_rank + p.nadj >= R.cap) {
+    int n = blk_compact(d.ref, B, sc->n_rank, d.rank);
     if (tid == 0) sc->n_rank = n;
   }
-  if (sc->n_alist + p.nadj >= d.cap) {
-    int n = blk_compact(d.alist, sc->n_alist, d.apos);
+  if (sc->n_alist + p.nadj >= R.cap) {
+    int n = blk_compact(d.alist, B, sc->n_alist, d.apos);
     if (tid == 0) sc->n_alist = n;
   }
-  if (sc->n_gorder + p.nadj >= d.cap) {
-    int n = blk_compact(d.gorder, sc->n_gorder, d.gpos);
+  if (sc->n_gorder + p.nadj >= R.cap) {
+    int n = blk_compact(d.gorder, B, sc->n_gorder, d.gpos);
     if (tid == 0) sc->n_gorder = n;
   }
   if (tid == 0) s_cnt = 0;
@@ -1454,7 +1554,7 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
   {
     int ng = sc->n_gorder, c = 0;
     for (int i = tid; i < ng; i += nt) {
-      int h = d.gorder[i];
+      int h = d.gorder[B + i];
       if (h < 0) continue;
       double z = d.pos[h].z;
       if (!(z < z0 || z > zmax)) ++c;
@@ -1473,34 +1573,34 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
     }
     __syncthreads();
     for (int i = tid; i < ng; i += nt)
-      if (d.gorder[i] >= 0) {
+      if (d.gorder[B + i] >= 0) {
         atomicMin(&s_min, i);
         atomicMax(&s_max, i);
       }
     __syncthreads();
     if (s_min == INT_MAX) {
-      if (tid == 0) raise_error(sc, DML_E_NO_PARTICLES, t);
+      if (tid == 0) raise_error(d.g, DML_E_NO_PARTICLES, t);
       return;
     }
-    const int href = d.gorder[s_min], hlast = d.gorder[s_max];
-    dml_u4 w0 = dml_draw(p.seed, step, (uint64_t)t, DML_RNG_GCMC, 0);
-    dml_u4 w1 = dml_draw(p.seed, step, (uint64_t)t, DML_RNG_GCMC, 1);
-    dml_u4 w2 = dml_draw(p.seed, step, (uint64_t)t, DML_RNG_GCMC, 2);
+    const int href = d.gorder[B + s_min], hlast = d.gorder[B + s_max];
+    dml_u4 w0 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 0);
+    dml_u4 w1 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 1);
+    dml_u4 w2 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 2);
     double coin = dml_u53(w0.w[0], w0.w[1]);
     double uacc = dml_u53(w0.w[2], w0.w[3]);
     if (coin < 0.5) {
       // creation attempt (dana.F90:627-677)
       if (p.act * v / (double)(n + 1) < uacc) continue;
-      double r0 = dml_u53(w1.w[0], w1.w[1]) * p.box[0];
-      double r1 = dml_u53(w1.w[2], w1.w[3]) * p.box[1];
+      double r0 = dml_u53(w1.w[0], w1.w[1]) * R.box[0];
+      double r1 = dml_u53(w1.w[2], w1.w[3]) * R.box[1];
       double r2 = dml_u53(w2.w[0], w2.w[1]) * (zmax - z0) + z0;
-      double4 R = make_double4(r0, r1, r2, 0.0);
+      double4 Rt = make_double4(r0, r1, r2, 0.0);
       bool ov = false;
       for (int i = tid; i < ng && !ov; i += nt) {
-        int h = d.gorder[i];
+        int h = d.gorder[B + i];
         if (h < 0) continue;
         double vx, vy, vz;  // distance(o%pos, r, o%pbc) = r - o%pos
-        vdist_nint(p, R, d.pos[h], vx, vy, vz);
+        vdist_nint(R, Rt, d.pos[h], vx, vy, vz);
         if (dot3(vx, vy, vz) < p.rc2) ov = true;
       }
       if (__syncthreads_or(ov)) continue;
@@ -1515,22 +1615,23 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
       __syncthreads();
       if (ns >= nat + sc->nlimbo)
         for (int i = tid; i < ns; i += nt)
-          if (d.state[i] == ST_NULL) atomicMin(&s_min, i);
+          if (d.state[B + i] == ST_NULL) atomicMin(&s_min, i);
       if (nb >= bnat)
         for (int b = tid; b < nb; b += nt)
-          if (d.b2hs[b] < 0) atomicMin(&s_sel, b);
+          if (d.b2hs[B + b] < 0) atomicMin(&s_sel, b);
       __syncthreads();
-      int slot = ns >= nat + sc->nlimbo ? s_min : ns;
-      int bs = nb >= bnat ? s_sel : nb;
-      if (slot == INT_MAX || bs == INT_MAX) {
-        if (tid == 0) raise_error(sc, DML_E_INDEX, t);
+      int lslot = ns >= nat + sc->nlimbo ? s_min : ns;   // local hs slot
+      int lbs = nb >= bnat ? s_sel : nb;                 // local hs%b slot
+      if (lslot == INT_MAX || lbs == INT_MAX) {
+        if (tid == 0) raise_error(d.g, DML_E_INDEX, t);
         return;
       }
-      if (slot >= d.cap || bs >= d.cap || sc->n_rank >= d.cap || sc->n_alist >= d.cap ||
-          sc->n_gorder >= d.cap) {
-        if (tid == 0) raise_error(sc, DML_E_CAPACITY, t);
+      if (lslot >= R.cap || lbs >= R.cap || sc->n_rank >= R.cap || sc->n_alist >= R.cap ||
+          sc->n_gorder >= R.cap) {
+        if (tid == 0) raise_error(d.g, DML_E_CAPACITY, t);
         return;
       }
+      const int slot = B + lslot, bs = B + lbs;
       __syncthreads();
       if (tid == 0) {
         // atom_asign(o, ref) then pos, pos_old = r (dana.F90:659-663)
@@ -1540,10 +1641,10 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
         d.acel[slot] = d.acel[href];
         d.epot[slot] = d.epot[href];
         d.typ[slot] = (int8_t)typ;
-        d.pos[slot] = R;
-        d.pos_old[slot] = R;
+        d.pos[slot] = Rt;
+        d.pos_old[slot] = Rt;
         d.old_cg[slot] = make_double4(1e8, 1e8, 1e8, 0.0);
-        d.posf[slot] = to_f4(R, typ);
+        d.posf[slot] = to_f4(Rt, typ);
         d.skip[slot] = 0;
         d.id[slot] = sc->next_id;
         sc->next_id += 1;
@@ -1551,44 +1652,44 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
         // Maxwell velocity to the last listed atom (dana.F90:666-668)
         double beta = sqrt(p.beta_num / p.mass[d.typ[href] - 1]);
         double nv[4];
-        dml_normal_quad(dml_draw(p.seed, step, (uint64_t)t, DML_RNG_GCMC_VEL, 0), nv);
+        dml_normal_quad(dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC_VEL, 0), nv);
         d.vel[hlast] = make_double4(beta * nv[0], beta * nv[1], beta * nv[2], 0.0);
         // sys
         int ap = sc->n_alist;
-        d.alist[ap] = slot;
-        d.apos[slot] = ap;
+        d.alist[B + ap] = slot;
+        d.apos[slot] = B + ap;
         sc->n_alist = ap + 1;
         // hs%ref
         int rk = sc->n_rank;
-        d.ref[rk] = slot;
-        d.rank[slot] = rk;
+        d.ref[B + rk] = slot;
+        d.rank[slot] = B + rk;
         sc->n_rank = rk + 1;
         sc->n_ref += 1;
         // hs%b (cgroup_attach_atom, Cells.F90:105-144)
         d.b2hs[bs] = slot;
         d.bslot[slot] = bs;
-        if (bs == nb) sc->n_b = nb + 1;
+        if (lbs == nb) sc->n_b = nb + 1;
         sc->b_nat = bnat;
-        if (p.use_cells) {
-          int c1 = cell_index(R.x, p.cell[0]), c2 = cell_index(R.y, p.cell[1]),
-              c3 = cell_index(R.z, p.cell[2]);
-          if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > p.ncells[0] + 1 || c2 > p.ncells[1] + 1 ||
-              c3 > p.ncells[2] + 1) {
-            raise_error(sc, DML_E_OUT_OF_TESSELLATION, slot);
+        if (R.use_cells) {
+          int c1 = cell_index(Rt.x, R.cell[0]), c2 = cell_index(Rt.y, R.cell[1]),
+              c3 = cell_index(Rt.z, R.cell[2]);
+          if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] + 1 || c2 > R.ncells[1] + 1 ||
+              c3 > R.ncells[2] + 1) {
+            raise_error(d.g, DML_E_OUT_OF_TESSELLATION, slot);
           } else {
-            int c = (c3 * p.head_dim[1] + c2) * p.head_dim[0] + c1;
+            int c = R.cell_off + (c3 * R.head_dim[1] + c2) * R.head_dim[0] + c1;
             d.ins_next[slot] = d.ins_head[c];
             d.ins_head[c] = slot;
           }
         }
         // hs (igroup slot)
         d.state[slot] = ST_LIVE;
-        if (slot == ns) sc->n_slots = ns + 1;
+        if (lslot == ns) sc->n_slots = ns + 1;
         sc->n_atoms = nat;
         // gcmc
         int gp = sc->n_gorder;
-        d.gorder[gp] = slot;
-        d.gpos[slot] = gp;
+        d.gorder[B + gp] = slot;
+        d.gpos[slot] = B + gp;
         d.in_gcmc[slot] = 1;
         sc->n_gorder = gp + 1;
         sc->n_gcmc += 1;
@@ -1596,17 +1697,17 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
       }
       __syncthreads();
       // ngroup_sort_atom: own list, then append to every hs%ref list within reach
-      if (tid < 32) gcmc_own_list(d, p, slot);
+      if (tid < 32) gcmc_own_list(d, p, R, slot);
       {
         int nr = sc->n_rank;
         double4 A = d.pos[slot];
         for (int q = tid; q < nr; q += nt) {
-          int j = d.ref[q];
+          int j = d.ref[B + q];
           if (j < 0 || j == slot) continue;
-          if (!list_entry_in(p, A, d.pos[j], false)) continue;
+          if (!list_entry_in(p, R, A, d.pos[j], false)) continue;
           int m = d.nn[j];
           if (m >= p.mnb) {
-            raise_error(sc, DML_E_NEIGH_OVERFLOW, j);
+            raise_error(d.g, DML_E_NEIGH_OVERFLOW, j);
             continue;
           }
           d.list[(size_t)j * p.mnb + m] = slot;
@@ -1632,7 +1733,7 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
         __syncthreads();
         for (int base = 0; base < ng && s_go; base += nt) {
           int i = base + tid;
-          int h = i < ng ? d.gorder[i] : -1;
+          int h = i < ng ? d.gorder[B + i] : -1;
           bool in = false;
           if (h >= 0) {
             double z = d.pos[h].z;
@@ -1650,7 +1751,7 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
         }
         hsel = s_sel;
         if (hsel < 0) {
-          if (tid == 0) raise_error(sc, DML_E_CHOSEN_MISSING, t);
+          if (tid == 0) raise_error(d.g, DML_E_CHOSEN_MISSING, t);
           return;
         }
       }
@@ -1668,12 +1769,12 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
           d.rank[h] = -1;
           sc->n_ref -= 1;
         }
-        if (p.use_cells) {
+        if (R.use_cells) {
           double4 P = d.pos[h];
-          int c1 = cell_index(P.x, p.cell[0]), c2 = cell_index(P.y, p.cell[1]),
-              c3 = cell_index(P.z, p.cell[2]);
-          if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > p.ncells[0] || c2 > p.ncells[1] || c3 > p.ncells[2])
-            raise_error(sc, DML_E_UNSUPPORTED, h);  // tessellation dropped (Cells.F90:320-327)
+          int c1 = cell_index(P.x, R.cell[0]), c2 = cell_index(P.y, R.cell[1]),
+              c3 = cell_index(P.z, R.cell[2]);
+          if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] || c2 > R.ncells[1] || c3 > R.ncells[2])
+            raise_error(d.g, DML_E_UNSUPPORTED, h);  // tessellation dropped (Cells.F90:320-327)
         }
         d.b2hs[d.bslot[h]] = -1;
         d.bslot[h] = -1;
@@ -1705,7 +1806,7 @@ __global__ void flush_kernel(uint4* buf, size_t n) {
 }  // namespace
 
 int k_step_begin(const Dev& d, cudaStream_t s) {
-  step_begin_kernel<<<1, 1, 0, s>>>(d.sc);
+  step_begin_kernel<<<1, 1, 0, s>>>(d.g);
   return 1;
 }
 
@@ -1764,17 +1865,18 @@ int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, 
   int nmax = n_slots > n_b ? n_slots : n_b;
   rebuild_prep_kernel<<<nblk(nmax), kBlock, 0, s>>>(d, p, n_slots, n_b, 0);
   int n = 1;
-  if (p.use_cells) {
+  if (d.any_cells) {
     cell_scan_kernel<<<1, 1024, 0, s>>>(d, d.ncell_tot, 0);
     cell_scatter_kernel<<<nblk(n_b), kBlock, 0, s>>>(d, n_b, 0);
     cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot, 0);
     list_cells_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
     n += 4;
-  } else {
+  }
+  if (d.any_verlet) {
     list_verlet_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank, n_b);
     n += 1;
   }
-  rebuild_done_kernel<<<1, 1, 0, s>>>(d);
+  rebuild_done_kernel<<<nblk(d.nrep), kBlock, 0, s>>>(d);
   return n + 1;
 }
 
@@ -1809,14 +1911,14 @@ int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
 
 int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
   int n = 0;
-  if (p.use_cells) {
+  if (d.any_cells) {
     rebuild_prep_kernel<<<nblk(cap), kBlock, 0, s>>>(d, p, cap, cap, 1);
     cell_scan_kernel<<<1, 1024, 0, s>>>(d, d.ncell_tot, 1);
     cell_scatter_kernel<<<nblk(cap), kBlock, 0, s>>>(d, cap, 1);
     cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot, 1);
     n += 4;
   }
-  gcmc_kernel<<<1, 1024, 0, s>>>(d, p);
+  gcmc_kernel<<<d.nrep, 1024, 0, s>>>(d, p);
   return n + 1;
 }
 

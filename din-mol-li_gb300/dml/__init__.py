@@ -53,6 +53,12 @@ def lib():
     L.dml_params_default.argtypes = [P(_abi.Params)]
     L.dml_params_default.restype = None
     L.dml_create.argtypes = [P(_abi.Params), P(vp)]
+    L.dml_create_batch.argtypes = [P(_abi.Params), i32, P(_abi.Replica), P(vp)]
+    L.dml_set_atoms_batch.argtypes = [vp, P(_abi.Atoms)]
+    L.dml_num_replicas.argtypes = [vp]
+    L.dml_get_atoms_replica.argtypes = [vp, i32, P(_abi.Atoms)]
+    L.dml_get_counters_replica.argtypes = [vp, i32, P(_abi.Counters)]
+    L.dml_get_neighbors_replica.argtypes = [vp, i32, P(i32), vp, vp, i32]
     L.dml_destroy.argtypes = [vp]
     L.dml_destroy.restype = None
     L.dml_set_atoms.argtypes = [vp, P(_abi.Atoms)]
@@ -117,16 +123,30 @@ def slab_system(nx, ny, nz_slab, box_z, n_ion, zlo, zhi, seed, a=3.51, dmin=2.5)
 
 
 class Simulation:
-    """One device context (dml_ctx); methods mirror the reference routines."""
+    """One device context (dml_ctx); methods mirror the reference routines.
 
-    def __init__(self, params):
+    With `replicas` (a list of `Replica`, see `replica_of`) the context runs
+    that many independent systems in every launch (dml_create_batch);
+    `set_atoms` then takes one array dict per replica and the per-replica
+    getters take `replica=`.
+    """
+
+    def __init__(self, params, replicas=None):
         self.lib = lib()
         self.params = params
         h = ctypes.c_void_p()
-        rc = self.lib.dml_create(ctypes.byref(params), ctypes.byref(h))
+        if replicas is None:
+            self.n_rep = 1
+            rc = self.lib.dml_create(ctypes.byref(params), ctypes.byref(h))
+        else:
+            self.n_rep = len(replicas)
+            arr = (_abi.Replica * self.n_rep)(*replicas)
+            rc = self.lib.dml_create_batch(ctypes.byref(params), self.n_rep, arr,
+                                           ctypes.byref(h))
         if rc != 0:
             raise DmlError(rc, "dml_create")
         self.h = h
+        self.batched = replicas is not None
 
     def close(self):
         if getattr(self, "h", None):
@@ -147,9 +167,16 @@ class Simulation:
             raise DmlError(rc, "%s: %s" % (what, self.lib.dml_last_error(self.h).decode()))
 
     def set_atoms(self, arrays):
-        n = len(arrays["z"])
-        a = _abi.atoms_struct(dict(arrays), n)
-        self._check(self.lib.dml_set_atoms(self.h, ctypes.byref(a)), "dml_set_atoms")
+        if not self.batched:
+            n = len(arrays["z"])
+            a = _abi.atoms_struct(dict(arrays), n)
+            self._check(self.lib.dml_set_atoms(self.h, ctypes.byref(a)), "dml_set_atoms")
+            return
+        if len(arrays) != self.n_rep:
+            raise ValueError("set_atoms: one array dict per replica")
+        keep = [dict(x) for x in arrays]
+        structs = (_abi.Atoms * self.n_rep)(*[_abi.atoms_struct(x, len(x["z"])) for x in keep])
+        self._check(self.lib.dml_set_atoms_batch(self.h, structs), "dml_set_atoms_batch")
 
     def setup(self):
         self._check(self.lib.dml_setup(self.h), "dml_setup")
@@ -202,18 +229,32 @@ class Simulation:
     def reset_counters(self):
         self._check(self.lib.dml_reset_counters(self.h), "dml_reset_counters")
 
-    def counters(self):
+    def counters(self, replica=None):
+        """Counters of one replica, or (replica=None) summed over replicas."""
         c = _abi.Counters()
-        self._check(self.lib.dml_get_counters(self.h, ctypes.byref(c)), "dml_get_counters")
+        if replica is None:
+            self._check(self.lib.dml_get_counters(self.h, ctypes.byref(c)), "dml_get_counters")
+        else:
+            self._check(self.lib.dml_get_counters_replica(self.h, replica, ctypes.byref(c)),
+                        "dml_get_counters_replica")
         return c.as_dict()
 
-    def get_atoms(self, n=None):
+    def get_atoms(self, n=None, replica=None):
+        if replica is None and self.batched:
+            replica = 0 if self.n_rep == 1 else None
+            if replica is None:
+                raise ValueError("get_atoms: pass replica= on a batch context")
         if n is None:
-            n = self.counters()["n_atoms"]
+            n = self.counters(replica)["n_atoms"]
         out = _abi.empty_atoms(n)
         a = _abi.atoms_struct(out, n)
-        self._check(self.lib.dml_get_atoms(self.h, ctypes.byref(a)), "dml_get_atoms")
-        return out
+        if replica is None:
+            self._check(self.lib.dml_get_atoms(self.h, ctypes.byref(a)), "dml_get_atoms")
+        else:
+            self._check(self.lib.dml_get_atoms_replica(self.h, replica, ctypes.byref(a)),
+                        "dml_get_atoms_replica")
+        n = a.n
+        return {k: v[:n] for k, v in out.items()}
 
     def time_steps(self, n, flush_l2=True):
         """Device time [ms] of n steps, each bracketed by CUDA events."""
@@ -240,11 +281,16 @@ class Simulation:
             raise DmlError(-n, "dml_launches_per_step")
         return n, r.value
 
-    def get_neighbors(self, ld):
-        n_ref = self.counters()["n_ref"]
+    def get_neighbors(self, ld, replica=None):
+        n_ref = self.counters(replica)["n_ref"]
         nn = np.zeros(max(n_ref, 1), np.int32)
         lst = np.zeros((max(n_ref, 1), ld), np.int32)
         nr = ctypes.c_int32()
-        self._check(self.lib.dml_get_neighbors(self.h, ctypes.byref(nr), nn.ctypes.data,
-                                               lst.ctypes.data, ld), "dml_get_neighbors")
+        if replica is None:
+            rc = self.lib.dml_get_neighbors(self.h, ctypes.byref(nr), nn.ctypes.data,
+                                            lst.ctypes.data, ld)
+        else:
+            rc = self.lib.dml_get_neighbors_replica(self.h, replica, ctypes.byref(nr),
+                                                    nn.ctypes.data, lst.ctypes.data, ld)
+        self._check(rc, "dml_get_neighbors")
         return nn[: nr.value], lst[: nr.value]

@@ -34,6 +34,28 @@ Z_LI, Z_CG, Z_F = 1, 2, 3
 _d33 = (ctypes.c_double * 3) * 3
 
 
+class Replica(ctypes.Structure):
+    """struct dml_replica: the per-replica values of a batch context."""
+    _fields_ = [
+        ("box", ctypes.c_double * 3),
+        ("z0", ctypes.c_double),
+        ("zmax", ctypes.c_double),
+        ("z1", ctypes.c_double),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+def replica_of(params, **kw):
+    """A Replica with params' box, z0, zmax, z1, seed, overridden by kw."""
+    r = Replica()
+    r.box[:] = list(kw.get("box", params.box))
+    r.z0 = kw.get("z0", params.z0)
+    r.zmax = kw.get("zmax", params.zmax)
+    r.z1 = kw.get("z1", params.z1)
+    r.seed = kw.get("seed", params.seed)
+    return r
+
+
 class Params(ctypes.Structure):
     _fields_ = [
         ("box", ctypes.c_double * 3),

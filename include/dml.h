@@ -150,6 +150,32 @@ int dml_create(const dml_params* p, dml_ctx** out);
  * attach loop :130-137).  Marks the neighbour list as not built. */
 int dml_set_atoms(dml_ctx* c, const dml_atoms* a);
 
+/* Independent replicas in one context (no counterpart in the reference,
+ * which runs one system per process; each replica is one `dana` run).
+ * Every replica has its own box, electrode plane z0, piston zmax, chunk
+ * plane z1 and random seed; all share the remaining dml_params (potential,
+ * integrator, reservoir, capacity per replica).  Every kernel of a step
+ * covers all replicas in one launch: a replica owns a block-aligned range
+ * of atom slots and its own cells, lists and counters, and the results of
+ * each replica are bit-identical to a one-replica context with the same
+ * replica values (the Philox key carries the replica's seed).
+ * dml_create is dml_create_batch with one replica taken from p. */
+typedef struct dml_replica {
+  double box[3];
+  double z0, zmax, z1;
+  uint64_t seed;
+} dml_replica;
+
+int dml_create_batch(const dml_params* p, int32_t n_rep, const dml_replica* reps,
+                     dml_ctx** out);
+
+/* Loads atoms[r] into replica r for r in [0, n_rep).  dml_set_atoms is the
+ * one-replica form and fails with DML_E_ARG on a context of several. */
+int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms);
+
+/* Replica count of a context, or -status. */
+int dml_num_replicas(dml_ctx* c);
+
 /* set_ermak (src/dana.F90:947-971) + test_update (:140) + fuerza (:142) +
  * calc_rho (:145, sets rho0): the start-up sequence before the step loop. */
 int dml_setup(dml_ctx* c);
@@ -251,7 +277,17 @@ int dml_get_atoms(dml_ctx* c, dml_atoms* a);
  * Limbo entries are written as -1.  n_ref is set to the member count. */
 int dml_get_neighbors(dml_ctx* c, int32_t* n_ref, int32_t* nn, int32_t* list, int32_t ld);
 
+/* Counters of one replica.  dml_get_counters sums the event counters and
+ * atom counts over replicas and reports replica 0's zmax, z0, rho, rho0
+ * (max_nn and passes as maxima). */
 int dml_get_counters(dml_ctx* c, dml_counters* out);
+int dml_get_counters_replica(dml_ctx* c, int32_t rep, dml_counters* out);
+
+/* One replica's atoms and neighbour lists (same layout as dml_get_atoms and
+ * dml_get_neighbors, which take a one-replica context). */
+int dml_get_atoms_replica(dml_ctx* c, int32_t rep, dml_atoms* a);
+int dml_get_neighbors_replica(dml_ctx* c, int32_t rep, int32_t* n_ref, int32_t* nn,
+                              int32_t* list, int32_t ld);
 
 /* Resets try and depo (salida, src/dana.F90:1171-1174). */
 int dml_reset_counters(dml_ctx* c);
