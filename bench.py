@@ -1,24 +1,32 @@
 #!/usr/bin/env python3
 """Benchmark of din-mol-Li's per-step hot path on GB300.
 
-Workload (config 2 of the benchmark set): a 351 x 351 x 320 Å box, a frozen
-bcc Li electrode of 100 x 100 x 4 cells (80 000 atoms) and 200 000 mobile
-Li+ ions placed uniformly in z in [15, 300) Å with 2.5 Å minimum separation
-(seeded synthetic data: the reference measures no dataset).  Ermak
-integrator, dt = 1 fs, piston reservoir with z0 = 160 Å, skin 10 Å.  A step
-is one iteration of the reference's loop body (src/dana.F90:173-265):
-ermak_a, fuerza, ermak_b, test_update, overlap_moveback, test_update,
-capture commit, calc_rho, maxz -- all on the device, plain FP64 form,
-bit-exact to the oracle.
+A step is one iteration of the reference's loop body (src/dana.F90:173-265):
+ermak_a, fuerza, ermak_b, test_update, overlap_moveback, test_update, capture
+commit, gcmc_run, calc_rho (and maxz with the piston), all on the device.
+
+Workloads (seeded synthetic systems; the reference measures no dataset):
+
+  c5 (default)  config 5: a batch of independent replicas, each a 40 x 40 x
+                2-cell bcc Li electrode (6400 atoms, 140.4 Å square) under
+                20 000 Li+ in a 300 Å box, GCMC reservoir slab z in [200, 300]
+                with 128 trials per step, Ermak, dt = 1 fs, skin 10 Å.  Timed
+                in the chosen form (mixed precision, all replicas in every
+                launch); the same batch in plain FP64 and a sample of replicas
+                run one per context in plain FP64 are timed beside it.
+  c2            config 2: one 351 x 351 x 320 Å system, 80 000 electrode atoms
+                and 200 000 Li+, piston reservoir, Ermak, plain FP64 (the form
+                bit-exact to the oracle).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload c5|c2] [--replicas R] [--form chosen|plain]
 
 Prints one JSON line.  `value` = mobile-ion steps per second over all ranks
-(device time, inputs resident, L2 flushed between steps).  `e2e` = the same
-metric through the C ABI with host arrays: upload, setup, K steps with a
-positions download every 100 steps (the reference's output cadence) and the
-final download, wall clock.  `--impl reference` times the CPU restatement of
-the reference (oracle/) on this host; rank 0 only.
+(device time with CUDA events, inputs resident, L2 flushed between steps).
+`e2e` = the same metric through the C ABI with host arrays: upload, setup, K
+steps with a download of every replica's positions every 100 steps (the
+reference's output cadence), wall clock.  `--impl reference` times the CPU
+restatement of the reference (oracle/) on this host; rank 0 only.
 """
 import argparse
 import json
@@ -35,20 +43,19 @@ for _p in (ROOT, PKG):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
-METRIC = "particle-steps/s on 1 GB300: mixed+batched vs plain FP64 at force err ≤1e-6"
+METRIC = "particle-steps/s on 1 GB300: mixed+batched vs plain FP64 at force err \u22641e-6"
 UNIT = "particle-steps/s"
-N_ION, N_CG = 200000, 80000
 NWR = 100  # output cadence of the reference's tests (entrada.ini nwr)
 
 # Algorithmic bytes per mobile ion and step, FP64 state touched once
 # (integrate: read pos, vel, acel, write pos, old_cg = 120 B; force + ermak_b:
 # read pos 24, vel, acel, element 49, write vel, acel 48, epot 8 = 129 B);
-# list-scanning phases add the 4-byte list entries they must read.
+# list-scanning phases add the 4-byte list entries they must read; gcmc reads
+# one position per gcmc member per trial.
 PHASE_BYTES_PER_ION = {"integrate": 120.0, "force_pairs": 24.0, "force_sum": 105.0,
                        "test_update1": 48.0, "overlap": 48.0, "test_update2": 48.0,
-                       "commit": 1.0, "rho_piston": 48.0}
+                       "commit": 1.0, "gcmc": 0.0, "rho_piston": 48.0}
 LIST_PHASES = ("force_pairs", "overlap")
-
 
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -162,21 +169,151 @@ def ncu_traffic(kernel_phase):
         return None
 
 
-def make_system(seed):
+class Workload:
+    """One benchmark system: parameters, per-replica values and atoms."""
+
+    def __init__(self, name, rank, n_rep):
+        import dml
+        from tests import systems
+
+        self.name = name
+        if name == "c5":
+            self.batched = True
+            self.p, self.reps, self.atoms = systems.c5_batch(n_rep, seed=11 + 1000 * rank)
+            self.n_electrode = 2 * systems.C5_CELLS ** 2 * 2 * n_rep
+            self.desc = ("config 5: %d replicas x (40x40x2-cell bcc Li electrode, 6400 atoms, "
+                         "+ 20000 Li+), 140.4x140.4x300 A, GCMC reservoir z in [200,300] with "
+                         "%d trials/step, Ermak dt=1fs, skin 10" % (n_rep, self.p.nadj))
+        elif name == "c2":
+            self.batched = False
+            self.p = systems.c2_params(seed=1234 + rank)
+            self.reps = None
+            self.atoms = [systems.c2_atoms(seed=7 + rank)]
+            self.n_electrode = 80000
+            self.desc = ("config 2: 200k Li+ over an 80k-atom bcc Li electrode, 351x351x320 A, "
+                         "Ermak dt=1fs, piston z0=160, skin 10")
+        else:
+            raise ValueError(name)
+        self.n_rep = len(self.atoms)
+        self.n_ion = sum(int((a["z"] != dml.Z_CG).sum()) for a in self.atoms)
+
+    def params(self, precision):
+        import ctypes
+
+        import dml
+
+        q = dml.Params()
+        ctypes.memmove(ctypes.byref(q), ctypes.byref(self.p), ctypes.sizeof(q))
+        q.precision = precision
+        return q
+
+    def replica_params(self, r, precision):
+        """Parameters of replica r alone (its box, planes and seed)."""
+        p = self.params(precision)
+        if self.batched:
+            q = self.reps[r]
+            p.box[:] = list(q.box)
+            p.z0, p.zmax, p.z1, p.seed = q.z0, q.zmax, q.z1, q.seed
+        return p
+
+    def open(self, precision, replicas=None):
+        """A loaded context (all replicas, or the listed ones one by one)."""
+        import dml
+
+        p = self.params(precision)
+        if not self.batched:
+            sim = dml.Simulation(p)
+            sim.set_atoms(self.atoms[0])
+            return sim
+        idx = list(range(self.n_rep)) if replicas is None else replicas
+        if len(idx) == 1:
+            sim = dml.Simulation(self.replica_params(idx[0], precision))
+            sim.set_atoms(self.atoms[idx[0]])
+            return sim
+        sim = dml.Simulation(p, replicas=[self.reps[i] for i in idx])
+        sim.set_atoms([self.atoms[i] for i in idx])
+        return sim
+
+
+def timed_steps(sim, args, clocks=None):
+    """W untimed steps, then K steps each bracketed by CUDA events (after setup)."""
+    sim.step(args.warmup)
+    c0 = sim.counters()
+    if clocks:
+        clocks.start()
+    ms = sim.time_steps(args.steps, flush_l2=True)
+    clk = clocks.stop() if clocks else None
+    c1 = sim.counters()
+    return ms, c0, c1, clk
+
+
+def force_error_probe(wl, nrep=4, steps=20):
+    """Mixed vs FP64 forces on identical positions: replica r runs `steps`
+    plain steps, then its state is loaded into one context of each form and
+    both run test_update, ermak_a (FP64 in both forms, so the positions stay
+    identical) and fuerza.  Relative error per mobile ion: |F_mixed - F_fp64|
+    / max(|F_fp64|, F_rms), F_rms the RMS force of the ions that interact
+    (ions with no pair inside r0 have exactly zero force in both forms); also
+    the absolute error and the relative error of the total energy."""
+    import numpy as np
+
     import dml
-    from tests import systems
 
-    p = systems.c2_params(seed=1234 + seed)
-    atoms = systems.c2_atoms(seed=7 + seed)
-    return p, atoms
+    EV = 96.485 * 100.0  # ui per eV (dana.F90:23)
+    rel, rel_all, absd, emix, epl, inter = [], [], [], 0.0, 0.0, 0
+    for r in range(min(nrep, wl.n_rep)):
+        sp = wl.open(dml.PRECISION_FP64, replicas=[r])
+        sp.setup()
+        sp.step(steps)
+        st = sp.get_atoms(replica=0) if wl.batched else sp.get_atoms()
+        stepno = sp.counters()["step"] + 1
+        sp.close()
+        out = []
+        for prec in (dml.PRECISION_MIXED, dml.PRECISION_FP64):
+            s = dml.Simulation(wl.replica_params(r, prec))
+            s.set_atoms(st)
+            s.test_update()
+            s.ermak_a(stepno)
+            s.fuerza()
+            a = s.get_atoms()
+            out.append((a["force"], a["epot"], a["z"]))
+            s.close()
+        (fm, em, z), (fp, ep, _) = out
+        mob = z != dml.Z_CG
+        fr = np.sqrt((fp[mob] ** 2).sum(1))
+        d = np.sqrt(((fm[mob] - fp[mob]) ** 2).sum(1))
+        hit = fr > 0
+        inter += int(hit.sum())
+        absd.append(d)
+        if hit.any():
+            frms = float(np.sqrt((fr[hit] ** 2).mean()))
+            rel.append(d / np.maximum(fr, frms))
+            rel_all.append(d / np.maximum(fr, float(np.sqrt((fr ** 2).mean()))))
+        emix += float(em.sum())
+        epl += float(ep.sum())
+    e = np.concatenate(rel) if rel else np.zeros(1)
+    ea = np.concatenate(rel_all) if rel_all else np.zeros(1)
+    return {"max_rel": float(e.max()), "rms_rel": float(np.sqrt((e ** 2).mean())),
+            "max_rel_floor_all_ions": float(ea.max()),
+            "max_abs_ev_per_A": float(np.concatenate(absd).max() / EV) if absd else 0.0,
+            "energy_rel": float(abs(emix - epl) / abs(epl)) if epl else 0.0,
+            "interacting_ions": inter, "replicas": min(nrep, wl.n_rep),
+            "state": "after %d FP64 steps, then ermak_a + fuerza in both forms" % steps,
+            "tolerance": 1e-6, "within": bool(e.max() <= 1e-6)}
 
 
-def cpu_baseline_sample(p, atoms, budget_s=12.0, max_steps=200):
-    """Oracle (serial CPU restatement) on the same system: steps after setup."""
+def cpu_baseline_sample(wl, budget_s=12.0, max_steps=200):
+    """Oracle (serial CPU restatement) on replica 0 of the workload, plain FP64."""
+    import dml
     from tests import oracle_lib
 
+    p = wl.params(dml.PRECISION_FP64)
+    if wl.batched:
+        r = wl.reps[0]
+        p.box[:] = list(r.box)
+        p.z0, p.zmax, p.z1, p.seed = r.z0, r.zmax, r.z1, r.seed
     o = oracle_lib.Oracle(p)
-    o.set_atoms(atoms)
+    o.set_atoms(wl.atoms[0])
     o.setup()
     n_ion0 = o.counters()["n_ref"]
     t0 = time.perf_counter()
@@ -192,29 +329,18 @@ def cpu_baseline_sample(p, atoms, budget_s=12.0, max_steps=200):
 
 
 def run_reference(args, ws, rank):
+    """The oracle timed on this host: replica 0 of the workload."""
     if rank != 0:
         return 0
-    p, atoms = make_system(0)
-    from tests import oracle_lib
-
-    o = oracle_lib.Oracle(p)
-    o.set_atoms(atoms)
-    o.setup()
-    o.step(min(args.warmup, 3))
+    wl = Workload(args.workload, 0, args.replicas)
     k = min(args.steps, 60)
-    n0 = o.counters()["n_ref"]
-    t0 = time.perf_counter()
-    o.step(k)
-    dt = time.perf_counter() - t0
-    n1 = o.counters()["n_ref"]
-    v = 0.5 * (n0 + n1) * k / dt
-    sample = "config 2 system (80k electrode + 200k ions), %d timed steps after setup" % k
+    v, steps, dt = cpu_baseline_sample(wl, budget_s=60.0, max_steps=k)
+    sample = ("%s; oracle on one replica (%d atoms), %d timed steps after setup"
+              % (wl.desc, len(wl.atoms[0]["z"]), steps))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
-            "steps": k, "warmup": min(args.warmup, 3), "ms_per_step": 1e3 * dt / k,
+            "steps": steps, "warmup": 0, "ms_per_step": 1e3 * dt / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": "config 2: 200k Li+ over an 80k-atom bcc Li electrode, Ermak, "
-                                   "piston", "n_ion": N_ION, "n_electrode": N_CG},
+            "data": "synthetic", "config": {"workload": wl.desc, "form": "plain FP64 (CPU)"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -222,40 +348,14 @@ def run_reference(args, ws, rank):
     return 0
 
 
-def run_gpu(args, ws, rank, local):
-    import numpy as np
-
-    import dml
-
-    dml.build()
-    dist = Dist(ws)
-    p, atoms = make_system(rank)
-    sim = dml.Simulation(p)
-    sim.set_atoms(atoms)
-    sim.setup()
-    sim.step(args.warmup)
-    n_ion0 = sim.counters()["n_ref"]
-    clocks = Clocks(local)
-    dist.barrier()
-    clocks.start()
-    nupd0 = sim.counters()["nupd"]
-    ms = sim.time_steps(args.steps, flush_l2=True)
-    clk = clocks.stop()
-    dist.barrier()
-    c = sim.counters()
-    n_ion = 0.5 * (n_ion0 + c["n_ref"])
-    ms_max = dist.reduce(ms, "max")
-    ions_all = dist.reduce(n_ion, "sum")
-    value = ions_all * args.steps / (ms_max / 1e3)
-    per_step, per_rebuild = sim.launches_per_step()
-    launches = per_step * args.steps + per_rebuild * (c["nupd"] - nupd0)
-
-    # Per-phase device times (same work, un-graphed) for the roofline.
-    nprof = max(3, min(args.steps, 20))
+def roofline_of(sim, wl, nprof):
+    """Dominant phase of un-graphed steps: algorithmic bytes / event time."""
     ph = sim.profile_steps(nprof, flush_l2=True)
+    c = sim.counters()
+    n_ion = c["n_ref"]
     nn_mean = None
     try:
-        nn, _ = sim.get_neighbors(p.mnb)
+        nn, _ = sim.get_neighbors(sim.params.mnb, replica=0 if wl.batched else None)
         nn_mean = float(nn.mean())
     except Exception:  # noqa: BLE001
         pass
@@ -264,56 +364,120 @@ def run_gpu(args, ws, rank, local):
     byts = PHASE_BYTES_PER_ION[dom] * n_ion
     if dom in LIST_PHASES and nn_mean:
         byts += 4.0 * nn_mean * n_ion
+    if dom == "gcmc":
+        byts = sim.params.nadj * 24.0 * n_ion
     peak, peak_kind = measured_peaks()
     achieved = byts / t_launch / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": ncu_traffic(dom), "kernel_phase": dom,
-                "peak_source": peak_kind,
-                "phase_ms_per_step": {k: v / nprof for k, v in ph.items()}}
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": ncu_traffic(wl.name + ":" + dom),
+            "kernel_phase": dom, "peak_source": peak_kind, "bytes_per_step": byts,
+            "phase_ms_per_step": {k: v / nprof for k, v in ph.items()}}
+
+
+def run_gpu(args, ws, rank, local):
+    import dml
+
+    dml.build()
+    dist = Dist(ws)
+    wl = Workload(args.workload, rank, args.replicas)
+    form = args.form or ("chosen" if wl.batched else "plain")
+    prec = dml.PRECISION_MIXED if form == "chosen" else dml.PRECISION_FP64
+    clocks = Clocks(local)
+
+    # Main arm: the whole workload in one context.
+    sim = wl.open(prec)
+    sim.setup()
+    dist.barrier()
+    ms, c0, c1, clk = timed_steps(sim, args, clocks)
+    dist.barrier()
+    n_ion = 0.5 * (c0["n_ref"] + c1["n_ref"])
+    ms_max = dist.reduce(ms, "max")
+    ions_all = dist.reduce(n_ion, "sum")
+    value = ions_all * args.steps / (ms_max / 1e3)
+    per_step, per_rebuild = sim.launches_per_step()
+    launches = per_step * args.steps + per_rebuild * (c1["list_builds"] - c0["list_builds"])
+    roofline = roofline_of(sim, wl, max(3, min(args.steps, 10)))
+    counters = {k: c1[k] - c0[k] for k in ("choques", "depo", "try_", "choques3", "gcmc_ins",
+                                           "gcmc_del", "list_builds")}
+    counters["n_ref"] = c1["n_ref"]
     sim.close()
+
+    # Comparison arms (chosen form only): the same batch in plain FP64, and
+    # replicas run one per context in plain FP64 (the reference's way: one
+    # system per run).
+    compare = None
+    if form == "chosen" and not args.no_compare:
+        compare = {}
+        compare["force_error"] = force_error_probe(wl)
+        sp = wl.open(dml.PRECISION_FP64)
+        sp.setup()
+        ms_p, p0, p1, _ = timed_steps(sp, args)
+        np_ion = 0.5 * (p0["n_ref"] + p1["n_ref"])
+        compare["plain_fp64_batched"] = {"value": np_ion * args.steps / (ms_p / 1e3),
+                                         "ms_per_step": ms_p / args.steps,
+                                         "depo": p1["depo"] - p0["depo"]}
+        sp.close()
+        tot_ion_steps, tot_s = 0.0, 0.0
+        nsolo = min(wl.n_rep, 4)
+        for r in range(nsolo):
+            s1 = wl.open(dml.PRECISION_FP64, replicas=[r])
+            s1.setup()
+            ms_1, q0, q1, _ = timed_steps(s1, args)
+            tot_ion_steps += 0.5 * (q0["n_ref"] + q1["n_ref"]) * args.steps
+            tot_s += ms_1 / 1e3
+            s1.close()
+        solo = tot_ion_steps / tot_s
+        compare["plain_fp64_one_replica_per_context"] = {
+            "value": solo, "replicas_timed": nsolo,
+            "ms_per_step_per_replica": 1e3 * tot_s / nsolo / args.steps}
+        compare["speedup_vs_plain_one_per_context"] = value / dist.reduce(solo, "sum") * 1.0
+        compare["speedup_vs_plain_batched"] = value / compare["plain_fp64_batched"]["value"]
 
     # End to end through the C ABI with host buffers.
     e2e = None
     if rank == 0 and not args.no_e2e:
-        pos_bytes = atoms["pos"].nbytes + atoms["z"].nbytes
+        h2d = sum(a["pos"].nbytes + a["z"].nbytes for a in wl.atoms)
         t0 = time.perf_counter()
-        s2 = dml.Simulation(p)
-        s2.set_atoms(atoms)
+        s2 = wl.open(prec)
         s2.setup()
         done, d2h = 0, 0
-        n_atoms = len(atoms["z"])
         while done < args.steps:
             k = min(NWR, args.steps - done)
             s2.step(k)
             done += k
-            out = s2.get_atoms(n_atoms)
-            d2h += out["pos"].nbytes + out["z"].nbytes
+            for r in range(wl.n_rep):
+                out = s2.get_atoms(replica=r) if wl.batched else s2.get_atoms()
+                d2h += out["pos"].nbytes + out["z"].nbytes
         t1 = time.perf_counter()
         s2.close()
         e2e = {"value": n_ion * args.steps / (t1 - t0), "unit": UNIT,
-               "h2d_bytes_per_step": pos_bytes / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
                "wall_s": t1 - t0}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        v, k, dt = cpu_baseline_sample(p, atoms)
+        v, k, dt = cpu_baseline_sample(wl)
         cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": "oracle (serial C++ restatement) on the same system: %d steps after "
-                         "setup in %.1f s" % (k, dt)}
+               "sample": "oracle (serial C++ restatement, plain FP64) on replica 0 of the same "
+                         "workload (%d atoms): %d steps after setup in %.1f s"
+                         % (len(wl.atoms[0]["z"]), k, dt)}
     dist.close()
     if rank != 0:
         return 0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "config 2: 200k Li+ over an 80k-atom bcc Li electrode, "
-                                   "351x351x320 A, Ermak dt=1fs, piston z0=160, skin 10",
-                       "form": "plain FP64 (bit-exact to the oracle)", "n_ion": N_ION,
-                       "n_electrode": N_CG, "parallelism": "replicas" if ws > 1 else "single",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 pair forces, int64 fixed-point sums, f64 integration" if form == "chosen"
+            else "f64",
+            "data": "synthetic",
+            "config": {"workload": wl.desc,
+                       "form": ("chosen: mixed precision, %d replicas in every launch" % wl.n_rep)
+                       if form == "chosen" else "plain FP64 (bit-exact to the oracle)",
+                       "replicas": wl.n_rep, "n_ion": wl.n_ion, "n_electrode": wl.n_electrode,
+                       "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "flushed between steps (256 MiB write outside the timed events)"},
             "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-            "cpu_baseline": cpu, "counters": {k: c[k] for k in ("nupd", "choques", "depo", "try_",
-                                                                 "choques3", "n_ref")}}
+            "cpu_baseline": cpu, "compare": compare, "counters": counters}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -324,8 +488,12 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c5", choices=["c5", "c2"])
+    ap.add_argument("--replicas", type=int, default=256)
+    ap.add_argument("--form", default=None, choices=["chosen", "plain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-compare", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

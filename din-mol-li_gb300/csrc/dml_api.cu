@@ -87,6 +87,7 @@ void make_repconst(const dml_params& P, const dml_replica& r, RepConst& R) {
   for (int k = 0; k < 3; ++k) {
     if (R.ncells[k] < 1) R.ncells[k] = 1;
     R.cell[k] = r.box[k] / (double)R.ncells[k];
+    R.inv_cellf[k] = (float)(1.0 / R.cell[k]);
     R.head_dim[k] = R.ncells[k] + 2;
   }
   R.ncell = R.use_cells ? R.head_dim[0] * R.head_dim[1] * R.head_dim[2] : 0;
@@ -116,9 +117,7 @@ void make_kparams(const dml_params& P, double maxc, KParams& K) {
       K.c0[i][j] = eps * 12.0 * K.b0[i][j];
       K.r0f_pref2[i][j] = (float)((r0 + margin) * (r0 + margin));
       K.pair_on[i][j] = eps != 0.0;
-      K.r0sqf[i][j] = (float)(r0 * r0);
-      K.epsf[i][j] = (float)eps;
-      K.c12f[i][j] = r0 > 0.0 ? (float)(12.0 * eps / (r0 * r0)) : 0.0f;
+      K.c12[i][j] = r0 > 0.0 ? 12.0 * eps / (r0 * r0) : 0.0;
     }
   for (int t = 0; t < 3; ++t) K.mass[t] = P.mass[t];
   // set_ermak (dana.F90:947-971)
@@ -274,6 +273,7 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
   if ((rc = test_update()) != 0) return rc;
   mark(DML_PHASE_COMMIT);
   n += k_capture_commit(d, k, cap, s);
+  mark(DML_PHASE_GCMC);
   if (c->P.reservoir == DML_RESERVOIR_GCMC) n += k_gcmc(d, k, cap, s);
   mark(DML_PHASE_RHO_PISTON);
   n += k_calc_rho(d, k, cap, s);
@@ -475,11 +475,13 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     R.cap = cap;
     R.nblk = cap / kBlock;
     R.cell_off = ncell;
-    ncell += R.ncell;
+    ncell += R.ncell + (R.use_cells ? 1 : 0);  // + the replica's sentinel cell
     total += cap;
     if (R.use_cells) any_cells = 1; else any_verlet = 1;
   }
   d.cap = total;
+  d.max_rep_cap = 0;
+  for (int r = 0; r < nrep; ++r) d.max_rep_cap = std::max(d.max_rep_cap, c->rc[r].cap);
   d.ncell_tot = ncell;
   d.any_cells = any_cells;
   d.any_verlet = any_verlet;
@@ -520,10 +522,12 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.in_gcmc, cap);
   AL(d.ins_head, ncell + 1);
   AL(d.ins_next, cap);
-  AL(d.facc, 4 * (size_t)cap);
+  // only the form in use gets its force accumulators
+  const bool mixed = c->P.precision == DML_PRECISION_MIXED;
+  AL(d.facc, mixed ? 4 * (size_t)cap : 4);
   AL(d.cand, (size_t)c->K.cand_cap);
   AL(d.ev_count, cap);
-  AL(d.ev, (size_t)cap * c->P.event_cap);
+  AL(d.ev, mixed ? 1 : (size_t)cap * c->P.event_cap);
   AL(d.near_count, cap);
   AL(d.near, (size_t)cap * kNearCap);
   AL(d.uf, cap);
@@ -613,6 +617,8 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     S.n_gcmc = ng;
     S.b_nat = n;
     S.nlimbo = 0;
+    S.free_lo = n;  // slots are dense after loading
+    S.bfree_lo = n;
     S.next_id = max_id + 1;
   }
   cudaStream_t st = c->stream;
@@ -853,6 +859,7 @@ int dml_get_counters_replica(dml_ctx* c, int32_t rep, dml_counters* o) {
   o->choques3 = (int64_t)s.choques3;
   o->nupd = (int64_t)s.nupd;
   o->step = c->h_g->step;
+  o->list_builds = c->h_g->list_builds;
   o->gcmc_ins = (int64_t)s.gcmc_ins;
   o->gcmc_del = (int64_t)s.gcmc_del;
   o->n_atoms = s.n_atoms;

@@ -39,11 +39,13 @@ constexpr int kBlock = 256;
 struct RepConst {
   double box[3], one_box[3], halfbox[3];
   double cell[3];
+  float inv_cellf[3];       // 1 / cell in FP32 (cell-index estimates)
   float boxf[3], halfboxf[3];
   int ncells[3];
   int head_dim[3];          // ncells + 2
   int use_cells;
-  int cell_off, ncell;      // this replica's range of the cell arrays
+  int cell_off, ncell;      // this replica's cells [cell_off, cell_off + ncell), then
+                            // one sentinel cell (always empty) whose start is the end
   int base, cap, nblk;      // positions [base, base + cap), cap / kBlock blocks
   unsigned long long seed;  // Philox key of this replica
 };
@@ -72,6 +74,9 @@ struct Scalars {
   int n_gcmc;      // gcmc%nat
   int nlimbo;      // hs%nlimbo
   int b_nat;       // hs%b%nat
+  int free_lo;     // every local hs slot below this one is in use (live or limbo)
+  int bfree_lo;    // every local hs%b slot below this one holds an atom
+  int halo;        // an atom sat in a halo cell at the last cell sort
   long long next_id;
 };
 
@@ -89,6 +94,7 @@ struct Global {
   int n_cand;      // entries in the force candidate queue
   int any_rebuild; // some replica rebuilds its list this test_update
   unsigned int ticket_rep;  // replicas finished with the displacement test
+  long long list_builds;    // rebuild kernels run (some replica rebuilt)
 };
 
 struct EvRec {            // one interacting list entry seen from one atom
@@ -108,11 +114,11 @@ struct KParams {
   double eps[3][3], r0sq[3][3], b0[3][3], c0[3][3];  // b0 = r0^6, c0 = eps*12*b0
   float r0f_pref2[3][3];    // FP32 pre-filter thresholds (r0 + margin)^2
   int pair_on[3][3];        // eps != 0 (other pairs add signed zeros only)
-  // mixed form: FP32 pair math, int64 fixed-point sums
+  // mixed form: FP32 force vectors, int64 fixed-point sums
   int mixed;
+  double c12[3][3];         // 12 eps / r0^2 (scalar pair force of the mixed form)
   int cand_cap;
   float rcf;                // rc (FP32, pre-filters)
-  float r0sqf[3][3], epsf[3][3], c12f[3][3];  // c12 = 12 eps / r0^2
   double fix_scale, fix_inv; // 2^32 per eV/Å in ui/Å, and its inverse
   float rlist_lo2, rlist_hi2; // list shell bounds (FP32)
   float margin;             // FP32 position error bound
@@ -167,6 +173,7 @@ struct Dev {
   int* rep_of;        // [cap] replica of every position
   int nrep;
   int cap;            // positions over all replicas (sum of the replica caps)
+  int max_rep_cap;    // largest replica capacity
   int any_cells, any_verlet;  // some replica uses linked cells / the all-pairs build
 };
 

@@ -96,6 +96,37 @@ __device__ __forceinline__ int cell_index(double x, double cell) {
   return (int)q + 1;
 }
 
+// int(x / cell) + 1 estimated from the FP32 copy of the coordinate (the
+// FP64 division issues on GB300's narrow FP64 pipe).  With xf = RN32(x) and
+// inv = RN32(1/cell) the FP32 quotient q is within 3 * 2^-24 |q| of x/cell,
+// so when q lies farther than 4e-7 q + 1e-6 from every integer, int(x/cell)
+// = floor(q) exactly; otherwise kCellUndecided asks for cell_index.  The
+// integer comes from adding 1.5 * 2^23 (round to nearest, FP32 adds only).
+constexpr int kCellUndecided = INT_MIN + 1;
+__device__ __forceinline__ int cell_index_est(float xf, float inv) {
+  const float M = 12582912.0f;
+  float q = xf * inv;
+  float r = (q + M) - M;
+  float dq = fabsf(q - r);
+  if (q > 0.0f && q < 4194304.0f && dq > 4e-7f * q + 1e-6f)
+    return (__float_as_int((q - 0.5f) + M) - 0x4B400000) + 1;
+  return kCellUndecided;
+}
+
+// Cell indices of a point from its FP32 and (when needed) FP64 coordinates.
+__device__ __forceinline__ void cell_index3(const RepConst& R, float4 Pf, const double4* P,
+                                            int& c1, int& c2, int& c3) {
+  c1 = cell_index_est(Pf.x, R.inv_cellf[0]);
+  c2 = cell_index_est(Pf.y, R.inv_cellf[1]);
+  c3 = cell_index_est(Pf.z, R.inv_cellf[2]);
+  if (c1 == kCellUndecided || c2 == kCellUndecided || c3 == kCellUndecided) {
+    double4 Q = *P;
+    if (c1 == kCellUndecided) c1 = cell_index(Q.x, R.cell[0]);
+    if (c2 == kCellUndecided) c2 = cell_index(Q.y, R.cell[1]);
+    if (c3 == kCellUndecided) c3 = cell_index(Q.z, R.cell[2]);
+  }
+}
+
 // cgroup_sort_atom's range test (Cells.F90:289-294): 0 <= int(x/cell)+1 <=
 // ncells+1 in every dimension, NaN out of range.  The quotient is formed only
 // for coordinates within 1e-9 relative of a bound; elsewhere the bounds
@@ -477,8 +508,8 @@ __global__ void ermak_b_kernel(Dev d, KParams p, int n_rank) {
 
 
 // ------------------------------------------------------- mixed-precision force
-// The chosen form of fuerza: the pair difference and the core (r0/r)^2,
-// (r0/r)^6 are taken in FP64 (positions reach 350 Å, where an FP32
+// The chosen form of fuerza: the pair difference, the core (r0/r)^2,
+// (r0/r)^6, (r0/r)^6 - 1 and the scalar force and energy are taken in FP64 (positions reach 350 Å, where an FP32
 // coordinate has a 3e-5 Å ulp), the pair force and energy in FP32, and both
 // are accumulated as int64 fixed point (2^32 per eV/Å and per eV).  Integer addition is associative, so the sums do not
 // depend on the order of the atomics: deterministic without ordering.
@@ -509,13 +540,16 @@ __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
     // The force polynomial, the vector and the energy are FP32.
     double r2d = dot3(dx, dy, dz);
     if (r2d > p.r0sq[k - 1][m - 1]) continue;
+    // The scalars |F|/r = 12 eps b (b-1) / r^2 and half the pair energy
+    // eps (b-1)^2 / 2 are formed from the FP64 core and rounded once (b - 1
+    // before any rounding: near the cut-off b -> 1); the force vector is the
+    // FP32 product of that scalar with the FP32 difference.
     double qd = p.r0sq[k - 1][m - 1] / r2d;
-    float b = (float)(qd * qd * qd);                      // (r0/r)^6
-    float qf = (float)qd;
+    double bd = qd * qd * qd;
+    double bm1 = bd - 1.0;
+    float fr = (float)(p.c12[k - 1][m - 1] * qd * (bd * bm1));
+    float e = (float)(0.5 * p.eps[k - 1][m - 1] * (bm1 * bm1));
     float vx = (float)dx, vy = (float)dy, vz = (float)dz;
-    float eps = p.epsf[k - 1][m - 1];
-    float fr = p.c12f[k - 1][m - 1] * (b * (b - 1.0f)) * qf;  // |F|/r = 12 eps b (b-1) / r^2
-    float e = 0.5f * (eps * b * (b - 2.0f) + eps);          // half the pair energy
     long long fx = to_fixed(p, fr * vx, p.fix_scale);
     long long fy = to_fixed(p, fr * vy, p.fix_scale);
     long long fz = to_fixed(p, fr * vz, p.fix_scale);
@@ -719,6 +753,7 @@ __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int 
       d.pos_old[s] = d.pos[s];
     } else if (st == ST_LIMBO) {
       d.state[s] = ST_NULL;
+      atomicMin(&sc->free_lo, s - R.base);  // the slot is free again
     }
   }
   if (R.use_cells && s < n_b) {
@@ -727,33 +762,42 @@ __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int 
       d.cell_of[s] = -1;
       return;
     }
-    double4 P = d.pos[hs];
-    int c1 = cell_index(P.x, R.cell[0]);
-    int c2 = cell_index(P.y, R.cell[1]);
-    int c3 = cell_index(P.z, R.cell[2]);
+    int c1, c2, c3;
+    cell_index3(R, d.posf[hs], d.pos + hs, c1, c2, c3);
     if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] + 1 || c2 > R.ncells[1] + 1 ||
         c3 > R.ncells[2] + 1) {
       raise_error(d.g, DML_E_OUT_OF_TESSELLATION, hs);
       d.cell_of[s] = -1;
       return;
     }
+    // the 27-cell stencil never visits the halo: searches over cells that
+    // must see every atom (GCMC) fall back to full scans for this replica
+    if (c1 == 0 || c2 == 0 || c3 == 0 || c1 > R.ncells[0] || c2 > R.ncells[1] ||
+        c3 > R.ncells[2])
+      sc->halo = 1;
     int lin = R.cell_off + (c3 * R.head_dim[1] + c2) * R.head_dim[0] + c1;
     d.cell_of[s] = lin;
     atomicAdd(&d.cell_count[lin], 1);
   }
 }
 
-// Exclusive scan of the cell counts (one block).
-__global__ void cell_scan_kernel(Dev d, int ncell, int force) {
-  if (!force && !d.g->any_rebuild) return;
+// Exclusive scan of one replica's cell counts (one block per replica),
+// starting at the replica's first position: its cell_atoms range is
+// [base, base + cap).  The sentinel after its last cell receives the end.
+__global__ void cell_scan_kernel(Dev d, int force) {
+  const RepConst& R = d.rc[blockIdx.x];
+  const Scalars* sc = d.sc + blockIdx.x;
+  if (!R.use_cells) return;
+  if (!force && !sc->rebuild) return;
+  const int ncell = R.ncell + 1;
   __shared__ int wsum[32];
   __shared__ int carry;
-  if (threadIdx.x == 0) carry = 0;
+  if (threadIdx.x == 0) carry = R.base;
   __syncthreads();
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int base = 0; base < ncell; base += blockDim.x) {
     int i = base + threadIdx.x;
-    int v = i < ncell ? d.cell_count[i] : 0;
+    int v = i < ncell ? d.cell_count[R.cell_off + i] : 0;
     int x = v;
     for (int o = 1; o < 32; o <<= 1) {
       int y = __shfl_up_sync(0xffffffffu, x, o);
@@ -772,14 +816,13 @@ __global__ void cell_scan_kernel(Dev d, int ncell, int force) {
     __syncthreads();
     int pre = (wid > 0 ? wsum[wid - 1] : 0) + x - v;
     if (i < ncell) {
-      d.cell_start[i] = carry + pre;
-      d.cell_fill[i] = 0;
+      d.cell_start[R.cell_off + i] = carry + pre;
+      d.cell_fill[R.cell_off + i] = 0;
     }
     __syncthreads();
     if (threadIdx.x == blockDim.x - 1) carry += pre + v;
     __syncthreads();
   }
-  if (threadIdx.x == 0) d.cell_start[ncell] = carry;
 }
 
 __global__ void cell_scatter_kernel(Dev d, int n_b, int force) {
@@ -806,8 +849,10 @@ __global__ void cell_order_kernel(Dev d, int ncell, int force) {
   int c = warp_id_global();
   int lane = threadIdx.x & 31;
   if (c >= ncell) return;
+  // counted in this sort (replicas that do not sort keep zero counts)
+  int num = __shfl_sync(0xffffffffu, lane == 0 ? d.cell_count[c] : 0, 0);
+  if (num == 0) return;
   int start = d.cell_start[c];
-  int num = d.cell_start[c + 1] - start;
   if (lane == 0) d.cell_count[c] = 0;
   if (num == 1 && lane == 0) d.cell_atoms[start] = d.b2hs[d.cell_atoms[start]];
   if (num <= 1) return;
@@ -838,7 +883,8 @@ __global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
   if (h < 0) return;
   double4 P = d.pos[h];
   float4 Pf = d.posf[h];
-  int rc[3] = {cell_index(P.x, R.cell[0]), cell_index(P.y, R.cell[1]), cell_index(P.z, R.cell[2])};
+  int rc[3];
+  cell_index3(R, Pf, d.pos + h, rc[0], rc[1], rc[2]);
   if (rc[0] == INT_MIN || rc[1] == INT_MIN || rc[2] == INT_MIN) {
     if (lane == 0) raise_error(d.g, DML_E_OUT_OF_TESSELLATION, h);
     return;
@@ -954,7 +1000,10 @@ __global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
 
 __global__ void rebuild_done_kernel(Dev d) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r == 0) d.g->any_rebuild = 0;
+  if (r == 0) {
+    if (d.g->any_rebuild) d.g->list_builds += 1;
+    d.g->any_rebuild = 0;
+  }
   if (r >= d.nrep) return;
   if (d.sc[r].rebuild) d.sc[r].listed = 1;
 }
@@ -1454,7 +1503,7 @@ __device__ __forceinline__ bool list_entry_in(const KParams& p, const RepConst& 
 
 // Own list of a newly attached atom i, one warp (ngroup_cells_atom,
 // Neighbor.F90:550-603, or ngroup_verlet_atom :426-463).
-__device__ void gcmc_own_list(const Dev& d, const KParams& p, const RepConst& R, int i) {
+__device__ void gcmc_own_list(const Dev& d, const KParams& p, const RepConst& R, int i, int nb_loc) {
   int lane = threadIdx.x & 31;
   double4 P = d.pos[i];
   int* row = d.list + (size_t)i * p.mnb;
@@ -1497,7 +1546,7 @@ __device__ void gcmc_own_list(const Dev& d, const KParams& p, const RepConst& R,
       }
     }
   } else {
-    int n_b = R.base + d.sc[d.rep_of[i]].n_b;
+    int n_b = R.base + nb_loc;
     for (int base = R.base; base < n_b; base += 32) {
       int b = base + lane;
       bool inc = false;
@@ -1518,22 +1567,63 @@ __device__ void gcmc_own_list(const Dev& d, const KParams& p, const RepConst& R,
   }
 }
 
-__global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
-  // one block per replica; its positions are [R.base, R.base + R.cap)
+constexpr int kGcmcThreads = 256;
+
+__device__ __forceinline__ bool in_slab(double z, double z0, double zmax) {
+  return !(z < z0) && !(z > zmax);
+}
+
+// Linear index of stencil cell `nabor` (map order) around the point's cell.
+__device__ __forceinline__ int stencil_cell(const RepConst& R, double4 P, int nabor) {
+  int rc[3] = {cell_index(P.x, R.cell[0]), cell_index(P.y, R.cell[1]), cell_index(P.z, R.cell[2])};
+  int nc[3];
+  for (int k = 0; k < 3; ++k) {
+    int t = c_map[nabor][k] + rc[k] - 1;
+    t = (t + R.ncells[k]) % R.ncells[k];
+    nc[k] = t + 1;
+  }
+  return R.cell_off + (nc[2] * R.head_dim[1] + nc[1]) * R.head_dim[0] + nc[0];
+}
+
+// gcmc_run, one block of kGcmcThreads per replica.  With linked cells and no
+// atom in a halo cell, the per-trial searches look only at the 27 cells
+// around the trial point (cell edges >= rc + skin): the hard-core test over
+// the gcmc group (`dr < rc^2` for some member, so the order of the search
+// does not matter) and the appends to the lists of hs%ref members within
+// rc + skin (each row gets at most one entry per insertion, so the order of
+// the rows does not matter).  The m-th in-slab member of the deletion walk is
+// found from per-chunk counts of in-slab members kept in shared memory
+// (chunks of kGcmcThreads gorder positions), the first free slots from
+// hints below which every slot is taken, and the group's first and last
+// members (the template atom and the atom that receives the Maxwell
+// velocity) are tracked across trials.  Replicas without cells, or with an
+// atom in a halo cell, scan the whole group as the reference does.
+__global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
+  extern __shared__ int s_chunk[];  // in-slab members per gorder chunk
   const int rep = blockIdx.x;
   const RepConst& R = d.rc[rep];
-  Scalars* sc = d.sc + rep;
+  Scalars* const sc_g = d.sc + rep;
+  // The replica's scalars live in shared memory for the whole call (one
+  // thread updates them between barriers) and are written back at the end.
+  __shared__ Scalars ss;
+  Scalars* const sc = &ss;
   const int B = R.base;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  __shared__ int s_min, s_max, s_cnt, s_sel, s_go;
-  __shared__ int s_n;
-  const long long step = d.g->step;
-  const double z0 = sc->z0, zmax = sc->zmax;
-  const double v = R.box[0] * R.box[1] * (zmax - z0);
-  if (!sc->listed) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
+  const int nw = nt >> 5;
+  __shared__ int s_first, s_last, s_n, s_slot, s_bslot, s_sel, s_dpre, s_pick, s_ppos;
+  __shared__ int s_cells[27], s_dup[27], s_start[27], s_pre[28], s_ca[27], s_cc[27];
+  __shared__ int s_ccin[27], s_cbase[27];
+  constexpr int KF = 8;  // flattened stencil entries a thread keeps in registers
+  if (!sc_g->listed) {
     if (tid == 0) raise_error(d.g, DML_E_STATE, 0);
     return;
   }
+  if (tid == 0) ss = *sc_g;
+  __syncthreads();
+  const long long step = d.g->step;
+  const double z0 = sc->z0, zmax = sc->zmax;
+  const double v = R.box[0] * R.box[1] * (zmax - z0);
+  __shared__ int s_fast;
   if (R.use_cells)
     for (int c = tid; c < R.ncell; c += nt) d.ins_head[R.cell_off + c] = -1;
   // order arrays grow by appends: compact them before they could overflow
@@ -1549,40 +1639,53 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
     int n = blk_compact(d.gorder, B, sc->n_gorder, d.gpos);
     if (tid == 0) sc->n_gorder = n;
   }
-  if (tid == 0) s_cnt = 0;
-  __syncthreads();
-  {
-    int ng = sc->n_gorder, c = 0;
-    for (int i = tid; i < ng; i += nt) {
-      int h = d.gorder[B + i];
-      if (h < 0) continue;
-      double z = d.pos[h].z;
-      if (!(z < z0 || z > zmax)) ++c;
-    }
-    if (c) atomicAdd(&s_cnt, c);
+  __syncthreads();  // compacted counts visible to every thread
+  if (tid == 0) {
+    s_first = INT_MAX;
+    s_last = -1;
+    s_n = 0;
+    s_fast = R.use_cells && !sc->halo;
   }
-  __syncthreads();
-  if (tid == 0) s_n = s_cnt;
-  __syncthreads();
-  for (int t = 1; t <= p.nadj; ++t) {
-    int n = s_n;
-    int ng = sc->n_gorder;
-    if (tid == 0) {
-      s_min = INT_MAX;
-      s_max = -1;
-    }
+  {
+    const int ng = sc->n_gorder;
+    for (int k = tid; k * nt < ng; k += nt) s_chunk[k] = 0;
     __syncthreads();
-    for (int i = tid; i < ng; i += nt)
-      if (d.gorder[B + i] >= 0) {
-        atomicMin(&s_min, i);
-        atomicMax(&s_max, i);
+    // in-slab count per chunk, the control-volume count n, first and last member
+    int lo = INT_MAX, hi = -1;
+    for (int base = 0; base < ng; base += nt) {
+      int i = base + tid;
+      int h = i < ng ? d.gorder[B + i] : -1;
+      int in = 0;
+      if (h >= 0) {
+        lo = min(lo, i);
+        hi = max(hi, i);
+        in = in_slab(d.pos[h].z, z0, zmax);
       }
-    __syncthreads();
-    if (s_min == INT_MAX) {
-      if (tid == 0) raise_error(d.g, DML_E_NO_PARTICLES, t);
-      return;
+      unsigned m = __ballot_sync(0xffffffffu, in);
+      if (lane == 0 && m) {
+        atomicAdd(&s_chunk[base / nt], __popc(m));
+        atomicAdd(&s_n, __popc(m));
+      }
     }
-    const int href = d.gorder[B + s_min], hlast = d.gorder[B + s_max];
+    for (int off = 16; off > 0; off >>= 1) {
+      lo = min(lo, __shfl_down_sync(0xffffffffu, lo, off));
+      hi = max(hi, __shfl_down_sync(0xffffffffu, hi, off));
+    }
+    if (lane == 0) {
+      atomicMin(&s_first, lo);
+      atomicMax(&s_last, hi);
+    }
+  }
+  for (int t = 1; t <= p.nadj; ++t) {
+    __syncthreads();
+    const int n = s_n, first = s_first, last = s_last;
+    const bool fast = s_fast != 0;
+    if (first == INT_MAX) {
+      if (tid == 0) raise_error(d.g, DML_E_NO_PARTICLES, t);
+      break;
+    }
+    const int ng = sc->n_gorder;
+    const int href = d.gorder[B + first], hlast = d.gorder[B + last];
     dml_u4 w0 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 0);
     dml_u4 w1 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 1);
     dml_u4 w2 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 2);
@@ -1596,50 +1699,143 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
       double r2 = dml_u53(w2.w[0], w2.w[1]) * (zmax - z0) + z0;
       double4 Rt = make_double4(r0, r1, r2, 0.0);
       bool ov = false;
-      for (int i = tid; i < ng && !ov; i += nt) {
-        int h = d.gorder[B + i];
-        if (h < 0) continue;
-        double vx, vy, vz;  // distance(o%pos, r, o%pbc) = r - o%pos
-        vdist_nint(R, Rt, d.pos[h], vx, vy, vz);
-        if (dot3(vx, vy, vz) < p.rc2) ov = true;
+      // stencil entries (cell atoms) of this thread: slot, list flags, cell
+      int fj[KF];
+      int ff[KF], fq[KF];
+      bool flat = false;
+      if (fast) {
+        if (tid < 27) {
+          int c = stencil_cell(R, Rt, tid);
+          int st = d.cell_start[c];
+          s_cells[tid] = c;
+          s_start[tid] = st;
+          s_pre[tid] = d.cell_start[c + 1] - st;  // count, made a prefix below
+          s_ca[tid] = 0;
+        }
+        __syncthreads();
+        if (tid < 27) {
+          int dup = 0;
+          for (int q = 0; q < tid; ++q) dup |= s_cells[q] == s_cells[tid];
+          s_dup[tid] = dup;
+        }
+        if (wid == 1) {
+          int v = lane < 27 ? s_pre[lane] : 0, x = v;
+          for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+          }
+          if (lane < 27) s_pre[lane] = x - v;
+          if (lane == 26) s_pre[27] = x;
+        }
+        __syncthreads();
+        // The 27 cells as one index space f in [0, T): hard-core test over
+        // the gcmc members among them, and (for the lists, if accepted) the
+        // own-list and append flags from the same distance.
+        const int T = s_pre[27];
+        flat = T <= KF * nt;
+#pragma unroll
+        for (int k = 0; k < KF; ++k) {
+          fj[k] = -1;
+          ff[k] = 0;
+          fq[k] = 0;
+        }
+        for (int k = 0, f = tid; f < T; ++k, f += nt) {
+          int lo = 0, hi = 26;  // cell q with s_pre[q] <= f < s_pre[q + 1]
+          while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (s_pre[mid] <= f) lo = mid; else hi = mid - 1;
+          }
+          const int q = lo;
+          const int j = d.cell_atoms[s_start[q] + f - s_pre[q]];
+          double vx, vy, vz;  // distance(o%pos, r, o%pbc) = r - o%pos
+          vdist_nint(R, Rt, d.pos[j], vx, vy, vz);
+          const double rd = dot3(vx, vy, vz);
+          if (d.in_gcmc[j] && rd < p.rc2) ov = true;
+          if (flat) {
+            const bool live = d.state[j] == ST_LIVE;
+            int fl = 0;
+            if (live && rd < p.rlist2) fl |= 1;  // own list (ngroup_cells_atom)
+            if (live && !s_dup[q] && d.rank[j] >= 0 && !(rd > p.rlist2)) fl |= 2;  // append
+#pragma unroll
+            for (int kk = 0; kk < KF; ++kk)
+              if (kk == k) {
+                fj[kk] = j;
+                ff[kk] = fl;
+                fq[kk] = q;
+              }
+          }
+        }
+        if (tid < 27)  // this run's insertions, at the heads of the chains
+          for (int h = d.ins_head[s_cells[tid]]; h >= 0 && !ov; h = d.ins_next[h]) {
+            if (!d.in_gcmc[h]) continue;
+            double vx, vy, vz;
+            vdist_nint(R, Rt, d.pos[h], vx, vy, vz);
+            if (dot3(vx, vy, vz) < p.rc2) ov = true;
+          }
+      } else {
+        for (int i = tid; i < ng && !ov; i += nt) {
+          int h = d.gorder[B + i];
+          if (h < 0) continue;
+          double vx, vy, vz;
+          vdist_nint(R, Rt, d.pos[h], vx, vy, vz);
+          if (dot3(vx, vy, vz) < p.rc2) ov = true;
+        }
       }
       if (__syncthreads_or(ov)) continue;
-      s_n = n + 1;  // every thread writes the same value
       // first free hs slot (limbo slots are not free) and hs%b slot
-      int nat = sc->n_atoms + 1, bnat = sc->b_nat + 1;
-      int ns = sc->n_slots, nb = sc->n_b;
-      if (tid == 0) {
-        s_min = INT_MAX;
-        s_sel = INT_MAX;
+      const int nat = sc->n_atoms + 1, bnat = sc->b_nat + 1;
+      const int ns = sc->n_slots, nb = sc->n_b;
+      if (wid == 0) {
+        int res = ns;
+        if (ns >= nat + sc->nlimbo) {
+          res = INT_MAX;
+          for (int base = sc->free_lo; base < ns; base += 32) {
+            int i = base + lane;
+            unsigned m = __ballot_sync(0xffffffffu, i < ns && d.state[B + i] == ST_NULL);
+            if (m) {
+              res = base + __ffs(m) - 1;
+              break;
+            }
+          }
+        }
+        if (lane == 0) s_slot = res;
+      } else if (wid == 1) {
+        int res = nb;
+        if (nb >= bnat) {
+          res = INT_MAX;
+          for (int base = sc->bfree_lo; base < nb; base += 32) {
+            int b = base + lane;
+            unsigned m = __ballot_sync(0xffffffffu, b < nb && d.b2hs[B + b] < 0);
+            if (m) {
+              res = base + __ffs(m) - 1;
+              break;
+            }
+          }
+        }
+        if (lane == 0) s_bslot = res;
       }
       __syncthreads();
-      if (ns >= nat + sc->nlimbo)
-        for (int i = tid; i < ns; i += nt)
-          if (d.state[B + i] == ST_NULL) atomicMin(&s_min, i);
-      if (nb >= bnat)
-        for (int b = tid; b < nb; b += nt)
-          if (d.b2hs[B + b] < 0) atomicMin(&s_sel, b);
-      __syncthreads();
-      int lslot = ns >= nat + sc->nlimbo ? s_min : ns;   // local hs slot
-      int lbs = nb >= bnat ? s_sel : nb;                 // local hs%b slot
+      const int lslot = s_slot, lbs = s_bslot;  // local hs and hs%b slots
       if (lslot == INT_MAX || lbs == INT_MAX) {
         if (tid == 0) raise_error(d.g, DML_E_INDEX, t);
-        return;
+        break;
       }
       if (lslot >= R.cap || lbs >= R.cap || sc->n_rank >= R.cap || sc->n_alist >= R.cap ||
-          sc->n_gorder >= R.cap) {
+          ng >= R.cap) {
         if (tid == 0) raise_error(d.g, DML_E_CAPACITY, t);
-        return;
+        break;
       }
       const int slot = B + lslot, bs = B + lbs;
-      __syncthreads();
       if (tid == 0) {
-        // atom_asign(o, ref) then pos, pos_old = r (dana.F90:659-663)
-        int typ = d.typ[href];
-        d.vel[slot] = d.vel[href];
-        d.force[slot] = d.force[href];
-        d.acel[slot] = d.acel[href];
-        d.epot[slot] = d.epot[href];
+        // atom_asign(o, ref) then pos, pos_old = r (dana.F90:659-663); the
+        // template's values are loaded before any store
+        const int typ = d.typ[href];
+        const double4 tv = d.vel[href], tf = d.force[href], ta = d.acel[href];
+        const double te = d.epot[href];
+        d.vel[slot] = tv;
+        d.force[slot] = tf;
+        d.acel[slot] = ta;
+        d.epot[slot] = te;
         d.typ[slot] = (int8_t)typ;
         d.pos[slot] = Rt;
         d.pos_old[slot] = Rt;
@@ -1650,7 +1846,7 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
         sc->next_id += 1;
         d.ev_count[slot] = 0;
         // Maxwell velocity to the last listed atom (dana.F90:666-668)
-        double beta = sqrt(p.beta_num / p.mass[d.typ[href] - 1]);
+        double beta = sqrt(p.beta_num / p.mass[typ - 1]);
         double nv[4];
         dml_normal_quad(dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC_VEL, 0), nv);
         d.vel[hlast] = make_double4(beta * nv[0], beta * nv[1], beta * nv[2], 0.0);
@@ -1670,6 +1866,7 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
         d.bslot[slot] = bs;
         if (lbs == nb) sc->n_b = nb + 1;
         sc->b_nat = bnat;
+        sc->bfree_lo = lbs + 1;
         if (R.use_cells) {
           int c1 = cell_index(Rt.x, R.cell[0]), c2 = cell_index(Rt.y, R.cell[1]),
               c3 = cell_index(Rt.z, R.cell[2]);
@@ -1680,116 +1877,250 @@ __global__ void __launch_bounds__(1024) gcmc_kernel(Dev d, KParams p) {
             int c = R.cell_off + (c3 * R.head_dim[1] + c2) * R.head_dim[0] + c1;
             d.ins_next[slot] = d.ins_head[c];
             d.ins_head[c] = slot;
+            // a halo cell is outside every stencil: full scans from here on
+            if (c1 == 0 || c2 == 0 || c3 == 0 || c1 > R.ncells[0] || c2 > R.ncells[1] ||
+                c3 > R.ncells[2])
+              s_fast = 0;
           }
         }
         // hs (igroup slot)
         d.state[slot] = ST_LIVE;
         if (lslot == ns) sc->n_slots = ns + 1;
+        sc->free_lo = lslot + 1;
         sc->n_atoms = nat;
-        // gcmc
-        int gp = sc->n_gorder;
-        d.gorder[B + gp] = slot;
-        d.gpos[slot] = B + gp;
+        // gcmc: appended at the end of the group
+        d.gorder[B + ng] = slot;
+        d.gpos[slot] = B + ng;
         d.in_gcmc[slot] = 1;
-        sc->n_gorder = gp + 1;
+        sc->n_gorder = ng + 1;
         sc->n_gcmc += 1;
         sc->gcmc_ins += 1;
+        if (ng % nt == 0) s_chunk[ng / nt] = 0;  // a new chunk
+        if (in_slab(Rt.z, z0, zmax)) s_chunk[ng / nt] += 1;
+        s_last = ng;
+        s_n = n + 1;
       }
       __syncthreads();
       // ngroup_sort_atom: own list, then append to every hs%ref list within reach
-      if (tid < 32) gcmc_own_list(d, p, R, slot);
-      {
-        int nr = sc->n_rank;
-        double4 A = d.pos[slot];
-        for (int q = tid; q < nr; q += nt) {
-          int j = d.ref[B + q];
-          if (j < 0 || j == slot) continue;
-          if (!list_entry_in(p, R, A, d.pos[j], false)) continue;
-          int m = d.nn[j];
-          if (m >= p.mnb) {
-            raise_error(d.g, DML_E_NEIGH_OVERFLOW, j);
-            continue;
+      auto append = [&](int j) {
+        int m = d.nn[j];
+        if (m >= p.mnb) {
+          raise_error(d.g, DML_E_NEIGH_OVERFLOW, j);
+          return;
+        }
+        d.list[(size_t)j * p.mnb + m] = slot;
+        d.nn[j] = m + 1;
+      };
+      if (flat) {
+        // Own list in stencil order: per cell, this run's insertions (chain,
+        // most recent first) then the sorted cell atoms in order.
+#pragma unroll
+        for (int k = 0; k < KF; ++k) {
+          if (fj[k] < 0) continue;
+          if (ff[k] & 1) atomicAdd(&s_ca[fq[k]], 1);
+          if (ff[k] & 2) append(fj[k]);
+        }
+        if (tid < 27) {
+          const int q = tid;
+          int cnt = 0;
+          for (int j = d.ins_head[s_cells[q]]; j >= 0; j = d.ins_next[j]) {
+            if (j == slot || d.state[j] != ST_LIVE) continue;
+            double vx, vy, vz;
+            vdist_nint(R, d.pos[j], Rt, vx, vy, vz);
+            double rd = dot3(vx, vy, vz);
+            if (rd < p.rlist2) ++cnt;
+            if (!s_dup[q] && d.rank[j] >= 0 && !(rd > p.rlist2)) append(j);
           }
-          d.list[(size_t)j * p.mnb + m] = slot;
-          d.nn[j] = m + 1;
+          s_cc[q] = cnt;
+        }
+        __syncthreads();
+        if (tid == 0) {
+          int acc = 0, cc = 0;
+          for (int q = 0; q < 27; ++q) {
+            s_cbase[q] = acc;
+            cc += s_cc[q];
+            s_ccin[q] = cc;
+            acc += s_cc[q] + s_ca[q];
+          }
+          if (acc > p.mnb) raise_error(d.g, DML_E_NEIGH_OVERFLOW, slot);
+          d.nn[slot] = acc > p.mnb ? p.mnb : acc;
+        }
+        __syncthreads();
+        int* row = d.list + (size_t)slot * p.mnb;
+        const int T = s_pre[27];
+        int carry = 0;
+#pragma unroll
+        for (int k = 0; k < KF; ++k) {
+          if (k * nt >= T) break;  // block-uniform
+          int own = (fj[k] >= 0 && (ff[k] & 1)) ? 1 : 0;
+          int tot;
+          int e = blk_scan_excl(own, &tot);
+          if (own) {
+            int pos = s_ccin[fq[k]] + carry + e;
+            if (pos < p.mnb) row[pos] = fj[k];
+          }
+          carry += tot;
+        }
+        if (tid < 27) {
+          const int q = tid;
+          int k = s_cbase[q];
+          for (int j = d.ins_head[s_cells[q]]; j >= 0; j = d.ins_next[j]) {
+            if (j == slot || d.state[j] != ST_LIVE) continue;
+            double vx, vy, vz;
+            vdist_nint(R, d.pos[j], Rt, vx, vy, vz);
+            if (dot3(vx, vy, vz) < p.rlist2) {
+              if (k < p.mnb) row[k] = j;
+              ++k;
+            }
+          }
+        }
+      } else {
+        if (wid == 0) gcmc_own_list(d, p, R, slot, sc->n_b);
+        if (fast) {
+          for (int q = wid; q < 27; q += nw) {
+            if (s_dup[q]) continue;
+            int c = s_cells[q];
+            int start = d.cell_start[c], num = d.cell_start[c + 1] - start;
+            for (int idx = lane; idx < num; idx += 32) {
+              int j = d.cell_atoms[start + idx];
+              if (j == slot || d.state[j] != ST_LIVE || d.rank[j] < 0) continue;
+              if (list_entry_in(p, R, Rt, d.pos[j], false)) append(j);
+            }
+            if (lane == 0)
+              for (int j = d.ins_head[c]; j >= 0; j = d.ins_next[j]) {
+                if (j == slot || d.state[j] != ST_LIVE || d.rank[j] < 0) continue;
+                if (list_entry_in(p, R, Rt, d.pos[j], false)) append(j);
+              }
+          }
+        } else {
+          int nr = sc->n_rank;
+          for (int q = tid; q < nr; q += nt) {
+            int j = d.ref[B + q];
+            if (j < 0 || j == slot) continue;
+            if (list_entry_in(p, R, Rt, d.pos[j], false)) append(j);
+          }
         }
       }
-      __syncthreads();
     } else {
       // destruction attempt (dana.F90:680-707)
       if ((double)n / (v * p.act) < uacc) continue;
       double upick = dml_u53(w2.w[2], w2.w[3]);
       int m = (int)floor(upick * (double)n) + 1;
       if (m > n) m = n;
-      int hsel = -1;
+      int hsel = -1, psel = -1;
       if (m <= 0) {
         hsel = hlast;  // the walk never reaches m == 0 and ends on the last atom
+        psel = last;
       } else {
+        // chunk holding the m-th in-slab member
         if (tid == 0) {
-          s_cnt = 0;
-          s_go = 1;
           s_sel = -1;
+          s_pick = -1;
+        }
+        const int nch = (ng + nt - 1) / nt;
+        int carry = 0;
+        for (int base = 0; base < nch; base += nt) {
+          int k = base + tid;
+          int c = k < nch ? s_chunk[k] : 0;
+          int tot;
+          int pre = blk_scan_excl(c, &tot);
+          if (c > 0 && carry + pre < m && m <= carry + pre + c) {
+            s_sel = k;
+            s_dpre = carry + pre;
+          }
+          carry += tot;
+          if (carry >= m) break;
         }
         __syncthreads();
-        for (int base = 0; base < ng && s_go; base += nt) {
-          int i = base + tid;
-          int h = i < ng ? d.gorder[B + i] : -1;
-          bool in = false;
-          if (h >= 0) {
-            double z = d.pos[h].z;
-            in = !(z < z0) && !(z > zmax);
-          }
-          int tot;
-          int pre = blk_scan_excl(in ? 1 : 0, &tot);
-          if (in && s_cnt + pre + 1 == m) s_sel = h;
-          __syncthreads();
-          if (tid == 0) {
-            s_cnt += tot;
-            if (s_sel >= 0) s_go = 0;
-          }
-          __syncthreads();
+        const int k = s_sel;
+        if (k < 0) {
+          if (tid == 0) raise_error(d.g, DML_E_CHOSEN_MISSING, t);
+          break;
         }
-        hsel = s_sel;
+        int i = k * nt + tid;
+        int h = i < ng ? d.gorder[B + i] : -1;
+        bool in = h >= 0 && in_slab(d.pos[h].z, z0, zmax);
+        int tot;
+        int pre = blk_scan_excl(in ? 1 : 0, &tot);
+        if (in && s_dpre + pre + 1 == m) {
+          s_pick = h;
+          s_ppos = i;
+        }
+        __syncthreads();
+        hsel = s_pick;
+        psel = s_ppos;
         if (hsel < 0) {
           if (tid == 0) raise_error(d.g, DML_E_CHOSEN_MISSING, t);
-          return;
+          break;
         }
       }
-      s_n = n - 1;
-      __syncthreads();
       if (tid == 0) {
-        // atom_destroy: gcmc, hs (nn, hs%ref, hs%b), sys (Groups.F90:433-467)
-        int h = hsel;
+        // atom_destroy: gcmc, hs (nn, hs%ref, hs%b), sys (Groups.F90:433-467);
+        // the atom's indices are loaded before any store
+        const int h = hsel;
+        const double4 P = d.pos[h];
+        const int gp = d.gpos[h], rk = d.rank[h], bsl = d.bslot[h], ap = d.apos[h];
+        const float4 pf = d.posf[h];
+        if (in_slab(P.z, z0, zmax)) s_chunk[psel / nt] -= 1;
         d.in_gcmc[h] = 0;
-        d.gorder[d.gpos[h]] = -1;
+        d.gorder[gp] = -1;
         sc->n_gcmc -= 1;
         d.nn[h] = 0;
-        if (d.rank[h] >= 0) {
-          d.ref[d.rank[h]] = -1;
+        if (rk >= 0) {
+          d.ref[rk] = -1;
           d.rank[h] = -1;
           sc->n_ref -= 1;
         }
         if (R.use_cells) {
-          double4 P = d.pos[h];
           int c1 = cell_index(P.x, R.cell[0]), c2 = cell_index(P.y, R.cell[1]),
               c3 = cell_index(P.z, R.cell[2]);
           if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] || c2 > R.ncells[1] || c3 > R.ncells[2])
             raise_error(d.g, DML_E_UNSUPPORTED, h);  // tessellation dropped (Cells.F90:320-327)
         }
-        d.b2hs[d.bslot[h]] = -1;
+        d.b2hs[bsl] = -1;
         d.bslot[h] = -1;
+        if (bsl - B < sc->bfree_lo) sc->bfree_lo = bsl - B;
         sc->b_nat -= 1;
         d.state[h] = ST_LIMBO;
         sc->nlimbo += 1;
         sc->n_atoms -= 1;
-        float4 f = d.posf[h];
-        f.w = __int_as_float(0);
-        d.posf[h] = f;
-        d.alist[d.apos[h]] = -1;
+        d.posf[h] = make_float4(pf.x, pf.y, pf.z, __int_as_float(0));
+        d.alist[ap] = -1;
         sc->gcmc_del += 1;
+        s_n = n - 1;
       }
       __syncthreads();
+      // new first / last member when one of them left the group
+      if (wid == 0 && psel == first) {
+        int res = INT_MAX;
+        for (int base = psel + 1; base < ng; base += 32) {
+          int i = base + lane;
+          unsigned mk = __ballot_sync(0xffffffffu, i < ng && d.gorder[B + i] >= 0);
+          if (mk) {
+            res = base + __ffs(mk) - 1;
+            break;
+          }
+        }
+        if (lane == 0) s_first = res;
+      }
+      if (wid == 1 && psel == last) {
+        int res = -1;
+        for (int top = psel - 1; top >= 0; top -= 32) {
+          int i = top - lane;
+          unsigned mk = __ballot_sync(0xffffffffu, i >= 0 && d.gorder[B + i] >= 0);
+          if (mk) {
+            res = top - (__ffs(mk) - 1);
+            break;
+          }
+        }
+        if (lane == 0) s_last = res;
+      }
     }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    ss.halo = 0;
+    *sc_g = ss;
   }
 }
 
@@ -1866,7 +2197,7 @@ int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, 
   rebuild_prep_kernel<<<nblk(nmax), kBlock, 0, s>>>(d, p, n_slots, n_b, 0);
   int n = 1;
   if (d.any_cells) {
-    cell_scan_kernel<<<1, 1024, 0, s>>>(d, d.ncell_tot, 0);
+    cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 0);
     cell_scatter_kernel<<<nblk(n_b), kBlock, 0, s>>>(d, n_b, 0);
     cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot, 0);
     list_cells_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
@@ -1913,12 +2244,15 @@ int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
   int n = 0;
   if (d.any_cells) {
     rebuild_prep_kernel<<<nblk(cap), kBlock, 0, s>>>(d, p, cap, cap, 1);
-    cell_scan_kernel<<<1, 1024, 0, s>>>(d, d.ncell_tot, 1);
+    cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1);
     cell_scatter_kernel<<<nblk(cap), kBlock, 0, s>>>(d, cap, 1);
     cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot, 1);
     n += 4;
   }
-  gcmc_kernel<<<d.nrep, 1024, 0, s>>>(d, p);
+  size_t shm = sizeof(int) * (size_t)(d.max_rep_cap / kGcmcThreads + 2);
+  if (shm > 48 * 1024)
+    cudaFuncSetAttribute(gcmc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+  gcmc_kernel<<<d.nrep, kGcmcThreads, shm, s>>>(d, p);
   return n + 1;
 }
 

@@ -126,6 +126,7 @@ class Counters(ctypes.Structure):
         ("z0", ctypes.c_double),
         ("rho", ctypes.c_double),
         ("rho0", ctypes.c_double),
+        ("list_builds", ctypes.c_int64),
     ]
 
     def as_dict(self):

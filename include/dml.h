@@ -134,6 +134,8 @@ typedef struct dml_counters {
   double z0;          /* current z0 */
   double rho;         /* last calc_rho */
   double rho0;        /* initial rho */
+  int64_t list_builds; /* test_updates that rebuilt some replica's list (one
+                          launch of the rebuild kernels each) */
 } dml_counters;
 
 typedef struct dml_ctx dml_ctx;
@@ -239,8 +241,9 @@ enum {
   DML_PHASE_OVERLAP = 4,     /* overlap_moveback */
   DML_PHASE_TEST_UPDATE2 = 5,/* test_update after the overlaps */
   DML_PHASE_COMMIT = 6,      /* F -> CG commit */
-  DML_PHASE_RHO_PISTON = 7,  /* calc_rho + maxz */
-  DML_NPHASE = 8
+  DML_PHASE_GCMC = 7,        /* gcmc_run (empty without the GCMC reservoir) */
+  DML_PHASE_RHO_PISTON = 8,  /* calc_rho + maxz */
+  DML_NPHASE = 9
 };
 int dml_time_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* ms);
 int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phase_ms,

@@ -99,3 +99,65 @@ def c5_small_params(seed=7, nadj=32):
     # deleted atoms hold limbo slots until the next list rebuild
     p.capacity = 16384
     return p
+
+
+C5_CELLS, C5_IONS = 40, 20000
+
+
+def c5_params(seed=11, precision=dml.PRECISION_MIXED, nadj=128, cells=C5_CELLS, n_ion=C5_IONS):
+    """Config 5 replica: 40 x 40 x 2-cell electrode (140.4 Å square), 300 Å
+    high, GCMC reservoir slab z in [200, 300] with `nadj` trials per step
+    (half creations, half destructions on average), Ermak, dt = 1 fs,
+    skin 10 Å.  The activity puts the ideal-gas count of the slab at the
+    initial ion density, so the mean ion count stays fixed."""
+    a = 3.51
+    L = cells * a
+    p = dml.default_params()
+    p.box[:] = [L, L, 300.0]
+    p.z0, p.zmax = 200.0, 300.0
+    p.h = 1e-3
+    p.skin = 10.0
+    p.reservoir = dml.RESERVOIR_GCMC
+    p.nadj = nadj
+    p.act = n_ion / (L * L * (300.0 - 15.0))
+    p.precision = precision
+    p.seed = seed
+    p.mnb = 512
+    # room for insertions while deleted atoms wait in limbo for a rebuild
+    p.capacity = 2 * cells * cells * 2 + n_ion + 16384
+    return p
+
+
+def c5_batch(n_rep, seed=11, precision=dml.PRECISION_MIXED, nadj=128, cells=C5_CELLS,
+             n_ion=C5_IONS):
+    """n_rep config-5 replicas, each with its own Philox seed and ion
+    placement.  Ions start at least rc = 3.2 Å apart: without a piston,
+    ions left within rc of each other at their step-start positions would
+    be moved back forever by overlap_moveback."""
+    p = c5_params(seed, precision, nadj, cells, n_ion)
+    reps = [dml.replica_of(p, seed=seed * 100003 + r) for r in range(n_rep)]
+    atoms = [dml.slab_system(cells, cells, 2, 300.0, n_ion, 15.0, 300.0,
+                             seed * 7919 + r, dmin=3.2) for r in range(n_rep)]
+    p.act = slab_activity(p, atoms[0], seed)
+    return p, reps, atoms
+
+
+def slab_activity(p, atoms, seed, samples=20000):
+    """Activity that keeps the slab count of `atoms` fixed on average:
+    creation and destruction balance when act * V * P_ins = N_slab, with
+    P_ins the chance that a uniform point of the slab lies at least rc from
+    every ion (the hard-core test), estimated here by sampling."""
+    import numpy as np
+    from scipy.spatial import cKDTree
+
+    L = p.box[0]
+    ions = atoms["pos"][atoms["z"] != dml.Z_CG]
+    n_slab = int(((ions[:, 2] >= p.z0) & (ions[:, 2] <= p.zmax)).sum())
+    rng = np.random.default_rng(seed)
+    pts = np.column_stack([rng.random(samples) * L, rng.random(samples) * L,
+                           p.z0 + rng.random(samples) * (p.zmax - p.z0)])
+    big = 4.0 * p.box[2] + 100.0  # no wrap along z
+    tree = cKDTree(np.mod(ions, [L, L, big]), boxsize=[L, L, big])
+    d, _ = tree.query(pts, k=1)
+    p_ins = max(float((d >= p.rc).mean()), 1e-3)
+    return n_slab / (L * L * (p.zmax - p.z0) * p_ins)

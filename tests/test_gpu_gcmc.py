@@ -76,3 +76,33 @@ def test_ermak_gcmc_with_electrode():
     assert_same_lists(g, o, "ermak+gcmc end")
     c = g.counters()
     assert c["gcmc_ins"] > 0 and c["gcmc_del"] > 0
+
+
+def test_config5_shape_gcmc_matches_oracle():
+    """Config-5 geometry at test size: 15 x 15 x 2-cell electrode (52.65 Å),
+    1500 ions, GCMC slab z in [60, 100] with 64 trials per step and the
+    activity that balances the slab count.  Three or more cells along every
+    axis, so each trial searches its 27 stencil cells; the list rebuilds free
+    limbo slots that later insertions take (Brownian moves, small skin)."""
+    p = systems.c5_params(seed=3, precision=dml.PRECISION_FP64, nadj=64, cells=15, n_ion=1500)
+    p.box[2] = 100.0
+    p.z0, p.zmax = 60.0, 100.0
+    p.skin = 2.0  # Brownian moves of ~0.4 Å: a rebuild every few steps
+    p.integrator = dml.INTEGRATOR_BROWNIAN
+    p.h = 1e-4
+    p.mnb = 512
+    atoms = dml.slab_system(15, 15, 2, 100.0, 1500, 15.0, 100.0, 21, dmin=3.2)
+    p.act = systems.slab_activity(p, atoms, 3)
+    g, o = make_pair(p, atoms)
+    g.setup()
+    o.setup()
+    done = 0
+    for chunk in [1, 9, 40]:
+        g.step(chunk)
+        o.step(chunk)
+        done += chunk
+        assert_same_state(g, o, "config-5 shape after %d" % done, FIELDS)
+        assert_same_counters(g, o, "config-5 shape after %d" % done, COUNTERS)
+    assert_same_lists(g, o, "config-5 shape end", ld=512)
+    c = g.counters()
+    assert c["gcmc_ins"] > 50 and c["gcmc_del"] > 50 and c["nupd"] > 1
