@@ -88,9 +88,11 @@ void make_repconst(const dml_params& P, const dml_replica& r, RepConst& R) {
     if (R.ncells[k] < 1) R.ncells[k] = 1;
     R.cell[k] = r.box[k] / (double)R.ncells[k];
     R.inv_cellf[k] = (float)(1.0 / R.cell[k]);
+    R.cellf[k] = (float)R.cell[k];
     R.head_dim[k] = R.ncells[k] + 2;
   }
   R.ncell = R.use_cells ? R.head_dim[0] * R.head_dim[1] * R.head_dim[2] : 0;
+  R.tess_hif = (float)((R.ncells[2] + 1) * R.cell[2]);
   R.seed = r.seed;
 }
 
@@ -107,6 +109,8 @@ void make_kparams(const dml_params& P, double maxc, KParams& K) {
   K.rlist2 = rl * rl;
   K.skin = P.skin;
   K.rlist_lo2 = (float)((rl - margin) * (rl - margin));
+  K.rc_lo2 = (float)((P.rc - margin) * (P.rc - margin));
+  K.rc_hi2 = (float)((P.rc + margin) * (P.rc + margin));
   K.rlist_hi2 = (float)((rl + margin) * (rl + margin));
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
@@ -161,6 +165,7 @@ void make_kparams(const dml_params& P, double maxc, KParams& K) {
   K.fix_inv = 1.0 / K.fix_scale;
   K.act = P.act;
   K.beta_num = P.kb_module * P.temp;
+  for (int t = 0; t < 3; ++t) K.beta_t[t] = std::sqrt(K.beta_num / P.mass[t]);
   K.nadj = P.nadj;
 }
 
@@ -253,22 +258,25 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
     return 0;
   };
   mark(DML_PHASE_INTEGRATE);
-  n += k_step_begin(d, s);
-  if (c->P.integrator == DML_INTEGRATOR_ERMAK) {
+  const bool ermak = c->P.integrator == DML_INTEGRATOR_ERMAK;
+  n += k_step_begin(d, ermak ? 0 : 1, s);
+  if (ermak) {
     n += k_ermak_a(d, k, cap, s);
+    n += k_overlap_prepare(d, k, cap, s);
     mark(DML_PHASE_FORCE_PAIRS);
-    n += k_force_pairs(d, k, cap, s);
+    n += k_force_pairs(d, k, cap, true, s);  // + overlap_moveback's near entries
     mark(DML_PHASE_FORCE_SUM);
     n += k_force_sum(d, k, cap, true, s);  // fuerza + ermak_b
   } else {
     n += k_brownian(d, k, cap, s);
+    n += k_overlap_prepare(d, k, cap, s);
     mark(DML_PHASE_FORCE_PAIRS);
     mark(DML_PHASE_FORCE_SUM);
   }
   mark(DML_PHASE_TEST_UPDATE1);
   if ((rc = test_update()) != 0) return rc;
   mark(DML_PHASE_OVERLAP);
-  n += k_overlap(d, k, cap, cap, s);
+  n += k_overlap(d, k, cap, cap, false, s);
   mark(DML_PHASE_TEST_UPDATE2);
   if ((rc = test_update()) != 0) return rc;
   mark(DML_PHASE_COMMIT);
@@ -498,6 +506,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.pos_old, cap);
   AL(d.ranv, cap);
   AL(d.posf, cap);
+  AL(d.posf_old, cap);
   AL(d.epot, cap);
   AL(d.typ, cap);
   AL(d.skip, cap);
@@ -533,7 +542,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.uf, cap);
   AL(d.comp_size, cap);
   AL(d.comp_id, cap);
-  AL(d.comp_off, cap);
+  AL(d.comp_rank, cap);
   AL(d.comp_fill, cap);
   AL(d.comp_members, cap);
   AL(d.comp_list, 2 * (size_t)cap);
@@ -547,7 +556,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
 
   // Host staging, position order (replica r at [base, base + cap)).
   std::vector<double4> pos(cap), vel(cap), acel(cap), force(cap), pos_old(cap), old_cg(cap);
-  std::vector<float4> posf(cap, make_float4(0.f, 0.f, 0.f, 0.f));
+  std::vector<float4> posf(cap, make_float4(0.f, 0.f, 0.f, 0.f)), posf_old(cap, posf[0]);
   std::vector<double> epot(cap, 0.0);
   std::vector<int8_t> typ(cap, 0), skip(cap, 0), state(cap, ST_NULL), in_gcmc(cap, 0);
   std::vector<long long> id(cap, 0);
@@ -584,6 +593,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
       float zbits;
       std::memcpy(&zbits, &z, sizeof zbits);  // element as integer bits in w
       posf[h] = make_float4((float)pos[h].x, (float)pos[h].y, (float)pos[h].z, zbits);
+      posf_old[h] = make_float4((float)pos_old[h].x, (float)pos_old[h].y, (float)pos_old[h].z, 0.f);
       bool in_ref = a->in_ref ? a->in_ref[i] != 0 : (z != DML_Z_CG);
       if (in_ref) {
         rank[h] = B + nref;
@@ -629,6 +639,8 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   CK(cudaMemcpyAsync(d.pos_old, pos_old.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.old_cg, old_cg.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.posf, posf.data(), sizeof(float4) * cap, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(d.posf_old, posf_old.data(), sizeof(float4) * cap, cudaMemcpyHostToDevice,
+                     st));
   CK(cudaMemcpyAsync(d.epot, epot.data(), sizeof(double) * cap, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.typ, typ.data(), cap, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(d.skip, skip.data(), cap, cudaMemcpyHostToDevice, st));
@@ -673,7 +685,7 @@ int dml_test_update(dml_ctx* c, int32_t* rebuilt) {
 
 int dml_force(dml_ctx* c) {
   if (!c || !c->loaded) return DML_E_STATE;
-  k_force_pairs(c->D, c->K, c->D.cap, c->stream);
+  k_force_pairs(c->D, c->K, c->D.cap, false, c->stream);
   k_force_sum(c->D, c->K, c->D.cap, false, c->stream);
   return finish(c);
 }
@@ -704,7 +716,7 @@ int dml_overlap_moveback(dml_ctx* c, int64_t step) {
   if (!c || !c->loaded) return DML_E_STATE;
   int rc = set_step(c, step);
   if (rc) return rc;
-  k_overlap(c->D, c->K, c->D.cap, c->D.cap, c->stream);
+  k_overlap(c->D, c->K, c->D.cap, c->D.cap, true, c->stream);
   return finish(c);
 }
 

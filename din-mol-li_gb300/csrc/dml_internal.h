@@ -6,6 +6,7 @@
 // slots, so every per-atom array is indexed by hs slot:
 //   pos      double4 (x, y, z, 0)            32 B, one sector per gather
 //   posf     float4  (x, y, z, element bits)  16 B, the FP32 pre-filter copy
+//   posf_old float4  FP32 copy of pos_old (displacement test)
 //   vel, acel, force, old_cg, pos_old, ranv  double4
 //   epot double, typ/skip/state int8, id int64, rank/bslot int32
 // `ref` holds hs slots in hs%ref order (holes = -1 after captures); ranks
@@ -40,6 +41,7 @@ struct RepConst {
   double box[3], one_box[3], halfbox[3];
   double cell[3];
   float inv_cellf[3];       // 1 / cell in FP32 (cell-index estimates)
+  float cellf[3], tess_hif; // cell and (ncells_z + 1) * cell_z in FP32 (range tests)
   float boxf[3], halfboxf[3];
   int ncells[3];
   int head_dim[3];          // ncells + 2
@@ -95,6 +97,7 @@ struct Global {
   int any_rebuild; // some replica rebuilds its list this test_update
   unsigned int ticket_rep;  // replicas finished with the displacement test
   long long list_builds;    // rebuild kernels run (some replica rebuilt)
+  int near_stale;           // near lists must be searched in the overlap phase
 };
 
 struct EvRec {            // one interacting list entry seen from one atom
@@ -119,6 +122,8 @@ struct KParams {
   double c12[3][3];         // 12 eps / r0^2 (scalar pair force of the mixed form)
   int cand_cap;
   float rcf;                // rc (FP32, pre-filters)
+  float rc_lo2, rc_hi2;     // (rc -+ margin)^2: FP32 hard-core test decided outside
+  double beta_t[3];         // sqrt(kB T / m) per element (gcmc_run's Maxwell draw)
   double fix_scale, fix_inv; // 2^32 per eV/Å in ui/Å, and its inverse
   float rlist_lo2, rlist_hi2; // list shell bounds (FP32)
   float margin;             // FP32 position error bound
@@ -141,7 +146,7 @@ struct KParams {
 // All device buffers of one context.
 struct Dev {
   double4 *pos, *vel, *acel, *force, *old_cg, *pos_old, *ranv;
-  float4* posf;
+  float4 *posf, *posf_old;
   double* epot;
   int8_t *typ, *skip, *state, *active;
   long long* id;
@@ -162,7 +167,7 @@ struct Dev {
   int8_t* in_gcmc;
   int *ins_head, *ins_next;  // atoms inserted at cell-chain heads during gcmc_run
   // overlap
-  int *near_count, *near, *uf, *comp_size, *comp_id, *comp_off, *comp_fill, *comp_members, *comp_list;
+  int *near_count, *near, *uf, *comp_size, *comp_id, *comp_rank, *comp_fill, *comp_members, *comp_list;
   // reductions
   unsigned long long* part;  // per-block partials (top-2, as double bits)
   int nblk_part;
@@ -178,10 +183,10 @@ struct Dev {
 };
 
 // ---- kernel launchers (dml_kernels.cu); each returns the kernels it queued ----
-int k_step_begin(const Dev& d, cudaStream_t s);
+int k_step_begin(const Dev& d, int near_stale, cudaStream_t s);
 int k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
-int k_force_pairs(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
+int k_force_pairs(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s);
 int k_force_sum(const Dev& d, const KParams& p, int n_slots, bool fuse_ermak_b, cudaStream_t s);
 int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
@@ -189,7 +194,11 @@ int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_ra
 int k_pbc_dispmax_cond(const Dev& d, const KParams& p, int n_slots,
                        cudaGraphConditionalHandle h, cudaStream_t s);
 int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, cudaStream_t s);
-int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStream_t s);
+// overlap_moveback: standalone (its own delta and near search) or as the
+// second half of a fused step whose first half ran k_overlap_prepare.
+int k_overlap_prepare(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
+int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool standalone,
+              cudaStream_t s);
 int k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
 int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);

@@ -153,7 +153,14 @@ __device__ __forceinline__ int warp_id_global() {
 }
 
 // ----------------------------------------------------------------- step
-__global__ void step_begin_kernel(Global* g) { g->step += 1; }
+// A new step: the counter, the displacement bound delta of this step's
+// overlap search, and whether its near lists still need a search of their
+// own (always with the Brownian integrator, which has no force scan).
+__global__ void step_begin_kernel(Global* g, int near_stale) {
+  g->step += 1;
+  g->delta2_bits = 0ull;
+  g->near_stale = near_stale;
+}
 
 // atom_pbc (dana.F90:1187-1250) on registers; returns true when deposited.
 __device__ __forceinline__ bool atom_pbc_dev(const KParams& p, const RepConst& R, Scalars* sc,
@@ -244,7 +251,10 @@ __global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
   d.pos[h] = np;
   d.posf[h] = to_f4(np, typ);
   d.ranv[h] = make_double4(rv[0], rv[1], rv[2], 0.0);
-  if (po_changed) d.pos_old[h] = po;
+  if (po_changed) {
+    d.pos_old[h] = po;
+    d.posf_old[h] = to_f4(po, 0);
+  }
   if (v_changed) d.vel[h] = V;
   if (typ != typ0) d.typ[h] = (int8_t)typ;
   if (!depos) d.skip[h] = 0;
@@ -286,9 +296,49 @@ __global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
   d.pos[h] = np;
   d.posf[h] = to_f4(np, typ);
   d.vel[h] = V;
-  if (po_changed) d.pos_old[h] = po;
+  if (po_changed) {
+    d.pos_old[h] = po;
+    d.posf_old[h] = to_f4(po, 0);
+  }
   if (typ != typ0) d.typ[h] = (int8_t)typ;
   if (!depos) d.skip[h] = 0;
+}
+
+// Union-find over hs slots (overlap components): path halving, union by
+// smaller root; bounded loops report DML_E_OVERLAP_PASSES.
+__device__ int uf_find(volatile int* uf, int x) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    int px = uf[x];
+    if (px == x) return x;
+    int ppx = uf[px];
+    if (ppx != px) atomicCAS((int*)&uf[x], px, ppx);
+    x = px;
+  }
+  return -1;
+}
+
+__device__ void uf_union(Global* g, volatile int* uf, int a, int b) {
+  for (int it = 0; it < (1 << 20); ++it) {
+    a = uf_find(uf, a);
+    b = uf_find(uf, b);
+    if (a < 0 || b < 0) break;
+    if (a == b) return;
+    if (a < b) {
+      int t = a;
+      a = b;
+      b = t;
+    }
+    if (atomicCAS((int*)&uf[a], a, b) == a) return;
+  }
+  raise_error(g, DML_E_OVERLAP_PASSES, -1);
+}
+
+// Near radius of overlap_moveback, rc + 2 delta in FP32 with margin (a
+// superset of the pairs that can touch during the passes).
+__device__ __forceinline__ float near_radius2(const Dev& d, const KParams& p) {
+  float delta = sqrtf(__double2float_ru(__longlong_as_double((long long)d.g->delta2_bits)));
+  float rnf = (p.rcf + 2.0f * delta) * 1.000001f + 4.0f * p.margin + 1e-3f;
+  return rnf * rnf;
 }
 
 // ---------------------------------------------------------------- fuerza
@@ -313,6 +363,7 @@ __device__ __forceinline__ bool force_candidate(const KParams& p, const RepConst
 // On GB300 an FP64 instruction occupies the narrow FP64 pipe for the whole
 // warp whatever its active lanes, so the exact FP64 work is done afterwards
 // on the dense queue (force_exact_kernel), 32 entries per instruction.
+template <bool NEAR>
 __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n_rank) {
   int r = warp_id_global();  // grids are sized by capacity
   int lane = threadIdx.x & 31;
@@ -326,6 +377,12 @@ __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n
   float4 Pf = d.posf[h];
   int n = d.nn[h];
   const int* row = d.list + (size_t)h * p.mnb;
+  // With NEAR the same pass records overlap_moveback's near entries (list
+  // entries within rc + 2 delta, list order) and unites their components.
+  const float rn2 = NEAR ? near_radius2(d, p) : 0.0f;
+  int* near = d.near + (size_t)h * kNearCap;
+  int ncnt = 0;
+  bool any = false;
   for (int base = 0; base < n; base += 64) {
     int jj0 = base + lane, jj1 = jj0 + 32;
     int j0 = jj0 < n ? __ldg(row + jj0) : -1;
@@ -338,19 +395,48 @@ __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n
     bool c1 = j1 >= 0 && force_candidate(p, R, Pf, k, Q1, m1);
     unsigned b0 = __ballot_sync(0xffffffffu, c0), b1 = __ballot_sync(0xffffffffu, c1);
     int tot = __popc(b0) + __popc(b1);
-    if (tot == 0) continue;
-    int base_q = 0;
-    if (lane == 0) base_q = atomicAdd(&d.g->n_cand, tot);
-    base_q = __shfl_sync(0xffffffffu, base_q, 0);
-    unsigned lt = (1u << lane) - 1u;
-    if (c0) {
-      int q = base_q + __popc(b0 & lt);
-      if (q < p.cand_cap) d.cand[q] = make_int4(r, jj0, h, j0);
+    if (tot != 0) {
+      int base_q = 0;
+      if (lane == 0) base_q = atomicAdd(&d.g->n_cand, tot);
+      base_q = __shfl_sync(0xffffffffu, base_q, 0);
+      unsigned lt = (1u << lane) - 1u;
+      if (c0) {
+        int q = base_q + __popc(b0 & lt);
+        if (q < p.cand_cap) d.cand[q] = make_int4(r, jj0, h, j0);
+      }
+      if (c1) {
+        int q = base_q + __popc(b0) + __popc(b1 & lt);
+        if (q < p.cand_cap) d.cand[q] = make_int4(r, jj1, h, j1);
+      }
     }
-    if (c1) {
-      int q = base_q + __popc(b0) + __popc(b1 & lt);
-      if (q < p.cand_cap) d.cand[q] = make_int4(r, jj1, h, j1);
+    if (NEAR) {
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        int j = half ? j1 : j0;
+        float4 Q = half ? Q1 : Q0;
+        bool inc = false;
+        if (j >= 0 && elem_of(Q) != 0) {
+          float fx, fy, fz;
+          vdist_nint_f(R, Pf, Q, fx, fy, fz);
+          inc = fx * fx + fy * fy + fz * fz <= rn2;
+        }
+        unsigned bal = __ballot_sync(0xffffffffu, inc);
+        int pre = __popc(bal & ((1u << lane) - 1u));
+        if (inc) {
+          if (ncnt + pre < kNearCap) near[ncnt + pre] = j;
+          if (elem_of(Q) != DML_Z_CG) {
+            uf_union(d.g, (volatile int*)d.uf, h, j);
+            d.active[j] = 1;
+          }
+        }
+        ncnt += __popc(bal);
+        any = any || bal != 0;
+      }
     }
+  }
+  if (NEAR && lane == 0) {
+    d.near_count[h] = ncnt > kNearCap ? -1 : ncnt;
+    if (any) d.active[h] = 1;
   }
 }
 
@@ -623,8 +709,34 @@ __device__ __forceinline__ void top2_merge(unsigned long long& a1, unsigned long
 }
 
 // do_pbc (Groups.F90:1440-1467) + inq_dispmax (Neighbor.F90:635-666) + the
-// update decision (Neighbor.F90:697-710).  The top-2 of squared
-// displacements is order independent, so a tree reduction is exact.
+// update decision (Neighbor.F90:697-710), sqrt(d1) + sqrt(d2) > skin with
+// d1 >= d2 the two largest |pos - pos_old|^2 (exact FP64 in the reference).
+//
+// Most atoms need no FP64 here: an atom whose FP32 coordinates lie farther
+// than the margin from 0 and the box edge (x, y) and from the tessellation
+// bounds (z) is neither wrapped nor out of the tessellation, and its FP32
+// displacement |posf - posf_old| is within the margin e of the exact one in
+// sqrt space.  The FP32 top-2 F1 >= F2 then decides whenever sqrt(F1) +
+// sqrt(F2) is farther than 4e from skin; otherwise the replica's last block
+// takes the exact top-2 over the atoms with sqrt(rdf) >= sqrt(F2) - 3e (any
+// atom of the exact top-2 qualifies) and decides in FP64 as the reference.
+__device__ __forceinline__ double4 ldcg_d4(const double4* p) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+  double2 a = __ldcg(q), b = __ldcg(q + 1);
+  return make_double4(a.x, a.y, b.x, b.y);
+}
+
+__device__ __forceinline__ void top2f(float& a1, float& a2, float b1, float b2) {
+  float hi = fmaxf(a1, b1), lo1 = fminf(a1, b1), lo2 = fmaxf(a2, b2);
+  a1 = hi;
+  a2 = fmaxf(lo1, lo2);
+}
+
+__device__ __forceinline__ float disp2f(float4 P, float4 O) {
+  float x = P.x - O.x, y = P.y - O.y, z = P.z - O.z;
+  return (x * x + y * y) + z * z;
+}
+
 __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
                                    cudaGraphConditionalHandle cond_handle) {
   // grids are sized by capacity; the block's replica gives the live count
@@ -633,49 +745,61 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned long long tiny = (unsigned long long)__double_as_longlong(1.e-16);
-  unsigned long long a1 = tiny, a2 = tiny;
+  const float tinyf = 1e-16f;
+  const float e = p.margin;
+  float a1 = tinyf, a2 = tinyf;
   if (s < n_slots && d.state[s] == ST_LIVE) {
-    double4 P = d.pos[s];
-    double4 O = d.pos_old[s];
-    bool ch = false;
-    if (P.x >= R.box[0]) {
-      P.x = P.x - R.box[0];
-      O.x = O.x - R.box[0];
-      ch = true;
-    } else if (P.x < 0.0) {
-      P.x = P.x + R.box[0];
-      O.x = O.x + R.box[0];
-      ch = true;
+    float4 Pf = d.posf[s], Of = d.posf_old[s];
+    bool safe = Pf.x > e && Pf.x < R.boxf[0] - e && Pf.y > e && Pf.y < R.boxf[1] - e;
+    if (safe && R.use_cells)
+      safe = Pf.z > -2.0f * R.cellf[2] + e && Pf.z < R.tess_hif - e;
+    if (!safe) {
+      double4 P = d.pos[s];
+      double4 O = d.pos_old[s];
+      bool ch = false;
+      if (P.x >= R.box[0]) {
+        P.x = P.x - R.box[0];
+        O.x = O.x - R.box[0];
+        ch = true;
+      } else if (P.x < 0.0) {
+        P.x = P.x + R.box[0];
+        O.x = O.x + R.box[0];
+        ch = true;
+      }
+      if (P.y >= R.box[1]) {
+        P.y = P.y - R.box[1];
+        O.y = O.y - R.box[1];
+        ch = true;
+      } else if (P.y < 0.0) {
+        P.y = P.y + R.box[1];
+        O.y = O.y + R.box[1];
+        ch = true;
+      }
+      if (ch) {
+        d.pos[s] = P;
+        d.pos_old[s] = O;
+        Pf = to_f4(P, d.typ[s]);
+        Of = to_f4(O, 0);
+        d.posf[s] = Pf;
+        d.posf_old[s] = Of;
+      }
+      // cgroup_sort runs at every test_update (Neighbor.F90:687-691) and
+      // stops on an atom outside the tessellation (Cells.F90:293-294).
+      if (R.use_cells && !in_tessellation(R, P)) raise_error(d.g, DML_E_OUT_OF_TESSELLATION, s);
     }
-    if (P.y >= R.box[1]) {
-      P.y = P.y - R.box[1];
-      O.y = O.y - R.box[1];
-      ch = true;
-    } else if (P.y < 0.0) {
-      P.y = P.y + R.box[1];
-      O.y = O.y + R.box[1];
-      ch = true;
-    }
-    if (ch) {
-      d.pos[s] = P;
-      d.pos_old[s] = O;
-      d.posf[s] = to_f4(P, d.typ[s]);
-    }
-    // cgroup_sort runs at every test_update (Neighbor.F90:687-691) and stops
-    // on an atom outside the tessellation (Cells.F90:293-294), rebuild or not.
-    if (R.use_cells && !in_tessellation(R, P)) raise_error(d.g, DML_E_OUT_OF_TESSELLATION, s);
-    double rd = dot3(P.x - O.x, P.y - O.y, P.z - O.z);
+    float rdf = disp2f(Pf, Of);
     // a NaN displacement never passes `rd > dispmax` (Neighbor.F90:657-661)
-    if (rd == rd) top2_merge(a1, a2, (unsigned long long)__double_as_longlong(rd), tiny);
+    if (rdf == rdf) top2f(a1, a2, rdf, tinyf);
   }
   for (int off = 16; off > 0; off >>= 1) {
-    unsigned long long b1 = __shfl_down_sync(0xffffffffu, a1, off);
-    unsigned long long b2 = __shfl_down_sync(0xffffffffu, a2, off);
-    top2_merge(a1, a2, b1, b2);
+    float b1 = __shfl_down_sync(0xffffffffu, a1, off);
+    float b2 = __shfl_down_sync(0xffffffffu, a2, off);
+    top2f(a1, a2, b1, b2);
   }
-  __shared__ unsigned long long w1[32], w2[32];
+  __shared__ float w1[32], w2[32];
+  __shared__ unsigned long long x1[32], x2[32];
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nwarp = blockDim.x >> 5;
   if (lane == 0) {
     w1[wid] = a1;
     w2[wid] = a2;
@@ -683,10 +807,10 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
   __syncthreads();
   __shared__ bool last;
   if (threadIdx.x == 0) {
-    unsigned long long b1 = tiny, b2 = tiny;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) top2_merge(b1, b2, w1[w], w2[w]);
-    d.part[2 * blockIdx.x] = b1;
-    d.part[2 * blockIdx.x + 1] = b2;
+    float b1 = tinyf, b2 = tinyf;
+    for (int w = 0; w < nwarp; ++w) top2f(b1, b2, w1[w], w2[w]);
+    d.part[2 * blockIdx.x] = __float_as_uint(b1);
+    d.part[2 * blockIdx.x + 1] = __float_as_uint(b2);
     __threadfence();
     unsigned t = atomicAdd(&sc->ticket, 1u);
     last = (t == (unsigned)R.nblk - 1u);
@@ -694,17 +818,16 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
   __syncthreads();
   if (!last) return;
   __threadfence();
-  // last block of this replica: parallel top-2 over the replica's partials
-  unsigned long long b1 = tiny, b2 = tiny;
+  // last block of this replica: FP32 top-2 over the replica's partials
+  float b1 = tinyf, b2 = tinyf;
   const int b0 = R.base / kBlock;
-  for (int b = b0 + threadIdx.x; b < b0 + R.nblk; b += blockDim.x) {
-    unsigned long long c1 = __ldcg(d.part + 2 * b), c2 = __ldcg(d.part + 2 * b + 1);
-    top2_merge(b1, b2, c1, c2);
-  }
+  for (int b = b0 + threadIdx.x; b < b0 + R.nblk; b += blockDim.x)
+    top2f(b1, b2, __uint_as_float((unsigned)__ldcg(d.part + 2 * b)),
+          __uint_as_float((unsigned)__ldcg(d.part + 2 * b + 1)));
   for (int off = 16; off > 0; off >>= 1) {
-    unsigned long long c1 = __shfl_down_sync(0xffffffffu, b1, off);
-    unsigned long long c2 = __shfl_down_sync(0xffffffffu, b2, off);
-    top2_merge(b1, b2, c1, c2);
+    float c1 = __shfl_down_sync(0xffffffffu, b1, off);
+    float c2 = __shfl_down_sync(0xffffffffu, b2, off);
+    top2f(b1, b2, c1, c2);
   }
   __syncthreads();
   if (lane == 0) {
@@ -712,11 +835,56 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
     w2[wid] = b2;
   }
   __syncthreads();
+  __shared__ int s_dec;  // 0 keep, 1 rebuild, 2 undecided
+  __shared__ float s_s2;
   if (threadIdx.x == 0) {
+    float F1 = tinyf, F2 = tinyf;
+    for (int w = 0; w < nwarp; ++w) top2f(F1, F2, w1[w], w2[w]);
+    float sum = sqrtf(F1) + sqrtf(F2);
+    int dec;
+    if (!sc->listed) dec = 1;
+    else if (sum + 4.0f * e < (float)p.skin) dec = 0;
+    else if (sum - 4.0f * e > (float)p.skin) dec = 1;
+    else dec = 2;
+    s_dec = dec;
+    s_s2 = sqrtf(F2);
+  }
+  __syncthreads();
+  int rebuild = s_dec;
+  if (rebuild == 2) {
+    // exact top-2 over the candidates (every slot of the replica, read through L2)
+    const unsigned long long tiny = (unsigned long long)__double_as_longlong(1.e-16);
     unsigned long long e1 = tiny, e2 = tiny;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) top2_merge(e1, e2, w1[w], w2[w]);
-    double d1 = __longlong_as_double((long long)e1), d2 = __longlong_as_double((long long)e2);
-    int rebuild = (!sc->listed) || (sqrt(d1) + sqrt(d2) > p.skin);
+    const float thr = s_s2 - 3.0f * e;
+    for (int q = R.base + threadIdx.x; q < n_slots; q += blockDim.x) {
+      if (__ldcg(d.state + q) != ST_LIVE) continue;
+      float4 Pf = __ldcg(d.posf + q), Of = __ldcg(d.posf_old + q);
+      float rdf = disp2f(Pf, Of);
+      if (!(rdf == rdf) || sqrtf(rdf) < thr) continue;
+      double4 P = ldcg_d4(d.pos + q), O = ldcg_d4(d.pos_old + q);
+      double rd = dot3(P.x - O.x, P.y - O.y, P.z - O.z);
+      if (rd == rd) top2_merge(e1, e2, (unsigned long long)__double_as_longlong(rd), tiny);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      unsigned long long c1 = __shfl_down_sync(0xffffffffu, e1, off);
+      unsigned long long c2 = __shfl_down_sync(0xffffffffu, e2, off);
+      top2_merge(e1, e2, c1, c2);
+    }
+    if (lane == 0) {
+      x1[wid] = e1;
+      x2[wid] = e2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long f1 = tiny, f2 = tiny;
+      for (int w = 0; w < nwarp; ++w) top2_merge(f1, f2, x1[w], x2[w]);
+      double d1 = __longlong_as_double((long long)f1), d2 = __longlong_as_double((long long)f2);
+      s_dec = sqrt(d1) + sqrt(d2) > p.skin ? 1 : 0;
+    }
+    __syncthreads();
+    rebuild = s_dec;
+  }
+  if (threadIdx.x == 0) {
     sc->rebuild = rebuild;
     if (rebuild) {
       sc->nupd += 1;
@@ -730,6 +898,7 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
     if (t2 == (unsigned)d.nrep - 1u) {
       int any = atomicAdd(&d.g->any_rebuild, 0);
       d.g->ticket_rep = 0;
+      if (any) d.g->near_stale = 1;  // lists change: the near entries too
       if (cond) cudaGraphSetConditional(cond_handle, any ? 1u : 0u);
     }
   }
@@ -751,6 +920,7 @@ __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int 
     int st = d.state[s];
     if (st == ST_LIVE) {
       d.pos_old[s] = d.pos[s];
+      d.posf_old[s] = d.posf[s];
     } else if (st == ST_LIMBO) {
       d.state[s] = ST_NULL;
       atomicMin(&sc->free_lo, s - R.base);  // the slot is free again
@@ -1018,6 +1188,11 @@ __global__ void rebuild_done_kernel(Dev d) {
 // commute, so each component is replayed in rank order by one thread and
 // gives exactly the reference's result.
 
+__global__ void delta_reset_kernel(Global* g) { g->delta2_bits = 0ull; }
+
+// Resets the component state and takes delta = max |pos - old_cg| over the
+// moving atoms (positions after the integrator; they do not change until
+// overlap_moveback except by whole box lengths).
 __global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
   // grids are sized by capacity; the block's replica gives the live count
   const int rep = block_rep(d);
@@ -1053,36 +1228,10 @@ __global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
     atomicMax(&d.g->delta2_bits, (unsigned long long)__double_as_longlong(dd));
 }
 
-__device__ int uf_find(volatile int* uf, int x) {
-  for (int it = 0; it < (1 << 22); ++it) {
-    int px = uf[x];
-    if (px == x) return x;
-    int ppx = uf[px];
-    if (ppx != px) atomicCAS((int*)&uf[x], px, ppx);
-    x = px;
-  }
-  return -1;
-}
-
-__device__ void uf_union(Global* g, volatile int* uf, int a, int b) {
-  for (int it = 0; it < (1 << 20); ++it) {
-    a = uf_find(uf, a);
-    b = uf_find(uf, b);
-    if (a < 0 || b < 0) break;
-    if (a == b) return;
-    if (a < b) {
-      int t = a;
-      a = b;
-      b = t;
-    }
-    if (atomicCAS((int*)&uf[a], a, b) == a) return;
-  }
-  raise_error(g, DML_E_OVERLAP_PASSES, -1);
-}
-
 // Near entries of every hs%ref member: list entries within rc + 2 delta
 // (FP32 with margin; a superset is harmless) in list order.
-__global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p, int n_rank) {
+__global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p, int gated) {
+  if (gated && !d.g->near_stale) return;  // the force scan found them
   int r = warp_id_global();  // grids are sized by capacity
   int lane = threadIdx.x & 31;
   const int rep = d.rep_of[r];
@@ -1092,9 +1241,7 @@ __global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p
   int h = d.ref[r];
   if (h < 0) return;
   // rc + 2 delta in FP32 (sqrtf is exact to an ulp; the margin covers it)
-  float delta = sqrtf(__double2float_ru(__longlong_as_double((long long)d.g->delta2_bits)));
-  float rnf = (p.rcf + 2.0f * delta) * 1.000001f + 4.0f * p.margin + 1e-3f;
-  float rn2 = rnf * rnf;
+  const float rn2 = near_radius2(d, p);
   float4 Pf = d.posf[h];
   int n = d.nn[h];
   const int* row = d.list + (size_t)h * p.mnb;
@@ -1143,7 +1290,6 @@ __global__ void overlap_count_kernel(Dev d, int n_rank) {
   // grids are sized by capacity; the block's replica gives the live count
   const int rep = block_rep(d);
   int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r == 0) d.g->delta2_bits = 0ull;
   if (r - d.rc[rep].base >= d.sc[rep].n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
@@ -1185,7 +1331,27 @@ __global__ void overlap_scatter_kernel(Dev d, int n_rank) {
   int root = d.uf[h];
   int cid = d.comp_id[root];
   int idx = d.comp_list[2 * cid] + atomicAdd(&d.comp_fill[root], 1);
-  d.comp_members[idx] = h;
+  d.comp_rank[idx] = r;  // the component's ranks, in no particular order
+}
+
+// Members of every component in rank order: each member's place is the
+// number of smaller ranks in its component (contiguous loads, all members
+// in parallel).
+__global__ void overlap_order_kernel(Dev d, int n_rank) {
+  // grids are sized by capacity; the block's replica gives the live count
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r - R.base >= sc->n_rank) return;
+  int h = d.ref[r];
+  if (h < 0 || !d.active[h]) return;
+  int cid = d.comp_id[d.uf[h]];
+  int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
+  const int* rk = d.comp_rank + off;
+  int before = 0;
+  for (int i = 0; i < sz; ++i) before += rk[i] < r;
+  d.comp_members[off + before] = h;
 }
 
 // Examination of o1 = x in pass `pass` (dana.F90:871-935).
@@ -1244,7 +1410,7 @@ __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, in
   }
 }
 
-// One thread per component; members sorted by rank first.  With
+// One thread per component, members in rank order.  With
 // `all_passes` (prob >= 1: a contact capture never fails, so no atom is left
 // with skip = false unless an ion was moved back in its own component) the
 // component runs every pass itself: pass p of the reference examines exactly
@@ -1255,17 +1421,7 @@ __global__ void overlap_pass1_kernel(Dev d, KParams p, int all_passes) {
   int cid = blockIdx.x * blockDim.x + threadIdx.x;
   if (cid >= d.g->n_comp) return;
   int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
-  int* mem = d.comp_members + off;
-  for (int i = 1; i < sz; ++i) {
-    int v = mem[i];
-    int rv = d.rank[v];
-    int q = i;
-    while (q > 0 && d.rank[mem[q - 1]] > rv) {
-      mem[q] = mem[q - 1];
-      --q;
-    }
-    mem[q] = v;
-  }
+  const int* mem = d.comp_members + off;
   int pass = 1;
   for (;;) {
     int again = 0;
@@ -1471,6 +1627,29 @@ __device__ int blk_scan_excl(int v, int* total) {
   return r;
 }
 
+// First index in [lo, hi) where pred holds, or INT_MAX; every thread of the
+// block calls it (the result lands in *s_res and is returned to all).  Each
+// thread tests 8 strided indices per round, so the loads of a round are
+// independent and a round covers 8 * blockDim.x indices.
+template <class Pred>
+__device__ int blk_find_first(int lo, int hi, Pred pred, int* s_res) {
+  if (threadIdx.x == 0) *s_res = INT_MAX;
+  __syncthreads();
+  for (int base = lo; base < hi; base += 8 * (int)blockDim.x) {
+    int best = INT_MAX;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      int i = base + k * (int)blockDim.x + (int)threadIdx.x;
+      if (i < hi && pred(i)) best = min(best, i);
+    }
+    if (best != INT_MAX) atomicMin(s_res, best);
+    if (__syncthreads_or(best != INT_MAX)) break;
+  }
+  int r = *s_res;
+  __syncthreads();
+  return r;
+}
+
 // Stable in-place compaction of an order array (holes = -1); pos_of[h]
 // receives the new position of every member.
 __device__ int blk_compact(int* arr, int off, int n, int* pos_of) {
@@ -1568,14 +1747,25 @@ __device__ void gcmc_own_list(const Dev& d, const KParams& p, const RepConst& R,
 }
 
 constexpr int kGcmcThreads = 256;
+constexpr int kGcmcTrialBatch = 256;  // trials drawn ahead into shared memory
 
 __device__ __forceinline__ bool in_slab(double z, double z0, double zmax) {
   return !(z < z0) && !(z > zmax);
 }
 
+// One trial of gcmc_run: its uniforms (coin, acceptance, the three
+// coordinates, the pick) and trial point, drawn before the trials run.
+struct GcmcTrial {
+  double coin, uacc, upick;
+  double4 r;   // trial point (x, y, z)
+  float4 rf;   // its FP32 copy
+};
+
 // Linear index of stencil cell `nabor` (map order) around the point's cell.
-__device__ __forceinline__ int stencil_cell(const RepConst& R, double4 P, int nabor) {
-  int rc[3] = {cell_index(P.x, R.cell[0]), cell_index(P.y, R.cell[1]), cell_index(P.z, R.cell[2])};
+__device__ __forceinline__ int stencil_cell(const RepConst& R, float4 Pf, const double4* P,
+                                            int nabor) {
+  int rc[3];
+  cell_index3(R, Pf, P, rc[0], rc[1], rc[2]);
   int nc[3];
   for (int k = 0; k < 3; ++k) {
     int t = c_map[nabor][k] + rc[k] - 1;
@@ -1599,7 +1789,10 @@ __device__ __forceinline__ int stencil_cell(const RepConst& R, double4 P, int na
 // velocity) are tracked across trials.  Replicas without cells, or with an
 // atom in a halo cell, scan the whole group as the reference does.
 __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
-  extern __shared__ int s_chunk[];  // in-slab members per gorder chunk
+  // dynamic shared memory: the trials, then in-slab members per gorder chunk
+  extern __shared__ double4 s_dyn[];
+  GcmcTrial* const s_tr = (GcmcTrial*)s_dyn;
+  int* const s_chunk = (int*)(s_tr + kGcmcTrialBatch);
   const int rep = blockIdx.x;
   const RepConst& R = d.rc[rep];
   Scalars* const sc_g = d.sc + rep;
@@ -1611,6 +1804,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
   const int nw = nt >> 5;
   __shared__ int s_first, s_last, s_n, s_slot, s_bslot, s_sel, s_dpre, s_pick, s_ppos;
+  __shared__ int s_dec, s_m;
   __shared__ int s_cells[27], s_dup[27], s_start[27], s_pre[28], s_ca[27], s_cc[27];
   __shared__ int s_ccin[27], s_cbase[27];
   constexpr int KF = 8;  // flattened stencil entries a thread keeps in registers
@@ -1624,6 +1818,27 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
   const double z0 = sc->z0, zmax = sc->zmax;
   const double v = R.box[0] * R.box[1] * (zmax - z0);
   __shared__ int s_fast;
+  // the trials' draws (the ran() calls of dana.F90:620-690, keyed Philox
+  // here), kGcmcTrialBatch trials at a time
+  auto draw_trials = [&](int t0) {
+    __syncthreads();
+    for (int i = tid; i < kGcmcTrialBatch && t0 + i <= p.nadj; i += nt) {
+    const int t = t0 + i - 1;
+    dml_u4 w0 = dml_draw(R.seed, step, (uint64_t)(t + 1), DML_RNG_GCMC, 0);
+    dml_u4 w1 = dml_draw(R.seed, step, (uint64_t)(t + 1), DML_RNG_GCMC, 1);
+    dml_u4 w2 = dml_draw(R.seed, step, (uint64_t)(t + 1), DML_RNG_GCMC, 2);
+    GcmcTrial tr;
+    tr.coin = dml_u53(w0.w[0], w0.w[1]);
+    tr.uacc = dml_u53(w0.w[2], w0.w[3]);
+    double r0 = dml_u53(w1.w[0], w1.w[1]) * R.box[0];
+    double r1 = dml_u53(w1.w[2], w1.w[3]) * R.box[1];
+    double r2 = dml_u53(w2.w[0], w2.w[1]) * (zmax - z0) + z0;
+    tr.r = make_double4(r0, r1, r2, 0.0);
+    tr.rf = make_float4((float)r0, (float)r1, (float)r2, 0.0f);
+    tr.upick = dml_u53(w2.w[2], w2.w[3]);
+    s_tr[i] = tr;
+    }
+  };
   if (R.use_cells)
     for (int c = tid; c < R.ncell; c += nt) d.ins_head[R.cell_off + c] = -1;
   // order arrays grow by appends: compact them before they could overflow
@@ -1677,7 +1892,9 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
     }
   }
   for (int t = 1; t <= p.nadj; ++t) {
+    if ((t - 1) % kGcmcTrialBatch == 0) draw_trials(t);
     __syncthreads();
+    const GcmcTrial& tr = s_tr[(t - 1) % kGcmcTrialBatch];
     const int n = s_n, first = s_first, last = s_last;
     const bool fast = s_fast != 0;
     if (first == INT_MAX) {
@@ -1685,19 +1902,27 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
       break;
     }
     const int ng = sc->n_gorder;
-    const int href = d.gorder[B + first], hlast = d.gorder[B + last];
-    dml_u4 w0 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 0);
-    dml_u4 w1 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 1);
-    dml_u4 w2 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 2);
-    double coin = dml_u53(w0.w[0], w0.w[1]);
-    double uacc = dml_u53(w0.w[2], w0.w[3]);
-    if (coin < 0.5) {
+    // Metropolis decisions in one thread (FP64 on GB300's narrow pipe)
+    if (tid == 0) {
+      int dec;
+      if (tr.coin < 0.5) {
+        dec = (p.act * v / (double)(n + 1) < tr.uacc) ? 0 : 1;  // creation
+      } else {
+        dec = ((double)n / (v * p.act) < tr.uacc) ? 0 : 2;    // destruction
+        int m = (int)floor(tr.upick * (double)n) + 1;
+        s_m = m > n ? n : m;
+      }
+      s_dec = dec;
+    }
+    __syncthreads();
+    const int dec = s_dec;
+    if (dec == 0) continue;
+    const int hlast = d.gorder[B + last];
+    if (dec == 1) {
       // creation attempt (dana.F90:627-677)
-      if (p.act * v / (double)(n + 1) < uacc) continue;
-      double r0 = dml_u53(w1.w[0], w1.w[1]) * R.box[0];
-      double r1 = dml_u53(w1.w[2], w1.w[3]) * R.box[1];
-      double r2 = dml_u53(w2.w[0], w2.w[1]) * (zmax - z0) + z0;
-      double4 Rt = make_double4(r0, r1, r2, 0.0);
+      const int href = d.gorder[B + first];
+      const double4 Rt = tr.r;
+      const float4 Rtf = tr.rf;
       bool ov = false;
       // stencil entries (cell atoms) of this thread: slot, list flags, cell
       int fj[KF];
@@ -1705,7 +1930,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
       bool flat = false;
       if (fast) {
         if (tid < 27) {
-          int c = stencil_cell(R, Rt, tid);
+          int c = stencil_cell(R, Rtf, &Rt, tid);
           int st = d.cell_start[c];
           s_cells[tid] = c;
           s_start[tid] = st;
@@ -1747,15 +1972,33 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
           }
           const int q = lo;
           const int j = d.cell_atoms[s_start[q] + f - s_pre[q]];
-          double vx, vy, vz;  // distance(o%pos, r, o%pbc) = r - o%pos
-          vdist_nint(R, Rt, d.pos[j], vx, vy, vz);
-          const double rd = dot3(vx, vy, vz);
-          if (d.in_gcmc[j] && rd < p.rc2) ov = true;
-          if (flat) {
+          // FP32 distance decides outside the margins; FP64 (the
+          // reference's vdistance, r - o%pos) inside them
+          float fx, fy, fz;
+          vdist_nint_f(R, Rtf, d.posf[j], fx, fy, fz);
+          const float df = fx * fx + fy * fy + fz * fz;
+          double rd = -1.0;
+          auto exact = [&]() {
+            if (rd < 0.0) {
+              double vx, vy, vz;
+              vdist_nint(R, Rt, d.pos[j], vx, vy, vz);
+              rd = dot3(vx, vy, vz);
+            }
+            return rd;
+          };
+          if (df <= p.rc_hi2 && d.in_gcmc[j] && (df < p.rc_lo2 || exact() < p.rc2)) ov = true;
+          if (flat && df <= p.rlist_hi2) {
             const bool live = d.state[j] == ST_LIVE;
+            bool own, app;
+            if (df < p.rlist_lo2) {
+              own = app = true;
+            } else {
+              own = exact() < p.rlist2;
+              app = !(exact() > p.rlist2);
+            }
             int fl = 0;
-            if (live && rd < p.rlist2) fl |= 1;  // own list (ngroup_cells_atom)
-            if (live && !s_dup[q] && d.rank[j] >= 0 && !(rd > p.rlist2)) fl |= 2;  // append
+            if (live && own) fl |= 1;  // own list (ngroup_cells_atom)
+            if (live && app && !s_dup[q] && d.rank[j] >= 0) fl |= 2;  // append
 #pragma unroll
             for (int kk = 0; kk < KF; ++kk)
               if (kk == k) {
@@ -1785,34 +2028,21 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
       // first free hs slot (limbo slots are not free) and hs%b slot
       const int nat = sc->n_atoms + 1, bnat = sc->b_nat + 1;
       const int ns = sc->n_slots, nb = sc->n_b;
-      if (wid == 0) {
-        int res = ns;
-        if (ns >= nat + sc->nlimbo) {
-          res = INT_MAX;
-          for (int base = sc->free_lo; base < ns; base += 32) {
-            int i = base + lane;
-            unsigned m = __ballot_sync(0xffffffffu, i < ns && d.state[B + i] == ST_NULL);
-            if (m) {
-              res = base + __ffs(m) - 1;
-              break;
-            }
-          }
+      {
+        const int8_t* st = d.state + B;
+        const int* b2 = d.b2hs + B;
+        int res = ns >= nat + sc->nlimbo
+                      ? blk_find_first(sc->free_lo, ns, [&](int i) { return st[i] == ST_NULL; },
+                                       &s_slot)
+                      : ns;
+        int bres = nb >= bnat
+                       ? blk_find_first(sc->bfree_lo, nb, [&](int b) { return b2[b] < 0; },
+                                        &s_bslot)
+                       : nb;
+        if (tid == 0) {
+          s_slot = res;
+          s_bslot = bres;
         }
-        if (lane == 0) s_slot = res;
-      } else if (wid == 1) {
-        int res = nb;
-        if (nb >= bnat) {
-          res = INT_MAX;
-          for (int base = sc->bfree_lo; base < nb; base += 32) {
-            int b = base + lane;
-            unsigned m = __ballot_sync(0xffffffffu, b < nb && d.b2hs[B + b] < 0);
-            if (m) {
-              res = base + __ffs(m) - 1;
-              break;
-            }
-          }
-        }
-        if (lane == 0) s_bslot = res;
       }
       __syncthreads();
       const int lslot = s_slot, lbs = s_bslot;  // local hs and hs%b slots
@@ -1839,6 +2069,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
         d.typ[slot] = (int8_t)typ;
         d.pos[slot] = Rt;
         d.pos_old[slot] = Rt;
+        d.posf_old[slot] = Rtf;
         d.old_cg[slot] = make_double4(1e8, 1e8, 1e8, 0.0);
         d.posf[slot] = to_f4(Rt, typ);
         d.skip[slot] = 0;
@@ -1846,7 +2077,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
         sc->next_id += 1;
         d.ev_count[slot] = 0;
         // Maxwell velocity to the last listed atom (dana.F90:666-668)
-        double beta = sqrt(p.beta_num / p.mass[typ - 1]);
+        const double beta = p.beta_t[typ - 1];
         double nv[4];
         dml_normal_quad(dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC_VEL, 0), nv);
         d.vel[hlast] = make_double4(beta * nv[0], beta * nv[1], beta * nv[2], 0.0);
@@ -1868,8 +2099,8 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
         sc->b_nat = bnat;
         sc->bfree_lo = lbs + 1;
         if (R.use_cells) {
-          int c1 = cell_index(Rt.x, R.cell[0]), c2 = cell_index(Rt.y, R.cell[1]),
-              c3 = cell_index(Rt.z, R.cell[2]);
+          int c1, c2, c3;
+          cell_index3(R, Rtf, &Rt, c1, c2, c3);
           if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] + 1 || c2 > R.ncells[1] + 1 ||
               c3 > R.ncells[2] + 1) {
             raise_error(d.g, DML_E_OUT_OF_TESSELLATION, slot);
@@ -2003,10 +2234,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
       }
     } else {
       // destruction attempt (dana.F90:680-707)
-      if ((double)n / (v * p.act) < uacc) continue;
-      double upick = dml_u53(w2.w[2], w2.w[3]);
-      int m = (int)floor(upick * (double)n) + 1;
-      if (m > n) m = n;
+      const int m = s_m;
       int hsel = -1, psel = -1;
       if (m <= 0) {
         hsel = hlast;  // the walk never reaches m == 0 and ends on the last atom
@@ -2072,8 +2300,8 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
           sc->n_ref -= 1;
         }
         if (R.use_cells) {
-          int c1 = cell_index(P.x, R.cell[0]), c2 = cell_index(P.y, R.cell[1]),
-              c3 = cell_index(P.z, R.cell[2]);
+          int c1, c2, c3;
+          cell_index3(R, pf, &P, c1, c2, c3);
           if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] || c2 > R.ncells[1] || c3 > R.ncells[2])
             raise_error(d.g, DML_E_UNSUPPORTED, h);  // tessellation dropped (Cells.F90:320-327)
         }
@@ -2136,8 +2364,8 @@ __global__ void flush_kernel(uint4* buf, size_t n) {
 
 }  // namespace
 
-int k_step_begin(const Dev& d, cudaStream_t s) {
-  step_begin_kernel<<<1, 1, 0, s>>>(d.g);
+int k_step_begin(const Dev& d, int near_stale, cudaStream_t s) {
+  step_begin_kernel<<<1, 1, 0, s>>>(d.g, near_stale);
   return 1;
 }
 
@@ -2151,8 +2379,11 @@ int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   return 1;
 }
 
-int k_force_pairs(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
-  force_scan_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+int k_force_pairs(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s) {
+  if (near)
+    force_scan_kernel<true><<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  else
+    force_scan_kernel<false><<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
   if (p.mixed)
     force_exact_mixed_kernel<<<152 * 4, kBlock, 0, s>>>(d, p);
   else
@@ -2211,17 +2442,29 @@ int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, 
   return n + 1;
 }
 
-int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, cudaStream_t s) {
+int k_overlap_prepare(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
   overlap_init_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
-  overlap_detect_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  return 1;
+}
+
+int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool standalone,
+              cudaStream_t s) {
+  int n = 0;
+  if (standalone) {
+    delta_reset_kernel<<<1, 1, 0, s>>>(d.g);
+    n += 1 + k_overlap_prepare(d, p, n_slots, s);
+  }
+  overlap_detect_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, standalone ? 0 : 1);
   overlap_count_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
   overlap_assign_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, n_slots);
   overlap_scatter_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
+  overlap_order_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
   int all_passes = p.prob >= 1.0;
   overlap_pass1_kernel<<<nblk(n_rank, 128), 128, 0, s>>>(d, p, all_passes);
-  if (all_passes) return 6;
+  n += 6;
+  if (all_passes) return n;
   overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
-  return 7;
+  return n + 1;
 }
 
 int k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
@@ -2249,7 +2492,8 @@ int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
     cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot, 1);
     n += 4;
   }
-  size_t shm = sizeof(int) * (size_t)(d.max_rep_cap / kGcmcThreads + 2);
+  size_t shm = sizeof(GcmcTrial) * (size_t)kGcmcTrialBatch +
+               sizeof(int) * (size_t)(d.max_rep_cap / kGcmcThreads + 2);
   if (shm > 48 * 1024)
     cudaFuncSetAttribute(gcmc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
   gcmc_kernel<<<d.nrep, kGcmcThreads, shm, s>>>(d, p);
