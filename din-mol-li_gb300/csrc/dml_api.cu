@@ -124,6 +124,7 @@ void make_kparams(const dml_params& P, double maxc, KParams& K) {
       K.c12[i][j] = r0 > 0.0 ? 12.0 * eps / (r0 * r0) : 0.0;
     }
   for (int t = 0; t < 3; ++t) K.mass[t] = P.mass[t];
+  for (int t = 0; t < 3; ++t) K.inv_mass[t] = 1.0 / P.mass[t];
   // set_ermak (dana.F90:947-971)
   const double h = P.h, gama = P.gamma;
   double cc0 = std::exp(-h * gama);

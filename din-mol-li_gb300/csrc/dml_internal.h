@@ -124,6 +124,7 @@ struct KParams {
   float rcf;                // rc (FP32, pre-filters)
   float rc_lo2, rc_hi2;     // (rc -+ margin)^2: FP32 hard-core test decided outside
   double beta_t[3];         // sqrt(kB T / m) per element (gcmc_run's Maxwell draw)
+  double inv_mass[3];       // 1 / m (ermak_b of the mixed form)
   double fix_scale, fix_inv; // 2^32 per eV/Å in ui/Å, and its inverse
   float rlist_lo2, rlist_hi2; // list shell bounds (FP32)
   float margin;             // FP32 position error bound

@@ -342,91 +342,85 @@ __device__ __forceinline__ float near_radius2(const Dev& d, const KParams& p) {
 }
 
 // ---------------------------------------------------------------- fuerza
-// FP32 pre-filter of one entry: true when the entry may interact.  The
-// element of a non-live slot (limbo, Neighbor.F90:1089-1092) is 0 in posf.
-__device__ __forceinline__ bool force_candidate(const KParams& p, const RepConst& R, float4 Pf,
-                                                int k, float4 Q, int& m) {
-  m = elem_of(Q);
-  if (m == 0) return false;
-  if (k == DML_Z_CG && m == DML_Z_CG) return false;
-  if (!p.pair_on[k - 1][m - 1]) return false;  // eps = 0: contributes signed zeros only
-  float fx = Pf.x - Q.x, fy = Pf.y - Q.y, fz = Pf.z - Q.z;
-  if (fx > R.halfboxf[0]) fx -= R.boxf[0]; else if (fx < -R.halfboxf[0]) fx += R.boxf[0];
-  if (fy > R.halfboxf[1]) fy -= R.boxf[1]; else if (fy < -R.halfboxf[1]) fy += R.boxf[1];
-  float drf = fx * fx + fy * fy + fz * fz;
-  return drf <= p.r0f_pref2[k - 1][m - 1];
-}
-
-// Pass 1: one warp per hs%ref member scans its list row (two entries per
-// lane in flight) with the FP32 pre-filter and appends every possibly
-// interacting entry (r <= r0 + margin, eps != 0) to a compact queue.
+// Pass 1: the hs%ref members' list rows are scanned with the FP32
+// pre-filter and every possibly interacting entry (r <= r0 + margin,
+// eps != 0, not CG-CG) is appended to a compact queue.
 // On GB300 an FP64 instruction occupies the narrow FP64 pipe for the whole
 // warp whatever its active lanes, so the exact FP64 work is done afterwards
 // on the dense queue (force_exact_kernel), 32 entries per instruction.
 template <bool NEAR>
 __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n_rank) {
-  int r = warp_id_global();  // grids are sized by capacity
-  int lane = threadIdx.x & 31;
+  // Two hs%ref members per warp, one per half-warp, so that the dependent
+  // loads of two rows overlap; each lane keeps 4 entries in flight.
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, hl = lane & 15, half = lane >> 4;
+  const unsigned hmask = half ? 0xffff0000u : 0x0000ffffu;
+  const int r = 2 * warp_id_global() + half;  // grids are sized by capacity
   const int rep = d.rep_of[r];
   const RepConst& R = d.rc[rep];
-  Scalars* sc = d.sc + rep;
-  if (r - R.base >= sc->n_rank) return;
-  int h = d.ref[r];
-  if (h < 0) return;
-  int k = d.typ[h];
-  float4 Pf = d.posf[h];
-  int n = d.nn[h];
-  const int* row = d.list + (size_t)h * p.mnb;
+  int h = -1, k = 0, n = 0;
+  float4 Pf = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (r - R.base < d.sc[rep].n_rank) h = d.ref[r];
+  if (h >= 0) {
+    k = d.typ[h];
+    Pf = d.posf[h];
+    n = d.nn[h];
+  }
+  const int nmax = max(n, __shfl_xor_sync(FULL, n, 16));
+  if (nmax == 0) return;  // both halves idle
+  const int* row = d.list + (size_t)(h >= 0 ? h : 0) * p.mnb;
   // With NEAR the same pass records overlap_moveback's near entries (list
-  // entries within rc + 2 delta, list order) and unites their components.
+  // entries within rc + 2 delta, in list order) and unites their components.
   const float rn2 = NEAR ? near_radius2(d, p) : 0.0f;
-  int* near = d.near + (size_t)h * kNearCap;
+  int* near = d.near + (size_t)(h >= 0 ? h : 0) * kNearCap;
   int ncnt = 0;
   bool any = false;
-  for (int base = 0; base < n; base += 64) {
-    int jj0 = base + lane, jj1 = jj0 + 32;
-    int j0 = jj0 < n ? __ldg(row + jj0) : -1;
-    int j1 = jj1 < n ? __ldg(row + jj1) : -1;
-    float4 Q0 = make_float4(0.f, 0.f, 0.f, 0.f), Q1 = Q0;
-    if (j0 >= 0) Q0 = d.posf[j0];
-    if (j1 >= 0) Q1 = d.posf[j1];
-    int m0, m1;
-    bool c0 = j0 >= 0 && force_candidate(p, R, Pf, k, Q0, m0);
-    bool c1 = j1 >= 0 && force_candidate(p, R, Pf, k, Q1, m1);
-    unsigned b0 = __ballot_sync(0xffffffffu, c0), b1 = __ballot_sync(0xffffffffu, c1);
-    int tot = __popc(b0) + __popc(b1);
-    if (tot != 0) {
-      int base_q = 0;
-      if (lane == 0) base_q = atomicAdd(&d.g->n_cand, tot);
-      base_q = __shfl_sync(0xffffffffu, base_q, 0);
-      unsigned lt = (1u << lane) - 1u;
-      if (c0) {
-        int q = base_q + __popc(b0 & lt);
-        if (q < p.cand_cap) d.cand[q] = make_int4(r, jj0, h, j0);
-      }
-      if (c1) {
-        int q = base_q + __popc(b0) + __popc(b1 & lt);
-        if (q < p.cand_cap) d.cand[q] = make_int4(r, jj1, h, j1);
-      }
-    }
-    if (NEAR) {
+  const unsigned lt = (1u << lane) - 1u;
+  for (int base = 0; base < nmax; base += 64) {
+    int j[4];
+    float4 Q[4];
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        int j = half ? j1 : j0;
-        float4 Q = half ? Q1 : Q0;
-        bool inc = false;
-        if (j >= 0 && elem_of(Q) != 0) {
-          float fx, fy, fz;
-          vdist_nint_f(R, Pf, Q, fx, fy, fz);
-          inc = fx * fx + fy * fy + fz * fz <= rn2;
+    for (int u = 0; u < 4; ++u) {
+      int jj = base + 16 * u + hl;
+      j[u] = jj < n ? __ldg(row + jj) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) Q[u] = j[u] >= 0 ? d.posf[j[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      // one FP32 minimum-image distance serves both tests; the element of
+      // a slot that is not live (limbo, Neighbor.F90:1089-1092) is 0
+      const int m = elem_of(Q[u]);
+      const bool live = j[u] >= 0 && m != 0;
+      float df = 0.0f;
+      if (live) {
+        float fx = Pf.x - Q[u].x, fy = Pf.y - Q[u].y, fz = Pf.z - Q[u].z;
+        if (fx > R.halfboxf[0]) fx -= R.boxf[0]; else if (fx < -R.halfboxf[0]) fx += R.boxf[0];
+        if (fy > R.halfboxf[1]) fy -= R.boxf[1]; else if (fy < -R.halfboxf[1]) fy += R.boxf[1];
+        df = fx * fx + fy * fy + fz * fz;
+      }
+      // fuerza: r <= r0 + margin, eps != 0, not CG-CG (signed zeros only)
+      const bool cand = live && !(k == DML_Z_CG && m == DML_Z_CG) && p.pair_on[k - 1][m - 1] &&
+                        df <= p.r0f_pref2[k - 1][m - 1];
+      const unsigned bc = __ballot_sync(FULL, cand);
+      if (bc) {
+        int base_q = 0;
+        if (lane == 0) base_q = atomicAdd(&d.g->n_cand, __popc(bc));
+        base_q = __shfl_sync(FULL, base_q, 0);
+        if (cand) {
+          int q = base_q + __popc(bc & lt);
+          if (q < p.cand_cap) d.cand[q] = make_int4(r, base + 16 * u + hl, h, j[u]);
         }
-        unsigned bal = __ballot_sync(0xffffffffu, inc);
-        int pre = __popc(bal & ((1u << lane) - 1u));
+      }
+      if (NEAR) {
+        const bool inc = live && df <= rn2;
+        const unsigned bal = __ballot_sync(FULL, inc) & hmask;
         if (inc) {
-          if (ncnt + pre < kNearCap) near[ncnt + pre] = j;
-          if (elem_of(Q) != DML_Z_CG) {
-            uf_union(d.g, (volatile int*)d.uf, h, j);
-            d.active[j] = 1;
+          int pre = __popc(bal & lt);
+          if (ncnt + pre < kNearCap) near[ncnt + pre] = j[u];
+          if (m != DML_Z_CG) {
+            uf_union(d.g, (volatile int*)d.uf, h, j[u]);
+            d.active[j[u]] = 1;
           }
         }
         ncnt += __popc(bal);
@@ -434,7 +428,7 @@ __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n
       }
     }
   }
-  if (NEAR && lane == 0) {
+  if (NEAR && hl == 0 && h >= 0) {
     d.near_count[h] = ncnt > kNearCap ? -1 : ncnt;
     if (any) d.active[h] = 1;
   }
@@ -515,6 +509,22 @@ __device__ __forceinline__ void ermak_b_atom(const Dev& d, const KParams& p, int
   d.acel[h] = A;
 }
 
+// ermak_b of the mixed form: F/m as F * (1/m) (one FP64 multiply instead of
+// a division; the FP64 divide is a long sequence on GB300's narrow FP64
+// pipe), so the velocities differ from the plain form in the last bits.
+__device__ __forceinline__ void ermak_b_atom_mixed(const Dev& d, const KParams& p, int h, int typ,
+                                                   double4 F) {
+  if (typ == DML_Z_CG) return;
+  const double im = p.inv_mass[typ - 1];
+  double4 V = d.vel[h], A = d.acel[h], R = d.ranv[h];
+  double ax = F.x * im, ay = F.y * im, az = F.z * im;
+  V.x = p.cc0 * V.x + p.cc1mcc2 * A.x + p.cc2 * ax + R.x;
+  V.y = p.cc0 * V.y + p.cc1mcc2 * A.y + p.cc2 * ay + R.y;
+  V.z = p.cc0 * V.z + p.cc1mcc2 * A.z + p.cc2 * az + R.z;
+  d.vel[h] = V;
+  d.acel[h] = make_double4(ax, ay, az, 0.0);
+}
+
 // Pass 2: one thread per hs slot sums its recorded entries in key order,
 // i.e. in the reference's global accumulation order (hs%ref order x list
 // order, with the Newton reaction applied to both atoms of every entry).
@@ -589,7 +599,10 @@ __global__ void ermak_b_kernel(Dev d, KParams p, int n_rank) {
   if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
-  ermak_b_atom(d, p, h, d.typ[h], d.force[h]);
+  if (p.mixed)
+    ermak_b_atom_mixed(d, p, h, d.typ[h], d.force[h]);
+  else
+    ermak_b_atom(d, p, h, d.typ[h], d.force[h]);
 }
 
 
@@ -675,7 +688,11 @@ __global__ void force_fix_kernel(Dev d, KParams p, int n_slots) {
   double4 F;
   double ep;
   const double inv = p.fix_inv;
-  if (inref) {
+  if (inref && !any) {
+    // no pair inside r0: the sums are zero (no FP64 conversion needed)
+    F = make_double4(0.0, 0.0, 0.0, 0.0);
+    ep = 0.0;
+  } else if (inref) {
     F = make_double4((double)ax * inv, (double)ay * inv, (double)az * inv, 0.0);
     ep = (double)ae * inv;
   } else {
@@ -693,7 +710,7 @@ __global__ void force_fix_kernel(Dev d, KParams p, int n_slots) {
   }
   d.force[s] = F;
   d.epot[s] = ep;
-  if (FUSE_B && inref) ermak_b_atom(d, p, s, d.typ[s], F);
+  if (FUSE_B && inref) ermak_b_atom_mixed(d, p, s, d.typ[s], F);
 }
 
 // ----------------------------------------------------------- test_update
@@ -2380,10 +2397,12 @@ int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
 }
 
 int k_force_pairs(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s) {
+  // two hs%ref members per warp
+  const int nb = nblk_warps((n_rank + 1) / 2);
   if (near)
-    force_scan_kernel<true><<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+    force_scan_kernel<true><<<nb, kBlock, 0, s>>>(d, p, n_rank);
   else
-    force_scan_kernel<false><<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+    force_scan_kernel<false><<<nb, kBlock, 0, s>>>(d, p, n_rank);
   if (p.mixed)
     force_exact_mixed_kernel<<<152 * 4, kBlock, 0, s>>>(d, p);
   else
