@@ -10,7 +10,8 @@ Workloads (seeded synthetic systems; the reference measures no dataset):
   c5 (default)  config 5: a batch of independent replicas, each a 40 x 40 x
                 2-cell bcc Li electrode (6400 atoms, 140.4 Å square) under
                 20 000 Li+ in a 300 Å box, GCMC reservoir slab z in [200, 300]
-                with 128 trials per step, Ermak, dt = 1 fs, skin 10 Å.  Timed
+                with 128 trials per step, Ermak, dt = 1 fs, skin 2 Å (the
+                neighbour shell of the reference's GCMC run).  Timed
                 in the chosen form (mixed precision, all replicas in every
                 launch); the same batch in plain FP64 and a sample of replicas
                 run one per context in plain FP64 are timed beside it.
@@ -183,7 +184,7 @@ class Workload:
             self.n_electrode = 2 * systems.C5_CELLS ** 2 * 2 * n_rep
             self.desc = ("config 5: %d replicas x (40x40x2-cell bcc Li electrode, 6400 atoms, "
                          "+ 20000 Li+), 140.4x140.4x300 A, GCMC reservoir z in [200,300] with "
-                         "%d trials/step, Ermak dt=1fs, skin 10" % (n_rep, self.p.nadj))
+                         "%d trials/step, Ermak dt=1fs, skin 2" % (n_rep, self.p.nadj))
         elif name == "c2":
             self.batched = False
             self.p = systems.c2_params(seed=1234 + rank)

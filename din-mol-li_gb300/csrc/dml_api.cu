@@ -211,7 +211,7 @@ int set_step(dml_ctx* c, int64_t step) {
 // test_update inside a graph capture: the displacement-test kernel sets the
 // condition of an IF node whose body is the rebuild (update(), Neighbor.F90:
 // 608-633), so steps without a rebuild launch no rebuild kernel at all.
-int capture_test_update(dml_ctx* c, int* n_base, int* n_body) {
+int capture_test_update(dml_ctx* c, int* n_base, int* n_body, bool near_in_body) {
   cudaStream_t s = c->stream;
   cudaStreamCaptureStatus st;
   cudaGraph_t g;
@@ -232,6 +232,8 @@ int capture_test_update(dml_ctx* c, int* n_base, int* n_body) {
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CK(cudaStreamBeginCaptureToGraph(c->aux, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
   *n_body += k_rebuild(c->D, c->K, c->D.cap, c->D.cap, c->D.cap, c->aux);
+  // the rebuilt lists need overlap_moveback's near entries searched again
+  if (near_in_body) *n_body += k_overlap_detect(c->D, c->K, c->D.cap, 2, c->aux);
   cudaGraph_t outg;
   CK(cudaStreamEndCapture(c->aux, &outg));
   CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
@@ -253,33 +255,36 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
   auto mark = [&](int i) {
     if (ev) cudaEventRecord(ev[i], s);
   };
-  auto test_update = [&]() -> int {
-    if (capture) return capture_test_update(c, &n, &nb);
+  const bool ermak_ = c->P.integrator == DML_INTEGRATOR_ERMAK;
+  auto test_update = [&](bool first) -> int {
+    if (capture) return capture_test_update(c, &n, &nb, first && ermak_);
     n += k_test_update(d, k, cap, cap, cap, s);
     return 0;
   };
   mark(DML_PHASE_INTEGRATE);
   const bool ermak = c->P.integrator == DML_INTEGRATOR_ERMAK;
   n += k_step_begin(d, ermak ? 0 : 1, s);
+  n += k_rank_prefix(d, s);
   if (ermak) {
-    n += k_ermak_a(d, k, cap, s);
-    n += k_overlap_prepare(d, k, cap, s);
+    n += k_ermak_a(d, k, cap, s);  // + overlap_moveback's reset and delta
     mark(DML_PHASE_FORCE_PAIRS);
     n += k_force_pairs(d, k, cap, true, s);  // + overlap_moveback's near entries
     mark(DML_PHASE_FORCE_SUM);
     n += k_force_sum(d, k, cap, true, s);  // fuerza + ermak_b
   } else {
-    n += k_brownian(d, k, cap, s);
-    n += k_overlap_prepare(d, k, cap, s);
+    n += k_brownian(d, k, cap, s);  // + overlap_moveback's reset and delta
     mark(DML_PHASE_FORCE_PAIRS);
     mark(DML_PHASE_FORCE_SUM);
   }
   mark(DML_PHASE_TEST_UPDATE1);
-  if ((rc = test_update()) != 0) return rc;
+  if ((rc = test_update(true)) != 0) return rc;
   mark(DML_PHASE_OVERLAP);
-  n += k_overlap(d, k, cap, cap, false, s);
+  // near entries: found by the force scan (Ermak), searched again inside
+  // the first test_update's rebuild node (graph) or when stale (eager);
+  // the Brownian step has no force scan and always searches here
+  n += k_overlap(d, k, cap, cap, false, !ermak ? 2 : (capture ? 0 : 1), s);
   mark(DML_PHASE_TEST_UPDATE2);
-  if ((rc = test_update()) != 0) return rc;
+  if ((rc = test_update(false)) != 0) return rc;
   mark(DML_PHASE_COMMIT);
   n += k_capture_commit(d, k, cap, s);
   mark(DML_PHASE_GCMC);
@@ -553,6 +558,8 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.g, 1);
   AL(d.rc, nrep);
   AL(d.rep_of, cap);
+  AL(d.rank_pre, nrep + 1);
+  AL(d.big_cells, ncell + 1);
 #undef AL
 
   // Host staging, position order (replica r at [base, base + cap)).
@@ -674,6 +681,7 @@ int dml_set_atoms(dml_ctx* c, const dml_atoms* a) {
 
 int dml_test_update(dml_ctx* c, int32_t* rebuilt) {
   if (!c || !c->loaded) return DML_E_STATE;
+  k_rank_prefix(c->D, c->stream);  // rows in use of every replica
   k_test_update(c->D, c->K, c->D.cap, c->D.cap, c->D.cap, c->stream);
   int rc = finish(c);
   if (rc) return rc;
@@ -686,6 +694,7 @@ int dml_test_update(dml_ctx* c, int32_t* rebuilt) {
 
 int dml_force(dml_ctx* c) {
   if (!c || !c->loaded) return DML_E_STATE;
+  k_rank_prefix(c->D, c->stream);  // rows in use of every replica
   k_force_pairs(c->D, c->K, c->D.cap, false, c->stream);
   k_force_sum(c->D, c->K, c->D.cap, false, c->stream);
   return finish(c);
@@ -717,7 +726,8 @@ int dml_overlap_moveback(dml_ctx* c, int64_t step) {
   if (!c || !c->loaded) return DML_E_STATE;
   int rc = set_step(c, step);
   if (rc) return rc;
-  k_overlap(c->D, c->K, c->D.cap, c->D.cap, true, c->stream);
+  k_rank_prefix(c->D, c->stream);  // rows in use of every replica
+  k_overlap(c->D, c->K, c->D.cap, c->D.cap, true, 2, c->stream);
   return finish(c);
 }
 

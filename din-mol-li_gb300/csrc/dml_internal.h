@@ -85,7 +85,7 @@ struct Scalars {
 // Context-wide device state.
 struct Global {
   long long step;
-  unsigned long long delta2_bits;  // max |pos - old_cg|^2 over all hs%ref (as bits)
+  unsigned int delta2f_bits;  // FP32 upper bound of max |pos - old_cg|^2 over hs%ref (bits)
   int error;       // first dml_status raised on the device
   int err_info;
   int err_rep;
@@ -98,6 +98,7 @@ struct Global {
   unsigned int ticket_rep;  // replicas finished with the displacement test
   long long list_builds;    // rebuild kernels run (some replica rebuilt)
   int near_stale;           // near lists must be searched in the overlap phase
+  int n_big;                // entries of big_cells
 };
 
 struct EvRec {            // one interacting list entry seen from one atom
@@ -177,6 +178,9 @@ struct Dev {
   Global* g;          // context-wide state
   RepConst* rc;       // [nrep] per-replica constants
   int* rep_of;        // [cap] replica of every position
+  int* rank_pre;      // [nrep + 1] prefix of the replicas' n_rank (rows in use),
+                      // taken at the start of each step (n_rank changes in gcmc_run)
+  int* big_cells;     // cells too large for the per-thread sort of cell_order
   int nrep;
   int cap;            // positions over all replicas (sum of the replica caps)
   int max_rep_cap;    // largest replica capacity
@@ -185,6 +189,7 @@ struct Dev {
 
 // ---- kernel launchers (dml_kernels.cu); each returns the kernels it queued ----
 int k_step_begin(const Dev& d, int near_stale, cudaStream_t s);
+int k_rank_prefix(const Dev& d, cudaStream_t s);
 int k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_force_pairs(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s);
@@ -198,8 +203,11 @@ int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, 
 // overlap_moveback: standalone (its own delta and near search) or as the
 // second half of a fused step whose first half ran k_overlap_prepare.
 int k_overlap_prepare(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
+// detect: 0 no near search (done elsewhere), 1 only if the near lists are
+// stale, 2 always.
 int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool standalone,
-              cudaStream_t s);
+              int detect, cudaStream_t s);
+int k_overlap_detect(const Dev& d, const KParams& p, int n_rank, int mode, cudaStream_t s);
 int k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
 int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);

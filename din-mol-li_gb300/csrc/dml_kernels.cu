@@ -145,6 +145,51 @@ __device__ __forceinline__ bool in_tessellation(const RepConst& R, double4 P) {
          coord_in_tess(P.z, R.cell[2], R.ncells[2]);
 }
 
+// Prefix of the replicas' rows in use (one block): the warp-per-row kernels
+// walk only the rows in use, the capacity headroom of every replica skipped.
+__global__ void rank_prefix_kernel(Dev d) {
+  __shared__ int ws[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int base = 0; base < d.nrep; base += blockDim.x) {
+    int i = base + threadIdx.x;
+    int v = i < d.nrep ? d.sc[i].n_rank : 0, x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int w = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      ws[lane] = w;
+    }
+    __syncthreads();
+    int pre = (wid > 0 ? ws[wid - 1] : 0) + x - v;
+    if (i < d.nrep) d.rank_pre[i] = carry + pre;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry += pre + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) d.rank_pre[d.nrep] = carry;
+}
+
+// Rank (position in ref) of row i of the rows in use, replica by replica.
+__device__ __forceinline__ int row_rank(const Dev& d, int i) {
+  int lo = 0, hi = d.nrep - 1;  // largest replica whose first row is <= i
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(d.rank_pre + mid) <= i) lo = mid; else hi = mid - 1;
+  }
+  return d.rc[lo].base + (i - __ldg(d.rank_pre + lo));
+}
+
 // Replica of the block (replica capacities are multiples of the block size).
 __device__ __forceinline__ int block_rep(const Dev& d) { return d.rep_of[blockIdx.x * blockDim.x]; }
 
@@ -156,10 +201,41 @@ __device__ __forceinline__ int warp_id_global() {
 // A new step: the counter, the displacement bound delta of this step's
 // overlap search, and whether its near lists still need a search of their
 // own (always with the Brownian integrator, which has no force scan).
-__global__ void step_begin_kernel(Global* g, int near_stale) {
-  g->step += 1;
-  g->delta2_bits = 0ull;
-  g->near_stale = near_stale;
+__global__ void step_begin_kernel(Dev d, int near_stale) {
+  Global* g = d.g;
+  if (threadIdx.x == 0) {
+    g->step += 1;
+    g->delta2f_bits = 0u;
+    g->near_stale = near_stale;
+    // overlap_moveback's counters (reset per call in the standalone path)
+    g->again = 0;
+    g->n_comp = 0;
+    g->comp_total = 0;
+    g->passes = 1;
+  }
+  for (int r = threadIdx.x; r < d.nrep; r += blockDim.x) {
+    d.sc[r].passes = 1;
+    d.sc[r].again2 = 0;
+  }
+}
+
+// The integrators' share of overlap_moveback in a fused step: the
+// component state of the moving atom, and delta bounded from the FP32
+// positions (|x - RN32(x)| <= 2^-24 |x|; the near radius adds the margin).
+__device__ __forceinline__ void overlap_prepare_atom(const Dev& d, const RepConst& R, int h,
+                                                     float4 before, float4 after) {
+  d.uf[h] = h;
+  d.active[h] = 0;
+  d.comp_size[h] = 0;
+  d.comp_fill[h] = 0;
+  float x, y, z;
+  vdist_nint_f(R, after, before, x, y, z);
+  float dd = x * x + y * y + z * z;
+  if (!(dd == dd)) dd = 0.0f;  // a NaN position takes no part (and stops at test_update)
+  // non-negative floats order as their bit patterns: warp maximum, one atomic
+  const unsigned m = __activemask();
+  const unsigned v = __reduce_max_sync(m, __float_as_uint(dd));
+  if ((int)(threadIdx.x & 31) == __ffs(m) - 1 && v) atomicMax(&d.g->delta2f_bits, v);
 }
 
 // atom_pbc (dana.F90:1187-1250) on registers; returns true when deposited.
@@ -247,10 +323,12 @@ __global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
   int typ0 = typ;
   bool depos = atom_pbc_dev(p, R, sc, step, id, pp, po, po_changed, V, v_changed, P, typ, zmax);
   double4 np = make_double4(pp[0], pp[1], pp[2], 0.0);
+  const float4 before = d.posf[h], after = to_f4(np, typ);
   d.old_cg[h] = P;
   d.pos[h] = np;
-  d.posf[h] = to_f4(np, typ);
+  d.posf[h] = after;
   d.ranv[h] = make_double4(rv[0], rv[1], rv[2], 0.0);
+  overlap_prepare_atom(d, R, h, before, after);
   if (po_changed) {
     d.pos_old[h] = po;
     d.posf_old[h] = to_f4(po, 0);
@@ -292,10 +370,12 @@ __global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
   int typ0 = typ;
   bool depos = atom_pbc_dev(p, R, sc, step, id, pp, po, po_changed, V, v_changed, P, typ, zmax);
   double4 np = make_double4(pp[0], pp[1], pp[2], 0.0);
+  const float4 before = d.posf[h], after = to_f4(np, typ);
   d.old_cg[h] = P;
   d.pos[h] = np;
-  d.posf[h] = to_f4(np, typ);
+  d.posf[h] = after;
   d.vel[h] = V;
+  overlap_prepare_atom(d, R, h, before, after);
   if (po_changed) {
     d.pos_old[h] = po;
     d.posf_old[h] = to_f4(po, 0);
@@ -336,7 +416,7 @@ __device__ void uf_union(Global* g, volatile int* uf, int a, int b) {
 // Near radius of overlap_moveback, rc + 2 delta in FP32 with margin (a
 // superset of the pairs that can touch during the passes).
 __device__ __forceinline__ float near_radius2(const Dev& d, const KParams& p) {
-  float delta = sqrtf(__double2float_ru(__longlong_as_double((long long)d.g->delta2_bits)));
+  float delta = sqrtf(__uint_as_float(d.g->delta2f_bits));
   float rnf = (p.rcf + 2.0f * delta) * 1.000001f + 4.0f * p.margin + 1e-3f;
   return rnf * rnf;
 }
@@ -349,22 +429,25 @@ __device__ __forceinline__ float near_radius2(const Dev& d, const KParams& p) {
 // warp whatever its active lanes, so the exact FP64 work is done afterwards
 // on the dense queue (force_exact_kernel), 32 entries per instruction.
 template <bool NEAR>
-__global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n_rank) {
+__device__ __forceinline__ void force_scan_rows(const Dev& d, const KParams& p, int w,
+                                                int total) {
   // Two hs%ref members per warp, one per half-warp, so that the dependent
   // loads of two rows overlap; each lane keeps 4 entries in flight.
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, hl = lane & 15, half = lane >> 4;
   const unsigned hmask = half ? 0xffff0000u : 0x0000ffffu;
-  const int r = 2 * warp_id_global() + half;  // grids are sized by capacity
+  const int i = 2 * w + half;
+  const int r = i < total ? row_rank(d, i) : 0;
+  // the element comes with the position (posf.w)
   const int rep = d.rep_of[r];
   const RepConst& R = d.rc[rep];
   int h = -1, k = 0, n = 0;
   float4 Pf = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (r - R.base < d.sc[rep].n_rank) h = d.ref[r];
+  if (i < total) h = d.ref[r];
   if (h >= 0) {
-    k = d.typ[h];
     Pf = d.posf[h];
     n = d.nn[h];
+    k = elem_of(Pf);
   }
   const int nmax = max(n, __shfl_xor_sync(FULL, n, 16));
   if (nmax == 0) return;  // both halves idle
@@ -432,6 +515,14 @@ __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n
     d.near_count[h] = ncnt > kNearCap ? -1 : ncnt;
     if (any) d.active[h] = 1;
   }
+}
+
+// Rows of all hs%ref positions (in use or not) by a fixed grid of warps.
+template <bool NEAR>
+__global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n_rank) {
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int total = d.rank_pre[d.nrep];
+  for (int w = warp_id_global(); 2 * w < total; w += nw) force_scan_rows<NEAR>(d, p, w, total);
 }
 
 // Exact FP64 evaluation of the queued entries (dana.F90:1095-1134), one
@@ -930,6 +1021,7 @@ __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int 
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;
   n_b = R.base + sc->n_b;
+  if (blockIdx.x == 0 && threadIdx.x == 0) d.g->n_big = 0;  // cell_order's list
   if (!cells_only && !sc->rebuild) return;
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (!cells_only && s == R.base) sc->nlimbo = 0;
@@ -1031,11 +1123,8 @@ __global__ void cell_scatter_kernel(Dev d, int n_b, int force) {
 // cgroup_sort (Cells.F90:267-302), which prepends slots in increasing order.
 // One warp per cell; the sorted cell goes to comp_members (scratch) and is
 // copied back as hs slots (what the list stores).
-__global__ void cell_order_kernel(Dev d, int ncell, int force) {
-  if (!force && !d.g->any_rebuild) return;
-  int c = warp_id_global();
+__device__ __forceinline__ void cell_order_cell(const Dev& d, int c) {
   int lane = threadIdx.x & 31;
-  if (c >= ncell) return;
   // counted in this sort (replicas that do not sort keep zero counts)
   int num = __shfl_sync(0xffffffffu, lane == 0 ? d.cell_count[c] : 0, 0);
   if (num == 0) return;
@@ -1055,11 +1144,52 @@ __global__ void cell_order_kernel(Dev d, int ncell, int force) {
   for (int i = lane; i < num; i += 32) ((int*)seg)[i] = d.b2hs[tmp[i]];
 }
 
+// Cells of at most kSmallCell atoms are ordered by one thread each (a
+// sorting network in registers); larger ones are listed for a warp each.
+constexpr int kSmallCell = 16;
+__global__ void cell_order_small_kernel(Dev d, int ncell, int force) {
+  if (!force && !d.g->any_rebuild) return;
+  const int nt = gridDim.x * blockDim.x;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += nt) {
+    const int num = d.cell_count[c];
+    if (num == 0) continue;
+    if (num > kSmallCell) {
+      d.big_cells[atomicAdd(&d.g->n_big, 1)] = c;
+      continue;
+    }
+    d.cell_count[c] = 0;
+    const int start = d.cell_start[c];
+    int v[kSmallCell];
+#pragma unroll
+    for (int k = 0; k < kSmallCell; ++k) v[k] = k < num ? d.cell_atoms[start + k] : -1;
+    // descending odd-even transposition sort (the b slots are distinct, >= 0)
+#pragma unroll
+    for (int rnd = 0; rnd < kSmallCell; ++rnd) {
+#pragma unroll
+      for (int k = rnd & 1; k + 1 < kSmallCell; k += 2) {
+        int a = v[k], b = v[k + 1];
+        v[k] = max(a, b);
+        v[k + 1] = min(a, b);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kSmallCell; ++k)
+      if (k < num) d.cell_atoms[start + k] = d.b2hs[v[k]];
+  }
+}
+
+__global__ void cell_order_big_kernel(Dev d, int force) {
+  if (!force && !d.g->any_rebuild) return;
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int nb = d.g->n_big;
+  for (int q = warp_id_global(); q < nb; q += nw) cell_order_cell(d, d.big_cells[q]);
+}
+
 // ngroup_cells (Neighbor.F90:465-548): one warp per hs%ref member, the 27
 // stencil cells in map order (Cells.F90:28-36), each cell in chain order,
 // wrapped as cell_pbc with mic (Cells.F90:378-404), `rd < (rc+skin)^2`.
-__global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
-  int r = warp_id_global();  // grids are sized by capacity
+__device__ __forceinline__ void list_cells_row(const Dev& d, const KParams& p, int r,
+                                               int* tab) {
   int lane = threadIdx.x & 31;
   const int rep = d.rep_of[r];
   const RepConst& R = d.rc[rep];
@@ -1076,51 +1206,73 @@ __global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
     if (lane == 0) raise_error(d.g, DML_E_OUT_OF_TESSELLATION, h);
     return;
   }
-  int* row = d.list + (size_t)h * p.mnb;
-  int cnt = 0;
-  for (int nabor = 0; nabor < 27; ++nabor) {
+  // Lane q < 27 takes stencil cell q (map order): its start in tab[q], the
+  // exclusive prefix of the cell sizes in tab[27 + q], the total in tab[54].
+  // The 27 cells then form one index space f that keeps the list order
+  // (cell by cell, each cell in chain order), scanned 32 entries at a time.
+  __syncwarp();
+  int num = 0;
+  bool bad = false;
+  if (lane < 27) {
     int nc[3];
-    bool bad = false;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      int t = c_map[nabor][k] + rc[k] - 1;
+      int t = c_map[lane][k] + rc[k] - 1;
       t = (t + R.ncells[k]) % R.ncells[k];
       nc[k] = t + 1;
       if (nc[k] < 0 || nc[k] > R.ncells[k] + 1) bad = true;
     }
-    if (bad) {
-      if (lane == 0) raise_error(d.g, DML_E_OUT_OF_TESSELLATION, h);
-      return;
+    if (!bad) {
+      int c = R.cell_off + (nc[2] * R.head_dim[1] + nc[1]) * R.head_dim[0] + nc[0];
+      int st = d.cell_start[c];
+      num = d.cell_start[c + 1] - st;
+      tab[lane] = st;
     }
-    int c = R.cell_off + (nc[2] * R.head_dim[1] + nc[1]) * R.head_dim[0] + nc[0];
-    int start = d.cell_start[c];
-    int num = d.cell_start[c + 1] - start;
-    for (int base = 0; base < num; base += 32) {
-      int idx = base + lane;
-      bool inc = false;
-      int j = -1;
-      if (idx < num) {
-        j = d.cell_atoms[start + idx];  // hs slot, cells in descending b-slot order
-        if (j != h) {
-          float4 Q = d.posf[j];
-          float fx, fy, fz;
-          vdist_nint_f(R, Q, Pf, fx, fy, fz);
-          float drf = fx * fx + fy * fy + fz * fz;
-          if (drf < p.rlist_lo2) {
-            inc = true;
-          } else if (drf <= p.rlist_hi2) {
-            double vx, vy, vz;
-            vdist_nint(R, d.pos[j], P, vx, vy, vz);
-            double rd = dot3(vx, vy, vz);
-            inc = rd < p.rlist2;
-          }
+  }
+  if (__any_sync(0xffffffffu, bad)) {
+    if (lane == 0) raise_error(d.g, DML_E_OUT_OF_TESSELLATION, h);
+    return;
+  }
+  int x = num;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane < 27) tab[27 + lane] = x - num;
+  const int T = __shfl_sync(0xffffffffu, x, 26);
+  __syncwarp();
+  int* row = d.list + (size_t)h * p.mnb;
+  int cnt = 0;
+  for (int base = 0; base < T; base += 32) {
+    const int f = base + lane;
+    bool inc = false;
+    int j = -1;
+    if (f < T) {
+      int lo = 0, hi = 26;  // the cell holding f: largest q with prefix <= f
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (tab[27 + mid] <= f) lo = mid; else hi = mid - 1;
+      }
+      j = d.cell_atoms[tab[lo] + f - tab[27 + lo]];  // hs slot
+      if (j != h) {
+        float4 Q = d.posf[j];
+        float fx, fy, fz;
+        vdist_nint_f(R, Q, Pf, fx, fy, fz);
+        float drf = fx * fx + fy * fy + fz * fz;
+        if (drf < p.rlist_lo2) {
+          inc = true;
+        } else if (drf <= p.rlist_hi2) {
+          double vx, vy, vz;
+          vdist_nint(R, d.pos[j], P, vx, vy, vz);
+          double rd = dot3(vx, vy, vz);
+          inc = rd < p.rlist2;
         }
       }
-      unsigned bal = __ballot_sync(0xffffffffu, inc);
-      int pre = __popc(bal & ((1u << lane) - 1u));
-      if (inc && cnt + pre < p.mnb) row[cnt + pre] = j;
-      cnt += __popc(bal);
     }
+    unsigned bal = __ballot_sync(0xffffffffu, inc);
+    int pre = __popc(bal & ((1u << lane) - 1u));
+    if (inc && cnt + pre < p.mnb) row[cnt + pre] = j;
+    cnt += __popc(bal);
   }
   if (lane == 0) {
     if (cnt > p.mnb) {
@@ -1132,10 +1284,17 @@ __global__ void list_cells_kernel(Dev d, KParams p, int n_rank) {
   }
 }
 
+__global__ void __launch_bounds__(256) list_cells_kernel(Dev d, KParams p, int n_rank) {
+  __shared__ int tab[8][56];  // per warp: the stencil cells' starts and prefixes
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int total = d.rank_pre[d.nrep];
+  for (int i = warp_id_global(); i < total; i += nw)
+    list_cells_row(d, p, row_rank(d, i), tab[threadIdx.x >> 5]);
+}
+
 // ngroup_verlet (Neighbor.F90:358-424): all hs%b slots in index order,
 // `rd > (rc+skin)^2` rejected (so equality is kept), vdistance(ai, aj).
-__global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
-  int r = warp_id_global();  // grids are sized by capacity
+__device__ __forceinline__ void list_verlet_row(const Dev& d, const KParams& p, int r, int n_b) {
   int lane = threadIdx.x & 31;
   const int rep = d.rep_of[r];
   const RepConst& R = d.rc[rep];
@@ -1185,6 +1344,12 @@ __global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
   }
 }
 
+__global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int total = d.rank_pre[d.nrep];
+  for (int i = warp_id_global(); i < total; i += nw) list_verlet_row(d, p, row_rank(d, i), n_b);
+}
+
 __global__ void rebuild_done_kernel(Dev d) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r == 0) {
@@ -1205,7 +1370,7 @@ __global__ void rebuild_done_kernel(Dev d) {
 // commute, so each component is replayed in rank order by one thread and
 // gives exactly the reference's result.
 
-__global__ void delta_reset_kernel(Global* g) { g->delta2_bits = 0ull; }
+__global__ void delta_reset_kernel(Global* g) { g->delta2f_bits = 0u; }
 
 // Resets the component state and takes delta = max |pos - old_cg| over the
 // moving atoms (positions after the integrator; they do not change until
@@ -1242,19 +1407,19 @@ __global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
   }
   for (int off = 16; off > 0; off >>= 1) dd = fmax(dd, __shfl_down_sync(0xffffffffu, dd, off));
   if ((threadIdx.x & 31) == 0 && dd > 0.0)
-    atomicMax(&d.g->delta2_bits, (unsigned long long)__double_as_longlong(dd));
+    atomicMax(&d.g->delta2f_bits, __float_as_uint(__double2float_ru(dd)));
 }
 
 // Near entries of every hs%ref member: list entries within rc + 2 delta
 // (FP32 with margin; a superset is harmless) in list order.
-__global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p, int gated) {
-  if (gated && !d.g->near_stale) return;  // the force scan found them
-  int r = warp_id_global();  // grids are sized by capacity
+__device__ __forceinline__ void overlap_detect_row(const Dev& d, const KParams& p, int r,
+                                                   int only_rebuilt) {
   int lane = threadIdx.x & 31;
   const int rep = d.rep_of[r];
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   if (r - R.base >= sc->n_rank) return;
+  if (only_rebuilt && !sc->rebuild) return;  // its near entries are current
   int h = d.ref[r];
   if (h < 0) return;
   // rc + 2 delta in FP32 (sqrtf is exact to an ulp; the margin covers it)
@@ -1301,6 +1466,16 @@ __global__ void __launch_bounds__(256, 6) overlap_detect_kernel(Dev d, KParams p
   }
 }
 
+// mode 0: every replica; 1: only if some list was rebuilt since the force
+// scan, for the replicas that rebuilt; 2: the replicas that rebuilt.
+__global__ void __launch_bounds__(256) overlap_detect_kernel(Dev d, KParams p, int mode) {
+  if (mode == 1 && !d.g->near_stale) return;  // the force scan found them
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int total = d.rank_pre[d.nrep];
+  for (int i = warp_id_global(); i < total; i += nw)
+    overlap_detect_row(d, p, row_rank(d, i), mode != 0);
+}
+
 // Atoms with no near entry are examined trivially in pass 1 (skip = true)
 // and can never be moved; the others are counted per component root.
 __global__ void overlap_count_kernel(Dev d, int n_rank) {
@@ -1327,6 +1502,9 @@ __global__ void overlap_assign_kernel(Dev d, int n_slots) {
   n_slots = R.base + sc->n_slots;  // positions in use end here
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_slots) return;
+  // component roots are hs%ref members (their sizes are reset each step;
+  // an atom that left hs%ref keeps a stale one)
+  if (d.rank[s] < 0) return;
   int sz = d.comp_size[s];
   if (sz <= 0) return;
   int cid = atomicAdd(&d.g->n_comp, 1);
@@ -2371,6 +2549,10 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
 
 inline int nblk(int n, int b = kBlock) { return n > 0 ? (n + b - 1) / b : 1; }
 inline int nblk_warps(int n) { return n > 0 ? (n + (kBlock / 32) - 1) / (kBlock / 32) : 1; }
+// Fixed grid of the warp-per-row kernels (grid-stride over the rows): a
+// few resident blocks per SM instead of one block per 8 rows.
+constexpr int kRowGrid = 152 * 16;
+inline int nblk_rows(int rows) { int b = nblk_warps(rows); return b < kRowGrid ? b : kRowGrid; }
 
 // Overwrites a buffer larger than L2 (benchmark L2 flush between steps).
 __global__ void flush_kernel(uint4* buf, size_t n) {
@@ -2382,7 +2564,7 @@ __global__ void flush_kernel(uint4* buf, size_t n) {
 }  // namespace
 
 int k_step_begin(const Dev& d, int near_stale, cudaStream_t s) {
-  step_begin_kernel<<<1, 1, 0, s>>>(d.g, near_stale);
+  step_begin_kernel<<<1, 256, 0, s>>>(d, near_stale);
   return 1;
 }
 
@@ -2398,7 +2580,7 @@ int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
 
 int k_force_pairs(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s) {
   // two hs%ref members per warp
-  const int nb = nblk_warps((n_rank + 1) / 2);
+  const int nb = nblk_rows((n_rank + 1) / 2);
   if (near)
     force_scan_kernel<true><<<nb, kBlock, 0, s>>>(d, p, n_rank);
   else
@@ -2449,12 +2631,13 @@ int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, 
   if (d.any_cells) {
     cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 0);
     cell_scatter_kernel<<<nblk(n_b), kBlock, 0, s>>>(d, n_b, 0);
-    cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot, 0);
-    list_cells_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank);
-    n += 4;
+    cell_order_small_kernel<<<kRowGrid, kBlock, 0, s>>>(d, d.ncell_tot, 0);
+    cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 0);
+    list_cells_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+    n += 5;
   }
   if (d.any_verlet) {
-    list_verlet_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, n_rank, n_b);
+    list_verlet_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, n_rank, n_b);
     n += 1;
   }
   rebuild_done_kernel<<<nblk(d.nrep), kBlock, 0, s>>>(d);
@@ -2466,21 +2649,31 @@ int k_overlap_prepare(const Dev& d, const KParams& p, int n_slots, cudaStream_t 
   return 1;
 }
 
+int k_overlap_detect(const Dev& d, const KParams& p, int n_rank, int mode, cudaStream_t s) {
+  overlap_detect_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, mode);
+  return 1;
+}
+
+int k_rank_prefix(const Dev& d, cudaStream_t s) {
+  rank_prefix_kernel<<<1, 1024, 0, s>>>(d);
+  return 1;
+}
+
 int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool standalone,
-              cudaStream_t s) {
+              int detect, cudaStream_t s) {
   int n = 0;
   if (standalone) {
     delta_reset_kernel<<<1, 1, 0, s>>>(d.g);
     n += 1 + k_overlap_prepare(d, p, n_slots, s);
   }
-  overlap_detect_kernel<<<nblk_warps(n_rank), kBlock, 0, s>>>(d, p, standalone ? 0 : 1);
+  if (detect) n += k_overlap_detect(d, p, n_rank, detect == 1 ? 1 : 0, s);
   overlap_count_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
   overlap_assign_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, n_slots);
   overlap_scatter_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
   overlap_order_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
   int all_passes = p.prob >= 1.0;
   overlap_pass1_kernel<<<nblk(n_rank, 128), 128, 0, s>>>(d, p, all_passes);
-  n += 6;
+  n += 5;
   if (all_passes) return n;
   overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
   return n + 1;
@@ -2508,8 +2701,9 @@ int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
     rebuild_prep_kernel<<<nblk(cap), kBlock, 0, s>>>(d, p, cap, cap, 1);
     cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1);
     cell_scatter_kernel<<<nblk(cap), kBlock, 0, s>>>(d, cap, 1);
-    cell_order_kernel<<<nblk_warps(d.ncell_tot), kBlock, 0, s>>>(d, d.ncell_tot, 1);
-    n += 4;
+    cell_order_small_kernel<<<kRowGrid, kBlock, 0, s>>>(d, d.ncell_tot, 1);
+    cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 1);
+    n += 5;
   }
   size_t shm = sizeof(GcmcTrial) * (size_t)kGcmcTrialBatch +
                sizeof(int) * (size_t)(d.max_rep_cap / kGcmcThreads + 2);

@@ -108,21 +108,21 @@ def c5_params(seed=11, precision=dml.PRECISION_MIXED, nadj=128, cells=C5_CELLS, 
     """Config 5 replica: 40 x 40 x 2-cell electrode (140.4 Å square), 300 Å
     high, GCMC reservoir slab z in [200, 300] with `nadj` trials per step
     (half creations, half destructions on average), Ermak, dt = 1 fs,
-    skin 10 Å.  The activity puts the ideal-gas count of the slab at the
-    initial ion density, so the mean ion count stays fixed."""
+    neighbour skin 2 Å (nb_dcut of the reference's GCMC run, tests/gcmc).
+    slab_activity sets the activity that keeps the mean ion count fixed."""
     a = 3.51
     L = cells * a
     p = dml.default_params()
     p.box[:] = [L, L, 300.0]
     p.z0, p.zmax = 200.0, 300.0
     p.h = 1e-3
-    p.skin = 10.0
+    p.skin = 2.0
     p.reservoir = dml.RESERVOIR_GCMC
     p.nadj = nadj
     p.act = n_ion / (L * L * (300.0 - 15.0))
     p.precision = precision
     p.seed = seed
-    p.mnb = 512
+    p.mnb = 128
     # room for insertions while deleted atoms wait in limbo for a rebuild
     p.capacity = 2 * cells * cells * 2 + n_ion + 16384
     return p
