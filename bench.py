@@ -396,6 +396,7 @@ def run_gpu(args, ws, rank, local):
     ions_all = dist.reduce(n_ion, "sum")
     value = ions_all * args.steps / (ms_max / 1e3)
     per_step, per_rebuild = sim.launches_per_step()
+    tuning = sim.tuning()
     launches = per_step * args.steps + per_rebuild * (c1["list_builds"] - c0["list_builds"])
     roofline = roofline_of(sim, wl, max(3, min(args.steps, 10)))
     counters = {k: c1[k] - c0[k] for k in ("choques", "depo", "try_", "choques3", "gcmc_ins",
@@ -476,7 +477,8 @@ def run_gpu(args, ws, rank, local):
                        if form == "chosen" else "plain FP64 (bit-exact to the oracle)",
                        "replicas": wl.n_rep, "n_ion": wl.n_ion, "n_electrode": wl.n_electrode,
                        "parallelism": "replicas" if ws > 1 else "single",
-                       "l2": "flushed between steps (256 MiB write outside the timed events)"},
+                       "l2": "flushed between steps (256 MiB write outside the timed events)",
+                       "autotuner": tuning},
             "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "cpu_baseline": cpu, "compare": compare, "counters": counters}
     print(json.dumps(line), flush=True)

@@ -33,6 +33,7 @@ struct dml_ctx {
   cudaGraphExec_t step_graph = nullptr;
   int launches_per_step = 0;    // kernels of a step without a list rebuild
   int launches_per_rebuild = 0; // extra kernels when the list is rebuilt
+  float tune_us[4] = {0, 0, 0, 0};  // force-scan time per mapping (4, 8, 16, 32 lanes per row)
   void* flush_buf = nullptr;
   std::string last_error;
   Scalars* h_sc = nullptr;  // pinned mirror of the per-replica state
@@ -160,6 +161,7 @@ void make_kparams(const dml_params& P, double maxc, KParams& K) {
   K.ev_cap = P.event_cap;
   K.max_passes = P.max_passes;
   K.mixed = P.precision == DML_PRECISION_MIXED;
+  K.scan_lanes = 16;  // until the step graph is tuned
   K.rcf = (float)P.rc;
   // 2^32 per eV/Å; 1 eV = 96.485 * 100 ui (dana.F90:23)
   K.fix_scale = std::ldexp(1.0, 32) / (96.485 * 100.0);
@@ -298,8 +300,51 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
   return 0;
 }
 
+// Autotuner of the force scan's thread mapping: each mapping (4, 8, 16 or
+// 32 lanes per list row) scans the loaded lists a few times without side
+// effects (the candidate queue is cleared after every launch) and the
+// fastest is kept for the step graph.  Row lengths depend on the skin and
+// the density, so the best mapping is a property of the workload.
+int autotune_scan(dml_ctx* c) {
+  if (c->P.integrator != DML_INTEGRATOR_ERMAK) return 0;
+  cudaStream_t s = c->stream;
+  const int lanes[4] = {4, 8, 16, 32};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  k_rank_prefix(c->D, s);
+  KParams k = c->K;
+  float best = 1e30f;
+  int best_l = 16;
+  for (int v = 0; v < 4; ++v) {
+    k.scan_lanes = lanes[v];
+    k_force_scan(c->D, k, c->D.cap, false, s);  // warm-up
+    k_reset_candidates(c->D, s);
+    CK(cudaEventRecord(e0, s));
+    for (int rep = 0; rep < 3; ++rep) {
+      k_force_scan(c->D, k, c->D.cap, false, s);
+      k_reset_candidates(c->D, s);
+    }
+    CK(cudaEventRecord(e1, s));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    c->tune_us[v] = ms * 1e3f / 3.0f;
+    if (ms < best) {
+      best = ms;
+      best_l = lanes[v];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->K.scan_lanes = best_l;
+  return finish(c);
+}
+
 int build_step_graph(dml_ctx* c) {
   if (c->step_graph) return 0;
+  int trc = autotune_scan(c);
+  if (trc) return trc;
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
   int nb = 0, nr = 0;
@@ -857,6 +902,14 @@ int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phas
     }
   for (auto& e : ev) cudaEventDestroy(e);
   return finish(c);
+}
+
+int dml_get_tuning(dml_ctx* c, int32_t* scan_lanes, float* scan_us) {
+  if (!c) return DML_E_ARG;
+  if (scan_lanes) *scan_lanes = c->K.scan_lanes;
+  if (scan_us)
+    for (int v = 0; v < 4; ++v) scan_us[v] = c->tune_us[v];
+  return 0;
 }
 
 int dml_launches_per_step(dml_ctx* c, int32_t* per_rebuild) {

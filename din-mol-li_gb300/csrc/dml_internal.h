@@ -120,6 +120,7 @@ struct KParams {
   int pair_on[3][3];        // eps != 0 (other pairs add signed zeros only)
   // mixed form: FP32 force vectors, int64 fixed-point sums
   int mixed;
+  int scan_lanes;           // lanes per list row in the force scan (4, 8, 16, 32; tuned)
   double c12[3][3];         // 12 eps / r0^2 (scalar pair force of the mixed form)
   int cand_cap;
   float rcf;                // rc (FP32, pre-filters)
@@ -193,6 +194,8 @@ int k_rank_prefix(const Dev& d, cudaStream_t s);
 int k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_force_pairs(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s);
+int k_force_scan(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s);
+int k_reset_candidates(const Dev& d, cudaStream_t s);
 int k_force_sum(const Dev& d, const KParams& p, int n_slots, bool fuse_ermak_b, cudaStream_t s);
 int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,

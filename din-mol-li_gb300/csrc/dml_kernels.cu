@@ -428,15 +428,16 @@ __device__ __forceinline__ float near_radius2(const Dev& d, const KParams& p) {
 // On GB300 an FP64 instruction occupies the narrow FP64 pipe for the whole
 // warp whatever its active lanes, so the exact FP64 work is done afterwards
 // on the dense queue (force_exact_kernel), 32 entries per instruction.
-template <bool NEAR>
+template <bool NEAR, int L>
 __device__ __forceinline__ void force_scan_rows(const Dev& d, const KParams& p, int w,
                                                 int total) {
-  // Two hs%ref members per warp, one per half-warp, so that the dependent
-  // loads of two rows overlap; each lane keeps 4 entries in flight.
+  // 32 / L hs%ref members per warp, L lanes each, so that the dependent
+  // loads of several rows overlap; each lane keeps 4 entries in flight.
+  constexpr int U = 4, STEP = L * U;
   const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31, hl = lane & 15, half = lane >> 4;
-  const unsigned hmask = half ? 0xffff0000u : 0x0000ffffu;
-  const int i = 2 * w + half;
+  const int lane = threadIdx.x & 31, sl = lane % L, sub = lane / L;
+  const unsigned smask = (L == 32 ? FULL : ((1u << L) - 1u)) << (sub * L);
+  const int i = (32 / L) * w + sub;
   const int r = i < total ? row_rank(d, i) : 0;
   // the element comes with the position (posf.w)
   const int rep = d.rep_of[r];
@@ -449,8 +450,10 @@ __device__ __forceinline__ void force_scan_rows(const Dev& d, const KParams& p, 
     n = d.nn[h];
     k = elem_of(Pf);
   }
-  const int nmax = max(n, __shfl_xor_sync(FULL, n, 16));
-  if (nmax == 0) return;  // both halves idle
+  int nmax = n;
+#pragma unroll
+  for (int o = L; o < 32; o <<= 1) nmax = max(nmax, __shfl_xor_sync(FULL, nmax, o));
+  if (nmax == 0) return;  // every row of the warp is empty
   const int* row = d.list + (size_t)(h >= 0 ? h : 0) * p.mnb;
   // With NEAR the same pass records overlap_moveback's near entries (list
   // entries within rc + 2 delta, in list order) and unites their components.
@@ -459,18 +462,18 @@ __device__ __forceinline__ void force_scan_rows(const Dev& d, const KParams& p, 
   int ncnt = 0;
   bool any = false;
   const unsigned lt = (1u << lane) - 1u;
-  for (int base = 0; base < nmax; base += 64) {
-    int j[4];
-    float4 Q[4];
+  for (int base = 0; base < nmax; base += STEP) {
+    int j[U];
+    float4 Q[U];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      int jj = base + 16 * u + hl;
+    for (int u = 0; u < U; ++u) {
+      int jj = base + L * u + sl;
       j[u] = jj < n ? __ldg(row + jj) : -1;
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) Q[u] = j[u] >= 0 ? d.posf[j[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int u = 0; u < U; ++u) Q[u] = j[u] >= 0 ? d.posf[j[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < U; ++u) {
       // one FP32 minimum-image distance serves both tests; the element of
       // a slot that is not live (limbo, Neighbor.F90:1089-1092) is 0
       const int m = elem_of(Q[u]);
@@ -492,12 +495,12 @@ __device__ __forceinline__ void force_scan_rows(const Dev& d, const KParams& p, 
         base_q = __shfl_sync(FULL, base_q, 0);
         if (cand) {
           int q = base_q + __popc(bc & lt);
-          if (q < p.cand_cap) d.cand[q] = make_int4(r, base + 16 * u + hl, h, j[u]);
+          if (q < p.cand_cap) d.cand[q] = make_int4(r, base + L * u + sl, h, j[u]);
         }
       }
       if (NEAR) {
         const bool inc = live && df <= rn2;
-        const unsigned bal = __ballot_sync(FULL, inc) & hmask;
+        const unsigned bal = __ballot_sync(FULL, inc) & smask;
         if (inc) {
           int pre = __popc(bal & lt);
           if (ncnt + pre < kNearCap) near[ncnt + pre] = j[u];
@@ -511,18 +514,19 @@ __device__ __forceinline__ void force_scan_rows(const Dev& d, const KParams& p, 
       }
     }
   }
-  if (NEAR && hl == 0 && h >= 0) {
+  if (NEAR && sl == 0 && h >= 0) {
     d.near_count[h] = ncnt > kNearCap ? -1 : ncnt;
     if (any) d.active[h] = 1;
   }
 }
 
-// Rows of all hs%ref positions (in use or not) by a fixed grid of warps.
-template <bool NEAR>
-__global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p, int n_rank) {
+// The rows in use, 32 / L per warp, by a fixed grid of warps.
+template <bool NEAR, int L>
+__global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p) {
   const int nw = gridDim.x * (blockDim.x >> 5);
   const int total = d.rank_pre[d.nrep];
-  for (int w = warp_id_global(); 2 * w < total; w += nw) force_scan_rows<NEAR>(d, p, w, total);
+  for (int w = warp_id_global(); (32 / L) * w < total; w += nw)
+    force_scan_rows<NEAR, L>(d, p, w, total);
 }
 
 // Exact FP64 evaluation of the queued entries (dana.F90:1095-1134), one
@@ -2578,18 +2582,39 @@ int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   return 1;
 }
 
-int k_force_pairs(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s) {
-  // two hs%ref members per warp
-  const int nb = nblk_rows((n_rank + 1) / 2);
-  if (near)
-    force_scan_kernel<true><<<nb, kBlock, 0, s>>>(d, p, n_rank);
+template <bool NEAR>
+void launch_force_scan(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
+  const int L = p.scan_lanes;
+  const int nb = nblk_rows((n_rank + 32 / L - 1) / (32 / L));
+  if (L == 4)
+    force_scan_kernel<NEAR, 4><<<nb, kBlock, 0, s>>>(d, p);
+  else if (L == 8)
+    force_scan_kernel<NEAR, 8><<<nb, kBlock, 0, s>>>(d, p);
+  else if (L == 32)
+    force_scan_kernel<NEAR, 32><<<nb, kBlock, 0, s>>>(d, p);
   else
-    force_scan_kernel<false><<<nb, kBlock, 0, s>>>(d, p, n_rank);
+    force_scan_kernel<NEAR, 16><<<nb, kBlock, 0, s>>>(d, p);
+}
+
+int k_force_scan(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s) {
+  if (near)
+    launch_force_scan<true>(d, p, n_rank, s);
+  else
+    launch_force_scan<false>(d, p, n_rank, s);
+  return 1;
+}
+
+int k_force_pairs(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s) {
+  k_force_scan(d, p, n_rank, near, s);
   if (p.mixed)
     force_exact_mixed_kernel<<<152 * 4, kBlock, 0, s>>>(d, p);
   else
     force_exact_kernel<<<152 * 4, kBlock, 0, s>>>(d, p);
   return 2;
+}
+
+int k_reset_candidates(const Dev& d, cudaStream_t s) {
+  return cudaMemsetAsync(&d.g->n_cand, 0, sizeof(int), s) == cudaSuccess ? 0 : 1;
 }
 
 int k_force_sum(const Dev& d, const KParams& p, int n_slots, bool fuse_b, cudaStream_t s) {

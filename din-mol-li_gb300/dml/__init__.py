@@ -81,6 +81,7 @@ def lib():
     L.dml_time_steps.argtypes = [vp, i64, i32, P(ctypes.c_double)]
     L.dml_profile_steps.argtypes = [vp, i64, i32, vp, i32]
     L.dml_launches_per_step.argtypes = [vp, P(i32)]
+    L.dml_get_tuning.argtypes = [vp, P(i32), vp]
     L.dml_gen_bcc_slab.argtypes = [i32, i32, i32, ctypes.c_double, vp, i32]
     L.dml_gen_ions.argtypes = [ctypes.c_uint64, i32, ctypes.c_double, ctypes.c_double,
                                ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
@@ -272,6 +273,15 @@ class Simulation:
         self._check(self.lib.dml_profile_steps(self.h, n, 1 if flush_l2 else 0, out.ctypes.data,
                                                len(out)), "dml_profile_steps")
         return dict(zip(self.PHASES, out.tolist()))
+
+    def tuning(self):
+        """Autotuner choice: {"scan_lanes": L, "scan_us": {4: t, 8: t, 16: t, 32: t}}."""
+        lanes = ctypes.c_int32()
+        us = np.zeros(4, np.float32)
+        self._check(self.lib.dml_get_tuning(self.h, ctypes.byref(lanes), us.ctypes.data),
+                    "dml_get_tuning")
+        return {"scan_lanes": lanes.value,
+                "scan_us": {l: float(t) for l, t in zip((4, 8, 16, 32), us)}}
 
     def launches_per_step(self):
         """(kernels per step without a rebuild, extra kernels per rebuild)."""
