@@ -48,14 +48,27 @@ METRIC = "particle-steps/s on 1 GB300: mixed+batched vs plain FP64 at force err 
 UNIT = "particle-steps/s"
 NWR = 100  # output cadence of the reference's tests (entrada.ini nwr)
 
-# Algorithmic bytes per mobile ion and step, FP64 state touched once
-# (integrate: read pos, vel, acel, write pos, old_cg = 120 B; force + ermak_b:
-# read pos 24, vel, acel, element 49, write vel, acel 48, epot 8 = 129 B);
-# list-scanning phases add the 4-byte list entries they must read; gcmc reads
-# one position per gcmc member per trial.
-PHASE_BYTES_PER_ION = {"integrate": 120.0, "force_pairs": 24.0, "force_sum": 105.0,
-                       "test_update1": 48.0, "overlap": 48.0, "test_update2": 48.0,
-                       "commit": 1.0, "gcmc": 0.0, "rho_piston": 48.0}
+# The kernel that dominates each phase of a step, and its algorithmic bytes
+# per unit.  Units: "ion" = mobile ion (hs%ref member), "slot" = atom of hs%b
+# (electrode included), "trial" = GCMC trial.  Per ion: integrate reads pos,
+# vel, acel and writes pos, old_cg (120 B); force_sum (+ ermak_b) reads the
+# force accumulators, vel, acel, element and writes vel, acel, epot (105 B);
+# the displacement test and the overlap search read pos and one older
+# position (48 B); list phases add the 4-byte entries they must read.  The
+# cell sort reads a position and writes a cell index and a cell entry per
+# slot (32 B).  A GCMC trial reads the positions of the atoms in the 27 cells
+# around its point (24 B each; the cell volume is bounded below by
+# (rc + skin)^3, so the count is a lower bound).
+PHASE_KERNEL = {"integrate": ("ermak_a_kernel", "ion", 120.0),
+                "force_pairs": ("force_scan_kernel", "ion", 24.0),
+                "force_sum": ("force_fix_kernel", "ion", 105.0),
+                "test_update1": ("pbc_dispmax_kernel", "ion", 48.0),
+                "overlap": ("overlap_* (6 kernels)", "ion", 48.0),
+                "test_update2": ("pbc_dispmax_kernel", "ion", 48.0),
+                "commit": ("commit_kernel", "ion", 1.0),
+                "gcmc_cells": ("rebuild_prep/cell_* (5 kernels)", "slot", 32.0),
+                "gcmc": ("gcmc_kernel", "trial", 24.0),
+                "rho_piston": ("calc_rho_kernel", "ion", 48.0)}
 LIST_PHASES = ("force_pairs", "overlap")
 
 def dist_env():
@@ -350,7 +363,9 @@ def run_reference(args, ws, rank):
 
 
 def roofline_of(sim, wl, nprof):
-    """Dominant phase of un-graphed steps: algorithmic bytes / event time."""
+    """Dominant phase of profiled steps (the graph's kernels launched one by
+    one, CUDA events at the phase boundaries): its kernel's algorithmic bytes
+    per launch / its device time per step."""
     ph = sim.profile_steps(nprof, flush_l2=True)
     c = sim.counters()
     n_ion = c["n_ref"]
@@ -362,16 +377,26 @@ def roofline_of(sim, wl, nprof):
         pass
     dom = max(ph, key=ph.get)
     t_launch = ph[dom] / nprof / 1e3  # s per step of this phase
-    byts = PHASE_BYTES_PER_ION[dom] * n_ion
+    kernel, unit, per = PHASE_KERNEL[dom]
+    if unit == "ion":
+        units = n_ion
+    elif unit == "slot":
+        units = wl.n_ion + wl.n_electrode
+    else:
+        p = sim.params
+        rho = wl.n_ion / (wl.n_rep * p.box[0] * p.box[1] * (p.box[2] - 15.0))
+        per = 24.0 * 27.0 * rho * (p.rc + p.skin) ** 3
+        units = p.nadj * wl.n_rep
+    byts = per * units
     if dom in LIST_PHASES and nn_mean:
         byts += 4.0 * nn_mean * n_ion
-    if dom == "gcmc":
-        byts = sim.params.nadj * 24.0 * n_ion
     peak, peak_kind = measured_peaks()
     achieved = byts / t_launch / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "traffic": ncu_traffic(wl.name + ":" + dom),
-            "kernel_phase": dom, "peak_source": peak_kind, "bytes_per_step": byts,
+            "kernel": kernel, "kernel_phase": dom, "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": byts, "bytes_unit": unit,
+            "bytes_per_unit": per, "units_per_launch": units,
             "phase_ms_per_step": {k: v / nprof for k, v in ph.items()}}
 
 

@@ -248,7 +248,15 @@ int capture_test_update(dml_ctx* c, int* n_base, int* n_body, bool near_in_body)
 // `capture` the rebuilds become conditional graph nodes.  Returns 0 or a
 // status; the kernels queued are counted in *n_base (every step) and *n_body
 // (only when the list is rebuilt).
-int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_body) {
+// An idle stretch of the stream inside a profiled phase (a host read of the
+// rebuild condition), subtracted from that phase's time.
+struct ProfileGap {
+  cudaEvent_t a, b;
+  int phase;
+};
+
+int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_body,
+                 std::vector<ProfileGap>* gaps = nullptr) {
   const Dev& d = c->D;
   const KParams& k = c->K;
   cudaStream_t s = c->stream;
@@ -260,6 +268,26 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
   const bool ermak_ = c->P.integrator == DML_INTEGRATOR_ERMAK;
   auto test_update = [&](bool first) -> int {
     if (capture) return capture_test_update(c, &n, &nb, first && ermak_);
+    if (gaps) {
+      // the graph's kernels: the rebuild (and the near search after the
+      // first one) only when some replica rebuilds, decided on the host
+      n += k_pbc_dispmax(d, k, cap, s);
+      ProfileGap gp;
+      gp.phase = first ? DML_PHASE_TEST_UPDATE1 : DML_PHASE_TEST_UPDATE2;
+      CK(cudaEventCreate(&gp.a));
+      CK(cudaEventCreate(&gp.b));
+      CK(cudaEventRecord(gp.a, s));
+      int any = 0;
+      CK(cudaMemcpyAsync(&any, &d.g->any_rebuild, sizeof any, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      CK(cudaEventRecord(gp.b, s));
+      gaps->push_back(gp);
+      if (any) {
+        nb += k_rebuild(d, k, cap, cap, cap, s);
+        if (first && ermak_) nb += k_overlap_detect(d, k, cap, 2, s);
+      }
+      return 0;
+    }
     n += k_test_update(d, k, cap, cap, cap, s);
     return 0;
   };
@@ -284,13 +312,15 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
   // near entries: found by the force scan (Ermak), searched again inside
   // the first test_update's rebuild node (graph) or when stale (eager);
   // the Brownian step has no force scan and always searches here
-  n += k_overlap(d, k, cap, cap, false, !ermak ? 2 : (capture ? 0 : 1), s);
+  n += k_overlap(d, k, cap, cap, false, !ermak ? 2 : (capture || gaps ? 0 : 1), s);
   mark(DML_PHASE_TEST_UPDATE2);
   if ((rc = test_update(false)) != 0) return rc;
   mark(DML_PHASE_COMMIT);
   n += k_capture_commit(d, k, cap, s);
+  mark(DML_PHASE_GCMC_CELLS);
+  if (c->P.reservoir == DML_RESERVOIR_GCMC) n += k_gcmc_cells(d, k, cap, s);
   mark(DML_PHASE_GCMC);
-  if (c->P.reservoir == DML_RESERVOIR_GCMC) n += k_gcmc(d, k, cap, s);
+  if (c->P.reservoir == DML_RESERVOIR_GCMC) n += k_gcmc_trials(d, k, s);
   mark(DML_PHASE_RHO_PISTON);
   n += k_calc_rho(d, k, cap, s);
   if (c->P.reservoir == DML_RESERVOIR_PISTON) n += k_piston(d, k, cap, s);
@@ -604,6 +634,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.rc, nrep);
   AL(d.rep_of, cap);
   AL(d.rank_pre, nrep + 1);
+  AL(d.reb_pre, nrep + 1);
   AL(d.big_cells, ncell + 1);
 #undef AL
 
@@ -887,9 +918,10 @@ int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phas
   const int ne = DML_NPHASE + 1;
   std::vector<cudaEvent_t> ev(ne * nsteps);
   for (auto& e : ev) CK(cudaEventCreate(&e));
+  std::vector<ProfileGap> gaps;
   for (int64_t i = 0; i < nsteps; ++i) {
     if (flush_l2) k_flush(c->flush_buf, kFlushBytes, c->stream);
-    rc = enqueue_step(c, &ev[ne * i], false, nullptr, nullptr);
+    rc = enqueue_step(c, &ev[ne * i], false, nullptr, nullptr, &gaps);
     if (rc) return rc;
   }
   CK(cudaStreamSynchronize(c->stream));
@@ -900,6 +932,13 @@ int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phas
       CK(cudaEventElapsedTime(&t, ev[ne * i + k], ev[ne * i + k + 1]));
       phase_ms[k] += t;
     }
+  for (auto& gp : gaps) {
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, gp.a, gp.b));
+    phase_ms[gp.phase] -= t;
+    cudaEventDestroy(gp.a);
+    cudaEventDestroy(gp.b);
+  }
   for (auto& e : ev) cudaEventDestroy(e);
   return finish(c);
 }

@@ -181,6 +181,8 @@ struct Dev {
   int* rep_of;        // [cap] replica of every position
   int* rank_pre;      // [nrep + 1] prefix of the replicas' n_rank (rows in use),
                       // taken at the start of each step (n_rank changes in gcmc_run)
+  int* reb_pre;       // [nrep + 1] the same prefix over the replicas whose list the
+                      // last displacement test rebuilds (0 rows for the others)
   int* big_cells;     // cells too large for the per-thread sort of cell_order
   int nrep;
   int cap;            // positions over all replicas (sum of the replica caps)
@@ -216,6 +218,9 @@ int k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
 int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
 int k_flush(void* buf, size_t bytes, cudaStream_t s);
 int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s);
+int k_gcmc_cells(const Dev& d, const KParams& p, int cap, cudaStream_t s);
+int k_gcmc_trials(const Dev& d, const KParams& p, cudaStream_t s);
+int k_pbc_dispmax(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
 
 }  // namespace dml
 

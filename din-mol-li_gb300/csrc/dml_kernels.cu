@@ -180,15 +180,20 @@ __global__ void rank_prefix_kernel(Dev d) {
   if (threadIdx.x == 0) d.rank_pre[d.nrep] = carry;
 }
 
-// Rank (position in ref) of row i of the rows in use, replica by replica.
-__device__ __forceinline__ int row_rank(const Dev& d, int i) {
-  int lo = 0, hi = d.nrep - 1;  // largest replica whose first row is <= i
+// Rank (position in ref) of row i of the rows counted by the prefix `pre`
+// over replicas (rank_pre: the rows in use; reb_pre: those of the replicas
+// that rebuild).  A replica with no rows shares its prefix with the next
+// one, so the largest replica whose first row is <= i owns row i.
+__device__ __forceinline__ int row_rank_in(const Dev& d, const int* pre, int i) {
+  int lo = 0, hi = d.nrep - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
-    if (__ldg(d.rank_pre + mid) <= i) lo = mid; else hi = mid - 1;
+    if (__ldg(pre + mid) <= i) lo = mid; else hi = mid - 1;
   }
-  return d.rc[lo].base + (i - __ldg(d.rank_pre + lo));
+  return d.rc[lo].base + (i - __ldg(pre + lo));
 }
+
+__device__ __forceinline__ int row_rank(const Dev& d, int i) { return row_rank_in(d, d.rank_pre, i); }
 
 // Replica of the block (replica capacities are multiples of the block size).
 __device__ __forceinline__ int block_rep(const Dev& d) { return d.rep_of[blockIdx.x * blockDim.x]; }
@@ -996,6 +1001,7 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
     __syncthreads();
     rebuild = s_dec;
   }
+  __shared__ int s_lastrep;
   if (threadIdx.x == 0) {
     sc->rebuild = rebuild;
     if (rebuild) {
@@ -1005,14 +1011,53 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
     }
     sc->ticket = 0;
     __threadfence();
-    // the last replica to decide opens the rebuild subgraph if any rebuilds
     unsigned t2 = atomicAdd(&d.g->ticket_rep, 1u);
-    if (t2 == (unsigned)d.nrep - 1u) {
-      int any = atomicAdd(&d.g->any_rebuild, 0);
-      d.g->ticket_rep = 0;
-      if (any) d.g->near_stale = 1;  // lists change: the near entries too
-      if (cond) cudaGraphSetConditional(cond_handle, any ? 1u : 0u);
+    s_lastrep = t2 == (unsigned)d.nrep - 1u;
+  }
+  __syncthreads();
+  if (!s_lastrep) return;
+  // The last replica to decide: the rows of the replicas that rebuild (the
+  // list build walks only those), then the rebuild subgraph opens if any.
+  __threadfence();
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base0 = 0; base0 < d.nrep; base0 += blockDim.x) {
+    const int r = base0 + threadIdx.x;
+    int v = 0;
+    if (r < d.nrep) {
+      const volatile Scalars* q = d.sc + r;
+      v = q->rebuild ? q->n_rank : 0;
     }
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    __shared__ int wsum[32];
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      int w = lane < nwarp ? wsum[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    const int pre = (wid > 0 ? wsum[wid - 1] : 0) + x - v;
+    if (r < d.nrep) d.reb_pre[r] = carry + pre;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry += pre + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    d.reb_pre[d.nrep] = carry;
+    int any = atomicAdd(&d.g->any_rebuild, 0);
+    d.g->ticket_rep = 0;
+    if (any) d.g->near_stale = 1;  // lists change: the near entries too
+    if (cond) cudaGraphSetConditional(cond_handle, any ? 1u : 0u);
   }
 }
 
@@ -1291,9 +1336,9 @@ __device__ __forceinline__ void list_cells_row(const Dev& d, const KParams& p, i
 __global__ void __launch_bounds__(256) list_cells_kernel(Dev d, KParams p, int n_rank) {
   __shared__ int tab[8][56];  // per warp: the stencil cells' starts and prefixes
   const int nw = gridDim.x * (blockDim.x >> 5);
-  const int total = d.rank_pre[d.nrep];
+  const int total = d.reb_pre[d.nrep];  // rows of the replicas that rebuild
   for (int i = warp_id_global(); i < total; i += nw)
-    list_cells_row(d, p, row_rank(d, i), tab[threadIdx.x >> 5]);
+    list_cells_row(d, p, row_rank_in(d, d.reb_pre, i), tab[threadIdx.x >> 5]);
 }
 
 // ngroup_verlet (Neighbor.F90:358-424): all hs%b slots in index order,
@@ -1350,8 +1395,9 @@ __device__ __forceinline__ void list_verlet_row(const Dev& d, const KParams& p, 
 
 __global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
   const int nw = gridDim.x * (blockDim.x >> 5);
-  const int total = d.rank_pre[d.nrep];
-  for (int i = warp_id_global(); i < total; i += nw) list_verlet_row(d, p, row_rank(d, i), n_b);
+  const int total = d.reb_pre[d.nrep];  // rows of the replicas that rebuild
+  for (int i = warp_id_global(); i < total; i += nw)
+    list_verlet_row(d, p, row_rank_in(d, d.reb_pre, i), n_b);
 }
 
 __global__ void rebuild_done_kernel(Dev d) {
@@ -1475,9 +1521,11 @@ __device__ __forceinline__ void overlap_detect_row(const Dev& d, const KParams& 
 __global__ void __launch_bounds__(256) overlap_detect_kernel(Dev d, KParams p, int mode) {
   if (mode == 1 && !d.g->near_stale) return;  // the force scan found them
   const int nw = gridDim.x * (blockDim.x >> 5);
-  const int total = d.rank_pre[d.nrep];
+  // modes 1 and 2 walk only the rows of the replicas that rebuilt
+  const int* pre = mode != 0 ? d.reb_pre : d.rank_pre;
+  const int total = pre[d.nrep];
   for (int i = warp_id_global(); i < total; i += nw)
-    overlap_detect_row(d, p, row_rank(d, i), mode != 0);
+    overlap_detect_row(d, p, row_rank_in(d, pre, i), mode != 0);
 }
 
 // Atoms with no near entry are examined trivially in pass 1 (skip = true)
@@ -2637,10 +2685,14 @@ int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   return 1;
 }
 
+int k_pbc_dispmax(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
+  pbc_dispmax_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots, 0, 0);
+  return 1;
+}
+
 int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
                   cudaStream_t s) {
-  pbc_dispmax_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots, 0, 0);
-  return 1 + k_rebuild(d, p, n_slots, n_b, n_rank, s);
+  return k_pbc_dispmax(d, p, n_slots, s) + k_rebuild(d, p, n_slots, n_b, n_rank, s);
 }
 
 int k_pbc_dispmax_cond(const Dev& d, const KParams& p, int n_slots,
@@ -2720,16 +2772,23 @@ int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
   return 1;
 }
 
+// gcmc_run's searches need the cells of the current positions.
+int k_gcmc_cells(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
+  if (!d.any_cells) return 0;
+  rebuild_prep_kernel<<<nblk(cap), kBlock, 0, s>>>(d, p, cap, cap, 1);
+  cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1);
+  cell_scatter_kernel<<<nblk(cap), kBlock, 0, s>>>(d, cap, 1);
+  cell_order_small_kernel<<<kRowGrid, kBlock, 0, s>>>(d, d.ncell_tot, 1);
+  cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 1);
+  return 5;
+}
+
 int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
+  return k_gcmc_cells(d, p, cap, s) + k_gcmc_trials(d, p, s);
+}
+
+int k_gcmc_trials(const Dev& d, const KParams& p, cudaStream_t s) {
   int n = 0;
-  if (d.any_cells) {
-    rebuild_prep_kernel<<<nblk(cap), kBlock, 0, s>>>(d, p, cap, cap, 1);
-    cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1);
-    cell_scatter_kernel<<<nblk(cap), kBlock, 0, s>>>(d, cap, 1);
-    cell_order_small_kernel<<<kRowGrid, kBlock, 0, s>>>(d, d.ncell_tot, 1);
-    cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 1);
-    n += 5;
-  }
   size_t shm = sizeof(GcmcTrial) * (size_t)kGcmcTrialBatch +
                sizeof(int) * (size_t)(d.max_rep_cap / kGcmcThreads + 2);
   if (shm > 48 * 1024)

@@ -265,7 +265,7 @@ class Simulation:
         return ms.value
 
     PHASES = ["integrate", "force_pairs", "force_sum", "test_update1", "overlap",
-              "test_update2", "commit", "gcmc", "rho_piston"]
+              "test_update2", "commit", "gcmc_cells", "gcmc", "rho_piston"]
 
     def profile_steps(self, n, flush_l2=True):
         """Per-phase device time [ms] summed over n un-graphed steps."""

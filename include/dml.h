@@ -228,8 +228,10 @@ int dml_sync(dml_ctx* c);
  * each bracketed by CUDA events on the context stream; with flush_l2 a
  * 256 MiB buffer is overwritten between steps, outside the events.  *ms is
  * the sum of the per-step device times.  dml_profile_steps runs nsteps steps
- * without the graph, recording an event at every phase boundary, and adds
- * the device time of phase k (DML_PHASE_*) to phase_ms[k].
+ * without the graph but with the graph's kernels (the rebuild condition of
+ * each test_update is read on the host, and the idle time of that read is
+ * not counted), recording an event at every phase boundary, and adds the
+ * device time of phase k (DML_PHASE_*) to phase_ms[k].
  * dml_launches_per_step returns the kernels a step launches when the list is
  * not rebuilt (or -status); *per_rebuild (may be NULL) receives the kernels
  * each list rebuild adds (the rebuild is a conditional graph node). */
@@ -241,9 +243,10 @@ enum {
   DML_PHASE_OVERLAP = 4,     /* overlap_moveback */
   DML_PHASE_TEST_UPDATE2 = 5,/* test_update after the overlaps */
   DML_PHASE_COMMIT = 6,      /* F -> CG commit */
-  DML_PHASE_GCMC = 7,        /* gcmc_run (empty without the GCMC reservoir) */
-  DML_PHASE_RHO_PISTON = 8,  /* calc_rho + maxz */
-  DML_NPHASE = 9
+  DML_PHASE_GCMC_CELLS = 7,  /* gcmc_run: cell sort of the current positions */
+  DML_PHASE_GCMC = 8,        /* gcmc_run: the trials (empty without GCMC) */
+  DML_PHASE_RHO_PISTON = 9,  /* calc_rho + maxz */
+  DML_NPHASE = 10
 };
 int dml_time_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* ms);
 int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phase_ms,
