@@ -636,6 +636,14 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.rank_pre, nrep + 1);
   AL(d.reb_pre, nrep + 1);
   AL(d.big_cells, ncell + 1);
+  if (c->P.reservoir == DML_RESERVOIR_GCMC) {
+    const bool par = c->P.nadj <= kGcmcMaxTrials;
+    AL(d.grp, nrep);
+    AL(d.gpre, par ? (size_t)nrep * kGcmcMaxTrials : 1);
+    AL(d.gpm, par ? (size_t)nrep * kGcmcMaxTrials * kGcmcMaskW : 1);
+    AL(d.gw_mem, par ? (size_t)cap / 32 : 1);
+    AL(d.gw_slab, par ? (size_t)cap / 32 : 1);
+  }
 #undef AL
 
   // Host staging, position order (replica r at [base, base + cap)).

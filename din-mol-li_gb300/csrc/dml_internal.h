@@ -146,6 +146,36 @@ struct KParams {
   int nadj;
 };
 
+// gcmc_run of a replica with linked cells (the trials' searches limited to
+// the 27 cells around each trial point): per-trial data found in parallel
+// before the trials are decided in order.
+constexpr int kGcmcMaxTrials = 256;  // trials per call on this path (nadj)
+constexpr int kGcmcMaskW = kGcmcMaxTrials / 32;
+constexpr int kGcmcBlk = 8;          // gcmc members within rc of a trial point
+constexpr int kGcmcCand = 48;        // atoms within rc + skin of a trial point
+
+struct GcmcTrialPre {
+  double4 r;                 // trial point (dana.F90:643-645)
+  double coin, uacc, upick;  // the trial's uniforms (dana.F90:627-686)
+  double nv[3];              // Maxwell normals of an insertion (dana.F90:666-668)
+  int cell;                  // linear cell of the point
+  int n_blk;                 // gcmc members within rc (their gcmc%alist positions)
+  int n_cand;                // atoms within rc + skin of the 27 cells, stencil order
+  unsigned dup;              // bit q: stencil cell q repeats an earlier one
+  int cells[27];             // the stencil cells (map order)
+  int blk[kGcmcBlk];
+  int cand[kGcmcCand];       // hs slots
+  unsigned char cq[kGcmcCand];  // stencil index of the candidate
+  unsigned char cf[kGcmcCand];  // 1: own list (rd < (rc+skin)^2), 2: append (rd <= ...)
+};
+
+struct GcmcRepPre {
+  int fast;                  // this replica's trials run on the parallel path
+  int n_in, first, last, ng; // in-slab members, first/last member position, positions used
+  int n_holes, n_bholes;     // free hs / hs%b slots found (the first ones, ascending)
+  int holes[kGcmcMaxTrials], bholes[kGcmcMaxTrials];
+};
+
 // All device buffers of one context.
 struct Dev {
   double4 *pos, *vel, *acel, *force, *old_cg, *pos_old, *ranv;
@@ -184,6 +214,11 @@ struct Dev {
   int* reb_pre;       // [nrep + 1] the same prefix over the replicas whose list the
                       // last displacement test rebuilds (0 rows for the others)
   int* big_cells;     // cells too large for the per-thread sort of cell_order
+  // gcmc_run on the parallel path (allocated with the GCMC reservoir)
+  GcmcTrialPre* gpre;  // [nrep][kGcmcMaxTrials]
+  unsigned* gpm;       // [nrep][kGcmcMaxTrials][kGcmcMaskW] earlier trial points within rc
+  GcmcRepPre* grp;     // [nrep]
+  unsigned *gw_mem, *gw_slab;  // [cap / 32] membership / in-slab bits of gcmc%alist positions
   int nrep;
   int cap;            // positions over all replicas (sum of the replica caps)
   int max_rep_cap;    // largest replica capacity

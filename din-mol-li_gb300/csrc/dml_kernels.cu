@@ -2035,7 +2035,8 @@ __device__ __forceinline__ int stencil_cell(const RepConst& R, float4 Pf, const 
 // members (the template atom and the atom that receives the Maxwell
 // velocity) are tracked across trials.  Replicas without cells, or with an
 // atom in a halo cell, scan the whole group as the reference does.
-__global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
+__global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, int par) {
+  if (par && d.grp[blockIdx.x].fast) return;  // decided by gcmc_fast_kernel
   // dynamic shared memory: the trials, then in-slab members per gorder chunk
   extern __shared__ double4 s_dyn[];
   GcmcTrial* const s_tr = (GcmcTrial*)s_dyn;
@@ -2599,6 +2600,1012 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p) {
   }
 }
 
+// ------------------------------------------- gcmc_run with linked cells
+// The trials of gcmc_run are sequential, but on a replica with linked cells
+// whose atoms and trial points all lie in interior cells, everything a trial
+// reads can be found before any trial is decided:
+//  * its uniforms and point (keyed draws);
+//  * the gcmc members within rc of its point at the start of the call (the
+//    hard-core "blockers", recorded by gcmc%alist position): a member blocks
+//    the trial unless an earlier trial deleted it;
+//  * the earlier trial points within rc (an earlier insertion blocks it);
+//  * the atoms within rc + skin among its 27 stencil cells (own list and
+//    appends), each used unless deleted before the trial;
+//  * the membership and in-slab bits of every gcmc%alist position (the m-th
+//    in-slab member of a deletion);
+//  * the free hs and hs%b slots (igroup_attach_atom takes the first one).
+// gcmc_pre_kernel finds all of it, one block per replica; gcmc_fast_kernel
+// then decides the trials in order in one warp on shared-memory state and
+// applies their edits with the whole block.  A replica that does not
+// qualify (no cells, an atom or point in a halo cell, more than
+// kGcmcMaxTrials trials, a point with more than kGcmcBlk blockers or
+// kGcmcCand list atoms) runs gcmc_kernel instead.
+constexpr int kGcmcPreThreads = 1024;
+
+__device__ __forceinline__ bool hard_core_in(const KParams& p, const RepConst& R, double4 a,
+                                             float4 af, double4 b, float4 bf) {
+  // |a - b|^2 < rc^2 (dana.F90:649-651), FP32 outside the margins
+  float fx, fy, fz;
+  vdist_nint_f(R, af, bf, fx, fy, fz);
+  const float df = fx * fx + fy * fy + fz * fz;
+  if (df > p.rc_hi2) return false;
+  if (df < p.rc_lo2) return true;
+  double vx, vy, vz;
+  vdist_nint(R, a, b, vx, vy, vz);
+  return dot3(vx, vy, vz) < p.rc2;
+}
+
+// First `want` positions q in [lo, hi) with free(q), ascending, into out[];
+// returns how many were found.  Every thread of the block calls it.
+template <class Pred>
+__device__ int blk_collect(int lo, int hi, int want, Pred free_at, int* out, int* s_cnt) {
+  if (threadIdx.x == 0) *s_cnt = 0;
+  __syncthreads();
+  for (int base = lo; base < hi && *s_cnt < want; base += (int)blockDim.x) {
+    const int q = base + (int)threadIdx.x;
+    const bool f = q < hi && free_at(q);
+    int tot;
+    const int pre = blk_scan_excl(f ? 1 : 0, &tot);
+    const int c0 = *s_cnt;
+    if (f && c0 + pre < want) out[c0 + pre] = q;
+    __syncthreads();
+    if (threadIdx.x == 0) *s_cnt = c0 + tot;
+    __syncthreads();
+  }
+  const int n = min(*s_cnt, want);
+  __syncthreads();
+  return n;
+}
+
+__global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParams p) {
+  const int rep = blockIdx.x;
+  const RepConst& R = d.rc[rep];
+  Scalars* const sc = d.sc + rep;
+  GcmcRepPre* const gr = d.grp + rep;
+  const int B = R.base, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
+  const int nw = nt >> 5;
+  __shared__ int s_bad, s_cnt, s_ncrt;
+  __shared__ int s_lo, s_hi, s_nin;
+  __shared__ double4 s_r[kGcmcMaxTrials];
+  __shared__ float4 s_rf[kGcmcMaxTrials];
+  __shared__ unsigned char s_crt[kGcmcMaxTrials];
+  __shared__ int s_tab[32][56];  // per warp: stencil cell starts and prefixes
+  if (!sc->listed) {  // gcmc_kernel reports the state error
+    if (tid == 0) gr->fast = 0;
+    return;
+  }
+  // order arrays grow by appends: compact them before they could overflow
+  if (sc->n_rank + p.nadj >= R.cap) {
+    int n = blk_compact(d.ref, B, sc->n_rank, d.rank);
+    if (tid == 0) sc->n_rank = n;
+    __syncthreads();
+  }
+  if (sc->n_alist + p.nadj >= R.cap) {
+    int n = blk_compact(d.alist, B, sc->n_alist, d.apos);
+    if (tid == 0) sc->n_alist = n;
+    __syncthreads();
+  }
+  if (sc->n_gorder + p.nadj >= R.cap) {
+    int n = blk_compact(d.gorder, B, sc->n_gorder, d.gpos);
+    if (tid == 0) sc->n_gorder = n;
+    __syncthreads();
+  }
+  if (tid == 0) {
+    s_bad = !(R.use_cells && !sc->halo && p.nadj <= kGcmcMaxTrials);
+    s_ncrt = 0;
+    s_lo = INT_MAX;
+    s_hi = -1;
+    s_nin = 0;
+  }
+  __syncthreads();
+  if (s_bad) {
+    if (tid == 0) gr->fast = 0;
+    return;
+  }
+  const long long step = d.g->step;
+  const double z0 = sc->z0, zmax = sc->zmax;
+  const int ng = sc->n_gorder;
+  GcmcTrialPre* const pre = d.gpre + (size_t)rep * kGcmcMaxTrials;
+  unsigned* const pm = d.gpm + (size_t)rep * kGcmcMaxTrials * kGcmcMaskW;
+
+  // Membership and in-slab bits of the gcmc%alist positions [0, ng), the
+  // first and last member and the control-volume count (dana.F90:601-606).
+  {
+    unsigned* wm = d.gw_mem + B / 32;
+    unsigned* wsl = d.gw_slab + B / 32;
+    int lo = INT_MAX, hi = -1, cnt = 0;
+    constexpr int U = 4;  // positions per thread per round, loads in flight together
+    for (int base = 0; base < ng; base += U * nt) {
+      int h[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = base + u * nt + tid;
+        h[u] = i < ng ? d.gorder[B + i] : -1;
+      }
+      double zz[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) zz[u] = h[u] >= 0 ? d.pos[h[u]].z : 0.0;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = base + u * nt + tid;
+        const bool mem = h[u] >= 0;
+        const bool in = mem && in_slab(zz[u], z0, zmax);
+        const unsigned bm = __ballot_sync(0xffffffffu, mem);
+        const unsigned bs = __ballot_sync(0xffffffffu, in);
+        if (lane == 0 && i < ng) {
+          wm[i >> 5] = bm;
+          wsl[i >> 5] = bs;
+        }
+        if (mem) {
+          lo = min(lo, i);
+          hi = max(hi, i);
+        }
+        cnt += in;
+      }
+    }
+    // words past the used positions start empty (appends set their bits)
+    const int w0 = (ng + 31) >> 5, w1 = min((ng + p.nadj + 64) >> 5, R.cap >> 5);
+    for (int w = w0 + tid; w < w1; w += nt) {
+      wm[w] = 0u;
+      wsl[w] = 0u;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      lo = min(lo, __shfl_down_sync(0xffffffffu, lo, off));
+      hi = max(hi, __shfl_down_sync(0xffffffffu, hi, off));
+      cnt += __shfl_down_sync(0xffffffffu, cnt, off);
+    }
+    if (lane == 0) {
+      atomicMin(&s_lo, lo);
+      atomicMax(&s_hi, hi);
+      atomicAdd(&s_nin, cnt);
+    }
+  }
+
+  // The trials' draws (dana.F90:620-690, keyed Philox) and points.
+  if (tid < p.nadj) {
+    const int t = tid + 1;
+    GcmcTrialPre& tr = pre[tid];
+    dml_u4 w0 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 0);
+    dml_u4 w1 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 1);
+    dml_u4 w2 = dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC, 2);
+    const double coin = dml_u53(w0.w[0], w0.w[1]);
+    const double r0 = dml_u53(w1.w[0], w1.w[1]) * R.box[0];
+    const double r1 = dml_u53(w1.w[2], w1.w[3]) * R.box[1];
+    const double r2 = dml_u53(w2.w[0], w2.w[1]) * (zmax - z0) + z0;
+    const double4 r = make_double4(r0, r1, r2, 0.0);
+    const float4 rf = make_float4((float)r0, (float)r1, (float)r2, 0.0f);
+    tr.r = r;
+    tr.coin = coin;
+    tr.uacc = dml_u53(w0.w[2], w0.w[3]);
+    tr.upick = dml_u53(w2.w[2], w2.w[3]);
+    const bool crt = coin < 0.5;
+    s_r[tid] = r;
+    s_rf[tid] = rf;
+    s_crt[tid] = crt;
+    tr.n_blk = 0;
+    tr.n_cand = 0;
+    if (crt) {
+      atomicAdd(&s_ncrt, 1);
+      double nv[4];
+      dml_normal_quad(dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC_VEL, 0), nv);
+      tr.nv[0] = nv[0];
+      tr.nv[1] = nv[1];
+      tr.nv[2] = nv[2];
+      int c1, c2, c3;
+      cell_index3(R, rf, &r, c1, c2, c3);
+      // a point outside the interior cells (or the tessellation) takes the
+      // sequential path, which reports or handles it as the reference does
+      if (c1 < 1 || c2 < 1 || c3 < 1 || c1 > R.ncells[0] || c2 > R.ncells[1] || c3 > R.ncells[2])
+        s_bad = 1;
+      tr.cell = R.cell_off + (c3 * R.head_dim[1] + c2) * R.head_dim[0] + c1;
+    }
+  }
+  __syncthreads();
+
+  // Earlier creation points within rc of each creation point: an accepted
+  // earlier insertion sits there during this trial's hard-core test.
+  if (tid < p.nadj) {
+    unsigned m[kGcmcMaskW];
+#pragma unroll
+    for (int w = 0; w < kGcmcMaskW; ++w) m[w] = 0u;
+    if (s_crt[tid]) {
+      const double4 a = s_r[tid];
+      const float4 af = s_rf[tid];
+      for (int j = 0; j < tid; ++j)
+        if (s_crt[j] && hard_core_in(p, R, a, af, s_r[j], s_rf[j])) m[j >> 5] |= 1u << (j & 31);
+    }
+#pragma unroll
+    for (int w = 0; w < kGcmcMaskW; ++w) pm[tid * kGcmcMaskW + w] = m[w];
+  }
+
+  // Blockers and list candidates of every creation trial, one warp each,
+  // over the 27 stencil cells of the cell sort of this call.
+  int* tab = s_tab[wid];
+  for (int i = wid; i < p.nadj; i += nw) {
+    if (!s_crt[i]) continue;
+    GcmcTrialPre& tr = pre[i];
+    const double4 Rt = s_r[i];
+    const float4 Rtf = s_rf[i];
+    int num = 0, c = -1;
+    if (lane < 27) {
+      c = stencil_cell(R, Rtf, &Rt, lane);
+      const int st = d.cell_start[c];
+      num = d.cell_start[c + 1] - st;
+      tab[lane] = st;
+      tr.cells[lane] = c;
+    }
+    bool dupl = false;
+    for (int q = 0; q < 26; ++q) {
+      const int cq = __shfl_sync(0xffffffffu, c, q);
+      if (q < lane && cq == c) dupl = true;
+    }
+    const unsigned dupm = __ballot_sync(0xffffffffu, lane < 27 && dupl);
+    int x = num;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane < 27) tab[27 + lane] = x - num;
+    const int T = __shfl_sync(0xffffffffu, x, 26);
+    __syncwarp();
+    int nb = 0, nc = 0;
+    for (int base = 0; base < T; base += 32) {
+      const int f = base + lane;
+      bool isb = false, isc = false;
+      int j = -1, q = 0, fl = 0;
+      if (f < T) {
+        int lo = 0, hi = 26;  // stencil cell holding f
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (tab[27 + mid] <= f) lo = mid; else hi = mid - 1;
+        }
+        q = lo;
+        j = d.cell_atoms[tab[q] + f - tab[27 + q]];
+        const float4 Q = d.posf[j];
+        float fx, fy, fz;
+        vdist_nint_f(R, Rtf, Q, fx, fy, fz);
+        const float df = fx * fx + fy * fy + fz * fz;
+        if (df <= p.rlist_hi2) {
+          double rd = -1.0;
+          if (!(df < p.rc_lo2 && df < p.rlist_lo2)) {
+            double vx, vy, vz;
+            vdist_nint(R, Rt, d.pos[j], vx, vy, vz);
+            rd = dot3(vx, vy, vz);
+          }
+          if (df <= p.rc_hi2 && d.in_gcmc[j] && (df < p.rc_lo2 || rd < p.rc2)) isb = true;
+          const bool live = d.state[j] == ST_LIVE;
+          const bool own = df < p.rlist_lo2 || rd < p.rlist2;
+          const bool app = df < p.rlist_lo2 || !(rd > p.rlist2);
+          if (live && own) fl |= 1;
+          if (live && app && !((dupm >> q) & 1u) && d.rank[j] >= 0) fl |= 2;
+          isc = fl != 0;
+        }
+      }
+      const unsigned bb = __ballot_sync(0xffffffffu, isb);
+      const unsigned bc = __ballot_sync(0xffffffffu, isc);
+      if (isb) {
+        const int k = nb + __popc(bb & ((1u << lane) - 1u));
+        if (k < kGcmcBlk) tr.blk[k] = d.gpos[j] - B;
+      }
+      if (isc) {
+        const int k = nc + __popc(bc & ((1u << lane) - 1u));
+        if (k < kGcmcCand) {
+          tr.cand[k] = j;
+          tr.cq[k] = (unsigned char)q;
+          tr.cf[k] = (unsigned char)fl;
+        }
+      }
+      nb += __popc(bb);
+      nc += __popc(bc);
+    }
+    if (lane == 0) {
+      tr.n_blk = nb;
+      tr.n_cand = nc;
+      tr.dup = dupm;
+      if (nb > kGcmcBlk || nc > kGcmcCand) s_bad = 1;
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // The first free hs and hs%b slots (igroup_attach_atom, Groups.F90:
+  // 1083-1093): every insertion takes the lowest, deletions free no hs slot
+  // (limbo) but free their hs%b slot at once.
+  const int ncrt = s_ncrt;
+  const int ns = sc->n_slots, nbs = sc->n_b;
+  const int holes = ns - sc->n_atoms - sc->nlimbo;
+  const int bholes = nbs - sc->b_nat;
+  const int8_t* st = d.state + B;
+  const int* b2 = d.b2hs + B;
+  int nh = 0, nbh = 0;
+  if (holes > 0 && ncrt > 0)
+    nh = blk_collect(sc->free_lo, ns, min(holes, ncrt), [&](int q) { return st[q] == ST_NULL; },
+                     gr->holes, &s_cnt);
+  if (bholes > 0 && ncrt > 0)
+    nbh = blk_collect(sc->bfree_lo, nbs, min(bholes, ncrt), [&](int q) { return b2[q] < 0; },
+                      gr->bholes, &s_cnt);
+  if (tid == 0) {
+    gr->n_holes = nh;
+    gr->n_bholes = nbh;
+    gr->n_in = s_nin;
+    gr->first = s_lo;
+    gr->last = s_hi;
+    gr->ng = ng;
+    gr->fast = !s_bad;
+  }
+}
+
+constexpr int kGcmcFastThreads = 512;
+constexpr int kGcmcAppCap = 768;  // appends kept in shared memory (else applied trial by trial)
+
+struct Vel3 {
+  double x, y, z;
+};
+
+// Shared state of gcmc_fast_kernel (dynamic shared memory, followed by the
+// in-slab counts per 1024 positions and, when they fit, the bit words).
+struct GcmcSm {
+  Scalars ss;
+  double uacc[kGcmcMaxTrials], upick[kGcmcMaxTrials];
+  unsigned char crt[kGcmcMaxTrials], rin[kGcmcMaxTrials];  // creation trial; point in the slab
+  int nblk[kGcmcMaxTrials];
+  int blk[kGcmcMaxTrials][kGcmcBlk];
+  unsigned pm[kGcmcMaxTrials][kGcmcMaskW];
+  unsigned acc[kGcmcMaskW];  // trials whose insertion is a member now
+  int holes[kGcmcMaxTrials], bholes[kGcmcMaxTrials];
+  int nholes, nbholes;
+  // accepted insertions, in trial order (local slots)
+  int ins_trial[kGcmcMaxTrials], ins_slot[kGcmcMaxTrials], ins_bslot[kGcmcMaxTrials];
+  int ins_fpos[kGcmcMaxTrials], ins_lpos[kGcmcMaxTrials], ins_gpos[kGcmcMaxTrials];
+  int ins_rank[kGcmcMaxTrials], ins_alist[kGcmcMaxTrials], ins_cell[kGcmcMaxTrials];
+  int ins_del[kGcmcMaxTrials];  // trial that deleted the inserted atom, or INT_MAX
+  long long ins_id[kGcmcMaxTrials];
+  int pos2ins[kGcmcMaxTrials];  // insertion at gcmc%alist position ng0 + x
+  // accepted deletions, in trial order
+  int del_trial[kGcmcMaxTrials], del_pos[kGcmcMaxTrials], del_slot[kGcmcMaxTrials];
+  int del_bslot[kGcmcMaxTrials], del_reused[kGcmcMaxTrials];
+  int freed[kGcmcMaxTrials], freed_del[kGcmcMaxTrials];
+  unsigned char freed_used[kGcmcMaxTrials];
+  int nins, ndel;
+  // edits
+  int href[kGcmcMaxTrials], hlast[kGcmcMaxTrials], href_ins[kGcmcMaxTrials];
+  int hlast_ins[kGcmcMaxTrials], root[kGcmcMaxTrials], htyp[kGcmcMaxTrials], ityp[kGcmcMaxTrials];
+  Vel3 tvel[kGcmcMaxTrials], fvel[kGcmcMaxTrials];
+  float4 nv[kGcmcMaxTrials];  // Maxwell normals (FP32 values, exact)
+  int mw_slot[kGcmcMaxTrials];
+  Vel3 mw_vel[kGcmcMaxTrials];
+  int n_mw;
+  int napp, app_over;
+  int app_j[kGcmcAppCap], app_k[kGcmcAppCap], app_base[kGcmcAppCap];
+};
+
+// The m-th (1-based) set bit of the in-slab words over positions [0, ng),
+// or -1; one warp.
+__device__ int warp_select(const unsigned* wsl, const int* grp, int ng, int m) {
+  const int lane = threadIdx.x & 31;
+  const int ngrp = (ng + 1023) >> 10;
+  int acc = 0;
+  for (int g0 = 0; g0 < ngrp; g0 += 32) {
+    const int g = g0 + lane;
+    const int c = g < ngrp ? grp[g] : 0;
+    int x = c;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    const unsigned hit = __ballot_sync(0xffffffffu, acc + x >= m);
+    if (hit) {
+      const int L = __ffs(hit) - 1;
+      const int gg = g0 + L;
+      const int mr = m - acc - __shfl_sync(0xffffffffu, x - c, L);
+      const int wi = gg * 32 + lane;
+      const unsigned w = wi * 32 < ng ? wsl[wi] : 0u;
+      const int wc = __popc(w);
+      int y = wc;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int z = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= o) y += z;
+      }
+      const unsigned hit2 = __ballot_sync(0xffffffffu, y >= mr);
+      if (!hit2) return -1;
+      const int L2 = __ffs(hit2) - 1;
+      const int k = mr - __shfl_sync(0xffffffffu, y - wc, L2);
+      const unsigned ww = __shfl_sync(0xffffffffu, w, L2);
+      const bool set = (ww >> lane) & 1u;
+      const int below = __popc(ww & ((1u << lane) - 1u));
+      const unsigned hit3 = __ballot_sync(0xffffffffu, set && below == k - 1);
+      if (!hit3) return -1;
+      return (gg * 32 + L2) * 32 + (__ffs(hit3) - 1);
+    }
+    acc += __shfl_sync(0xffffffffu, x, 31);
+  }
+  return -1;
+}
+
+// First member position >= from (INT_MAX if none) / last member position
+// <= from (-1 if none); one warp.
+__device__ int warp_next_member(const unsigned* wm, int from, int ng) {
+  const int lane = threadIdx.x & 31;
+  if (from >= ng) return INT_MAX;
+  const int wlast = (ng - 1) >> 5;
+  for (int w0 = from >> 5; w0 <= wlast; w0 += 32) {
+    const int wi = w0 + lane;
+    unsigned w = wi <= wlast ? wm[wi] : 0u;
+    if (wi == (from >> 5)) w &= 0xffffffffu << (from & 31);
+    const unsigned hit = __ballot_sync(0xffffffffu, w != 0u);
+    if (hit) {
+      const int L = __ffs(hit) - 1;
+      const unsigned ww = __shfl_sync(0xffffffffu, w, L);
+      const int pos = (w0 + L) * 32 + __ffs(ww) - 1;
+      return pos < ng ? pos : INT_MAX;
+    }
+  }
+  return INT_MAX;
+}
+
+__device__ int warp_prev_member(const unsigned* wm, int from) {
+  const int lane = threadIdx.x & 31;
+  if (from < 0) return -1;
+  for (int w0 = from >> 5; w0 >= 0; w0 -= 32) {
+    const int wi = w0 - lane;
+    unsigned w = wi >= 0 ? wm[wi] : 0u;
+    if (wi == (from >> 5)) {
+      const int b = from & 31;
+      w &= b == 31 ? 0xffffffffu : ((1u << (b + 1)) - 1u);
+    }
+    const unsigned hit = __ballot_sync(0xffffffffu, w != 0u);
+    if (hit) {
+      const int L = __ffs(hit) - 1;
+      const unsigned ww = __shfl_sync(0xffffffffu, w, L);
+      return (w0 - L) * 32 + 31 - __clz(ww);
+    }
+  }
+  return -1;
+}
+
+// Whether hs slot j was deleted by a trial before trial i (before == true)
+// or at any trial of this call (before == false).
+__device__ __forceinline__ bool deleted_by(const GcmcSm& S, int j, int i, bool before) {
+  for (int q = 0; q < S.ndel; ++q)
+    if (S.del_slot[q] == j && (!before || S.del_trial[q] < i)) return true;
+  return false;
+}
+
+// The rows that insertion k appends its atom to (ngroup_sort_atom,
+// Neighbor.F90:303-317): hs%ref members within rc + skin of its point, at
+// most one entry per row, among the 27 stencil cells: this call's earlier
+// insertions, then the cell atoms.  Rows of atoms deleted in this call end
+// empty and are skipped.  fn(j) is called by the lane holding target j.
+template <class Fn>
+__device__ void gcmc_append_targets(const Dev& d, const KParams& p, const RepConst& R,
+                                    const GcmcSm& S, const GcmcTrialPre* pre, int k, Fn fn) {
+  const int lane = threadIdx.x & 31;
+  const GcmcTrialPre& tr = pre[S.ins_trial[k]];
+  const double4 Rt = tr.r;
+  const unsigned dup = tr.dup;
+  const int mycell = lane < 27 ? tr.cells[lane] : -1;
+  for (int k0 = 0; k0 < k; k0 += 32) {
+    const int k2 = k0 + lane;
+    const bool valid = k2 < k && S.ins_del[k2] == INT_MAX;
+    const int c2 = valid ? S.ins_cell[k2] : -2;
+    bool in = false;
+    for (int q = 0; q < 27; ++q) {
+      const int cq = __shfl_sync(0xffffffffu, mycell, q);
+      in |= valid && cq == c2 && !((dup >> q) & 1u);
+    }
+    if (in) {
+      double vx, vy, vz;
+      vdist_nint(R, pre[S.ins_trial[k2]].r, Rt, vx, vy, vz);
+      if (!(dot3(vx, vy, vz) > p.rlist2)) fn(R.base + S.ins_slot[k2]);
+    }
+  }
+  const int nc = tr.n_cand;
+  for (int c = lane; c < nc; c += 32) {
+    if (!(tr.cf[c] & 2)) continue;
+    const int j = tr.cand[c];
+    if (!deleted_by(S, j, 0, false)) fn(j);
+  }
+}
+
+__global__ void __launch_bounds__(kGcmcFastThreads)
+    gcmc_fast_kernel(Dev d, KParams p, int wmax, int gmax, int words_smem) {
+  const int rep = blockIdx.x;
+  const GcmcRepPre* const gr = d.grp + rep;
+  if (!gr->fast) return;
+  extern __shared__ double4 s_dyn[];
+  GcmcSm& S = *reinterpret_cast<GcmcSm*>(s_dyn);
+  int* const grp = reinterpret_cast<int*>(reinterpret_cast<char*>(s_dyn) + sizeof(GcmcSm));
+  const RepConst& R = d.rc[rep];
+  Scalars* const sc_g = d.sc + rep;
+  const int B = R.base, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
+  const int nw = nt >> 5;
+  const GcmcTrialPre* const pre = d.gpre + (size_t)rep * kGcmcMaxTrials;
+  const unsigned* const pmg = d.gpm + (size_t)rep * kGcmcMaxTrials * kGcmcMaskW;
+  const int ng0 = gr->ng;
+  const int nwords = min((ng0 + p.nadj + 63) >> 5, R.cap >> 5);
+  const int ngrp = (nwords + 31) >> 5;
+  unsigned *wm = d.gw_mem + B / 32, *wsl = d.gw_slab + B / 32;
+  if (words_smem) {
+    unsigned* sw = reinterpret_cast<unsigned*>(grp + gmax);
+    for (int w = tid; w < nwords; w += nt) {
+      sw[w] = wm[w];
+      sw[wmax + w] = wsl[w];
+    }
+    wm = sw;
+    wsl = sw + wmax;
+  }
+  if (tid == 0) {
+    S.ss = *sc_g;
+    S.nholes = gr->n_holes;
+    S.nbholes = gr->n_bholes;
+    S.napp = 0;
+    S.app_over = 0;
+  }
+  for (int i = tid; i < p.nadj; i += nt) {
+    const GcmcTrialPre& tr = pre[i];
+    S.crt[i] = tr.coin < 0.5;
+    S.rin[i] = in_slab(tr.r.z, sc_g->z0, sc_g->zmax);
+    S.uacc[i] = tr.uacc;
+    S.upick[i] = tr.upick;
+    S.nblk[i] = tr.coin < 0.5 ? tr.n_blk : 0;
+  }
+  for (int e = tid; e < p.nadj * kGcmcBlk; e += nt) {
+    const int i = e / kGcmcBlk, q = e - i * kGcmcBlk;
+    S.blk[i][q] = pre[i].blk[q];
+  }
+  for (int e = tid; e < p.nadj * kGcmcMaskW; e += nt) S.pm[e / kGcmcMaskW][e % kGcmcMaskW] = pmg[e];
+  for (int e = tid; e < kGcmcMaxTrials; e += nt) {
+    S.holes[e] = gr->holes[e];
+    S.bholes[e] = gr->bholes[e];
+  }
+  if (tid < kGcmcMaskW) S.acc[tid] = 0u;
+  __syncthreads();
+  // in-slab members per 1024 positions
+  for (int g = wid; g < ngrp; g += nw) {
+    const int wi = g * 32 + lane;
+    int c = wi < nwords ? __popc(wsl[wi]) : 0;
+    for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
+    if (lane == 0) grp[g] = c;
+  }
+  __syncthreads();
+
+  // The trials in order (dana.F90:620-710), one warp, shared state only.
+  if (wid == 0) {
+    const double z0 = S.ss.z0, zmax = S.ss.zmax;
+    const double v = R.box[0] * R.box[1] * (zmax - z0);
+    int n = gr->n_in, first = gr->first, last = gr->last, ng = ng0;
+    int ns = S.ss.n_slots, nb = S.ss.n_b, n_atoms = S.ss.n_atoms, nlimbo = S.ss.nlimbo;
+    int b_nat = S.ss.b_nat, free_lo = S.ss.free_lo, bfree_lo = S.ss.bfree_lo;
+    int n_alist = S.ss.n_alist, n_rank = S.ss.n_rank;
+    long long next_id = S.ss.next_id;
+    int hi = 0, bhi = 0, nins = 0, ndel = 0;
+    int err = 0, err_info = 0;
+    for (int i = 0; i < p.nadj; ++i) {
+      __syncwarp();
+      const int t = i + 1;
+      if (first == INT_MAX) {
+        err = DML_E_NO_PARTICLES;
+        err_info = t;
+        break;
+      }
+      const double uacc = S.uacc[i];
+      if (S.crt[i]) {
+        // creation attempt (dana.F90:627-677)
+        if (p.act * v / (double)(n + 1) < uacc) continue;
+        bool ov = false;
+        if (lane < S.nblk[i]) {
+          const int bp = S.blk[i][lane];
+          bool gone = false;
+          for (int q = 0; q < ndel; ++q) gone |= S.del_pos[q] == bp;
+          ov = !gone;
+        }
+        if (lane < kGcmcMaskW && (S.pm[i][lane] & S.acc[lane]) != 0u) ov = true;
+        if (__any_sync(0xffffffffu, ov)) continue;
+        // first free hs slot (limbo slots are not free) and hs%b slot
+        int lslot;
+        if (ns >= n_atoms + 1 + nlimbo) {
+          if (hi >= S.nholes) {
+            err = DML_E_INDEX;
+            err_info = t;
+            break;
+          }
+          lslot = S.holes[hi++];
+        } else {
+          lslot = ns;
+        }
+        int lbs;
+        if (nb >= b_nat + 1) {
+          const int co = bhi < S.nbholes ? S.bholes[bhi] : INT_MAX;
+          int fm = INT_MAX, fi = -1;
+          for (int q0 = 0; q0 < ndel; q0 += 32) {
+            const int q = q0 + lane;
+            const int val = q < ndel && !S.freed_used[q] ? S.freed[q] : INT_MAX;
+            const int mn = __reduce_min_sync(0xffffffffu, val);
+            if (mn < fm) {
+              fm = mn;
+              fi = q0 + __ffs(__ballot_sync(0xffffffffu, val == mn)) - 1;
+            }
+          }
+          if (co == INT_MAX && fm == INT_MAX) {
+            err = DML_E_INDEX;
+            err_info = t;
+            break;
+          }
+          if (co < fm) {
+            lbs = co;
+            ++bhi;
+          } else {
+            lbs = fm;
+            if (lane == 0) {
+              S.freed_used[fi] = 1;
+              S.del_reused[S.freed_del[fi]] = 1;
+            }
+          }
+        } else {
+          lbs = nb;
+        }
+        if (lslot >= R.cap || lbs >= R.cap || n_rank >= R.cap || n_alist >= R.cap || ng >= R.cap) {
+          err = DML_E_CAPACITY;
+          err_info = t;
+          break;
+        }
+        const bool in = S.rin[i] != 0;
+        if (lane == 0) {
+          S.ins_trial[nins] = i;
+          S.ins_slot[nins] = lslot;
+          S.ins_bslot[nins] = lbs;
+          S.ins_fpos[nins] = first;
+          S.ins_lpos[nins] = last;
+          S.ins_gpos[nins] = ng;
+          S.ins_rank[nins] = n_rank;
+          S.ins_alist[nins] = n_alist;
+          S.ins_id[nins] = next_id;
+          S.ins_del[nins] = INT_MAX;
+          S.pos2ins[ng - ng0] = nins;
+          wm[ng >> 5] |= 1u << (ng & 31);
+          if (in) {
+            wsl[ng >> 5] |= 1u << (ng & 31);
+            grp[ng >> 10] += 1;
+          }
+          S.acc[i >> 5] |= 1u << (i & 31);
+        }
+        n += 1;
+        last = ng;
+        ng += 1;
+        n_alist += 1;
+        n_rank += 1;
+        if (lbs == nb) nb += 1;
+        b_nat += 1;
+        bfree_lo = lbs + 1;
+        if (lslot == ns) ns += 1;
+        free_lo = lslot + 1;
+        n_atoms += 1;
+        next_id += 1;
+        nins += 1;
+      } else {
+        // destruction attempt (dana.F90:680-707)
+        if ((double)n / (v * p.act) < uacc) continue;
+        int m = (int)floor(S.upick[i] * (double)n) + 1;
+        if (m > n) m = n;
+        // m <= 0: the walk never reaches m == 0 and ends on the last member
+        const int psel = m <= 0 ? last : warp_select(wsl, grp, ng, m);
+        if (psel < 0) {
+          err = DML_E_CHOSEN_MISSING;
+          err_info = t;
+          break;
+        }
+        int h, bsl, kins = -1;
+        if (psel >= ng0) {
+          kins = S.pos2ins[psel - ng0];
+          h = B + S.ins_slot[kins];
+          bsl = S.ins_bslot[kins];
+        } else {
+          int hh = 0, bb = 0;
+          if (lane == 0) {
+            hh = d.gorder[B + psel];
+            bb = d.bslot[hh] - B;
+          }
+          h = __shfl_sync(0xffffffffu, hh, 0);
+          bsl = __shfl_sync(0xffffffffu, bb, 0);
+        }
+        const bool was_in = (wsl[psel >> 5] >> (psel & 31)) & 1u;
+        if (lane == 0) {
+          S.del_trial[ndel] = i;
+          S.del_pos[ndel] = psel;
+          S.del_slot[ndel] = h;
+          S.del_bslot[ndel] = bsl;
+          S.del_reused[ndel] = 0;
+          S.freed[ndel] = bsl;
+          S.freed_del[ndel] = ndel;
+          S.freed_used[ndel] = 0;
+          if (kins >= 0) {
+            S.ins_del[kins] = i;
+            const int ti = S.ins_trial[kins];
+            S.acc[ti >> 5] &= ~(1u << (ti & 31));
+          }
+          wm[psel >> 5] &= ~(1u << (psel & 31));
+          if (was_in) {
+            wsl[psel >> 5] &= ~(1u << (psel & 31));
+            grp[psel >> 10] -= 1;
+          }
+        }
+        ndel += 1;
+        if (bsl < bfree_lo) bfree_lo = bsl;
+        b_nat -= 1;
+        nlimbo += 1;
+        n_atoms -= 1;
+        n -= 1;
+        __syncwarp();
+        // new first / last member when one of them left the group
+        if (psel == first) first = warp_next_member(wm, psel + 1, ng);
+        if (psel == last) last = warp_prev_member(wm, psel - 1);
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      if (err) raise_error(d.g, err, err_info);
+      S.nins = nins;
+      S.ndel = ndel;
+      S.ss.n_slots = ns;
+      S.ss.n_b = nb;
+      S.ss.n_atoms = n_atoms;
+      S.ss.nlimbo = nlimbo;
+      S.ss.b_nat = b_nat;
+      S.ss.free_lo = free_lo;
+      S.ss.bfree_lo = bfree_lo;
+      S.ss.n_alist = n_alist;
+      S.ss.n_rank = n_rank;
+      S.ss.n_gorder = ng;
+      S.ss.next_id = next_id;
+      S.ss.n_ref += nins;
+      S.ss.n_gcmc += nins - ndel;
+      S.ss.gcmc_ins += (unsigned long long)nins;
+      S.ss.gcmc_del += (unsigned long long)ndel;
+      S.ss.halo = 0;
+    }
+  }
+  __syncthreads();
+  const int nins = S.nins, ndel = S.ndel;
+
+  // Templates (the first member) and Maxwell targets (the last member) of
+  // the insertions, as hs slots; pre-call values of the pre-call atoms.
+  for (int k = tid; k < nins; k += nt) {
+    const int fp = S.ins_fpos[k], lp = S.ins_lpos[k];
+    int hr, hri, hl, hli;
+    if (fp >= ng0) {
+      hri = S.pos2ins[fp - ng0];
+      hr = B + S.ins_slot[hri];
+    } else {
+      hri = -1;
+      hr = d.gorder[B + fp];
+    }
+    if (lp >= ng0) {
+      hli = S.pos2ins[lp - ng0];
+      hl = B + S.ins_slot[hli];
+    } else {
+      hli = -1;
+      hl = d.gorder[B + lp];
+    }
+    S.href[k] = hr;
+    S.href_ins[k] = hri;
+    S.hlast[k] = hl;
+    S.hlast_ins[k] = hli;
+    if (hri < 0) {
+      const double4 v0 = d.vel[hr];
+      S.tvel[k] = Vel3{v0.x, v0.y, v0.z};
+      S.htyp[k] = d.typ[hr];
+    }
+    const GcmcTrialPre& tr = pre[S.ins_trial[k]];
+    S.nv[k] = make_float4((float)tr.nv[0], (float)tr.nv[1], (float)tr.nv[2], 0.0f);
+    S.ins_cell[k] = tr.cell;
+  }
+  __syncthreads();
+  // atom_asign copies the template's velocity, then the Maxwell velocity
+  // goes to the last member (dana.F90:659-668): resolved in trial order.
+  if (tid == 0) {
+    int nmw = 0;
+    for (int k = 0; k < nins; ++k) {
+      const int hri = S.href_ins[k];
+      Vel3 tv;
+      int typ;
+      if (hri >= 0) {
+        S.root[k] = S.root[hri];
+        typ = S.ityp[hri];
+        tv = S.fvel[hri];
+      } else {
+        S.root[k] = S.href[k];
+        typ = S.htyp[k];
+        tv = S.tvel[k];
+        for (int q = nmw - 1; q >= 0; --q)
+          if (S.mw_slot[q] == S.href[k]) {
+            tv = S.mw_vel[q];
+            break;
+          }
+      }
+      S.ityp[k] = typ;
+      S.tvel[k] = tv;
+      S.fvel[k] = tv;
+      const double beta = p.beta_t[typ - 1];
+      const float4 nv = S.nv[k];
+      const Vel3 mv = Vel3{beta * (double)nv.x, beta * (double)nv.y, beta * (double)nv.z};
+      const int hli = S.hlast_ins[k];
+      if (hli >= 0) {
+        S.fvel[hli] = mv;
+      } else {
+        int q = 0;
+        while (q < nmw && S.mw_slot[q] != S.hlast[k]) ++q;
+        if (q == nmw) {
+          S.mw_slot[q] = S.hlast[k];
+          nmw += 1;
+        }
+        S.mw_vel[q] = mv;
+      }
+    }
+    S.n_mw = nmw;
+  }
+  __syncthreads();
+  // the inserted atoms (atom_asign and the attach loop, dana.F90:659-675)
+  for (int k = tid; k < nins; k += nt) {
+    const int slot = B + S.ins_slot[k], bs = B + S.ins_bslot[k];
+    const int root = S.root[k], typ = S.ityp[k];
+    const double4 tf = d.force[root], ta = d.acel[root];
+    const double te = d.epot[root];
+    const double4 Rt = pre[S.ins_trial[k]].r;
+    d.vel[slot] = make_double4(S.fvel[k].x, S.fvel[k].y, S.fvel[k].z, 0.0);
+    d.force[slot] = tf;
+    d.acel[slot] = ta;
+    d.epot[slot] = te;
+    d.typ[slot] = (int8_t)typ;
+    d.pos[slot] = Rt;
+    d.pos_old[slot] = Rt;
+    d.posf_old[slot] = make_float4((float)Rt.x, (float)Rt.y, (float)Rt.z, 0.0f);
+    d.old_cg[slot] = make_double4(1e8, 1e8, 1e8, 0.0);
+    d.posf[slot] = to_f4(Rt, typ);
+    d.skip[slot] = 0;
+    d.id[slot] = S.ins_id[k];
+    d.ev_count[slot] = 0;
+    d.alist[B + S.ins_alist[k]] = slot;
+    d.apos[slot] = B + S.ins_alist[k];
+    d.ref[B + S.ins_rank[k]] = slot;
+    d.rank[slot] = B + S.ins_rank[k];
+    // an atom deleted later in this call leaves its hs%b slot to the
+    // insertion that reuses it, or to the deletion that empties it
+    if (S.ins_del[k] == INT_MAX) d.b2hs[bs] = slot;
+    d.bslot[slot] = bs;
+    d.state[slot] = ST_LIVE;
+    d.gorder[B + S.ins_gpos[k]] = slot;
+    d.gpos[slot] = B + S.ins_gpos[k];
+    d.in_gcmc[slot] = 1;
+  }
+  for (int q = tid; q < S.n_mw; q += nt)
+    d.vel[S.mw_slot[q]] = make_double4(S.mw_vel[q].x, S.mw_vel[q].y, S.mw_vel[q].z, 0.0);
+  __syncthreads();
+  // the deleted atoms (atom_destroy: gcmc, hs (nn, hs%ref, hs%b), sys,
+  // Groups.F90:433-467); a freed hs%b slot that a later insertion took keeps it
+  for (int q = tid; q < ndel; q += nt) {
+    const int h = S.del_slot[q];
+    const int rk = d.rank[h], ap = d.apos[h];
+    const float4 pf = d.posf[h];
+    d.in_gcmc[h] = 0;
+    d.gorder[B + S.del_pos[q]] = -1;
+    d.nn[h] = 0;
+    if (rk >= 0) {
+      d.ref[rk] = -1;
+      d.rank[h] = -1;
+      atomicSub(&S.ss.n_ref, 1);
+    }
+    if (!S.del_reused[q]) d.b2hs[B + S.del_bslot[q]] = -1;
+    d.bslot[h] = -1;
+    d.state[h] = ST_LIMBO;
+    d.posf[h] = make_float4(pf.x, pf.y, pf.z, __int_as_float(0));
+    d.alist[ap] = -1;
+  }
+  __syncthreads();
+  // Own lists (ngroup_cells_atom, Neighbor.F90:550-603): per stencil cell,
+  // this call's earlier insertions in that cell (chain heads, most recent
+  // first), then the sorted cell; atoms deleted before the trial left.
+  for (int k = wid; k < nins; k += nw) {
+    if (S.ins_del[k] != INT_MAX) continue;  // deleted later: its row ends empty
+    const int i = S.ins_trial[k];
+    const GcmcTrialPre& tr = pre[i];
+    const double4 Rt = tr.r;
+    const int slot = B + S.ins_slot[k];
+    int* row = d.list + (size_t)slot * p.mnb;
+    const int mycell = lane < 27 ? tr.cells[lane] : -1;
+    const int nc = tr.n_cand;
+    int cnt = 0, ci = 0;
+    for (int q = 0; q < 27; ++q) {
+      const int cq = __shfl_sync(0xffffffffu, mycell, q);
+      for (int kb = k - 1; kb >= 0; kb -= 32) {
+        const int k2 = kb - lane;
+        bool inc = false;
+        int j = -1;
+        if (k2 >= 0 && S.ins_cell[k2] == cq && S.ins_del[k2] > i) {
+          j = B + S.ins_slot[k2];
+          double vx, vy, vz;
+          vdist_nint(R, pre[S.ins_trial[k2]].r, Rt, vx, vy, vz);
+          inc = dot3(vx, vy, vz) < p.rlist2;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, inc);
+        const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+        if (inc && pos < p.mnb) row[pos] = j;
+        cnt += __popc(bal);
+      }
+      // candidates are in stencil order: those of cell q start at ci
+      for (;;) {
+        const int c = ci + lane;
+        const int qc = c < nc ? (int)tr.cq[c] : 1000;
+        const bool mine = qc == q;
+        bool inc = false;
+        int j = -1;
+        if (mine && (tr.cf[c] & 1)) {
+          j = tr.cand[c];
+          inc = !deleted_by(S, j, i, true);
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, inc);
+        const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+        if (inc && pos < p.mnb) row[pos] = j;
+        cnt += __popc(bal);
+        const unsigned bm = __ballot_sync(0xffffffffu, mine);
+        ci += __popc(bm);
+        if (bm != 0xffffffffu) break;  // a later cell (or the end) reached
+      }
+    }
+    if (lane == 0) {
+      if (cnt > p.mnb) raise_error(d.g, DML_E_NEIGH_OVERFLOW, slot);
+      d.nn[slot] = cnt > p.mnb ? p.mnb : cnt;
+    }
+  }
+  __syncthreads();
+  // Appends (ngroup_sort_atom): row j receives the atoms of the insertions
+  // that reach it, in trial order, after what it holds.
+  for (int k = wid; k < nins; k += nw)
+    gcmc_append_targets(d, p, R, S, pre, k, [&](int j) {
+      const int e = atomicAdd(&S.napp, 1);
+      if (e < kGcmcAppCap) {
+        S.app_j[e] = j;
+        S.app_k[e] = k;
+      } else {
+        S.app_over = 1;
+      }
+    });
+  __syncthreads();
+  if (!S.app_over) {
+    const int na = S.napp;
+    for (int e = tid; e < na; e += nt) S.app_base[e] = d.nn[S.app_j[e]];
+    __syncthreads();
+    for (int e = tid; e < na; e += nt) {
+      const int j = S.app_j[e], k = S.app_k[e];
+      int before = 0, cnt = 0;
+      for (int f = 0; f < na; ++f)
+        if (S.app_j[f] == j) {
+          cnt += 1;
+          before += S.app_k[f] < k;
+        }
+      const int m = S.app_base[e] + before;
+      if (m < p.mnb) d.list[(size_t)j * p.mnb + m] = B + S.ins_slot[k];
+      else raise_error(d.g, DML_E_NEIGH_OVERFLOW, j);
+      if (before == cnt - 1) d.nn[j] = min(S.app_base[e] + cnt, p.mnb);
+    }
+  } else if (wid == 0) {
+    // more appends than the shared table holds: one insertion at a time
+    for (int k = 0; k < nins; ++k) {
+      gcmc_append_targets(d, p, R, S, pre, k, [&](int j) {
+        const int m = d.nn[j];
+        if (m >= p.mnb) {
+          raise_error(d.g, DML_E_NEIGH_OVERFLOW, j);
+          return;
+        }
+        d.list[(size_t)j * p.mnb + m] = B + S.ins_slot[k];
+        d.nn[j] = m + 1;
+      });
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  if (tid == 0) *sc_g = S.ss;
+}
+
 inline int nblk(int n, int b = kBlock) { return n > 0 ? (n + b - 1) / b : 1; }
 inline int nblk_warps(int n) { return n > 0 ? (n + (kBlock / 32) - 1) / (kBlock / 32) : 1; }
 // Fixed grid of the warp-per-row kernels (grid-stride over the rows): a
@@ -2789,11 +3796,25 @@ int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
 
 int k_gcmc_trials(const Dev& d, const KParams& p, cudaStream_t s) {
   int n = 0;
+  // the parallel path: shared state, in-slab counts and (if they fit) the bit words
+  static_assert(sizeof(GcmcSm) <= 96 * 1024, "gcmc_fast_kernel shared state");
+  const int wmax = d.max_rep_cap / 32, gmax = (wmax + 31) / 32 + 1;
+  size_t fshm = sizeof(GcmcSm) + sizeof(int) * (size_t)gmax;
+  const int words_smem = fshm + 2 * sizeof(unsigned) * (size_t)wmax <= 200 * 1024;
+  if (words_smem) fshm += 2 * sizeof(unsigned) * (size_t)wmax;
+  const int par = d.gpre != nullptr && d.grp != nullptr && p.nadj <= kGcmcMaxTrials &&
+                  fshm <= 220 * 1024;
+  if (par) {
+    cudaFuncSetAttribute(gcmc_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fshm);
+    gcmc_pre_kernel<<<d.nrep, kGcmcPreThreads, 0, s>>>(d, p);
+    gcmc_fast_kernel<<<d.nrep, kGcmcFastThreads, fshm, s>>>(d, p, wmax, gmax, words_smem);
+    n += 2;
+  }
   size_t shm = sizeof(GcmcTrial) * (size_t)kGcmcTrialBatch +
                sizeof(int) * (size_t)(d.max_rep_cap / kGcmcThreads + 2);
   if (shm > 48 * 1024)
     cudaFuncSetAttribute(gcmc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-  gcmc_kernel<<<d.nrep, kGcmcThreads, shm, s>>>(d, p);
+  gcmc_kernel<<<d.nrep, kGcmcThreads, shm, s>>>(d, p, par);
   return n + 1;
 }
 

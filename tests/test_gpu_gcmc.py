@@ -106,3 +106,37 @@ def test_config5_shape_gcmc_matches_oracle():
     assert_same_lists(g, o, "config-5 shape end", ld=512)
     c = g.counters()
     assert c["gcmc_ins"] > 50 and c["gcmc_del"] > 50 and c["nupd"] > 1
+
+
+@pytest.mark.parametrize("capacity", [0, 600000])
+def test_dense_gcmc_many_trials_matches_oracle(capacity):
+    """256 trials per step (the most one call decides on the parallel path)
+    at a high activity: insertions blocked by earlier insertions of the same
+    call, deletions of atoms inserted in the same call, hs%b slots freed and
+    taken again within one call, limbo slots freed by rebuilds.  The larger
+    capacity keeps the membership bits in global memory instead of shared
+    memory."""
+    p = systems.c5_params(seed=5, precision=dml.PRECISION_FP64, nadj=256, cells=12, n_ion=900)
+    p.box[2] = 80.0
+    p.z0, p.zmax = 50.0, 80.0
+    p.skin = 2.0
+    p.integrator = dml.INTEGRATOR_BROWNIAN
+    p.h = 1e-4
+    p.mnb = 256
+    if capacity:
+        p.capacity = capacity
+    atoms = dml.slab_system(12, 12, 2, 80.0, 900, 15.0, 80.0, 31, dmin=3.2)
+    p.act = 3.0 * systems.slab_activity(p, atoms, 5)
+    g, o = make_pair(p, atoms)
+    g.setup()
+    o.setup()
+    done = 0
+    for chunk in [1, 4, 15]:
+        g.step(chunk)
+        o.step(chunk)
+        done += chunk
+        assert_same_state(g, o, "dense gcmc after %d" % done, FIELDS)
+        assert_same_counters(g, o, "dense gcmc after %d" % done, COUNTERS)
+        assert_same_lists(g, o, "dense gcmc after %d" % done, ld=256)
+    c = g.counters()
+    assert c["gcmc_ins"] > 200 and c["gcmc_del"] > 200
