@@ -263,9 +263,10 @@ def timed_steps(sim, args, clocks=None):
 
 def force_error_probe(wl, nrep=4, steps=20):
     """Mixed vs FP64 forces on identical positions: replica r runs `steps`
-    plain steps, then its state is loaded into one context of each form and
-    both run test_update, ermak_a (FP64 in both forms, so the positions stay
-    identical) and fuerza.  Relative error per mobile ion: |F_mixed - F_fp64|
+    plain steps and one more ermak_a (the move that brings ions inside each
+    other's r0), then that state is loaded into one context of each form and
+    both run test_update and fuerza at those positions.  Relative error per
+    mobile ion: |F_mixed - F_fp64|
     / max(|F_fp64|, F_rms), F_rms the RMS force of the ions that interact
     (ions with no pair inside r0 have exactly zero force in both forms); also
     the absolute error and the relative error of the total energy."""
@@ -279,15 +280,14 @@ def force_error_probe(wl, nrep=4, steps=20):
         sp = wl.open(dml.PRECISION_FP64, replicas=[r])
         sp.setup()
         sp.step(steps)
+        sp.ermak_a(sp.counters()["step"] + 1)
         st = sp.get_atoms(replica=0) if wl.batched else sp.get_atoms()
-        stepno = sp.counters()["step"] + 1
         sp.close()
         out = []
         for prec in (dml.PRECISION_MIXED, dml.PRECISION_FP64):
             s = dml.Simulation(wl.replica_params(r, prec))
             s.set_atoms(st)
             s.test_update()
-            s.ermak_a(stepno)
             s.fuerza()
             a = s.get_atoms()
             out.append((a["force"], a["epot"], a["z"]))
@@ -312,7 +312,8 @@ def force_error_probe(wl, nrep=4, steps=20):
             "max_abs_ev_per_A": float(np.concatenate(absd).max() / EV) if absd else 0.0,
             "energy_rel": float(abs(emix - epl) / abs(epl)) if epl else 0.0,
             "interacting_ions": inter, "replicas": min(nrep, wl.n_rep),
-            "state": "after %d FP64 steps, then ermak_a + fuerza in both forms" % steps,
+            "state": "after %d FP64 steps and an FP64 ermak_a, fuerza in both forms at those "
+                     "positions" % steps,
             "tolerance": 1e-6, "within": bool(e.max() <= 1e-6)}
 
 

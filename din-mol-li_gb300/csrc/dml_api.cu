@@ -170,6 +170,21 @@ void make_kparams(const dml_params& P, double maxc, KParams& K) {
   K.beta_num = P.kb_module * P.temp;
   for (int t = 0; t < 3; ++t) K.beta_t[t] = std::sqrt(K.beta_num / P.mass[t]);
   K.nadj = P.nadj;
+  K.cc0f = (float)K.cc0;
+  K.cc1f = (float)K.cc1;
+  K.cc2f = (float)K.cc2;
+  K.cc2hf = (float)K.cc2h;
+  K.cc1mcc2f = (float)K.cc1mcc2;
+  K.crv1f = (float)K.crv1;
+  K.crv2f = (float)K.crv2;
+  for (int t = 0; t < 3; ++t) {
+    K.rfacf[t] = (float)K.rfac[t];
+    K.vfacf[t] = (float)K.vfac[t];
+    K.inv_massf[t] = (float)K.inv_mass[t];
+  }
+  K.fac_scf = (float)K.fac_sc;
+  K.fac_seif = (float)K.fac_sei;
+  K.inv_hf = (float)(1.0 / P.h);
 }
 
 int read_scalars(dml_ctx* c) {
@@ -550,7 +565,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   if (c->loaded) return DML_E_STATE;
   const int nrep = c->D.nrep;
   Dev& d = c->D;
-  // capacities: positions per replica, a multiple of the block size
+  // capacities: positions per replica, a multiple of kSpan
   int total = 0, ncell = 0, any_cells = 0, any_verlet = 0;
   for (int r = 0; r < nrep; ++r) {
     const dml_atoms* a = atoms + r;
@@ -558,11 +573,11 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     int want = c->P.capacity > 0 ? c->P.capacity
                                  : (c->P.reservoir == DML_RESERVOIR_GCMC ? 2 * a->n + 1024 : a->n);
     int cap = std::max(a->n, want);
-    cap = (cap + kBlock - 1) / kBlock * kBlock;
+    cap = (cap + kSpan - 1) / kSpan * kSpan;
     RepConst& R = c->rc[r];
     R.base = total;
     R.cap = cap;
-    R.nblk = cap / kBlock;
+    R.nblk = cap / kSpan;
     R.cell_off = ncell;
     ncell += R.ncell + (R.use_cells ? 1 : 0);  // + the replica's sentinel cell
     total += cap;
@@ -673,6 +688,10 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
       pos[h] = v3(a->pos, 0.0);
       vel[h] = v3(a->vel, 0.0);
       acel[h] = v3(a->acel, 0.0);
+      if (c->K.mixed) {  // FP32 velocity side (chosen form)
+        vel[h] = pack_f3((float)vel[h].x, (float)vel[h].y, (float)vel[h].z);
+        acel[h] = pack_f3((float)acel[h].x, (float)acel[h].y, (float)acel[h].z);
+      }
       force[h] = v3(a->force, 0.0);
       pos_old[h] = a->pos_old ? v3(a->pos_old, 0.0) : pos[h];
       old_cg[h] = v3(a->old_cg, 1e8);
@@ -1080,8 +1099,14 @@ int dml_get_atoms_replica(dml_ctx* c, int32_t rep, dml_atoms* a) {
       dst[3 * i + 2] = v.z;
     };
     put(a->pos, pos[h]);
-    put(a->vel, vel[h]);
-    put(a->acel, acel[h]);
+    if (c->K.mixed) {
+      const float4 v = unpack_f3(vel[h]), ac = unpack_f3(acel[h]);
+      put(a->vel, make_double4(v.x, v.y, v.z, 0.0));
+      put(a->acel, make_double4(ac.x, ac.y, ac.z, 0.0));
+    } else {
+      put(a->vel, vel[h]);
+      put(a->acel, acel[h]);
+    }
     put(a->force, force[h]);
     put(a->pos_old, pos_old[h]);
     put(a->old_cg, old_cg[h]);

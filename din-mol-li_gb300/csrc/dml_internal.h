@@ -28,13 +28,15 @@ enum { ST_NULL = 0, ST_LIVE = 1, ST_LIMBO = 2 };
 
 constexpr int kNearCap = 32;   // near-contact entries per atom (overlap)
 constexpr int kBlock = 256;
+constexpr int kSlotU = 4;                 // positions per thread of the per-position kernels
+constexpr int kSpan = kBlock * kSlotU;    // positions per block; replica capacities are multiples
 
 // Replicas.  A context holds one or more independent systems ("replicas",
 // the batched form); a single system is a batch of one.  Replica r owns the
 // positions [base, base + cap) of every per-atom array (hs slots, hs%b
 // slots, hs%ref ranks, sys%alist and gcmc%alist positions), with cap a
-// multiple of kBlock, so every thread block lies inside one replica and
-// loads its replica's constants and state once.
+// multiple of kSpan, so every thread block of the per-position kernels lies
+// inside one replica and loads its replica's constants and state once.
 
 // Per-replica constants (read-only during steps).
 struct RepConst {
@@ -48,7 +50,7 @@ struct RepConst {
   int use_cells;
   int cell_off, ncell;      // this replica's cells [cell_off, cell_off + ncell), then
                             // one sentinel cell (always empty) whose start is the end
-  int base, cap, nblk;      // positions [base, base + cap), cap / kBlock blocks
+  int base, cap, nblk;      // positions [base, base + cap), cap / kSpan blocks
   unsigned long long seed;  // Philox key of this replica
 };
 
@@ -144,7 +146,30 @@ struct KParams {
   // gcmc_run (dana.F90:590-713)
   double act, beta_num;     // beta = sqrt(beta_num / mass), beta_num = kB(module) * T
   int nadj;
+  // chosen form: the velocity-side constants in FP32
+  float cc0f, cc1f, cc2f, cc2hf, cc1mcc2f, crv1f, crv2f;
+  float rfacf[3], vfacf[3], inv_massf[3];
+  float fac_scf, fac_seif, inv_hf;
 };
+
+// Chosen form: velocities, accelerations and the Ermak velocity noise are
+// FP32, kept as a float4 (x, y, z, 0) in the first 16 bytes of their double4
+// slot, so the arrays and their copies are the same in both forms.
+__host__ __device__ inline double4 pack_f3(float x, float y, float z) {
+  double4 r = {0.0, 0.0, 0.0, 0.0};
+  float f[4] = {x, y, z, 0.0f};
+  unsigned char* dst = reinterpret_cast<unsigned char*>(&r);
+  const unsigned char* src = reinterpret_cast<const unsigned char*>(f);
+  for (int i = 0; i < 16; ++i) dst[i] = src[i];
+  return r;
+}
+__host__ __device__ inline float4 unpack_f3(const double4& v) {
+  float f[4];
+  const unsigned char* src = reinterpret_cast<const unsigned char*>(&v);
+  unsigned char* dst = reinterpret_cast<unsigned char*>(f);
+  for (int i = 0; i < 16; ++i) dst[i] = src[i];
+  return make_float4(f[0], f[1], f[2], 0.0f);
+}
 
 // gcmc_run of a replica with linked cells (the trials' searches limited to
 // the 27 cells around each trial point): per-trial data found in parallel

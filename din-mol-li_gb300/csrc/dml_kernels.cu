@@ -195,8 +195,15 @@ __device__ __forceinline__ int row_rank_in(const Dev& d, const int* pre, int i) 
 
 __device__ __forceinline__ int row_rank(const Dev& d, int i) { return row_rank_in(d, d.rank_pre, i); }
 
-// Replica of the block (replica capacities are multiples of the block size).
-__device__ __forceinline__ int block_rep(const Dev& d) { return d.rep_of[blockIdx.x * blockDim.x]; }
+// Per-position kernels: a block of kBlock threads covers kSpan consecutive
+// positions (kSlotU per thread, kBlock apart, so each load instruction of a
+// warp stays coalesced).  Replica capacities are multiples of kSpan, so a
+// block lies inside one replica and loads that replica's constants and live
+// counts once for all its positions.
+__device__ __forceinline__ int block_rep(const Dev& d) { return d.rep_of[blockIdx.x * kSpan]; }
+__device__ __forceinline__ int span_pos(int u) {
+  return blockIdx.x * kSpan + u * kBlock + (int)threadIdx.x;
+}
 
 __device__ __forceinline__ int warp_id_global() {
   return (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -291,18 +298,88 @@ __device__ __forceinline__ bool atom_pbc_dev(const KParams& p, const RepConst& R
   return depos;
 }
 
+// FP32 velocity-side values of the chosen form in their double4 slots.
+__device__ __forceinline__ float4 ldv(const double4* a, int h) {
+  return *reinterpret_cast<const float4*>(a + h);
+}
+__device__ __forceinline__ void stv(double4* a, int h, float x, float y, float z) {
+  *reinterpret_cast<float4*>(a + h) = make_float4(x, y, z, 0.0f);
+}
+
+// No atom_pbc action (wrap, mirror at zmax, capture at z <= 0) can apply to
+// a position whose FP32 copy lies farther than the margin from 0 and the box
+// edge in x and y and from 0 and zmax in z.
+__device__ __forceinline__ bool pbc_quiet(const KParams& p, const RepConst& R, float4 f,
+                                          float zmaxf) {
+  const float e = p.margin;
+  return f.x > e && f.x < R.boxf[0] - e && f.y > e && f.y < R.boxf[1] - e && f.z > e &&
+         f.z < zmaxf - e;
+}
+
+// ermak_a of the chosen form: each coordinate's increment (about 1e-2 Å per
+// step) is formed in FP32 from the FP32 velocity, acceleration and noise and
+// added to the FP64 position; atom_pbc runs in FP64 for the atoms near a
+// wall, the box edge or the capture plane, as in the plain form.
+__device__ __forceinline__ void ermak_a_mixed_atom(const Dev& d, const KParams& p,
+                                                   const RepConst& R, Scalars* sc, int h,
+                                                   long long step, double zmax) {
+  const double4 P = d.pos[h];
+  const float4 V = ldv(d.vel, h), A = ldv(d.acel, h);
+  int typ = d.typ[h];
+  const long long id = d.id[h];
+  const float rf = p.rfacf[typ - 1], vf = p.vfacf[typ - 1];
+  float nq[8];
+  dml_normal_quadf(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 0), &nq[0]);
+  dml_normal_quadf(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 1), &nq[4]);
+  const float vv[3] = {V.x, V.y, V.z}, aa[3] = {A.x, A.y, A.z};
+  double pp[3] = {P.x, P.y, P.z};
+  float rv[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    const float r1 = nq[2 * j], r2 = nq[2 * j + 1];
+    const float inc = p.cc1f * vv[j] + p.cc2hf * aa[j] + rf * r1;
+    pp[j] = pp[j] + (double)inc;
+    rv[j] = vf * (p.crv1f * r1 + p.crv2f * r2);
+  }
+  const int typ0 = typ;
+  const float4 before = d.posf[h];
+  float4 after = to_f4(make_double4(pp[0], pp[1], pp[2], 0.0), typ);
+  bool depos = false, po_changed = false, v_changed = false;
+  double4 po;
+  if (!pbc_quiet(p, R, after, (float)zmax)) {
+    po = d.pos_old[h];
+    double4 Vd = make_double4(V.x, V.y, V.z, 0.0);
+    depos = atom_pbc_dev(p, R, sc, step, id, pp, po, po_changed, Vd, v_changed, P, typ, zmax);
+    after = to_f4(make_double4(pp[0], pp[1], pp[2], 0.0), typ);
+  }
+  d.old_cg[h] = P;
+  d.pos[h] = make_double4(pp[0], pp[1], pp[2], 0.0);
+  d.posf[h] = after;
+  stv(d.ranv, h, rv[0], rv[1], rv[2]);
+  overlap_prepare_atom(d, R, h, before, after);
+  if (po_changed) {
+    d.pos_old[h] = po;
+    d.posf_old[h] = to_f4(po, 0);
+  }
+  if (v_changed) stv(d.vel, h, V.x, V.y, -V.z);  // the mirror at zmax reverses vz
+  if (typ != typ0) d.typ[h] = (int8_t)typ;
+  if (!depos) d.skip[h] = 0;
+}
+
 // ermak_a (dana.F90:974-1028): one thread per hs%ref member.
-__global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
-  // grids are sized by capacity; the block's replica gives the live count
-  const int rep = block_rep(d);
+__device__ __forceinline__ void ermak_a_at(Dev d, KParams p, int n_rank, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = pos;
   if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
   long long step = d.g->step;
   double zmax = sc->zmax;
+  if (p.mixed) {
+    ermak_a_mixed_atom(d, p, R, sc, h, step, zmax);
+    return;
+  }
   double4 P = d.pos[h];
   double4 V = d.vel[h];
   double4 A = d.acel[h];
@@ -343,13 +420,17 @@ __global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
   if (!depos) d.skip[h] = 0;
 }
 
-// cbrownian_hs (dana.F90:798-846): one thread per hs%ref member.
-__global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
-  // grids are sized by capacity; the block's replica gives the live count
+__global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
   const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) ermak_a_at(d, p, n_rank, rep, span_pos(u));
+}
+
+// cbrownian_hs (dana.F90:798-846): one thread per hs%ref member.
+__device__ __forceinline__ void brownian_at(Dev d, KParams p, int n_rank, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = pos;
   if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
@@ -358,6 +439,43 @@ __global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
   double4 P = d.pos[h];
   int typ = d.typ[h];
   long long id = d.id[h];
+  if (p.mixed) {
+    // chosen form: FP32 increments added to the FP64 position, FP32 velocity
+    const float facf = P.z > p.dif_switch_z ? p.fac_scf : p.fac_seif;
+    float nf[4];
+    dml_normal_quadf(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_BROWN, 0), nf);
+    double pp[3] = {P.x, P.y, P.z};
+    float vf[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const float inc = nf[j] * facf;
+      pp[j] = pp[j] + (double)inc;
+      vf[j] = inc * p.inv_hf;
+    }
+    const int typ0 = typ;
+    const float4 before = d.posf[h];
+    float4 after = to_f4(make_double4(pp[0], pp[1], pp[2], 0.0), typ);
+    bool depos = false, po_changed = false, v_changed = false;
+    double4 po;
+    if (!pbc_quiet(p, R, after, (float)zmax)) {
+      po = d.pos_old[h];
+      double4 Vd = make_double4(vf[0], vf[1], vf[2], 0.0);
+      depos = atom_pbc_dev(p, R, sc, step, id, pp, po, po_changed, Vd, v_changed, P, typ, zmax);
+      after = to_f4(make_double4(pp[0], pp[1], pp[2], 0.0), typ);
+    }
+    d.old_cg[h] = P;
+    d.pos[h] = make_double4(pp[0], pp[1], pp[2], 0.0);
+    d.posf[h] = after;
+    stv(d.vel, h, vf[0], vf[1], vf[2]);
+    overlap_prepare_atom(d, R, h, before, after);
+    if (po_changed) {
+      d.pos_old[h] = po;
+      d.posf_old[h] = to_f4(po, 0);
+    }
+    if (typ != typ0) d.typ[h] = (int8_t)typ;
+    if (!depos) d.skip[h] = 0;
+    return;
+  }
   double fac = P.z > p.dif_switch_z ? p.fac_sc : p.fac_sei;
   double nrm[4];
   dml_normal_quad(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_BROWN, 0), nrm);
@@ -387,6 +505,12 @@ __global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
   }
   if (typ != typ0) d.typ[h] = (int8_t)typ;
   if (!depos) d.skip[h] = 0;
+}
+
+__global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
+  const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) brownian_at(d, p, n_rank, rep, span_pos(u));
 }
 
 // Union-find over hs slots (overlap components): path halving, union by
@@ -612,30 +736,29 @@ __device__ __forceinline__ void ermak_b_atom(const Dev& d, const KParams& p, int
 // ermak_b of the mixed form: F/m as F * (1/m) (one FP64 multiply instead of
 // a division; the FP64 divide is a long sequence on GB300's narrow FP64
 // pipe), so the velocities differ from the plain form in the last bits.
+// ermak_b of the chosen form (FP32 velocity side); the force arrives as
+// FP32 (from the fixed-point sums), zero for the many atoms with no pair.
 __device__ __forceinline__ void ermak_b_atom_mixed(const Dev& d, const KParams& p, int h, int typ,
-                                                   double4 F) {
+                                                   float fx, float fy, float fz) {
   if (typ == DML_Z_CG) return;
-  const double im = p.inv_mass[typ - 1];
-  double4 V = d.vel[h], A = d.acel[h], R = d.ranv[h];
-  double ax = F.x * im, ay = F.y * im, az = F.z * im;
-  V.x = p.cc0 * V.x + p.cc1mcc2 * A.x + p.cc2 * ax + R.x;
-  V.y = p.cc0 * V.y + p.cc1mcc2 * A.y + p.cc2 * ay + R.y;
-  V.z = p.cc0 * V.z + p.cc1mcc2 * A.z + p.cc2 * az + R.z;
-  d.vel[h] = V;
-  d.acel[h] = make_double4(ax, ay, az, 0.0);
+  const float im = p.inv_massf[typ - 1];
+  const float4 V = ldv(d.vel, h), A = ldv(d.acel, h), R = ldv(d.ranv, h);
+  const float ax = fx * im, ay = fy * im, az = fz * im;
+  stv(d.vel, h, p.cc0f * V.x + p.cc1mcc2f * A.x + p.cc2f * ax + R.x,
+      p.cc0f * V.y + p.cc1mcc2f * A.y + p.cc2f * ay + R.y,
+      p.cc0f * V.z + p.cc1mcc2f * A.z + p.cc2f * az + R.z);
+  stv(d.acel, h, ax, ay, az);
 }
 
 // Pass 2: one thread per hs slot sums its recorded entries in key order,
 // i.e. in the reference's global accumulation order (hs%ref order x list
 // order, with the Newton reaction applied to both atoms of every entry).
 template <bool FUSE_B>
-__global__ void force_sum_kernel(Dev d, KParams p, int n_slots) {
-  // grids are sized by capacity; the block's replica gives the live count
-  const int rep = block_rep(d);
+__device__ __forceinline__ void force_sum_at(Dev d, KParams p, int n_slots, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = pos;
   if (s == 0) d.g->n_cand = 0;
   if (s >= n_slots) return;
   if (d.state[s] != ST_LIVE) return;
@@ -690,19 +813,31 @@ __global__ void force_sum_kernel(Dev d, KParams p, int n_slots) {
   if (FUSE_B && inref) ermak_b_atom(d, p, s, d.typ[s], F);
 }
 
-__global__ void ermak_b_kernel(Dev d, KParams p, int n_rank) {
-  // grids are sized by capacity; the block's replica gives the live count
+template <bool FUSE_B>
+__global__ void force_sum_kernel(Dev d, KParams p, int n_slots) {
   const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) force_sum_at<FUSE_B>(d, p, n_slots, rep, span_pos(u));
+}
+
+__device__ __forceinline__ void ermak_b_at(Dev d, KParams p, int n_rank, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = pos;
   if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
-  if (p.mixed)
-    ermak_b_atom_mixed(d, p, h, d.typ[h], d.force[h]);
-  else
+  if (p.mixed) {
+    const double4 F = d.force[h];
+    ermak_b_atom_mixed(d, p, h, d.typ[h], (float)F.x, (float)F.y, (float)F.z);
+  } else
     ermak_b_atom(d, p, h, d.typ[h], d.force[h]);
+}
+
+__global__ void ermak_b_kernel(Dev d, KParams p, int n_rank) {
+  const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) ermak_b_at(d, p, n_rank, rep, span_pos(u));
 }
 
 
@@ -772,11 +907,9 @@ __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
 
 // Fixed point -> double, accumulators cleared, ermak_b fused.
 template <bool FUSE_B>
-__global__ void force_fix_kernel(Dev d, KParams p, int n_slots) {
-  // grids are sized by capacity; the block's replica gives the live count
-  const int rep = block_rep(d);
+__device__ __forceinline__ void force_fix_at(Dev d, KParams p, int n_slots, int rep, int pos) {
   n_slots = d.rc[rep].base + d.sc[rep].n_slots;
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = pos;
   if (s == 0) d.g->n_cand = 0;
   if (s >= n_slots) return;
   if (d.state[s] != ST_LIVE) return;
@@ -790,8 +923,10 @@ __global__ void force_fix_kernel(Dev d, KParams p, int n_slots) {
   const double inv = p.fix_inv;
   if (inref && !any) {
     // no pair inside r0: the sums are zero (no FP64 conversion needed)
-    F = make_double4(0.0, 0.0, 0.0, 0.0);
-    ep = 0.0;
+    d.force[s] = make_double4(0.0, 0.0, 0.0, 0.0);
+    d.epot[s] = 0.0;
+    if (FUSE_B) ermak_b_atom_mixed(d, p, s, d.typ[s], 0.0f, 0.0f, 0.0f);
+    return;
   } else if (inref) {
     F = make_double4((double)ax * inv, (double)ay * inv, (double)az * inv, 0.0);
     ep = (double)ae * inv;
@@ -810,7 +945,14 @@ __global__ void force_fix_kernel(Dev d, KParams p, int n_slots) {
   }
   d.force[s] = F;
   d.epot[s] = ep;
-  if (FUSE_B && inref) ermak_b_atom_mixed(d, p, s, d.typ[s], F);
+  if (FUSE_B && inref) ermak_b_atom_mixed(d, p, s, d.typ[s], (float)F.x, (float)F.y, (float)F.z);
+}
+
+template <bool FUSE_B>
+__global__ void force_fix_kernel(Dev d, KParams p, int n_slots) {
+  const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) force_fix_at<FUSE_B>(d, p, n_slots, rep, span_pos(u));
 }
 
 // ----------------------------------------------------------- test_update
@@ -861,10 +1003,12 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
   const float tinyf = 1e-16f;
   const float e = p.margin;
   float a1 = tinyf, a2 = tinyf;
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) {
+  const int s = span_pos(u);
   if (s < n_slots && d.state[s] == ST_LIVE) {
     float4 Pf = d.posf[s], Of = d.posf_old[s];
     bool safe = Pf.x > e && Pf.x < R.boxf[0] - e && Pf.y > e && Pf.y < R.boxf[1] - e;
@@ -908,6 +1052,7 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
     // a NaN displacement never passes `rd > dispmax` (Neighbor.F90:657-661)
     if (rdf == rdf) top2f(a1, a2, rdf, tinyf);
   }
+  }
   for (int off = 16; off > 0; off >>= 1) {
     float b1 = __shfl_down_sync(0xffffffffu, a1, off);
     float b2 = __shfl_down_sync(0xffffffffu, a2, off);
@@ -937,7 +1082,7 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
   __threadfence();
   // last block of this replica: FP32 top-2 over the replica's partials
   float b1 = tinyf, b2 = tinyf;
-  const int b0 = R.base / kBlock;
+  const int b0 = R.base / kSpan;
   for (int b = b0 + threadIdx.x; b < b0 + R.nblk; b += blockDim.x)
     top2f(b1, b2, __uint_as_float((unsigned)__ldcg(d.part + 2 * b)),
           __uint_as_float((unsigned)__ldcg(d.part + 2 * b + 1)));
@@ -1064,15 +1209,14 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
 // update() (Neighbor.F90:608-633) part 1: pos_old = pos, limbo cleaned
 // (igroup_clean, Groups.F90:1036-1053), cell index of every hs%b slot
 // (cgroup_sort_atom, Cells.F90:281-302) and the per-cell counts.
-__global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int cells_only) {
-  const int rep = block_rep(d);
+__device__ __forceinline__ void rebuild_prep_at(Dev d, KParams p, int n_slots, int n_b, int cells_only, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;
   n_b = R.base + sc->n_b;
   if (blockIdx.x == 0 && threadIdx.x == 0) d.g->n_big = 0;  // cell_order's list
   if (!cells_only && !sc->rebuild) return;
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = pos;
   if (!cells_only && s == R.base) sc->nlimbo = 0;
   if (!cells_only && s < n_slots) {
     int st = d.state[s];
@@ -1107,6 +1251,12 @@ __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int 
     d.cell_of[s] = lin;
     atomicAdd(&d.cell_count[lin], 1);
   }
+}
+
+__global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int cells_only) {
+  const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) rebuild_prep_at(d, p, n_slots, n_b, cells_only, rep, span_pos(u));
 }
 
 // Exclusive scan of one replica's cell counts (one block per replica),
@@ -1153,19 +1303,24 @@ __global__ void cell_scan_kernel(Dev d, int force) {
   }
 }
 
-__global__ void cell_scatter_kernel(Dev d, int n_b, int force) {
-  const int rep = block_rep(d);
+__device__ __forceinline__ void cell_scatter_at(Dev d, int n_b, int force, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_b = R.base + sc->n_b;
   if (!R.use_cells) return;            // no cells: cell_of is never written
   if (!force && !sc->rebuild) return;  // its cell_of entries are from an older sort
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = pos;
   if (b >= n_b) return;
   int c = d.cell_of[b];
   if (c < 0) return;
   int idx = d.cell_start[c] + atomicAdd(&d.cell_fill[c], 1);
   d.cell_atoms[idx] = b;
+}
+
+__global__ void cell_scatter_kernel(Dev d, int n_b, int force) {
+  const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) cell_scatter_at(d, n_b, force, rep, span_pos(u));
 }
 
 // Orders each cell by descending hs%b slot: the chain order of
@@ -1425,13 +1580,11 @@ __global__ void delta_reset_kernel(Global* g) { g->delta2f_bits = 0u; }
 // Resets the component state and takes delta = max |pos - old_cg| over the
 // moving atoms (positions after the integrator; they do not change until
 // overlap_moveback except by whole box lengths).
-__global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
-  // grids are sized by capacity; the block's replica gives the live count
-  const int rep = block_rep(d);
+__device__ __forceinline__ void overlap_init_at(Dev d, KParams p, int n_slots, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = pos;
   if (s == 0) {
     d.g->again = 0;
     d.g->n_comp = 0;
@@ -1458,6 +1611,12 @@ __global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
   for (int off = 16; off > 0; off >>= 1) dd = fmax(dd, __shfl_down_sync(0xffffffffu, dd, off));
   if ((threadIdx.x & 31) == 0 && dd > 0.0)
     atomicMax(&d.g->delta2f_bits, __float_as_uint(__double2float_ru(dd)));
+}
+
+__global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
+  const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) overlap_init_at(d, p, n_slots, rep, span_pos(u));
 }
 
 // Near entries of every hs%ref member: list entries within rc + 2 delta
@@ -1530,10 +1689,8 @@ __global__ void __launch_bounds__(256) overlap_detect_kernel(Dev d, KParams p, i
 
 // Atoms with no near entry are examined trivially in pass 1 (skip = true)
 // and can never be moved; the others are counted per component root.
-__global__ void overlap_count_kernel(Dev d, int n_rank) {
-  // grids are sized by capacity; the block's replica gives the live count
-  const int rep = block_rep(d);
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void overlap_count_at(Dev d, int n_rank, int rep, int pos) {
+  const int r = pos;
   if (r - d.rc[rep].base >= d.sc[rep].n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
@@ -1546,13 +1703,17 @@ __global__ void overlap_count_kernel(Dev d, int n_rank) {
   atomicAdd(&d.comp_size[root], 1);
 }
 
-__global__ void overlap_assign_kernel(Dev d, int n_slots) {
-  // grids are sized by capacity; the block's replica gives the live count
+__global__ void overlap_count_kernel(Dev d, int n_rank) {
   const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) overlap_count_at(d, n_rank, rep, span_pos(u));
+}
+
+__device__ __forceinline__ void overlap_assign_at(Dev d, int n_slots, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = pos;
   if (s >= n_slots) return;
   // component roots are hs%ref members (their sizes are reset each step;
   // an atom that left hs%ref keeps a stale one)
@@ -1566,12 +1727,16 @@ __global__ void overlap_assign_kernel(Dev d, int n_slots) {
   d.comp_list[2 * cid + 1] = sz;
 }
 
-__global__ void overlap_scatter_kernel(Dev d, int n_rank) {
-  // grids are sized by capacity; the block's replica gives the live count
+__global__ void overlap_assign_kernel(Dev d, int n_slots) {
   const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) overlap_assign_at(d, n_slots, rep, span_pos(u));
+}
+
+__device__ __forceinline__ void overlap_scatter_at(Dev d, int n_rank, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = pos;
   if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0 || !d.active[h]) return;
@@ -1581,15 +1746,19 @@ __global__ void overlap_scatter_kernel(Dev d, int n_rank) {
   d.comp_rank[idx] = r;  // the component's ranks, in no particular order
 }
 
+__global__ void overlap_scatter_kernel(Dev d, int n_rank) {
+  const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) overlap_scatter_at(d, n_rank, rep, span_pos(u));
+}
+
 // Members of every component in rank order: each member's place is the
 // number of smaller ranks in its component (contiguous loads, all members
 // in parallel).
-__global__ void overlap_order_kernel(Dev d, int n_rank) {
-  // grids are sized by capacity; the block's replica gives the live count
-  const int rep = block_rep(d);
+__device__ __forceinline__ void overlap_order_at(Dev d, int n_rank, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = pos;
   if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0 || !d.active[h]) return;
@@ -1599,6 +1768,12 @@ __global__ void overlap_order_kernel(Dev d, int n_rank) {
   int before = 0;
   for (int i = 0; i < sz; ++i) before += rk[i] < r;
   d.comp_members[off + before] = h;
+}
+
+__global__ void overlap_order_kernel(Dev d, int n_rank) {
+  const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) overlap_order_at(d, n_rank, rep, span_pos(u));
 }
 
 // Examination of o1 = x in pass `pass` (dana.F90:871-935).
@@ -1750,12 +1925,10 @@ __global__ void overlap_passn_kernel(Dev d, KParams p) {
 // ------------------------------------------------- capture commit, rho, piston
 // dana.F90:228-236: every F member of hs%ref becomes CG and leaves hs%ref
 // (its rank becomes a hole; the order of the remaining members is kept).
-__global__ void commit_kernel(Dev d, int n_rank) {
-  // grids are sized by capacity; the block's replica gives the live count
-  const int rep = block_rep(d);
+__device__ __forceinline__ void commit_at(Dev d, int n_rank, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = pos;
   if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
@@ -1775,6 +1948,12 @@ __global__ void commit_kernel(Dev d, int n_rank) {
   }
 }
 
+__global__ void commit_kernel(Dev d, int n_rank) {
+  const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) commit_at(d, n_rank, rep, span_pos(u));
+}
+
 // calc_rho (dana.F90:521-549): integer count, so any reduction order is exact.
 __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
   // grids are sized by capacity; the block's replica gives the live count
@@ -1782,15 +1961,24 @@ __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
   double z0 = sc->z0;
   double zt = p.ztop_is_z1 != 0.0 ? sc->z1 : sc->zmax;
   int c = 0;
-  if (s < n_slots && d.state[s] == ST_LIVE) {
-    double z = d.pos[s].z;
-    c = (z > z0 && z < zt) ? 1 : 0;
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) {
+    const int s = span_pos(u);
+    if (s < n_slots && d.state[s] == ST_LIVE) {
+      double z = d.pos[s].z;
+      c += (z > z0 && z < zt) ? 1 : 0;
+    }
   }
-  c = __syncthreads_count(c);
+  for (int off = 16; off > 0; off >>= 1) c += __shfl_down_sync(0xffffffffu, c, off);
+  __shared__ int s_c;
+  if (threadIdx.x == 0) s_c = 0;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(&s_c, c);
+  __syncthreads();
+  c = s_c;
   __shared__ bool last;
   if (threadIdx.x == 0) {
     if (c) atomicAdd(&sc->rho_count, c);
@@ -1810,13 +1998,11 @@ __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
 }
 
 // maxz (dana.F90:776-794)
-__global__ void piston_kernel(Dev d, KParams p, int n_slots) {
-  // grids are sized by capacity; the block's replica gives the live count
-  const int rep = block_rep(d);
+__device__ __forceinline__ void piston_at(Dev d, KParams p, int n_slots, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = pos;
   double z0 = sc->z0;
   double lohi = (p.h_over_tau * ((sc->rho0 - sc->rho) / sc->rho));
   if (s < n_slots && d.state[s] == ST_LIVE) {
@@ -1832,6 +2018,12 @@ __global__ void piston_kernel(Dev d, KParams p, int n_slots) {
     sc->lohi = lohi;
     sc->zmax = zm - lohi * (zm - z0);
   }
+}
+
+__global__ void piston_kernel(Dev d, KParams p, int n_slots) {
+  const int rep = block_rep(d);
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) piston_at(d, p, n_slots, rep, span_pos(u));
 }
 
 
@@ -2328,7 +2520,9 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
         const double beta = p.beta_t[typ - 1];
         double nv[4];
         dml_normal_quad(dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC_VEL, 0), nv);
-        d.vel[hlast] = make_double4(beta * nv[0], beta * nv[1], beta * nv[2], 0.0);
+        d.vel[hlast] = p.mixed ? pack_f3((float)(beta * nv[0]), (float)(beta * nv[1]),
+                                         (float)(beta * nv[2]))
+                               : make_double4(beta * nv[0], beta * nv[1], beta * nv[2], 0.0);
         // sys
         int ap = sc->n_alist;
         d.alist[B + ap] = slot;
@@ -3427,7 +3621,11 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
       S.fvel[k] = tv;
       const double beta = p.beta_t[typ - 1];
       const float4 nv = S.nv[k];
-      const Vel3 mv = Vel3{beta * (double)nv.x, beta * (double)nv.y, beta * (double)nv.z};
+      Vel3 mv = Vel3{beta * (double)nv.x, beta * (double)nv.y, beta * (double)nv.z};
+      if (p.mixed) {  // the slot holds FP32 values (chosen form)
+        const double4 pk = pack_f3((float)mv.x, (float)mv.y, (float)mv.z);
+        mv = Vel3{pk.x, pk.y, pk.z};
+      }
       const int hli = S.hlast_ins[k];
       if (hli >= 0) {
         S.fvel[hli] = mv;
@@ -3607,6 +3805,8 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
 }
 
 inline int nblk(int n, int b = kBlock) { return n > 0 ? (n + b - 1) / b : 1; }
+// blocks of the per-position kernels over n positions (a multiple of kSpan)
+inline int nspan(int n) { return n > 0 ? (n + kSpan - 1) / kSpan : 1; }
 inline int nblk_warps(int n) { return n > 0 ? (n + (kBlock / 32) - 1) / (kBlock / 32) : 1; }
 // Fixed grid of the warp-per-row kernels (grid-stride over the rows): a
 // few resident blocks per SM instead of one block per 8 rows.
@@ -3628,12 +3828,12 @@ int k_step_begin(const Dev& d, int near_stale, cudaStream_t s) {
 }
 
 int k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
-  ermak_a_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  ermak_a_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, p, n_rank);
   return 1;
 }
 
 int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
-  brownian_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  brownian_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, p, n_rank);
   return 1;
 }
 
@@ -3675,25 +3875,25 @@ int k_reset_candidates(const Dev& d, cudaStream_t s) {
 int k_force_sum(const Dev& d, const KParams& p, int n_slots, bool fuse_b, cudaStream_t s) {
   if (p.mixed) {
     if (fuse_b)
-      force_fix_kernel<true><<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+      force_fix_kernel<true><<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
     else
-      force_fix_kernel<false><<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+      force_fix_kernel<false><<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
     return 1;
   }
   if (fuse_b)
-    force_sum_kernel<true><<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+    force_sum_kernel<true><<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
   else
-    force_sum_kernel<false><<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+    force_sum_kernel<false><<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
   return 1;
 }
 
 int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
-  ermak_b_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  ermak_b_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, p, n_rank);
   return 1;
 }
 
 int k_pbc_dispmax(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
-  pbc_dispmax_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots, 0, 0);
+  pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots, 0, 0);
   return 1;
 }
 
@@ -3704,17 +3904,17 @@ int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_ra
 
 int k_pbc_dispmax_cond(const Dev& d, const KParams& p, int n_slots,
                        cudaGraphConditionalHandle h, cudaStream_t s) {
-  pbc_dispmax_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots, 1, h);
+  pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots, 1, h);
   return 1;
 }
 
 int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, cudaStream_t s) {
   int nmax = n_slots > n_b ? n_slots : n_b;
-  rebuild_prep_kernel<<<nblk(nmax), kBlock, 0, s>>>(d, p, n_slots, n_b, 0);
+  rebuild_prep_kernel<<<nspan(nmax), kBlock, 0, s>>>(d, p, n_slots, n_b, 0);
   int n = 1;
   if (d.any_cells) {
     cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 0);
-    cell_scatter_kernel<<<nblk(n_b), kBlock, 0, s>>>(d, n_b, 0);
+    cell_scatter_kernel<<<nspan(n_b), kBlock, 0, s>>>(d, n_b, 0);
     cell_order_small_kernel<<<kRowGrid, kBlock, 0, s>>>(d, d.ncell_tot, 0);
     cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 0);
     list_cells_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, n_rank);
@@ -3729,7 +3929,7 @@ int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, 
 }
 
 int k_overlap_prepare(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
-  overlap_init_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  overlap_init_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
   return 1;
 }
 
@@ -3751,10 +3951,10 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
     n += 1 + k_overlap_prepare(d, p, n_slots, s);
   }
   if (detect) n += k_overlap_detect(d, p, n_rank, detect == 1 ? 1 : 0, s);
-  overlap_count_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
-  overlap_assign_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, n_slots);
-  overlap_scatter_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
-  overlap_order_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
+  overlap_count_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
+  overlap_assign_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, n_slots);
+  overlap_scatter_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
+  overlap_order_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
   int all_passes = p.prob >= 1.0;
   overlap_pass1_kernel<<<nblk(n_rank, 128), 128, 0, s>>>(d, p, all_passes);
   n += 5;
@@ -3765,26 +3965,26 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
 
 int k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   (void)p;
-  commit_kernel<<<nblk(n_rank), kBlock, 0, s>>>(d, n_rank);
+  commit_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
   return 1;
 }
 
 int k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
-  calc_rho_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  calc_rho_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
   return 1;
 }
 
 int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
-  piston_kernel<<<nblk(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  piston_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
   return 1;
 }
 
 // gcmc_run's searches need the cells of the current positions.
 int k_gcmc_cells(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
   if (!d.any_cells) return 0;
-  rebuild_prep_kernel<<<nblk(cap), kBlock, 0, s>>>(d, p, cap, cap, 1);
+  rebuild_prep_kernel<<<nspan(cap), kBlock, 0, s>>>(d, p, cap, cap, 1);
   cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1);
-  cell_scatter_kernel<<<nblk(cap), kBlock, 0, s>>>(d, cap, 1);
+  cell_scatter_kernel<<<nspan(cap), kBlock, 0, s>>>(d, cap, 1);
   cell_order_small_kernel<<<kRowGrid, kBlock, 0, s>>>(d, d.ncell_tot, 1);
   cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 1);
   return 5;

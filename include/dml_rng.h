@@ -239,10 +239,12 @@ DML_HD void dml_sincosf_2pi(float u, float* sn, float* cs) {
 }
 
 /* Two standard normals from two 32-bit words (Box-Muller): a uniform in
- * (0,1] from the first word, an angle from the top 24 bits of the second. */
-DML_HD void dml_normal_pair32(uint32_t a, uint32_t b, double* n0, double* n1) {
+ * (0,1] from the first word, an angle from the top 24 bits of the second.
+ * RN32(a + 1) is taken from a 32-bit conversion (a + 1 = 2^32 is exact). */
+DML_HD void dml_normal_pair32f(uint32_t a, uint32_t b, float* n0, float* n1) {
 #if defined(__CUDA_ARCH__)
-  float u1 = __fmul_rn(__ull2float_rn((unsigned long long)a + 1ull), 0x1.0p-32f); /* (0,1] */
+  float a1 = a == 0xFFFFFFFFu ? 0x1.0p+32f : __uint2float_rn(a + 1u);
+  float u1 = __fmul_rn(a1, 0x1.0p-32f); /* (0,1] */
   float u2 = __fmul_rn(__uint2float_rn(b >> 8), 0x1.0p-24f);
 #else
   float u1 = (float)((uint64_t)a + 1ull) * 0x1.0p-32f;
@@ -251,11 +253,23 @@ DML_HD void dml_normal_pair32(uint32_t a, uint32_t b, double* n0, double* n1) {
   float r = DMLF_SQRT(DMLF_MUL(-2.0f, dml_logf(u1)));
   float s, c;
   dml_sincosf_2pi(u2, &s, &c);
-  *n0 = (double)DMLF_MUL(r, c);
-  *n1 = (double)DMLF_MUL(r, s);
+  *n0 = DMLF_MUL(r, c);
+  *n1 = DMLF_MUL(r, s);
 }
 
-/* Four standard normals from one 128-bit draw. */
+DML_HD void dml_normal_pair32(uint32_t a, uint32_t b, double* n0, double* n1) {
+  float f0, f1;
+  dml_normal_pair32f(a, b, &f0, &f1);
+  *n0 = (double)f0;
+  *n1 = (double)f1;
+}
+
+/* Four standard normals from one 128-bit draw (FP32 values). */
+DML_HD void dml_normal_quadf(dml_u4 w, float* n) {
+  dml_normal_pair32f(w.w[0], w.w[1], &n[0], &n[1]);
+  dml_normal_pair32f(w.w[2], w.w[3], &n[2], &n[3]);
+}
+
 DML_HD void dml_normal_quad(dml_u4 w, double* n) {
   dml_normal_pair32(w.w[0], w.w[1], &n[0], &n[1]);
   dml_normal_pair32(w.w[2], w.w[3], &n[2], &n[3]);
