@@ -20,6 +20,8 @@
 
 using namespace dml;
 
+constexpr int kScanMappings = 6;  // lanes per list row tried by the force-scan autotuner
+
 struct dml_ctx {
   dml_params P;
   KParams K;
@@ -33,7 +35,7 @@ struct dml_ctx {
   cudaGraphExec_t step_graph = nullptr;
   int launches_per_step = 0;    // kernels of a step without a list rebuild
   int launches_per_rebuild = 0; // extra kernels when the list is rebuilt
-  float tune_us[4] = {0, 0, 0, 0};  // force-scan time per mapping (4, 8, 16, 32 lanes per row)
+  float tune_us[kScanMappings] = {};  // force-scan time per mapping (1, 2, 4, 8, 16, 32 lanes per row)
   void* flush_buf = nullptr;
   std::string last_error;
   Scalars* h_sc = nullptr;  // pinned mirror of the per-replica state
@@ -95,6 +97,23 @@ void make_repconst(const dml_params& P, const dml_replica& r, RepConst& R) {
   R.ncell = R.use_cells ? R.head_dim[0] * R.head_dim[1] * R.head_dim[2] : 0;
   R.tess_hif = (float)((R.ncells[2] + 1) * R.cell[2]);
   R.seed = r.seed;
+  // gcmc_run's trial points lie in [z0, zmax]: their 27-cell stencils reach
+  // the layers of those points and one more on either side, wrapped along z
+  // like every stencil (Cells.F90:378-404); its cell sort covers only those.
+  R.gl_all = 1;
+  R.gl_mask = 0;
+  const int nz = R.ncells[2];
+  if (R.use_cells && P.reservoir == DML_RESERVOIR_GCMC && nz <= 62) {
+    const int lo = std::max(0, (int)(r.z0 / R.cell[2]) + 1);
+    const int hi = std::min(nz + 1, (int)(r.zmax / R.cell[2]) + 1);
+    unsigned long long m = 0;
+    for (int c = lo; c <= hi; ++c)
+      for (int o = -1; o <= 1; ++o) m |= 1ull << (((c - 1 + o) % nz + 2 * nz) % nz + 1);
+    if (lo <= hi && __builtin_popcountll(m) < nz) {
+      R.gl_all = 0;
+      R.gl_mask = m;
+    }
+  }
 }
 
 // Context-wide constants (see KParams); maxc bounds every coordinate.
@@ -353,7 +372,7 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
 int autotune_scan(dml_ctx* c) {
   if (c->P.integrator != DML_INTEGRATOR_ERMAK) return 0;
   cudaStream_t s = c->stream;
-  const int lanes[4] = {4, 8, 16, 32};
+  const int lanes[kScanMappings] = {1, 2, 4, 8, 16, 32};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -361,7 +380,7 @@ int autotune_scan(dml_ctx* c) {
   KParams k = c->K;
   float best = 1e30f;
   int best_l = 16;
-  for (int v = 0; v < 4; ++v) {
+  for (int v = 0; v < kScanMappings; ++v) {
     k.scan_lanes = lanes[v];
     k_force_scan(c->D, k, c->D.cap, false, s);  // warm-up
     k_reset_candidates(c->D, s);
@@ -974,7 +993,7 @@ int dml_get_tuning(dml_ctx* c, int32_t* scan_lanes, float* scan_us) {
   if (!c) return DML_E_ARG;
   if (scan_lanes) *scan_lanes = c->K.scan_lanes;
   if (scan_us)
-    for (int v = 0; v < 4; ++v) scan_us[v] = c->tune_us[v];
+    for (int v = 0; v < kScanMappings; ++v) scan_us[v] = c->tune_us[v];
   return 0;
 }
 

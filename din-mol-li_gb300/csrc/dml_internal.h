@@ -52,6 +52,10 @@ struct RepConst {
                             // one sentinel cell (always empty) whose start is the end
   int base, cap, nblk;      // positions [base, base + cap), cap / kSpan blocks
   unsigned long long seed;  // Philox key of this replica
+  // z layers of cells that gcmc_run's searches reach (bit c3, 1 <= c3 <=
+  // ncells[2]); gl_all: every layer (its cell sort then covers them all)
+  unsigned long long gl_mask;
+  int gl_all;
 };
 
 // Per-replica device state (mutable).
@@ -81,6 +85,8 @@ struct Scalars {
   int free_lo;     // every local hs slot below this one is in use (live or limbo)
   int bfree_lo;    // every local hs%b slot below this one holds an atom
   int halo;        // an atom sat in a halo cell at the last cell sort
+  int dec;         // displacement test: 0 keep, 1 rebuild, 2 decided in FP64
+  float thr;       // its FP32 candidate threshold for the FP64 top-2
   long long next_id;
 };
 
@@ -177,7 +183,7 @@ __host__ __device__ inline float4 unpack_f3(const double4& v) {
 constexpr int kGcmcMaxTrials = 256;  // trials per call on this path (nadj)
 constexpr int kGcmcMaskW = kGcmcMaxTrials / 32;
 constexpr int kGcmcBlk = 8;          // gcmc members within rc of a trial point
-constexpr int kGcmcCand = 48;        // atoms within rc + skin of a trial point
+constexpr int kGcmcCand = 48;        // atoms within rc + skin of a trial point (<= 64)
 
 struct GcmcTrialPre {
   double4 r;                 // trial point (dana.F90:643-645)

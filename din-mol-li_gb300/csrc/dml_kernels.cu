@@ -996,8 +996,16 @@ __device__ __forceinline__ float disp2f(float4 P, float4 O) {
   return (x * x + y * y) + z * z;
 }
 
-__global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
-                                   cudaGraphConditionalHandle cond_handle) {
+__device__ __forceinline__ void decide_rebuild(const Dev& d, Scalars* sc, int rebuild) {
+  sc->rebuild = rebuild;
+  if (rebuild) {
+    sc->nupd += 1;
+    sc->max_nn = 0;
+    atomicOr(&d.g->any_rebuild, 1);
+  }
+}
+
+__global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots) {
   // grids are sized by capacity; the block's replica gives the live count
   const int rep = block_rep(d);
   const RepConst& R = d.rc[rep];
@@ -1097,35 +1105,53 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
     w2[wid] = b2;
   }
   __syncthreads();
-  __shared__ int s_dec;  // 0 keep, 1 rebuild, 2 undecided
-  __shared__ float s_s2;
   if (threadIdx.x == 0) {
     float F1 = tinyf, F2 = tinyf;
     for (int w = 0; w < nwarp; ++w) top2f(F1, F2, w1[w], w2[w]);
     float sum = sqrtf(F1) + sqrtf(F2);
-    int dec;
+    int dec;  // 0 keep, 1 rebuild, 2 undecided: dispmax_exact_kernel decides
     if (!sc->listed) dec = 1;
     else if (sum + 4.0f * e < (float)p.skin) dec = 0;
     else if (sum - 4.0f * e > (float)p.skin) dec = 1;
     else dec = 2;
-    s_dec = dec;
-    s_s2 = sqrtf(F2);
+    sc->dec = dec;
+    sc->thr = sqrtf(F2) - 3.0f * e;
+    sc->ticket = 0;
+    if (dec != 2) decide_rebuild(d, sc, dec);
   }
-  __syncthreads();
-  int rebuild = s_dec;
-  if (rebuild == 2) {
-    // exact top-2 over the candidates (every slot of the replica, read through L2)
+}
+
+// The replicas whose FP32 top-2 lies within the margins of the skin: the
+// exact FP64 top-2 over the candidates (sqrt(rdf) >= sqrt(F2) - 3e, which
+// holds for every atom of the exact top-2), spread over the replica's blocks
+// and merged by its last one.  Then the last replica to decide prefixes the
+// rows of the replicas that rebuild (the list build walks only those) and
+// opens the rebuild subgraph if any.
+__global__ void dispmax_exact_kernel(Dev d, KParams p, int cond,
+                                     cudaGraphConditionalHandle cond_handle) {
+  const int rep = block_rep(d);
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nwarp = blockDim.x >> 5;
+  __shared__ int s_close;  // this block closes its replica's decision
+  __shared__ unsigned long long x1[32], x2[32];
+  if (sc->dec == 2) {
+    const int n_slots = R.base + sc->n_slots;
+    const float thr = sc->thr;
     const unsigned long long tiny = (unsigned long long)__double_as_longlong(1.e-16);
     unsigned long long e1 = tiny, e2 = tiny;
-    const float thr = s_s2 - 3.0f * e;
-    for (int q = R.base + threadIdx.x; q < n_slots; q += blockDim.x) {
-      if (__ldcg(d.state + q) != ST_LIVE) continue;
-      float4 Pf = __ldcg(d.posf + q), Of = __ldcg(d.posf_old + q);
-      float rdf = disp2f(Pf, Of);
-      if (!(rdf == rdf) || sqrtf(rdf) < thr) continue;
-      double4 P = ldcg_d4(d.pos + q), O = ldcg_d4(d.pos_old + q);
-      double rd = dot3(P.x - O.x, P.y - O.y, P.z - O.z);
-      if (rd == rd) top2_merge(e1, e2, (unsigned long long)__double_as_longlong(rd), tiny);
+#pragma unroll
+    for (int u = 0; u < kSlotU; ++u) {
+      const int q = span_pos(u);
+      if (q < n_slots && d.state[q] == ST_LIVE) {
+        const float rdf = disp2f(d.posf[q], d.posf_old[q]);
+        if (rdf == rdf && sqrtf(rdf) >= thr) {
+          const double4 P = d.pos[q], O = d.pos_old[q];
+          const double rd = dot3(P.x - O.x, P.y - O.y, P.z - O.z);
+          if (rd == rd) top2_merge(e1, e2, (unsigned long long)__double_as_longlong(rd), tiny);
+        }
+      }
     }
     for (int off = 16; off > 0; off >>= 1) {
       unsigned long long c1 = __shfl_down_sync(0xffffffffu, e1, off);
@@ -1140,21 +1166,46 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots, int cond,
     if (threadIdx.x == 0) {
       unsigned long long f1 = tiny, f2 = tiny;
       for (int w = 0; w < nwarp; ++w) top2_merge(f1, f2, x1[w], x2[w]);
-      double d1 = __longlong_as_double((long long)f1), d2 = __longlong_as_double((long long)f2);
-      s_dec = sqrt(d1) + sqrt(d2) > p.skin ? 1 : 0;
+      d.part[2 * blockIdx.x] = f1;
+      d.part[2 * blockIdx.x + 1] = f2;
+      __threadfence();
+      const unsigned t = atomicAdd(&sc->ticket, 1u);
+      s_close = t == (unsigned)R.nblk - 1u;
     }
     __syncthreads();
-    rebuild = s_dec;
+    if (s_close) {
+      __threadfence();
+      unsigned long long f1 = tiny, f2 = tiny;
+      const int b0 = R.base / kSpan;
+      for (int b = b0 + threadIdx.x; b < b0 + R.nblk; b += blockDim.x)
+        top2_merge(f1, f2, __ldcg(d.part + 2 * b), __ldcg(d.part + 2 * b + 1));
+      for (int off = 16; off > 0; off >>= 1) {
+        unsigned long long c1 = __shfl_down_sync(0xffffffffu, f1, off);
+        unsigned long long c2 = __shfl_down_sync(0xffffffffu, f2, off);
+        top2_merge(f1, f2, c1, c2);
+      }
+      __syncthreads();
+      if (lane == 0) {
+        x1[wid] = f1;
+        x2[wid] = f2;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned long long g1 = tiny, g2 = tiny;
+        for (int w = 0; w < nwarp; ++w) top2_merge(g1, g2, x1[w], x2[w]);
+        const double d1 = __longlong_as_double((long long)g1);
+        const double d2 = __longlong_as_double((long long)g2);
+        decide_rebuild(d, sc, sqrt(d1) + sqrt(d2) > p.skin ? 1 : 0);
+        sc->ticket = 0;
+      }
+    }
+  } else {
+    if (threadIdx.x == 0) s_close = blockIdx.x * kSpan == R.base;  // the replica's first block
+    __syncthreads();
   }
+  if (!s_close) return;
   __shared__ int s_lastrep;
   if (threadIdx.x == 0) {
-    sc->rebuild = rebuild;
-    if (rebuild) {
-      sc->nupd += 1;
-      sc->max_nn = 0;
-      atomicOr(&d.g->any_rebuild, 1);
-    }
-    sc->ticket = 0;
     __threadfence();
     unsigned t2 = atomicAdd(&d.g->ticket_rep, 1u);
     s_lastrep = t2 == (unsigned)d.nrep - 1u;
@@ -1247,6 +1298,11 @@ __device__ __forceinline__ void rebuild_prep_at(Dev d, KParams p, int n_slots, i
     if (c1 == 0 || c2 == 0 || c3 == 0 || c1 > R.ncells[0] || c2 > R.ncells[1] ||
         c3 > R.ncells[2])
       sc->halo = 1;
+    // the sort for gcmc_run covers only the layers its searches reach
+    if (cells_only && !R.gl_all && !((R.gl_mask >> c3) & 1ull)) {
+      d.cell_of[s] = -1;
+      return;
+    }
     int lin = R.cell_off + (c3 * R.head_dim[1] + c2) * R.head_dim[0] + c1;
     d.cell_of[s] = lin;
     atomicAdd(&d.cell_count[lin], 1);
@@ -1259,23 +1315,14 @@ __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int 
   for (int u = 0; u < kSlotU; ++u) rebuild_prep_at(d, p, n_slots, n_b, cells_only, rep, span_pos(u));
 }
 
-// Exclusive scan of one replica's cell counts (one block per replica),
-// starting at the replica's first position: its cell_atoms range is
-// [base, base + cap).  The sentinel after its last cell receives the end.
-__global__ void cell_scan_kernel(Dev d, int force) {
-  const RepConst& R = d.rc[blockIdx.x];
-  const Scalars* sc = d.sc + blockIdx.x;
-  if (!R.use_cells) return;
-  if (!force && !sc->rebuild) return;
-  const int ncell = R.ncell + 1;
+// Exclusive scan of one replica's cell counts over the cells [c0, c1) of the
+// replica (one block), continuing from *carry; cell c1 receives the end.
+__device__ void cell_scan_range(const Dev& d, const RepConst& R, int c0, int c1, int* carry) {
   __shared__ int wsum[32];
-  __shared__ int carry;
-  if (threadIdx.x == 0) carry = R.base;
-  __syncthreads();
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int base = 0; base < ncell; base += blockDim.x) {
-    int i = base + threadIdx.x;
-    int v = i < ncell ? d.cell_count[R.cell_off + i] : 0;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int base = c0; base < c1; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const int v = i < c1 ? d.cell_count[R.cell_off + i] : 0;
     int x = v;
     for (int o = 1; o < 32; o <<= 1) {
       int y = __shfl_up_sync(0xffffffffu, x, o);
@@ -1292,14 +1339,42 @@ __global__ void cell_scan_kernel(Dev d, int force) {
       wsum[lane] = ws;
     }
     __syncthreads();
-    int pre = (wid > 0 ? wsum[wid - 1] : 0) + x - v;
-    if (i < ncell) {
-      d.cell_start[R.cell_off + i] = carry + pre;
+    const int pre = (wid > 0 ? wsum[wid - 1] : 0) + x - v;
+    if (i < c1) {
+      d.cell_start[R.cell_off + i] = *carry + pre;
       d.cell_fill[R.cell_off + i] = 0;
     }
     __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) carry += pre + v;
+    if (threadIdx.x == blockDim.x - 1) *carry += pre + v;
     __syncthreads();
+  }
+  if (threadIdx.x == 0) d.cell_start[R.cell_off + c1] = *carry;
+  __syncthreads();
+}
+
+// The cell starts of one replica (one block per replica), from its first
+// position: its cell_atoms range is [base, base + cap).  A full sort covers
+// every cell and the sentinel after the last; the sort for gcmc_run covers
+// the runs of z layers its searches reach, each followed by its end.
+__global__ void cell_scan_kernel(Dev d, int force) {
+  const RepConst& R = d.rc[blockIdx.x];
+  const Scalars* sc = d.sc + blockIdx.x;
+  if (!R.use_cells) return;
+  if (!force && !sc->rebuild) return;
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = R.base;
+  __syncthreads();
+  if (!force || R.gl_all) {
+    cell_scan_range(d, R, 0, R.ncell, &carry);  // cell ncell is the sentinel
+    return;
+  }
+  const int layer = R.head_dim[0] * R.head_dim[1];
+  for (int a = 1; a <= R.ncells[2]; ++a) {
+    if (!((R.gl_mask >> a) & 1ull)) continue;
+    int b = a;
+    while (b + 1 <= R.ncells[2] && ((R.gl_mask >> (b + 1)) & 1ull)) ++b;
+    cell_scan_range(d, R, a * layer, (b + 1) * layer, &carry);
+    a = b;
   }
 }
 
@@ -2814,7 +2889,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
 // qualify (no cells, an atom or point in a halo cell, more than
 // kGcmcMaxTrials trials, a point with more than kGcmcBlk blockers or
 // kGcmcCand list atoms) runs gcmc_kernel instead.
-constexpr int kGcmcPreThreads = 1024;
+constexpr int kGcmcPreThreads = 512;
 
 __device__ __forceinline__ bool hard_core_in(const KParams& p, const RepConst& R, double4 a,
                                              float4 af, double4 b, float4 bf) {
@@ -2830,20 +2905,30 @@ __device__ __forceinline__ bool hard_core_in(const KParams& p, const RepConst& R
 }
 
 // First `want` positions q in [lo, hi) with free(q), ascending, into out[];
-// returns how many were found.  Every thread of the block calls it.
+// returns how many were found.  Every thread of the block calls it; each
+// thread tests kCollectV consecutive positions per round.
+constexpr int kCollectV = 8;
 template <class Pred>
 __device__ int blk_collect(int lo, int hi, int want, Pred free_at, int* out, int* s_cnt) {
   if (threadIdx.x == 0) *s_cnt = 0;
   __syncthreads();
-  for (int base = lo; base < hi && *s_cnt < want; base += (int)blockDim.x) {
-    const int q = base + (int)threadIdx.x;
-    const bool f = q < hi && free_at(q);
+  for (int base = lo; base < hi && *s_cnt < want; base += kCollectV * (int)blockDim.x) {
+    const int q0 = base + kCollectV * (int)threadIdx.x;
+    unsigned m = 0u;
+#pragma unroll
+    for (int v = 0; v < kCollectV; ++v)
+      if (q0 + v < hi && free_at(q0 + v)) m |= 1u << v;
     int tot;
-    const int pre = blk_scan_excl(f ? 1 : 0, &tot);
-    const int c0 = *s_cnt;
-    if (f && c0 + pre < want) out[c0 + pre] = q;
+    const int pre = blk_scan_excl(__popc(m), &tot);
+    int k = *s_cnt + pre;
+#pragma unroll
+    for (int v = 0; v < kCollectV; ++v)
+      if ((m >> v) & 1u) {
+        if (k < want) out[k] = q0 + v;
+        ++k;
+      }
     __syncthreads();
-    if (threadIdx.x == 0) *s_cnt = c0 + tot;
+    if (threadIdx.x == 0) *s_cnt += tot;
     __syncthreads();
   }
   const int n = min(*s_cnt, want);
@@ -2863,7 +2948,7 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
   __shared__ double4 s_r[kGcmcMaxTrials];
   __shared__ float4 s_rf[kGcmcMaxTrials];
   __shared__ unsigned char s_crt[kGcmcMaxTrials];
-  __shared__ int s_tab[32][56];  // per warp: stencil cell starts and prefixes
+  __shared__ int s_tab[kGcmcPreThreads / 32][56];  // per warp: stencil cell starts and prefixes
   if (!sc->listed) {  // gcmc_kernel reports the state error
     if (tid == 0) gr->fast = 0;
     return;
@@ -3710,8 +3795,19 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
     const int slot = B + S.ins_slot[k];
     int* row = d.list + (size_t)slot * p.mnb;
     const int mycell = lane < 27 ? tr.cells[lane] : -1;
+    // the trial's candidates, two per lane (c = lane, lane + 32), in stencil
+    // order: stencil index, and whether it joins the own list
     const int nc = tr.n_cand;
-    int cnt = 0, ci = 0;
+    int cj[2], cqq[2];
+    bool cown[2];
+#pragma unroll
+    for (int h2 = 0; h2 < 2; ++h2) {
+      const int c = lane + 32 * h2;
+      cj[h2] = c < nc ? tr.cand[c] : -1;
+      cqq[h2] = c < nc ? (int)tr.cq[c] : -1;
+      cown[h2] = c < nc && (tr.cf[c] & 1) && !deleted_by(S, cj[h2], i, true);
+    }
+    int cnt = 0;
     for (int q = 0; q < 27; ++q) {
       const int cq = __shfl_sync(0xffffffffu, mycell, q);
       for (int kb = k - 1; kb >= 0; kb -= 32) {
@@ -3729,24 +3825,13 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
         if (inc && pos < p.mnb) row[pos] = j;
         cnt += __popc(bal);
       }
-      // candidates are in stencil order: those of cell q start at ci
-      for (;;) {
-        const int c = ci + lane;
-        const int qc = c < nc ? (int)tr.cq[c] : 1000;
-        const bool mine = qc == q;
-        bool inc = false;
-        int j = -1;
-        if (mine && (tr.cf[c] & 1)) {
-          j = tr.cand[c];
-          inc = !deleted_by(S, j, i, true);
-        }
+#pragma unroll
+      for (int h2 = 0; h2 < 2; ++h2) {
+        const bool inc = cown[h2] && cqq[h2] == q;
         const unsigned bal = __ballot_sync(0xffffffffu, inc);
         const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
-        if (inc && pos < p.mnb) row[pos] = j;
+        if (inc && pos < p.mnb) row[pos] = cj[h2];
         cnt += __popc(bal);
-        const unsigned bm = __ballot_sync(0xffffffffu, mine);
-        ci += __popc(bm);
-        if (bm != 0xffffffffu) break;  // a later cell (or the end) reached
       }
     }
     if (lane == 0) {
@@ -3841,7 +3926,11 @@ template <bool NEAR>
 void launch_force_scan(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   const int L = p.scan_lanes;
   const int nb = nblk_rows((n_rank + 32 / L - 1) / (32 / L));
-  if (L == 4)
+  if (L == 1)
+    force_scan_kernel<NEAR, 1><<<nb, kBlock, 0, s>>>(d, p);
+  else if (L == 2)
+    force_scan_kernel<NEAR, 2><<<nb, kBlock, 0, s>>>(d, p);
+  else if (L == 4)
     force_scan_kernel<NEAR, 4><<<nb, kBlock, 0, s>>>(d, p);
   else if (L == 8)
     force_scan_kernel<NEAR, 8><<<nb, kBlock, 0, s>>>(d, p);
@@ -3893,8 +3982,9 @@ int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
 }
 
 int k_pbc_dispmax(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
-  pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots, 0, 0);
-  return 1;
+  pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  dispmax_exact_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, 0, 0);
+  return 2;
 }
 
 int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
@@ -3904,8 +3994,9 @@ int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_ra
 
 int k_pbc_dispmax_cond(const Dev& d, const KParams& p, int n_slots,
                        cudaGraphConditionalHandle h, cudaStream_t s) {
-  pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots, 1, h);
-  return 1;
+  pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+  dispmax_exact_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, 1, h);
+  return 2;
 }
 
 int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, cudaStream_t s) {

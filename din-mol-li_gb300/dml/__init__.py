@@ -275,13 +275,13 @@ class Simulation:
         return dict(zip(self.PHASES, out.tolist()))
 
     def tuning(self):
-        """Autotuner choice: {"scan_lanes": L, "scan_us": {4: t, 8: t, 16: t, 32: t}}."""
+        """Autotuner choice: {"scan_lanes": L, "scan_us": {1: t, 2: t, ..., 32: t}}."""
         lanes = ctypes.c_int32()
-        us = np.zeros(4, np.float32)
+        us = np.zeros(6, np.float32)
         self._check(self.lib.dml_get_tuning(self.h, ctypes.byref(lanes), us.ctypes.data),
                     "dml_get_tuning")
         return {"scan_lanes": lanes.value,
-                "scan_us": {l: float(t) for l, t in zip((4, 8, 16, 32), us)}}
+                "scan_us": {l: float(t) for l, t in zip((1, 2, 4, 8, 16, 32), us)}}
 
     def launches_per_step(self):
         """(kernels per step without a rebuild, extra kernels per rebuild)."""
