@@ -18,9 +18,16 @@ Workloads (seeded synthetic systems; the reference measures no dataset):
   c2            config 2: one 351 x 351 x 320 Å system, 80 000 electrode atoms
                 and 200 000 Li+, piston reservoir, Ermak, plain FP64 (the form
                 bit-exact to the oracle).
+  c4            config 4: 1024 replicas of uneven size (L x L x 2-cell
+                electrode, L in 5..40 cells, 50..20 000 ions, 1 M height),
+                Brownian, chosen form, all replicas in every launch.
+  c3            config 3, an accuracy study rather than a bench line: config
+                2's system in the chosen form against the plain FP64 form,
+                force and energy errors at steps 0, K/10 and K (default K =
+                10 000) and deposition counts over --seeds seeds.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload c5|c2] [--replicas R] [--form chosen|plain]
+                  [--workload c5|c2|c3|c4] [--replicas R] [--form chosen|plain]
 
 Prints one JSON line.  `value` = mobile-ion steps per second over all ranks
 (device time with CUDA events, inputs resident, L2 flushed between steps).
@@ -198,6 +205,14 @@ class Workload:
             self.desc = ("config 5: %d replicas x (40x40x2-cell bcc Li electrode, 6400 atoms, "
                          "+ 20000 Li+), 140.4x140.4x300 A, GCMC reservoir z in [200,300] with "
                          "%d trials/step, Ermak dt=1fs, skin 2" % (n_rep, self.p.nadj))
+        elif name == "c4":
+            self.batched = True
+            self.p, self.reps, self.atoms = systems.c4_batch(n_rep, seed=13 + 1000 * rank)
+            self.n_electrode = sum(int((a["z"] == dml.Z_CG).sum()) for a in self.atoms)
+            self.desc = ("config 4: %d replicas of uneven size (L x L x 2-cell bcc Li electrode, "
+                         "L uniform in 5..40; ions log-uniform in 50..20000; height by the 1 M "
+                         "rule, at least 20 A), Brownian dt=5e-5 ps, skin 2, piston at half "
+                         "height" % n_rep)
         elif name == "c2":
             self.batched = False
             self.p = systems.c2_params(seed=1234 + rank)
@@ -401,6 +416,115 @@ def roofline_of(sim, wl, nprof):
             "phase_ms_per_step": {k: v / nprof for k, v in ph.items()}}
 
 
+def force_error_at(p, state, step):
+    """Mixed vs FP64 forces at the positions reached by one FP64 ermak_a from
+    `state` (the move brings ions inside each other's r0): both forms run
+    test_update and fuerza on identical positions.  Metrics as in
+    force_error_probe."""
+    import copy
+
+    import numpy as np
+
+    import dml
+
+    EV = 96.485 * 100.0
+    q = copy.copy(p)
+    q.precision = dml.PRECISION_FP64
+    s0 = dml.Simulation(q)
+    s0.set_atoms(state)
+    s0.test_update()
+    s0.ermak_a(step)
+    moved = s0.get_atoms()
+    s0.close()
+    out = []
+    for prec in (dml.PRECISION_MIXED, dml.PRECISION_FP64):
+        q = copy.copy(p)
+        q.precision = prec
+        s1 = dml.Simulation(q)
+        s1.set_atoms(moved)
+        s1.test_update()
+        s1.fuerza()
+        a = s1.get_atoms()
+        out.append((a["force"], a["epot"], a["z"]))
+        s1.close()
+    (fm, em, z), (fp, ep, _) = out
+    mob = z != dml.Z_CG
+    fr = np.sqrt((fp[mob] ** 2).sum(1))
+    dd = np.sqrt(((fm[mob] - fp[mob]) ** 2).sum(1))
+    hit = fr > 0
+    frms = float(np.sqrt((fr[hit] ** 2).mean())) if hit.any() else 1.0
+    rel = dd / np.maximum(fr, frms)
+    return {"max_rel": float(rel.max()), "rms_rel": float(np.sqrt((rel[hit] ** 2).mean()))
+            if hit.any() else 0.0, "max_abs_ev_per_A": float(dd.max() / EV),
+            "energy_rel": float(abs(em.sum() - ep.sum()) / abs(ep.sum())) if ep.sum() else 0.0,
+            "interacting_ions": int(hit.sum())}
+
+
+def run_accuracy(args):
+    """Config 3: config 2's system (80k electrode atoms, 200k Li+) in the
+    chosen form against the plain FP64 form (bit-exact to the oracle): the
+    force and energy error at steps 0, 1/10 and all of the run (seed 0), and
+    the deposition count of each form over `--seeds` seeds (Philox streams
+    keyed by seed, step and atom, shared by both forms)."""
+    import copy
+    import statistics as st
+
+    import dml
+    from tests import systems
+
+    dml.build()
+    steps = args.steps
+    marks = [0, steps // 10, steps]
+    errors, depo = {}, {"fp64": [], "mixed": []}
+    rate = {"fp64": [], "mixed": []}
+    for seed in range(args.seeds):
+        p = systems.c2_params(seed=1234 + seed)
+        atoms = systems.c2_atoms(seed=7 + seed)
+        sims = {}
+        for form, prec in (("fp64", dml.PRECISION_FP64), ("mixed", dml.PRECISION_MIXED)):
+            q = copy.copy(p)
+            q.precision = prec
+            sims[form] = dml.Simulation(q)
+            sims[form].set_atoms(atoms)
+            sims[form].setup()
+        done = 0
+        for m in marks:
+            if m > done:
+                for form, sim in sims.items():
+                    c0 = sim.counters()
+                    t0 = time.perf_counter()
+                    sim.step(m - done)
+                    dt = time.perf_counter() - t0
+                    c1 = sim.counters()
+                    rate[form].append(0.5 * (c0["n_ref"] + c1["n_ref"]) * (m - done) / dt)
+                done = m
+            if seed == 0:
+                st_fp = sims["fp64"].get_atoms()
+                errors[str(m)] = force_error_at(p, st_fp, sims["fp64"].counters()["step"] + 1)
+        for form, sim in sims.items():
+            depo[form].append(int(sim.counters()["depo"]))
+            sim.close()
+    mf, mm = st.mean(depo["fp64"]), st.mean(depo["mixed"])
+    sf = st.stdev(depo["fp64"]) if len(depo["fp64"]) > 1 else 0.0
+    diff = [a - b for a, b in zip(depo["mixed"], depo["fp64"])]
+    line = {"metric": METRIC, "workload": "config 3: config 2's system (351x351x320 A, 80k "
+            "electrode atoms + 200k Li+, Ermak dt=1fs, piston z0=160, skin 10) in the chosen "
+            "form vs the plain FP64 form", "steps": steps, "seeds": args.seeds,
+            "value": st.mean(rate["mixed"]), "unit": UNIT,
+            "plain_fp64_value": st.mean(rate["fp64"]),
+            "value_note": "wall-clock particle-steps/s of the runs below (step() calls, "
+                          "including list rebuilds)",
+            "force_error_at_step": errors, "force_error_tolerance": 1e-6,
+            "deposition": {"fp64": depo["fp64"], "mixed": depo["mixed"],
+                           "fp64_mean": mf, "fp64_sigma": sf, "mixed_mean": mm,
+                           "mean_difference_in_fp64_sigma": (mm - mf) / sf if sf else None,
+                           "per_seed_difference": diff,
+                           "within_1_sigma": bool(sf == 0.0 or abs(mm - mf) <= sf)},
+            "data": "synthetic", "dtype": "f32 pair forces, int64 fixed-point sums, f64 positions"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_gpu(args, ws, rank, local):
     import dml
 
@@ -514,21 +638,28 @@ def run_gpu(args, ws, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="c5", choices=["c5", "c2"])
-    ap.add_argument("--replicas", type=int, default=256)
+    ap.add_argument("--workload", default="c5", choices=["c5", "c2", "c3", "c4"])
+    ap.add_argument("--seeds", type=int, default=8)
+    ap.add_argument("--replicas", type=int, default=None)
     ap.add_argument("--form", default=None, choices=["chosen", "plain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-compare", action="store_true")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 10000 if args.workload == "c3" else 100
+    if args.replicas is None:
+        args.replicas = 1024 if args.workload == "c4" else 256
     if args.warmup < 3:
         args.warmup = 3
     ws, rank, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, ws, rank)
+    if args.workload == "c3":
+        return run_accuracy(args) if rank == 0 else 0
     if ws > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
     return run_gpu(args, ws, rank, local)

@@ -97,6 +97,19 @@ void make_repconst(const dml_params& P, const dml_replica& r, RepConst& R) {
   R.ncell = R.use_cells ? R.head_dim[0] * R.head_dim[1] * R.head_dim[2] : 0;
   R.tess_hif = (float)((R.ncells[2] + 1) * R.cell[2]);
   R.seed = r.seed;
+  // FP32 coordinates carry at most 2^-24 relative rounding; a difference of
+  // two of them and its square stay well inside 64 ulps of maxc.
+  const double maxc = 2.0 * std::max({r.box[0], r.box[1], r.box[2], r.zmax}) + 100.0;
+  const double margin = std::max(1e-3, 64.0 * std::ldexp(maxc, -24));
+  const double rl = P.rc + P.skin;
+  R.margin = (float)margin;
+  R.rlist_lo2 = (float)((rl - margin) * (rl - margin));
+  R.rlist_hi2 = (float)((rl + margin) * (rl + margin));
+  R.rc_lo2 = (float)((P.rc - margin) * (P.rc - margin));
+  R.rc_hi2 = (float)((P.rc + margin) * (P.rc + margin));
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      R.r0f_pref2[i][j] = (float)((P.r0[i][j] + margin) * (P.r0[i][j] + margin));
   // gcmc_run's trial points lie in [z0, zmax]: their 27-cell stencils reach
   // the layers of those points and one more on either side, wrapped along z
   // like every stencil (Cells.F90:378-404); its cell sort covers only those.
@@ -116,22 +129,13 @@ void make_repconst(const dml_params& P, const dml_replica& r, RepConst& R) {
   }
 }
 
-// Context-wide constants (see KParams); maxc bounds every coordinate.
-void make_kparams(const dml_params& P, double maxc, KParams& K) {
+// Context-wide constants (see KParams).
+void make_kparams(const dml_params& P, KParams& K) {
   std::memset(&K, 0, sizeof K);
-  maxc = 2.0 * maxc + 100.0;
-  // FP32 coordinates carry at most 2^-24 relative rounding; a difference of
-  // two of them and its square stay well inside 64 ulps of maxc.
-  double margin = std::max(1e-3, 64.0 * std::ldexp(maxc, -24));
-  K.margin = (float)margin;
   K.rc2 = P.rc * P.rc;
   double rl = P.rc + P.skin;
   K.rlist2 = rl * rl;
   K.skin = P.skin;
-  K.rlist_lo2 = (float)((rl - margin) * (rl - margin));
-  K.rc_lo2 = (float)((P.rc - margin) * (P.rc - margin));
-  K.rc_hi2 = (float)((P.rc + margin) * (P.rc + margin));
-  K.rlist_hi2 = (float)((rl + margin) * (rl + margin));
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
       double r0 = P.r0[i][j], eps = P.eps[i][j];
@@ -139,7 +143,6 @@ void make_kparams(const dml_params& P, double maxc, KParams& K) {
       K.r0sq[i][j] = r0 * r0;
       K.b0[i][j] = pow6h(r0);
       K.c0[i][j] = eps * 12.0 * K.b0[i][j];
-      K.r0f_pref2[i][j] = (float)((r0 + margin) * (r0 + margin));
       K.pair_on[i][j] = eps != 0.0;
       K.c12[i][j] = r0 > 0.0 ? 12.0 * eps / (r0 * r0) : 0.0;
     }
@@ -181,6 +184,7 @@ void make_kparams(const dml_params& P, double maxc, KParams& K) {
   K.max_passes = P.max_passes;
   K.mixed = P.precision == DML_PRECISION_MIXED;
   K.scan_lanes = 16;  // until the step graph is tuned
+  K.near_lanes = 32;
   K.rcf = (float)P.rc;
   // 2^32 per eV/Å; 1 eV = 96.485 * 100 ui (dana.F90:23)
   K.fix_scale = std::ldexp(1.0, 32) / (96.485 * 100.0);
@@ -364,14 +368,18 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
   return 0;
 }
 
-// Autotuner of the force scan's thread mapping: each mapping (4, 8, 16 or
-// 32 lanes per list row) scans the loaded lists a few times without side
-// effects (the candidate queue is cleared after every launch) and the
-// fastest is kept for the step graph.  Row lengths depend on the skin and
-// the density, so the best mapping is a property of the workload.
+// Autotuner of the thread mapping of the step's per-row scan: the force
+// scan (Ermak) or the near-contact search of overlap_moveback (Brownian,
+// which has no force scan and searches every step).  Each mapping (1, 2, 4,
+// 8, 16 or 32 lanes per list row) scans the loaded lists a few times and the
+// fastest is kept for the step graph.  The trial scans change nothing the
+// next step reads: the candidate queue is cleared after each one, and the
+// near entries, unions and active flags are reset or rewritten by every
+// step before they are used.  Row lengths depend on the skin, the density
+// and the electrode, so the best mapping is a property of the workload.
 int autotune_scan(dml_ctx* c) {
-  if (c->P.integrator != DML_INTEGRATOR_ERMAK) return 0;
   cudaStream_t s = c->stream;
+  const bool ermak = c->P.integrator == DML_INTEGRATOR_ERMAK;
   const int lanes[kScanMappings] = {1, 2, 4, 8, 16, 32};
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
@@ -379,16 +387,21 @@ int autotune_scan(dml_ctx* c) {
   k_rank_prefix(c->D, s);
   KParams k = c->K;
   float best = 1e30f;
-  int best_l = 16;
-  for (int v = 0; v < kScanMappings; ++v) {
-    k.scan_lanes = lanes[v];
-    k_force_scan(c->D, k, c->D.cap, false, s);  // warm-up
-    k_reset_candidates(c->D, s);
-    CK(cudaEventRecord(e0, s));
-    for (int rep = 0; rep < 3; ++rep) {
+  int best_l = 32;
+  auto scan = [&]() {
+    if (ermak) {
       k_force_scan(c->D, k, c->D.cap, false, s);
       k_reset_candidates(c->D, s);
+    } else {
+      k_overlap_detect(c->D, k, c->D.cap, 0, s);
     }
+  };
+  for (int v = 0; v < kScanMappings; ++v) {
+    k.scan_lanes = lanes[v];
+    k.near_lanes = lanes[v];
+    scan();  // warm-up
+    CK(cudaEventRecord(e0, s));
+    for (int rep = 0; rep < 3; ++rep) scan();
     CK(cudaEventRecord(e1, s));
     CK(cudaEventSynchronize(e1));
     float ms = 0;
@@ -401,7 +414,10 @@ int autotune_scan(dml_ctx* c) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  c->K.scan_lanes = best_l;
+  if (ermak)
+    c->K.scan_lanes = best_l;
+  else
+    c->K.near_lanes = best_l;
   return finish(c);
 }
 
@@ -519,12 +535,10 @@ int dml_create_batch(const dml_params* p, int32_t n_rep, const dml_replica* reps
   double rmax = p->rc + p->skin;
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) rmax = std::max(rmax, p->r0[i][j]);
-  double maxc = 0.0;
   for (int r = 0; r < n_rep; ++r) {
     const dml_replica& q = reps[r];
     if (!(q.box[0] > 0 && q.box[1] > 0 && q.box[2] > 0)) return DML_E_ARG;
     if (q.box[0] * 0.5 <= rmax + 0.01 || q.box[1] * 0.5 <= rmax + 0.01) return DML_E_ARG;
-    maxc = std::max({maxc, q.box[0], q.box[1], q.box[2], q.zmax});
   }
   dml_ctx* c = new dml_ctx();
   c->P = *p;
@@ -533,7 +547,7 @@ int dml_create_batch(const dml_params* p, int32_t n_rep, const dml_replica* reps
   if (c->P.event_cap <= 0) c->P.event_cap = 64;
   if (c->P.event_cap > 128) c->P.event_cap = 128;
   c->reps.assign(reps, reps + n_rep);
-  make_kparams(c->P, maxc, c->K);
+  make_kparams(c->P, c->K);
   c->rc.resize(n_rep);
   for (int r = 0; r < n_rep; ++r) make_repconst(c->P, reps[r], c->rc[r]);
   cudaError_t e = cudaGetDevice(&c->device);
@@ -991,7 +1005,8 @@ int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phas
 
 int dml_get_tuning(dml_ctx* c, int32_t* scan_lanes, float* scan_us) {
   if (!c) return DML_E_ARG;
-  if (scan_lanes) *scan_lanes = c->K.scan_lanes;
+  if (scan_lanes)
+    *scan_lanes = c->P.integrator == DML_INTEGRATOR_ERMAK ? c->K.scan_lanes : c->K.near_lanes;
   if (scan_us)
     for (int v = 0; v < kScanMappings; ++v) scan_us[v] = c->tune_us[v];
   return 0;

@@ -52,7 +52,13 @@ struct RepConst {
                             // one sentinel cell (always empty) whose start is the end
   int base, cap, nblk;      // positions [base, base + cap), cap / kSpan blocks
   unsigned long long seed;  // Philox key of this replica
-  // z layers of cells that gcmc_run's searches reach (bit c3, 1 <= c3 <=
+  // FP32 pre-filter bounds of this replica: the error margin of an FP32
+  // coordinate difference (64 ulps of twice the largest coordinate, at least
+  // 1e-3 Å) and the squared cut-offs widened or narrowed by it
+  float margin;
+  float rlist_lo2, rlist_hi2, rc_lo2, rc_hi2;
+  float r0f_pref2[3][3];    // (r0 + margin)^2 per element pair
+  // z layers of cells that gcmc_run's searches reach (bit c3, 1 <=
   // ncells[2]); gl_all: every layer (its cell sort then covers them all)
   unsigned long long gl_mask;
   int gl_all;
@@ -124,20 +130,17 @@ struct KParams {
   double rlist2;            // (rc+skin)^2
   double skin;
   double eps[3][3], r0sq[3][3], b0[3][3], c0[3][3];  // b0 = r0^6, c0 = eps*12*b0
-  float r0f_pref2[3][3];    // FP32 pre-filter thresholds (r0 + margin)^2
   int pair_on[3][3];        // eps != 0 (other pairs add signed zeros only)
   // mixed form: FP32 force vectors, int64 fixed-point sums
   int mixed;
-  int scan_lanes;           // lanes per list row in the force scan (4, 8, 16, 32; tuned)
+  int scan_lanes;           // lanes per list row in the force scan (1 .. 32; tuned)
+  int near_lanes;           // lanes per list row in the near search (1 .. 32; tuned)
   double c12[3][3];         // 12 eps / r0^2 (scalar pair force of the mixed form)
   int cand_cap;
   float rcf;                // rc (FP32, pre-filters)
-  float rc_lo2, rc_hi2;     // (rc -+ margin)^2: FP32 hard-core test decided outside
   double beta_t[3];         // sqrt(kB T / m) per element (gcmc_run's Maxwell draw)
   double inv_mass[3];       // 1 / m (ermak_b of the mixed form)
   double fix_scale, fix_inv; // 2^32 per eV/Å in ui/Å, and its inverse
-  float rlist_lo2, rlist_hi2; // list shell bounds (FP32)
-  float margin;             // FP32 position error bound
   double mass[3];
   // Ermak (set_ermak, dana.F90:947-971)
   double cc0, cc1, cc2, cc2h, cc1mcc2, crv1, crv2;

@@ -311,7 +311,7 @@ __device__ __forceinline__ void stv(double4* a, int h, float x, float y, float z
 // edge in x and y and from 0 and zmax in z.
 __device__ __forceinline__ bool pbc_quiet(const KParams& p, const RepConst& R, float4 f,
                                           float zmaxf) {
-  const float e = p.margin;
+  const float e = R.margin;
   return f.x > e && f.x < R.boxf[0] - e && f.y > e && f.y < R.boxf[1] - e && f.z > e &&
          f.z < zmaxf - e;
 }
@@ -544,9 +544,9 @@ __device__ void uf_union(Global* g, volatile int* uf, int a, int b) {
 
 // Near radius of overlap_moveback, rc + 2 delta in FP32 with margin (a
 // superset of the pairs that can touch during the passes).
-__device__ __forceinline__ float near_radius2(const Dev& d, const KParams& p) {
+__device__ __forceinline__ float near_radius2(const Dev& d, const KParams& p, const RepConst& R) {
   float delta = sqrtf(__uint_as_float(d.g->delta2f_bits));
-  float rnf = (p.rcf + 2.0f * delta) * 1.000001f + 4.0f * p.margin + 1e-3f;
+  float rnf = (p.rcf + 2.0f * delta) * 1.000001f + 4.0f * R.margin + 1e-3f;
   return rnf * rnf;
 }
 
@@ -586,7 +586,7 @@ __device__ __forceinline__ void force_scan_rows(const Dev& d, const KParams& p, 
   const int* row = d.list + (size_t)(h >= 0 ? h : 0) * p.mnb;
   // With NEAR the same pass records overlap_moveback's near entries (list
   // entries within rc + 2 delta, in list order) and unites their components.
-  const float rn2 = NEAR ? near_radius2(d, p) : 0.0f;
+  const float rn2 = NEAR ? near_radius2(d, p, R) : 0.0f;
   int* near = d.near + (size_t)(h >= 0 ? h : 0) * kNearCap;
   int ncnt = 0;
   bool any = false;
@@ -616,7 +616,7 @@ __device__ __forceinline__ void force_scan_rows(const Dev& d, const KParams& p, 
       }
       // fuerza: r <= r0 + margin, eps != 0, not CG-CG (signed zeros only)
       const bool cand = live && !(k == DML_Z_CG && m == DML_Z_CG) && p.pair_on[k - 1][m - 1] &&
-                        df <= p.r0f_pref2[k - 1][m - 1];
+                        df <= R.r0f_pref2[k - 1][m - 1];
       const unsigned bc = __ballot_sync(FULL, cand);
       if (bc) {
         int base_q = 0;
@@ -1012,7 +1012,7 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots) {
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
   const float tinyf = 1e-16f;
-  const float e = p.margin;
+  const float e = R.margin;
   float a1 = tinyf, a2 = tinyf;
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) {
@@ -1538,9 +1538,9 @@ __device__ __forceinline__ void list_cells_row(const Dev& d, const KParams& p, i
         float fx, fy, fz;
         vdist_nint_f(R, Q, Pf, fx, fy, fz);
         float drf = fx * fx + fy * fy + fz * fz;
-        if (drf < p.rlist_lo2) {
+        if (drf < R.rlist_lo2) {
           inc = true;
-        } else if (drf <= p.rlist_hi2) {
+        } else if (drf <= R.rlist_hi2) {
           double vx, vy, vz;
           vdist_nint(R, d.pos[j], P, vx, vy, vz);
           double rd = dot3(vx, vy, vz);
@@ -1598,9 +1598,9 @@ __device__ __forceinline__ void list_verlet_row(const Dev& d, const KParams& p, 
         float fx, fy, fz;
         vdist_nint_f(R, Pf, Q, fx, fy, fz);
         float drf = fx * fx + fy * fy + fz * fz;
-        if (drf < p.rlist_lo2) {
+        if (drf < R.rlist_lo2) {
           inc = true;
-        } else if (drf <= p.rlist_hi2) {
+        } else if (drf <= R.rlist_hi2) {
           double vx, vy, vz;
           vdist_nint(R, P, d.pos[j], vx, vy, vz);
           double rd = dot3(vx, vy, vz);
@@ -1694,57 +1694,72 @@ __global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
   for (int u = 0; u < kSlotU; ++u) overlap_init_at(d, p, n_slots, rep, span_pos(u));
 }
 
-// Near entries of every hs%ref member: list entries within rc + 2 delta
-// (FP32 with margin; a superset is harmless) in list order.
-__device__ __forceinline__ void overlap_detect_row(const Dev& d, const KParams& p, int r,
-                                                   int only_rebuilt) {
-  int lane = threadIdx.x & 31;
+// Near entries of hs%ref members: list entries within rc + 2 delta (FP32
+// with margin; a superset is harmless) in list order.  32 / L members per
+// warp, L lanes each, 4 entries in flight per lane; the mapping is tuned
+// for the workload (with the Brownian integrator this search runs every step).
+template <int L>
+__device__ __forceinline__ void overlap_detect_rows(const Dev& d, const KParams& p, const int* pre,
+                                                    int w, int total, int only_rebuilt) {
+  constexpr int U = 4, STEP = L * U;
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, sl = lane % L, sub = lane / L;
+  const unsigned smask = (L == 32 ? FULL : ((1u << L) - 1u)) << (sub * L);
+  const int i = (32 / L) * w + sub;
+  const int r = i < total ? row_rank_in(d, pre, i) : 0;
   const int rep = d.rep_of[r];
   const RepConst& R = d.rc[rep];
-  Scalars* sc = d.sc + rep;
-  if (r - R.base >= sc->n_rank) return;
-  if (only_rebuilt && !sc->rebuild) return;  // its near entries are current
-  int h = d.ref[r];
-  if (h < 0) return;
+  const Scalars* sc = d.sc + rep;
+  int h = -1, n = 0;
+  float4 Pf = make_float4(0.f, 0.f, 0.f, 0.f);
+  // rows of replicas whose near entries are current stay as they are
+  if (i < total && r - R.base < sc->n_rank && !(only_rebuilt && !sc->rebuild)) h = d.ref[r];
+  if (h >= 0) {
+    Pf = d.posf[h];
+    n = d.nn[h];
+  }
+  int nmax = n;
+#pragma unroll
+  for (int o = L; o < 32; o <<= 1) nmax = max(nmax, __shfl_xor_sync(FULL, nmax, o));
   // rc + 2 delta in FP32 (sqrtf is exact to an ulp; the margin covers it)
-  const float rn2 = near_radius2(d, p);
-  float4 Pf = d.posf[h];
-  int n = d.nn[h];
-  const int* row = d.list + (size_t)h * p.mnb;
-  int* near = d.near + (size_t)h * kNearCap;
+  const float rn2 = near_radius2(d, p, R);
+  const int* row = d.list + (size_t)(h >= 0 ? h : 0) * p.mnb;
+  int* near = d.near + (size_t)(h >= 0 ? h : 0) * kNearCap;
+  const unsigned lt = (1u << lane) - 1u;
   int cnt = 0;
   bool any = false;
-  for (int base = 0; base < n; base += 64) {
-    int jj0 = base + lane, jj1 = jj0 + 32;
-    int j0 = jj0 < n ? __ldg(row + jj0) : -1;
-    int j1 = jj1 < n ? __ldg(row + jj1) : -1;
-    float4 Q0 = make_float4(0.f, 0.f, 0.f, 0.f), Q1 = Q0;
-    if (j0 >= 0) Q0 = d.posf[j0];
-    if (j1 >= 0) Q1 = d.posf[j1];
+  for (int base = 0; base < nmax; base += STEP) {
+    int j[U];
+    float4 Q[U];
 #pragma unroll
-    for (int half = 0; half < 2; ++half) {
-      int j = half ? j1 : j0;
-      float4 Q = half ? Q1 : Q0;
+    for (int u = 0; u < U; ++u) {
+      const int jj = base + L * u + sl;
+      j[u] = jj < n ? __ldg(row + jj) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) Q[u] = j[u] >= 0 ? d.posf[j[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
       bool inc = false;
-      if (j >= 0 && elem_of(Q) != 0) {
+      if (j[u] >= 0 && elem_of(Q[u]) != 0) {
         float fx, fy, fz;
-        vdist_nint_f(R, Pf, Q, fx, fy, fz);
+        vdist_nint_f(R, Pf, Q[u], fx, fy, fz);
         inc = fx * fx + fy * fy + fz * fz <= rn2;
       }
-      unsigned bal = __ballot_sync(0xffffffffu, inc);
-      int pre = __popc(bal & ((1u << lane) - 1u));
+      const unsigned bal = __ballot_sync(FULL, inc) & smask;
       if (inc) {
-        if (cnt + pre < kNearCap) near[cnt + pre] = j;
-        if (elem_of(Q) != DML_Z_CG) {
-          uf_union(d.g, (volatile int*)d.uf, h, j);
-          d.active[j] = 1;
+        const int pos = cnt + __popc(bal & lt);
+        if (pos < kNearCap) near[pos] = j[u];
+        if (elem_of(Q[u]) != DML_Z_CG) {
+          uf_union(d.g, (volatile int*)d.uf, h, j[u]);
+          d.active[j[u]] = 1;
         }
       }
       cnt += __popc(bal);
       any = any || bal != 0;
     }
   }
-  if (lane == 0) {
+  if (sl == 0 && h >= 0) {
     d.near_count[h] = cnt > kNearCap ? -1 : cnt;
     if (any) d.active[h] = 1;
   }
@@ -1752,14 +1767,15 @@ __device__ __forceinline__ void overlap_detect_row(const Dev& d, const KParams& 
 
 // mode 0: every replica; 1: only if some list was rebuilt since the force
 // scan, for the replicas that rebuilt; 2: the replicas that rebuilt.
+template <int L>
 __global__ void __launch_bounds__(256) overlap_detect_kernel(Dev d, KParams p, int mode) {
   if (mode == 1 && !d.g->near_stale) return;  // the force scan found them
   const int nw = gridDim.x * (blockDim.x >> 5);
   // modes 1 and 2 walk only the rows of the replicas that rebuilt
   const int* pre = mode != 0 ? d.reb_pre : d.rank_pre;
   const int total = pre[d.nrep];
-  for (int i = warp_id_global(); i < total; i += nw)
-    overlap_detect_row(d, p, row_rank_in(d, pre, i), mode != 0);
+  for (int w = warp_id_global(); (32 / L) * w < total; w += nw)
+    overlap_detect_rows<L>(d, p, pre, w, total, mode != 0);
 }
 
 // Atoms with no near entry are examined trivially in pass 1 (skip = true)
@@ -2501,11 +2517,11 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
             }
             return rd;
           };
-          if (df <= p.rc_hi2 && d.in_gcmc[j] && (df < p.rc_lo2 || exact() < p.rc2)) ov = true;
-          if (flat && df <= p.rlist_hi2) {
+          if (df <= R.rc_hi2 && d.in_gcmc[j] && (df < R.rc_lo2 || exact() < p.rc2)) ov = true;
+          if (flat && df <= R.rlist_hi2) {
             const bool live = d.state[j] == ST_LIVE;
             bool own, app;
-            if (df < p.rlist_lo2) {
+            if (df < R.rlist_lo2) {
               own = app = true;
             } else {
               own = exact() < p.rlist2;
@@ -2897,8 +2913,8 @@ __device__ __forceinline__ bool hard_core_in(const KParams& p, const RepConst& R
   float fx, fy, fz;
   vdist_nint_f(R, af, bf, fx, fy, fz);
   const float df = fx * fx + fy * fy + fz * fz;
-  if (df > p.rc_hi2) return false;
-  if (df < p.rc_lo2) return true;
+  if (df > R.rc_hi2) return false;
+  if (df < R.rc_lo2) return true;
   double vx, vy, vz;
   vdist_nint(R, a, b, vx, vy, vz);
   return dot3(vx, vy, vz) < p.rc2;
@@ -3144,17 +3160,17 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
         float fx, fy, fz;
         vdist_nint_f(R, Rtf, Q, fx, fy, fz);
         const float df = fx * fx + fy * fy + fz * fz;
-        if (df <= p.rlist_hi2) {
+        if (df <= R.rlist_hi2) {
           double rd = -1.0;
-          if (!(df < p.rc_lo2 && df < p.rlist_lo2)) {
+          if (!(df < R.rc_lo2 && df < R.rlist_lo2)) {
             double vx, vy, vz;
             vdist_nint(R, Rt, d.pos[j], vx, vy, vz);
             rd = dot3(vx, vy, vz);
           }
-          if (df <= p.rc_hi2 && d.in_gcmc[j] && (df < p.rc_lo2 || rd < p.rc2)) isb = true;
+          if (df <= R.rc_hi2 && d.in_gcmc[j] && (df < R.rc_lo2 || rd < p.rc2)) isb = true;
           const bool live = d.state[j] == ST_LIVE;
-          const bool own = df < p.rlist_lo2 || rd < p.rlist2;
-          const bool app = df < p.rlist_lo2 || !(rd > p.rlist2);
+          const bool own = df < R.rlist_lo2 || rd < p.rlist2;
+          const bool app = df < R.rlist_lo2 || !(rd > p.rlist2);
           if (live && own) fl |= 1;
           if (live && app && !((dupm >> q) & 1u) && d.rank[j] >= 0) fl |= 2;
           isc = fl != 0;
@@ -4025,7 +4041,16 @@ int k_overlap_prepare(const Dev& d, const KParams& p, int n_slots, cudaStream_t 
 }
 
 int k_overlap_detect(const Dev& d, const KParams& p, int n_rank, int mode, cudaStream_t s) {
-  overlap_detect_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, mode);
+  const int L = p.near_lanes;
+  const int nb = nblk_rows((n_rank + 32 / L - 1) / (32 / L));
+  switch (L) {
+    case 1: overlap_detect_kernel<1><<<nb, kBlock, 0, s>>>(d, p, mode); break;
+    case 2: overlap_detect_kernel<2><<<nb, kBlock, 0, s>>>(d, p, mode); break;
+    case 4: overlap_detect_kernel<4><<<nb, kBlock, 0, s>>>(d, p, mode); break;
+    case 8: overlap_detect_kernel<8><<<nb, kBlock, 0, s>>>(d, p, mode); break;
+    case 16: overlap_detect_kernel<16><<<nb, kBlock, 0, s>>>(d, p, mode); break;
+    default: overlap_detect_kernel<32><<<nb, kBlock, 0, s>>>(d, p, mode); break;
+  }
   return 1;
 }
 

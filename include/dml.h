@@ -288,10 +288,12 @@ int dml_get_neighbors(dml_ctx* c, int32_t* n_ref, int32_t* nn, int32_t* list, in
  * (max_nn and passes as maxima). */
 int dml_get_counters(dml_ctx* c, dml_counters* out);
 
-/* Autotuner result (no counterpart in the reference): the force scan's
- * lanes per list row chosen when the step graph was built (1, 2, 4, 8, 16 or
- * 32), and the measured time of each mapping in microseconds (scan_us[6], in
- * that order, zero before tuning).  Either pointer may be NULL. */
+/* Autotuner result (no counterpart in the reference): the lanes per list
+ * row (1, 2, 4, 8, 16 or 32) chosen, when the step graph was built, for the
+ * step's per-row scan (the force scan with the Ermak integrator, the
+ * near-contact search of overlap_moveback with the Brownian one), and the
+ * measured time of each mapping in microseconds (scan_us[6], in that order,
+ * zero before tuning).  Either pointer may be NULL. */
 int dml_get_tuning(dml_ctx* c, int32_t* scan_lanes, float* scan_us);
 int dml_get_counters_replica(dml_ctx* c, int32_t rep, dml_counters* out);
 

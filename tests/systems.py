@@ -161,3 +161,42 @@ def slab_activity(p, atoms, seed, samples=20000):
     d, _ = tree.query(pts, k=1)
     p_ins = max(float((d >= p.rc).mean()), 1e-3)
     return n_slab / (L * L * (p.zmax - p.z0) * p_ins)
+
+
+C4_REPLICAS = 1024
+
+
+def c4_batch(n_rep=C4_REPLICAS, seed=13, precision=dml.PRECISION_MIXED):
+    """Config 4: n_rep independent replicas of uneven size.  Replica r: a
+    2-cell-thick bcc electrode of L x L cells, L uniform in 5..40; N ions,
+    log-uniform in 50..20 000; the height set by the reference's 1 M rule
+    (dana.F90:349-353: N = 6.022e-4 Lx Ly h, h above z = 10 Å, at least
+    20 Å); its own Philox seed.  Brownian integrator with the reference's
+    Brownian GCMC run time step and shell (tests/gcmc: 5e-5 ps, nb_dcut
+    2 Å), piston reservoir at half height (the ratio of tests/ermak), ions
+    at least rc = 3.2 Å apart."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    p = dml.default_params()
+    p.integrator = dml.INTEGRATOR_BROWNIAN
+    p.reservoir = dml.RESERVOIR_PISTON
+    p.h = 5e-5
+    p.skin = 2.0
+    p.precision = precision
+    p.seed = seed
+    p.mnb = 128
+    a = 3.51
+    reps, atoms = [], []
+    for r in range(n_rep):
+        cells = int(rng.integers(5, 41))
+        n_ion = int(round(float(np.exp(rng.uniform(np.log(50.0), np.log(20000.0))))))
+        L = cells * a
+        height = max(20.0, n_ion / (6.022e-4 * L * L))
+        lz = 10.0 + height
+        rseed = seed * 100003 + r
+        reps.append(dml.replica_of(p, box=[L, L, lz], z0=0.5 * lz, zmax=lz, seed=rseed))
+        atoms.append(dml.slab_system(cells, cells, 2, lz, n_ion, 10.0, lz, rseed, dmin=3.2))
+    p.box[:] = list(reps[0].box)
+    p.z0, p.zmax = reps[0].z0, reps[0].zmax
+    return p, reps, atoms
