@@ -599,7 +599,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   const int nrep = c->D.nrep;
   Dev& d = c->D;
   // capacities: positions per replica, a multiple of kSpan
-  int total = 0, ncell = 0, any_cells = 0, any_verlet = 0;
+  int total = 0, ncell = 0, any_cells = 0, any_verlet = 0, n_cch = 0;
   for (int r = 0; r < nrep; ++r) {
     const dml_atoms* a = atoms + r;
     if (a->n <= 0 || !a->pos || !a->z) return DML_E_ARG;
@@ -612,6 +612,8 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     R.cap = cap;
     R.nblk = cap / kSpan;
     R.cell_off = ncell;
+    R.cch0 = n_cch;
+    n_cch += (R.ncell + kCellChunk - 1) / kCellChunk;
     ncell += R.ncell + (R.use_cells ? 1 : 0);  // + the replica's sentinel cell
     total += cap;
     if (R.use_cells) any_cells = 1; else any_verlet = 1;
@@ -620,6 +622,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   d.max_rep_cap = 0;
   for (int r = 0; r < nrep; ++r) d.max_rep_cap = std::max(d.max_rep_cap, c->rc[r].cap);
   d.ncell_tot = ncell;
+  d.n_cch = n_cch;
   d.any_cells = any_cells;
   d.any_verlet = any_verlet;
   const int cap = total;
@@ -684,6 +687,18 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.rank_pre, nrep + 1);
   AL(d.reb_pre, nrep + 1);
   AL(d.big_cells, ncell + 1);
+  AL(d.cch_rep, n_cch > 0 ? n_cch : 1);
+  {
+    std::vector<int> cr(n_cch > 0 ? n_cch : 1, 0);
+    for (int r = 0; r < nrep; ++r) {
+      const RepConst& R = c->rc[r];
+      for (int q = 0; q < (R.ncell + kCellChunk - 1) / kCellChunk; ++q) cr[R.cch0 + q] = r;
+    }
+    // on the context stream, after the zeroing of the new allocation
+    CK(cudaMemcpyAsync(d.cch_rep, cr.data(), sizeof(int) * cr.size(), cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
   if (c->P.reservoir == DML_RESERVOIR_GCMC) {
     const bool par = c->P.nadj <= kGcmcMaxTrials;
     AL(d.grp, nrep);

@@ -30,6 +30,7 @@ constexpr int kNearCap = 32;   // near-contact entries per atom (overlap)
 constexpr int kBlock = 256;
 constexpr int kSlotU = 4;                 // positions per thread of the per-position kernels
 constexpr int kSpan = kBlock * kSlotU;    // positions per block; replica capacities are multiples
+constexpr int kCellChunk = kBlock * 4;    // cells per block of the per-cell kernels
 
 // Replicas.  A context holds one or more independent systems ("replicas",
 // the batched form); a single system is a batch of one.  Replica r owns the
@@ -50,6 +51,7 @@ struct RepConst {
   int use_cells;
   int cell_off, ncell;      // this replica's cells [cell_off, cell_off + ncell), then
                             // one sentinel cell (always empty) whose start is the end
+  int cch0;                 // its first chunk of kCellChunk cells (per-cell kernels)
   int base, cap, nblk;      // positions [base, base + cap), cap / kSpan blocks
   unsigned long long seed;  // Philox key of this replica
   // FP32 pre-filter bounds of this replica: the error margin of an FP32
@@ -248,6 +250,8 @@ struct Dev {
   int* reb_pre;       // [nrep + 1] the same prefix over the replicas whose list the
                       // last displacement test rebuilds (0 rows for the others)
   int* big_cells;     // cells too large for the per-thread sort of cell_order
+  int* cch_rep;       // [n_cch] replica of every chunk of kCellChunk cells
+  int n_cch;
   // gcmc_run on the parallel path (allocated with the GCMC reservoir)
   GcmcTrialPre* gpre;  // [nrep][kGcmcMaxTrials]
   unsigned* gpm;       // [nrep][kGcmcMaxTrials][kGcmcMaskW] earlier trial points within rc

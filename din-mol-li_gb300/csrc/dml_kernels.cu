@@ -1014,11 +1014,25 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots) {
   const float tinyf = 1e-16f;
   const float e = R.margin;
   float a1 = tinyf, a2 = tinyf;
+  // the loads of all the thread's positions are issued before any is used
+  bool live[kSlotU];
+  float4 Pfu[kSlotU], Ofu[kSlotU];
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) {
+    const int s = span_pos(u);
+    live[u] = s < n_slots && d.state[s] == ST_LIVE;
+  }
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) {
+    const int s = span_pos(u);
+    Pfu[u] = live[u] ? d.posf[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    Ofu[u] = live[u] ? d.posf_old[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) {
   const int s = span_pos(u);
-  if (s < n_slots && d.state[s] == ST_LIVE) {
-    float4 Pf = d.posf[s], Of = d.posf_old[s];
+  if (live[u]) {
+    float4 Pf = Pfu[u], Of = Ofu[u];
     bool safe = Pf.x > e && Pf.x < R.boxf[0] - e && Pf.y > e && Pf.y < R.boxf[1] - e;
     if (safe && R.use_cells)
       safe = Pf.z > -2.0f * R.cellf[2] + e && Pf.z < R.tess_hif - e;
@@ -1425,11 +1439,29 @@ __device__ __forceinline__ void cell_order_cell(const Dev& d, int c) {
 
 // Cells of at most kSmallCell atoms are ordered by one thread each (a
 // sorting network in registers); larger ones are listed for a warp each.
+// A block covers one chunk of kCellChunk cells of one replica; chunks of
+// replicas that do not sort (and, for gcmc_run's sort, of z layers its
+// searches do not reach) are skipped whole.
 constexpr int kSmallCell = 16;
-__global__ void cell_order_small_kernel(Dev d, int ncell, int force) {
+__global__ void cell_order_small_kernel(Dev d, int force) {
   if (!force && !d.g->any_rebuild) return;
-  const int nt = gridDim.x * blockDim.x;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += nt) {
+  const int rep = d.cch_rep[blockIdx.x];
+  const RepConst& R = d.rc[rep];
+  if (!R.use_cells) return;
+  if (!force && !d.sc[rep].rebuild) return;
+  const int c0 = (blockIdx.x - R.cch0) * kCellChunk;
+  if (force && !R.gl_all) {
+    const int layer = R.head_dim[0] * R.head_dim[1];
+    const int l0 = c0 / layer, l1 = (min(c0 + kCellChunk, R.ncell) - 1) / layer;
+    const unsigned long long span =
+        (l1 - l0 >= 63 ? ~0ull : ((2ull << (l1 - l0)) - 1ull)) << l0;
+    if (l0 > 63 || !(R.gl_mask & span)) return;
+  }
+#pragma unroll 1
+  for (int u = 0; u < kCellChunk / kBlock; ++u) {
+    const int ci = c0 + u * kBlock + (int)threadIdx.x;
+    if (ci >= R.ncell) break;
+    const int c = R.cell_off + ci;
     const int num = d.cell_count[c];
     if (num == 0) continue;
     if (num > kSmallCell) {
@@ -4022,7 +4054,7 @@ int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, 
   if (d.any_cells) {
     cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 0);
     cell_scatter_kernel<<<nspan(n_b), kBlock, 0, s>>>(d, n_b, 0);
-    cell_order_small_kernel<<<kRowGrid, kBlock, 0, s>>>(d, d.ncell_tot, 0);
+    cell_order_small_kernel<<<d.n_cch > 0 ? d.n_cch : 1, kBlock, 0, s>>>(d, 0);
     cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 0);
     list_cells_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, n_rank);
     n += 5;
@@ -4101,7 +4133,7 @@ int k_gcmc_cells(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
   rebuild_prep_kernel<<<nspan(cap), kBlock, 0, s>>>(d, p, cap, cap, 1);
   cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1);
   cell_scatter_kernel<<<nspan(cap), kBlock, 0, s>>>(d, cap, 1);
-  cell_order_small_kernel<<<kRowGrid, kBlock, 0, s>>>(d, d.ncell_tot, 1);
+  cell_order_small_kernel<<<d.n_cch > 0 ? d.n_cch : 1, kBlock, 0, s>>>(d, 1);
   cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 1);
   return 5;
 }
