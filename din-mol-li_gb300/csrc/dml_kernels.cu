@@ -1832,22 +1832,42 @@ __global__ void overlap_count_kernel(Dev d, int n_rank) {
   for (int u = 0; u < kSlotU; ++u) overlap_count_at(d, n_rank, rep, span_pos(u));
 }
 
+// Component numbers and member ranges, one atomic per warp on each counter
+// (the components are independent, so their numbering is free).  Every
+// lane of the warp calls it.
 __device__ __forceinline__ void overlap_assign_at(Dev d, int n_slots, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
   const int s = pos;
-  if (s >= n_slots) return;
+  const int lane = threadIdx.x & 31;
   // component roots are hs%ref members (their sizes are reset each step;
   // an atom that left hs%ref keeps a stale one)
-  if (d.rank[s] < 0) return;
-  int sz = d.comp_size[s];
-  if (sz <= 0) return;
-  int cid = atomicAdd(&d.g->n_comp, 1);
-  int off = atomicAdd(&d.g->comp_total, sz);
-  d.comp_id[s] = cid;
-  d.comp_list[2 * cid] = off;
-  d.comp_list[2 * cid + 1] = sz;
+  int sz = 0;
+  if (s < n_slots && d.rank[s] >= 0) sz = d.comp_size[s];
+  const bool has = sz > 0;
+  const unsigned m = __ballot_sync(0xffffffffu, has);
+  if (!m) return;
+  int x = has ? sz : 0;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, x, 31);
+  const int leader = __ffs(m) - 1;
+  int bc = 0, bt = 0;
+  if (lane == leader) {
+    bc = atomicAdd(&d.g->n_comp, __popc(m));
+    bt = atomicAdd(&d.g->comp_total, total);
+  }
+  bc = __shfl_sync(0xffffffffu, bc, leader);
+  bt = __shfl_sync(0xffffffffu, bt, leader);
+  if (has) {
+    const int cid = bc + __popc(m & ((1u << lane) - 1u));
+    d.comp_id[s] = cid;
+    d.comp_list[2 * cid] = bt + x - sz;
+    d.comp_list[2 * cid + 1] = sz;
+  }
 }
 
 __global__ void overlap_assign_kernel(Dev d, int n_slots) {
@@ -3290,9 +3310,9 @@ struct GcmcSm {
   int pos2ins[kGcmcMaxTrials];  // insertion at gcmc%alist position ng0 + x
   // accepted deletions, in trial order
   int del_trial[kGcmcMaxTrials], del_pos[kGcmcMaxTrials], del_slot[kGcmcMaxTrials];
-  int del_bslot[kGcmcMaxTrials], del_reused[kGcmcMaxTrials];
-  int freed[kGcmcMaxTrials], freed_del[kGcmcMaxTrials];
-  unsigned char freed_used[kGcmcMaxTrials];
+  int del_bslot[kGcmcMaxTrials], del_reused[kGcmcMaxTrials], del_kins[kGcmcMaxTrials];
+  int freed[kGcmcMaxTrials], freed_del[kGcmcMaxTrials];  // min-heap of freed hs%b slots
+  double qc[2 * kGcmcMaxTrials + 1], qd[2 * kGcmcMaxTrials + 1];  // acceptance quotients
   int nins, ndel;
   // edits
   int href[kGcmcMaxTrials], hlast[kGcmcMaxTrials], href_ins[kGcmcMaxTrials];
@@ -3496,16 +3516,28 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
   }
   __syncthreads();
 
+  // Acceptance quotients for every control-volume count the call can reach
+  // (n0 - nadj .. n0 + nadj), the same expressions as the sequential search.
+  const int n0 = gr->n_in, qb = n0 - p.nadj;
+  {
+    const double v = R.box[0] * R.box[1] * (S.ss.zmax - S.ss.z0);
+    for (int t = tid; t <= 2 * p.nadj; t += nt) {
+      const int n = qb + t;
+      S.qc[t] = p.act * v / (double)(n + 1);  // creation (dana.F90:630)
+      S.qd[t] = (double)n / (v * p.act);      // destruction (dana.F90:683)
+    }
+  }
+  __syncthreads();
+
   // The trials in order (dana.F90:620-710), one warp, shared state only.
+  // hs%b slots, which no decision reads, are assigned afterwards.
   if (wid == 0) {
-    const double z0 = S.ss.z0, zmax = S.ss.zmax;
-    const double v = R.box[0] * R.box[1] * (zmax - z0);
-    int n = gr->n_in, first = gr->first, last = gr->last, ng = ng0;
-    int ns = S.ss.n_slots, nb = S.ss.n_b, n_atoms = S.ss.n_atoms, nlimbo = S.ss.nlimbo;
-    int b_nat = S.ss.b_nat, free_lo = S.ss.free_lo, bfree_lo = S.ss.bfree_lo;
+    int n = n0, first = gr->first, last = gr->last, ng = ng0;
+    int ns = S.ss.n_slots, n_atoms = S.ss.n_atoms, nlimbo = S.ss.nlimbo;
+    int free_lo = S.ss.free_lo;
     int n_alist = S.ss.n_alist, n_rank = S.ss.n_rank;
     long long next_id = S.ss.next_id;
-    int hi = 0, bhi = 0, nins = 0, ndel = 0;
+    int hi = 0, nins = 0, ndel = 0;
     int err = 0, err_info = 0;
     for (int i = 0; i < p.nadj; ++i) {
       __syncwarp();
@@ -3518,17 +3550,17 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
       const double uacc = S.uacc[i];
       if (S.crt[i]) {
         // creation attempt (dana.F90:627-677)
-        if (p.act * v / (double)(n + 1) < uacc) continue;
+        if (S.qc[n - qb] < uacc) continue;
+        // a blocker still in the group (its membership bit), or an earlier
+        // insertion of this call still in it
         bool ov = false;
         if (lane < S.nblk[i]) {
           const int bp = S.blk[i][lane];
-          bool gone = false;
-          for (int q = 0; q < ndel; ++q) gone |= S.del_pos[q] == bp;
-          ov = !gone;
+          ov = (wm[bp >> 5] >> (bp & 31)) & 1u;
         }
         if (lane < kGcmcMaskW && (S.pm[i][lane] & S.acc[lane]) != 0u) ov = true;
         if (__any_sync(0xffffffffu, ov)) continue;
-        // first free hs slot (limbo slots are not free) and hs%b slot
+        // first free hs slot (limbo slots are not free)
         int lslot;
         if (ns >= n_atoms + 1 + nlimbo) {
           if (hi >= S.nholes) {
@@ -3540,47 +3572,14 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
         } else {
           lslot = ns;
         }
-        int lbs;
-        if (nb >= b_nat + 1) {
-          const int co = bhi < S.nbholes ? S.bholes[bhi] : INT_MAX;
-          int fm = INT_MAX, fi = -1;
-          for (int q0 = 0; q0 < ndel; q0 += 32) {
-            const int q = q0 + lane;
-            const int val = q < ndel && !S.freed_used[q] ? S.freed[q] : INT_MAX;
-            const int mn = __reduce_min_sync(0xffffffffu, val);
-            if (mn < fm) {
-              fm = mn;
-              fi = q0 + __ffs(__ballot_sync(0xffffffffu, val == mn)) - 1;
-            }
-          }
-          if (co == INT_MAX && fm == INT_MAX) {
-            err = DML_E_INDEX;
-            err_info = t;
-            break;
-          }
-          if (co < fm) {
-            lbs = co;
-            ++bhi;
-          } else {
-            lbs = fm;
-            if (lane == 0) {
-              S.freed_used[fi] = 1;
-              S.del_reused[S.freed_del[fi]] = 1;
-            }
-          }
-        } else {
-          lbs = nb;
-        }
-        if (lslot >= R.cap || lbs >= R.cap || n_rank >= R.cap || n_alist >= R.cap || ng >= R.cap) {
+        if (lslot >= R.cap || n_rank >= R.cap || n_alist >= R.cap || ng >= R.cap) {
           err = DML_E_CAPACITY;
           err_info = t;
           break;
         }
-        const bool in = S.rin[i] != 0;
         if (lane == 0) {
           S.ins_trial[nins] = i;
           S.ins_slot[nins] = lslot;
-          S.ins_bslot[nins] = lbs;
           S.ins_fpos[nins] = first;
           S.ins_lpos[nins] = last;
           S.ins_gpos[nins] = ng;
@@ -3590,7 +3589,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
           S.ins_del[nins] = INT_MAX;
           S.pos2ins[ng - ng0] = nins;
           wm[ng >> 5] |= 1u << (ng & 31);
-          if (in) {
+          if (S.rin[i]) {
             wsl[ng >> 5] |= 1u << (ng & 31);
             grp[ng >> 10] += 1;
           }
@@ -3601,9 +3600,6 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
         ng += 1;
         n_alist += 1;
         n_rank += 1;
-        if (lbs == nb) nb += 1;
-        b_nat += 1;
-        bfree_lo = lbs + 1;
         if (lslot == ns) ns += 1;
         free_lo = lslot + 1;
         n_atoms += 1;
@@ -3611,7 +3607,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
         nins += 1;
       } else {
         // destruction attempt (dana.F90:680-707)
-        if ((double)n / (v * p.act) < uacc) continue;
+        if (S.qd[n - qb] < uacc) continue;
         int m = (int)floor(S.upick[i] * (double)n) + 1;
         if (m > n) m = n;
         // m <= 0: the walk never reaches m == 0 and ends on the last member
@@ -3621,30 +3617,12 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
           err_info = t;
           break;
         }
-        int h, bsl, kins = -1;
-        if (psel >= ng0) {
-          kins = S.pos2ins[psel - ng0];
-          h = B + S.ins_slot[kins];
-          bsl = S.ins_bslot[kins];
-        } else {
-          int hh = 0, bb = 0;
-          if (lane == 0) {
-            hh = d.gorder[B + psel];
-            bb = d.bslot[hh] - B;
-          }
-          h = __shfl_sync(0xffffffffu, hh, 0);
-          bsl = __shfl_sync(0xffffffffu, bb, 0);
-        }
+        const int kins = psel >= ng0 ? S.pos2ins[psel - ng0] : -1;
         const bool was_in = (wsl[psel >> 5] >> (psel & 31)) & 1u;
         if (lane == 0) {
           S.del_trial[ndel] = i;
           S.del_pos[ndel] = psel;
-          S.del_slot[ndel] = h;
-          S.del_bslot[ndel] = bsl;
-          S.del_reused[ndel] = 0;
-          S.freed[ndel] = bsl;
-          S.freed_del[ndel] = ndel;
-          S.freed_used[ndel] = 0;
+          S.del_kins[ndel] = kins;
           if (kins >= 0) {
             S.ins_del[kins] = i;
             const int ti = S.ins_trial[kins];
@@ -3657,8 +3635,6 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
           }
         }
         ndel += 1;
-        if (bsl < bfree_lo) bfree_lo = bsl;
-        b_nat -= 1;
         nlimbo += 1;
         n_atoms -= 1;
         n -= 1;
@@ -3674,12 +3650,9 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
       S.nins = nins;
       S.ndel = ndel;
       S.ss.n_slots = ns;
-      S.ss.n_b = nb;
       S.ss.n_atoms = n_atoms;
       S.ss.nlimbo = nlimbo;
-      S.ss.b_nat = b_nat;
       S.ss.free_lo = free_lo;
-      S.ss.bfree_lo = bfree_lo;
       S.ss.n_alist = n_alist;
       S.ss.n_rank = n_rank;
       S.ss.n_gorder = ng;
@@ -3693,6 +3666,97 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
   }
   __syncthreads();
   const int nins = S.nins, ndel = S.ndel;
+  // the deleted atoms' hs and hs%b slots
+  for (int q = tid; q < ndel; q += nt) {
+    const int kins = S.del_kins[q];
+    if (kins >= 0) {
+      S.del_slot[q] = B + S.ins_slot[kins];
+    } else {
+      const int h = d.gorder[B + S.del_pos[q]];
+      S.del_slot[q] = h;
+      S.del_bslot[q] = d.bslot[h] - B;
+    }
+  }
+  __syncthreads();
+  // hs%b slots (cgroup_attach_atom, Cells.F90:105-144, and igroup's first
+  // free slot) in trial order: an insertion takes the lower of the next
+  // original hole and the lowest slot freed by an earlier deletion of this
+  // call (a min-heap), or appends when there is no hole.
+  if (tid == 0) {
+    int nb = S.ss.n_b, b_nat = S.ss.b_nat, bfree_lo = S.ss.bfree_lo, bhi = 0, nh = 0;
+    int a = 0, b = 0;
+    bool bad = false;
+    while (a < nins || b < ndel) {
+      if (b >= ndel || (a < nins && S.ins_trial[a] < S.del_trial[b])) {
+        int lbs = -1;
+        if (nb >= b_nat + 1) {
+          const int co = bhi < S.nbholes ? S.bholes[bhi] : INT_MAX;
+          const int fm = nh > 0 ? S.freed[0] : INT_MAX;
+          if (co == INT_MAX && fm == INT_MAX) {
+            if (!bad) raise_error(d.g, DML_E_INDEX, S.ins_trial[a] + 1);
+            bad = true;
+          } else if (co < fm) {
+            lbs = co;
+            ++bhi;
+          } else {
+            lbs = fm;
+            S.del_reused[S.freed_del[0]] = 1;
+            // pop the heap root
+            --nh;
+            int vx = S.freed[nh], vd = S.freed_del[nh], x = 0;
+            for (;;) {
+              int c = 2 * x + 1;
+              if (c >= nh) break;
+              if (c + 1 < nh && S.freed[c + 1] < S.freed[c]) ++c;
+              if (S.freed[c] >= vx) break;
+              S.freed[x] = S.freed[c];
+              S.freed_del[x] = S.freed_del[c];
+              x = c;
+            }
+            S.freed[x] = vx;
+            S.freed_del[x] = vd;
+          }
+        } else {
+          lbs = nb;
+        }
+        if (lbs >= R.cap) {
+          if (!bad) raise_error(d.g, DML_E_CAPACITY, S.ins_trial[a] + 1);
+          bad = true;
+          lbs = -1;
+        }
+        S.ins_bslot[a] = lbs;
+        if (lbs >= 0) {
+          if (lbs == nb) nb += 1;
+          b_nat += 1;
+          bfree_lo = lbs + 1;
+        }
+        ++a;
+      } else {
+        const int kins = S.del_kins[b];
+        const int bsl = kins >= 0 ? S.ins_bslot[kins] : S.del_bslot[b];
+        S.del_bslot[b] = bsl;
+        S.del_reused[b] = 0;
+        if (bsl >= 0) {
+          // push on the heap
+          int x = nh++;
+          while (x > 0 && S.freed[(x - 1) / 2] > bsl) {
+            S.freed[x] = S.freed[(x - 1) / 2];
+            S.freed_del[x] = S.freed_del[(x - 1) / 2];
+            x = (x - 1) / 2;
+          }
+          S.freed[x] = bsl;
+          S.freed_del[x] = b;
+          if (bsl < bfree_lo) bfree_lo = bsl;
+          b_nat -= 1;
+        }
+        ++b;
+      }
+    }
+    S.ss.n_b = nb;
+    S.ss.b_nat = b_nat;
+    S.ss.bfree_lo = bfree_lo;
+  }
+  __syncthreads();
 
   // Templates (the first member) and Maxwell targets (the last member) of
   // the insertions, as hs slots; pre-call values of the pre-call atoms.
@@ -3801,8 +3865,8 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
     d.rank[slot] = B + S.ins_rank[k];
     // an atom deleted later in this call leaves its hs%b slot to the
     // insertion that reuses it, or to the deletion that empties it
-    if (S.ins_del[k] == INT_MAX) d.b2hs[bs] = slot;
-    d.bslot[slot] = bs;
+    if (S.ins_del[k] == INT_MAX && S.ins_bslot[k] >= 0) d.b2hs[bs] = slot;
+    d.bslot[slot] = S.ins_bslot[k] >= 0 ? bs : -1;
     d.state[slot] = ST_LIVE;
     d.gorder[B + S.ins_gpos[k]] = slot;
     d.gpos[slot] = B + S.ins_gpos[k];
@@ -3825,7 +3889,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
       d.rank[h] = -1;
       atomicSub(&S.ss.n_ref, 1);
     }
-    if (!S.del_reused[q]) d.b2hs[B + S.del_bslot[q]] = -1;
+    if (!S.del_reused[q] && S.del_bslot[q] >= 0) d.b2hs[B + S.del_bslot[q]] = -1;
     d.bslot[h] = -1;
     d.state[h] = ST_LIMBO;
     d.posf[h] = make_float4(pf.x, pf.y, pf.z, __int_as_float(0));
@@ -4145,7 +4209,7 @@ int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
 int k_gcmc_trials(const Dev& d, const KParams& p, cudaStream_t s) {
   int n = 0;
   // the parallel path: shared state, in-slab counts and (if they fit) the bit words
-  static_assert(sizeof(GcmcSm) <= 96 * 1024, "gcmc_fast_kernel shared state");
+  static_assert(sizeof(GcmcSm) <= 100 * 1024, "gcmc_fast_kernel shared state");
   const int wmax = d.max_rep_cap / 32, gmax = (wmax + 31) / 32 + 1;
   size_t fshm = sizeof(GcmcSm) + sizeof(int) * (size_t)gmax;
   const int words_smem = fshm + 2 * sizeof(unsigned) * (size_t)wmax <= 200 * 1024;
