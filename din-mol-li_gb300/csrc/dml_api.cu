@@ -125,6 +125,17 @@ void make_repconst(const dml_params& P, const dml_replica& r, RepConst& R) {
     if (lo <= hi && __builtin_popcountll(m) < nz) {
       R.gl_all = 0;
       R.gl_mask = m;
+      // z is not periodic: a layer wrapped into a stencil from the far end of
+      // the box lies farther than rc + skin in z from every trial point, so
+      // none of its atoms can be a blocker or a list atom.  Its cells are
+      // scanned (and read) empty; only the layers within reach are counted.
+      const double reach = P.rc + P.skin + 1.0;
+      unsigned long long cm = 0;
+      for (int L = 1; L <= nz; ++L)
+        if (((m >> L) & 1ull) && (double)L * R.cell[2] >= r.z0 - reach &&
+            (double)(L - 1) * R.cell[2] <= r.zmax + reach)
+          cm |= 1ull << L;
+      R.gl_cmask = cm;
     }
   }
 }
@@ -678,6 +689,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.comp_fill, cap);
   AL(d.comp_members, cap);
   AL(d.comp_list, 2 * (size_t)cap);
+  AL(d.act_list, cap);
   d.nblk_part = cap / kBlock + 1;
   AL(d.part, 2 * (size_t)d.nblk_part);
   AL(d.sc, nrep);

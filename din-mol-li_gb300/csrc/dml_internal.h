@@ -63,6 +63,7 @@ struct RepConst {
   // z layers of cells that gcmc_run's searches reach (bit c3, 1 <=
   // ncells[2]); gl_all: every layer (its cell sort then covers them all)
   unsigned long long gl_mask;
+  unsigned long long gl_cmask;  // of those, the layers whose atoms can be within reach in z
   int gl_all;
 };
 
@@ -115,6 +116,7 @@ struct Global {
   long long list_builds;    // rebuild kernels run (some replica rebuilt)
   int near_stale;           // near lists must be searched in the overlap phase
   int n_big;                // entries of big_cells
+  int n_act;                // entries of act_list
 };
 
 struct EvRec {            // one interacting list entry seen from one atom
@@ -237,6 +239,7 @@ struct Dev {
   int *ins_head, *ins_next;  // atoms inserted at cell-chain heads during gcmc_run
   // overlap
   int *near_count, *near, *uf, *comp_size, *comp_id, *comp_rank, *comp_fill, *comp_members, *comp_list;
+  int* act_list;      // ranks of the hs%ref members with a near contact this step
   // reductions
   unsigned long long* part;  // per-block partials (top-2, as double bits)
   int nblk_part;

@@ -223,6 +223,7 @@ __global__ void step_begin_kernel(Dev d, int near_stale) {
     g->again = 0;
     g->n_comp = 0;
     g->comp_total = 0;
+    g->n_act = 0;
     g->passes = 1;
   }
   for (int r = threadIdx.x; r < d.nrep; r += blockDim.x) {
@@ -1312,8 +1313,8 @@ __device__ __forceinline__ void rebuild_prep_at(Dev d, KParams p, int n_slots, i
     if (c1 == 0 || c2 == 0 || c3 == 0 || c1 > R.ncells[0] || c2 > R.ncells[1] ||
         c3 > R.ncells[2])
       sc->halo = 1;
-    // the sort for gcmc_run covers only the layers its searches reach
-    if (cells_only && !R.gl_all && !((R.gl_mask >> c3) & 1ull)) {
+    // the sort for gcmc_run holds only the atoms its searches can reach
+    if (cells_only && !R.gl_all && !((R.gl_cmask >> c3) & 1ull)) {
       d.cell_of[s] = -1;
       return;
     }
@@ -1696,6 +1697,7 @@ __device__ __forceinline__ void overlap_init_at(Dev d, KParams p, int n_slots, i
     d.g->again = 0;
     d.g->n_comp = 0;
     d.g->comp_total = 0;
+    d.g->n_act = 0;
     d.g->passes = 1;
   }
   if (s == R.base) {
@@ -1811,16 +1813,28 @@ __global__ void __launch_bounds__(256) overlap_detect_kernel(Dev d, KParams p, i
 }
 
 // Atoms with no near entry are examined trivially in pass 1 (skip = true)
-// and can never be moved; the others are counted per component root.
+// and can never be moved; the others are counted per component root and
+// listed (act_list) for the component passes.  Every lane calls it.
 __device__ __forceinline__ void overlap_count_at(Dev d, int n_rank, int rep, int pos) {
   const int r = pos;
-  if (r - d.rc[rep].base >= d.sc[rep].n_rank) return;
-  int h = d.ref[r];
-  if (h < 0) return;
-  if (!d.active[h]) {
-    d.skip[h] = 1;
-    return;
+  const int lane = threadIdx.x & 31;
+  int h = -1;
+  bool act = false;
+  if (r - d.rc[rep].base < d.sc[rep].n_rank) {
+    h = d.ref[r];
+    if (h >= 0) {
+      if (d.active[h]) act = true;
+      else d.skip[h] = 1;
+    }
   }
+  const unsigned m = __ballot_sync(0xffffffffu, act);
+  if (!m) return;
+  const int leader = __ffs(m) - 1;
+  int b = 0;
+  if (lane == leader) b = atomicAdd(&d.g->n_act, __popc(m));
+  b = __shfl_sync(0xffffffffu, b, leader);
+  if (!act) return;
+  d.act_list[b + __popc(m & ((1u << lane) - 1u))] = r;
   int root = uf_find((volatile int*)d.uf, h);
   d.uf[h] = root;
   atomicAdd(&d.comp_size[root], 1);
@@ -1832,91 +1846,72 @@ __global__ void overlap_count_kernel(Dev d, int n_rank) {
   for (int u = 0; u < kSlotU; ++u) overlap_count_at(d, n_rank, rep, span_pos(u));
 }
 
-// Component numbers and member ranges, one atomic per warp on each counter
-// (the components are independent, so their numbering is free).  Every
-// lane of the warp calls it.
-__device__ __forceinline__ void overlap_assign_at(Dev d, int n_slots, int rep, int pos) {
-  const RepConst& R = d.rc[rep];
-  Scalars* sc = d.sc + rep;
-  n_slots = R.base + sc->n_slots;  // positions in use end here
-  const int s = pos;
+// Component numbers and member ranges for the roots among the listed
+// members, one atomic per warp on each counter (the components are
+// independent, so their numbering is free).
+__global__ void overlap_assign_kernel(Dev d) {
+  const int n = d.g->n_act;
   const int lane = threadIdx.x & 31;
-  // component roots are hs%ref members (their sizes are reset each step;
-  // an atom that left hs%ref keeps a stale one)
-  int sz = 0;
-  if (s < n_slots && d.rank[s] >= 0) sz = d.comp_size[s];
-  const bool has = sz > 0;
-  const unsigned m = __ballot_sync(0xffffffffu, has);
-  if (!m) return;
-  int x = has ? sz : 0;
-  for (int o = 1; o < 32; o <<= 1) {
-    const int y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  const int total = __shfl_sync(0xffffffffu, x, 31);
-  const int leader = __ffs(m) - 1;
-  int bc = 0, bt = 0;
-  if (lane == leader) {
-    bc = atomicAdd(&d.g->n_comp, __popc(m));
-    bt = atomicAdd(&d.g->comp_total, total);
-  }
-  bc = __shfl_sync(0xffffffffu, bc, leader);
-  bt = __shfl_sync(0xffffffffu, bt, leader);
-  if (has) {
-    const int cid = bc + __popc(m & ((1u << lane) - 1u));
-    d.comp_id[s] = cid;
-    d.comp_list[2 * cid] = bt + x - sz;
-    d.comp_list[2 * cid + 1] = sz;
+  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    int h = -1, sz = 0;
+    if (i < n) {
+      h = d.ref[d.act_list[i]];
+      if (d.uf[h] == h) sz = d.comp_size[h];
+    }
+    const bool has = sz > 0;
+    const unsigned m = __ballot_sync(0xffffffffu, has);
+    if (!m) continue;
+    int x = has ? sz : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, x, 31);
+    const int leader = __ffs(m) - 1;
+    int bc = 0, bt = 0;
+    if (lane == leader) {
+      bc = atomicAdd(&d.g->n_comp, __popc(m));
+      bt = atomicAdd(&d.g->comp_total, total);
+    }
+    bc = __shfl_sync(0xffffffffu, bc, leader);
+    bt = __shfl_sync(0xffffffffu, bt, leader);
+    if (has) {
+      const int cid = bc + __popc(m & ((1u << lane) - 1u));
+      d.comp_id[h] = cid;
+      d.comp_list[2 * cid] = bt + x - sz;
+      d.comp_list[2 * cid + 1] = sz;
+    }
   }
 }
 
-__global__ void overlap_assign_kernel(Dev d, int n_slots) {
-  const int rep = block_rep(d);
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) overlap_assign_at(d, n_slots, rep, span_pos(u));
-}
-
-__device__ __forceinline__ void overlap_scatter_at(Dev d, int n_rank, int rep, int pos) {
-  const RepConst& R = d.rc[rep];
-  Scalars* sc = d.sc + rep;
-  const int r = pos;
-  if (r - R.base >= sc->n_rank) return;
-  int h = d.ref[r];
-  if (h < 0 || !d.active[h]) return;
-  int root = d.uf[h];
-  int cid = d.comp_id[root];
-  int idx = d.comp_list[2 * cid] + atomicAdd(&d.comp_fill[root], 1);
-  d.comp_rank[idx] = r;  // the component's ranks, in no particular order
-}
-
-__global__ void overlap_scatter_kernel(Dev d, int n_rank) {
-  const int rep = block_rep(d);
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) overlap_scatter_at(d, n_rank, rep, span_pos(u));
+__global__ void overlap_scatter_kernel(Dev d) {
+  const int n = d.g->n_act;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int r = d.act_list[i];
+    const int h = d.ref[r];
+    const int root = d.uf[h];
+    const int cid = d.comp_id[root];
+    const int idx = d.comp_list[2 * cid] + atomicAdd(&d.comp_fill[root], 1);
+    d.comp_rank[idx] = r;  // the component's ranks, in no particular order
+  }
 }
 
 // Members of every component in rank order: each member's place is the
 // number of smaller ranks in its component (contiguous loads, all members
 // in parallel).
-__device__ __forceinline__ void overlap_order_at(Dev d, int n_rank, int rep, int pos) {
-  const RepConst& R = d.rc[rep];
-  Scalars* sc = d.sc + rep;
-  const int r = pos;
-  if (r - R.base >= sc->n_rank) return;
-  int h = d.ref[r];
-  if (h < 0 || !d.active[h]) return;
-  int cid = d.comp_id[d.uf[h]];
-  int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
-  const int* rk = d.comp_rank + off;
-  int before = 0;
-  for (int i = 0; i < sz; ++i) before += rk[i] < r;
-  d.comp_members[off + before] = h;
-}
-
-__global__ void overlap_order_kernel(Dev d, int n_rank) {
-  const int rep = block_rep(d);
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) overlap_order_at(d, n_rank, rep, span_pos(u));
+__global__ void overlap_order_kernel(Dev d) {
+  const int n = d.g->n_act;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int r = d.act_list[i];
+    const int h = d.ref[r];
+    const int cid = d.comp_id[d.uf[h]];
+    const int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
+    const int* rk = d.comp_rank + off;
+    int before = 0;
+    for (int q = 0; q < sz; ++q) before += rk[q] < r;
+    d.comp_members[off + before] = h;
+  }
 }
 
 // Examination of o1 = x in pass `pass` (dana.F90:871-935).
@@ -4164,9 +4159,9 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
   }
   if (detect) n += k_overlap_detect(d, p, n_rank, detect == 1 ? 1 : 0, s);
   overlap_count_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
-  overlap_assign_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, n_slots);
-  overlap_scatter_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
-  overlap_order_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
+  overlap_assign_kernel<<<152 * 4, kBlock, 0, s>>>(d);
+  overlap_scatter_kernel<<<152 * 4, kBlock, 0, s>>>(d);
+  overlap_order_kernel<<<152 * 4, kBlock, 0, s>>>(d);
   int all_passes = p.prob >= 1.0;
   overlap_pass1_kernel<<<nblk(n_rank, 128), 128, 0, s>>>(d, p, all_passes);
   n += 5;
