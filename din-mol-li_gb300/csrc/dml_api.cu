@@ -647,7 +647,8 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.force, cap);
   AL(d.old_cg, cap);
   AL(d.pos_old, cap);
-  AL(d.ranv, cap);
+  AL(d.ranv, c->P.precision == DML_PRECISION_MIXED ? 1 : (size_t)cap);
+  AL(d.ranvf, c->P.precision == DML_PRECISION_MIXED ? (size_t)cap : 1);
   AL(d.posf, cap);
   AL(d.posf_old, cap);
   AL(d.epot, cap);
@@ -748,9 +749,11 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
       pos[h] = v3(a->pos, 0.0);
       vel[h] = v3(a->vel, 0.0);
       acel[h] = v3(a->acel, 0.0);
-      if (c->K.mixed) {  // FP32 velocity side (chosen form)
-        vel[h] = pack_f3((float)vel[h].x, (float)vel[h].y, (float)vel[h].z);
-        acel[h] = pack_f3((float)acel[h].x, (float)acel[h].y, (float)acel[h].z);
+      if (c->K.mixed) {  // FP32 velocity and acceleration in one slot (chosen form)
+        const double4 v = pack_f3((float)vel[h].x, (float)vel[h].y, (float)vel[h].z);
+        const double4 a = pack_f3((float)acel[h].x, (float)acel[h].y, (float)acel[h].z);
+        vel[h] = make_double4(v.x, v.y, a.x, a.y);
+        acel[h] = make_double4(0.0, 0.0, 0.0, 0.0);
       }
       force[h] = v3(a->force, 0.0);
       pos_old[h] = a->pos_old ? v3(a->pos_old, 0.0) : pos[h];
@@ -1161,7 +1164,8 @@ int dml_get_atoms_replica(dml_ctx* c, int32_t rep, dml_atoms* a) {
     };
     put(a->pos, pos[h]);
     if (c->K.mixed) {
-      const float4 v = unpack_f3(vel[h]), ac = unpack_f3(acel[h]);
+      const float4 v = unpack_f3(vel[h]);
+      const float4 ac = unpack_f3(make_double4(vel[h].z, vel[h].w, 0.0, 0.0));
       put(a->vel, make_double4(v.x, v.y, v.z, 0.0));
       put(a->acel, make_double4(ac.x, ac.y, ac.z, 0.0));
     } else {

@@ -165,9 +165,11 @@ struct KParams {
   float fac_scf, fac_seif, inv_hf;
 };
 
-// Chosen form: velocities, accelerations and the Ermak velocity noise are
-// FP32, kept as a float4 (x, y, z, 0) in the first 16 bytes of their double4
-// slot, so the arrays and their copies are the same in both forms.
+// Chosen form: velocities and accelerations are FP32, both in the `vel`
+// slot of the atom (velocity in its first 16 bytes, acceleration in its last
+// 16, each a float4 (x, y, z, 0)), so ermak_a reads and ermak_b writes one
+// 32-byte sector; copies and zeroing of the slot work as in the plain form.
+// The Ermak velocity noise is a float4 array of its own (ranvf).
 __host__ __device__ inline double4 pack_f3(float x, float y, float z) {
   double4 r = {0.0, 0.0, 0.0, 0.0};
   float f[4] = {x, y, z, 0.0f};
@@ -217,6 +219,7 @@ struct GcmcRepPre {
 // All device buffers of one context.
 struct Dev {
   double4 *pos, *vel, *acel, *force, *old_cg, *pos_old, *ranv;
+  float4* ranvf;      // chosen form: FP32 Ermak velocity noise
   float4 *posf, *posf_old;
   double* epot;
   int8_t *typ, *skip, *state, *active;

@@ -299,12 +299,21 @@ __device__ __forceinline__ bool atom_pbc_dev(const KParams& p, const RepConst& R
   return depos;
 }
 
-// FP32 velocity-side values of the chosen form in their double4 slots.
-__device__ __forceinline__ float4 ldv(const double4* a, int h) {
-  return *reinterpret_cast<const float4*>(a + h);
+// The chosen form's FP32 velocity (first half) and acceleration (second
+// half) of an atom's vel slot.
+__device__ __forceinline__ void ldva(const double4* vel, int h, float4& v, float4& a) {
+  const float4* q = reinterpret_cast<const float4*>(vel + h);
+  v = q[0];
+  a = q[1];
 }
-__device__ __forceinline__ void stv(double4* a, int h, float x, float y, float z) {
-  *reinterpret_cast<float4*>(a + h) = make_float4(x, y, z, 0.0f);
+__device__ __forceinline__ void stv(double4* vel, int h, float x, float y, float z) {
+  *reinterpret_cast<float4*>(vel + h) = make_float4(x, y, z, 0.0f);
+}
+__device__ __forceinline__ void stva(double4* vel, int h, float vx, float vy, float vz, float ax,
+                                     float ay, float az) {
+  float4* q = reinterpret_cast<float4*>(vel + h);
+  q[0] = make_float4(vx, vy, vz, 0.0f);
+  q[1] = make_float4(ax, ay, az, 0.0f);
 }
 
 // No atom_pbc action (wrap, mirror at zmax, capture at z <= 0) can apply to
@@ -325,7 +334,8 @@ __device__ __forceinline__ void ermak_a_mixed_atom(const Dev& d, const KParams& 
                                                    const RepConst& R, Scalars* sc, int h,
                                                    long long step, double zmax) {
   const double4 P = d.pos[h];
-  const float4 V = ldv(d.vel, h), A = ldv(d.acel, h);
+  float4 V, A;
+  ldva(d.vel, h, V, A);
   int typ = d.typ[h];
   const long long id = d.id[h];
   const float rf = p.rfacf[typ - 1], vf = p.vfacf[typ - 1];
@@ -356,7 +366,7 @@ __device__ __forceinline__ void ermak_a_mixed_atom(const Dev& d, const KParams& 
   d.old_cg[h] = P;
   d.pos[h] = make_double4(pp[0], pp[1], pp[2], 0.0);
   d.posf[h] = after;
-  stv(d.ranv, h, rv[0], rv[1], rv[2]);
+  d.ranvf[h] = make_float4(rv[0], rv[1], rv[2], 0.0f);
   overlap_prepare_atom(d, R, h, before, after);
   if (po_changed) {
     d.pos_old[h] = po;
@@ -743,12 +753,13 @@ __device__ __forceinline__ void ermak_b_atom_mixed(const Dev& d, const KParams& 
                                                    float fx, float fy, float fz) {
   if (typ == DML_Z_CG) return;
   const float im = p.inv_massf[typ - 1];
-  const float4 V = ldv(d.vel, h), A = ldv(d.acel, h), R = ldv(d.ranv, h);
+  float4 V, A;
+  ldva(d.vel, h, V, A);
+  const float4 R = d.ranvf[h];
   const float ax = fx * im, ay = fy * im, az = fz * im;
-  stv(d.vel, h, p.cc0f * V.x + p.cc1mcc2f * A.x + p.cc2f * ax + R.x,
-      p.cc0f * V.y + p.cc1mcc2f * A.y + p.cc2f * ay + R.y,
-      p.cc0f * V.z + p.cc1mcc2f * A.z + p.cc2f * az + R.z);
-  stv(d.acel, h, ax, ay, az);
+  stva(d.vel, h, p.cc0f * V.x + p.cc1mcc2f * A.x + p.cc2f * ax + R.x,
+       p.cc0f * V.y + p.cc1mcc2f * A.y + p.cc2f * ay + R.y,
+       p.cc0f * V.z + p.cc1mcc2f * A.z + p.cc2f * az + R.z, ax, ay, az);
 }
 
 // Pass 2: one thread per hs slot sums its recorded entries in key order,
@@ -2658,9 +2669,10 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
         const double beta = p.beta_t[typ - 1];
         double nv[4];
         dml_normal_quad(dml_draw(R.seed, step, (uint64_t)t, DML_RNG_GCMC_VEL, 0), nv);
-        d.vel[hlast] = p.mixed ? pack_f3((float)(beta * nv[0]), (float)(beta * nv[1]),
-                                         (float)(beta * nv[2]))
-                               : make_double4(beta * nv[0], beta * nv[1], beta * nv[2], 0.0);
+        if (p.mixed)
+          stv(d.vel, hlast, (float)(beta * nv[0]), (float)(beta * nv[1]), (float)(beta * nv[2]));
+        else
+          d.vel[hlast] = make_double4(beta * nv[0], beta * nv[1], beta * nv[2], 0.0);
         // sys
         int ap = sc->n_alist;
         d.alist[B + ap] = slot;
@@ -3777,8 +3789,9 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
     S.hlast[k] = hl;
     S.hlast_ins[k] = hli;
     if (hri < 0) {
+      // the velocity (chosen form: the first half of the slot, two doubles)
       const double4 v0 = d.vel[hr];
-      S.tvel[k] = Vel3{v0.x, v0.y, v0.z};
+      S.tvel[k] = Vel3{v0.x, v0.y, p.mixed ? 0.0 : v0.z};
       S.htyp[k] = d.typ[hr];
     }
     const GcmcTrialPre& tr = pre[S.ins_trial[k]];
@@ -3814,9 +3827,9 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
       const double beta = p.beta_t[typ - 1];
       const float4 nv = S.nv[k];
       Vel3 mv = Vel3{beta * (double)nv.x, beta * (double)nv.y, beta * (double)nv.z};
-      if (p.mixed) {  // the slot holds FP32 values (chosen form)
+      if (p.mixed) {  // the velocity half of the slot holds FP32 values (chosen form)
         const double4 pk = pack_f3((float)mv.x, (float)mv.y, (float)mv.z);
-        mv = Vel3{pk.x, pk.y, pk.z};
+        mv = Vel3{pk.x, pk.y, 0.0};
       }
       const int hli = S.hlast_ins[k];
       if (hli >= 0) {
@@ -3841,7 +3854,12 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
     const double4 tf = d.force[root], ta = d.acel[root];
     const double te = d.epot[root];
     const double4 Rt = pre[S.ins_trial[k]].r;
-    d.vel[slot] = make_double4(S.fvel[k].x, S.fvel[k].y, S.fvel[k].z, 0.0);
+    if (p.mixed) {  // velocity resolved above, acceleration of the template
+      const double4 tva = d.vel[root];
+      d.vel[slot] = make_double4(S.fvel[k].x, S.fvel[k].y, tva.z, tva.w);
+    } else {
+      d.vel[slot] = make_double4(S.fvel[k].x, S.fvel[k].y, S.fvel[k].z, 0.0);
+    }
     d.force[slot] = tf;
     d.acel[slot] = ta;
     d.epot[slot] = te;
@@ -3867,8 +3885,12 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
     d.gpos[slot] = B + S.ins_gpos[k];
     d.in_gcmc[slot] = 1;
   }
-  for (int q = tid; q < S.n_mw; q += nt)
-    d.vel[S.mw_slot[q]] = make_double4(S.mw_vel[q].x, S.mw_vel[q].y, S.mw_vel[q].z, 0.0);
+  for (int q = tid; q < S.n_mw; q += nt) {
+    if (p.mixed)  // the velocity half only
+      *reinterpret_cast<double2*>(d.vel + S.mw_slot[q]) = make_double2(S.mw_vel[q].x, S.mw_vel[q].y);
+    else
+      d.vel[S.mw_slot[q]] = make_double4(S.mw_vel[q].x, S.mw_vel[q].y, S.mw_vel[q].z, 0.0);
+  }
   __syncthreads();
   // the deleted atoms (atom_destroy: gcmc, hs (nn, hs%ref, hs%b), sys,
   // Groups.F90:433-467); a freed hs%b slot that a later insertion took keeps it
