@@ -31,6 +31,7 @@ constexpr int kBlock = 256;
 constexpr int kSlotU = 4;                 // positions per thread of the per-position kernels
 constexpr int kSpan = kBlock * kSlotU;    // positions per block; replica capacities are multiples
 constexpr int kCellChunk = kBlock * 4;    // cells per block of the per-cell kernels
+constexpr int kCntStride = 32, kCntGlist = 0, kCntAct = 1;  // pr_cnt layout
 
 // Replicas.  A context holds one or more independent systems ("replicas",
 // the batched form); a single system is a batch of one.  Replica r owns the
@@ -116,7 +117,6 @@ struct Global {
   long long list_builds;    // rebuild kernels run (some replica rebuilt)
   int near_stale;           // near lists must be searched in the overlap phase
   int n_big;                // entries of big_cells
-  int n_act;                // entries of act_list
 };
 
 struct EvRec {            // one interacting list entry seen from one atom
@@ -242,7 +242,12 @@ struct Dev {
   int *ins_head, *ins_next;  // atoms inserted at cell-chain heads during gcmc_run
   // overlap
   int *near_count, *near, *uf, *comp_size, *comp_id, *comp_rank, *comp_fill, *comp_members, *comp_list;
-  int* act_list;      // ranks of the hs%ref members with a near contact this step
+  int* act_list;      // ranks of the hs%ref members with a near contact this step, replica
+                      // r's at [base, base + pr_cnt[r * kCntStride + kCntAct])
+  int2* glist;        // gcmc_run's cell sort: (hs%b slot, cell) of the atoms within reach,
+                      // replica r's entries at [base, base + pr_cnt[r * kCntStride + kCntGlist])
+  int* pr_cnt;        // per-replica list counters, one 128-byte line per replica (kept
+                      // apart from the replica scalars that every block reads)
   // reductions
   unsigned long long* part;  // per-block partials (top-2, as double bits)
   int nblk_part;

@@ -223,12 +223,12 @@ __global__ void step_begin_kernel(Dev d, int near_stale) {
     g->again = 0;
     g->n_comp = 0;
     g->comp_total = 0;
-    g->n_act = 0;
     g->passes = 1;
   }
   for (int r = threadIdx.x; r < d.nrep; r += blockDim.x) {
     d.sc[r].passes = 1;
     d.sc[r].again2 = 0;
+    d.pr_cnt[r * kCntStride + kCntAct] = 0;
   }
 }
 
@@ -377,7 +377,9 @@ __device__ __forceinline__ void ermak_a_mixed_atom(const Dev& d, const KParams& 
   if (!depos) d.skip[h] = 0;
 }
 
-// ermak_a (dana.F90:974-1028): one thread per hs%ref member.
+// ermak_a (dana.F90:974-1028): one thread per hs%ref member; one kernel
+// per form, so that each gets only the registers its own path needs.
+template <bool MIXED>
 __device__ __forceinline__ void ermak_a_at(Dev d, KParams p, int n_rank, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
@@ -387,7 +389,7 @@ __device__ __forceinline__ void ermak_a_at(Dev d, KParams p, int n_rank, int rep
   if (h < 0) return;
   long long step = d.g->step;
   double zmax = sc->zmax;
-  if (p.mixed) {
+  if (MIXED) {
     ermak_a_mixed_atom(d, p, R, sc, h, step, zmax);
     return;
   }
@@ -431,13 +433,16 @@ __device__ __forceinline__ void ermak_a_at(Dev d, KParams p, int n_rank, int rep
   if (!depos) d.skip[h] = 0;
 }
 
-__global__ void ermak_a_kernel(Dev d, KParams p, int n_rank) {
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlock, 4) ermak_a_kernel(Dev d, KParams p, int n_rank) {
   const int rep = block_rep(d);
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) ermak_a_at(d, p, n_rank, rep, span_pos(u));
+#pragma unroll 1
+  for (int u = 0; u < kSlotU; ++u) ermak_a_at<MIXED>(d, p, n_rank, rep, span_pos(u));
 }
 
-// cbrownian_hs (dana.F90:798-846): one thread per hs%ref member.
+// cbrownian_hs (dana.F90:798-846): one thread per hs%ref member; one kernel
+// per form.
+template <bool MIXED>
 __device__ __forceinline__ void brownian_at(Dev d, KParams p, int n_rank, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
@@ -450,7 +455,7 @@ __device__ __forceinline__ void brownian_at(Dev d, KParams p, int n_rank, int re
   double4 P = d.pos[h];
   int typ = d.typ[h];
   long long id = d.id[h];
-  if (p.mixed) {
+  if (MIXED) {
     // chosen form: FP32 increments added to the FP64 position, FP32 velocity
     const float facf = P.z > p.dif_switch_z ? p.fac_scf : p.fac_seif;
     float nf[4];
@@ -518,10 +523,11 @@ __device__ __forceinline__ void brownian_at(Dev d, KParams p, int n_rank, int re
   if (!depos) d.skip[h] = 0;
 }
 
-__global__ void brownian_kernel(Dev d, KParams p, int n_rank) {
+template <bool MIXED>
+__global__ void __launch_bounds__(kBlock, 4) brownian_kernel(Dev d, KParams p, int n_rank) {
   const int rep = block_rep(d);
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) brownian_at(d, p, n_rank, rep, span_pos(u));
+#pragma unroll 1
+  for (int u = 0; u < kSlotU; ++u) brownian_at<MIXED>(d, p, n_rank, rep, span_pos(u));
 }
 
 // Union-find over hs slots (overlap components): path halving, union by
@@ -1424,6 +1430,64 @@ __global__ void cell_scatter_kernel(Dev d, int n_b, int force) {
   for (int u = 0; u < kSlotU; ++u) cell_scatter_at(d, n_b, force, rep, span_pos(u));
 }
 
+// gcmc_run's cell sort, binning pass: every live atom's cell (coalesced
+// over hs slots, so no gather), the range check and the halo flag of
+// cgroup_sort_atom (Cells.F90:281-302) for all, the count and a list entry
+// (hs%b slot, cell) for the atoms of the z layers the trials can reach.
+__device__ __forceinline__ void gcmc_bin_at(const Dev& d, int rep, int pos) {
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  const int s = pos;
+  const int lane = threadIdx.x & 31;
+  int lin = -1;
+  if (R.use_cells && s < R.base + sc->n_slots && d.state[s] == ST_LIVE) {
+    int c1, c2, c3;
+    cell_index3(R, d.posf[s], d.pos + s, c1, c2, c3);
+    if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] + 1 || c2 > R.ncells[1] + 1 ||
+        c3 > R.ncells[2] + 1) {
+      raise_error(d.g, DML_E_OUT_OF_TESSELLATION, s);
+    } else {
+      // the 27-cell stencil never visits the halo: trials fall back to full scans
+      if (c1 == 0 || c2 == 0 || c3 == 0 || c1 > R.ncells[0] || c2 > R.ncells[1] ||
+          c3 > R.ncells[2])
+        sc->halo = 1;
+      if (R.gl_all || ((R.gl_cmask >> c3) & 1ull))
+        lin = R.cell_off + (c3 * R.head_dim[1] + c2) * R.head_dim[0] + c1;
+    }
+  }
+  const bool in = lin >= 0;
+  const unsigned m = __ballot_sync(0xffffffffu, in);
+  if (!m) return;
+  const int leader = __ffs(m) - 1;
+  int b = 0;
+  if (lane == leader) b = atomicAdd(d.pr_cnt + rep * kCntStride + kCntGlist, __popc(m));
+  b = __shfl_sync(0xffffffffu, b, leader);
+  if (!in) return;
+  atomicAdd(&d.cell_count[lin], 1);
+  d.glist[R.base + b + __popc(m & ((1u << lane) - 1u))] = make_int2(d.bslot[s], lin);
+}
+
+__global__ void gcmc_bin_kernel(Dev d) {
+  const int rep = block_rep(d);
+  if (blockIdx.x == 0 && threadIdx.x == 0) d.g->n_big = 0;  // cell_order's list
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) gcmc_bin_at(d, rep, span_pos(u));
+}
+
+// gcmc_run's cell sort, scatter pass over each replica's listed atoms.
+__global__ void gcmc_scatter_kernel(Dev d) {
+  const int rep = block_rep(d);
+  const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntGlist];
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) {
+    const int i = span_pos(u);
+    if (i < end) {
+      const int2 e = d.glist[i];
+      d.cell_atoms[d.cell_start[e.y] + atomicAdd(&d.cell_fill[e.y], 1)] = e.x;
+    }
+  }
+}
+
 // Orders each cell by descending hs%b slot: the chain order of
 // cgroup_sort (Cells.F90:267-302), which prepends slots in increasing order.
 // One warp per cell; the sorted cell goes to comp_members (scratch) and is
@@ -1460,6 +1524,8 @@ __global__ void cell_order_small_kernel(Dev d, int force) {
   const int rep = d.cch_rep[blockIdx.x];
   const RepConst& R = d.rc[rep];
   if (!R.use_cells) return;
+  // the gcmc_run sort's list has been scattered: empty it for the next sort
+  if (force && blockIdx.x == R.cch0 && threadIdx.x == 0) d.pr_cnt[rep * kCntStride + kCntGlist] = 0;
   if (!force && !d.sc[rep].rebuild) return;
   const int c0 = (blockIdx.x - R.cch0) * kCellChunk;
   if (force && !R.gl_all) {
@@ -1708,12 +1774,12 @@ __device__ __forceinline__ void overlap_init_at(Dev d, KParams p, int n_slots, i
     d.g->again = 0;
     d.g->n_comp = 0;
     d.g->comp_total = 0;
-    d.g->n_act = 0;
     d.g->passes = 1;
   }
   if (s == R.base) {
     sc->passes = 1;
     sc->again2 = 0;
+    d.pr_cnt[rep * kCntStride + kCntAct] = 0;
   }
   double dd = 0.0;
   if (s < n_slots) {
@@ -1842,10 +1908,10 @@ __device__ __forceinline__ void overlap_count_at(Dev d, int n_rank, int rep, int
   if (!m) return;
   const int leader = __ffs(m) - 1;
   int b = 0;
-  if (lane == leader) b = atomicAdd(&d.g->n_act, __popc(m));
+  if (lane == leader) b = atomicAdd(d.pr_cnt + rep * kCntStride + kCntAct, __popc(m));
   b = __shfl_sync(0xffffffffu, b, leader);
   if (!act) return;
-  d.act_list[b + __popc(m & ((1u << lane) - 1u))] = r;
+  d.act_list[d.rc[rep].base + b + __popc(m & ((1u << lane) - 1u))] = r;
   int root = uf_find((volatile int*)d.uf, h);
   d.uf[h] = root;
   atomicAdd(&d.comp_size[root], 1);
@@ -1859,46 +1925,55 @@ __global__ void overlap_count_kernel(Dev d, int n_rank) {
 
 // Component numbers and member ranges for the roots among the listed
 // members, one atomic per warp on each counter (the components are
-// independent, so their numbering is free).
-__global__ void overlap_assign_kernel(Dev d) {
-  const int n = d.g->n_act;
+// independent, so their numbering is free).  Per position of each replica's
+// list segment; every lane calls it.
+__device__ __forceinline__ void overlap_assign_at(const Dev& d, int end, int i) {
   const int lane = threadIdx.x & 31;
-  for (int i0 = blockIdx.x * blockDim.x; i0 < n; i0 += gridDim.x * blockDim.x) {
-    const int i = i0 + threadIdx.x;
-    int h = -1, sz = 0;
-    if (i < n) {
-      h = d.ref[d.act_list[i]];
-      if (d.uf[h] == h) sz = d.comp_size[h];
-    }
-    const bool has = sz > 0;
-    const unsigned m = __ballot_sync(0xffffffffu, has);
-    if (!m) continue;
-    int x = has ? sz : 0;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    const int total = __shfl_sync(0xffffffffu, x, 31);
-    const int leader = __ffs(m) - 1;
-    int bc = 0, bt = 0;
-    if (lane == leader) {
-      bc = atomicAdd(&d.g->n_comp, __popc(m));
-      bt = atomicAdd(&d.g->comp_total, total);
-    }
-    bc = __shfl_sync(0xffffffffu, bc, leader);
-    bt = __shfl_sync(0xffffffffu, bt, leader);
-    if (has) {
-      const int cid = bc + __popc(m & ((1u << lane) - 1u));
-      d.comp_id[h] = cid;
-      d.comp_list[2 * cid] = bt + x - sz;
-      d.comp_list[2 * cid + 1] = sz;
-    }
+  int h = -1, sz = 0;
+  if (i < end) {
+    h = d.ref[d.act_list[i]];
+    if (d.uf[h] == h) sz = d.comp_size[h];
+  }
+  const bool has = sz > 0;
+  const unsigned m = __ballot_sync(0xffffffffu, has);
+  if (!m) return;
+  int x = has ? sz : 0;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, x, 31);
+  const int leader = __ffs(m) - 1;
+  int bc = 0, bt = 0;
+  if (lane == leader) {
+    bc = atomicAdd(&d.g->n_comp, __popc(m));
+    bt = atomicAdd(&d.g->comp_total, total);
+  }
+  bc = __shfl_sync(0xffffffffu, bc, leader);
+  bt = __shfl_sync(0xffffffffu, bt, leader);
+  if (has) {
+    const int cid = bc + __popc(m & ((1u << lane) - 1u));
+    d.comp_id[h] = cid;
+    d.comp_list[2 * cid] = bt + x - sz;
+    d.comp_list[2 * cid + 1] = sz;
   }
 }
 
+__global__ void overlap_assign_kernel(Dev d) {
+  const int rep = block_rep(d);
+  const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntAct];
+  if (blockIdx.x * kSpan >= end) return;  // block-uniform
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) overlap_assign_at(d, end, span_pos(u));
+}
+
 __global__ void overlap_scatter_kernel(Dev d) {
-  const int n = d.g->n_act;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  const int rep = block_rep(d);
+  const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntAct];
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) {
+    const int i = span_pos(u);
+    if (i >= end) break;
     const int r = d.act_list[i];
     const int h = d.ref[r];
     const int root = d.uf[h];
@@ -1912,8 +1987,12 @@ __global__ void overlap_scatter_kernel(Dev d) {
 // number of smaller ranks in its component (contiguous loads, all members
 // in parallel).
 __global__ void overlap_order_kernel(Dev d) {
-  const int n = d.g->n_act;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+  const int rep = block_rep(d);
+  const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntAct];
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) {
+    const int i = span_pos(u);
+    if (i >= end) break;
     const int r = d.act_list[i];
     const int h = d.ref[r];
     const int cid = d.comp_id[d.uf[h]];
@@ -4042,12 +4121,18 @@ int k_step_begin(const Dev& d, int near_stale, cudaStream_t s) {
 }
 
 int k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
-  ermak_a_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  if (p.mixed)
+    ermak_a_kernel<true><<<nspan(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  else
+    ermak_a_kernel<false><<<nspan(n_rank), kBlock, 0, s>>>(d, p, n_rank);
   return 1;
 }
 
 int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
-  brownian_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  if (p.mixed)
+    brownian_kernel<true><<<nspan(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+  else
+    brownian_kernel<false><<<nspan(n_rank), kBlock, 0, s>>>(d, p, n_rank);
   return 1;
 }
 
@@ -4181,9 +4266,9 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
   }
   if (detect) n += k_overlap_detect(d, p, n_rank, detect == 1 ? 1 : 0, s);
   overlap_count_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
-  overlap_assign_kernel<<<152 * 4, kBlock, 0, s>>>(d);
-  overlap_scatter_kernel<<<152 * 4, kBlock, 0, s>>>(d);
-  overlap_order_kernel<<<152 * 4, kBlock, 0, s>>>(d);
+  overlap_assign_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d);
+  overlap_scatter_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d);
+  overlap_order_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d);
   int all_passes = p.prob >= 1.0;
   overlap_pass1_kernel<<<nblk(n_rank, 128), 128, 0, s>>>(d, p, all_passes);
   n += 5;
@@ -4211,9 +4296,10 @@ int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
 // gcmc_run's searches need the cells of the current positions.
 int k_gcmc_cells(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
   if (!d.any_cells) return 0;
-  rebuild_prep_kernel<<<nspan(cap), kBlock, 0, s>>>(d, p, cap, cap, 1);
+  (void)p;
+  gcmc_bin_kernel<<<nspan(cap), kBlock, 0, s>>>(d);
   cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1);
-  cell_scatter_kernel<<<nspan(cap), kBlock, 0, s>>>(d, cap, 1);
+  gcmc_scatter_kernel<<<nspan(cap), kBlock, 0, s>>>(d);
   cell_order_small_kernel<<<d.n_cch > 0 ? d.n_cch : 1, kBlock, 0, s>>>(d, 1);
   cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 1);
   return 5;
