@@ -598,7 +598,8 @@ def run_gpu(args, ws, rank, local):
             s2.step(k)
             done += k
             for r in range(wl.n_rep):
-                out = s2.get_atoms(replica=r) if wl.batched else s2.get_atoms()
+                out = (s2.get_atoms(replica=r, fields=("pos", "z")) if wl.batched
+                       else s2.get_atoms(fields=("pos", "z")))
                 d2h += out["pos"].nbytes + out["z"].nbytes
         t1 = time.perf_counter()
         s2.close()

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -724,70 +725,95 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   }
 #undef AL
 
-  // Host staging, position order (replica r at [base, base + cap)).
-  std::vector<double4> pos(cap), vel(cap), acel(cap), force(cap), pos_old(cap), old_cg(cap);
-  std::vector<float4> posf(cap, make_float4(0.f, 0.f, 0.f, 0.f)), posf_old(cap, posf[0]);
-  std::vector<double> epot(cap, 0.0);
-  std::vector<int8_t> typ(cap, 0), skip(cap, 0), state(cap, ST_NULL), in_gcmc(cap, 0);
-  std::vector<long long> id(cap, 0);
-  std::vector<int> rank(cap, -1), ref(cap, -1), slot(cap, -1), alist(cap, -1), apos(cap, -1),
-      gorder(cap, -1), gpos(cap, -1), rep_of(cap, 0);
+  // Compact upload: the caller's arrays concatenated over the replicas in one
+  // host buffer, one copy, and load_atoms_kernel expanding them into the
+  // position layout (replica r at [base, base + cap)).  Positions no atom
+  // takes keep the zero fill of dalloc or the -1 fill below.
+  std::vector<int> off(nrep + 1, 0);
+  for (int r = 0; r < nrep; ++r) off[r + 1] = off[r] + atoms[r].n;
+  const int n_tot = off[nrep];
+  auto any_of = [&](auto field) {
+    for (int r = 0; r < nrep; ++r)
+      if (atoms[r].*field) return true;
+    return false;
+  };
+  const bool has_vel = any_of(&dml_atoms::vel), has_acel = any_of(&dml_atoms::acel),
+             has_force = any_of(&dml_atoms::force), has_pold = any_of(&dml_atoms::pos_old),
+             has_ocg = any_of(&dml_atoms::old_cg), has_epot = any_of(&dml_atoms::epot),
+             has_skip = any_of(&dml_atoms::skip), has_id = any_of(&dml_atoms::id);
+  // section offsets in the staging buffer, each 16-byte aligned
+  size_t nb = 0;
+  auto sec = [&](bool on, size_t bytes) {
+    if (!on) return (size_t)-1;
+    const size_t at = nb;
+    nb += (bytes + 15) / 16 * 16;
+    return at;
+  };
+  const size_t v3 = sizeof(double) * 3 * (size_t)n_tot;
+  const size_t o_pos = sec(true, v3), o_vel = sec(has_vel, v3), o_acel = sec(has_acel, v3),
+               o_force = sec(has_force, v3), o_pold = sec(has_pold, v3),
+               o_ocg = sec(has_ocg, v3), o_epot = sec(has_epot, sizeof(double) * n_tot),
+               o_id = sec(has_id, sizeof(long long) * n_tot),
+               o_z = sec(true, sizeof(int) * n_tot), o_rk = sec(true, sizeof(int) * n_tot),
+               o_gk = sec(true, sizeof(int) * n_tot), o_off = sec(true, sizeof(int) * (nrep + 1)),
+               o_skip = sec(has_skip, n_tot);
+  std::unique_ptr<unsigned char[]> hb(new unsigned char[nb > 0 ? nb : 16]);
+  auto at = [&](size_t o) { return hb.get() + o; };
+  std::memcpy(at(o_off), off.data(), sizeof(int) * (nrep + 1));
   std::memset(c->h_sc, 0, sizeof(Scalars) * nrep);
+  const bool gcmc = c->P.reservoir == DML_RESERVOIR_GCMC;
   for (int r = 0; r < nrep; ++r) {
     const dml_atoms* a = atoms + r;
-    const RepConst& R = c->rc[r];
-    const int n = a->n, B = R.base;
-    for (int q = 0; q < R.cap; ++q) rep_of[B + q] = r;
+    const int n = a->n, o = off[r];
+    auto put3 = [&](size_t sec_off, const double* src, double def) {
+      if (sec_off == (size_t)-1) return;
+      double* dst = reinterpret_cast<double*>(at(sec_off)) + 3 * (size_t)o;
+      if (src) std::memcpy(dst, src, sizeof(double) * 3 * n);
+      else std::fill(dst, dst + 3 * (size_t)n, def);
+    };
+    put3(o_pos, a->pos, 0.0);
+    put3(o_vel, a->vel, 0.0);
+    put3(o_acel, a->acel, 0.0);
+    put3(o_force, a->force, 0.0);
+    put3(o_pold, a->pos_old ? a->pos_old : a->pos, 0.0);  // pos_old defaults to pos
+    put3(o_ocg, a->old_cg, 1e8);
+    if (has_epot) {
+      double* dst = reinterpret_cast<double*>(at(o_epot)) + o;
+      if (a->epot) std::memcpy(dst, a->epot, sizeof(double) * n);
+      else std::fill(dst, dst + n, 0.0);
+    }
+    if (has_skip) {
+      int8_t* dst = reinterpret_cast<int8_t*>(at(o_skip)) + o;
+      if (a->skip) std::memcpy(dst, a->skip, n);
+      else std::memset(dst, 0, n);
+    }
+    int64_t max_id = n - 1;
+    if (has_id) {
+      long long* dst = reinterpret_cast<long long*>(at(o_id)) + o;
+      if (a->id) {
+        max_id = -1;
+        for (int i = 0; i < n; ++i) {
+          dst[i] = a->id[i];
+          max_id = std::max<int64_t>(max_id, a->id[i]);
+        }
+      } else {
+        for (int i = 0; i < n; ++i) dst[i] = i;
+      }
+    }
+    int* zd = reinterpret_cast<int*>(at(o_z)) + o;
+    int* rk = reinterpret_cast<int*>(at(o_rk)) + o;
+    int* gk = reinterpret_cast<int*>(at(o_gk)) + o;
     int nref = 0, ng = 0;
-    int64_t max_id = -1;
     for (int i = 0; i < n; ++i) {
-      auto v3 = [&](const double* src, double def) {
-        if (!src) return make_double4(def, def, def, 0.0);
-        return make_double4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0.0);
-      };
-      int z = a->z[i];
+      const int z = a->z[i];
       if (z < 1 || z > 3) return DML_E_ARG;
-      const int h = B + i;  // hs slot = hs%b slot = sys%alist position
-      pos[h] = v3(a->pos, 0.0);
-      vel[h] = v3(a->vel, 0.0);
-      acel[h] = v3(a->acel, 0.0);
-      if (c->K.mixed) {  // FP32 velocity and acceleration in one slot (chosen form)
-        const double4 v = pack_f3((float)vel[h].x, (float)vel[h].y, (float)vel[h].z);
-        const double4 a = pack_f3((float)acel[h].x, (float)acel[h].y, (float)acel[h].z);
-        vel[h] = make_double4(v.x, v.y, a.x, a.y);
-        acel[h] = make_double4(0.0, 0.0, 0.0, 0.0);
-      }
-      force[h] = v3(a->force, 0.0);
-      pos_old[h] = a->pos_old ? v3(a->pos_old, 0.0) : pos[h];
-      old_cg[h] = v3(a->old_cg, 1e8);
-      epot[h] = a->epot ? a->epot[i] : 0.0;
-      typ[h] = (int8_t)z;
-      skip[h] = a->skip ? (a->skip[i] != 0) : 0;
-      state[h] = ST_LIVE;
-      id[h] = a->id ? a->id[i] : i;
-      max_id = std::max<int64_t>(max_id, id[h]);
-      float zbits;
-      std::memcpy(&zbits, &z, sizeof zbits);  // element as integer bits in w
-      posf[h] = make_float4((float)pos[h].x, (float)pos[h].y, (float)pos[h].z, zbits);
-      posf_old[h] = make_float4((float)pos_old[h].x, (float)pos_old[h].y, (float)pos_old[h].z, 0.f);
-      bool in_ref = a->in_ref ? a->in_ref[i] != 0 : (z != DML_Z_CG);
-      if (in_ref) {
-        rank[h] = B + nref;
-        ref[B + nref] = h;
-        ++nref;
-      }
-      slot[h] = h;
-      alist[h] = h;
-      apos[h] = h;
+      zd[i] = z;
+      // hs%ref holds the mobile atoms in sys order
+      const bool in_ref = a->in_ref ? a->in_ref[i] != 0 : (z != DML_Z_CG);
+      rk[i] = in_ref ? nref++ : -1;
       // gcmc attach loop (dana.F90:130-137): z == 1 atoms in sys order
-      bool gm = c->P.reservoir == DML_RESERVOIR_GCMC &&
-                (a->in_gcmc ? a->in_gcmc[i] != 0 : z == DML_Z_LI);
-      if (gm) {
-        gpos[h] = B + ng;
-        gorder[B + ng] = h;
-        in_gcmc[h] = 1;
-        ++ng;
-      }
+      const bool gm = gcmc && (a->in_gcmc ? a->in_gcmc[i] != 0 : z == DML_Z_LI);
+      gk[i] = gm ? ng++ : -1;
     }
     Scalars& S = c->h_sc[r];
     S.zmax = c->reps[r].zmax;
@@ -808,31 +834,37 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     S.next_id = max_id + 1;
   }
   cudaStream_t st = c->stream;
-  CK(cudaMemcpyAsync(d.pos, pos.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.vel, vel.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.acel, acel.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.force, force.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.pos_old, pos_old.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.old_cg, old_cg.data(), sizeof(double4) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.posf, posf.data(), sizeof(float4) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.posf_old, posf_old.data(), sizeof(float4) * cap, cudaMemcpyHostToDevice,
-                     st));
-  CK(cudaMemcpyAsync(d.epot, epot.data(), sizeof(double) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.typ, typ.data(), cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.skip, skip.data(), cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.state, state.data(), cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.in_gcmc, in_gcmc.data(), cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.id, id.data(), sizeof(long long) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.rank, rank.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.ref, ref.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.bslot, slot.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.b2hs, slot.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.alist, alist.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.apos, apos.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.gorder, gorder.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.gpos, gpos.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.rep_of, rep_of.data(), sizeof(int) * cap, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(d.rc, c->rc.data(), sizeof(RepConst) * nrep, cudaMemcpyHostToDevice, st));
+  unsigned char* db = nullptr;
+  CK(cudaMalloc(&db, nb > 0 ? nb : 16));
+  LoadIn in{};
+  auto dp = [&](size_t o) -> const void* { return o == (size_t)-1 ? nullptr : db + o; };
+  in.pos = static_cast<const double*>(dp(o_pos));
+  in.vel = static_cast<const double*>(dp(o_vel));
+  in.acel = static_cast<const double*>(dp(o_acel));
+  in.force = static_cast<const double*>(dp(o_force));
+  in.pos_old = static_cast<const double*>(dp(o_pold));
+  in.old_cg = static_cast<const double*>(dp(o_ocg));
+  in.epot = static_cast<const double*>(dp(o_epot));
+  in.id = static_cast<const long long*>(dp(o_id));
+  in.z = static_cast<const int*>(dp(o_z));
+  in.rk = static_cast<const int*>(dp(o_rk));
+  in.gk = static_cast<const int*>(dp(o_gk));
+  in.off = static_cast<const int*>(dp(o_off));
+  in.skip = static_cast<const int8_t*>(dp(o_skip));
+  in.n_tot = n_tot;
+  cudaError_t e = cudaMemcpyAsync(db, hb.get(), nb, cudaMemcpyHostToDevice, st);
+  // every index array of the layout starts at -1 (no atom, no slot)
+  for (int* a : {d.rank, d.ref, d.bslot, d.b2hs, d.alist, d.apos, d.gorder, d.gpos})
+    if (e == cudaSuccess) e = cudaMemsetAsync(a, 0xFF, sizeof(int) * cap, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d.rc, c->rc.data(), sizeof(RepConst) * nrep, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    k_load_atoms(d, c->K, in, st);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(db);
+  if (e != cudaSuccess) return cuda_fail(c, e, "load_atoms");
   CK(cudaMemcpyAsync(d.sc, c->h_sc, sizeof(Scalars) * nrep, cudaMemcpyHostToDevice, st));
   std::memset(c->h_g, 0, sizeof(Global));
   CK(cudaMemcpyAsync(d.g, c->h_g, sizeof(Global), cudaMemcpyHostToDevice, st));
@@ -1135,18 +1167,19 @@ int dml_get_atoms_replica(dml_ctx* c, int32_t rep, dml_atoms* a) {
     if (!ns) return cudaSuccess;
     return cudaMemcpyAsync(dst, (const char*)src + elem * B, elem * ns, cudaMemcpyDeviceToHost, s);
   };
-  CK(get(pos.data(), d.pos, sizeof(double4)));
-  if (a->vel) CK(get(vel.data(), d.vel, sizeof(double4)));
-  if (a->acel) CK(get(acel.data(), d.acel, sizeof(double4)));
+  // only the fields asked for travel (NULL outputs are skipped)
+  if (a->pos) CK(get(pos.data(), d.pos, sizeof(double4)));
+  if (a->vel || a->acel) CK(get(vel.data(), d.vel, sizeof(double4)));
+  if (a->acel && !c->K.mixed) CK(get(acel.data(), d.acel, sizeof(double4)));
   if (a->force) CK(get(force.data(), d.force, sizeof(double4)));
   if (a->pos_old) CK(get(pos_old.data(), d.pos_old, sizeof(double4)));
   if (a->old_cg) CK(get(old_cg.data(), d.old_cg, sizeof(double4)));
   if (a->epot) CK(get(epot.data(), d.epot, sizeof(double)));
-  CK(get(typ.data(), d.typ, 1));
+  if (a->z) CK(get(typ.data(), d.typ, 1));
   if (a->skip) CK(get(skip.data(), d.skip, 1));
-  CK(get(ing.data(), d.in_gcmc, 1));
-  CK(get(id.data(), d.id, sizeof(long long)));
-  CK(get(rank.data(), d.rank, sizeof(int)));
+  if (a->in_gcmc) CK(get(ing.data(), d.in_gcmc, 1));
+  if (a->id) CK(get(id.data(), d.id, sizeof(long long)));
+  if (a->in_ref) CK(get(rank.data(), d.rank, sizeof(int)));
   CK(cudaStreamSynchronize(s));
   int n = 0;
   for (int q = 0; q < nal; ++q)

@@ -274,7 +274,19 @@ struct Dev {
   int any_cells, any_verlet;  // some replica uses linked cells / the all-pairs build
 };
 
+// Compact per-atom input of dml_set_atoms_batch on the device: the replicas'
+// atoms concatenated (replica r's at [off[r], off[r + 1])), absent optional
+// arrays NULL.  rk / gk: the atom's place in hs%ref / gcmc%alist, or -1.
+struct LoadIn {
+  const double *pos, *vel, *acel, *force, *pos_old, *old_cg, *epot;
+  const int *z, *rk, *gk, *off;
+  const int8_t* skip;
+  const long long* id;
+  int n_tot;
+};
+
 // ---- kernel launchers (dml_kernels.cu); each returns the kernels it queued ----
+int k_load_atoms(const Dev& d, const KParams& p, const LoadIn& in, cudaStream_t s);
 int k_step_begin(const Dev& d, int near_stale, cudaStream_t s);
 int k_rank_prefix(const Dev& d, cudaStream_t s);
 int k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);

@@ -4097,6 +4097,72 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
   if (tid == 0) *sc_g = S.ss;
 }
 
+// dml_set_atoms_batch on the device: the replica of every position, then
+// every loaded atom's slot (hs slot = hs%b slot = sys%alist position) from
+// the compact input.  Positions left unused keep the -1 / zero fill.
+__global__ void load_rep_kernel(Dev d) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < d.cap; q += gridDim.x * blockDim.x) {
+    int lo = 0, hi = d.nrep - 1;  // largest replica whose base is <= q
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (d.rc[mid].base <= q) lo = mid; else hi = mid - 1;
+    }
+    d.rep_of[q] = lo;
+  }
+}
+
+__global__ void load_atoms_kernel(Dev d, KParams p, LoadIn in) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < in.n_tot; i += gridDim.x * blockDim.x) {
+    int lo = 0, hi = d.nrep - 1;  // replica of compact atom i
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (in.off[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    const int li = i - in.off[lo], B = d.rc[lo].base, h = B + li;
+    auto v3 = [&](const double* a, double def) {
+      return a ? make_double4(a[3 * i], a[3 * i + 1], a[3 * i + 2], 0.0)
+               : make_double4(def, def, def, 0.0);
+    };
+    const int z = in.z[i];
+    const double4 P = v3(in.pos, 0.0);
+    const double4 O = in.pos_old ? v3(in.pos_old, 0.0) : P;
+    d.pos[h] = P;
+    d.pos_old[h] = O;
+    d.posf[h] = to_f4(P, z);
+    d.posf_old[h] = to_f4(O, 0);
+    const double4 V = v3(in.vel, 0.0), A = v3(in.acel, 0.0);
+    if (p.mixed) {  // FP32 velocity and acceleration in one slot (chosen form)
+      float4* q = reinterpret_cast<float4*>(d.vel + h);
+      q[0] = make_float4((float)V.x, (float)V.y, (float)V.z, 0.0f);
+      q[1] = make_float4((float)A.x, (float)A.y, (float)A.z, 0.0f);
+    } else {
+      d.vel[h] = V;
+      d.acel[h] = A;
+    }
+    d.force[h] = v3(in.force, 0.0);
+    d.old_cg[h] = v3(in.old_cg, 1e8);
+    d.epot[h] = in.epot ? in.epot[i] : 0.0;
+    d.typ[h] = (int8_t)z;
+    d.skip[h] = in.skip ? (int8_t)(in.skip[i] != 0) : (int8_t)0;
+    d.state[h] = ST_LIVE;
+    d.id[h] = in.id ? in.id[i] : (long long)li;
+    d.alist[h] = h;
+    d.apos[h] = h;
+    d.bslot[h] = h;
+    d.b2hs[h] = h;
+    const int rk = in.rk[i], gk = in.gk[i];
+    if (rk >= 0) {
+      d.rank[h] = B + rk;
+      d.ref[B + rk] = h;
+    }
+    if (gk >= 0) {
+      d.gpos[h] = B + gk;
+      d.gorder[B + gk] = h;
+      d.in_gcmc[h] = 1;
+    }
+  }
+}
+
 inline int nblk(int n, int b = kBlock) { return n > 0 ? (n + b - 1) / b : 1; }
 // blocks of the per-position kernels over n positions (a multiple of kSpan)
 inline int nspan(int n) { return n > 0 ? (n + kSpan - 1) / kSpan : 1; }
@@ -4339,4 +4405,12 @@ int k_flush(void* buf, size_t bytes, cudaStream_t s) {
   return 1;
 }
 
+}  // namespace dml
+
+namespace dml {
+int k_load_atoms(const Dev& d, const KParams& p, const LoadIn& in, cudaStream_t s) {
+  load_rep_kernel<<<152 * 8, kBlock, 0, s>>>(d);
+  load_atoms_kernel<<<152 * 8, kBlock, 0, s>>>(d, p, in);
+  return 2;
+}
 }  // namespace dml

@@ -240,14 +240,16 @@ class Simulation:
                         "dml_get_counters_replica")
         return c.as_dict()
 
-    def get_atoms(self, n=None, replica=None):
+    def get_atoms(self, n=None, replica=None, fields=None):
+        """Atom state in sys%alist order; `fields` (names of dml_atoms
+        members) limits what is copied back."""
         if replica is None and self.batched:
             replica = 0 if self.n_rep == 1 else None
             if replica is None:
                 raise ValueError("get_atoms: pass replica= on a batch context")
         if n is None:
             n = self.counters(replica)["n_atoms"]
-        out = _abi.empty_atoms(n)
+        out = _abi.empty_atoms(n, fields)
         a = _abi.atoms_struct(out, n)
         if replica is None:
             self._check(self.lib.dml_get_atoms(self.h, ctypes.byref(a)), "dml_get_atoms")

@@ -170,11 +170,14 @@ def atoms_struct(arrays, n):
     return a
 
 
-def empty_atoms(n):
+def empty_atoms(n, fields=None):
+    """Output arrays for n atoms: every field, or only those named in fields."""
     import numpy as np
 
     out = {}
     for name, (dt, comp) in ATOM_FIELDS.items():
+        if fields is not None and name not in fields:
+            continue
         shape = (n, comp) if comp > 1 else (n,)
         out[name] = np.zeros(shape, dtype=dt)
     return out
