@@ -1076,6 +1076,27 @@ int dml_get_tuning(dml_ctx* c, int32_t* scan_lanes, float* scan_us) {
   return 0;
 }
 
+int dml_check_conversions(const double* x, int64_t n, float* f32, double* back) {
+  if (n < 0 || (n > 0 && (!x || !f32 || !back))) return DML_E_ARG;
+  if (n == 0) return 0;
+  double *dx = nullptr, *db = nullptr;
+  float* df = nullptr;
+  cudaError_t e = cudaMalloc(&dx, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&db, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&df, sizeof(float) * n);
+  if (e == cudaSuccess) e = cudaMemcpy(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_check_conversions(dx, df, db, n, 0);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(f32, df, sizeof(float) * n, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(back, db, sizeof(double) * n, cudaMemcpyDeviceToHost);
+  cudaFree(dx);
+  cudaFree(db);
+  cudaFree(df);
+  return e == cudaSuccess ? 0 : DML_E_CUDA;
+}
+
 int dml_launches_per_step(dml_ctx* c, int32_t* per_rebuild) {
   if (!c) return -DML_E_ARG;
   if (!c->launches_per_step) {

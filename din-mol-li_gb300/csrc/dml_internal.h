@@ -287,6 +287,7 @@ struct LoadIn {
 
 // ---- kernel launchers (dml_kernels.cu); each returns the kernels it queued ----
 int k_load_atoms(const Dev& d, const KParams& p, const LoadIn& in, cudaStream_t s);
+int k_check_conversions(const double* x, float* f32, double* back, long long n, cudaStream_t s);
 int k_step_begin(const Dev& d, int near_stale, cudaStream_t s);
 int k_rank_prefix(const Dev& d, cudaStream_t s);
 int k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);

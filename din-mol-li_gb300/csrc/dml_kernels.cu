@@ -37,10 +37,40 @@ __device__ __forceinline__ void count_add(unsigned long long* c, unsigned long l
   atomicAdd(c, v);
 }
 
+// Conversions between binary64 and binary32 on the integer pipes.  GB300
+// issues FP64-pipe instructions (conversions included) at 1/64 of the FP32
+// rate, so the integrators, which convert six values per atom, do the
+// conversion of normal numbers in integer arithmetic following the IEEE 754
+// encodings (same results as the hardware conversion; the rare operands
+// outside the normal range take the hardware path).
+//
+// binary64 -> binary32, round to nearest, ties to even: a double with
+// biased exponent E in [897, 1150] is a normal float of exponent E - 896 after
+// rounding away the low 29 mantissa bits (a carry out of the mantissa
+// increments the exponent, E - 896 = 255 being the overflow to infinity).
+__device__ __forceinline__ float f64_to_f32_rn(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long a = u & 0x7FFFFFFFFFFFFFFFull;
+  if (a < (897ull << 52) || a >= (1151ull << 52)) return __double2float_rn(x);
+  unsigned long long em = a - (896ull << 52);
+  em += 0x0FFFFFFFull + ((em >> 29) & 1ull);
+  return __uint_as_float((unsigned)(em >> 29) | ((unsigned)(u >> 32) & 0x80000000u));
+}
+
+// binary32 -> binary64 (exact): a normal float's exponent rebiased by
+// 1023 - 127 = 896, its 23 mantissa bits the top of the double's 52.
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned b = __float_as_uint(f), e = (b >> 23) & 0xFFu;
+  if (e == 0u || e == 0xFFu) return (double)f;  // zero, subnormal, inf, NaN
+  const unsigned hi = (b & 0x80000000u) | (((b & 0x7FFFFFFFu) >> 3) + (896u << 20));
+  return __hiloint2double((int)hi, (int)(b << 29));
+}
+
 // FP32 copy of a position; w carries the element as integer bits (0 for a
 // slot that is not live), so reading it needs no conversion instruction.
 __device__ __forceinline__ float4 to_f4(double4 p, int typ) {
-  return make_float4((float)p.x, (float)p.y, (float)p.z, __int_as_float(typ));
+  return make_float4(f64_to_f32_rn(p.x), f64_to_f32_rn(p.y), f64_to_f32_rn(p.z),
+                     __int_as_float(typ));
 }
 
 __device__ __forceinline__ int elem_of(float4 q) { return __float_as_int(q.w); }
@@ -100,8 +130,10 @@ __device__ __forceinline__ int cell_index(double x, double cell) {
 // FP64 division issues on GB300's narrow FP64 pipe).  With xf = RN32(x) and
 // inv = RN32(1/cell) the FP32 quotient q is within 3 * 2^-24 |q| of x/cell,
 // so when q lies farther than 4e-7 q + 1e-6 from every integer, int(x/cell)
-// = floor(q) exactly; otherwise kCellUndecided asks for cell_index.  The
-// integer comes from adding 1.5 * 2^23 (round to nearest, FP32 adds only).
+// = floor(q) exactly; for -0.999 < q <= 0 the true quotient lies in (-1, 0]
+// (|q| < 1, error below 2e-7), where int() gives 0; otherwise kCellUndecided
+// asks for cell_index.  The integer comes from adding 1.5 * 2^23 (round to
+// nearest, FP32 adds only).
 constexpr int kCellUndecided = INT_MIN + 1;
 __device__ __forceinline__ int cell_index_est(float xf, float inv) {
   const float M = 12582912.0f;
@@ -110,6 +142,8 @@ __device__ __forceinline__ int cell_index_est(float xf, float inv) {
   float dq = fabsf(q - r);
   if (q > 0.0f && q < 4194304.0f && dq > 4e-7f * q + 1e-6f)
     return (__float_as_int((q - 0.5f) + M) - 0x4B400000) + 1;
+  // x/cell in (-1, 0] (coordinates on the lower box faces): int() truncates to 0
+  if (q <= 0.0f && q > -0.999f) return 1;
   return kCellUndecided;
 }
 
@@ -330,14 +364,32 @@ __device__ __forceinline__ bool pbc_quiet(const KParams& p, const RepConst& R, f
 // step) is formed in FP32 from the FP32 velocity, acceleration and noise and
 // added to the FP64 position; atom_pbc runs in FP64 for the atoms near a
 // wall, the box edge or the capture plane, as in the plain form.
+// One atom's inputs to the chosen form's ermak_a, loaded one atom ahead of
+// the arithmetic so that a thread's next loads are in flight while it draws
+// and integrates the current atom.
+struct ErmIn {
+  double2 Pxy;
+  double Pz;
+  float4 V, A, before;
+  long long id;
+  int typ;
+};
+__device__ __forceinline__ void erm_load(const Dev& d, int h, ErmIn& in) {
+  in.Pxy = reinterpret_cast<const double2*>(d.pos + h)[0];
+  in.Pz = reinterpret_cast<const double*>(d.pos + h)[2];
+  ldva(d.vel, h, in.V, in.A);
+  in.typ = d.typ[h];
+  in.id = d.id[h];
+  in.before = d.posf[h];
+}
 __device__ __forceinline__ void ermak_a_mixed_atom(const Dev& d, const KParams& p,
                                                    const RepConst& R, Scalars* sc, int h,
-                                                   long long step, double zmax) {
-  const double4 P = d.pos[h];
-  float4 V, A;
-  ldva(d.vel, h, V, A);
-  int typ = d.typ[h];
-  const long long id = d.id[h];
+                                                   const ErmIn& in, long long step, double zmax,
+                                                   float zmaxf) {
+  const double4 P = make_double4(in.Pxy.x, in.Pxy.y, in.Pz, 0.0);
+  const float4 V = in.V, A = in.A;
+  int typ = in.typ;
+  const long long id = in.id;
   const float rf = p.rfacf[typ - 1], vf = p.vfacf[typ - 1];
   float nq[8];
   dml_normal_quadf(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 0), &nq[0]);
@@ -349,15 +401,15 @@ __device__ __forceinline__ void ermak_a_mixed_atom(const Dev& d, const KParams& 
   for (int j = 0; j < 3; ++j) {
     const float r1 = nq[2 * j], r2 = nq[2 * j + 1];
     const float inc = p.cc1f * vv[j] + p.cc2hf * aa[j] + rf * r1;
-    pp[j] = pp[j] + (double)inc;
+    pp[j] = pp[j] + f32_to_f64(inc);
     rv[j] = vf * (p.crv1f * r1 + p.crv2f * r2);
   }
   const int typ0 = typ;
-  const float4 before = d.posf[h];
+  const float4 before = in.before;
   float4 after = to_f4(make_double4(pp[0], pp[1], pp[2], 0.0), typ);
   bool depos = false, po_changed = false, v_changed = false;
   double4 po;
-  if (!pbc_quiet(p, R, after, (float)zmax)) {
+  if (!pbc_quiet(p, R, after, zmaxf)) {
     po = d.pos_old[h];
     double4 Vd = make_double4(V.x, V.y, V.z, 0.0);
     depos = atom_pbc_dev(p, R, sc, step, id, pp, po, po_changed, Vd, v_changed, P, typ, zmax);
@@ -380,19 +432,11 @@ __device__ __forceinline__ void ermak_a_mixed_atom(const Dev& d, const KParams& 
 // ermak_a (dana.F90:974-1028): one thread per hs%ref member; one kernel
 // per form, so that each gets only the registers its own path needs.
 template <bool MIXED>
-__device__ __forceinline__ void ermak_a_at(Dev d, KParams p, int n_rank, int rep, int pos) {
+__device__ __forceinline__ void ermak_a_at(const Dev& d, const KParams& p, int rep, int h,
+                                           long long step, double zmax, float zmaxf) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
-  const int r = pos;
-  if (r - R.base >= sc->n_rank) return;
-  int h = d.ref[r];
-  if (h < 0) return;
-  long long step = d.g->step;
-  double zmax = sc->zmax;
-  if (MIXED) {
-    ermak_a_mixed_atom(d, p, R, sc, h, step, zmax);
-    return;
-  }
+  if (MIXED) return;
   double4 P = d.pos[h];
   double4 V = d.vel[h];
   double4 A = d.acel[h];
@@ -433,25 +477,51 @@ __device__ __forceinline__ void ermak_a_at(Dev d, KParams p, int n_rank, int rep
   if (!depos) d.skip[h] = 0;
 }
 
+// The block's hs%ref entries are read first, all four at once, and the
+// replica's scalars once; the chosen form then loads each atom's inputs
+// while the previous atom is integrated (three blocks per SM leave the
+// registers for the second set).
 template <bool MIXED>
-__global__ void __launch_bounds__(kBlock, 4) ermak_a_kernel(Dev d, KParams p, int n_rank) {
+__global__ void __launch_bounds__(kBlock, 3) ermak_a_kernel(Dev d, KParams p, int n_rank) {
   const int rep = block_rep(d);
+  const int end = d.rc[rep].base + d.sc[rep].n_rank;
+  if ((int)blockIdx.x * kSpan >= end) return;
+  int h0 = span_pos(0) < end ? d.ref[span_pos(0)] : -1;
+  int h1 = span_pos(1) < end ? d.ref[span_pos(1)] : -1;
+  int h2 = span_pos(2) < end ? d.ref[span_pos(2)] : -1;
+  int h3 = span_pos(3) < end ? d.ref[span_pos(3)] : -1;
+  const long long step = d.g->step;
+  const double zmax = d.sc[rep].zmax;
+  const float zmaxf = (float)zmax;
+  if (!MIXED) {
 #pragma unroll 1
-  for (int u = 0; u < kSlotU; ++u) ermak_a_at<MIXED>(d, p, n_rank, rep, span_pos(u));
+    for (int u = 0; u < kSlotU; ++u) {
+      if (h0 >= 0) ermak_a_at<MIXED>(d, p, rep, h0, step, zmax, zmaxf);
+      h0 = h1; h1 = h2; h2 = h3;
+    }
+    return;
+  }
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  ErmIn cur;
+  if (h0 >= 0) erm_load(d, h0, cur);
+#pragma unroll 1
+  for (int u = 0; u < kSlotU; ++u) {
+    ErmIn nxt;
+    if (h1 >= 0) erm_load(d, h1, nxt);
+    if (h0 >= 0) ermak_a_mixed_atom(d, p, R, sc, h0, cur, step, zmax, zmaxf);
+    cur = nxt;
+    h0 = h1; h1 = h2; h2 = h3; h3 = -1;
+  }
 }
 
 // cbrownian_hs (dana.F90:798-846): one thread per hs%ref member; one kernel
 // per form.
 template <bool MIXED>
-__device__ __forceinline__ void brownian_at(Dev d, KParams p, int n_rank, int rep, int pos) {
+__device__ __forceinline__ void brownian_at(const Dev& d, const KParams& p, int rep, int h,
+                                            long long step, double zmax, float zmaxf) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
-  const int r = pos;
-  if (r - R.base >= sc->n_rank) return;
-  int h = d.ref[r];
-  if (h < 0) return;
-  long long step = d.g->step;
-  double zmax = sc->zmax;
   double4 P = d.pos[h];
   int typ = d.typ[h];
   long long id = d.id[h];
@@ -465,7 +535,7 @@ __device__ __forceinline__ void brownian_at(Dev d, KParams p, int n_rank, int re
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       const float inc = nf[j] * facf;
-      pp[j] = pp[j] + (double)inc;
+      pp[j] = pp[j] + f32_to_f64(inc);
       vf[j] = inc * p.inv_hf;
     }
     const int typ0 = typ;
@@ -473,7 +543,7 @@ __device__ __forceinline__ void brownian_at(Dev d, KParams p, int n_rank, int re
     float4 after = to_f4(make_double4(pp[0], pp[1], pp[2], 0.0), typ);
     bool depos = false, po_changed = false, v_changed = false;
     double4 po;
-    if (!pbc_quiet(p, R, after, (float)zmax)) {
+    if (!pbc_quiet(p, R, after, zmaxf)) {
       po = d.pos_old[h];
       double4 Vd = make_double4(vf[0], vf[1], vf[2], 0.0);
       depos = atom_pbc_dev(p, R, sc, step, id, pp, po, po_changed, Vd, v_changed, P, typ, zmax);
@@ -523,11 +593,27 @@ __device__ __forceinline__ void brownian_at(Dev d, KParams p, int n_rank, int re
   if (!depos) d.skip[h] = 0;
 }
 
+// hs%ref entries and the replica's scalars read first, as in ermak_a.
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock, 4) brownian_kernel(Dev d, KParams p, int n_rank) {
   const int rep = block_rep(d);
+  const int end = d.rc[rep].base + d.sc[rep].n_rank;
+  if ((int)blockIdx.x * kSpan >= end) return;
+  int h0 = span_pos(0) < end ? d.ref[span_pos(0)] : -1;
+  int h1 = span_pos(1) < end ? d.ref[span_pos(1)] : -1;
+  int h2 = span_pos(2) < end ? d.ref[span_pos(2)] : -1;
+  int h3 = span_pos(3) < end ? d.ref[span_pos(3)] : -1;
+  static_assert(kSlotU == 4, "four hs%ref entries per thread");
+  const long long step = d.g->step;
+  const double zmax = d.sc[rep].zmax;
+  const float zmaxf = (float)zmax;
 #pragma unroll 1
-  for (int u = 0; u < kSlotU; ++u) brownian_at<MIXED>(d, p, n_rank, rep, span_pos(u));
+  for (int u = 0; u < kSlotU; ++u) {
+    if (h0 >= 0) brownian_at<MIXED>(d, p, rep, h0, step, zmax, zmaxf);
+    h0 = h1;
+    h1 = h2;
+    h2 = h3;
+  }
 }
 
 // Union-find over hs slots (overlap components): path halving, union by
@@ -1548,6 +1634,16 @@ __global__ void cell_order_small_kernel(Dev d, int force) {
     }
     d.cell_count[c] = 0;
     const int start = d.cell_start[c];
+    if (num == 1) {  // most occupied cells: nothing to order
+      d.cell_atoms[start] = d.b2hs[d.cell_atoms[start]];
+      continue;
+    }
+    if (num == 2) {
+      const int a = d.cell_atoms[start], b = d.cell_atoms[start + 1];
+      d.cell_atoms[start] = d.b2hs[max(a, b)];
+      d.cell_atoms[start + 1] = d.b2hs[min(a, b)];
+      continue;
+    }
     int v[kSmallCell];
 #pragma unroll
     for (int k = 0; k < kSmallCell; ++k) v[k] = k < num ? d.cell_atoms[start + k] : -1;
@@ -4408,6 +4504,21 @@ int k_flush(void* buf, size_t bytes, cudaStream_t s) {
 }  // namespace dml
 
 namespace dml {
+__global__ void check_conversions_kernel(const double* x, float* f32, double* back,
+                                         long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float f = f64_to_f32_rn(x[i]);
+    f32[i] = f;
+    back[i] = f32_to_f64(f);
+  }
+}
+
+int k_check_conversions(const double* x, float* f32, double* back, long long n, cudaStream_t s) {
+  check_conversions_kernel<<<152 * 4, kBlock, 0, s>>>(x, f32, back, n);
+  return 1;
+}
+
 int k_load_atoms(const Dev& d, const KParams& p, const LoadIn& in, cudaStream_t s) {
   load_rep_kernel<<<152 * 8, kBlock, 0, s>>>(d);
   load_atoms_kernel<<<152 * 8, kBlock, 0, s>>>(d, p, in);

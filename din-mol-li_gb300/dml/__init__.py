@@ -82,6 +82,7 @@ def lib():
     L.dml_profile_steps.argtypes = [vp, i64, i32, vp, i32]
     L.dml_launches_per_step.argtypes = [vp, P(i32)]
     L.dml_get_tuning.argtypes = [vp, P(i32), vp]
+    L.dml_check_conversions.argtypes = [vp, i64, vp, vp]
     L.dml_gen_bcc_slab.argtypes = [i32, i32, i32, ctypes.c_double, vp, i32]
     L.dml_gen_ions.argtypes = [ctypes.c_uint64, i32, ctypes.c_double, ctypes.c_double,
                                ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
@@ -93,6 +94,18 @@ def default_params():
     p = _abi.Params()
     lib().dml_params_default(ctypes.byref(p))
     return p
+
+
+def check_conversions(x):
+    """The device's float64 -> float32 (round to nearest even) and exact
+    float32 -> float64 conversions applied to x: (f32, back)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    f32 = np.zeros(x.shape, np.float32)
+    back = np.zeros(x.shape, np.float64)
+    rc = lib().dml_check_conversions(x.ctypes.data, x.size, f32.ctypes.data, back.ctypes.data)
+    if rc:
+        raise DmlError(rc, "dml_check_conversions")
+    return f32, back
 
 
 def bcc_slab(nx, ny, nz, a=3.51):

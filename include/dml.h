@@ -318,6 +318,14 @@ int dml_gen_bcc_slab(int32_t nx, int32_t ny, int32_t nz, double a, double* pos_o
 int dml_gen_ions(uint64_t seed, int32_t n, double box_x, double box_y, double zlo, double zhi,
                  double dmin, double* pos_out);
 
+/* Diagnostic (no counterpart in the reference): runs the device's
+ * binary64 -> binary32 conversion (round to nearest, ties to even) that
+ * makes the FP32 position copies, and the exact binary32 -> binary64
+ * conversion that the integrators apply to FP32 increments, over n values
+ * on the default stream: f32[i] = RN32(x[i]), back[i] = f32[i] as a double.
+ * Host arrays; returns 0 or DML_E_CUDA. */
+int dml_check_conversions(const double* x, int64_t n, float* f32, double* back);
+
 const char* dml_strerror(int code);
 
 /* Text of the last CUDA or argument error of this context. */

@@ -73,3 +73,33 @@ def test_mixed_is_deterministic():
         g.close()
     for k in out[0]:
         assert np.array_equal(out[0][k], out[1][k]), k
+
+
+def test_device_conversions_match_ieee():
+    """The integer-pipe conversions behind the FP32 position copies and the
+    integrators' FP32 increments equal IEEE 754 round-to-nearest-even (numpy)
+    over random bit patterns, positions in the box range, halfway cases,
+    mantissa carries and the subnormal, overflow, zero, inf and NaN edges."""
+    rng = np.random.default_rng(3)
+    bits = rng.integers(0, 2 ** 64, 200000, dtype=np.uint64)
+    anyd = bits.view(np.float64)
+    box = rng.uniform(-50.0, 400.0, 200000)
+    f = rng.uniform(-300.0, 300.0, 50000).astype(np.float32).astype(np.float64)
+    ulp = np.spacing(f.astype(np.float32)).astype(np.float64)
+    ties = np.concatenate([f + ulp / 2, f - ulp / 2, f + ulp / 2 * (1 + 2 ** -40)])
+    carry = np.array([1.0 - 2 ** -25, 2.0 - 2 ** -24, 255.99999999, -(2.0 - 2 ** -25)])
+    fmax = float(np.finfo(np.float32).max)
+    tiny = float(np.finfo(np.float32).tiny)
+    edges = np.array([0.0, -0.0, 5e-324, -5e-324, tiny, -tiny, tiny * (1 - 2 ** -30),
+                      tiny * 2 ** -10, fmax, -fmax, fmax * (1 + 2 ** -25), fmax * 2,
+                      np.inf, -np.inf, np.nan, 1e-45, 1.4e-45, 3e-39, 1e300, -1e-300])
+    x = np.concatenate([anyd, box, ties, carry, edges])
+    f32, back = dml.check_conversions(x)
+    with np.errstate(over="ignore", invalid="ignore"):
+        want = x.astype(np.float32)
+    nan = np.isnan(want)
+    assert np.array_equal(np.isnan(f32), nan)
+    assert np.array_equal(f32[~nan].view(np.uint32), want[~nan].view(np.uint32))
+    wb = f32.astype(np.float64)
+    assert np.array_equal(np.isnan(back), nan)
+    assert np.array_equal(back[~nan].view(np.uint64), wb[~nan].view(np.uint64))
