@@ -350,14 +350,15 @@ __device__ __forceinline__ void stva(double4* vel, int h, float vx, float vy, fl
   q[1] = make_float4(ax, ay, az, 0.0f);
 }
 
-// No atom_pbc action (wrap, mirror at zmax, capture at z <= 0) can apply to
-// a position whose FP32 copy lies farther than the margin from 0 and the box
-// edge in x and y and from 0 and zmax in z.
+// No atom_pbc action (wrap when x > box or x < 0, mirror when z > zmax,
+// capture when z <= 0) can apply to a position whose FP32 copy f = RN32(x)
+// satisfies 0 < f < RN32(bound) in every test: rounding to nearest is
+// monotone, so x >= bound gives f >= RN32(bound) and x <= 0 gives f <= 0.
+// boxf and zmaxf are RN32 of the FP64 bounds; a NaN is never quiet.
 __device__ __forceinline__ bool pbc_quiet(const KParams& p, const RepConst& R, float4 f,
                                           float zmaxf) {
-  const float e = R.margin;
-  return f.x > e && f.x < R.boxf[0] - e && f.y > e && f.y < R.boxf[1] - e && f.z > e &&
-         f.z < zmaxf - e;
+  return f.x > 0.0f && f.x < R.boxf[0] && f.y > 0.0f && f.y < R.boxf[1] && f.z > 0.0f &&
+         f.z < zmaxf;
 }
 
 // ermak_a of the chosen form: each coordinate's increment (about 1e-2 Å per
@@ -660,28 +661,21 @@ __device__ __forceinline__ float near_radius2(const Dev& d, const KParams& p, co
 // On GB300 an FP64 instruction occupies the narrow FP64 pipe for the whole
 // warp whatever its active lanes, so the exact FP64 work is done afterwards
 // on the dense queue (force_exact_kernel), 32 entries per instruction.
+// One warp-wide pass over 32 / L rows, L lanes each (the lanes of a row
+// agree on rep, r, h; h < 0 for no row).  Every lane of the warp takes part.
+// Pf and n are the row owner's FP32 position and list length.
 template <bool NEAR, int L>
-__device__ __forceinline__ void force_scan_rows(const Dev& d, const KParams& p, int w,
-                                                int total) {
-  // 32 / L hs%ref members per warp, L lanes each, so that the dependent
-  // loads of several rows overlap; each lane keeps 4 entries in flight.
+__device__ __forceinline__ void force_scan_row(const Dev& d, const KParams& p, int rep, int r,
+                                               int h, float4 Pf, int n) {
+  // each lane keeps 4 entries in flight
   constexpr int U = 4, STEP = L * U;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, sl = lane % L, sub = lane / L;
   const unsigned smask = (L == 32 ? FULL : ((1u << L) - 1u)) << (sub * L);
-  const int i = (32 / L) * w + sub;
-  const int r = i < total ? row_rank(d, i) : 0;
-  // the element comes with the position (posf.w)
-  const int rep = d.rep_of[r];
   const RepConst& R = d.rc[rep];
-  int h = -1, k = 0, n = 0;
-  float4 Pf = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (i < total) h = d.ref[r];
-  if (h >= 0) {
-    Pf = d.posf[h];
-    n = d.nn[h];
-    k = elem_of(Pf);
-  }
+  // the element comes with the position (posf.w)
+  const int k = h >= 0 ? elem_of(Pf) : 0;
+  if (h < 0) n = 0;
   int nmax = n;
 #pragma unroll
   for (int o = L; o < 32; o <<= 1) nmax = max(nmax, __shfl_xor_sync(FULL, nmax, o));
@@ -752,13 +746,53 @@ __device__ __forceinline__ void force_scan_rows(const Dev& d, const KParams& p, 
   }
 }
 
-// The rows in use, 32 / L per warp, by a fixed grid of warps.
+// The rows in use, 32 / L per warp (L lanes each, so that the dependent
+// loads of several rows overlap), by a fixed grid of warps; a row's rank
+// comes from the replicas' prefix of rows in use.
 template <bool NEAR, int L>
 __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p) {
   const int nw = gridDim.x * (blockDim.x >> 5);
   const int total = d.rank_pre[d.nrep];
-  for (int w = warp_id_global(); (32 / L) * w < total; w += nw)
-    force_scan_rows<NEAR, L>(d, p, w, total);
+  const int sub = (threadIdx.x & 31) / L;
+  for (int w = warp_id_global(); (32 / L) * w < total; w += nw) {
+    const int i = (32 / L) * w + sub;
+    const int r = i < total ? row_rank(d, i) : 0;
+    const int h = i < total ? d.ref[r] : -1;
+    float4 Pf = make_float4(0.f, 0.f, 0.f, 0.f);
+    int n = 0;
+    if (h >= 0) {
+      Pf = d.posf[h];
+      n = d.nn[h];
+    }
+    force_scan_row<NEAR, L>(d, p, d.rep_of[r], r, h, Pf, n);
+  }
+}
+
+// One lane per row: the rank positions of the replica's span, four per
+// thread, their hs%ref entries, positions and list lengths loaded up front.
+template <bool NEAR>
+__global__ void __launch_bounds__(kBlock) force_scan_span_kernel(Dev d, KParams p) {
+  const int rep = block_rep(d);
+  const int end = d.rc[rep].base + d.sc[rep].n_rank;
+  if ((int)blockIdx.x * kSpan >= end) return;  // whole block: warps stay full
+  static_assert(kSlotU == 4, "four rows per thread");
+  int h0 = span_pos(0) < end ? d.ref[span_pos(0)] : -1;
+  int h1 = span_pos(1) < end ? d.ref[span_pos(1)] : -1;
+  int h2 = span_pos(2) < end ? d.ref[span_pos(2)] : -1;
+  int h3 = span_pos(3) < end ? d.ref[span_pos(3)] : -1;
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 P0 = h0 >= 0 ? d.posf[h0] : z4, P1 = h1 >= 0 ? d.posf[h1] : z4;
+  float4 P2 = h2 >= 0 ? d.posf[h2] : z4, P3 = h3 >= 0 ? d.posf[h3] : z4;
+  int n0 = h0 >= 0 ? d.nn[h0] : 0, n1 = h1 >= 0 ? d.nn[h1] : 0;
+  int n2 = h2 >= 0 ? d.nn[h2] : 0, n3 = h3 >= 0 ? d.nn[h3] : 0;
+  // one copy of the row body, the rows rotated through registers
+#pragma unroll 1
+  for (int u = 0; u < kSlotU; ++u) {
+    force_scan_row<NEAR, 1>(d, p, rep, span_pos(u), h0, P0, n0);
+    h0 = h1; h1 = h2; h2 = h3;
+    P0 = P1; P1 = P2; P2 = P3;
+    n0 = n1; n1 = n2; n2 = n3;
+  }
 }
 
 // Exact FP64 evaluation of the queued entries (dana.F90:1095-1134), one
@@ -1137,7 +1171,11 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots) {
   const int s = span_pos(u);
   if (live[u]) {
     float4 Pf = Pfu[u], Of = Ofu[u];
-    bool safe = Pf.x > e && Pf.x < R.boxf[0] - e && Pf.y > e && Pf.y < R.boxf[1] - e;
+    // no wrap (x >= box or x < 0, exact as in pbc_quiet; +0.0f rounds from
+    // x in [0, 2^-150], which needs none) and inside the tessellation in x, y
+    const bool sx = (Pf.x > 0.0f || __float_as_uint(Pf.x) == 0u) && Pf.x < R.boxf[0];
+    const bool sy = (Pf.y > 0.0f || __float_as_uint(Pf.y) == 0u) && Pf.y < R.boxf[1];
+    bool safe = sx && sy;
     if (safe && R.use_cells)
       safe = Pf.z > -2.0f * R.cellf[2] + e && Pf.z < R.tess_hif - e;
     if (!safe) {
@@ -4303,7 +4341,7 @@ void launch_force_scan(const Dev& d, const KParams& p, int n_rank, cudaStream_t 
   const int L = p.scan_lanes;
   const int nb = nblk_rows((n_rank + 32 / L - 1) / (32 / L));
   if (L == 1)
-    force_scan_kernel<NEAR, 1><<<nb, kBlock, 0, s>>>(d, p);
+    force_scan_span_kernel<NEAR><<<nspan(n_rank), kBlock, 0, s>>>(d, p);
   else if (L == 2)
     force_scan_kernel<NEAR, 2><<<nb, kBlock, 0, s>>>(d, p);
   else if (L == 4)
