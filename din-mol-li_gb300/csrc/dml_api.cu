@@ -632,7 +632,13 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   }
   d.cap = total;
   d.max_rep_cap = 0;
-  for (int r = 0; r < nrep; ++r) d.max_rep_cap = std::max(d.max_rep_cap, c->rc[r].cap);
+  d.gcmc_rows = 0;
+  for (int r = 0; r < nrep; ++r) {
+    const RepConst& R = c->rc[r];
+    d.max_rep_cap = std::max(d.max_rep_cap, R.cap);
+    // rows of gcmc_run's shared-memory sort; larger replicas run sequentially
+    if (R.use_cells) d.gcmc_rows = std::max(d.gcmc_rows, std::min(R.head_dim[1] * R.head_dim[2], 16384));
+  }
   d.ncell_tot = ncell;
   d.n_cch = n_cch;
   d.any_cells = any_cells;

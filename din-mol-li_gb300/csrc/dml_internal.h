@@ -271,6 +271,7 @@ struct Dev {
   int nrep;
   int cap;            // positions over all replicas (sum of the replica caps)
   int max_rep_cap;    // largest replica capacity
+  int gcmc_rows;      // most cell rows (z layer, y row) of a replica with cells
   int any_cells, any_verlet;  // some replica uses linked cells / the all-pairs build
 };
 

@@ -1508,15 +1508,22 @@ __device__ void cell_scan_range(const Dev& d, const RepConst& R, int c0, int c1,
   __syncthreads();
 }
 
+// The cell sort of gcmc_run on the device-wide cell arrays runs for the
+// replicas whose trials run sequentially (gcmc_kernel): their sorts only.
+__device__ __forceinline__ bool gcmc_sorts(const Dev& d, int rep, int par) {
+  return !par || !d.grp[rep].fast;
+}
+
 // The cell starts of one replica (one block per replica), from its first
 // position: its cell_atoms range is [base, base + cap).  A full sort covers
 // every cell and the sentinel after the last; the sort for gcmc_run covers
 // the runs of z layers its searches reach, each followed by its end.
-__global__ void cell_scan_kernel(Dev d, int force) {
+__global__ void cell_scan_kernel(Dev d, int force, int par) {
   const RepConst& R = d.rc[blockIdx.x];
   const Scalars* sc = d.sc + blockIdx.x;
   if (!R.use_cells) return;
   if (!force && !sc->rebuild) return;
+  if (force && !gcmc_sorts(d, blockIdx.x, par)) return;
   __shared__ int carry;
   if (threadIdx.x == 0) carry = R.base;
   __syncthreads();
@@ -1554,64 +1561,6 @@ __global__ void cell_scatter_kernel(Dev d, int n_b, int force) {
   for (int u = 0; u < kSlotU; ++u) cell_scatter_at(d, n_b, force, rep, span_pos(u));
 }
 
-// gcmc_run's cell sort, binning pass: every live atom's cell (coalesced
-// over hs slots, so no gather), the range check and the halo flag of
-// cgroup_sort_atom (Cells.F90:281-302) for all, the count and a list entry
-// (hs%b slot, cell) for the atoms of the z layers the trials can reach.
-__device__ __forceinline__ void gcmc_bin_at(const Dev& d, int rep, int pos) {
-  const RepConst& R = d.rc[rep];
-  Scalars* sc = d.sc + rep;
-  const int s = pos;
-  const int lane = threadIdx.x & 31;
-  int lin = -1;
-  if (R.use_cells && s < R.base + sc->n_slots && d.state[s] == ST_LIVE) {
-    int c1, c2, c3;
-    cell_index3(R, d.posf[s], d.pos + s, c1, c2, c3);
-    if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] + 1 || c2 > R.ncells[1] + 1 ||
-        c3 > R.ncells[2] + 1) {
-      raise_error(d.g, DML_E_OUT_OF_TESSELLATION, s);
-    } else {
-      // the 27-cell stencil never visits the halo: trials fall back to full scans
-      if (c1 == 0 || c2 == 0 || c3 == 0 || c1 > R.ncells[0] || c2 > R.ncells[1] ||
-          c3 > R.ncells[2])
-        sc->halo = 1;
-      if (R.gl_all || ((R.gl_cmask >> c3) & 1ull))
-        lin = R.cell_off + (c3 * R.head_dim[1] + c2) * R.head_dim[0] + c1;
-    }
-  }
-  const bool in = lin >= 0;
-  const unsigned m = __ballot_sync(0xffffffffu, in);
-  if (!m) return;
-  const int leader = __ffs(m) - 1;
-  int b = 0;
-  if (lane == leader) b = atomicAdd(d.pr_cnt + rep * kCntStride + kCntGlist, __popc(m));
-  b = __shfl_sync(0xffffffffu, b, leader);
-  if (!in) return;
-  atomicAdd(&d.cell_count[lin], 1);
-  d.glist[R.base + b + __popc(m & ((1u << lane) - 1u))] = make_int2(d.bslot[s], lin);
-}
-
-__global__ void gcmc_bin_kernel(Dev d) {
-  const int rep = block_rep(d);
-  if (blockIdx.x == 0 && threadIdx.x == 0) d.g->n_big = 0;  // cell_order's list
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) gcmc_bin_at(d, rep, span_pos(u));
-}
-
-// gcmc_run's cell sort, scatter pass over each replica's listed atoms.
-__global__ void gcmc_scatter_kernel(Dev d) {
-  const int rep = block_rep(d);
-  const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntGlist];
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) {
-    const int i = span_pos(u);
-    if (i < end) {
-      const int2 e = d.glist[i];
-      d.cell_atoms[d.cell_start[e.y] + atomicAdd(&d.cell_fill[e.y], 1)] = e.x;
-    }
-  }
-}
-
 // Orders each cell by descending hs%b slot: the chain order of
 // cgroup_sort (Cells.F90:267-302), which prepends slots in increasing order.
 // One warp per cell; the sorted cell goes to comp_members (scratch) and is
@@ -1643,14 +1592,13 @@ __device__ __forceinline__ void cell_order_cell(const Dev& d, int c) {
 // replicas that do not sort (and, for gcmc_run's sort, of z layers its
 // searches do not reach) are skipped whole.
 constexpr int kSmallCell = 16;
-__global__ void cell_order_small_kernel(Dev d, int force) {
+__global__ void cell_order_small_kernel(Dev d, int force, int par) {
   if (!force && !d.g->any_rebuild) return;
   const int rep = d.cch_rep[blockIdx.x];
   const RepConst& R = d.rc[rep];
   if (!R.use_cells) return;
-  // the gcmc_run sort's list has been scattered: empty it for the next sort
-  if (force && blockIdx.x == R.cch0 && threadIdx.x == 0) d.pr_cnt[rep * kCntStride + kCntGlist] = 0;
   if (!force && !d.sc[rep].rebuild) return;
+  if (force && !gcmc_sorts(d, rep, par)) return;
   const int c0 = (blockIdx.x - R.cch0) * kCellChunk;
   if (force && !R.gl_all) {
     const int layer = R.head_dim[0] * R.head_dim[1];
@@ -2554,6 +2502,195 @@ __device__ __forceinline__ bool in_slab(double z, double z0, double zmax) {
   return !(z < z0) && !(z > zmax);
 }
 
+// gcmc_run's preparation, one block per replica: the order arrays grow by
+// appends and are compacted before they could overflow; the listing of
+// gcmc_bin_kernel starts empty, the member bounds at their identities, and
+// the bit words past the used gcmc%alist positions (appends set bits there)
+// are cleared.
+__global__ void gcmc_prep_kernel(Dev d, KParams p, int par) {
+  const int rep = blockIdx.x;
+  const RepConst& R = d.rc[rep];
+  Scalars* const sc = d.sc + rep;
+  const int B = R.base, tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0) d.pr_cnt[rep * kCntStride + kCntGlist] = 0;
+  if (!sc->listed) return;  // gcmc_kernel reports the state error
+  if (sc->n_rank + p.nadj >= R.cap) {
+    int n = blk_compact(d.ref, B, sc->n_rank, d.rank);
+    if (tid == 0) sc->n_rank = n;
+    __syncthreads();
+  }
+  if (sc->n_alist + p.nadj >= R.cap) {
+    int n = blk_compact(d.alist, B, sc->n_alist, d.apos);
+    if (tid == 0) sc->n_alist = n;
+    __syncthreads();
+  }
+  if (sc->n_gorder + p.nadj >= R.cap) {
+    int n = blk_compact(d.gorder, B, sc->n_gorder, d.gpos);
+    if (tid == 0) sc->n_gorder = n;
+    __syncthreads();
+  }
+  if (!par) return;
+  const int ng = sc->n_gorder;
+  GcmcRepPre* const gr = d.grp + rep;
+  if (tid == 0) {
+    gr->first = INT_MAX;
+    gr->last = -1;
+    gr->n_in = 0;
+    gr->ng = ng;
+  }
+  unsigned* wm = d.gw_mem + B / 32;
+  unsigned* wsl = d.gw_slab + B / 32;
+  const int w0 = (ng + 31) >> 5, w1 = min((ng + p.nadj + 64) >> 5, R.cap >> 5);
+  for (int w = w0 + tid; w < w1; w += nt) {
+    wm[w] = 0u;
+    wsl[w] = 0u;
+  }
+}
+
+// in_slab(z) of an atom from z's FP32 copy zf = RN32(z): rounding is
+// monotone, so zf beyond RN32 of a bound decides the comparison; zf equal to
+// it (or NaN) takes the FP64 coordinate.
+__device__ __forceinline__ bool in_slab_at(const Dev& d, int h, float zf, float z0f, float zmaxf,
+                                           double z0, double zmax) {
+  if (zf > z0f && zf < zmaxf) return true;
+  if (zf < z0f || zf > zmaxf) return false;
+  return in_slab(d.pos[h].z, z0, zmax);
+}
+
+// gcmc_run's cell sort, binning pass: every live atom's cell (coalesced
+// over hs slots, so no gather), the range check and the halo flag of
+// cgroup_sort_atom (Cells.F90:281-302) for all, and a list entry (hs slot,
+// cell) for the atoms of the z layers the trials can reach.
+__device__ __forceinline__ void gcmc_bin_at(const Dev& d, int rep, int pos) {
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  const int s = pos;
+  const int lane = threadIdx.x & 31;
+  int lin = -1;
+  if (R.use_cells && s < R.base + sc->n_slots && d.state[s] == ST_LIVE) {
+    int c1, c2, c3;
+    cell_index3(R, d.posf[s], d.pos + s, c1, c2, c3);
+    if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] + 1 || c2 > R.ncells[1] + 1 ||
+        c3 > R.ncells[2] + 1) {
+      raise_error(d.g, DML_E_OUT_OF_TESSELLATION, s);
+    } else {
+      // the 27-cell stencil never visits the halo: trials fall back to full scans
+      if (c1 == 0 || c2 == 0 || c3 == 0 || c1 > R.ncells[0] || c2 > R.ncells[1] ||
+          c3 > R.ncells[2])
+        sc->halo = 1;
+      if (R.gl_all || ((R.gl_cmask >> c3) & 1ull))
+        lin = R.cell_off + (c3 * R.head_dim[1] + c2) * R.head_dim[0] + c1;
+    }
+  }
+  const bool in = lin >= 0;
+  const unsigned m = __ballot_sync(0xffffffffu, in);
+  if (!m) return;
+  const int leader = __ffs(m) - 1;
+  int b = 0;
+  if (lane == leader) b = atomicAdd(d.pr_cnt + rep * kCntStride + kCntGlist, __popc(m));
+  b = __shfl_sync(0xffffffffu, b, leader);
+  if (!in) return;
+  d.glist[R.base + b + __popc(m & ((1u << lane) - 1u))] = make_int2(s, lin);
+}
+
+// The membership and in-slab bits of the gcmc%alist positions [0, ng) for
+// the parallel trials (one word per warp: positions of a warp are 32
+// aligned consecutive ones), the first and last member and the
+// control-volume count (dana.F90:601-606), reduced over the block.
+__device__ __forceinline__ void gcmc_member_words(const Dev& d, int rep) {
+  const RepConst& R = d.rc[rep];
+  const Scalars* sc = d.sc + rep;
+  GcmcRepPre* const gr = d.grp + rep;
+  const int B = R.base, lane = threadIdx.x & 31;
+  const int ng = gr->ng;
+  __shared__ int s_lo, s_hi, s_cnt;
+  if (threadIdx.x == 0) {
+    s_lo = INT_MAX;
+    s_hi = -1;
+    s_cnt = 0;
+  }
+  __syncthreads();
+  if ((int)blockIdx.x * kSpan - B < ng) {
+    const double z0 = sc->z0, zmax = sc->zmax;
+    const float z0f = (float)z0, zmaxf = (float)zmax;
+    int h[kSlotU];
+#pragma unroll
+    for (int u = 0; u < kSlotU; ++u) {
+      const int i = span_pos(u) - B;
+      h[u] = i < ng ? d.gorder[B + i] : -1;
+    }
+    float zf[kSlotU];
+#pragma unroll
+    for (int u = 0; u < kSlotU; ++u) zf[u] = h[u] >= 0 ? d.posf[h[u]].z : 0.0f;
+    int lo = INT_MAX, hi = -1, cnt = 0;
+#pragma unroll
+    for (int u = 0; u < kSlotU; ++u) {
+      const int i = span_pos(u) - B;
+      const bool mem = h[u] >= 0;
+      const bool in = mem && in_slab_at(d, h[u], zf[u], z0f, zmaxf, z0, zmax);
+      const unsigned bm = __ballot_sync(0xffffffffu, mem);
+      const unsigned bs = __ballot_sync(0xffffffffu, in);
+      if (lane == 0 && i < ng) {
+        d.gw_mem[(B + i) >> 5] = bm;
+        d.gw_slab[(B + i) >> 5] = bs;
+      }
+      if (bm) {
+        lo = min(lo, i - lane + __ffs(bm) - 1);
+        hi = max(hi, i - lane + 31 - __clz(bm));
+      }
+      cnt += __popc(bs);
+    }
+    if (lane == 0 && hi >= 0) {
+      atomicMin(&s_lo, lo);
+      atomicMax(&s_hi, hi);
+      atomicAdd(&s_cnt, cnt);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && s_hi >= 0) {
+    atomicMin(&gr->first, s_lo);
+    atomicMax(&gr->last, s_hi);
+    atomicAdd(&gr->n_in, s_cnt);
+  }
+}
+
+__global__ void gcmc_bin_kernel(Dev d, int par) {
+  const int rep = block_rep(d);
+  if (blockIdx.x == 0 && threadIdx.x == 0) d.g->n_big = 0;  // cell_order's list
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) gcmc_bin_at(d, rep, span_pos(u));
+  if (par) gcmc_member_words(d, rep);
+}
+
+// The cell counts of the sequentially run replicas' listed atoms.
+__global__ void gcmc_count_kernel(Dev d, int par) {
+  const int rep = block_rep(d);
+  if (!gcmc_sorts(d, rep, par)) return;
+  const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntGlist];
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) {
+    const int i = span_pos(u);
+    if (i < end) atomicAdd(&d.cell_count[d.glist[i].y], 1);
+  }
+}
+
+// Scatter pass over each sorting replica's listed atoms (cell_atoms holds
+// hs%b slots until cell_order turns them into hs slots).
+__global__ void gcmc_scatter_kernel(Dev d, int par) {
+  const int rep = block_rep(d);
+  if (!gcmc_sorts(d, rep, par)) return;
+  const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntGlist];
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) {
+    const int i = span_pos(u);
+    if (i < end) {
+      const int2 e = d.glist[i];
+      d.cell_atoms[d.cell_start[e.y] + atomicAdd(&d.cell_fill[e.y], 1)] = d.bslot[e.x];
+    }
+  }
+}
+
+
 // One trial of gcmc_run: its uniforms (coin, acceptance, the three
 // coordinates, the pick) and trial point, drawn before the trials run.
 struct GcmcTrial {
@@ -3224,6 +3361,18 @@ __device__ int blk_collect(int lo, int hi, int want, Pred free_at, int* out, int
   return n;
 }
 
+// Candidate records of one creation trial (per warp): stencil index and
+// hs%b slot as one ordering key, the atom, its list flags.
+struct GcmcCandRec {
+  unsigned long long key[kGcmcCand];
+  int j[kGcmcCand];
+  unsigned char fl[kGcmcCand];
+};
+
+// Dynamic shared memory of gcmc_pre_kernel: the row ends of the cell-row
+// sort, then the sorted hs slots.
+__host__ __device__ constexpr int gcmc_pre_sort_cap() { return 12288; }
+
 __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParams p) {
   const int rep = blockIdx.x;
   const RepConst& R = d.rc[rep];
@@ -3231,38 +3380,31 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
   GcmcRepPre* const gr = d.grp + rep;
   const int B = R.base, tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
   const int nw = nt >> 5;
+  const unsigned lt = (1u << lane) - 1u;
   __shared__ int s_bad, s_cnt, s_ncrt;
-  __shared__ int s_lo, s_hi, s_nin;
   __shared__ double4 s_r[kGcmcMaxTrials];
   __shared__ float4 s_rf[kGcmcMaxTrials];
   __shared__ unsigned char s_crt[kGcmcMaxTrials];
-  __shared__ int s_tab[kGcmcPreThreads / 32][56];  // per warp: stencil cell starts and prefixes
+  __shared__ int s_tab[kGcmcPreThreads / 32][56];  // per warp: stencil cells, row segments
+  __shared__ int s_nb[kGcmcPreThreads / 32], s_nc[kGcmcPreThreads / 32];
+  __shared__ GcmcCandRec s_rec[kGcmcPreThreads / 32];
+  extern __shared__ int s_pre_dyn[];
+  int* const rowend = s_pre_dyn;
+  int* const sorted = s_pre_dyn + d.gcmc_rows;
   if (!sc->listed) {  // gcmc_kernel reports the state error
     if (tid == 0) gr->fast = 0;
     return;
   }
-  // order arrays grow by appends: compact them before they could overflow
-  if (sc->n_rank + p.nadj >= R.cap) {
-    int n = blk_compact(d.ref, B, sc->n_rank, d.rank);
-    if (tid == 0) sc->n_rank = n;
-    __syncthreads();
-  }
-  if (sc->n_alist + p.nadj >= R.cap) {
-    int n = blk_compact(d.alist, B, sc->n_alist, d.apos);
-    if (tid == 0) sc->n_alist = n;
-    __syncthreads();
-  }
-  if (sc->n_gorder + p.nadj >= R.cap) {
-    int n = blk_compact(d.gorder, B, sc->n_gorder, d.gpos);
-    if (tid == 0) sc->n_gorder = n;
-    __syncthreads();
-  }
+  const int nrows = R.head_dim[1] * R.head_dim[2];
+  const int n_gl = d.pr_cnt[rep * kCntStride + kCntGlist];
   if (tid == 0) {
-    s_bad = !(R.use_cells && !sc->halo && p.nadj <= kGcmcMaxTrials);
+    s_bad = !(R.use_cells && !sc->halo && p.nadj <= kGcmcMaxTrials &&
+              n_gl <= gcmc_pre_sort_cap() && nrows <= d.gcmc_rows);
     s_ncrt = 0;
-    s_lo = INT_MAX;
-    s_hi = -1;
-    s_nin = 0;
+  }
+  if (tid < kGcmcPreThreads / 32) {
+    s_nb[tid] = 0;
+    s_nc[tid] = 0;
   }
   __syncthreads();
   if (s_bad) {
@@ -3271,62 +3413,8 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
   }
   const long long step = d.g->step;
   const double z0 = sc->z0, zmax = sc->zmax;
-  const int ng = sc->n_gorder;
   GcmcTrialPre* const pre = d.gpre + (size_t)rep * kGcmcMaxTrials;
   unsigned* const pm = d.gpm + (size_t)rep * kGcmcMaxTrials * kGcmcMaskW;
-
-  // Membership and in-slab bits of the gcmc%alist positions [0, ng), the
-  // first and last member and the control-volume count (dana.F90:601-606).
-  {
-    unsigned* wm = d.gw_mem + B / 32;
-    unsigned* wsl = d.gw_slab + B / 32;
-    int lo = INT_MAX, hi = -1, cnt = 0;
-    constexpr int U = 4;  // positions per thread per round, loads in flight together
-    for (int base = 0; base < ng; base += U * nt) {
-      int h[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int i = base + u * nt + tid;
-        h[u] = i < ng ? d.gorder[B + i] : -1;
-      }
-      double zz[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) zz[u] = h[u] >= 0 ? d.pos[h[u]].z : 0.0;
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int i = base + u * nt + tid;
-        const bool mem = h[u] >= 0;
-        const bool in = mem && in_slab(zz[u], z0, zmax);
-        const unsigned bm = __ballot_sync(0xffffffffu, mem);
-        const unsigned bs = __ballot_sync(0xffffffffu, in);
-        if (lane == 0 && i < ng) {
-          wm[i >> 5] = bm;
-          wsl[i >> 5] = bs;
-        }
-        if (mem) {
-          lo = min(lo, i);
-          hi = max(hi, i);
-        }
-        cnt += in;
-      }
-    }
-    // words past the used positions start empty (appends set their bits)
-    const int w0 = (ng + 31) >> 5, w1 = min((ng + p.nadj + 64) >> 5, R.cap >> 5);
-    for (int w = w0 + tid; w < w1; w += nt) {
-      wm[w] = 0u;
-      wsl[w] = 0u;
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-      lo = min(lo, __shfl_down_sync(0xffffffffu, lo, off));
-      hi = max(hi, __shfl_down_sync(0xffffffffu, hi, off));
-      cnt += __shfl_down_sync(0xffffffffu, cnt, off);
-    }
-    if (lane == 0) {
-      atomicMin(&s_lo, lo);
-      atomicMax(&s_hi, hi);
-      atomicAdd(&s_nin, cnt);
-    }
-  }
 
   // The trials' draws (dana.F90:620-690, keyed Philox) and points.
   if (tid < p.nadj) {
@@ -3340,7 +3428,7 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
     const double r1 = dml_u53(w1.w[2], w1.w[3]) * R.box[1];
     const double r2 = dml_u53(w2.w[0], w2.w[1]) * (zmax - z0) + z0;
     const double4 r = make_double4(r0, r1, r2, 0.0);
-    const float4 rf = make_float4((float)r0, (float)r1, (float)r2, 0.0f);
+    const float4 rf = to_f4(r, 0);
     tr.r = r;
     tr.coin = coin;
     tr.uacc = dml_u53(w0.w[2], w0.w[3]);
@@ -3367,6 +3455,32 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
       tr.cell = R.cell_off + (c3 * R.head_dim[1] + c2) * R.head_dim[0] + c1;
     }
   }
+  // The atoms gcmc_bin_kernel listed (live, in the layers the trials reach),
+  // counting-sorted by cell row (z layer, y row) in shared memory: row r's
+  // hs slots are sorted[rowend[r - 1] .. rowend[r]) (from 0 for r = 0).
+  const int hd0 = R.head_dim[0];
+  for (int r = tid; r < nrows; r += nt) rowend[r] = 0;
+  __syncthreads();
+  const int2* const gl = d.glist + B;
+  for (int i = tid; i < n_gl; i += nt) atomicAdd(&rowend[(gl[i].y - R.cell_off) / hd0], 1);
+  __syncthreads();
+  {
+    const int per = (nrows + nt - 1) / nt, r0 = tid * per, r1 = min(r0 + per, nrows);
+    int sum = 0;
+    for (int r = r0; r < r1; ++r) sum += rowend[r];
+    int tot;
+    int run = blk_scan_excl(sum, &tot);
+    for (int r = r0; r < r1; ++r) {
+      const int c = rowend[r];
+      rowend[r] = run;  // the row's start, advanced to its end by the scatter
+      run += c;
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < n_gl; i += nt) {
+    const int2 e = gl[i];
+    sorted[atomicAdd(&rowend[(e.y - R.cell_off) / hd0], 1)] = e.x;
+  }
   __syncthreads();
 
   // Earlier creation points within rc of each creation point: an accepted
@@ -3385,91 +3499,118 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
     for (int w = 0; w < kGcmcMaskW; ++w) pm[tid * kGcmcMaskW + w] = m[w];
   }
 
-  // Blockers and list candidates of every creation trial, one warp each,
-  // over the 27 stencil cells of the cell sort of this call.
-  int* tab = s_tab[wid];
+  // Blockers and list candidates of every creation trial, one warp each:
+  // the atoms of the (at most 9) cell rows through its 27 stencil cells
+  // within rc + skin (FP32, FP64 inside the margins), each matched to the
+  // stencil cells holding it; the candidates then in the order of the
+  // stencil walk (map order, each cell by descending hs%b slot).
+  int* const wc = s_tab[wid];        // [0, 27): the stencil cells
+  int* const segst = s_tab[wid] + 27;  // [0, 9): row segment starts in sorted[]
+  int* const segpre = s_tab[wid] + 36; // [0, 10): exclusive prefix of their sizes
+  int* const segrow = s_tab[wid] + 46; // [0, 9): the rows
+  GcmcCandRec& rec = s_rec[wid];
   for (int i = wid; i < p.nadj; i += nw) {
     if (!s_crt[i]) continue;
     GcmcTrialPre& tr = pre[i];
     const double4 Rt = s_r[i];
     const float4 Rtf = s_rf[i];
-    int num = 0, c = -1;
+    int c = -1;
     if (lane < 27) {
       c = stencil_cell(R, Rtf, &Rt, lane);
-      const int st = d.cell_start[c];
-      num = d.cell_start[c + 1] - st;
-      tab[lane] = st;
       tr.cells[lane] = c;
+      wc[lane] = c;
     }
-    bool dupl = false;
+    const int row = lane < 27 ? (c - R.cell_off) / hd0 : -1;
+    bool dupl = false, rdup = false;
     for (int q = 0; q < 26; ++q) {
       const int cq = __shfl_sync(0xffffffffu, c, q);
+      const int rq = __shfl_sync(0xffffffffu, row, q);
       if (q < lane && cq == c) dupl = true;
+      if (q < lane && rq == row) rdup = true;
     }
     const unsigned dupm = __ballot_sync(0xffffffffu, lane < 27 && dupl);
-    int x = num;
+    const unsigned rm = __ballot_sync(0xffffffffu, lane < 27 && !rdup);
+    const int nseg = __popc(rm);
+    // the distinct rows compacted to lanes [0, nseg): start and size
+    if (lane < 27 && !rdup) segrow[__popc(rm & lt)] = row;
+    __syncwarp();
+    int ssz = 0;
+    if (lane < nseg) {
+      const int r = segrow[lane];
+      const int st = r > 0 ? rowend[r - 1] : 0;
+      segst[lane] = st;
+      ssz = rowend[r] - st;
+    }
+    int x = ssz;
     for (int o = 1; o < 32; o <<= 1) {
       const int y = __shfl_up_sync(0xffffffffu, x, o);
       if (lane >= o) x += y;
     }
-    if (lane < 27) tab[27 + lane] = x - num;
-    const int T = __shfl_sync(0xffffffffu, x, 26);
+    if (lane < nseg) segpre[lane] = x - ssz;
+    const int T = nseg > 0 ? __shfl_sync(0xffffffffu, x, nseg - 1) : 0;
     __syncwarp();
-    int nb = 0, nc = 0;
     for (int base = 0; base < T; base += 32) {
       const int f = base + lane;
-      bool isb = false, isc = false;
-      int j = -1, q = 0, fl = 0;
       if (f < T) {
-        int lo = 0, hi = 26;  // stencil cell holding f
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (tab[27 + mid] <= f) lo = mid; else hi = mid - 1;
-        }
-        q = lo;
-        j = d.cell_atoms[tab[q] + f - tab[27 + q]];
+        int k = 0;
+        while (k + 1 < nseg && segpre[k + 1] <= f) ++k;
+        const int j = sorted[segst[k] + f - segpre[k]];
         const float4 Q = d.posf[j];
         float fx, fy, fz;
         vdist_nint_f(R, Rtf, Q, fx, fy, fz);
         const float df = fx * fx + fy * fy + fz * fz;
         if (df <= R.rlist_hi2) {
-          double rd = -1.0;
-          if (!(df < R.rc_lo2 && df < R.rlist_lo2)) {
+          // its cell in the cell sort, matched against the stencil below
+          int a1, a2, a3;
+          cell_index3(R, Q, d.pos + j, a1, a2, a3);
+          const int lin = R.cell_off + (a3 * R.head_dim[1] + a2) * hd0 + a1;
+          const bool mem = d.in_gcmc[j] != 0;
+          double rd = -1.0;  // FP64 only inside the margins of rc and rc + skin
+          if (df >= R.rlist_lo2 || (mem && df >= R.rc_lo2 && df <= R.rc_hi2)) {
             double vx, vy, vz;
             vdist_nint(R, Rt, d.pos[j], vx, vy, vz);
             rd = dot3(vx, vy, vz);
           }
-          if (df <= R.rc_hi2 && d.in_gcmc[j] && (df < R.rc_lo2 || rd < p.rc2)) isb = true;
-          const bool live = d.state[j] == ST_LIVE;
+          const bool isb = df <= R.rc_hi2 && mem && (df < R.rc_lo2 || rd < p.rc2);
           const bool own = df < R.rlist_lo2 || rd < p.rlist2;
-          const bool app = df < R.rlist_lo2 || !(rd > p.rlist2);
-          if (live && own) fl |= 1;
-          if (live && app && !((dupm >> q) & 1u) && d.rank[j] >= 0) fl |= 2;
-          isc = fl != 0;
+          const bool app = (df < R.rlist_lo2 || !(rd > p.rlist2)) && d.rank[j] >= 0;
+          for (int q = 0; q < 27; ++q) {
+            if (wc[q] != lin) continue;
+            if (isb) {
+              const int kb = atomicAdd(&s_nb[wid], 1);
+              if (kb < kGcmcBlk) tr.blk[kb] = d.gpos[j] - B;
+            }
+            const int fl = (own ? 1 : 0) | (app && !((dupm >> q) & 1u) ? 2 : 0);
+            if (fl) {
+              const int kc = atomicAdd(&s_nc[wid], 1);
+              if (kc < kGcmcCand) {
+                rec.key[kc] = ((unsigned long long)q << 32) | (unsigned)~d.bslot[j];
+                rec.j[kc] = j;
+                rec.fl[kc] = (unsigned char)fl;
+              }
+            }
+          }
         }
       }
-      const unsigned bb = __ballot_sync(0xffffffffu, isb);
-      const unsigned bc = __ballot_sync(0xffffffffu, isc);
-      if (isb) {
-        const int k = nb + __popc(bb & ((1u << lane) - 1u));
-        if (k < kGcmcBlk) tr.blk[k] = d.gpos[j] - B;
-      }
-      if (isc) {
-        const int k = nc + __popc(bc & ((1u << lane) - 1u));
-        if (k < kGcmcCand) {
-          tr.cand[k] = j;
-          tr.cq[k] = (unsigned char)q;
-          tr.cf[k] = (unsigned char)fl;
-        }
-      }
-      nb += __popc(bb);
-      nc += __popc(bc);
     }
+    __syncwarp();
+    const int nb = s_nb[wid], nc = s_nc[wid], nk = min(nc, kGcmcCand);
+    for (int k = lane; k < nk; k += 32) {
+      const unsigned long long key = rec.key[k];
+      int rank = 0;
+      for (int m = 0; m < nk; ++m) rank += rec.key[m] < key;
+      tr.cand[rank] = rec.j[k];
+      tr.cq[rank] = (unsigned char)(key >> 32);
+      tr.cf[rank] = rec.fl[k];
+    }
+    __syncwarp();
     if (lane == 0) {
       tr.n_blk = nb;
       tr.n_cand = nc;
       tr.dup = dupm;
       if (nb > kGcmcBlk || nc > kGcmcCand) s_bad = 1;
+      s_nb[wid] = 0;
+      s_nc[wid] = 0;
     }
     __syncwarp();
   }
@@ -3494,10 +3635,6 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
   if (tid == 0) {
     gr->n_holes = nh;
     gr->n_bholes = nbh;
-    gr->n_in = s_nin;
-    gr->first = s_lo;
-    gr->last = s_hi;
-    gr->ng = ng;
     gr->fast = !s_bad;
   }
 }
@@ -4418,9 +4555,9 @@ int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, 
   rebuild_prep_kernel<<<nspan(nmax), kBlock, 0, s>>>(d, p, n_slots, n_b, 0);
   int n = 1;
   if (d.any_cells) {
-    cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 0);
+    cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 0, 0);
     cell_scatter_kernel<<<nspan(n_b), kBlock, 0, s>>>(d, n_b, 0);
-    cell_order_small_kernel<<<d.n_cch > 0 ? d.n_cch : 1, kBlock, 0, s>>>(d, 0);
+    cell_order_small_kernel<<<d.n_cch > 0 ? d.n_cch : 1, kBlock, 0, s>>>(d, 0, 0);
     cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 0);
     list_cells_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, n_rank);
     n += 5;
@@ -4493,43 +4630,72 @@ int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
   return 1;
 }
 
-// gcmc_run's searches need the cells of the current positions.
+// Whether gcmc_run's trials take the parallel path (gcmc_pre_kernel and
+// gcmc_fast_kernel, for the replicas that qualify), with the dynamic shared
+// memory of gcmc_fast_kernel and whether its bit words fit there.
+struct GcmcLaunch {
+  int par, wmax, gmax, words_smem;
+  size_t fshm, pshm;
+};
+static GcmcLaunch gcmc_launch(const Dev& d, const KParams& p) {
+  GcmcLaunch L;
+  static_assert(sizeof(GcmcSm) <= 100 * 1024, "gcmc_fast_kernel shared state");
+  L.wmax = d.max_rep_cap / 32;
+  L.gmax = (L.wmax + 31) / 32 + 1;
+  L.fshm = sizeof(GcmcSm) + sizeof(int) * (size_t)L.gmax;
+  L.words_smem = L.fshm + 2 * sizeof(unsigned) * (size_t)L.wmax <= 200 * 1024;
+  if (L.words_smem) L.fshm += 2 * sizeof(unsigned) * (size_t)L.wmax;
+  L.pshm = sizeof(int) * ((size_t)d.gcmc_rows + gcmc_pre_sort_cap());
+  L.par = d.gpre != nullptr && d.grp != nullptr && p.nadj <= kGcmcMaxTrials &&
+          L.fshm <= 220 * 1024 && d.gcmc_rows > 0;
+  return L;
+}
+
+// gcmc_run's searches need the cells of the current positions: the
+// preparation, then the listing of the atoms the trials can reach (and the
+// parallel path's bit words).
 int k_gcmc_cells(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
   if (!d.any_cells) return 0;
-  (void)p;
-  gcmc_bin_kernel<<<nspan(cap), kBlock, 0, s>>>(d);
-  cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1);
-  gcmc_scatter_kernel<<<nspan(cap), kBlock, 0, s>>>(d);
-  cell_order_small_kernel<<<d.n_cch > 0 ? d.n_cch : 1, kBlock, 0, s>>>(d, 1);
-  cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 1);
-  return 5;
+  const GcmcLaunch L = gcmc_launch(d, p);
+  gcmc_prep_kernel<<<d.nrep, 512, 0, s>>>(d, p, L.par);
+  gcmc_bin_kernel<<<nspan(cap), kBlock, 0, s>>>(d, L.par);
+  return 2;
 }
 
 int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s) {
   return k_gcmc_cells(d, p, cap, s) + k_gcmc_trials(d, p, s);
 }
 
+// The trials: on the parallel path the per-replica searches, then the cell
+// sort of the replicas that run sequentially (all of them otherwise), the
+// parallel decisions and the sequential gcmc_kernel.
 int k_gcmc_trials(const Dev& d, const KParams& p, cudaStream_t s) {
   int n = 0;
-  // the parallel path: shared state, in-slab counts and (if they fit) the bit words
-  static_assert(sizeof(GcmcSm) <= 100 * 1024, "gcmc_fast_kernel shared state");
-  const int wmax = d.max_rep_cap / 32, gmax = (wmax + 31) / 32 + 1;
-  size_t fshm = sizeof(GcmcSm) + sizeof(int) * (size_t)gmax;
-  const int words_smem = fshm + 2 * sizeof(unsigned) * (size_t)wmax <= 200 * 1024;
-  if (words_smem) fshm += 2 * sizeof(unsigned) * (size_t)wmax;
-  const int par = d.gpre != nullptr && d.grp != nullptr && p.nadj <= kGcmcMaxTrials &&
-                  fshm <= 220 * 1024;
-  if (par) {
-    cudaFuncSetAttribute(gcmc_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fshm);
-    gcmc_pre_kernel<<<d.nrep, kGcmcPreThreads, 0, s>>>(d, p);
-    gcmc_fast_kernel<<<d.nrep, kGcmcFastThreads, fshm, s>>>(d, p, wmax, gmax, words_smem);
-    n += 2;
+  const GcmcLaunch L = gcmc_launch(d, p);
+  if (L.par) {
+    cudaFuncSetAttribute(gcmc_pre_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.pshm);
+    gcmc_pre_kernel<<<d.nrep, kGcmcPreThreads, L.pshm, s>>>(d, p);
+    n += 1;
+  }
+  if (d.any_cells) {
+    const int cap = d.cap;
+    gcmc_count_kernel<<<nspan(cap), kBlock, 0, s>>>(d, L.par);
+    cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1, L.par);
+    gcmc_scatter_kernel<<<nspan(cap), kBlock, 0, s>>>(d, L.par);
+    cell_order_small_kernel<<<d.n_cch > 0 ? d.n_cch : 1, kBlock, 0, s>>>(d, 1, L.par);
+    cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 1);
+    n += 5;
+  }
+  if (L.par) {
+    cudaFuncSetAttribute(gcmc_fast_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.fshm);
+    gcmc_fast_kernel<<<d.nrep, kGcmcFastThreads, L.fshm, s>>>(d, p, L.wmax, L.gmax, L.words_smem);
+    n += 1;
   }
   size_t shm = sizeof(GcmcTrial) * (size_t)kGcmcTrialBatch +
                sizeof(int) * (size_t)(d.max_rep_cap / kGcmcThreads + 2);
   if (shm > 48 * 1024)
     cudaFuncSetAttribute(gcmc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
-  gcmc_kernel<<<d.nrep, kGcmcThreads, shm, s>>>(d, p, par);
+  gcmc_kernel<<<d.nrep, kGcmcThreads, shm, s>>>(d, p, L.par);
   return n + 1;
 }
 
