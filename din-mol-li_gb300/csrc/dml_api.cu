@@ -726,6 +726,8 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     AL(d.grp, nrep);
     AL(d.gpre, par ? (size_t)nrep * kGcmcMaxTrials : 1);
     AL(d.gpm, par ? (size_t)nrep * kGcmcMaxTrials * kGcmcMaskW : 1);
+    AL(d.glp, par ? (size_t)cap : 1);
+    AL(d.gsort, par ? (size_t)cap : 1);
     AL(d.gw_mem, par ? (size_t)cap / 32 : 1);
     AL(d.gw_slab, par ? (size_t)cap / 32 : 1);
   }
@@ -1100,6 +1102,27 @@ int dml_check_conversions(const double* x, int64_t n, float* f32, double* back) 
   cudaFree(dx);
   cudaFree(db);
   cudaFree(df);
+  return e == cudaSuccess ? 0 : DML_E_CUDA;
+}
+
+int dml_check_pick(const uint64_t* k, const int32_t* n, int64_t count, int32_t* m) {
+  if (count < 0 || (count > 0 && (!k || !n || !m))) return DML_E_ARG;
+  if (count == 0) return 0;
+  unsigned long long* dk = nullptr;
+  int *dn = nullptr, *dm = nullptr;
+  cudaError_t e = cudaMalloc(&dk, sizeof(unsigned long long) * count);
+  if (e == cudaSuccess) e = cudaMalloc(&dn, sizeof(int) * count);
+  if (e == cudaSuccess) e = cudaMalloc(&dm, sizeof(int) * count);
+  if (e == cudaSuccess) e = cudaMemcpy(dk, k, sizeof(unsigned long long) * count, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dn, n, sizeof(int) * count, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_check_pick(dk, dn, dm, count, 0);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(m, dm, sizeof(int) * count, cudaMemcpyDeviceToHost);
+  cudaFree(dk);
+  cudaFree(dn);
+  cudaFree(dm);
   return e == cudaSuccess ? 0 : DML_E_CUDA;
 }
 

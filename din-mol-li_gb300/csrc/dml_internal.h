@@ -197,6 +197,7 @@ constexpr int kGcmcCand = 48;        // atoms within rc + skin of a trial point 
 struct GcmcTrialPre {
   double4 r;                 // trial point (dana.F90:643-645)
   double coin, uacc, upick;  // the trial's uniforms (dana.F90:627-686)
+  unsigned long long kpick;  // upick * 2^53 (the 53-bit integer it is made of)
   double nv[3];              // Maxwell normals of an insertion (dana.F90:666-668)
   int cell;                  // linear cell of the point
   int n_blk;                 // gcmc members within rc (their gcmc%alist positions)
@@ -207,6 +208,7 @@ struct GcmcTrialPre {
   int cand[kGcmcCand];       // hs slots
   unsigned char cq[kGcmcCand];  // stencil index of the candidate
   unsigned char cf[kGcmcCand];  // 1: own list (rd < (rc+skin)^2), 2: append (rd <= ...)
+  unsigned ckey[kGcmcCand];     // ~hs%b slot of the candidate (its order within a cell)
 };
 
 struct GcmcRepPre {
@@ -244,8 +246,10 @@ struct Dev {
   int *near_count, *near, *uf, *comp_size, *comp_id, *comp_rank, *comp_fill, *comp_members, *comp_list;
   int* act_list;      // ranks of the hs%ref members with a near contact this step, replica
                       // r's at [base, base + pr_cnt[r * kCntStride + kCntAct])
-  int2* glist;        // gcmc_run's cell sort: (hs%b slot, cell) of the atoms within reach,
+  int2* glist;        // gcmc_run's cell sort: (hs slot, cell) of the atoms within reach,
                       // replica r's entries at [base, base + pr_cnt[r * kCntStride + kCntGlist])
+  float4* glp;        // the same entries' FP32 positions, w = hs slot (integer bits)
+  float4* gsort;      // glp ordered by cell row (gcmc_pre_kernel), replica r's from base
   int* pr_cnt;        // per-replica list counters, one 128-byte line per replica (kept
                       // apart from the replica scalars that every block reads)
   // reductions
@@ -289,6 +293,7 @@ struct LoadIn {
 // ---- kernel launchers (dml_kernels.cu); each returns the kernels it queued ----
 int k_load_atoms(const Dev& d, const KParams& p, const LoadIn& in, cudaStream_t s);
 int k_check_conversions(const double* x, float* f32, double* back, long long n, cudaStream_t s);
+int k_check_pick(const unsigned long long* k, const int* n, int* m, long long count, cudaStream_t s);
 int k_step_begin(const Dev& d, int near_stale, cudaStream_t s);
 int k_rank_prefix(const Dev& d, cudaStream_t s);
 int k_ermak_a(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);

@@ -21,11 +21,26 @@ namespace dml {
 
 namespace {
 
-__constant__ int c_map[27][3] = {
-    {0, 0, 0},   {1, 0, 0},   {1, 1, 0},    {0, 1, 0},   {-1, 1, 0},  {1, 0, -1}, {1, 1, -1},
-    {0, 1, -1},  {-1, 1, -1}, {1, 0, 1},    {1, 1, 1},   {0, 1, 1},   {-1, 1, 1}, {0, 0, 1},
-    {-1, 0, 0},  {-1, -1, 0}, {0, -1, 0},   {1, -1, 0},  {-1, 0, 1},  {-1, -1, 1}, {0, -1, 1},
-    {1, -1, 1},  {-1, 0, -1}, {-1, -1, -1}, {0, -1, -1}, {1, -1, -1}, {0, 0, -1}};
+// The 27-cell stencil map of the linked cells (Cells.F90:28-36): offset of
+// cell q along axis k in {-1, 0, 1}, packed as 2 bits (offset + 1) per cell
+// in immediates, so that lanes asking for different cells read no memory
+// (a constant-bank read with lane-dependent addresses serializes).
+__device__ __forceinline__ int map_off(int q, int k) {
+  const unsigned long long w = k == 0 ? 0x19090904686869ull
+                               : k == 1 ? 0x10101016a6a6a5ull
+                                        : 0xaa55aa80155ull;
+  return (int)((w >> (2 * q)) & 3ull) - 1;
+}
+
+// Stencil index of the cell at offset (o1, o2, o3) in {-1, 0, 1}^3: the
+// inverse of map_off, entry (o1 + 1) * 9 + (o2 + 1) * 3 + o3 + 1, 5 bits each.
+__device__ __forceinline__ int map_inv(int o1, int o2, int o3) {
+  const int i = (o1 + 1) * 9 + (o2 + 1) * 3 + o3 + 1;
+  const unsigned long long w = i < 12 ? 0xa430c2224eb4df7ull
+                               : i < 24 ? 0x484b58e5633b41aull
+                                        : 0x2846ull;
+  return (int)((w >> (5 * (i % 12))) & 31ull);
+}
 
 __device__ __forceinline__ void raise_error(Global* g, int code, int info) {
   if (atomicCAS(&g->error, 0, code) == 0) g->err_info = info;
@@ -64,6 +79,47 @@ __device__ __forceinline__ double f32_to_f64(float f) {
   if (e == 0u || e == 0xFFu) return (double)f;  // zero, subnormal, inf, NaN
   const unsigned hi = (b & 0x80000000u) | (((b & 0x7FFFFFFFu) >> 3) + (896u << 20));
   return __hiloint2double((int)hi, (int)(b << 29));
+}
+
+// a < b for binary64 values on the integer pipes (IEEE comparison: false
+// with a NaN, -0 equal to +0): sign-magnitude mapped to two's complement.
+__device__ __forceinline__ bool f64_lt(double a, double b) {
+  long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  const long long inf = 0x7FF0000000000000LL, mag = 0x7FFFFFFFFFFFFFFFLL;
+  if ((x & mag) > inf || (y & mag) > inf) return false;
+  x = x >= 0 ? x : LLONG_MIN - x;
+  y = y >= 0 ? y : LLONG_MIN - y;
+  return x < y;
+}
+
+// The deletion walk's pick (dana.F90:686-690), m = int(upick * n) + 1 capped
+// at n, with upick = k * 2^-53 (k < 2^53) and n >= 0, exactly as the binary64
+// product rounds: k * n (up to 84 bits) rounded to nearest even at 53
+// significant bits, then scaled by 2^-53 (exact) and truncated.
+__host__ __device__ inline int gcmc_pick_index(unsigned long long k, int n) {
+  if (n <= 0) return n < 0 ? n : 0;
+  const unsigned long long un = (unsigned long long)n;
+  const unsigned long long lo = k * un;
+#if defined(__CUDA_ARCH__)
+  const unsigned long long hi = __umul64hi(k, un);
+#else
+  const unsigned long long hi = (unsigned long long)(((unsigned __int128)k * un) >> 64);
+#endif
+#if defined(__CUDA_ARCH__)
+  const int len = hi ? 128 - __clzll((long long)hi) : (lo ? 64 - __clzll((long long)lo) : 0);
+#else
+  const int len = hi ? 128 - __builtin_clzll(hi) : (lo ? 64 - __builtin_clzll(lo) : 0);
+#endif  // bit length of k * n
+  unsigned long long q = 0;  // int(RN53(k n) / 2^53)
+  if (len > 53) {
+    const int sft = len - 53;  // 1 .. 31
+    unsigned long long top = (lo >> sft) | (hi << (64 - sft));
+    const unsigned long long r = lo & ((1ull << sft) - 1ull), half = 1ull << (sft - 1);
+    if (r > half || (r == half && (top & 1ull))) top += 1ull;
+    q = top >> (53 - sft);
+  }
+  const long long m = (long long)q + 1;
+  return m > n ? n : (int)m;
 }
 
 // FP32 copy of a position; w carries the element as integer bits (0 for a
@@ -1688,7 +1744,7 @@ __device__ __forceinline__ void list_cells_row(const Dev& d, const KParams& p, i
     int nc[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      int t = c_map[lane][k] + rc[k] - 1;
+      int t = map_off(lane, k) + rc[k] - 1;
       t = (t + R.ncells[k]) % R.ncells[k];
       nc[k] = t + 1;
       if (nc[k] < 0 || nc[k] > R.ncells[k] + 1) bad = true;
@@ -2441,7 +2497,7 @@ __device__ void gcmc_own_list(const Dev& d, const KParams& p, const RepConst& R,
     for (int nabor = 0; nabor < 27; ++nabor) {
       int nc[3];
       for (int k = 0; k < 3; ++k) {
-        int t = c_map[nabor][k] + rc[k] - 1;
+        int t = map_off(nabor, k) + rc[k] - 1;
         t = (t + R.ncells[k]) % R.ncells[k];
         nc[k] = t + 1;
       }
@@ -2560,16 +2616,19 @@ __device__ __forceinline__ bool in_slab_at(const Dev& d, int h, float zf, float 
 // gcmc_run's cell sort, binning pass: every live atom's cell (coalesced
 // over hs slots, so no gather), the range check and the halo flag of
 // cgroup_sort_atom (Cells.F90:281-302) for all, and a list entry (hs slot,
-// cell) for the atoms of the z layers the trials can reach.
-__device__ __forceinline__ void gcmc_bin_at(const Dev& d, int rep, int pos) {
+// cell; with the parallel trials also the FP32 position) for the atoms of
+// the z layers the trials can reach.
+__device__ __forceinline__ void gcmc_bin_at(const Dev& d, int rep, int pos, int par) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   const int s = pos;
   const int lane = threadIdx.x & 31;
   int lin = -1;
+  float4 Pf = make_float4(0.f, 0.f, 0.f, 0.f);
   if (R.use_cells && s < R.base + sc->n_slots && d.state[s] == ST_LIVE) {
     int c1, c2, c3;
-    cell_index3(R, d.posf[s], d.pos + s, c1, c2, c3);
+    Pf = d.posf[s];
+    cell_index3(R, Pf, d.pos + s, c1, c2, c3);
     if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] + 1 || c2 > R.ncells[1] + 1 ||
         c3 > R.ncells[2] + 1) {
       raise_error(d.g, DML_E_OUT_OF_TESSELLATION, s);
@@ -2590,7 +2649,9 @@ __device__ __forceinline__ void gcmc_bin_at(const Dev& d, int rep, int pos) {
   if (lane == leader) b = atomicAdd(d.pr_cnt + rep * kCntStride + kCntGlist, __popc(m));
   b = __shfl_sync(0xffffffffu, b, leader);
   if (!in) return;
-  d.glist[R.base + b + __popc(m & ((1u << lane) - 1u))] = make_int2(s, lin);
+  const int at = R.base + b + __popc(m & ((1u << lane) - 1u));
+  d.glist[at] = make_int2(s, lin);
+  if (par) d.glp[at] = make_float4(Pf.x, Pf.y, Pf.z, __int_as_float(s));
 }
 
 // The membership and in-slab bits of the gcmc%alist positions [0, ng) for
@@ -2658,7 +2719,7 @@ __global__ void gcmc_bin_kernel(Dev d, int par) {
   const int rep = block_rep(d);
   if (blockIdx.x == 0 && threadIdx.x == 0) d.g->n_big = 0;  // cell_order's list
 #pragma unroll
-  for (int u = 0; u < kSlotU; ++u) gcmc_bin_at(d, rep, span_pos(u));
+  for (int u = 0; u < kSlotU; ++u) gcmc_bin_at(d, rep, span_pos(u), par);
   if (par) gcmc_member_words(d, rep);
 }
 
@@ -2700,13 +2761,23 @@ struct GcmcTrial {
 };
 
 // Linear index of stencil cell `nabor` (map order) around the point's cell.
+// Stencil cell `nabor` (map order) of the interior cell (t1, t2, t3), with
+// the periodic wrap of cell_pbc.
+__device__ __forceinline__ int stencil_cell_of(const RepConst& R, int t1, int t2, int t3,
+                                               int nabor) {
+  const int x = (map_off(nabor, 0) + t1 - 1 + R.ncells[0]) % R.ncells[0] + 1;
+  const int y = (map_off(nabor, 1) + t2 - 1 + R.ncells[1]) % R.ncells[1] + 1;
+  const int z = (map_off(nabor, 2) + t3 - 1 + R.ncells[2]) % R.ncells[2] + 1;
+  return R.cell_off + (z * R.head_dim[1] + y) * R.head_dim[0] + x;
+}
+
 __device__ __forceinline__ int stencil_cell(const RepConst& R, float4 Pf, const double4* P,
                                             int nabor) {
   int rc[3];
   cell_index3(R, Pf, P, rc[0], rc[1], rc[2]);
   int nc[3];
   for (int k = 0; k < 3; ++k) {
-    int t = c_map[nabor][k] + rc[k] - 1;
+    int t = map_off(nabor, k) + rc[k] - 1;
     t = (t + R.ncells[k]) % R.ncells[k];
     nc[k] = t + 1;
   }
@@ -3315,6 +3386,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
 // kGcmcMaxTrials trials, a point with more than kGcmcBlk blockers or
 // kGcmcCand list atoms) runs gcmc_kernel instead.
 constexpr int kGcmcPreThreads = 512;
+constexpr int kGcmcPairQ = 2048;  // queued pairs within rc + skin (more: sequential path)
 
 __device__ __forceinline__ bool hard_core_in(const KParams& p, const RepConst& R, double4 a,
                                              float4 af, double4 b, float4 bf) {
@@ -3330,14 +3402,15 @@ __device__ __forceinline__ bool hard_core_in(const KParams& p, const RepConst& R
 }
 
 // First `want` positions q in [lo, hi) with free(q), ascending, into out[];
-// returns how many were found.  Every thread of the block calls it; each
-// thread tests kCollectV consecutive positions per round.
-constexpr int kCollectV = 8;
+// returns how many were found.  Every thread of the block calls it; per
+// round each thread tests a run of kCollectV consecutive positions (their
+// loads all in flight), one block scan places the finds.
+constexpr int kCollectV = 32;
 template <class Pred>
 __device__ int blk_collect(int lo, int hi, int want, Pred free_at, int* out, int* s_cnt) {
   if (threadIdx.x == 0) *s_cnt = 0;
   __syncthreads();
-  for (int base = lo; base < hi && *s_cnt < want; base += kCollectV * (int)blockDim.x) {
+  for (int base = lo; base < hi; base += kCollectV * (int)blockDim.x) {
     const int q0 = base + kCollectV * (int)threadIdx.x;
     unsigned m = 0u;
 #pragma unroll
@@ -3346,32 +3419,19 @@ __device__ int blk_collect(int lo, int hi, int want, Pred free_at, int* out, int
     int tot;
     const int pre = blk_scan_excl(__popc(m), &tot);
     int k = *s_cnt + pre;
-#pragma unroll
-    for (int v = 0; v < kCollectV; ++v)
-      if ((m >> v) & 1u) {
-        if (k < want) out[k] = q0 + v;
-        ++k;
-      }
+    while (m != 0u && k < want) {
+      out[k++] = q0 + __ffs(m) - 1;
+      m &= m - 1u;
+    }
     __syncthreads();
     if (threadIdx.x == 0) *s_cnt += tot;
     __syncthreads();
+    if (*s_cnt >= want) break;
   }
   const int n = min(*s_cnt, want);
   __syncthreads();
   return n;
 }
-
-// Candidate records of one creation trial (per warp): stencil index and
-// hs%b slot as one ordering key, the atom, its list flags.
-struct GcmcCandRec {
-  unsigned long long key[kGcmcCand];
-  int j[kGcmcCand];
-  unsigned char fl[kGcmcCand];
-};
-
-// Dynamic shared memory of gcmc_pre_kernel: the row ends of the cell-row
-// sort, then the sorted hs slots.
-__host__ __device__ constexpr int gcmc_pre_sort_cap() { return 12288; }
 
 __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParams p) {
   const int rep = blockIdx.x;
@@ -3385,12 +3445,19 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
   __shared__ double4 s_r[kGcmcMaxTrials];
   __shared__ float4 s_rf[kGcmcMaxTrials];
   __shared__ unsigned char s_crt[kGcmcMaxTrials];
-  __shared__ int s_tab[kGcmcPreThreads / 32][56];  // per warp: stencil cells, row segments
-  __shared__ int s_nb[kGcmcPreThreads / 32], s_nc[kGcmcPreThreads / 32];
-  __shared__ GcmcCandRec s_rec[kGcmcPreThreads / 32];
-  extern __shared__ int s_pre_dyn[];
-  int* const rowend = s_pre_dyn;
-  int* const sorted = s_pre_dyn + d.gcmc_rows;
+  // per creation trial (compacted): trial, cell, repeats, row segments of
+  // its stencil in gs (start, exclusive prefix of the sizes), counts
+  __shared__ int s_nct;
+  __shared__ short s_ct[kGcmcMaxTrials];
+  __shared__ short s_tc[kGcmcMaxTrials][3];  // by trial: the point's cell
+  __shared__ unsigned s_dup[kGcmcMaxTrials];
+  __shared__ int s_segst[kGcmcMaxTrials][9], s_segpre[kGcmcMaxTrials][10];
+  __shared__ int s_tpre[kGcmcMaxTrials + 1];
+  __shared__ int s_nb[kGcmcMaxTrials], s_nc[kGcmcMaxTrials];
+  __shared__ unsigned s_pm[kGcmcMaxTrials][kGcmcMaskW];
+  __shared__ int s_npq;                  // pairs within rc + skin: (trial, place in gs)
+  __shared__ int2 s_pq[kGcmcPairQ];
+  extern __shared__ int rowend[];  // the row ends of the cell-row sort
   if (!sc->listed) {  // gcmc_kernel reports the state error
     if (tid == 0) gr->fast = 0;
     return;
@@ -3398,13 +3465,10 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
   const int nrows = R.head_dim[1] * R.head_dim[2];
   const int n_gl = d.pr_cnt[rep * kCntStride + kCntGlist];
   if (tid == 0) {
-    s_bad = !(R.use_cells && !sc->halo && p.nadj <= kGcmcMaxTrials &&
-              n_gl <= gcmc_pre_sort_cap() && nrows <= d.gcmc_rows);
+    s_bad = !(R.use_cells && !sc->halo && p.nadj <= kGcmcMaxTrials && nrows <= d.gcmc_rows);
     s_ncrt = 0;
-  }
-  if (tid < kGcmcPreThreads / 32) {
-    s_nb[tid] = 0;
-    s_nc[tid] = 0;
+    s_nct = 0;
+    s_npq = 0;
   }
   __syncthreads();
   if (s_bad) {
@@ -3433,6 +3497,7 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
     tr.coin = coin;
     tr.uacc = dml_u53(w0.w[2], w0.w[3]);
     tr.upick = dml_u53(w2.w[2], w2.w[3]);
+    tr.kpick = ((unsigned long long)(w2.w[2] >> 5) << 26) | (w2.w[3] >> 6);
     const bool crt = coin < 0.5;
     s_r[tid] = r;
     s_rf[tid] = rf;
@@ -3453,16 +3518,30 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
       if (c1 < 1 || c2 < 1 || c3 < 1 || c1 > R.ncells[0] || c2 > R.ncells[1] || c3 > R.ncells[2])
         s_bad = 1;
       tr.cell = R.cell_off + (c3 * R.head_dim[1] + c2) * R.head_dim[0] + c1;
+      s_tc[tid][0] = (short)c1;
+      s_tc[tid][1] = (short)c2;
+      s_tc[tid][2] = (short)c3;
+      s_ct[atomicAdd(&s_nct, 1)] = (short)tid;
     }
   }
+  for (int e = tid; e < kGcmcMaxTrials * kGcmcMaskW; e += nt) (&s_pm[0][0])[e] = 0u;
   // The atoms gcmc_bin_kernel listed (live, in the layers the trials reach),
-  // counting-sorted by cell row (z layer, y row) in shared memory: row r's
-  // hs slots are sorted[rowend[r - 1] .. rowend[r]) (from 0 for r = 0).
+  // counting-sorted by cell row (z layer, y row), the counts in shared
+  // memory: row r's FP32 positions and hs slots are gs[rowend[r - 1] ..
+  // rowend[r]) (from 0 for r = 0), contiguous for the searches below.
   const int hd0 = R.head_dim[0];
   for (int r = tid; r < nrows; r += nt) rowend[r] = 0;
   __syncthreads();
   const int2* const gl = d.glist + B;
-  for (int i = tid; i < n_gl; i += nt) atomicAdd(&rowend[(gl[i].y - R.cell_off) / hd0], 1);
+  constexpr int kSortU = 4;  // entries per thread per round, loads in flight together
+  for (int i0 = tid; i0 < n_gl; i0 += kSortU * nt) {
+    int cl[kSortU];
+#pragma unroll
+    for (int u = 0; u < kSortU; ++u) cl[u] = i0 + u * nt < n_gl ? gl[i0 + u * nt].y : -1;
+#pragma unroll
+    for (int u = 0; u < kSortU; ++u)
+      if (cl[u] >= 0) atomicAdd(&rowend[(cl[u] - R.cell_off) / hd0], 1);
+  }
   __syncthreads();
   {
     const int per = (nrows + nt - 1) / nt, r0 = tid * per, r1 = min(r0 + per, nrows);
@@ -3477,142 +3556,247 @@ __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParam
     }
   }
   __syncthreads();
-  for (int i = tid; i < n_gl; i += nt) {
-    const int2 e = gl[i];
-    sorted[atomicAdd(&rowend[(e.y - R.cell_off) / hd0], 1)] = e.x;
+  float4* const gs = d.gsort + B;
+  for (int i0 = tid; i0 < n_gl; i0 += kSortU * nt) {
+    int cl[kSortU];
+    float4 rec[kSortU];
+#pragma unroll
+    for (int u = 0; u < kSortU; ++u) {
+      const bool on = i0 + u * nt < n_gl;
+      cl[u] = on ? gl[i0 + u * nt].y : -1;
+      rec[u] = on ? d.glp[B + i0 + u * nt] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < kSortU; ++u)
+      if (cl[u] >= 0) gs[atomicAdd(&rowend[(cl[u] - R.cell_off) / hd0], 1)] = rec[u];
   }
   __syncthreads();
 
   // Earlier creation points within rc of each creation point: an accepted
-  // earlier insertion sits there during this trial's hard-core test.
-  if (tid < p.nadj) {
-    unsigned m[kGcmcMaskW];
-#pragma unroll
-    for (int w = 0; w < kGcmcMaskW; ++w) m[w] = 0u;
-    if (s_crt[tid]) {
-      const double4 a = s_r[tid];
-      const float4 af = s_rf[tid];
-      for (int j = 0; j < tid; ++j)
-        if (s_crt[j] && hard_core_in(p, R, a, af, s_r[j], s_rf[j])) m[j >> 5] |= 1u << (j & 31);
-    }
-#pragma unroll
-    for (int w = 0; w < kGcmcMaskW; ++w) pm[tid * kGcmcMaskW + w] = m[w];
+  // earlier insertion sits there during this trial's hard-core test (all
+  // ordered pairs of creation trials of the block).
+  const int nct = s_nct;
+  for (int e = tid; e < nct * nct; e += nt) {
+    const int ia = s_ct[e / nct], ib = s_ct[e % nct];
+    if (ib < ia && hard_core_in(p, R, s_r[ia], s_rf[ia], s_r[ib], s_rf[ib]))
+      atomicOr(&s_pm[ia][ib >> 5], 1u << (ib & 31));
   }
+  __syncthreads();
+  for (int e = tid; e < p.nadj * kGcmcMaskW; e += nt) pm[e] = (&s_pm[0][0])[e];
 
-  // Blockers and list candidates of every creation trial, one warp each:
-  // the atoms of the (at most 9) cell rows through its 27 stencil cells
-  // within rc + skin (FP32, FP64 inside the margins), each matched to the
-  // stencil cells holding it; the candidates then in the order of the
-  // stencil walk (map order, each cell by descending hs%b slot).
-  int* const wc = s_tab[wid];        // [0, 27): the stencil cells
-  int* const segst = s_tab[wid] + 27;  // [0, 9): row segment starts in sorted[]
-  int* const segpre = s_tab[wid] + 36; // [0, 10): exclusive prefix of their sizes
-  int* const segrow = s_tab[wid] + 46; // [0, 9): the rows
-  GcmcCandRec& rec = s_rec[wid];
-  for (int i = wid; i < p.nadj; i += nw) {
-    if (!s_crt[i]) continue;
-    GcmcTrialPre& tr = pre[i];
-    const double4 Rt = s_r[i];
-    const float4 Rtf = s_rf[i];
-    int c = -1;
-    if (lane < 27) {
-      c = stencil_cell(R, Rtf, &Rt, lane);
-      tr.cells[lane] = c;
-      wc[lane] = c;
-    }
-    const int row = lane < 27 ? (c - R.cell_off) / hd0 : -1;
-    bool dupl = false, rdup = false;
-    for (int q = 0; q < 26; ++q) {
-      const int cq = __shfl_sync(0xffffffffu, c, q);
-      const int rq = __shfl_sync(0xffffffffu, row, q);
-      if (q < lane && cq == c) dupl = true;
-      if (q < lane && rq == row) rdup = true;
-    }
-    const unsigned dupm = __ballot_sync(0xffffffffu, lane < 27 && dupl);
-    const unsigned rm = __ballot_sync(0xffffffffu, lane < 27 && !rdup);
-    const int nseg = __popc(rm);
-    // the distinct rows compacted to lanes [0, nseg): start and size
-    if (lane < 27 && !rdup) segrow[__popc(rm & lt)] = row;
-    __syncwarp();
-    int ssz = 0;
-    if (lane < nseg) {
-      const int r = segrow[lane];
-      const int st = r > 0 ? rowend[r - 1] : 0;
-      segst[lane] = st;
-      ssz = rowend[r] - st;
-    }
-    int x = ssz;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane < nseg) segpre[lane] = x - ssz;
-    const int T = nseg > 0 ? __shfl_sync(0xffffffffu, x, nseg - 1) : 0;
-    __syncwarp();
-    for (int base = 0; base < T; base += 32) {
-      const int f = base + lane;
-      if (f < T) {
-        int k = 0;
-        while (k + 1 < nseg && segpre[k + 1] <= f) ++k;
-        const int j = sorted[segst[k] + f - segpre[k]];
-        const float4 Q = d.posf[j];
-        float fx, fy, fz;
-        vdist_nint_f(R, Rtf, Q, fx, fy, fz);
-        const float df = fx * fx + fy * fy + fz * fz;
-        if (df <= R.rlist_hi2) {
-          // its cell in the cell sort, matched against the stencil below
-          int a1, a2, a3;
-          cell_index3(R, Q, d.pos + j, a1, a2, a3);
-          const int lin = R.cell_off + (a3 * R.head_dim[1] + a2) * hd0 + a1;
-          const bool mem = d.in_gcmc[j] != 0;
-          double rd = -1.0;  // FP64 only inside the margins of rc and rc + skin
-          if (df >= R.rlist_lo2 || (mem && df >= R.rc_lo2 && df <= R.rc_hi2)) {
-            double vx, vy, vz;
-            vdist_nint(R, Rt, d.pos[j], vx, vy, vz);
-            rd = dot3(vx, vy, vz);
+  // Blockers and list candidates of every creation trial: the atoms of the
+  // (at most 9) cell rows through its 27 stencil cells within rc + skin
+  // (FP32, FP64 inside the margins), each matched to the stencil cells that
+  // hold it; the candidates then put in the order of the stencil walk (map
+  // order, each cell by descending hs%b slot).  Setup per creation trial,
+  // then all (trial, row atom) pairs of the block, then a sort per trial.
+  const int n1 = R.ncells[0], n2 = R.ncells[1], n3 = R.ncells[2];
+  const int hd1 = R.head_dim[1];
+  // fewer than 3 cells along an axis: stencil cells repeat
+  const bool small = n1 < 3 || n2 < 3 || n3 < 3;
+  // the stencil cells (map order) of every creation trial
+  for (int e = tid; e < nct * 27; e += nt) {
+    const int i = s_ct[e / 27], q = e % 27;
+    pre[i].cells[q] = stencil_cell_of(R, s_tc[i][0], s_tc[i][1], s_tc[i][2], q);
+  }
+  // the 9 rows (dz, dy) through the stencil: start in gs, size
+  for (int e = tid; e < nct * 9; e += nt) {
+    const int c = e / 9, k = e % 9, i = s_ct[c];
+    const int z = (s_tc[i][2] - 1 + k / 3 - 1 + n3) % n3 + 1;
+    const int y = (s_tc[i][1] - 1 + k % 3 - 1 + n2) % n2 + 1;
+    const int row = z * hd1 + y;
+    const int st = row > 0 ? rowend[row - 1] : 0;
+    s_segst[c][k] = st;
+    s_segpre[c][k] = rowend[row] - st;  // the size; a prefix below
+  }
+  __syncthreads();
+  for (int c = tid; c < nct; c += nt) {
+    const int i = s_ct[c];
+    unsigned dupm = 0u;
+    if (small) {
+      // a repeated stencil cell (dup bit), a repeated row (scanned once)
+      for (int q = 1; q < 27; ++q)
+        for (int q2 = 0; q2 < q; ++q2)
+          if (pre[i].cells[q2] == pre[i].cells[q]) {
+            dupm |= 1u << q;
+            break;
           }
-          const bool isb = df <= R.rc_hi2 && mem && (df < R.rc_lo2 || rd < p.rc2);
-          const bool own = df < R.rlist_lo2 || rd < p.rlist2;
-          const bool app = (df < R.rlist_lo2 || !(rd > p.rlist2)) && d.rank[j] >= 0;
-          for (int q = 0; q < 27; ++q) {
-            if (wc[q] != lin) continue;
-            if (isb) {
-              const int kb = atomicAdd(&s_nb[wid], 1);
-              if (kb < kGcmcBlk) tr.blk[kb] = d.gpos[j] - B;
-            }
-            const int fl = (own ? 1 : 0) | (app && !((dupm >> q) & 1u) ? 2 : 0);
-            if (fl) {
-              const int kc = atomicAdd(&s_nc[wid], 1);
-              if (kc < kGcmcCand) {
-                rec.key[kc] = ((unsigned long long)q << 32) | (unsigned)~d.bslot[j];
-                rec.j[kc] = j;
-                rec.fl[kc] = (unsigned char)fl;
-              }
-            }
+      for (int k = 1; k < 9; ++k)
+        for (int k2 = 0; k2 < k; ++k2)
+          if ((s_tc[i][2] - 1 + k / 3 - 1 + n3) % n3 == (s_tc[i][2] - 1 + k2 / 3 - 1 + n3) % n3 &&
+              (s_tc[i][1] - 1 + k % 3 - 1 + n2) % n2 == (s_tc[i][1] - 1 + k2 % 3 - 1 + n2) % n2) {
+            s_segpre[c][k] = 0;
+            break;
+          }
+    }
+    int T = 0;
+    for (int k = 0; k < 9; ++k) {
+      const int sz = s_segpre[c][k];
+      s_segpre[c][k] = T;
+      T += sz;
+    }
+    s_segpre[c][9] = T;
+    s_tpre[c] = T;
+    s_dup[c] = dupm;
+    s_nb[c] = 0;
+    s_nc[c] = 0;
+  }
+  __syncthreads();
+  // the pairs of each creation trial start at the exclusive prefix s_tpre
+  {
+    const int v = tid < nct ? s_tpre[tid] : 0;
+    int tot;
+    const int e = blk_scan_excl(v, &tot);
+    if (tid < nct) s_tpre[tid] = e;
+    if (tid == 0) s_tpre[nct] = tot;
+  }
+  __syncthreads();
+  // Every (trial, row atom) pair of the block: each thread walks a
+  // contiguous range of them (so a row's records are read in order), kPairU
+  // loads in flight; the pairs within rc + skin (FP32 with margin) are queued
+  // and then evaluated by the whole block.
+  constexpr int kPairU = 4;
+  const int npair = s_tpre[nct];
+  {
+    const int per = (npair + nt - 1) / nt;
+    const int e_beg = min(tid * per, npair), e_end = min(e_beg + per, npair);
+    int c = 0, k = 0;
+    if (e_beg < e_end) {
+      int lo = 0, hi = nct - 1;  // the trial: last c with s_tpre[c] <= e_beg
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_tpre[mid] <= e_beg) lo = mid; else hi = mid - 1;
+      }
+      c = lo;
+      while (s_segpre[c][k + 1] <= e_beg - s_tpre[c]) ++k;
+    }
+    for (int e = e_beg; e < e_end;) {
+      const int f = e - s_tpre[c];
+      const int len = min(s_segpre[c][k + 1] - f, e_end - e);
+      const int g0 = s_segst[c][k] + f - s_segpre[c][k];
+      const float4 Rtf = s_rf[s_ct[c]];
+      for (int r0 = 0; r0 < len; r0 += kPairU) {
+        float4 QQ[kPairU];
+#pragma unroll
+        for (int u = 0; u < kPairU; ++u)
+          QQ[u] = r0 + u < len ? gs[g0 + r0 + u] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < kPairU; ++u) {
+          float fx, fy, fz;
+          vdist_nint_f(R, Rtf, QQ[u], fx, fy, fz);
+          const float df = fx * fx + fy * fy + fz * fz;
+          if (r0 + u < len && df <= R.rlist_hi2) {
+            const int qn = atomicAdd(&s_npq, 1);
+            if (qn < kGcmcPairQ) s_pq[qn] = make_int2(c, g0 + r0 + u);
           }
         }
       }
+      e += len;
+      if (e < e_end) {  // the next segment with pairs (of this trial or a later one)
+        while (s_tpre[c + 1] <= e) ++c, k = 0;
+        const int f2 = e - s_tpre[c];
+        while (s_segpre[c][k + 1] <= f2) ++k;
+      }
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && s_npq > kGcmcPairQ) s_bad = 1;
+  const int npq = min(s_npq, kGcmcPairQ);
+  for (int x = tid; x < npq; x += nt) {
+    const int c = s_pq[x].x, i = s_ct[c];
+    const float4 Q = gs[s_pq[x].y];
+    const int j = __float_as_int(Q.w);
+    float fx, fy, fz;
+    vdist_nint_f(R, s_rf[i], Q, fx, fy, fz);
+    const float df = fx * fx + fy * fy + fz * fz;
+    int a1, a2, a3;
+    cell_index3(R, Q, d.pos + j, a1, a2, a3);  // its cell in the cell sort
+    const bool mem = d.in_gcmc[j] != 0;
+    const bool inref = d.rank[j] >= 0;
+    const unsigned key = ~(unsigned)d.bslot[j];
+    double rd = -1.0;  // FP64 only inside the margins of rc and rc + skin
+    if (df >= R.rlist_lo2 || (mem && df >= R.rc_lo2 && df <= R.rc_hi2)) {
+      double vx, vy, vz;
+      vdist_nint(R, s_r[i], d.pos[j], vx, vy, vz);
+      rd = dot3(vx, vy, vz);
+    }
+    const bool isb = df <= R.rc_hi2 && mem && (df < R.rc_lo2 || rd < p.rc2);
+    const bool own = df < R.rlist_lo2 || rd < p.rlist2;
+    const bool app = (df < R.rlist_lo2 || !(rd > p.rlist2)) && inref;
+    GcmcTrialPre& tr = pre[i];
+    const unsigned dupm = s_dup[c];
+    auto emit = [&](int q) {
+      if (isb) {
+        const int kb = atomicAdd(&s_nb[c], 1);
+        if (kb < kGcmcBlk) tr.blk[kb] = d.gpos[j] - B;
+      }
+      const int fl = (own ? 1 : 0) | (app && !((dupm >> q) & 1u) ? 2 : 0);
+      if (fl) {
+        const int kc = atomicAdd(&s_nc[c], 1);
+        if (kc < kGcmcCand) {
+          tr.cand[kc] = j;
+          tr.cq[kc] = (unsigned char)q;
+          tr.cf[kc] = (unsigned char)fl;
+          tr.ckey[kc] = key;
+        }
+      }
+    };
+    if (!small) {
+      // the offset from the trial's cell, wrapped; a stencil cell when in {-1, 0, 1}^3
+      int o1 = a1 - s_tc[i][0], o2 = a2 - s_tc[i][1], o3 = a3 - s_tc[i][2];
+      o1 = o1 > 1 ? o1 - n1 : (o1 < -1 ? o1 + n1 : o1);
+      o2 = o2 > 1 ? o2 - n2 : (o2 < -1 ? o2 + n2 : o2);
+      o3 = o3 > 1 ? o3 - n3 : (o3 < -1 ? o3 + n3 : o3);
+      if (o1 >= -1 && o1 <= 1 && o2 >= -1 && o2 <= 1 && o3 >= -1 && o3 <= 1)
+        emit(map_inv(o1, o2, o3));
+    } else {
+      const int lin = R.cell_off + (a3 * hd1 + a2) * R.head_dim[0] + a1;
+      for (int q = 0; q < 27; ++q)
+        if (tr.cells[q] == lin) emit(q);
+    }
+  }
+  __syncthreads();
+  // each trial's candidates in stencil-walk order (a rank sort per warp)
+  for (int c = wid; c < nct; c += nw) {
+    GcmcTrialPre& tr = pre[s_ct[c]];
+    const int nb = s_nb[c], nc = s_nc[c], nk = min(nc, kGcmcCand);
+    int j0 = -1, j1 = -1, q0 = 0, q1 = 0, f0 = 0, f1 = 0;
+    unsigned long long k0 = ~0ull, k1 = ~0ull;
+    if (lane < nk) {
+      j0 = tr.cand[lane];
+      q0 = tr.cq[lane];
+      f0 = tr.cf[lane];
+      k0 = ((unsigned long long)q0 << 32) | tr.ckey[lane];
+    }
+    if (lane + 32 < nk) {
+      j1 = tr.cand[lane + 32];
+      q1 = tr.cq[lane + 32];
+      f1 = tr.cf[lane + 32];
+      k1 = ((unsigned long long)q1 << 32) | tr.ckey[lane + 32];
+    }
+    int r0 = 0, r1 = 0;
+    for (int m = 0; m < nk; ++m) {
+      const unsigned long long km = __shfl_sync(0xffffffffu, m < 32 ? k0 : k1, m & 31);
+      r0 += km < k0;
+      r1 += km < k1;
     }
     __syncwarp();
-    const int nb = s_nb[wid], nc = s_nc[wid], nk = min(nc, kGcmcCand);
-    for (int k = lane; k < nk; k += 32) {
-      const unsigned long long key = rec.key[k];
-      int rank = 0;
-      for (int m = 0; m < nk; ++m) rank += rec.key[m] < key;
-      tr.cand[rank] = rec.j[k];
-      tr.cq[rank] = (unsigned char)(key >> 32);
-      tr.cf[rank] = rec.fl[k];
+    if (lane < nk) {
+      tr.cand[r0] = j0;
+      tr.cq[r0] = (unsigned char)q0;
+      tr.cf[r0] = (unsigned char)f0;
     }
-    __syncwarp();
+    if (lane + 32 < nk) {
+      tr.cand[r1] = j1;
+      tr.cq[r1] = (unsigned char)q1;
+      tr.cf[r1] = (unsigned char)f1;
+    }
     if (lane == 0) {
       tr.n_blk = nb;
       tr.n_cand = nc;
-      tr.dup = dupm;
+      tr.dup = s_dup[c];
       if (nb > kGcmcBlk || nc > kGcmcCand) s_bad = 1;
-      s_nb[wid] = 0;
-      s_nc[wid] = 0;
     }
-    __syncwarp();
   }
   __syncthreads();
 
@@ -3650,7 +3834,8 @@ struct Vel3 {
 // in-slab counts per 1024 positions and, when they fit, the bit words).
 struct GcmcSm {
   Scalars ss;
-  double uacc[kGcmcMaxTrials], upick[kGcmcMaxTrials];
+  double uacc[kGcmcMaxTrials];
+  unsigned long long kpick[kGcmcMaxTrials];
   unsigned char crt[kGcmcMaxTrials], rin[kGcmcMaxTrials];  // creation trial; point in the slab
   int nblk[kGcmcMaxTrials];
   int blk[kGcmcMaxTrials][kGcmcBlk];
@@ -3724,6 +3909,37 @@ __device__ int warp_select(const unsigned* wsl, const int* grp, int ng, int m) {
     acc += __shfl_sync(0xffffffffu, x, 31);
   }
   return -1;
+}
+
+// warp_select with the inclusive in-slab counts per 1024 positions held in
+// registers (group lane in P0, group lane + 32 in P1): the group is one
+// ballot, the word a scan of its 32 words, the bit a ballot.
+__device__ int warp_select_reg(const unsigned* wsl, int P0, int P1, int ng, int m) {
+  const int lane = threadIdx.x & 31;
+  const unsigned h0 = __ballot_sync(0xffffffffu, P0 >= m), h1 = __ballot_sync(0xffffffffu, P1 >= m);
+  if (!h0 && !h1) return -1;
+  const int gg = h0 ? __ffs(h0) - 1 : 32 + __ffs(h1) - 1;
+  const int gp = gg - 1;  // members before group gg
+  const int before0 = __shfl_sync(0xffffffffu, P0, gp & 31), before1 = __shfl_sync(0xffffffffu, P1, gp & 31);
+  const int mr = m - (gp < 0 ? 0 : (gp < 32 ? before0 : before1));
+  const int wi = gg * 32 + lane;
+  const unsigned w = wi * 32 < ng ? wsl[wi] : 0u;
+  const int wc = __popc(w);
+  int y = wc;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int z = __shfl_up_sync(0xffffffffu, y, o);
+    if (lane >= o) y += z;
+  }
+  const unsigned hit2 = __ballot_sync(0xffffffffu, y >= mr);
+  if (!hit2) return -1;
+  const int L2 = __ffs(hit2) - 1;
+  const int k = mr - __shfl_sync(0xffffffffu, y - wc, L2);
+  const unsigned ww = __shfl_sync(0xffffffffu, w, L2);
+  const bool set = (ww >> lane) & 1u;
+  const int below = __popc(ww & ((1u << lane) - 1u));
+  const unsigned hit3 = __ballot_sync(0xffffffffu, set && below == k - 1);
+  if (!hit3) return -1;
+  return (gg * 32 + L2) * 32 + (__ffs(hit3) - 1);
 }
 
 // First member position >= from (INT_MAX if none) / last member position
@@ -3850,7 +4066,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
     S.crt[i] = tr.coin < 0.5;
     S.rin[i] = in_slab(tr.r.z, sc_g->z0, sc_g->zmax);
     S.uacc[i] = tr.uacc;
-    S.upick[i] = tr.upick;
+    S.kpick[i] = tr.kpick;
     S.nblk[i] = tr.coin < 0.5 ? tr.n_blk : 0;
   }
   for (int e = tid; e < p.nadj * kGcmcBlk; e += nt) {
@@ -3889,6 +4105,22 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
   // The trials in order (dana.F90:620-710), one warp, shared state only.
   // hs%b slots, which no decision reads, are assigned afterwards.
   if (wid == 0) {
+    // in-slab members up to and including 1024-position group g, for g =
+    // lane (P0) and lane + 32 (P1): the first step of the deletion pick
+    const bool reg_sel = ngrp <= 64;
+    int P0 = 0, P1 = 0;
+    if (reg_sel) {
+      P0 = lane < ngrp ? grp[lane] : 0;
+      P1 = lane + 32 < ngrp ? grp[lane + 32] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y0 = __shfl_up_sync(0xffffffffu, P0, o), y1 = __shfl_up_sync(0xffffffffu, P1, o);
+        if (lane >= o) {
+          P0 += y0;
+          P1 += y1;
+        }
+      }
+      P1 += __shfl_sync(0xffffffffu, P0, 31);
+    }
     int n = n0, first = gr->first, last = gr->last, ng = ng0;
     int ns = S.ss.n_slots, n_atoms = S.ss.n_atoms, nlimbo = S.ss.nlimbo;
     int free_lo = S.ss.free_lo;
@@ -3907,7 +4139,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
       const double uacc = S.uacc[i];
       if (S.crt[i]) {
         // creation attempt (dana.F90:627-677)
-        if (S.qc[n - qb] < uacc) continue;
+        if (f64_lt(S.qc[n - qb], uacc)) continue;
         // a blocker still in the group (its membership bit), or an earlier
         // insertion of this call still in it
         bool ov = false;
@@ -3952,6 +4184,11 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
           }
           S.acc[i >> 5] |= 1u << (i & 31);
         }
+        if (S.rin[i]) {
+          const int g = ng >> 10;
+          P0 += lane >= g;
+          P1 += lane + 32 >= g;
+        }
         n += 1;
         last = ng;
         ng += 1;
@@ -3964,18 +4201,20 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
         nins += 1;
       } else {
         // destruction attempt (dana.F90:680-707)
-        if (S.qd[n - qb] < uacc) continue;
-        int m = (int)floor(S.upick[i] * (double)n) + 1;
-        if (m > n) m = n;
+        if (f64_lt(S.qd[n - qb], uacc)) continue;
+        const int m = gcmc_pick_index(S.kpick[i], n);
         // m <= 0: the walk never reaches m == 0 and ends on the last member
-        const int psel = m <= 0 ? last : warp_select(wsl, grp, ng, m);
+        const int psel = m <= 0 ? last : (reg_sel ? warp_select_reg(wsl, P0, P1, ng, m)
+                                                  : warp_select(wsl, grp, ng, m));
         if (psel < 0) {
           err = DML_E_CHOSEN_MISSING;
           err_info = t;
           break;
         }
         const int kins = psel >= ng0 ? S.pos2ins[psel - ng0] : -1;
-        const bool was_in = (wsl[psel >> 5] >> (psel & 31)) & 1u;
+        // lane 0's reading, taken before it clears the bit, for every lane
+        const bool was_in =
+            __shfl_sync(0xffffffffu, (int)((wsl[psel >> 5] >> (psel & 31)) & 1u), 0) != 0;
         if (lane == 0) {
           S.del_trial[ndel] = i;
           S.del_pos[ndel] = psel;
@@ -3990,6 +4229,11 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
             wsl[psel >> 5] &= ~(1u << (psel & 31));
             grp[psel >> 10] -= 1;
           }
+        }
+        if (was_in) {
+          const int g = psel >> 10;
+          P0 -= lane >= g;
+          P1 -= lane + 32 >= g;
         }
         ndel += 1;
         nlimbo += 1;
@@ -4645,7 +4889,7 @@ static GcmcLaunch gcmc_launch(const Dev& d, const KParams& p) {
   L.fshm = sizeof(GcmcSm) + sizeof(int) * (size_t)L.gmax;
   L.words_smem = L.fshm + 2 * sizeof(unsigned) * (size_t)L.wmax <= 200 * 1024;
   if (L.words_smem) L.fshm += 2 * sizeof(unsigned) * (size_t)L.wmax;
-  L.pshm = sizeof(int) * ((size_t)d.gcmc_rows + gcmc_pre_sort_cap());
+  L.pshm = sizeof(int) * (size_t)d.gcmc_rows;
   L.par = d.gpre != nullptr && d.grp != nullptr && p.nadj <= kGcmcMaxTrials &&
           L.fshm <= 220 * 1024 && d.gcmc_rows > 0;
   return L;
@@ -4716,6 +4960,18 @@ __global__ void check_conversions_kernel(const double* x, float* f32, double* ba
     f32[i] = f;
     back[i] = f32_to_f64(f);
   }
+}
+
+__global__ void check_pick_kernel(const unsigned long long* k, const int* n, int* m,
+                                  long long count) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x)
+    m[i] = gcmc_pick_index(k[i], n[i]);
+}
+
+int k_check_pick(const unsigned long long* k, const int* n, int* m, long long count, cudaStream_t s) {
+  check_pick_kernel<<<152 * 4, kBlock, 0, s>>>(k, n, m, count);
+  return 1;
 }
 
 int k_check_conversions(const double* x, float* f32, double* back, long long n, cudaStream_t s) {

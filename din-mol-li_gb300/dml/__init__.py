@@ -83,6 +83,7 @@ def lib():
     L.dml_launches_per_step.argtypes = [vp, P(i32)]
     L.dml_get_tuning.argtypes = [vp, P(i32), vp]
     L.dml_check_conversions.argtypes = [vp, i64, vp, vp]
+    L.dml_check_pick.argtypes = [vp, vp, i64, vp]
     L.dml_gen_bcc_slab.argtypes = [i32, i32, i32, ctypes.c_double, vp, i32]
     L.dml_gen_ions.argtypes = [ctypes.c_uint64, i32, ctypes.c_double, ctypes.c_double,
                                ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
@@ -106,6 +107,17 @@ def check_conversions(x):
     if rc:
         raise DmlError(rc, "dml_check_conversions")
     return f32, back
+
+
+def check_pick(k, n):
+    """The device's deletion pick int(k * 2^-53 * n) + 1 (capped at n)."""
+    k = np.ascontiguousarray(k, dtype=np.uint64)
+    n = np.ascontiguousarray(n, dtype=np.int32)
+    m = np.zeros(k.shape, np.int32)
+    rc = lib().dml_check_pick(k.ctypes.data, n.ctypes.data, k.size, m.ctypes.data)
+    if rc:
+        raise DmlError(rc, "dml_check_pick")
+    return m
 
 
 def bcc_slab(nx, ny, nz, a=3.51):

@@ -326,6 +326,13 @@ int dml_gen_ions(uint64_t seed, int32_t n, double box_x, double box_y, double zl
  * Host arrays; returns 0 or DML_E_CUDA. */
 int dml_check_conversions(const double* x, int64_t n, float* f32, double* back);
 
+/* Diagnostic (no counterpart in the reference): the device's deletion pick
+ * of gcmc_run, m[i] = int(upick * n[i]) + 1 capped at n[i] with upick =
+ * k[i] * 2^-53 (k[i] < 2^53), computed in integer arithmetic as the binary64
+ * product rounds (src/dana.F90:686-690).  Host arrays; returns 0 or
+ * DML_E_CUDA. */
+int dml_check_pick(const uint64_t* k, const int32_t* n, int64_t count, int32_t* m);
+
 const char* dml_strerror(int code);
 
 /* Text of the last CUDA or argument error of this context. */

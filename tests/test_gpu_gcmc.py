@@ -140,3 +140,28 @@ def test_dense_gcmc_many_trials_matches_oracle(capacity):
         assert_same_lists(g, o, "dense gcmc after %d" % done, ld=256)
     c = g.counters()
     assert c["gcmc_ins"] > 200 and c["gcmc_del"] > 200
+
+
+def test_deletion_pick_matches_binary64():
+    """The integer form of the deletion pick equals int(upick * n) + 1 (capped
+    at n) evaluated in binary64, for random draws and counts and for products
+    that sit on or next to a rounding boundary."""
+    import numpy as np
+
+    rng = np.random.default_rng(11)
+    k = rng.integers(0, 2 ** 53, 300000, dtype=np.uint64)
+    n = rng.integers(0, 2 ** 31 - 1, 300000).astype(np.int32)
+    n[:100000] = rng.integers(0, 40000, 100000)
+    # products just below an integer: upick close to j / n
+    nn = rng.integers(1, 40000, 50000)
+    j = (rng.random(50000) * nn).astype(np.int64)
+    base = (j.astype(np.float64) / nn * 2.0 ** 53).astype(np.uint64)
+    edge_k = np.concatenate([base - 2, base - 1, base, base + 1, base + 2]).clip(0, 2 ** 53 - 1)
+    edge_n = np.tile(nn, 5).astype(np.int32)
+    k = np.concatenate([k, edge_k.astype(np.uint64), np.array([0, 2 ** 53 - 1, 2 ** 53 - 1, 1], np.uint64)])
+    n = np.concatenate([n, edge_n, np.array([0, 0, 2 ** 31 - 1, 1], np.int32)])
+    m = dml.check_pick(k, n)
+    upick = k.astype(np.float64) * 2.0 ** -53  # exact: k < 2^53
+    want = np.floor(upick * n.astype(np.float64)).astype(np.int64) + 1
+    want = np.minimum(want, n.astype(np.int64))
+    assert np.array_equal(m.astype(np.int64), want)
