@@ -1648,14 +1648,8 @@ __device__ __forceinline__ void cell_order_cell(const Dev& d, int c) {
 // replicas that do not sort (and, for gcmc_run's sort, of z layers its
 // searches do not reach) are skipped whole.
 constexpr int kSmallCell = 16;
-__global__ void cell_order_small_kernel(Dev d, int force, int par) {
-  if (!force && !d.g->any_rebuild) return;
-  const int rep = d.cch_rep[blockIdx.x];
-  const RepConst& R = d.rc[rep];
-  if (!R.use_cells) return;
-  if (!force && !d.sc[rep].rebuild) return;
-  if (force && !gcmc_sorts(d, rep, par)) return;
-  const int c0 = (blockIdx.x - R.cch0) * kCellChunk;
+__device__ void cell_order_chunk(const Dev& d, const RepConst& R, int force, int chunk) {
+  const int c0 = chunk * kCellChunk;
   if (force && !R.gl_all) {
     const int layer = R.head_dim[0] * R.head_dim[1];
     const int l0 = c0 / layer, l1 = (min(c0 + kCellChunk, R.ncell) - 1) / layer;
@@ -1703,6 +1697,26 @@ __global__ void cell_order_small_kernel(Dev d, int force, int par) {
     for (int k = 0; k < kSmallCell; ++k)
       if (k < num) d.cell_atoms[start + k] = d.b2hs[v[k]];
   }
+}
+
+__global__ void cell_order_small_kernel(Dev d, int force, int par) {
+  if (!force && !d.g->any_rebuild) return;
+  const int rep = d.cch_rep[blockIdx.x];
+  const RepConst& R = d.rc[rep];
+  if (!R.use_cells) return;
+  if (!force && !d.sc[rep].rebuild) return;
+  if (force && !gcmc_sorts(d, rep, par)) return;
+  cell_order_chunk(d, R, force, blockIdx.x - R.cch0);
+}
+
+// gcmc_run's sort with the parallel trials: one block per replica, which
+// leaves at once unless the replica's trials run sequentially (the rare
+// case, where its chunks are ordered one after another).
+__global__ void gcmc_order_kernel(Dev d) {
+  const int rep = blockIdx.x;
+  const RepConst& R = d.rc[rep];
+  if (!R.use_cells || !gcmc_sorts(d, rep, 1)) return;
+  for (int q = 0; q < (R.ncell + kCellChunk - 1) / kCellChunk; ++q) cell_order_chunk(d, R, 1, q);
 }
 
 __global__ void cell_order_big_kernel(Dev d, int force) {
@@ -2721,6 +2735,25 @@ __global__ void gcmc_bin_kernel(Dev d, int par) {
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) gcmc_bin_at(d, rep, span_pos(u), par);
   if (par) gcmc_member_words(d, rep);
+}
+
+// The same two passes, one block per replica (the parallel trials: most
+// replicas leave at once).
+__global__ void gcmc_count_rep_kernel(Dev d) {
+  const int rep = blockIdx.x;
+  if (!gcmc_sorts(d, rep, 1)) return;
+  const int B = d.rc[rep].base, end = B + d.pr_cnt[rep * kCntStride + kCntGlist];
+  for (int i = B + threadIdx.x; i < end; i += blockDim.x) atomicAdd(&d.cell_count[d.glist[i].y], 1);
+}
+
+__global__ void gcmc_scatter_rep_kernel(Dev d) {
+  const int rep = blockIdx.x;
+  if (!gcmc_sorts(d, rep, 1)) return;
+  const int B = d.rc[rep].base, end = B + d.pr_cnt[rep * kCntStride + kCntGlist];
+  for (int i = B + threadIdx.x; i < end; i += blockDim.x) {
+    const int2 e = d.glist[i];
+    d.cell_atoms[d.cell_start[e.y] + atomicAdd(&d.cell_fill[e.y], 1)] = d.bslot[e.x];
+  }
 }
 
 // The cell counts of the sequentially run replicas' listed atoms.
@@ -4921,12 +4954,19 @@ int k_gcmc_trials(const Dev& d, const KParams& p, cudaStream_t s) {
     gcmc_pre_kernel<<<d.nrep, kGcmcPreThreads, L.pshm, s>>>(d, p);
     n += 1;
   }
-  if (d.any_cells) {
+  if (d.any_cells && L.par) {  // the replicas that run sequentially (usually none)
+    gcmc_count_rep_kernel<<<d.nrep, kBlock, 0, s>>>(d);
+    cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1, 1);
+    gcmc_scatter_rep_kernel<<<d.nrep, kBlock, 0, s>>>(d);
+    gcmc_order_kernel<<<d.nrep, kBlock, 0, s>>>(d);
+    cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 1);
+    n += 5;
+  } else if (d.any_cells) {  // all replicas
     const int cap = d.cap;
-    gcmc_count_kernel<<<nspan(cap), kBlock, 0, s>>>(d, L.par);
-    cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1, L.par);
-    gcmc_scatter_kernel<<<nspan(cap), kBlock, 0, s>>>(d, L.par);
-    cell_order_small_kernel<<<d.n_cch > 0 ? d.n_cch : 1, kBlock, 0, s>>>(d, 1, L.par);
+    gcmc_count_kernel<<<nspan(cap), kBlock, 0, s>>>(d, 0);
+    cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 1, 0);
+    gcmc_scatter_kernel<<<nspan(cap), kBlock, 0, s>>>(d, 0);
+    cell_order_small_kernel<<<d.n_cch > 0 ? d.n_cch : 1, kBlock, 0, s>>>(d, 1, 0);
     cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 1);
     n += 5;
   }
