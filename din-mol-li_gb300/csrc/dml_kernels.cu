@@ -1199,7 +1199,7 @@ __device__ __forceinline__ void decide_rebuild(const Dev& d, Scalars* sc, int re
   }
 }
 
-__global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots) {
+__global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p, int n_slots) {
   // grids are sized by capacity; the block's replica gives the live count
   const int rep = block_rep(d);
   const RepConst& R = d.rc[rep];
@@ -1208,19 +1208,20 @@ __global__ void pbc_dispmax_kernel(Dev d, KParams p, int n_slots) {
   const float tinyf = 1e-16f;
   const float e = R.margin;
   float a1 = tinyf, a2 = tinyf;
-  // the loads of all the thread's positions are issued before any is used
+  // The loads of all the thread's positions are issued together: a slot is
+  // live exactly when its FP32 copy carries an element (w != 0; limbo and
+  // free slots hold 0), so no state load has to come first.  Blocks past
+  // the replica's slots in use only take part in the reduction.
   bool live[kSlotU];
   float4 Pfu[kSlotU], Ofu[kSlotU];
+  const bool used = (int)blockIdx.x * kSpan < n_slots;
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) {
     const int s = span_pos(u);
-    live[u] = s < n_slots && d.state[s] == ST_LIVE;
-  }
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) {
-    const int s = span_pos(u);
-    Pfu[u] = live[u] ? d.posf[s] : make_float4(0.f, 0.f, 0.f, 0.f);
-    Ofu[u] = live[u] ? d.posf_old[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool in = used && s < n_slots;
+    Pfu[u] = in ? d.posf[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    Ofu[u] = in ? d.posf_old[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    live[u] = in && elem_of(Pfu[u]) != 0;
   }
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) {
