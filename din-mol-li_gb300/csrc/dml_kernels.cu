@@ -2344,12 +2344,26 @@ __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
   n_slots = R.base + sc->n_slots;  // positions in use end here
   double z0 = sc->z0;
   double zt = p.ztop_is_z1 != 0.0 ? sc->z1 : sc->zmax;
-  int c = 0;
+  // z > z0 && z < zt from the FP32 copy zf = RN32(z) (monotone rounding:
+  // zf beyond RN32 of a bound decides), FP64 when zf equals one (or NaN);
+  // a slot is live exactly when its FP32 copy carries an element
+  const float z0f = (float)z0, ztf = (float)zt;
+  const bool used = (int)blockIdx.x * kSpan < n_slots;
+  float4 Pf[kSlotU];
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) {
     const int s = span_pos(u);
-    if (s < n_slots && d.state[s] == ST_LIVE) {
-      double z = d.pos[s].z;
+    Pf[u] = used && s < n_slots ? d.posf[s] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  int c = 0;
+#pragma unroll
+  for (int u = 0; u < kSlotU; ++u) {
+    if (elem_of(Pf[u]) == 0) continue;
+    const float zf = Pf[u].z;
+    if (zf > z0f && zf < ztf) {
+      c += 1;
+    } else if (!(zf < z0f || zf > ztf)) {
+      const double z = d.pos[span_pos(u)].z;
       c += (z > z0 && z < zt) ? 1 : 0;
     }
   }
@@ -2639,10 +2653,11 @@ __device__ __forceinline__ void gcmc_bin_at(const Dev& d, int rep, int pos, int 
   const int s = pos;
   const int lane = threadIdx.x & 31;
   int lin = -1;
-  float4 Pf = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (R.use_cells && s < R.base + sc->n_slots && d.state[s] == ST_LIVE) {
+  // a slot is live exactly when its FP32 copy carries an element
+  const float4 Pf = R.use_cells && s < R.base + sc->n_slots ? d.posf[s]
+                                                             : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (elem_of(Pf) != 0) {
     int c1, c2, c3;
-    Pf = d.posf[s];
     cell_index3(R, Pf, d.pos + s, c1, c2, c3);
     if (c1 < 0 || c2 < 0 || c3 < 0 || c1 > R.ncells[0] + 1 || c2 > R.ncells[1] + 1 ||
         c3 > R.ncells[2] + 1) {
