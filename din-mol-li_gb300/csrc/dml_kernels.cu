@@ -4316,6 +4316,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
   }
   __syncthreads();
   const int nins = S.nins, ndel = S.ndel;
+  for (int k = tid; k < nins; k += nt) S.ins_cell[k] = pre[S.ins_trial[k]].cell;
   // the deleted atoms' hs and hs%b slots
   for (int q = tid; q < ndel; q += nt) {
     const int kins = S.del_kins[q];
@@ -4328,166 +4329,225 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
     }
   }
   __syncthreads();
-  // hs%b slots (cgroup_attach_atom, Cells.F90:105-144, and igroup's first
-  // free slot) in trial order: an insertion takes the lower of the next
-  // original hole and the lowest slot freed by an earlier deletion of this
-  // call (a min-heap), or appends when there is no hole.
-  if (tid == 0) {
-    int nb = S.ss.n_b, b_nat = S.ss.b_nat, bfree_lo = S.ss.bfree_lo, bhi = 0, nh = 0;
-    int a = 0, b = 0;
-    bool bad = false;
-    while (a < nins || b < ndel) {
-      if (b >= ndel || (a < nins && S.ins_trial[a] < S.del_trial[b])) {
-        int lbs = -1;
-        if (nb >= b_nat + 1) {
-          const int co = bhi < S.nbholes ? S.bholes[bhi] : INT_MAX;
-          const int fm = nh > 0 ? S.freed[0] : INT_MAX;
-          if (co == INT_MAX && fm == INT_MAX) {
-            if (!bad) raise_error(d.g, DML_E_INDEX, S.ins_trial[a] + 1);
-            bad = true;
-          } else if (co < fm) {
-            lbs = co;
-            ++bhi;
-          } else {
-            lbs = fm;
-            S.del_reused[S.freed_del[0]] = 1;
-            // pop the heap root
-            --nh;
-            int vx = S.freed[nh], vd = S.freed_del[nh], x = 0;
-            for (;;) {
-              int c = 2 * x + 1;
-              if (c >= nh) break;
-              if (c + 1 < nh && S.freed[c + 1] < S.freed[c]) ++c;
-              if (S.freed[c] >= vx) break;
-              S.freed[x] = S.freed[c];
-              S.freed_del[x] = S.freed_del[c];
-              x = c;
+  // Three independent parts at once: warp 0 assigns the hs%b slots, warp 1
+  // resolves the templates and Maxwell velocities, the other warps write the
+  // inserted atoms' own lists.
+  if (wid == 0) {
+    // hs%b slots (cgroup_attach_atom, Cells.F90:105-144, and igroup's first
+    // free slot) in trial order: an insertion takes the lower of the next
+    // original hole and the lowest slot freed by an earlier deletion of this
+    // call (a min-heap), or appends when there is no hole.
+    if (lane == 0) {
+      int nb = S.ss.n_b, b_nat = S.ss.b_nat, bfree_lo = S.ss.bfree_lo, bhi = 0, nh = 0;
+      int a = 0, b = 0;
+      bool bad = false;
+      while (a < nins || b < ndel) {
+        if (b >= ndel || (a < nins && S.ins_trial[a] < S.del_trial[b])) {
+          int lbs = -1;
+          if (nb >= b_nat + 1) {
+            const int co = bhi < S.nbholes ? S.bholes[bhi] : INT_MAX;
+            const int fm = nh > 0 ? S.freed[0] : INT_MAX;
+            if (co == INT_MAX && fm == INT_MAX) {
+              if (!bad) raise_error(d.g, DML_E_INDEX, S.ins_trial[a] + 1);
+              bad = true;
+            } else if (co < fm) {
+              lbs = co;
+              ++bhi;
+            } else {
+              lbs = fm;
+              S.del_reused[S.freed_del[0]] = 1;
+              // pop the heap root
+              --nh;
+              int vx = S.freed[nh], vd = S.freed_del[nh], x = 0;
+              for (;;) {
+                int c = 2 * x + 1;
+                if (c >= nh) break;
+                if (c + 1 < nh && S.freed[c + 1] < S.freed[c]) ++c;
+                if (S.freed[c] >= vx) break;
+                S.freed[x] = S.freed[c];
+                S.freed_del[x] = S.freed_del[c];
+                x = c;
+              }
+              S.freed[x] = vx;
+              S.freed_del[x] = vd;
             }
-            S.freed[x] = vx;
-            S.freed_del[x] = vd;
+          } else {
+            lbs = nb;
           }
+          if (lbs >= R.cap) {
+            if (!bad) raise_error(d.g, DML_E_CAPACITY, S.ins_trial[a] + 1);
+            bad = true;
+            lbs = -1;
+          }
+          S.ins_bslot[a] = lbs;
+          if (lbs >= 0) {
+            if (lbs == nb) nb += 1;
+            b_nat += 1;
+            bfree_lo = lbs + 1;
+          }
+          ++a;
         } else {
-          lbs = nb;
-        }
-        if (lbs >= R.cap) {
-          if (!bad) raise_error(d.g, DML_E_CAPACITY, S.ins_trial[a] + 1);
-          bad = true;
-          lbs = -1;
-        }
-        S.ins_bslot[a] = lbs;
-        if (lbs >= 0) {
-          if (lbs == nb) nb += 1;
-          b_nat += 1;
-          bfree_lo = lbs + 1;
-        }
-        ++a;
-      } else {
-        const int kins = S.del_kins[b];
-        const int bsl = kins >= 0 ? S.ins_bslot[kins] : S.del_bslot[b];
-        S.del_bslot[b] = bsl;
-        S.del_reused[b] = 0;
-        if (bsl >= 0) {
-          // push on the heap
-          int x = nh++;
-          while (x > 0 && S.freed[(x - 1) / 2] > bsl) {
-            S.freed[x] = S.freed[(x - 1) / 2];
-            S.freed_del[x] = S.freed_del[(x - 1) / 2];
-            x = (x - 1) / 2;
+          const int kins = S.del_kins[b];
+          const int bsl = kins >= 0 ? S.ins_bslot[kins] : S.del_bslot[b];
+          S.del_bslot[b] = bsl;
+          S.del_reused[b] = 0;
+          if (bsl >= 0) {
+            // push on the heap
+            int x = nh++;
+            while (x > 0 && S.freed[(x - 1) / 2] > bsl) {
+              S.freed[x] = S.freed[(x - 1) / 2];
+              S.freed_del[x] = S.freed_del[(x - 1) / 2];
+              x = (x - 1) / 2;
+            }
+            S.freed[x] = bsl;
+            S.freed_del[x] = b;
+            if (bsl < bfree_lo) bfree_lo = bsl;
+            b_nat -= 1;
           }
-          S.freed[x] = bsl;
-          S.freed_del[x] = b;
-          if (bsl < bfree_lo) bfree_lo = bsl;
-          b_nat -= 1;
+          ++b;
         }
-        ++b;
       }
+      S.ss.n_b = nb;
+      S.ss.b_nat = b_nat;
+      S.ss.bfree_lo = bfree_lo;
     }
-    S.ss.n_b = nb;
-    S.ss.b_nat = b_nat;
-    S.ss.bfree_lo = bfree_lo;
-  }
-  __syncthreads();
-
-  // Templates (the first member) and Maxwell targets (the last member) of
-  // the insertions, as hs slots; pre-call values of the pre-call atoms.
-  for (int k = tid; k < nins; k += nt) {
-    const int fp = S.ins_fpos[k], lp = S.ins_lpos[k];
-    int hr, hri, hl, hli;
-    if (fp >= ng0) {
-      hri = S.pos2ins[fp - ng0];
-      hr = B + S.ins_slot[hri];
-    } else {
-      hri = -1;
-      hr = d.gorder[B + fp];
-    }
-    if (lp >= ng0) {
-      hli = S.pos2ins[lp - ng0];
-      hl = B + S.ins_slot[hli];
-    } else {
-      hli = -1;
-      hl = d.gorder[B + lp];
-    }
-    S.href[k] = hr;
-    S.href_ins[k] = hri;
-    S.hlast[k] = hl;
-    S.hlast_ins[k] = hli;
-    if (hri < 0) {
-      // the velocity (chosen form: the first half of the slot, two doubles)
-      const double4 v0 = d.vel[hr];
-      S.tvel[k] = Vel3{v0.x, v0.y, p.mixed ? 0.0 : v0.z};
-      S.htyp[k] = d.typ[hr];
-    }
-    const GcmcTrialPre& tr = pre[S.ins_trial[k]];
-    S.nv[k] = make_float4((float)tr.nv[0], (float)tr.nv[1], (float)tr.nv[2], 0.0f);
-    S.ins_cell[k] = tr.cell;
-  }
-  __syncthreads();
-  // atom_asign copies the template's velocity, then the Maxwell velocity
-  // goes to the last member (dana.F90:659-668): resolved in trial order.
-  if (tid == 0) {
-    int nmw = 0;
-    for (int k = 0; k < nins; ++k) {
-      const int hri = S.href_ins[k];
-      Vel3 tv;
-      int typ;
-      if (hri >= 0) {
-        S.root[k] = S.root[hri];
-        typ = S.ityp[hri];
-        tv = S.fvel[hri];
+  } else if (wid == 1) {
+    // Templates (the first member) and Maxwell targets (the last member) of
+    // the insertions, as hs slots; pre-call values of the pre-call atoms.
+    for (int k = lane; k < nins; k += 32) {
+      const int fp = S.ins_fpos[k], lp = S.ins_lpos[k];
+      int hr, hri, hl, hli;
+      if (fp >= ng0) {
+        hri = S.pos2ins[fp - ng0];
+        hr = B + S.ins_slot[hri];
       } else {
-        S.root[k] = S.href[k];
-        typ = S.htyp[k];
-        tv = S.tvel[k];
-        for (int q = nmw - 1; q >= 0; --q)
-          if (S.mw_slot[q] == S.href[k]) {
-            tv = S.mw_vel[q];
-            break;
+        hri = -1;
+        hr = d.gorder[B + fp];
+      }
+      if (lp >= ng0) {
+        hli = S.pos2ins[lp - ng0];
+        hl = B + S.ins_slot[hli];
+      } else {
+        hli = -1;
+        hl = d.gorder[B + lp];
+      }
+      S.href[k] = hr;
+      S.href_ins[k] = hri;
+      S.hlast[k] = hl;
+      S.hlast_ins[k] = hli;
+      if (hri < 0) {
+        // the velocity (chosen form: the first half of the slot, two doubles)
+        const double4 v0 = d.vel[hr];
+        S.tvel[k] = Vel3{v0.x, v0.y, p.mixed ? 0.0 : v0.z};
+        S.htyp[k] = d.typ[hr];
+      }
+      const GcmcTrialPre& tr = pre[S.ins_trial[k]];
+      S.nv[k] = make_float4((float)tr.nv[0], (float)tr.nv[1], (float)tr.nv[2], 0.0f);
+    }
+    __syncwarp();
+    // atom_asign copies the template's velocity, then the Maxwell velocity
+    // goes to the last member (dana.F90:659-668): resolved in trial order.
+    if (lane == 0) {
+      int nmw = 0;
+      for (int k = 0; k < nins; ++k) {
+        const int hri = S.href_ins[k];
+        Vel3 tv;
+        int typ;
+        if (hri >= 0) {
+          S.root[k] = S.root[hri];
+          typ = S.ityp[hri];
+          tv = S.fvel[hri];
+        } else {
+          S.root[k] = S.href[k];
+          typ = S.htyp[k];
+          tv = S.tvel[k];
+          for (int q = nmw - 1; q >= 0; --q)
+            if (S.mw_slot[q] == S.href[k]) {
+              tv = S.mw_vel[q];
+              break;
+            }
+        }
+        S.ityp[k] = typ;
+        S.tvel[k] = tv;
+        S.fvel[k] = tv;
+        const double beta = p.beta_t[typ - 1];
+        const float4 nv = S.nv[k];
+        Vel3 mv = Vel3{beta * (double)nv.x, beta * (double)nv.y, beta * (double)nv.z};
+        if (p.mixed) {  // the velocity half of the slot holds FP32 values (chosen form)
+          const double4 pk = pack_f3((float)mv.x, (float)mv.y, (float)mv.z);
+          mv = Vel3{pk.x, pk.y, 0.0};
+        }
+        const int hli = S.hlast_ins[k];
+        if (hli >= 0) {
+          S.fvel[hli] = mv;
+        } else {
+          int q = 0;
+          while (q < nmw && S.mw_slot[q] != S.hlast[k]) ++q;
+          if (q == nmw) {
+            S.mw_slot[q] = S.hlast[k];
+            nmw += 1;
           }
-      }
-      S.ityp[k] = typ;
-      S.tvel[k] = tv;
-      S.fvel[k] = tv;
-      const double beta = p.beta_t[typ - 1];
-      const float4 nv = S.nv[k];
-      Vel3 mv = Vel3{beta * (double)nv.x, beta * (double)nv.y, beta * (double)nv.z};
-      if (p.mixed) {  // the velocity half of the slot holds FP32 values (chosen form)
-        const double4 pk = pack_f3((float)mv.x, (float)mv.y, (float)mv.z);
-        mv = Vel3{pk.x, pk.y, 0.0};
-      }
-      const int hli = S.hlast_ins[k];
-      if (hli >= 0) {
-        S.fvel[hli] = mv;
-      } else {
-        int q = 0;
-        while (q < nmw && S.mw_slot[q] != S.hlast[k]) ++q;
-        if (q == nmw) {
-          S.mw_slot[q] = S.hlast[k];
-          nmw += 1;
+          S.mw_vel[q] = mv;
         }
-        S.mw_vel[q] = mv;
+      }
+      S.n_mw = nmw;
+    }
+  } else {
+    // Own lists (ngroup_cells_atom, Neighbor.F90:550-603): per stencil cell,
+    // this call's earlier insertions in that cell (chain heads, most recent
+    // first), then the sorted cell; atoms deleted before the trial left.
+    for (int k = wid - 2; k < nins; k += nw - 2) {
+      if (S.ins_del[k] != INT_MAX) continue;  // deleted later: its row ends empty
+      const int i = S.ins_trial[k];
+      const GcmcTrialPre& tr = pre[i];
+      const double4 Rt = tr.r;
+      const int slot = B + S.ins_slot[k];
+      int* row = d.list + (size_t)slot * p.mnb;
+      const int mycell = lane < 27 ? tr.cells[lane] : -1;
+      // the trial's candidates, two per lane (c = lane, lane + 32), in stencil
+      // order: stencil index, and whether it joins the own list
+      const int nc = tr.n_cand;
+      int cj[2], cqq[2];
+      bool cown[2];
+  #pragma unroll
+      for (int h2 = 0; h2 < 2; ++h2) {
+        const int c = lane + 32 * h2;
+        cj[h2] = c < nc ? tr.cand[c] : -1;
+        cqq[h2] = c < nc ? (int)tr.cq[c] : -1;
+        cown[h2] = c < nc && (tr.cf[c] & 1) && !deleted_by(S, cj[h2], i, true);
+      }
+      int cnt = 0;
+      for (int q = 0; q < 27; ++q) {
+        const int cq = __shfl_sync(0xffffffffu, mycell, q);
+        for (int kb = k - 1; kb >= 0; kb -= 32) {
+          const int k2 = kb - lane;
+          bool inc = false;
+          int j = -1;
+          if (k2 >= 0 && S.ins_cell[k2] == cq && S.ins_del[k2] > i) {
+            j = B + S.ins_slot[k2];
+            double vx, vy, vz;
+            vdist_nint(R, pre[S.ins_trial[k2]].r, Rt, vx, vy, vz);
+            inc = dot3(vx, vy, vz) < p.rlist2;
+          }
+          const unsigned bal = __ballot_sync(0xffffffffu, inc);
+          const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+          if (inc && pos < p.mnb) row[pos] = j;
+          cnt += __popc(bal);
+        }
+  #pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const bool inc = cown[h2] && cqq[h2] == q;
+          const unsigned bal = __ballot_sync(0xffffffffu, inc);
+          const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+          if (inc && pos < p.mnb) row[pos] = cj[h2];
+          cnt += __popc(bal);
+        }
+      }
+      if (lane == 0) {
+        if (cnt > p.mnb) raise_error(d.g, DML_E_NEIGH_OVERFLOW, slot);
+        d.nn[slot] = cnt > p.mnb ? p.mnb : cnt;
       }
     }
-    S.n_mw = nmw;
   }
   __syncthreads();
   // the inserted atoms (atom_asign and the attach loop, dana.F90:659-675)
@@ -4554,62 +4614,6 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
     d.state[h] = ST_LIMBO;
     d.posf[h] = make_float4(pf.x, pf.y, pf.z, __int_as_float(0));
     d.alist[ap] = -1;
-  }
-  __syncthreads();
-  // Own lists (ngroup_cells_atom, Neighbor.F90:550-603): per stencil cell,
-  // this call's earlier insertions in that cell (chain heads, most recent
-  // first), then the sorted cell; atoms deleted before the trial left.
-  for (int k = wid; k < nins; k += nw) {
-    if (S.ins_del[k] != INT_MAX) continue;  // deleted later: its row ends empty
-    const int i = S.ins_trial[k];
-    const GcmcTrialPre& tr = pre[i];
-    const double4 Rt = tr.r;
-    const int slot = B + S.ins_slot[k];
-    int* row = d.list + (size_t)slot * p.mnb;
-    const int mycell = lane < 27 ? tr.cells[lane] : -1;
-    // the trial's candidates, two per lane (c = lane, lane + 32), in stencil
-    // order: stencil index, and whether it joins the own list
-    const int nc = tr.n_cand;
-    int cj[2], cqq[2];
-    bool cown[2];
-#pragma unroll
-    for (int h2 = 0; h2 < 2; ++h2) {
-      const int c = lane + 32 * h2;
-      cj[h2] = c < nc ? tr.cand[c] : -1;
-      cqq[h2] = c < nc ? (int)tr.cq[c] : -1;
-      cown[h2] = c < nc && (tr.cf[c] & 1) && !deleted_by(S, cj[h2], i, true);
-    }
-    int cnt = 0;
-    for (int q = 0; q < 27; ++q) {
-      const int cq = __shfl_sync(0xffffffffu, mycell, q);
-      for (int kb = k - 1; kb >= 0; kb -= 32) {
-        const int k2 = kb - lane;
-        bool inc = false;
-        int j = -1;
-        if (k2 >= 0 && S.ins_cell[k2] == cq && S.ins_del[k2] > i) {
-          j = B + S.ins_slot[k2];
-          double vx, vy, vz;
-          vdist_nint(R, pre[S.ins_trial[k2]].r, Rt, vx, vy, vz);
-          inc = dot3(vx, vy, vz) < p.rlist2;
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, inc);
-        const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
-        if (inc && pos < p.mnb) row[pos] = j;
-        cnt += __popc(bal);
-      }
-#pragma unroll
-      for (int h2 = 0; h2 < 2; ++h2) {
-        const bool inc = cown[h2] && cqq[h2] == q;
-        const unsigned bal = __ballot_sync(0xffffffffu, inc);
-        const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
-        if (inc && pos < p.mnb) row[pos] = cj[h2];
-        cnt += __popc(bal);
-      }
-    }
-    if (lane == 0) {
-      if (cnt > p.mnb) raise_error(d.g, DML_E_NEIGH_OVERFLOW, slot);
-      d.nn[slot] = cnt > p.mnb ? p.mnb : cnt;
-    }
   }
   __syncthreads();
   // Appends (ngroup_sort_atom): row j receives the atoms of the insertions
