@@ -2820,6 +2820,28 @@ __device__ __forceinline__ int stencil_cell_of(const RepConst& R, int t1, int t2
   return R.cell_off + (z * R.head_dim[1] + y) * R.head_dim[0] + x;
 }
 
+// Cell coordinates of a linear cell index of a replica.
+__device__ __forceinline__ void cell_coords(const RepConst& R, int lin, int& x, int& y, int& z) {
+  int l = lin - R.cell_off;
+  x = l % R.head_dim[0];
+  l /= R.head_dim[0];
+  y = l % R.head_dim[1];
+  z = l / R.head_dim[1];
+}
+
+// The stencil index (map order) of cell (a1, a2, a3) around the interior
+// cell (t1, t2, t3), or -1: the wrapped offsets in {-1, 0, 1}^3 (at least 3
+// cells along every axis, so that the 27 stencil cells are distinct).
+__device__ __forceinline__ int stencil_index_of(const RepConst& R, int t1, int t2, int t3,
+                                                int a1, int a2, int a3) {
+  int o1 = a1 - t1, o2 = a2 - t2, o3 = a3 - t3;
+  o1 = o1 > 1 ? o1 - R.ncells[0] : (o1 < -1 ? o1 + R.ncells[0] : o1);
+  o2 = o2 > 1 ? o2 - R.ncells[1] : (o2 < -1 ? o2 + R.ncells[1] : o2);
+  o3 = o3 > 1 ? o3 - R.ncells[2] : (o3 < -1 ? o3 + R.ncells[2] : o3);
+  if (o1 < -1 || o1 > 1 || o2 < -1 || o2 > 1 || o3 < -1 || o3 > 1) return -1;
+  return map_inv(o1, o2, o3);
+}
+
 __device__ __forceinline__ int stencil_cell(const RepConst& R, float4 Pf, const double4* P,
                                             int nabor) {
   int rc[3];
@@ -4053,14 +4075,26 @@ __device__ void gcmc_append_targets(const Dev& d, const KParams& p, const RepCon
   const double4 Rt = tr.r;
   const unsigned dup = tr.dup;
   const int mycell = lane < 27 ? tr.cells[lane] : -1;
+  // at least 3 cells along every axis: the stencil index from the offsets
+  const bool small = R.ncells[0] < 3 || R.ncells[1] < 3 || R.ncells[2] < 3;
+  int t1 = 0, t2 = 0, t3 = 0;
+  if (!small) cell_coords(R, tr.cell, t1, t2, t3);
   for (int k0 = 0; k0 < k; k0 += 32) {
     const int k2 = k0 + lane;
     const bool valid = k2 < k && S.ins_del[k2] == INT_MAX;
     const int c2 = valid ? S.ins_cell[k2] : -2;
     bool in = false;
-    for (int q = 0; q < 27; ++q) {
-      const int cq = __shfl_sync(0xffffffffu, mycell, q);
-      in |= valid && cq == c2 && !((dup >> q) & 1u);
+    if (!small) {
+      if (valid) {
+        int a1, a2, a3;
+        cell_coords(R, c2, a1, a2, a3);
+        in = stencil_index_of(R, t1, t2, t3, a1, a2, a3) >= 0;
+      }
+    } else {
+      for (int q = 0; q < 27; ++q) {
+        const int cq = __shfl_sync(0xffffffffu, mycell, q);
+        in |= valid && cq == c2 && !((dup >> q) & 1u);
+      }
     }
     if (in) {
       double vx, vy, vz;
@@ -4496,6 +4530,8 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
     // Own lists (ngroup_cells_atom, Neighbor.F90:550-603): per stencil cell,
     // this call's earlier insertions in that cell (chain heads, most recent
     // first), then the sorted cell; atoms deleted before the trial left.
+    // fewer than 3 cells along an axis: stencil cells repeat (general walk)
+    const bool R_small = R.ncells[0] < 3 || R.ncells[1] < 3 || R.ncells[2] < 3;
     for (int k = wid - 2; k < nins; k += nw - 2) {
       if (S.ins_del[k] != INT_MAX) continue;  // deleted later: its row ends empty
       const int i = S.ins_trial[k];
@@ -4517,6 +4553,51 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
         cown[h2] = c < nc && (tr.cf[c] & 1) && !deleted_by(S, cj[h2], i, true);
       }
       int cnt = 0;
+      if (!R_small && k <= 64) {
+        // each earlier insertion's stencil index (k2 = k - 1 - lane - 32 h2,
+        // most recent first), -1 when outside the stencil, deleted before
+        // the trial or beyond rc + skin; then the stencil walk by ballots
+        int eq[2], ej[2];
+        int t1, t2, t3;
+        cell_coords(R, tr.cell, t1, t2, t3);
+  #pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const int k2 = k - 1 - lane - 32 * h2;
+          eq[h2] = -1;
+          ej[h2] = -1;
+          if (k2 >= 0 && S.ins_del[k2] > i) {
+            int a1, a2, a3;
+            cell_coords(R, S.ins_cell[k2], a1, a2, a3);
+            const int q = stencil_index_of(R, t1, t2, t3, a1, a2, a3);
+            if (q >= 0) {
+              double vx, vy, vz;
+              vdist_nint(R, pre[S.ins_trial[k2]].r, Rt, vx, vy, vz);
+              if (dot3(vx, vy, vz) < p.rlist2) {
+                eq[h2] = q;
+                ej[h2] = B + S.ins_slot[k2];
+              }
+            }
+          }
+        }
+        for (int q = 0; q < 27; ++q) {
+  #pragma unroll
+          for (int h2 = 0; h2 < 2; ++h2) {
+            const bool inc = eq[h2] == q;
+            const unsigned bal = __ballot_sync(0xffffffffu, inc);
+            const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+            if (inc && pos < p.mnb) row[pos] = ej[h2];
+            cnt += __popc(bal);
+          }
+  #pragma unroll
+          for (int h2 = 0; h2 < 2; ++h2) {
+            const bool inc = cown[h2] && cqq[h2] == q;
+            const unsigned bal = __ballot_sync(0xffffffffu, inc);
+            const int pos = cnt + __popc(bal & ((1u << lane) - 1u));
+            if (inc && pos < p.mnb) row[pos] = cj[h2];
+            cnt += __popc(bal);
+          }
+        }
+      } else
       for (int q = 0; q < 27; ++q) {
         const int cq = __shfl_sync(0xffffffffu, mycell, q);
         for (int kb = k - 1; kb >= 0; kb -= 32) {
