@@ -67,15 +67,18 @@ NWR = 100  # output cadence of the reference's tests (entrada.ini nwr)
 # around its point (24 B each; the cell volume is bounded below by
 # (rc + skin)^3, so the count is a lower bound).
 PHASE_KERNEL = {"integrate": ("ermak_a_kernel", "ion", 120.0),
-                "force_pairs": ("force_scan_kernel", "ion", 24.0),
+                "force_pairs": ("force_scan_span_kernel + force_exact_mixed_kernel", "ion", 24.0),
                 "force_sum": ("force_fix_kernel", "ion", 105.0),
-                "test_update1": ("pbc_dispmax_kernel", "ion", 48.0),
+                "test_update1": ("pbc_dispmax_kernel + dispmax_exact_kernel", "ion", 48.0),
                 "overlap": ("overlap_* (6 kernels)", "ion", 48.0),
-                "test_update2": ("pbc_dispmax_kernel", "ion", 48.0),
+                "test_update2": ("pbc_dispmax_kernel + dispmax_exact_kernel", "ion", 48.0),
                 "commit": ("commit_kernel", "ion", 1.0),
-                "gcmc_cells": ("rebuild_prep/cell_* (5 kernels)", "slot", 32.0),
-                "gcmc": ("gcmc_kernel", "trial", 24.0),
+                "gcmc_cells": ("gcmc_prep_kernel + gcmc_bin_kernel", "slot", 32.0),
+                "gcmc": ("gcmc_pre_kernel + gcmc_fast_kernel", "trial", 24.0),
                 "rho_piston": ("calc_rho_kernel", "ion", 48.0)}
+# The roofline line reports the integrator (one kernel, the largest share of
+# the step's launch list); the other phases are listed with their times.
+ROOFLINE_PHASE = "integrate"
 LIST_PHASES = ("force_pairs", "overlap")
 
 def dist_env():
@@ -379,9 +382,12 @@ def run_reference(args, ws, rank):
 
 
 def roofline_of(sim, wl, nprof):
-    """Dominant phase of profiled steps (the graph's kernels launched one by
-    one, CUDA events at the phase boundaries): its kernel's algorithmic bytes
-    per launch / its device time per step."""
+    """The integrator's roofline in profiled steps (the graph's kernels
+    launched one by one, CUDA events at the phase boundaries): its
+    algorithmic bytes per launch / its device time per step, with every
+    phase's time per step."""
+    import dml
+
     ph = sim.profile_steps(nprof, flush_l2=True)
     c = sim.counters()
     n_ion = c["n_ref"]
@@ -391,9 +397,11 @@ def roofline_of(sim, wl, nprof):
         nn_mean = float(nn.mean())
     except Exception:  # noqa: BLE001
         pass
-    dom = max(ph, key=ph.get)
+    dom = ROOFLINE_PHASE
     t_launch = ph[dom] / nprof / 1e3  # s per step of this phase
     kernel, unit, per = PHASE_KERNEL[dom]
+    if dom == "integrate" and sim.params.integrator == dml.INTEGRATOR_BROWNIAN:
+        kernel = "brownian_kernel"
     if unit == "ion":
         units = n_ion
     elif unit == "slot":
