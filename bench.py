@@ -605,9 +605,7 @@ def run_gpu(args, ws, rank, local):
             k = min(NWR, args.steps - done)
             s2.step(k)
             done += k
-            for r in range(wl.n_rep):
-                out = (s2.get_atoms(replica=r, fields=("pos", "z")) if wl.batched
-                       else s2.get_atoms(fields=("pos", "z")))
+            for out in s2.get_atoms_batch(fields=("pos", "z")):
                 d2h += out["pos"].nbytes + out["z"].nbytes
         t1 = time.perf_counter()
         s2.close()

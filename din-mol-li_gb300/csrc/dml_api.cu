@@ -39,6 +39,10 @@ struct dml_ctx {
   float tune_us[kScanMappings] = {};  // force-scan time per mapping (1, 2, 4, 8, 16, 32 lanes per row)
   void* flush_buf = nullptr;
   std::string last_error;
+  void* h_stage = nullptr;   // pinned staging of atom downloads, grown on demand
+  size_t h_stage_bytes = 0;
+  void* d_stage = nullptr;   // device packing of batch downloads, grown on demand
+  size_t d_stage_bytes = 0;
   Scalars* h_sc = nullptr;  // pinned mirror of the per-replica state
   Global* h_g = nullptr;    // pinned mirror of the context-wide state
   std::vector<void*> allocs;
@@ -408,6 +412,10 @@ int autotune_scan(dml_ctx* c) {
       k_overlap_detect(c->D, k, c->D.cap, 0, s);
     }
   };
+  // Mappings in order of lanes; the search stops at the first one that is
+  // slower than the previous and than 1.25x the best (times grow with the
+  // lanes past the best); untimed mappings keep tune_us 0.
+  float prev = 1e30f;
   for (int v = 0; v < kScanMappings; ++v) {
     k.scan_lanes = lanes[v];
     k.near_lanes = lanes[v];
@@ -423,6 +431,8 @@ int autotune_scan(dml_ctx* c) {
       best = ms;
       best_l = lanes[v];
     }
+    if (ms > prev && ms > 1.25f * best) break;
+    prev = ms;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -599,6 +609,8 @@ void dml_destroy(dml_ctx* c) {
   for (void* p : c->allocs) cudaFree(p);
   if (c->flush_buf) cudaFree(c->flush_buf);
   if (c->h_sc) cudaFreeHost(c->h_sc);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
+  if (c->d_stage) cudaFree(c->d_stage);
   if (c->h_g) cudaFreeHost(c->h_g);
   if (c->stream) cudaStreamDestroy(c->stream);
   if (c->aux) cudaStreamDestroy(c->aux);
@@ -608,6 +620,10 @@ void dml_destroy(dml_ctx* c) {
 int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   if (!c || !atoms) return DML_E_ARG;
   if (c->loaded) return DML_E_STATE;
+  // The runtime's last-error slot is shared by every caller in the process:
+  // clear what an earlier call left there, so that the launch checks below
+  // report this call's own launches.
+  (void)cudaGetLastError();
   const int nrep = c->D.nrep;
   Dev& d = c->D;
   // capacities: positions per replica, a multiple of kSpan
@@ -765,17 +781,60 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
                o_z = sec(true, sizeof(int) * n_tot), o_rk = sec(true, sizeof(int) * n_tot),
                o_gk = sec(true, sizeof(int) * n_tot), o_off = sec(true, sizeof(int) * (nrep + 1)),
                o_skip = sec(has_skip, n_tot);
-  std::unique_ptr<unsigned char[]> hb(new unsigned char[nb > 0 ? nb : 16]);
-  auto at = [&](size_t o) { return hb.get() + o; };
-  std::memcpy(at(o_off), off.data(), sizeof(int) * (nrep + 1));
+  // The device buffer has the section layout above.  Each replica's parts of
+  // the sections are assembled in one half of a pinned buffer (pageable
+  // copies are slow here) and sent while the next replica fills the other
+  // half; an event guards a half until its copies have read it.
+  cudaStream_t st = c->stream;
+  unsigned char* db = nullptr;
+  CK(cudaMalloc(&db, nb > 0 ? nb : 16));
+  size_t per_atom = 24 + 12;  // pos; z, hs%ref and gcmc places
+  for (bool on : {has_vel, has_acel, has_force, has_pold, has_ocg}) per_atom += on ? 24 : 0;
+  per_atom += (has_epot ? 8 : 0) + (has_id ? 8 : 0) + (has_skip ? 1 : 0);
+  int nmax = 0;
+  for (int r = 0; r < nrep; ++r) nmax = std::max(nmax, atoms[r].n);
+  const size_t half = (size_t)nmax * per_atom + 16 * 16;
+  cudaError_t e = cudaSuccess;
+  if (2 * half > c->h_stage_bytes) {
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    c->h_stage = nullptr;
+    c->h_stage_bytes = 0;
+    e = cudaMallocHost(&c->h_stage, 2 * half);
+    if (e == cudaSuccess) c->h_stage_bytes = 2 * half;
+  }
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(ev[0], st);
+  if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(db + o_off, off.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice, st);
   std::memset(c->h_sc, 0, sizeof(Scalars) * nrep);
   const bool gcmc = c->P.reservoir == DML_RESERVOIR_GCMC;
-  for (int r = 0; r < nrep; ++r) {
+  int bad_z = 0;
+  for (int r = 0; r < nrep && e == cudaSuccess && !bad_z; ++r) {
     const dml_atoms* a = atoms + r;
     const int n = a->n, o = off[r];
+    e = cudaEventSynchronize(ev[r & 1]);  // the half's previous copies are done
+    if (e != cudaSuccess) break;
+    unsigned char* const base = static_cast<unsigned char*>(c->h_stage) + (size_t)(r & 1) * half;
+    size_t lo = 0;
+    struct Part {
+      size_t at, dst, bytes;
+    };
+    Part parts[16];
+    int np = 0;
+    // this replica's part of section sec_off (elem bytes per atom)
+    auto part = [&](size_t sec_off, size_t elem) -> unsigned char* {
+      if (sec_off == (size_t)-1) return nullptr;
+      unsigned char* q = base + lo;
+      parts[np++] = Part{lo, sec_off + elem * (size_t)o, elem * (size_t)n};
+      lo += (elem * (size_t)n + 15) / 16 * 16;
+      return q;
+    };
     auto put3 = [&](size_t sec_off, const double* src, double def) {
-      if (sec_off == (size_t)-1) return;
-      double* dst = reinterpret_cast<double*>(at(sec_off)) + 3 * (size_t)o;
+      double* dst = reinterpret_cast<double*>(part(sec_off, 24));
+      if (!dst) return;
       if (src) std::memcpy(dst, src, sizeof(double) * 3 * n);
       else std::fill(dst, dst + 3 * (size_t)n, def);
     };
@@ -786,18 +845,18 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     put3(o_pold, a->pos_old ? a->pos_old : a->pos, 0.0);  // pos_old defaults to pos
     put3(o_ocg, a->old_cg, 1e8);
     if (has_epot) {
-      double* dst = reinterpret_cast<double*>(at(o_epot)) + o;
+      double* dst = reinterpret_cast<double*>(part(o_epot, 8));
       if (a->epot) std::memcpy(dst, a->epot, sizeof(double) * n);
       else std::fill(dst, dst + n, 0.0);
     }
     if (has_skip) {
-      int8_t* dst = reinterpret_cast<int8_t*>(at(o_skip)) + o;
+      int8_t* dst = reinterpret_cast<int8_t*>(part(o_skip, 1));
       if (a->skip) std::memcpy(dst, a->skip, n);
       else std::memset(dst, 0, n);
     }
     int64_t max_id = n - 1;
     if (has_id) {
-      long long* dst = reinterpret_cast<long long*>(at(o_id)) + o;
+      long long* dst = reinterpret_cast<long long*>(part(o_id, 8));
       if (a->id) {
         max_id = -1;
         for (int i = 0; i < n; ++i) {
@@ -808,13 +867,16 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
         for (int i = 0; i < n; ++i) dst[i] = i;
       }
     }
-    int* zd = reinterpret_cast<int*>(at(o_z)) + o;
-    int* rk = reinterpret_cast<int*>(at(o_rk)) + o;
-    int* gk = reinterpret_cast<int*>(at(o_gk)) + o;
+    int* zd = reinterpret_cast<int*>(part(o_z, 4));
+    int* rk = reinterpret_cast<int*>(part(o_rk, 4));
+    int* gk = reinterpret_cast<int*>(part(o_gk, 4));
     int nref = 0, ng = 0;
     for (int i = 0; i < n; ++i) {
       const int z = a->z[i];
-      if (z < 1 || z > 3) return DML_E_ARG;
+      if (z < 1 || z > 3) {
+        bad_z = 1;
+        break;
+      }
       zd[i] = z;
       // hs%ref holds the mobile atoms in sys order
       const bool in_ref = a->in_ref ? a->in_ref[i] != 0 : (z != DML_Z_CG);
@@ -823,6 +885,12 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
       const bool gm = gcmc && (a->in_gcmc ? a->in_gcmc[i] != 0 : z == DML_Z_LI);
       gk[i] = gm ? ng++ : -1;
     }
+    if (bad_z) break;
+    for (int k = 0; k < np && e == cudaSuccess; ++k)
+      if (parts[k].bytes)
+        e = cudaMemcpyAsync(db + parts[k].dst, base + parts[k].at, parts[k].bytes,
+                            cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[r & 1], st);
     Scalars& S = c->h_sc[r];
     S.zmax = c->reps[r].zmax;
     S.z0 = c->reps[r].z0;
@@ -841,9 +909,18 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     S.bfree_lo = n;
     S.next_id = max_id + 1;
   }
-  cudaStream_t st = c->stream;
-  unsigned char* db = nullptr;
-  CK(cudaMalloc(&db, nb > 0 ? nb : 16));
+  // the staging halves are read by the copies: wait for them before leaving
+  if (ev[0] && ev[1]) {
+    const cudaError_t e2 = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (ev[0]) cudaEventDestroy(ev[0]);
+  if (ev[1]) cudaEventDestroy(ev[1]);
+  if (e != cudaSuccess || bad_z) {
+    cudaFree(db);
+    if (bad_z) return DML_E_ARG;
+    return cuda_fail(c, e, "staged atom upload");
+  }
   LoadIn in{};
   auto dp = [&](size_t o) -> const void* { return o == (size_t)-1 ? nullptr : db + o; };
   in.pos = static_cast<const double*>(dp(o_pos));
@@ -860,19 +937,28 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   in.off = static_cast<const int*>(dp(o_off));
   in.skip = static_cast<const int8_t*>(dp(o_skip));
   in.n_tot = n_tot;
-  cudaError_t e = cudaMemcpyAsync(db, hb.get(), nb, cudaMemcpyHostToDevice, st);
+  const char* what = "cudaMemsetAsync (index arrays)";
   // every index array of the layout starts at -1 (no atom, no slot)
   for (int* a : {d.rank, d.ref, d.bslot, d.b2hs, d.alist, d.apos, d.gorder, d.gpos})
-    if (e == cudaSuccess) e = cudaMemsetAsync(a, 0xFF, sizeof(int) * cap, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d.rc, c->rc.data(), sizeof(RepConst) * nrep, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+      what = "cudaMemsetAsync (index arrays)";
+      e = cudaMemsetAsync(a, 0xFF, sizeof(int) * cap, st);
+    }
   if (e == cudaSuccess) {
+    what = "cudaMemcpyAsync (replica constants)";
+    e = cudaMemcpyAsync(d.rc, c->rc.data(), sizeof(RepConst) * nrep, cudaMemcpyHostToDevice, st);
+  }
+  if (e == cudaSuccess) {
+    what = "load_atoms_kernel launch";
     k_load_atoms(d, c->K, in, st);
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) {
+    what = "load_atoms_kernel";
+    e = cudaStreamSynchronize(st);
+  }
   cudaFree(db);
-  if (e != cudaSuccess) return cuda_fail(c, e, "load_atoms");
+  if (e != cudaSuccess) return cuda_fail(c, e, what);
   CK(cudaMemcpyAsync(d.sc, c->h_sc, sizeof(Scalars) * nrep, cudaMemcpyHostToDevice, st));
   std::memset(c->h_g, 0, sizeof(Global));
   CK(cudaMemcpyAsync(d.g, c->h_g, sizeof(Global), cudaMemcpyHostToDevice, st));
@@ -1205,31 +1291,65 @@ int dml_get_atoms_replica(dml_ctx* c, int32_t rep, dml_atoms* a) {
   const int ns = c->h_sc[rep].n_slots, nal = c->h_sc[rep].n_alist;
   const Dev& d = c->D;
   cudaStream_t s = c->stream;
-  std::vector<int> alist(nal);
+  // One pinned buffer holds the sys%alist segment and the requested fields
+  // (16-byte aligned sections, uninitialised: every byte read is copied in).
+  const bool want_vel = a->vel || a->acel;
+  const bool want_acel = a->acel && !c->K.mixed;
+  size_t nb = 0;
+  auto sec = [&](bool on, size_t bytes) {
+    const size_t at = nb;
+    if (on) nb += (bytes + 15) / 16 * 16;
+    return at;
+  };
+  const size_t o_al = sec(true, sizeof(int) * nal), o_pos = sec(a->pos, sizeof(double4) * ns),
+               o_vel = sec(want_vel, sizeof(double4) * ns),
+               o_acel = sec(want_acel, sizeof(double4) * ns),
+               o_force = sec(a->force, sizeof(double4) * ns),
+               o_pold = sec(a->pos_old, sizeof(double4) * ns),
+               o_ocg = sec(a->old_cg, sizeof(double4) * ns),
+               o_epot = sec(a->epot, sizeof(double) * ns), o_typ = sec(a->z, ns),
+               o_skip = sec(a->skip, ns), o_ing = sec(a->in_gcmc, ns),
+               o_id = sec(a->id, sizeof(long long) * ns), o_rank = sec(a->in_ref, sizeof(int) * ns);
+  if (nb > c->h_stage_bytes) {
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    c->h_stage = nullptr;
+    c->h_stage_bytes = 0;
+    CK(cudaMallocHost(&c->h_stage, nb + nb / 4));
+    c->h_stage_bytes = nb + nb / 4;
+  }
+  char* const hs = static_cast<char*>(c->h_stage);
+  const int* alist = reinterpret_cast<const int*>(hs + o_al);
+  const double4* pos = reinterpret_cast<const double4*>(hs + o_pos);
+  const double4* vel = reinterpret_cast<const double4*>(hs + o_vel);
+  const double4* acel = reinterpret_cast<const double4*>(hs + o_acel);
+  const double4* force = reinterpret_cast<const double4*>(hs + o_force);
+  const double4* pos_old = reinterpret_cast<const double4*>(hs + o_pold);
+  const double4* old_cg = reinterpret_cast<const double4*>(hs + o_ocg);
+  const double* epot = reinterpret_cast<const double*>(hs + o_epot);
+  const int8_t* typ = reinterpret_cast<const int8_t*>(hs + o_typ);
+  const int8_t* skip = reinterpret_cast<const int8_t*>(hs + o_skip);
+  const int8_t* ing = reinterpret_cast<const int8_t*>(hs + o_ing);
+  const long long* id = reinterpret_cast<const long long*>(hs + o_id);
+  const int* rank = reinterpret_cast<const int*>(hs + o_rank);
   if (nal)
-    CK(cudaMemcpyAsync(alist.data(), d.alist + B, sizeof(int) * nal, cudaMemcpyDeviceToHost, s));
-  std::vector<double4> pos(ns), vel(ns), acel(ns), force(ns), pos_old(ns), old_cg(ns);
-  std::vector<double> epot(ns);
-  std::vector<int8_t> typ(ns), skip(ns), ing(ns);
-  std::vector<long long> id(ns);
-  std::vector<int> rank(ns);
-  auto get = [&](void* dst, const void* src, size_t elem) -> cudaError_t {
+    CK(cudaMemcpyAsync(hs + o_al, d.alist + B, sizeof(int) * nal, cudaMemcpyDeviceToHost, s));
+  auto get = [&](size_t off, const void* src, size_t elem) -> cudaError_t {
     if (!ns) return cudaSuccess;
-    return cudaMemcpyAsync(dst, (const char*)src + elem * B, elem * ns, cudaMemcpyDeviceToHost, s);
+    return cudaMemcpyAsync(hs + off, (const char*)src + elem * B, elem * ns, cudaMemcpyDeviceToHost, s);
   };
   // only the fields asked for travel (NULL outputs are skipped)
-  if (a->pos) CK(get(pos.data(), d.pos, sizeof(double4)));
-  if (a->vel || a->acel) CK(get(vel.data(), d.vel, sizeof(double4)));
-  if (a->acel && !c->K.mixed) CK(get(acel.data(), d.acel, sizeof(double4)));
-  if (a->force) CK(get(force.data(), d.force, sizeof(double4)));
-  if (a->pos_old) CK(get(pos_old.data(), d.pos_old, sizeof(double4)));
-  if (a->old_cg) CK(get(old_cg.data(), d.old_cg, sizeof(double4)));
-  if (a->epot) CK(get(epot.data(), d.epot, sizeof(double)));
-  if (a->z) CK(get(typ.data(), d.typ, 1));
-  if (a->skip) CK(get(skip.data(), d.skip, 1));
-  if (a->in_gcmc) CK(get(ing.data(), d.in_gcmc, 1));
-  if (a->id) CK(get(id.data(), d.id, sizeof(long long)));
-  if (a->in_ref) CK(get(rank.data(), d.rank, sizeof(int)));
+  if (a->pos) CK(get(o_pos, d.pos, sizeof(double4)));
+  if (want_vel) CK(get(o_vel, d.vel, sizeof(double4)));
+  if (want_acel) CK(get(o_acel, d.acel, sizeof(double4)));
+  if (a->force) CK(get(o_force, d.force, sizeof(double4)));
+  if (a->pos_old) CK(get(o_pold, d.pos_old, sizeof(double4)));
+  if (a->old_cg) CK(get(o_ocg, d.old_cg, sizeof(double4)));
+  if (a->epot) CK(get(o_epot, d.epot, sizeof(double)));
+  if (a->z) CK(get(o_typ, d.typ, 1));
+  if (a->skip) CK(get(o_skip, d.skip, 1));
+  if (a->in_gcmc) CK(get(o_ing, d.in_gcmc, 1));
+  if (a->id) CK(get(o_id, d.id, sizeof(long long)));
+  if (a->in_ref) CK(get(o_rank, d.rank, sizeof(int)));
   CK(cudaStreamSynchronize(s));
   int n = 0;
   for (int q = 0; q < nal; ++q)
@@ -1247,19 +1367,20 @@ int dml_get_atoms_replica(dml_ctx* c, int32_t rep, dml_atoms* a) {
       dst[3 * i + 1] = v.y;
       dst[3 * i + 2] = v.z;
     };
-    put(a->pos, pos[h]);
-    if (c->K.mixed) {
+    // a section is read only when its field was requested (and copied)
+    if (a->pos) put(a->pos, pos[h]);
+    if (want_vel && c->K.mixed) {
       const float4 v = unpack_f3(vel[h]);
       const float4 ac = unpack_f3(make_double4(vel[h].z, vel[h].w, 0.0, 0.0));
       put(a->vel, make_double4(v.x, v.y, v.z, 0.0));
       put(a->acel, make_double4(ac.x, ac.y, ac.z, 0.0));
-    } else {
+    } else if (want_vel) {
       put(a->vel, vel[h]);
-      put(a->acel, acel[h]);
+      if (want_acel) put(a->acel, acel[h]);
     }
-    put(a->force, force[h]);
-    put(a->pos_old, pos_old[h]);
-    put(a->old_cg, old_cg[h]);
+    if (a->force) put(a->force, force[h]);
+    if (a->pos_old) put(a->pos_old, pos_old[h]);
+    if (a->old_cg) put(a->old_cg, old_cg[h]);
     if (a->epot) a->epot[i] = epot[h];
     if (a->z) a->z[i] = typ[h];
     if (a->skip) a->skip[i] = skip[h];
@@ -1268,6 +1389,155 @@ int dml_get_atoms_replica(dml_ctx* c, int32_t rep, dml_atoms* a) {
     if (a->id) a->id[i] = id[h];
     ++i;
   }
+  return 0;
+}
+
+int dml_get_atom_counts(dml_ctx* c, int32_t* out) {
+  if (!c || !out) return DML_E_ARG;
+  if (!c->loaded) return DML_E_STATE;
+  int rc = read_scalars(c);
+  if (rc) return rc;
+  for (int r = 0; r < c->D.nrep; ++r) out[r] = c->h_sc[r].n_atoms;
+  return 0;
+}
+
+int dml_get_atoms_batch(dml_ctx* c, dml_atoms* atoms) {
+  if (!c || !atoms) return DML_E_ARG;
+  if (!c->loaded) return DML_E_STATE;
+  const int nrep = c->D.nrep;
+  const dml_atoms& a0 = atoms[0];
+  auto same = [&](const dml_atoms& a) {
+    return !a.pos == !a0.pos && !a.vel == !a0.vel && !a.acel == !a0.acel &&
+           !a.force == !a0.force && !a.pos_old == !a0.pos_old && !a.old_cg == !a0.old_cg &&
+           !a.epot == !a0.epot && !a.z == !a0.z && !a.skip == !a0.skip &&
+           !a.in_ref == !a0.in_ref && !a.in_gcmc == !a0.in_gcmc && !a.id == !a0.id;
+  };
+  for (int r = 0; r < nrep; ++r)
+    if (!same(atoms[r])) return DML_E_ARG;
+  int rc = read_scalars(c);
+  if (rc) return rc;
+  std::vector<long long> off(nrep + 1, 0);
+  for (int r = 0; r < nrep; ++r) {
+    if (atoms[r].n < c->h_sc[r].n_atoms) return DML_E_ARG;
+    off[r + 1] = off[r] + c->h_sc[r].n_atoms;
+  }
+  const long long tot = off[nrep];
+  // device sections, 16-byte aligned: the packed members, the offsets, the error word
+  size_t nb = 0;
+  auto sec = [&](bool on, size_t bytes) {
+    const size_t at = nb;
+    if (on) nb += (bytes + 15) / 16 * 16;
+    return at;
+  };
+  const size_t v3 = sizeof(double) * 3 * (size_t)tot;
+  const size_t o_pos = sec(a0.pos, v3), o_vel = sec(a0.vel, v3), o_acel = sec(a0.acel, v3),
+               o_force = sec(a0.force, v3), o_pold = sec(a0.pos_old, v3),
+               o_ocg = sec(a0.old_cg, v3), o_epot = sec(a0.epot, sizeof(double) * tot),
+               o_z = sec(a0.z, sizeof(int) * tot), o_skip = sec(a0.skip, tot),
+               o_inref = sec(a0.in_ref, tot), o_ing = sec(a0.in_gcmc, tot),
+               o_id = sec(a0.id, sizeof(long long) * tot),
+               o_off = sec(true, sizeof(long long) * (nrep + 1)), o_err = sec(true, sizeof(int));
+  if (nb > c->d_stage_bytes) {
+    if (c->d_stage) cudaFree(c->d_stage);
+    c->d_stage = nullptr;
+    c->d_stage_bytes = 0;
+    CK(cudaMalloc(&c->d_stage, nb + nb / 4));
+    c->d_stage_bytes = nb + nb / 4;
+  }
+  char* const ds = static_cast<char*>(c->d_stage);
+  cudaStream_t s = c->stream;
+  PackOut o{};
+  auto dp = [&](bool on, size_t at) -> void* { return on ? ds + at : nullptr; };
+  o.pos = static_cast<double*>(dp(a0.pos, o_pos));
+  o.vel = static_cast<double*>(dp(a0.vel, o_vel));
+  o.acel = static_cast<double*>(dp(a0.acel, o_acel));
+  o.force = static_cast<double*>(dp(a0.force, o_force));
+  o.pos_old = static_cast<double*>(dp(a0.pos_old, o_pold));
+  o.old_cg = static_cast<double*>(dp(a0.old_cg, o_ocg));
+  o.epot = static_cast<double*>(dp(a0.epot, o_epot));
+  o.z = static_cast<int*>(dp(a0.z, o_z));
+  o.skip = static_cast<int8_t*>(dp(a0.skip, o_skip));
+  o.in_ref = static_cast<int8_t*>(dp(a0.in_ref, o_inref));
+  o.in_gcmc = static_cast<int8_t*>(dp(a0.in_gcmc, o_ing));
+  o.id = static_cast<long long*>(dp(a0.id, o_id));
+  o.off = reinterpret_cast<const long long*>(ds + o_off);
+  o.err = reinterpret_cast<int*>(ds + o_err);
+  CK(cudaMemcpyAsync(ds + o_off, off.data(), sizeof(long long) * (nrep + 1),
+                     cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(ds + o_err, 0, sizeof(int), s));
+  (void)cudaGetLastError();  // an error left by an earlier caller (the slot is shared)
+  k_pack_atoms(c->D, c->K, o, s);
+  CK(cudaGetLastError());
+  // The callers' arrays (pageable memory, where a direct device copy is
+  // slow): each replica's members travel to one half of a pinned buffer
+  // while the previous replica's half is copied out on the host.
+  struct Mem {
+    bool on;
+    size_t at, elem;
+  };
+  const Mem mem[12] = {{a0.pos != nullptr, o_pos, 24},   {a0.vel != nullptr, o_vel, 24},
+                       {a0.acel != nullptr, o_acel, 24}, {a0.force != nullptr, o_force, 24},
+                       {a0.pos_old != nullptr, o_pold, 24}, {a0.old_cg != nullptr, o_ocg, 24},
+                       {a0.epot != nullptr, o_epot, 8},  {a0.z != nullptr, o_z, 4},
+                       {a0.skip != nullptr, o_skip, 1},  {a0.in_ref != nullptr, o_inref, 1},
+                       {a0.in_gcmc != nullptr, o_ing, 1}, {a0.id != nullptr, o_id, 8}};
+  size_t per_atom = 0;
+  for (const Mem& m : mem)
+    if (m.on) per_atom += m.elem;
+  long long nmax = 0;
+  for (int r = 0; r < nrep; ++r) nmax = std::max(nmax, off[r + 1] - off[r]);
+  const size_t half = ((size_t)nmax * per_atom + 15) / 16 * 16 + 16 * 12;
+  if (2 * half > c->h_stage_bytes) {
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    c->h_stage = nullptr;
+    c->h_stage_bytes = 0;
+    CK(cudaMallocHost(&c->h_stage, 2 * half));
+    c->h_stage_bytes = 2 * half;
+  }
+  cudaEvent_t ev[2];
+  CK(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
+  char* const hs = static_cast<char*>(c->h_stage);
+  auto dst_of = [&](const dml_atoms& a, int k) -> void* {
+    void* const p[12] = {a.pos, a.vel, a.acel, a.force, a.pos_old, a.old_cg,
+                         a.epot, a.z, a.skip, a.in_ref, a.in_gcmc, a.id};
+    return p[k];
+  };
+  auto issue = [&](int r) -> cudaError_t {  // replica r's members into half r % 2
+    const size_t n = (size_t)(off[r + 1] - off[r]), b = (size_t)off[r];
+    size_t at = (size_t)(r & 1) * half;
+    for (const Mem& m : mem) {
+      if (!m.on) continue;
+      if (n) {
+        const cudaError_t e = cudaMemcpyAsync(hs + at, ds + m.at + m.elem * b, m.elem * n,
+                                              cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return e;
+      }
+      at += (m.elem * n + 15) / 16 * 16;
+    }
+    return cudaEventRecord(ev[r & 1], s);
+  };
+  cudaError_t e = issue(0);
+  for (int r = 0; r < nrep && e == cudaSuccess; ++r) {
+    if (r + 1 < nrep) e = issue(r + 1);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[r & 1]);
+    if (e != cudaSuccess) break;
+    const size_t n = (size_t)(off[r + 1] - off[r]);
+    size_t at = (size_t)(r & 1) * half;
+    for (int k = 0; k < 12; ++k) {
+      if (!mem[k].on) continue;
+      if (n) std::memcpy(dst_of(atoms[r], k), hs + at, mem[k].elem * n);
+      at += (mem[k].elem * n + 15) / 16 * 16;
+    }
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if (e != cudaSuccess) return cuda_fail(c, e, "dml_get_atoms_batch copies");
+  int err = 0;
+  CK(cudaMemcpyAsync(&err, ds + o_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (err) return DML_E_STATE;  // sys%alist and the atom count disagree
+  for (int r = 0; r < nrep; ++r) atoms[r].n = (int32_t)(off[r + 1] - off[r]);
   return 0;
 }
 

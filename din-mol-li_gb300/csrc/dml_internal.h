@@ -292,6 +292,17 @@ struct LoadIn {
 
 // ---- kernel launchers (dml_kernels.cu); each returns the kernels it queued ----
 int k_load_atoms(const Dev& d, const KParams& p, const LoadIn& in, cudaStream_t s);
+// Output of dml_get_atoms_batch on the device: per member a packed array
+// over all replicas (replica r's atoms from off[r]); NULL members are skipped.
+struct PackOut {
+  double *pos, *vel, *acel, *force, *pos_old, *old_cg, *epot;
+  int* z;
+  int8_t *skip, *in_ref, *in_gcmc;
+  long long* id;
+  const long long* off;  // [nrep + 1]
+  int* err;              // set when a replica's live count differs from off
+};
+int k_pack_atoms(const Dev& d, const KParams& p, const PackOut& o, cudaStream_t s);
 int k_check_conversions(const double* x, float* f32, double* back, long long n, cudaStream_t s);
 int k_check_pick(const unsigned long long* k, const int* n, int* m, long long count, cudaStream_t s);
 int k_step_begin(const Dev& d, int near_stale, cudaStream_t s);

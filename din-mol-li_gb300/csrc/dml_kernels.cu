@@ -5115,6 +5115,77 @@ int k_check_pick(const unsigned long long* k, const int* n, int* m, long long co
   return 1;
 }
 
+// dml_get_atoms_batch: one block per replica walks its sys%alist segment in
+// rounds of the block, numbering the live entries by a block scan, and
+// writes each live atom's requested members at its place in the output.
+__global__ void pack_atoms_kernel(Dev d, KParams p, PackOut o) {
+  const int rep = blockIdx.x;
+  const int B = d.rc[rep].base, nal = d.sc[rep].n_alist;
+  const long long base = o.off[rep];
+  __shared__ int s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int q0 = 0; q0 < nal; q0 += blockDim.x) {
+    const int q = q0 + (int)threadIdx.x;
+    const int h = q < nal ? d.alist[B + q] : -1;
+    int tot;
+    const int pre = blk_scan_excl(h >= 0 ? 1 : 0, &tot);
+    const long long i = base + s_carry + pre;
+    if (h >= 0 && i < o.off[rep + 1]) {
+      auto put3 = [&](double* dst, double x, double y, double z) {
+        dst[3 * i] = x;
+        dst[3 * i + 1] = y;
+        dst[3 * i + 2] = z;
+      };
+      if (o.pos) {
+        const double4 P = d.pos[h];
+        put3(o.pos, P.x, P.y, P.z);
+      }
+      if (o.vel || o.acel) {
+        const double4 V = d.vel[h];
+        if (p.mixed) {  // FP32 velocity and acceleration in the slot (chosen form)
+          const float4 v = unpack_f3(V), a = unpack_f3(make_double4(V.z, V.w, 0.0, 0.0));
+          if (o.vel) put3(o.vel, v.x, v.y, v.z);
+          if (o.acel) put3(o.acel, a.x, a.y, a.z);
+        } else {
+          if (o.vel) put3(o.vel, V.x, V.y, V.z);
+          if (o.acel) {
+            const double4 A = d.acel[h];
+            put3(o.acel, A.x, A.y, A.z);
+          }
+        }
+      }
+      if (o.force) {
+        const double4 F = d.force[h];
+        put3(o.force, F.x, F.y, F.z);
+      }
+      if (o.pos_old) {
+        const double4 O = d.pos_old[h];
+        put3(o.pos_old, O.x, O.y, O.z);
+      }
+      if (o.old_cg) {
+        const double4 O = d.old_cg[h];
+        put3(o.old_cg, O.x, O.y, O.z);
+      }
+      if (o.epot) o.epot[i] = d.epot[h];
+      if (o.z) o.z[i] = d.typ[h];
+      if (o.skip) o.skip[i] = d.skip[h];
+      if (o.in_ref) o.in_ref[i] = d.rank[h] >= 0 ? 1 : 0;
+      if (o.in_gcmc) o.in_gcmc[i] = d.in_gcmc[h];
+      if (o.id) o.id[i] = d.id[h];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && base + s_carry != o.off[rep + 1]) atomicExch(o.err, 1);
+}
+
+int k_pack_atoms(const Dev& d, const KParams& p, const PackOut& o, cudaStream_t s) {
+  pack_atoms_kernel<<<d.nrep, 1024, 0, s>>>(d, p, o);
+  return 1;
+}
+
 int k_check_conversions(const double* x, float* f32, double* back, long long n, cudaStream_t s) {
   check_conversions_kernel<<<152 * 4, kBlock, 0, s>>>(x, f32, back, n);
   return 1;

@@ -57,6 +57,8 @@ def lib():
     L.dml_set_atoms_batch.argtypes = [vp, P(_abi.Atoms)]
     L.dml_num_replicas.argtypes = [vp]
     L.dml_get_atoms_replica.argtypes = [vp, i32, P(_abi.Atoms)]
+    L.dml_get_atoms_batch.argtypes = [vp, vp]
+    L.dml_get_atom_counts.argtypes = [vp, vp]
     L.dml_get_counters_replica.argtypes = [vp, i32, P(_abi.Counters)]
     L.dml_get_neighbors_replica.argtypes = [vp, i32, P(i32), vp, vp, i32]
     L.dml_destroy.argtypes = [vp]
@@ -283,6 +285,21 @@ class Simulation:
                         "dml_get_atoms_replica")
         n = a.n
         return {k: v[:n] for k, v in out.items()}
+
+    def get_atoms_batch(self, fields=None):
+        """Every replica's atom state (dml_get_atoms_batch): a list of dicts
+        as get_atoms(replica=r) returns, one device pass and one copy per
+        replica and field."""
+        cnt = np.zeros(self.n_rep, np.int32)
+        self._check(self.lib.dml_get_atom_counts(self.h, cnt.ctypes.data), "dml_get_atom_counts")
+        counts = [int(n) for n in cnt]
+        outs = [_abi.empty_atoms(n, fields) for n in counts]
+        arr = (_abi.Atoms * len(outs))()
+        for r, (o, n) in enumerate(zip(outs, counts)):
+            a = _abi.atoms_struct(o, n)
+            arr[r] = a
+        self._check(self.lib.dml_get_atoms_batch(self.h, arr), "dml_get_atoms_batch")
+        return [{k: v[:arr[r].n] for k, v in o.items()} for r, o in enumerate(outs)]
 
     def time_steps(self, n, flush_l2=True):
         """Device time [ms] of n steps, each bracketed by CUDA events."""

@@ -179,5 +179,5 @@ def empty_atoms(n, fields=None):
         if fields is not None and name not in fields:
             continue
         shape = (n, comp) if comp > 1 else (n,)
-        out[name] = np.zeros(shape, dtype=dt)
+        out[name] = np.empty(shape, dtype=dt)  # every element below the count is written
     return out

@@ -300,6 +300,17 @@ int dml_get_counters_replica(dml_ctx* c, int32_t rep, dml_counters* out);
 /* One replica's atoms and neighbour lists (same layout as dml_get_atoms and
  * dml_get_neighbors, which take a one-replica context). */
 int dml_get_atoms_replica(dml_ctx* c, int32_t rep, dml_atoms* a);
+
+/* Every replica's atoms at once: atoms[r] as for dml_get_atoms_replica (n
+ * the capacity on entry, the count on return; NULL members are not
+ * copied).  The members requested must be the same for every replica.  The
+ * fields are packed on the device in sys%alist order and copied to the
+ * caller's arrays, one copy per replica and member. */
+int dml_get_atoms_batch(dml_ctx* c, dml_atoms* atoms);
+
+/* The atom count of every replica (out[n_rep]), from one read of the
+ * device state: the capacities dml_get_atoms_batch needs. */
+int dml_get_atom_counts(dml_ctx* c, int32_t* out);
 int dml_get_neighbors_replica(dml_ctx* c, int32_t rep, int32_t* n_ref, int32_t* nn,
                               int32_t* list, int32_t ld);
 

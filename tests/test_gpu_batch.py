@@ -170,3 +170,29 @@ def test_batch_api_errors():
     a = dml.atoms_struct(dict(atoms[0]), len(atoms[0]["z"]))
     assert lib.dml_get_atoms(g.h, ctypes.byref(a)) == 1
     assert lib.dml_num_replicas(g.h) == 2
+
+
+@pytest.mark.parametrize("precision", [dml.PRECISION_FP64, dml.PRECISION_MIXED])
+def test_batch_download_equals_per_replica(precision):
+    """dml_get_atoms_batch packs every replica on the device: each replica's
+    arrays equal dml_get_atoms_replica's, for every member and for a subset,
+    after GCMC has left holes in sys%alist."""
+    p = systems.c5_small_params(nadj=32)
+    p.precision = precision
+    reps = [dml.replica_of(p, seed=s) for s in (7, 8, 9)]
+    atoms = [systems.c1_atoms(seed=s, n_ion=n, dmin=3.2)
+             for s, n in ((7, 200), (8, 150), (9, 260))]
+    g = dml.Simulation(p, replicas=reps)
+    g.set_atoms(atoms)
+    g.setup()
+    g.step(15)
+    full = g.get_atoms_batch()
+    sub = g.get_atoms_batch(fields=("pos", "z"))
+    assert len(full) == len(sub) == 3
+    for r in range(3):
+        one = g.get_atoms(replica=r)
+        assert set(full[r]) == set(one)
+        for k in one:
+            assert same_bits(full[r][k], one[k]), "replica %d member %s" % (r, k)
+        assert set(sub[r]) == {"pos", "z"}
+        assert same_bits(sub[r]["pos"], one["pos"]) and np.array_equal(sub[r]["z"], one["z"])
