@@ -15,6 +15,8 @@
 #include <memory>
 #include <string>
 #include <vector>
+#include <atomic>
+#include <thread>
 
 #include "../../include/dml.h"
 #include "dml_internal.h"
@@ -794,30 +796,38 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   int nmax = 0;
   for (int r = 0; r < nrep; ++r) nmax = std::max(nmax, atoms[r].n);
   const size_t half = (size_t)nmax * per_atom + 16 * 16;
+  // host threads, each with its own slot of the pinned buffer and an event
+  const int K = std::max(1, std::min({8, nrep, (int)std::thread::hardware_concurrency()}));
   cudaError_t e = cudaSuccess;
-  if (2 * half > c->h_stage_bytes) {
+  if ((size_t)K * half > c->h_stage_bytes) {
     if (c->h_stage) cudaFreeHost(c->h_stage);
     c->h_stage = nullptr;
     c->h_stage_bytes = 0;
-    e = cudaMallocHost(&c->h_stage, 2 * half);
-    if (e == cudaSuccess) c->h_stage_bytes = 2 * half;
+    e = cudaMallocHost(&c->h_stage, (size_t)K * half);
+    if (e == cudaSuccess) c->h_stage_bytes = (size_t)K * half;
   }
-  cudaEvent_t ev[2] = {nullptr, nullptr};
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventRecord(ev[0], st);
-  if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
+  std::vector<cudaEvent_t> ev(K, nullptr);
+  for (int t = 0; t < K && e == cudaSuccess; ++t) {
+    e = cudaEventCreateWithFlags(&ev[t], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[t], st);
+  }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(db + o_off, off.data(), sizeof(int) * (nrep + 1), cudaMemcpyHostToDevice, st);
   std::memset(c->h_sc, 0, sizeof(Scalars) * nrep);
   const bool gcmc = c->P.reservoir == DML_RESERVOIR_GCMC;
-  int bad_z = 0;
-  for (int r = 0; r < nrep && e == cudaSuccess && !bad_z; ++r) {
+  std::atomic<int> bad_z{0};
+  std::vector<cudaError_t> terr(K, cudaSuccess);
+  // thread t fills replicas t, t + K, ... into its slot (the slot's previous
+  // copies are waited for first) and queues their copies on the stream
+  auto worker = [&](int t) {
+    cudaError_t& te = terr[t];
+    te = cudaSetDevice(c->device);
+    for (int r = t; r < nrep && te == cudaSuccess && !bad_z.load(); r += K) {
     const dml_atoms* a = atoms + r;
     const int n = a->n, o = off[r];
-    e = cudaEventSynchronize(ev[r & 1]);  // the half's previous copies are done
-    if (e != cudaSuccess) break;
-    unsigned char* const base = static_cast<unsigned char*>(c->h_stage) + (size_t)(r & 1) * half;
+    te = cudaEventSynchronize(ev[t]);  // the slot's previous copies are done
+    if (te != cudaSuccess) break;
+    unsigned char* const base = static_cast<unsigned char*>(c->h_stage) + (size_t)t * half;
     size_t lo = 0;
     struct Part {
       size_t at, dst, bytes;
@@ -874,7 +884,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     for (int i = 0; i < n; ++i) {
       const int z = a->z[i];
       if (z < 1 || z > 3) {
-        bad_z = 1;
+        bad_z.store(1);
         break;
       }
       zd[i] = z;
@@ -885,12 +895,12 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
       const bool gm = gcmc && (a->in_gcmc ? a->in_gcmc[i] != 0 : z == DML_Z_LI);
       gk[i] = gm ? ng++ : -1;
     }
-    if (bad_z) break;
-    for (int k = 0; k < np && e == cudaSuccess; ++k)
+    if (bad_z.load()) break;
+    for (int k = 0; k < np && te == cudaSuccess; ++k)
       if (parts[k].bytes)
-        e = cudaMemcpyAsync(db + parts[k].dst, base + parts[k].at, parts[k].bytes,
-                            cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaEventRecord(ev[r & 1], st);
+        te = cudaMemcpyAsync(db + parts[k].dst, base + parts[k].at, parts[k].bytes,
+                             cudaMemcpyHostToDevice, st);
+    if (te == cudaSuccess) te = cudaEventRecord(ev[t], st);
     Scalars& S = c->h_sc[r];
     S.zmax = c->reps[r].zmax;
     S.z0 = c->reps[r].z0;
@@ -908,17 +918,31 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     S.free_lo = n;  // slots are dense after loading
     S.bfree_lo = n;
     S.next_id = max_id + 1;
+    }
+  };
+  if (e == cudaSuccess) {
+    std::vector<std::thread> th;
+    int started = 1;
+    try {
+      for (; started < K; ++started) th.emplace_back(worker, started);
+    } catch (...) {  // no more threads: the caller's thread takes the rest
+    }
+    worker(0);
+    for (int t = started; t < K; ++t) worker(t);
+    for (std::thread& x : th) x.join();
+    for (int t = 0; t < K; ++t)
+      if (e == cudaSuccess) e = terr[t];
   }
-  // the staging halves are read by the copies: wait for them before leaving
-  if (ev[0] && ev[1]) {
+  // the pinned slots are read by the copies: wait for them before leaving
+  {
     const cudaError_t e2 = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = e2;
   }
-  if (ev[0]) cudaEventDestroy(ev[0]);
-  if (ev[1]) cudaEventDestroy(ev[1]);
-  if (e != cudaSuccess || bad_z) {
+  for (cudaEvent_t x : ev)
+    if (x) cudaEventDestroy(x);
+  if (e != cudaSuccess || bad_z.load()) {
     cudaFree(db);
-    if (bad_z) return DML_E_ARG;
+    if (bad_z.load()) return DML_E_ARG;
     return cuda_fail(c, e, "staged atom upload");
   }
   LoadIn in{};
@@ -1487,51 +1511,66 @@ int dml_get_atoms_batch(dml_ctx* c, dml_atoms* atoms) {
   long long nmax = 0;
   for (int r = 0; r < nrep; ++r) nmax = std::max(nmax, off[r + 1] - off[r]);
   const size_t half = ((size_t)nmax * per_atom + 15) / 16 * 16 + 16 * 12;
-  if (2 * half > c->h_stage_bytes) {
+  // host threads, each with its own slot of the pinned buffer and an event:
+  // thread t copies replicas t, t + K, ... through its slot
+  const int K = std::max(1, std::min({8, nrep, (int)std::thread::hardware_concurrency()}));
+  if ((size_t)K * half > c->h_stage_bytes) {
     if (c->h_stage) cudaFreeHost(c->h_stage);
     c->h_stage = nullptr;
     c->h_stage_bytes = 0;
-    CK(cudaMallocHost(&c->h_stage, 2 * half));
-    c->h_stage_bytes = 2 * half;
+    CK(cudaMallocHost(&c->h_stage, (size_t)K * half));
+    c->h_stage_bytes = (size_t)K * half;
   }
-  cudaEvent_t ev[2];
-  CK(cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming));
-  CK(cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming));
-  char* const hs = static_cast<char*>(c->h_stage);
+  std::vector<cudaEvent_t> ev(K, nullptr);
+  cudaError_t e = cudaSuccess;
+  for (int t = 0; t < K && e == cudaSuccess; ++t)
+    e = cudaEventCreateWithFlags(&ev[t], cudaEventDisableTiming);
   auto dst_of = [&](const dml_atoms& a, int k) -> void* {
     void* const p[12] = {a.pos, a.vel, a.acel, a.force, a.pos_old, a.old_cg,
                          a.epot, a.z, a.skip, a.in_ref, a.in_gcmc, a.id};
     return p[k];
   };
-  auto issue = [&](int r) -> cudaError_t {  // replica r's members into half r % 2
-    const size_t n = (size_t)(off[r + 1] - off[r]), b = (size_t)off[r];
-    size_t at = (size_t)(r & 1) * half;
-    for (const Mem& m : mem) {
-      if (!m.on) continue;
-      if (n) {
-        const cudaError_t e = cudaMemcpyAsync(hs + at, ds + m.at + m.elem * b, m.elem * n,
-                                              cudaMemcpyDeviceToHost, s);
-        if (e != cudaSuccess) return e;
+  std::vector<cudaError_t> terr(K, cudaSuccess);
+  auto worker = [&](int t) {
+    cudaError_t& te = terr[t];
+    te = cudaSetDevice(c->device);
+    unsigned char* const hs = static_cast<unsigned char*>(c->h_stage) + (size_t)t * half;
+    for (int r = t; r < nrep && te == cudaSuccess; r += K) {
+      const size_t n = (size_t)(off[r + 1] - off[r]), b = (size_t)off[r];
+      if (!n) continue;
+      size_t at = 0;
+      for (const Mem& m : mem) {
+        if (!m.on) continue;
+        if (te == cudaSuccess)
+          te = cudaMemcpyAsync(hs + at, ds + m.at + m.elem * b, m.elem * n, cudaMemcpyDeviceToHost, s);
+        at += (m.elem * n + 15) / 16 * 16;
       }
-      at += (m.elem * n + 15) / 16 * 16;
+      if (te == cudaSuccess) te = cudaEventRecord(ev[t], s);
+      if (te == cudaSuccess) te = cudaEventSynchronize(ev[t]);
+      if (te != cudaSuccess) break;
+      at = 0;
+      for (int k = 0; k < 12; ++k) {
+        if (!mem[k].on) continue;
+        std::memcpy(dst_of(atoms[r], k), hs + at, mem[k].elem * n);
+        at += (mem[k].elem * n + 15) / 16 * 16;
+      }
     }
-    return cudaEventRecord(ev[r & 1], s);
   };
-  cudaError_t e = issue(0);
-  for (int r = 0; r < nrep && e == cudaSuccess; ++r) {
-    if (r + 1 < nrep) e = issue(r + 1);
-    if (e == cudaSuccess) e = cudaEventSynchronize(ev[r & 1]);
-    if (e != cudaSuccess) break;
-    const size_t n = (size_t)(off[r + 1] - off[r]);
-    size_t at = (size_t)(r & 1) * half;
-    for (int k = 0; k < 12; ++k) {
-      if (!mem[k].on) continue;
-      if (n) std::memcpy(dst_of(atoms[r], k), hs + at, mem[k].elem * n);
-      at += (mem[k].elem * n + 15) / 16 * 16;
+  if (e == cudaSuccess) {
+    std::vector<std::thread> th;
+    int started = 1;
+    try {
+      for (; started < K; ++started) th.emplace_back(worker, started);
+    } catch (...) {  // no more threads: the caller's thread takes the rest
     }
+    worker(0);
+    for (int t = started; t < K; ++t) worker(t);
+    for (std::thread& x : th) x.join();
+    for (int t = 0; t < K; ++t)
+      if (e == cudaSuccess) e = terr[t];
   }
-  cudaEventDestroy(ev[0]);
-  cudaEventDestroy(ev[1]);
+  for (cudaEvent_t x : ev)
+    if (x) cudaEventDestroy(x);
   if (e != cudaSuccess) return cuda_fail(c, e, "dml_get_atoms_batch copies");
   int err = 0;
   CK(cudaMemcpyAsync(&err, ds + o_err, sizeof(int), cudaMemcpyDeviceToHost, s));
