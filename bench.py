@@ -335,8 +335,9 @@ def force_error_probe(wl, nrep=4, steps=20):
             "tolerance": 1e-6, "within": bool(e.max() <= 1e-6)}
 
 
-def cpu_baseline_sample(wl, budget_s=12.0, max_steps=200):
-    """Oracle (serial CPU restatement) on replica 0 of the workload, plain FP64."""
+def cpu_baseline_sample(wl, budget_s=12.0, max_steps=200, warmup=0):
+    """Oracle (serial CPU restatement) on replica 0 of the workload, plain FP64;
+    `warmup` untimed steps after setup."""
     import dml
     from tests import oracle_lib
 
@@ -348,6 +349,8 @@ def cpu_baseline_sample(wl, budget_s=12.0, max_steps=200):
     o = oracle_lib.Oracle(p)
     o.set_atoms(wl.atoms[0])
     o.setup()
+    if warmup > 0:
+        o.step(warmup)
     n_ion0 = o.counters()["n_ref"]
     t0 = time.perf_counter()
     steps = 0
@@ -367,11 +370,11 @@ def run_reference(args, ws, rank):
         return 0
     wl = Workload(args.workload, 0, args.replicas)
     k = min(args.steps, 60)
-    v, steps, dt = cpu_baseline_sample(wl, budget_s=60.0, max_steps=k)
-    sample = ("%s; oracle on one replica (%d atoms), %d timed steps after setup"
-              % (wl.desc, len(wl.atoms[0]["z"]), steps))
+    v, steps, dt = cpu_baseline_sample(wl, budget_s=60.0, max_steps=k, warmup=args.warmup)
+    sample = ("%s; oracle on one replica (%d atoms), %d timed steps after setup and %d "
+              "warm-up steps" % (wl.desc, len(wl.atoms[0]["z"]), steps, args.warmup))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
-            "steps": steps, "warmup": 0, "ms_per_step": 1e3 * dt / steps,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": wl.desc, "form": "plain FP64 (CPU)"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
