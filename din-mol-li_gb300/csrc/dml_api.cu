@@ -726,6 +726,9 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.rep_of, cap);
   AL(d.rank_pre, nrep + 1);
   AL(d.reb_pre, nrep + 1);
+  AL(d.rebc_pre, nrep + 1);
+  AL(d.chunk_sum, n_cch > 0 ? n_cch : 1);
+  AL(d.chunk_base, n_cch > 0 ? n_cch : 1);
   AL(d.big_cells, ncell + 1);
   AL(d.cch_rep, n_cch > 0 ? n_cch : 1);
   {

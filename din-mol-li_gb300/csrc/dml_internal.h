@@ -262,6 +262,8 @@ struct Dev {
   int* rep_of;        // [cap] replica of every position
   int* rank_pre;      // [nrep + 1] prefix of the replicas' n_rank (rows in use),
                       // taken at the start of each step (n_rank changes in gcmc_run)
+  int* rebc_pre;      // [nrep + 1] prefix of the cell chunks of the replicas that rebuild
+  int *chunk_sum, *chunk_base;  // [n_cch] cell counts per chunk, first cell_atoms place
   int* reb_pre;       // [nrep + 1] the same prefix over the replicas whose list the
                       // last displacement test rebuilds (0 rows for the others)
   int* big_cells;     // cells too large for the per-thread sort of cell_order

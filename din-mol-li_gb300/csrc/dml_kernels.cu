@@ -1426,43 +1426,67 @@ __global__ void dispmax_exact_kernel(Dev d, KParams p, int cond,
   __syncthreads();
   if (!s_lastrep) return;
   // The last replica to decide: the rows of the replicas that rebuild (the
-  // list build walks only those), then the rebuild subgraph opens if any.
+  // list build walks only those) and their cell chunks (the cell sort walks
+  // only those), then the rebuild subgraph opens if any.
   __threadfence();
-  __shared__ int carry;
-  if (threadIdx.x == 0) carry = 0;
+  __shared__ int carry, carry2;
+  if (threadIdx.x == 0) {
+    carry = 0;
+    carry2 = 0;
+  }
   __syncthreads();
   for (int base0 = 0; base0 < d.nrep; base0 += blockDim.x) {
     const int r = base0 + threadIdx.x;
-    int v = 0;
+    int v = 0, v2 = 0;
     if (r < d.nrep) {
       const volatile Scalars* q = d.sc + r;
+      const RepConst& Rr = d.rc[r];
       v = q->rebuild ? q->n_rank : 0;
+      v2 = q->rebuild && Rr.use_cells ? (Rr.ncell + kCellChunk - 1) / kCellChunk : 0;
     }
-    int x = v;
+    int x = v, x2 = v2;
     for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
+      int y = __shfl_up_sync(0xffffffffu, x, o), y2 = __shfl_up_sync(0xffffffffu, x2, o);
+      if (lane >= o) {
+        x += y;
+        x2 += y2;
+      }
     }
-    __shared__ int wsum[32];
-    if (lane == 31) wsum[wid] = x;
+    __shared__ int wsum[32], wsum2[32];
+    if (lane == 31) {
+      wsum[wid] = x;
+      wsum2[wid] = x2;
+    }
     __syncthreads();
     if (wid == 0) {
-      int w = lane < nwarp ? wsum[lane] : 0;
+      int w = lane < nwarp ? wsum[lane] : 0, w2 = lane < nwarp ? wsum2[lane] : 0;
       for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, w, o);
-        if (lane >= o) w += y;
+        int y = __shfl_up_sync(0xffffffffu, w, o), y2 = __shfl_up_sync(0xffffffffu, w2, o);
+        if (lane >= o) {
+          w += y;
+          w2 += y2;
+        }
       }
       wsum[lane] = w;
+      wsum2[lane] = w2;
     }
     __syncthreads();
     const int pre = (wid > 0 ? wsum[wid - 1] : 0) + x - v;
-    if (r < d.nrep) d.reb_pre[r] = carry + pre;
+    const int pre2 = (wid > 0 ? wsum2[wid - 1] : 0) + x2 - v2;
+    if (r < d.nrep) {
+      d.reb_pre[r] = carry + pre;
+      d.rebc_pre[r] = carry2 + pre2;
+    }
     __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) carry += pre + v;
+    if (threadIdx.x == blockDim.x - 1) {
+      carry += pre + v;
+      carry2 += pre2 + v2;
+    }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
     d.reb_pre[d.nrep] = carry;
+    d.rebc_pre[d.nrep] = carry2;
     int any = atomicAdd(&d.g->any_rebuild, 0);
     d.g->ticket_rep = 0;
     if (any) d.g->near_stale = 1;  // lists change: the near entries too
@@ -1708,6 +1732,134 @@ __global__ void cell_order_small_kernel(Dev d, int force, int par) {
   if (!force && !d.sc[rep].rebuild) return;
   if (force && !gcmc_sorts(d, rep, par)) return;
   cell_order_chunk(d, R, force, blockIdx.x - R.cch0);
+}
+
+__device__ int blk_scan_excl(int v, int* total) {
+  // exclusive scan over a block of up to 1024 threads
+  __shared__ int ws[32];
+  __shared__ int tot;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    int w = lane < nw ? ws[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    ws[lane] = w;
+    if (lane == 31) tot = w;
+  }
+  __syncthreads();
+  int r = (wid > 0 ? ws[wid - 1] : 0) + x - v;
+  *total = tot;
+  __syncthreads();
+  return r;
+}
+
+// The list rebuild's cell sort over the chunks of the replicas that rebuild
+// only (rebc_pre), on a fixed grid: a chunk's replica and index within it.
+__device__ __forceinline__ void reb_chunk(const Dev& d, int g, int& rep, int& q) {
+  int lo = 0, hi = d.nrep - 1;  // last replica whose prefix is <= g
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (d.rebc_pre[mid] <= g) lo = mid; else hi = mid - 1;
+  }
+  rep = lo;
+  q = g - d.rebc_pre[lo];
+}
+
+// Cell starts in three passes: the count of every chunk, the prefix over a
+// replica's chunks (from its first cell_atoms place, with the sentinel
+// cell's start), and each chunk's own prefix.
+__global__ void cell_chunk_sum_kernel(Dev d) {
+  __shared__ int ws[kBlock / 32];
+  const int total = d.rebc_pre[d.nrep];
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    int rep, q;
+    reb_chunk(d, g, rep, q);
+    const RepConst& R = d.rc[rep];
+    int v = 0;
+#pragma unroll
+    for (int u = 0; u < kCellChunk / kBlock; ++u) {
+      const int ci = q * kCellChunk + u * kBlock + (int)threadIdx.x;
+      if (ci < R.ncell) v += d.cell_count[R.cell_off + ci];
+    }
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int w = 0; w < kBlock / 32; ++w) t += ws[w];
+      d.chunk_sum[R.cch0 + q] = t;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void cell_chunk_scan_kernel(Dev d) {
+  const int rep = blockIdx.x;
+  const RepConst& R = d.rc[rep];
+  if (!R.use_cells || !d.sc[rep].rebuild) return;
+  const int nq = (R.ncell + kCellChunk - 1) / kCellChunk;
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = R.base;
+  __syncthreads();
+  for (int q0 = 0; q0 < nq; q0 += blockDim.x) {
+    const int q = q0 + (int)threadIdx.x;
+    const int v = q < nq ? d.chunk_sum[R.cch0 + q] : 0;
+    int tot;
+    const int pre = blk_scan_excl(v, &tot);
+    if (q < nq) d.chunk_base[R.cch0 + q] = carry + pre;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) d.cell_start[R.cell_off + R.ncell] = carry;  // the sentinel cell
+}
+
+__global__ void cell_chunk_fill_kernel(Dev d) {
+  const int total = d.rebc_pre[d.nrep];
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    int rep, q;
+    reb_chunk(d, g, rep, q);
+    const RepConst& R = d.rc[rep];
+    int v[kCellChunk / kBlock], s = 0;
+#pragma unroll
+    for (int u = 0; u < kCellChunk / kBlock; ++u) {  // 4 consecutive cells per thread
+      const int ci = q * kCellChunk + (int)threadIdx.x * (kCellChunk / kBlock) + u;
+      v[u] = ci < R.ncell ? d.cell_count[R.cell_off + ci] : 0;
+      s += v[u];
+    }
+    int tot;
+    int run = d.chunk_base[R.cch0 + q] + blk_scan_excl(s, &tot);
+#pragma unroll
+    for (int u = 0; u < kCellChunk / kBlock; ++u) {
+      const int ci = q * kCellChunk + (int)threadIdx.x * (kCellChunk / kBlock) + u;
+      if (ci < R.ncell) {
+        d.cell_start[R.cell_off + ci] = run;
+        d.cell_fill[R.cell_off + ci] = 0;
+      }
+      run += v[u];
+    }
+  }
+}
+
+// The rebuild's in-cell order over the same chunks.
+__global__ void cell_order_reb_kernel(Dev d) {
+  const int total = d.rebc_pre[d.nrep];
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    int rep, q;
+    reb_chunk(d, g, rep, q);
+    cell_order_chunk(d, d.rc[rep], 0, q);
+    __syncthreads();
+  }
 }
 
 // gcmc_run's sort with the parallel trials: one block per replica, which
@@ -2432,34 +2584,6 @@ __global__ void piston_kernel(Dev d, KParams p, int n_slots) {
 // heads, Cells.F90:299-300) and its appends to the other lists
 // (ngroup_sort_atom, Neighbor.F90:271-318).
 
-__device__ int blk_scan_excl(int v, int* total) {
-  // exclusive scan over a block of up to 1024 threads
-  __shared__ int ws[32];
-  __shared__ int tot;
-  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int x = v;
-  for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) ws[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    int nw = (blockDim.x + 31) >> 5;
-    int w = lane < nw ? ws[lane] : 0;
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += y;
-    }
-    ws[lane] = w;
-    if (lane == 31) tot = w;
-  }
-  __syncthreads();
-  int r = (wid > 0 ? ws[wid - 1] : 0) + x - v;
-  *total = tot;
-  __syncthreads();
-  return r;
-}
 
 // First index in [lo, hi) where pred holds, or INT_MAX; every thread of the
 // block calls it (the result lands in *s_res and is returned to all).  Each
@@ -4933,12 +5057,15 @@ int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, 
   rebuild_prep_kernel<<<nspan(nmax), kBlock, 0, s>>>(d, p, n_slots, n_b, 0);
   int n = 1;
   if (d.any_cells) {
-    cell_scan_kernel<<<d.nrep, 1024, 0, s>>>(d, 0, 0);
+    // cell starts and in-cell order over the rebuilding replicas' chunks
+    cell_chunk_sum_kernel<<<152 * 8, kBlock, 0, s>>>(d);
+    cell_chunk_scan_kernel<<<d.nrep, 1024, 0, s>>>(d);
+    cell_chunk_fill_kernel<<<152 * 8, kBlock, 0, s>>>(d);
     cell_scatter_kernel<<<nspan(n_b), kBlock, 0, s>>>(d, n_b, 0);
-    cell_order_small_kernel<<<d.n_cch > 0 ? d.n_cch : 1, kBlock, 0, s>>>(d, 0, 0);
+    cell_order_reb_kernel<<<152 * 8, kBlock, 0, s>>>(d);
     cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 0);
     list_cells_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, n_rank);
-    n += 5;
+    n += 7;
   }
   if (d.any_verlet) {
     list_verlet_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, n_rank, n_b);
