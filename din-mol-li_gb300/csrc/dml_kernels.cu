@@ -1682,23 +1682,36 @@ __device__ void cell_order_chunk(const Dev& d, const RepConst& R, int force, int
         (l1 - l0 >= 63 ? ~0ull : ((2ull << (l1 - l0)) - 1ull)) << l0;
     if (l0 > 63 || !(R.gl_mask & span)) return;
   }
-#pragma unroll 1
-  for (int u = 0; u < kCellChunk / kBlock; ++u) {
+  // The thread's four cells: counts and starts loaded together, then the
+  // one-atom cells (most occupied ones, nothing to order) in two batched
+  // rounds (the atom, its hs slot); the others one by one below.
+  constexpr int U = kCellChunk / kBlock;
+  int nums[U], sts[U], one[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
     const int ci = c0 + u * kBlock + (int)threadIdx.x;
-    if (ci >= R.ncell) break;
-    const int c = R.cell_off + ci;
-    const int num = d.cell_count[c];
-    if (num == 0) continue;
+    nums[u] = ci < R.ncell ? d.cell_count[R.cell_off + ci] : 0;
+    sts[u] = ci < R.ncell ? d.cell_start[R.cell_off + ci] : 0;
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) one[u] = nums[u] == 1 ? d.cell_atoms[sts[u]] : -1;
+#pragma unroll
+  for (int u = 0; u < U; ++u)
+    if (nums[u] == 1) {
+      d.cell_count[R.cell_off + c0 + u * kBlock + (int)threadIdx.x] = 0;
+      d.cell_atoms[sts[u]] = d.b2hs[one[u]];
+    }
+#pragma unroll 1
+  for (int u = 0; u < U; ++u) {
+    const int num = nums[u];
+    if (num <= 1) continue;
+    const int c = R.cell_off + c0 + u * kBlock + (int)threadIdx.x;
     if (num > kSmallCell) {
       d.big_cells[atomicAdd(&d.g->n_big, 1)] = c;
       continue;
     }
     d.cell_count[c] = 0;
-    const int start = d.cell_start[c];
-    if (num == 1) {  // most occupied cells: nothing to order
-      d.cell_atoms[start] = d.b2hs[d.cell_atoms[start]];
-      continue;
-    }
+    const int start = sts[u];
     if (num == 2) {
       const int a = d.cell_atoms[start], b = d.cell_atoms[start + 1];
       d.cell_atoms[start] = d.b2hs[max(a, b)];
