@@ -821,9 +821,10 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   std::vector<cudaError_t> terr(K, cudaSuccess);
   // thread t fills replicas t, t + K, ... into its slot (the slot's previous
   // copies are waited for first) and queues their copies on the stream
-  auto worker = [&](int t) {
+  // own: the thread was started here (the caller's thread keeps its device)
+  auto worker = [&](int t, bool own) {
     cudaError_t& te = terr[t];
-    te = cudaSetDevice(c->device);
+    te = own ? cudaSetDevice(c->device) : cudaSuccess;
     for (int r = t; r < nrep && te == cudaSuccess && !bad_z.load(); r += K) {
     const dml_atoms* a = atoms + r;
     const int n = a->n, o = off[r];
@@ -926,11 +927,11 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     std::vector<std::thread> th;
     int started = 1;
     try {
-      for (; started < K; ++started) th.emplace_back(worker, started);
+      for (; started < K; ++started) th.emplace_back(worker, started, true);
     } catch (...) {  // no more threads: the caller's thread takes the rest
     }
-    worker(0);
-    for (int t = started; t < K; ++t) worker(t);
+    worker(0, false);
+    for (int t = started; t < K; ++t) worker(t, false);
     for (std::thread& x : th) x.join();
     for (int t = 0; t < K; ++t)
       if (e == cudaSuccess) e = terr[t];
@@ -1533,9 +1534,10 @@ int dml_get_atoms_batch(dml_ctx* c, dml_atoms* atoms) {
     return p[k];
   };
   std::vector<cudaError_t> terr(K, cudaSuccess);
-  auto worker = [&](int t) {
+  // own: the thread was started here (the caller's thread keeps its device)
+  auto worker = [&](int t, bool own) {
     cudaError_t& te = terr[t];
-    te = cudaSetDevice(c->device);
+    te = own ? cudaSetDevice(c->device) : cudaSuccess;
     unsigned char* const hs = static_cast<unsigned char*>(c->h_stage) + (size_t)t * half;
     for (int r = t; r < nrep && te == cudaSuccess; r += K) {
       const size_t n = (size_t)(off[r + 1] - off[r]), b = (size_t)off[r];
@@ -1562,11 +1564,11 @@ int dml_get_atoms_batch(dml_ctx* c, dml_atoms* atoms) {
     std::vector<std::thread> th;
     int started = 1;
     try {
-      for (; started < K; ++started) th.emplace_back(worker, started);
+      for (; started < K; ++started) th.emplace_back(worker, started, true);
     } catch (...) {  // no more threads: the caller's thread takes the rest
     }
-    worker(0);
-    for (int t = started; t < K; ++t) worker(t);
+    worker(0, false);
+    for (int t = started; t < K; ++t) worker(t, false);
     for (std::thread& x : th) x.join();
     for (int t = 0; t < K; ++t)
       if (e == cudaSuccess) e = terr[t];
