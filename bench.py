@@ -32,11 +32,13 @@ Workloads (seeded synthetic systems; the reference measures no dataset):
 Prints one JSON line.  `value` = mobile-ion steps per second over all ranks
 (device time with CUDA events, inputs resident, L2 flushed between steps).
 `e2e` = the same metric through the C ABI with host arrays: upload, setup, K
-steps with a download of every replica's positions every 100 steps (the
-reference's output cadence), wall clock.  `--impl reference` times the CPU
+steps with, every 100 steps (the reference's output cadence), what salida
+writes for every replica: the frame (positions, elements) and the observables
+of dml_salida (energy, temperature, rho, try, depo); wall clock.  `--impl reference` times the CPU
 restatement of the reference (oracle/) on this host; rank 0 only.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -610,6 +612,7 @@ def run_gpu(args, ws, rank, local):
             done += k
             for out in s2.get_atoms_batch(fields=("pos", "z")):
                 d2h += out["pos"].nbytes + out["z"].nbytes
+            d2h += ctypes.sizeof(dml.Observables) * len(s2.salida())
         t1 = time.perf_counter()
         s2.close()
         e2e = {"value": n_ion * args.steps / (t1 - t0), "unit": UNIT,

@@ -44,6 +44,7 @@ struct dml_ctx {
   size_t h_stage_bytes = 0;
   void* d_stage = nullptr;   // device packing of batch downloads, grown on demand
   size_t d_stage_bytes = 0;
+  dml_observables* d_obs = nullptr;  // dml_salida's records, one per replica
   Scalars* h_sc = nullptr;  // pinned mirror of the per-replica state
   Global* h_g = nullptr;    // pinned mirror of the context-wide state
   std::vector<void*> allocs;
@@ -612,6 +613,7 @@ void dml_destroy(dml_ctx* c) {
   if (c->h_sc) cudaFreeHost(c->h_sc);
   if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->d_stage) cudaFree(c->d_stage);
+  if (c->d_obs) cudaFree(c->d_obs);
   if (c->h_g) cudaFreeHost(c->h_g);
   if (c->stream) cudaStreamDestroy(c->stream);
   if (c->aux) cudaStreamDestroy(c->aux);
@@ -906,6 +908,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     if (te == cudaSuccess) te = cudaEventRecord(ev[t], st);
     Scalars& S = c->h_sc[r];
     S.zmax = c->reps[r].zmax;
+    S.zmax_frame = S.zmax;
     S.z0 = c->reps[r].z0;
     S.z1 = c->reps[r].z1;
     S.n_slots = n;
@@ -1417,6 +1420,19 @@ int dml_get_atoms_replica(dml_ctx* c, int32_t rep, dml_atoms* a) {
     ++i;
   }
   return 0;
+}
+
+// salida (dana.F90:1143-1183): one kernel writes every replica's record
+// and zeroes try and depo on the device.
+int dml_salida(dml_ctx* c, dml_observables* out) {
+  if (!c || !out) return DML_E_ARG;
+  if (!c->loaded) return DML_E_STATE;
+  const int nrep = c->D.nrep;
+  if (!c->d_obs) CK(cudaMalloc(&c->d_obs, sizeof(dml_observables) * nrep));
+  k_salida(c->D, c->K, c->P.kb_driver, c->d_obs, c->stream);
+  CK(cudaMemcpyAsync(out, c->d_obs, sizeof(dml_observables) * nrep, cudaMemcpyDeviceToHost,
+                     c->stream));
+  return finish(c);
 }
 
 int dml_get_atom_counts(dml_ctx* c, int32_t* out) {

@@ -71,6 +71,7 @@ struct RepConst {
 // Per-replica device state (mutable).
 struct Scalars {
   double zmax, z0, z1, rho, rho0, lohi;
+  double zmax_frame;  // zmax before the last maxz (salida's info line)
   unsigned long long try_, depo, choques, choques3, nupd, gcmc_ins, gcmc_del;
   int n_slots;     // hs%amax (local slots in use)
   int n_b;         // hs%b%amax
@@ -305,6 +306,7 @@ struct PackOut {
   int* err;              // set when a replica's live count differs from off
 };
 int k_pack_atoms(const Dev& d, const KParams& p, const PackOut& o, cudaStream_t s);
+int k_salida(const Dev& d, const KParams& p, double kb, dml_observables* out, cudaStream_t s);
 int k_check_conversions(const double* x, float* f32, double* back, long long n, cudaStream_t s);
 int k_check_pick(const unsigned long long* k, const int* n, int* m, long long count, cudaStream_t s);
 int k_step_begin(const Dev& d, int near_stale, cudaStream_t s);

@@ -2575,6 +2575,7 @@ __device__ __forceinline__ void piston_at(Dev d, KParams p, int n_slots, int rep
   }
   if (s == R.base) {
     double zm = sc->zmax;
+    sc->zmax_frame = zm;
     sc->lohi = lohi;
     sc->zmax = zm - lohi * (zm - z0);
   }
@@ -5323,6 +5324,88 @@ __global__ void pack_atoms_kernel(Dev d, KParams p, PackOut o) {
 
 int k_pack_atoms(const Dev& d, const KParams& p, const PackOut& o, cudaStream_t s) {
   pack_atoms_kernel<<<d.nrep, 1024, 0, s>>>(d, p, o);
+  return 1;
+}
+
+// salida (dana.F90:1143-1183) and kion (:1342-1376) for every replica.  One
+// block per replica gathers its sys%alist segment in rounds of the block:
+// each live atom's epot, and for a non-CG atom m (v.v) (dot_product's order,
+// no contraction), go to shared memory at the atom's place in the list.  Two
+// threads in different warps then add the round's terms in list order, one
+// at a time, as the reference's loops do: energia over every atom, vdac over
+// the non-CG ones.  Thread 0 writes the record and resets try and depo.
+__global__ void __launch_bounds__(1024) salida_kernel(Dev d, KParams p, double kb,
+                                                      dml_observables* out) {
+  const int rep = blockIdx.x;
+  const int B = d.rc[rep].base, nal = d.sc[rep].n_alist;
+  __shared__ double s_e[1024], s_v[1024];
+  __shared__ unsigned char s_m[1024];
+  __shared__ double s_vdac;
+  __shared__ int s_j;
+  double energia = 0.0, vdac = 0.0;
+  int nat = 0, j = 0;
+  for (int q0 = 0; q0 < nal; q0 += blockDim.x) {
+    const int q = q0 + (int)threadIdx.x;
+    const int h = q < nal ? d.alist[B + q] : -1;
+    int tot;
+    const int k = blk_scan_excl(h >= 0 ? 1 : 0, &tot);
+    if (h >= 0) {
+      s_e[k] = d.epot[h];
+      const int z = d.typ[h];
+      s_m[k] = z != DML_Z_CG;
+      if (z != DML_Z_CG) {
+        const double4 V = d.vel[h];
+        double vx = V.x, vy = V.y, vz = V.z;
+        if (p.mixed) {  // FP32 velocity in the slot's first 16 bytes
+          const float4 v = unpack_f3(V);
+          vx = v.x;
+          vy = v.y;
+          vz = v.z;
+        }
+        double vd = vx * vx;
+        vd = vd + vy * vy;
+        vd = vd + vz * vz;
+        s_v[k] = vd * p.mass[z - 1];
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < tot; ++i) energia = energia + s_e[i];
+      nat += tot;
+    } else if (threadIdx.x == 32) {
+      for (int i = 0; i < tot; ++i)
+        if (s_m[i]) {
+          vdac = vdac + s_v[i];
+          j += 1;
+        }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 32) {
+    s_vdac = vdac;
+    s_j = j;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Scalars* sc = d.sc + rep;
+    dml_observables r;
+    r.step = d.g->step;
+    r.energia = energia;
+    r.temp = s_vdac / ((double)s_j * 3.0 * kb);
+    r.rho = sc->rho;
+    r.zmax = sc->zmax_frame;
+    r.try_ = (int64_t)sc->try_;
+    r.depo = (int64_t)sc->depo;
+    r.n_atoms = nat;
+    r.n_mobile = s_j;
+    out[rep] = r;
+    sc->try_ = 0;
+    sc->depo = 0;
+  }
+}
+
+int k_salida(const Dev& d, const KParams& p, double kb, dml_observables* out, cudaStream_t s) {
+  salida_kernel<<<d.nrep, 1024, 0, s>>>(d, p, kb, out);
   return 1;
 }
 

@@ -76,6 +76,7 @@ def lib():
     L.dml_calc_rho.argtypes = [vp, P(ctypes.c_double)]
     L.dml_get_neighbors.argtypes = [vp, P(i32), vp, vp, i32]
     L.dml_get_counters.argtypes = [vp, P(_abi.Counters)]
+    L.dml_salida.argtypes = [vp, vp]
     L.dml_strerror.restype = ctypes.c_char_p
     L.dml_strerror.argtypes = [ctypes.c_int]
     L.dml_last_error.restype = ctypes.c_char_p
@@ -256,6 +257,14 @@ class Simulation:
 
     def reset_counters(self):
         self._check(self.lib.dml_reset_counters(self.h), "dml_reset_counters")
+
+    def salida(self):
+        """salida's observables (dml_salida): one dict per replica with
+        energia, temp, rho, zmax (the info line's), try_ and depo; try and
+        depo are zero afterwards, as salida leaves them."""
+        out = (_abi.Observables * self.n_rep)()
+        self._check(self.lib.dml_salida(self.h, out), "dml_salida")
+        return [o.as_dict() for o in out]
 
     def counters(self, replica=None):
         """Counters of one replica, or (replica=None) summed over replicas."""

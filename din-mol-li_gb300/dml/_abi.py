@@ -133,6 +133,24 @@ class Counters(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class Observables(ctypes.Structure):
+    """dml_observables: what salida writes for one replica."""
+    _fields_ = [
+        ("step", ctypes.c_int64),
+        ("energia", ctypes.c_double),
+        ("temp", ctypes.c_double),
+        ("rho", ctypes.c_double),
+        ("zmax", ctypes.c_double),
+        ("try_", ctypes.c_int64),
+        ("depo", ctypes.c_int64),
+        ("n_atoms", ctypes.c_int32),
+        ("n_mobile", ctypes.c_int32),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 # Per-atom arrays of dml_atoms: name -> (numpy dtype, components)
 ATOM_FIELDS = {
     "pos": ("f8", 3),

@@ -317,6 +317,30 @@ int dml_get_neighbors_replica(dml_ctx* c, int32_t rep, int32_t* n_ref, int32_t* 
 /* Resets try and depo (salida, src/dana.F90:1171-1174). */
 int dml_reset_counters(dml_ctx* c);
 
+/* What salida (src/dana.F90:1143-1183) writes every nwr steps for one
+ * replica: units 12 to 16 and the info line of unit 11.  The frame itself
+ * (unit 11's elements and positions) is dml_get_atoms_batch with z and pos. */
+typedef struct dml_observables {
+  int64_t step;      /* steps done */
+  double energia;    /* sum of epot over sys%alist, in list order (unit 12) */
+  double temp;       /* kion (src/dana.F90:1342-1376): the sum over the
+                        non-CG atoms, in list order, of m (v.v), divided by
+                        j * 3 * kB_ui, j their count (unit 13) */
+  double rho;        /* the last calc_rho (unit 14) */
+  double zmax;       /* zmax before the last maxz: the value on salida's
+                        info line, which maxz follows in the step */
+  int64_t try_;      /* capture attempts since the last salida (unit 15) */
+  int64_t depo;      /* captures since the last salida (unit 16) */
+  int32_t n_atoms;   /* sys%nat */
+  int32_t n_mobile;  /* j of kion */
+} dml_observables;
+
+/* salida for every replica: out[n_rep] from one device pass over the
+ * replicas' atoms, after which try and depo are zero, as salida leaves them.
+ * The sums add one term at a time in sys%alist order, as the reference's
+ * loops do, so they equal those loops bit for bit. */
+int dml_salida(dml_ctx* c, dml_observables* out);
+
 /* Initial configurations (replaces pos_inic, src/dana.F90:330-396, which
  * cannot load an electrode).  dml_gen_bcc_slab writes the 2*nx*ny*nz atoms
  * of a bcc lattice with constant a (corner then body-centre atom per cell,

@@ -184,6 +184,7 @@ struct Sim {
 
   double box[3] = {1e6, 1e6, 1e6}, one_box[3] = {1e-6, 1e-6, 1e-6};
   double z0 = 0, z1 = 0, zmax = 0, dist = 0, rho = 0, rho0 = 0;
+  double zmax_frame = 0;  // zmax before the last maxz: salida's info line
   double rhomedia = 5.775329e-4, cstdev = 1.0754306e-4;  // dana.F90:445-446
   double cc0 = 0, cc1 = 0, cc2 = 0, sdr = 0, sdv = 0, crv1 = 0, crv2 = 0, skt = 0;
   std::vector<double> ranv;
@@ -774,6 +775,7 @@ struct Sim {
   }
   // maxz (dana.F90:776-794)
   void maxz() {
+    zmax_frame = zmax;
     double lohi = ((P.h / P.tau) * ((rho0 - rho) / rho));
     for (int h : all_list) {
       Atom& pa = at[h];
@@ -1058,6 +1060,39 @@ struct Sim {
     setup_done = true;
   }
 
+  // salida (dana.F90:1143-1183): energia, the sum of epot over sys%alist
+  // (:1155-1159), and kion(sys, temp) (:1342-1376), each adding one term at a
+  // time in list order; try and depo are written, then reset (:1168-1174).
+  dml_observables salida() {
+    dml_observables r;
+    std::memset(&r, 0, sizeof r);
+    double energia = 0.0;
+    for (int h : all_list) energia = energia + at[h].epot;
+    double vdac = 0.0;
+    int j = 0;
+    for (int h : all_list) {
+      const Atom& o1 = at[h];
+      if (o1.z == DML_Z_CG) continue;  // kion skips metallic Li
+      j = j + 1;
+      double vd = 0.0;  // dot_product(vel, vel)
+      for (int l = 0; l < 3; ++l) vd = vd + o1.vel[l] * o1.vel[l];
+      vd = vd * o1.mass;
+      vdac = vdac + vd;
+    }
+    r.step = step;
+    r.energia = energia;
+    r.temp = vdac / ((double)j * 3.0 * P.kb_driver);
+    r.rho = rho;
+    r.zmax = zmax_frame;
+    r.try_ = try_;
+    r.depo = depo;
+    r.n_atoms = (int32_t)all_list.size();
+    r.n_mobile = j;
+    try_ = 0;
+    depo = 0;
+    return r;
+  }
+
   Frame frame() const {
     Frame f;
     for (int h : all_list) {
@@ -1156,6 +1191,7 @@ orc_sim* orc_create(const dml_params* p, int32_t rng_mode, int32_t idum) {
   o->s.z0 = p->z0;
   o->s.z1 = p->z1;
   o->s.zmax = p->zmax;
+  o->s.zmax_frame = p->zmax;
   o->s.rcut_b = p->rc + p->skin;
   o->s.box_setvars();
   return o;
@@ -1341,6 +1377,11 @@ int orc_get_counters(orc_sim* o, dml_counters* c) {
 int orc_reset_counters(orc_sim* o) {
   o->s.try_ = 0;
   o->s.depo = 0;
+  return 0;
+}
+
+int orc_salida(orc_sim* o, dml_observables* out) {
+  *out = o->s.salida();
   return 0;
 }
 

@@ -89,6 +89,7 @@ int orc_get_atoms(orc_sim* o, dml_atoms* a);
 int orc_get_neighbors(orc_sim* o, int32_t* n_ref, int32_t* nn, int32_t* list, int32_t ld);
 int orc_get_counters(orc_sim* o, dml_counters* c);
 int orc_reset_counters(orc_sim* o);
+int orc_salida(orc_sim* o, dml_observables* out);
 const char* orc_errmsg(orc_sim* o);
 void orc_set_step(orc_sim* o, int64_t step);
 int orc_run_reference_case(const char* dir, int32_t max_n, int32_t* n_out, double* pos_out,

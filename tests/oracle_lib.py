@@ -49,6 +49,7 @@ def load():
     lib.orc_calc_rho.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     lib.orc_get_neighbors.argtypes = [vp, ctypes.POINTER(i32), vp, vp, i32]
     lib.orc_get_counters.argtypes = [vp, ctypes.POINTER(_abi.Counters)]
+    lib.orc_salida.argtypes = [vp, ctypes.POINTER(_abi.Observables)]
     lib.orc_errmsg.restype = ctypes.c_char_p
     lib.orc_errmsg.argtypes = [vp]
     lib.orc_set_step.argtypes = [vp, i64]
@@ -165,6 +166,11 @@ class Oracle:
         c = _abi.Counters()
         self._check(self.lib.orc_get_counters(self.h, ctypes.byref(c)))
         return c.as_dict()
+
+    def salida(self):
+        r = _abi.Observables()
+        self._check(self.lib.orc_salida(self.h, ctypes.byref(r)))
+        return r.as_dict()
 
     def get_atoms(self):
         n = self.counters()["n_atoms"]

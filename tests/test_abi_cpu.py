@@ -68,3 +68,34 @@ def test_create_rejects_unsupported_options_without_gpu():
     p.box[0] = 10.0  # minimum image ambiguous at the list radius
     h = ctypes.c_void_p()
     assert dml.lib().dml_create(ctypes.byref(p), ctypes.byref(h)) == 1
+
+
+def test_ctypes_mirrors_match_header_layout(tmp_path):
+    """Every ctypes mirror of a dml.h struct has the header's size and field
+    offsets, as gcc lays the header out on this host."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+
+        pytest.skip("no C compiler")
+    mirrors = {"dml_params": dml.Params, "dml_replica": dml.Replica, "dml_atoms": dml.Atoms,
+               "dml_counters": dml.Counters, "dml_observables": dml.Observables}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "dml.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                           str(exe)])
+    got = dict(l.split() for l in subprocess.check_output([str(exe)], text=True).splitlines())
+    for cname, py in mirrors.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(got[cname + "." + f]) == getattr(py, f).offset, cname + "." + f
