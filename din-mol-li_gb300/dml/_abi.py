@@ -25,6 +25,9 @@ STATUS = {
     18: "DML_E_NEAR_OVERFLOW",
     19: "DML_E_STATE",
 }
+# E_ARG, E_CUDA, ...: the status codes by name
+for _code, _name in STATUS.items():
+    globals()[_name[len("DML_"):]] = _code
 
 INTEGRATOR_BROWNIAN, INTEGRATOR_ERMAK = 0, 1
 RESERVOIR_NONE, RESERVOIR_PISTON, RESERVOIR_CHUNKS, RESERVOIR_GCMC = 0, 1, 2, 3

@@ -165,3 +165,69 @@ def test_deletion_pick_matches_binary64():
     want = np.floor(upick * n.astype(np.float64)).astype(np.int64) + 1
     want = np.minimum(want, n.astype(np.int64))
     assert np.array_equal(m.astype(np.int64), want)
+
+
+def config5_shape(n_fill=1500):
+    """The config-5 geometry of test_config5_shape_gcmc_matches_oracle, with
+    the activity that balances a slab of n_fill ions."""
+    p = systems.c5_params(seed=3, precision=dml.PRECISION_FP64, nadj=64, cells=15, n_ion=n_fill)
+    p.box[2] = 100.0
+    p.z0, p.zmax = 60.0, 100.0
+    p.skin = 2.0
+    p.integrator = dml.INTEGRATOR_BROWNIAN
+    p.h = 1e-4
+    p.mnb = 512
+    full = dml.slab_system(15, 15, 2, 100.0, n_fill, 15.0, 100.0, 21, dmin=3.2)
+    p.act = systems.slab_activity(p, full, 3)
+    return p
+
+
+def test_reservoir_filling_from_few_ions_batch():
+    """Replicas that start with 1, 4 and 30 ions under the activity of a
+    1500-ion slab: nearly every creation is accepted, so the group grows
+    from a single member to hundreds within the run (insertions into
+    near-empty cells, first and last members changing, many rebuilds).
+    Each replica stays bit-exact to its own oracle run."""
+    from tests.test_gpu_batch import run_batch_vs_oracles
+
+    p = config5_shape()
+    reps = [dml.replica_of(p, seed=s) for s in (41, 42, 43)]
+    atoms = [dml.slab_system(15, 15, 2, 100.0, n, 15.0, 100.0, s, dmin=3.2)
+             for n, s in ((1, 41), (4, 42), (30, 43))]
+    g, orcs = run_batch_vs_oracles(p, reps, atoms, [1, 9, 30])
+    for r, o in enumerate(orcs):
+        cg, co = g.counters(replica=r), o.counters()
+        for k in ("gcmc_ins", "gcmc_del", "n_ref", "nupd"):
+            assert cg[k] == co[k], "replica %d: %s gpu %r oracle %r" % (r, k, cg[k], co[k])
+        assert same_membership(g.get_atoms(replica=r), o.get_atoms()), "replica %d" % r
+        assert cg["n_ref"] > 300
+
+
+def same_membership(a, b):
+    return np.array_equal(a["in_gcmc"], b["in_gcmc"]) and np.array_equal(a["id"], b["id"])
+
+
+@pytest.mark.parametrize("geometry", ["cells", "all_pairs"])
+def test_error_parity_empty_gcmc_group(geometry):
+    """An electrode without ions: the first trial finds no template atom in
+    the gcmc group and both sides stop with 'No more particles' at step 1
+    (werr, dana.F90:624), on the parallel path (cells) and in gcmc_kernel
+    (all-pairs lists)."""
+    if geometry == "cells":
+        p = config5_shape()
+        full = dml.slab_system(15, 15, 2, 100.0, 1, 15.0, 100.0, 5, dmin=3.2)
+    else:
+        p = systems.c5_small_params(nadj=32)
+        p.box[2] = 40.0
+        p.z0, p.zmax = 20.0, 40.0
+        full = dml.slab_system(10, 10, 2, 40.0, 1, 10.0, 40.0, 5, dmin=3.2)
+    keep = full["z"] == dml.Z_CG
+    atoms = {k: v[keep] for k, v in full.items()}
+    g, o = make_pair(p, atoms)
+    g.setup()
+    o.setup()
+    with pytest.raises(RuntimeError, match="NO_PARTICLES"):
+        o.step(1)
+    with pytest.raises(dml.DmlError) as e:
+        g.step(1)
+    assert e.value.code == dml.E_NO_PARTICLES
