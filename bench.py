@@ -34,8 +34,9 @@ Prints one JSON line.  `value` = mobile-ion steps per second over all ranks
 `e2e` = the same metric through the C ABI with host arrays: upload, setup, K
 steps with, every 100 steps (the reference's output cadence), what salida
 writes for every replica: the frame (positions, elements) and the observables
-of dml_salida (energy, temperature, rho, try, depo); wall clock.  `--impl reference` times the CPU
-restatement of the reference (oracle/) on this host; rank 0 only.
+of dml_salida (energy, temperature, rho, try, depo); wall clock.
+`--impl reference` times the CPU restatement of the reference (oracle/) on
+this host, one replica per host thread; rank 0 only.
 """
 import argparse
 import ctypes
@@ -119,6 +120,14 @@ class Dist:
     def close(self):
         if self.ws > 1:
             self.tdist.destroy_process_group()
+
+
+def job_value(dist, n_ion, steps, ms):
+    """Whole-job particle-steps/s over all ranks: every rank's mobile ions x
+    steps over the slowest rank's time `ms` (milliseconds).  Returns it
+    with that time."""
+    ms_max = dist.reduce(ms, "max")
+    return dist.reduce(n_ion, "sum") * steps / (ms_max / 1e3), ms_max
 
 
 class Clocks:
@@ -623,9 +632,7 @@ def run_gpu(args, ws, rank, local):
     ms, c0, c1, clk = timed_steps(sim, args, clocks)
     dist.barrier()
     n_ion = 0.5 * (c0["n_ref"] + c1["n_ref"])
-    ms_max = dist.reduce(ms, "max")
-    ions_all = dist.reduce(n_ion, "sum")
-    value = ions_all * args.steps / (ms_max / 1e3)
+    value, ms_max = job_value(dist, n_ion, args.steps, ms)
     per_step, per_rebuild = sim.launches_per_step()
     tuning = sim.tuning()
     launches = per_step * args.steps + per_rebuild * (c1["list_builds"] - c0["list_builds"])
