@@ -69,3 +69,35 @@ def test_c5_small_runs():
     o.step(200)
     c = o.counters()
     assert c["gcmc_ins"] > 0 and c["gcmc_del"] > 0
+
+
+def test_list_overflow_stops_at_setup():
+    """More list entries than mnb: the reference writes past list(n, mnb)
+    unchecked (src/Neighbor.F90:44,149); here the build stops with
+    DML_E_NEIGH_OVERFLOW instead."""
+    import pytest
+
+    p = systems.c1_params()
+    p.mnb = 8
+    o = oracle_lib.Oracle(p)
+    o.set_atoms(systems.c1_atoms())
+    with pytest.raises(RuntimeError, match="NEIGH_OVERFLOW"):
+        o.setup()
+
+
+def test_deposit_above_z0_stops_the_run():
+    """A contact capture of an ion above z0 ends the run ('supero z0',
+    src/dana.F90:905-908) after try, depo and the element have changed."""
+    import pytest
+
+    from tests.test_salida_cpu import capture_params
+
+    p, atoms = capture_params()
+    p.z0 = 6.0  # just above the electrode's top layer
+    o = oracle_lib.Oracle(p)
+    o.set_atoms(atoms)
+    o.setup()
+    with pytest.raises(RuntimeError, match="DENDRITE"):
+        o.step(50)
+    c = o.counters()
+    assert c["depo"] >= 1 and c["try_"] >= c["depo"]
