@@ -630,14 +630,21 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   const int nrep = c->D.nrep;
   Dev& d = c->D;
   // capacities: positions per replica, a multiple of kSpan
+  // positions are indexed with int on the device: a context holds at most
+  // kMaxPositions of them (far beyond what HBM holds at this layout)
+  constexpr long long kMaxPositions = 1LL << 30;
   int total = 0, ncell = 0, any_cells = 0, any_verlet = 0, n_cch = 0;
   for (int r = 0; r < nrep; ++r) {
     const dml_atoms* a = atoms + r;
     if (a->n <= 0 || !a->pos || !a->z) return DML_E_ARG;
-    int want = c->P.capacity > 0 ? c->P.capacity
-                                 : (c->P.reservoir == DML_RESERVOIR_GCMC ? 2 * a->n + 1024 : a->n);
-    int cap = std::max(a->n, want);
-    cap = (cap + kSpan - 1) / kSpan * kSpan;
+    const long long want = c->P.capacity > 0 ? c->P.capacity
+                           : (c->P.reservoir == DML_RESERVOIR_GCMC ? 2LL * a->n + 1024 : a->n);
+    const long long capl = (std::max<long long>(a->n, want) + kSpan - 1) / kSpan * kSpan;
+    if (total + capl > kMaxPositions) {
+      c->last_error = "capacity: more than 2^30 atom positions in one context";
+      return DML_E_CAPACITY;
+    }
+    const int cap = (int)capl;
     RepConst& R = c->rc[r];
     R.base = total;
     R.cap = cap;
@@ -663,7 +670,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   d.any_cells = any_cells;
   d.any_verlet = any_verlet;
   const int cap = total;
-  c->K.cand_cap = 16 * cap;
+  c->K.cand_cap = (int)std::min<long long>(16LL * cap, 1LL << 30);  // writes are bounded by it
   int rc = 0;
 #define AL(ptr, cnt) \
   if ((rc = dalloc(c, &(ptr), (cnt))) != 0) return rc;
