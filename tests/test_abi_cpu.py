@@ -99,3 +99,18 @@ def test_ctypes_mirrors_match_header_layout(tmp_path):
         assert int(got[cname]) == ctypes.sizeof(py), cname
         for f, _ in py._fields_:
             assert int(got[cname + "." + f]) == getattr(py, f).offset, cname + "." + f
+
+
+def test_ion_placement_errors():
+    """Random sequential addition that cannot place every ion stops with
+    DML_E_RSA (the reference's own stop, src/dana.F90:386-389); malformed
+    boxes are DML_E_ARG."""
+    import pytest
+
+    with pytest.raises(dml.DmlError) as e:
+        dml.random_ions(1, 1000, 10.0, 10.0, 0.0, 10.0, 5.0)  # 1000 ions 5 Å apart in 10^3 Å^3
+    assert e.value.code == dml.E_RSA
+    with pytest.raises(dml.DmlError) as e:
+        dml.random_ions(1, 10, -1.0, 10.0, 0.0, 10.0, 1.0)
+    assert e.value.code == dml.E_ARG
+    assert dml.random_ions(1, 0, 10.0, 10.0, 0.0, 10.0, 1.0).shape == (0, 3)
