@@ -22,16 +22,23 @@ RNG_PHILOX = 1
 _lib = None
 
 
+def oracle_build():
+    """oracle/build.py as a module of its own name (not a bare "build",
+    which an installed package of that name could shadow)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("_dml_oracle_build",
+                                                  os.path.join(ROOT, "oracle", "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
 def load():
     global _lib
     if _lib is not None:
         return _lib
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import importlib
-
-    build = importlib.import_module("build")
-    sys.path.pop(0)
-    path = build.build()
+    path = oracle_build().build()
     lib = ctypes.CDLL(path)
     vp = ctypes.c_void_p
     i32, i64 = ctypes.c_int32, ctypes.c_int64
