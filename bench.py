@@ -30,7 +30,8 @@ Workloads (seeded synthetic systems; the reference measures no dataset):
                   [--workload c5|c2|c3|c4] [--replicas R] [--form chosen|plain]
 
 Prints one JSON line.  `value` = mobile-ion steps per second over all ranks
-(device time with CUDA events, inputs resident, L2 flushed between steps).
+(device time with CUDA events, inputs resident, L2 flushed between steps);
+`value_including_electrode` counts every atom, frozen electrode included.
 `e2e` = the same metric through the C ABI with host arrays: upload, setup, K
 steps with, every 100 steps (the reference's output cadence), what salida
 writes for every replica: the frame (positions, elements) and the observables
@@ -633,6 +634,8 @@ def run_gpu(args, ws, rank, local):
     dist.barrier()
     n_ion = 0.5 * (c0["n_ref"] + c1["n_ref"])
     value, ms_max = job_value(dist, n_ion, args.steps, ms)
+    # the same rate counting every atom, frozen electrode atoms included
+    value_all, _ = job_value(dist, 0.5 * (c0["n_atoms"] + c1["n_atoms"]), args.steps, ms)
     per_step, per_rebuild = sim.launches_per_step()
     tuning = sim.tuning()
     launches = per_step * args.steps + per_rebuild * (c1["list_builds"] - c0["list_builds"])
@@ -705,6 +708,7 @@ def run_gpu(args, ws, rank, local):
     if rank != 0:
         return 0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "value_including_electrode": value_all,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 pair forces, int64 fixed-point sums, f64 integration" if form == "chosen"
