@@ -241,6 +241,14 @@ class Workload:
         self.n_rep = len(self.atoms)
         self.n_ion = sum(int((a["z"] != dml.Z_CG).sum()) for a in self.atoms)
 
+    def config(self, ws):
+        """The `config` object of both arms' lines (the same workload)."""
+        return {"workload": self.desc, "replicas": self.n_rep, "n_ion": self.n_ion,
+                "n_electrode": self.n_electrode,
+                "parallelism": "replicas" if ws > 1 else "single",
+                "l2": "GPU arm: flushed between timed steps (256 MiB write outside the timed "
+                      "events); CPU reference arm: no flush"}
+
     def params(self, precision):
         import ctypes
 
@@ -456,7 +464,7 @@ def run_reference(args, ws, rank):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
             "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": wl.desc, "form": "plain FP64 (CPU)"},
+            "data": "synthetic", "config": wl.config(ws), "form": "plain FP64 (CPU oracle)",
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthr, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -714,13 +722,10 @@ def run_gpu(args, ws, rank, local):
             "dtype": "f32 pair forces, int64 fixed-point sums, f64 integration" if form == "chosen"
             else "f64",
             "data": "synthetic",
-            "config": {"workload": wl.desc,
-                       "form": ("chosen: mixed precision, %d replicas in every launch" % wl.n_rep)
-                       if form == "chosen" else "plain FP64 (bit-exact to the oracle)",
-                       "replicas": wl.n_rep, "n_ion": wl.n_ion, "n_electrode": wl.n_electrode,
-                       "parallelism": "replicas" if ws > 1 else "single",
-                       "l2": "flushed between steps (256 MiB write outside the timed events)",
-                       "autotuner": tuning},
+            "config": wl.config(ws),
+            "form": ("chosen: mixed precision, %d replicas in every launch" % wl.n_rep)
+            if form == "chosen" else "plain FP64 (bit-exact to the oracle)",
+            "autotuner": tuning,
             "clocks": clk, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "cpu_baseline": cpu, "compare": compare, "counters": counters}
     print(json.dumps(line), flush=True)

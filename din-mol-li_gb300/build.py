@@ -1,11 +1,12 @@
 """Builds libdml.so, the GB300 (sm_103a) implementation behind include/dml.h.
 
-Three translation units compiled in parallel and linked into one shared
+Four translation units compiled in parallel and linked into one shared
 library in din-mol-li_gb300/_build/:
   csrc/dml_kernels.cu  device kernels, --fmad=false (no contraction: the
                        plain form is bit-exact to the reference order)
   csrc/dml_api.cu      C ABI and host orchestration (-ffp-contract=off)
-  csrc/dml_config.cpp  initial-configuration generators (host)
+  csrc/dml_gen.cu      initial configurations: bcc electrode (host), random
+                       sequential addition of ions (device), --fmad=false
   csrc/dml_noalloc.cu  dml_force_noalloc, scratch in a static device array
 """
 import os
@@ -32,7 +33,8 @@ UNITS = [
      ["-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]),
     ("dml_api.cu", [NVCC, "-std=c++17", "-O2"] + ARCH +
      ["-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]),
-    ("dml_config.cpp", ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off"]),
+    ("dml_gen.cu", [NVCC, "-std=c++17", "-O3", "-lineinfo", "--fmad=false"] + ARCH +
+     ["-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off"]),
 ]
 
 

@@ -1286,6 +1286,19 @@ int dml_get_counters_replica(dml_ctx* c, int32_t rep, dml_counters* o) {
   return 0;
 }
 
+int dml_get_gcmc_paths(dml_ctx* c, int32_t rep, int64_t* parallel, int64_t* sequential) {
+  if (!c || rep < 0 || rep >= c->D.nrep) return DML_E_ARG;
+  int v[kCntStride] = {0};
+  if (c->loaded) {
+    CK(cudaMemcpyAsync(v, c->D.pr_cnt + (size_t)rep * kCntStride, sizeof v,
+                       cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  if (parallel) *parallel = v[kCntGcmcPar];
+  if (sequential) *sequential = v[kCntGcmcSeq];
+  return 0;
+}
+
 // Sums over replicas for the event counters and atom counts; the geometry
 // (zmax, z0, rho, rho0) is replica 0's, max_nn and passes the maxima.
 int dml_get_counters(dml_ctx* c, dml_counters* o) {

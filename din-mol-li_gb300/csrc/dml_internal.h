@@ -32,6 +32,7 @@ constexpr int kSlotU = 4;                 // positions per thread of the per-pos
 constexpr int kSpan = kBlock * kSlotU;    // positions per block; replica capacities are multiples
 constexpr int kCellChunk = kBlock * 4;    // cells per block of the per-cell kernels
 constexpr int kCntStride = 32, kCntGlist = 0, kCntAct = 1;  // pr_cnt layout
+constexpr int kCntGcmcPar = 2, kCntGcmcSeq = 3;  // gcmc_run calls per path (diagnostic)
 
 // Replicas.  A context holds one or more independent systems ("replicas",
 // the batched form); a single system is a batch of one.  Replica r owns the

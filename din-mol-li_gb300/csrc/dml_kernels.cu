@@ -3008,6 +3008,7 @@ __device__ __forceinline__ int stencil_cell(const RepConst& R, float4 Pf, const 
 // atom in a halo cell, scan the whole group as the reference does.
 __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, int par) {
   if (par && d.grp[blockIdx.x].fast) return;  // decided by gcmc_fast_kernel
+  if (threadIdx.x == 0) d.pr_cnt[blockIdx.x * kCntStride + kCntGcmcSeq] += 1;
   // dynamic shared memory: the trials, then in-slab members per gorder chunk
   extern __shared__ double4 s_dyn[];
   GcmcTrial* const s_tr = (GcmcTrial*)s_dyn;
@@ -4253,6 +4254,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
   const int rep = blockIdx.x;
   const GcmcRepPre* const gr = d.grp + rep;
   if (!gr->fast) return;
+  if (threadIdx.x == 0) d.pr_cnt[rep * kCntStride + kCntGcmcPar] += 1;
   extern __shared__ double4 s_dyn[];
   GcmcSm& S = *reinterpret_cast<GcmcSm*>(s_dyn);
   int* const grp = reinterpret_cast<int*>(reinterpret_cast<char*>(s_dyn) + sizeof(GcmcSm));

@@ -2,13 +2,15 @@
 // (fuerza, src/dana.F90:1055-1139) over caller-provided arrays, for callers
 // that cannot allocate device memory.
 //
-// Who needs it: code that runs while a stream is being captured into a CUDA
-// graph (cudaMalloc is not allowed there), hosts whose device memory is owned
-// by another allocator or runtime (a Fortran or C driver that hands over
-// buffers it already has), and real-time loops that must not allocate.  They
-// pass inputs and outputs; the scratch the kernels need -- the per-atom
-// buckets that order the interacting list entries, as in the context path --
-// lives in one file-scope static device array of fixed size.
+// Who cannot allocate: a host program whose device memory belongs to another
+// allocator or runtime (a Fortran driver whose arrays a CUDA Fortran or
+// OpenACC runtime owns, a framework whose caching allocator has reserved the
+// free memory, so that a cudaMalloc of ours would fail); and a time-stepping
+// loop that must not call cudaMalloc or cudaFree, because cudaFree waits for
+// the whole device and both stall the host inside the loop.  Such a caller
+// passes inputs and outputs it already owns; the scratch the kernels need --
+// the per-atom buckets that order the interacting list entries, as in the
+// context path -- lives in one file-scope static device array of fixed size.
 //
 // Limits: at most kNoallocMaxAtoms (16384) atoms and kNoallocEvCap (32)
 // interacting list entries per atom per call; more atoms return
@@ -17,12 +19,17 @@
 // loads the library until the process exits.
 //
 // Set-up: the first call on a device (with that device current) takes the
-// array's device address with cudaGetSymbolAddress; make that first call
-// before any stream capture.  All calls share the array and the array keeps
-// the last call's contents: each call clears what must start at zero, and
-// calls that overlap on the GPU (different streams, or host threads) race on
-// it.  Compiled with --fmad=false, so results are bit-identical to dml_force
-// on the same positions and lists.
+// array's device address with cudaGetSymbolAddress and keeps it for later
+// calls on that device; make that first call before any stream capture.  The
+// kept address does not survive cudaDeviceReset (the module is loaded again
+// afterwards at another address): do not call this after a reset.  All calls
+// share the array and the array keeps the last call's contents: each call
+// clears what must start at zero, and calls that overlap on the GPU
+// (different streams, or host threads) race on it.  Each call ends by
+// reading its status back to the host and waiting for its stream.  When the
+// status is not 0, force and epot are left as the caller passed them.
+// Compiled with --fmad=false, so results are bit-identical to dml_force on
+// the same positions and lists.
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -166,9 +173,11 @@ __global__ void noalloc_pairs_kernel(NoallocScratch* sc, NoallocParams p, int n_
 
 // Ordered sums: hs%ref members start from zero, other atoms add to the
 // caller's values (fuerza zeroes only hs%ref, dana.F90:1067-1073).
+// A call whose pair kernel or member marks raised an error writes nothing.
 __global__ void noalloc_sum_kernel(NoallocScratch* sc, int n_atoms, double* force, double* epot) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_atoms) return;
+  if (*(volatile int*)&sc->error != 0) return;
   int cnt = sc->ev_count[s];
   bool inref = sc->is_ref[s] != 0;
   if (!inref && cnt == 0) return;

@@ -90,6 +90,8 @@ def lib():
     L.dml_gen_bcc_slab.argtypes = [i32, i32, i32, ctypes.c_double, vp, i32]
     L.dml_gen_ions.argtypes = [ctypes.c_uint64, i32, ctypes.c_double, ctypes.c_double,
                                ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
+    L.dml_gen_ions_batch.argtypes = [i32, P(_abi.IonSpec), vp, vp]
+    L.dml_get_gcmc_paths.argtypes = [vp, i32, P(i64), P(i64)]
     _lib = L
     return L
 
@@ -134,12 +136,28 @@ def bcc_slab(nx, ny, nz, a=3.51):
 
 
 def random_ions(seed, n, box_x, box_y, zlo, zhi, dmin):
-    """RSA ions with minimum separation dmin (x,y periodic)."""
+    """RSA ions with minimum separation dmin (x,y periodic), placed on the GPU."""
     out = np.zeros((n, 3))
     rc = lib().dml_gen_ions(seed, n, box_x, box_y, zlo, zhi, dmin, out.ctypes.data)
     if rc < 0:
         raise DmlError(-rc, "dml_gen_ions")
     return out
+
+
+def random_ions_batch(specs):
+    """RSA ions of several systems in one GPU launch (dml_gen_ions_batch).
+    specs: sequence of (seed, n, box_x, box_y, zlo, zhi, dmin).  Returns
+    (list of [n][3] arrays, per-system status array, call status)."""
+    arr = (_abi.IonSpec * len(specs))(*[_abi.ion_spec(*s) for s in specs])
+    total = sum(int(s[1]) for s in specs)
+    out = np.zeros((total, 3))
+    st = np.zeros(len(specs), np.int32)
+    rc = lib().dml_gen_ions_batch(len(specs), arr, out.ctypes.data, st.ctypes.data)
+    parts, off = [], 0
+    for s in specs:
+        parts.append(out[off:off + int(s[1])].copy())
+        off += int(s[1])
+    return parts, st, rc
 
 
 def slab_system(nx, ny, nz_slab, box_z, n_ion, zlo, zhi, seed, a=3.51, dmin=2.5):
@@ -343,6 +361,13 @@ class Simulation:
         if n < 0:
             raise DmlError(-n, "dml_launches_per_step")
         return n, r.value
+
+    def gcmc_paths(self, replica=0):
+        """(parallel, sequential) gcmc_run calls of a replica so far."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.dml_get_gcmc_paths(self.h, replica, ctypes.byref(a),
+                                                 ctypes.byref(b)), "dml_get_gcmc_paths")
+        return a.value, b.value
 
     def get_neighbors(self, ld, replica=None):
         n_ref = self.counters(replica)["n_ref"]

@@ -48,6 +48,24 @@ class Replica(ctypes.Structure):
     ]
 
 
+class IonSpec(ctypes.Structure):
+    """struct dml_ion_spec: one system of dml_gen_ions_batch."""
+    _fields_ = [
+        ("seed", ctypes.c_uint64),
+        ("n", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
+        ("box_x", ctypes.c_double),
+        ("box_y", ctypes.c_double),
+        ("zlo", ctypes.c_double),
+        ("zhi", ctypes.c_double),
+        ("dmin", ctypes.c_double),
+    ]
+
+
+def ion_spec(seed, n, box_x, box_y, zlo, zhi, dmin):
+    return IonSpec(seed, n, 0, box_x, box_y, zlo, zhi, dmin)
+
+
 def replica_of(params, **kw):
     """A Replica with params' box, z0, zmax, z1, seed, overridden by kw."""
     r = Replica()

@@ -253,23 +253,28 @@ int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phas
                       int32_t nphase);
 int dml_launches_per_step(dml_ctx* c, int32_t* per_rebuild);
 
-/* Pair force and energy (the fuerza of dml_force) over caller-provided
- * device-accessible arrays, allocating nothing.  This entry point has no
- * counterpart in the reference.  It serves callers that cannot allocate
- * device memory: code running while a stream is captured into a CUDA graph
- * (cudaMalloc is not allowed there), drivers whose device buffers belong to
- * another runtime, loops that must not allocate.  Its scratch lives in one
- * static device array sized for at most 16384 atoms and 32 interacting list
+/* No counterpart in the reference.  The plain FP64 pair force and energy of
+ * dml_force, computed over device arrays the caller owns, allocating
+ * nothing.  For callers that cannot allocate device memory: a host whose
+ * device memory belongs to another allocator or runtime (where a cudaMalloc
+ * of this library would fail or fight that allocator), and a time-stepping
+ * loop that must not call cudaMalloc or cudaFree, which stall the host.
+ * Scratch lives in one static device array, held by every GPU that loads the
+ * library until exit, sized for at most 16384 atoms and 32 interacting list
  * entries per atom: more atoms return DML_E_CAPACITY before any launch, more
- * entries DML_E_EVENT_OVERFLOW.  Inputs: pos [n][3], z [n] (DML_Z_*), the
- * hs%ref members ref [n_ref] (atom indices in hs%ref order) and their lists
- * nn [n_ref], list [n_ref][ld] (atom indices, -1 for limbo).  force [n][3]
- * and epot [n] are outputs for hs%ref members (zeroed, then summed) and are
- * added to for the other atoms, as fuerza does.  Results equal dml_force's
- * bit for bit.  The first call on a device sets up the array's address
- * (cudaGetSymbolAddress) and should come before any stream capture.  Calls
- * share the array: calls that overlap on the GPU race.  The call queues on
- * `stream` (a cudaStream_t, NULL = default) and returns when it is done. */
+ * entries DML_E_EVENT_OVERFLOW.
+ * Inputs: pos [n][3], z [n] (DML_Z_*), the mobile atoms ref [n_ref] (atom
+ * indices, in the order their forces are summed) and their neighbour lists
+ * nn [n_ref], list [n_ref][ld] (atom indices, -1 for an empty entry).
+ * Outputs: force [n][3] and epot [n]; the mobile atoms' values are zeroed,
+ * then summed, the other atoms' values are added to.  On a nonzero return
+ * force and epot are left as passed.  Results equal dml_force's bit for bit.
+ * The first call on a device takes the array's address
+ * (cudaGetSymbolAddress) and keeps it: make it before any stream capture,
+ * and do not call after cudaDeviceReset.  Calls share the array: calls that
+ * overlap on the GPU race.  The call queues on `stream` (a cudaStream_t,
+ * NULL = default), reads its status back and returns when the stream is
+ * idle. */
 int dml_force_noalloc(const dml_params* p, int32_t n_atoms, const double* pos, const int32_t* z,
                       int32_t n_ref, const int32_t* ref, const int32_t* nn, const int32_t* list,
                       int32_t ld, double* force, double* epot, void* stream);
@@ -296,6 +301,13 @@ int dml_get_counters(dml_ctx* c, dml_counters* out);
  * zero before tuning).  Either pointer may be NULL. */
 int dml_get_tuning(dml_ctx* c, int32_t* scan_lanes, float* scan_us);
 int dml_get_counters_replica(dml_ctx* c, int32_t rep, dml_counters* out);
+
+/* Diagnostic (no counterpart in the reference): how many gcmc_run calls of
+ * replica `rep` ran on the parallel path (trials searched at once, decided
+ * in order by one warp) and how many on the sequential one (a replica
+ * without cells, an atom in a halo cell, or a search beyond the parallel
+ * path's bounds).  Either pointer may be NULL. */
+int dml_get_gcmc_paths(dml_ctx* c, int32_t rep, int64_t* parallel, int64_t* sequential);
 
 /* One replica's atoms and neighbour lists (same layout as dml_get_atoms and
  * dml_get_neighbors, which take a one-replica context). */
@@ -341,15 +353,32 @@ typedef struct dml_observables {
  * loops do, so they equal those loops bit for bit. */
 int dml_salida(dml_ctx* c, dml_observables* out);
 
-/* Initial configurations (replaces pos_inic, src/dana.F90:330-396, which
- * cannot load an electrode).  dml_gen_bcc_slab writes the 2*nx*ny*nz atoms
- * of a bcc lattice with constant a (corner then body-centre atom per cell,
- * x fastest) and returns the count, or -status.  dml_gen_ions places n ions
- * uniformly in [0,box_x) x [0,box_y) x [zlo,zhi) by random sequential
- * addition with minimum-image separation >= dmin (the rule of
- * dana.F90:361-389), drawing from the seeded Philox stream; returns 0 or
- * -status. */
+/* Initial configurations (replace pos_inic, src/dana.F90:330-396, which
+ * cannot load an electrode).  dml_gen_bcc_slab writes, on the host, the
+ * 2*nx*ny*nz atoms of a bcc lattice with constant a (corner then body-centre
+ * atom per cell, x fastest) and returns the count, or -status.
+ * dml_gen_ions_batch places the ions of n_sys systems on the GPU, one thread
+ * block per system: system s gets specs[s].n ions in [0,box_x) x [0,box_y) x
+ * [zlo,zhi) by random sequential addition, ion i keeping the first of its
+ * tries whose minimum-image distance (x, y periodic) to every earlier ion is
+ * at least dmin, or failing after 10 000 tries (the rule of
+ * dana.F90:361-389).  The k-th try of ion i is the keyed Philox draw
+ * (seed, k, i).  The result is bit-identical to placing the ions one by
+ * one.  Outputs are host arrays: pos_out [sum n][3] (system s after the
+ * earlier systems' ions), status [n_sys] (0 or DML_E_RSA; may be NULL).
+ * Returns 0, the first nonzero system status, or DML_E_ARG / DML_E_NOMEM /
+ * DML_E_CUDA / DML_E_CAPACITY (more than 2^28 grid cells).  dml_gen_ions is
+ * the one-system form; it returns 0 or -status. */
+typedef struct dml_ion_spec {
+  uint64_t seed;
+  int32_t n;
+  int32_t pad;
+  double box_x, box_y, zlo, zhi, dmin;
+} dml_ion_spec;
+
 int dml_gen_bcc_slab(int32_t nx, int32_t ny, int32_t nz, double a, double* pos_out, int32_t cap);
+int dml_gen_ions_batch(int32_t n_sys, const dml_ion_spec* specs, double* pos_out,
+                       int32_t* status);
 int dml_gen_ions(uint64_t seed, int32_t n, double box_x, double box_y, double zlo, double zhi,
                  double dmin, double* pos_out);
 

@@ -1,6 +1,6 @@
 """Build recipe for the oracle (test infrastructure only).
 
-Compiles dana_oracle.cpp into oracle/_build/liboracle.so with the flags that
+Compiles dana_oracle.cpp and oracle_gen.cpp into oracle/_build/liboracle.so with the flags that
 keep the reference's floating-point evaluation order: no FMA contraction
 (-ffp-contract=off) and no value-changing optimisation (no -ffast-math).
 The same source and flags give identical results on x86_64 and aarch64.
@@ -12,7 +12,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
-SRC = [os.path.join(HERE, "dana_oracle.cpp")]
+SRC = [os.path.join(HERE, "dana_oracle.cpp"), os.path.join(HERE, "oracle_gen.cpp")]
 DEPS = SRC + [os.path.join(HERE, "oracle.h"),
               os.path.join(HERE, "..", "include", "dml.h"),
               os.path.join(HERE, "..", "include", "dml_rng.h")]

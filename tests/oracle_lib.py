@@ -69,8 +69,46 @@ def load():
     lib.orc_rng_sincosf_2pi.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_float),
                                         ctypes.POINTER(ctypes.c_float)]
     lib.orc_rng_normal_quad.argtypes = [vp, vp]
+    lib.orc_gen_bcc_slab.argtypes = [i32, i32, i32, ctypes.c_double, vp, i32]
+    lib.orc_gen_ions.argtypes = [ctypes.c_uint64, i32, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
     _lib = lib
     return lib
+
+
+def bcc_slab(nx, ny, nz, a=3.51):
+    """Frozen bcc Li electrode: 2*nx*ny*nz positions (oracle/oracle_gen.cpp)."""
+    n = 2 * nx * ny * nz
+    out = np.zeros((n, 3))
+    rc = load().orc_gen_bcc_slab(nx, ny, nz, a, out.ctypes.data, n)
+    if rc < 0:
+        raise RuntimeError("orc_gen_bcc_slab: %s" % _abi.STATUS.get(-rc, rc))
+    return out
+
+
+def gen_ions(seed, n, box_x, box_y, zlo, zhi, dmin):
+    """Serial random sequential addition (oracle/oracle_gen.cpp): the checker
+    of the device generator.  Returns (positions, status)."""
+    out = np.zeros((n, 3))
+    rc = load().orc_gen_ions(seed, n, box_x, box_y, zlo, zhi, dmin, out.ctypes.data)
+    return out, -rc if rc < 0 else 0
+
+
+def random_ions(seed, n, box_x, box_y, zlo, zhi, dmin):
+    out, st = gen_ions(seed, n, box_x, box_y, zlo, zhi, dmin)
+    if st:
+        raise RuntimeError("orc_gen_ions: %s" % _abi.STATUS.get(st, st))
+    return out
+
+
+def slab_system(nx, ny, nz_slab, box_z, n_ion, zlo, zhi, seed, a=3.51, dmin=2.5):
+    """Electrode slab followed by ions, as sys%alist-ordered arrays."""
+    slab = bcc_slab(nx, ny, nz_slab, a)
+    ions = random_ions(seed, n_ion, nx * a, ny * a, zlo, zhi, dmin)
+    pos = np.concatenate([slab, ions])
+    z = np.concatenate([np.full(len(slab), _abi.Z_CG, np.int32),
+                        np.full(n_ion, _abi.Z_LI, np.int32)])
+    return {"pos": pos, "z": z}
 
 
 def default_params():

@@ -3,6 +3,12 @@
 The reference measures no public dataset; its configurations are generated.
 These follow the benchmark configurations: a frozen bcc Li slab (a = 3.51 Å)
 under ions placed by random sequential addition.
+
+Built without the CUDA library: parameters are ctypes structures filled
+here, and atoms come from the oracle's serial generators
+(oracle/oracle_gen.cpp), which the device generator equals bit for bit
+(tests/test_gpu_rsa.py).  So the CPU arms of bench.py and the CPU tests load
+nothing of the product.
 """
 import os
 import sys
@@ -12,13 +18,34 @@ PKG = os.path.join(ROOT, "din-mol-li_gb300")
 if PKG not in sys.path:
     sys.path.insert(0, PKG)
 
-import dml  # noqa: E402
+from dml import _abi as dml  # noqa: E402  (structures and constants only)
+from tests import oracle_lib  # noqa: E402
+
+# dml_params_default's list capacity (the reference's mnb = 10000 is sized
+# for its host memory; tests/test_abi_cpu.py checks the two defaults agree)
+DEFAULT_MNB = 1024
+
+
+def default_params():
+    """dml_params_default: the reference's constants, as the oracle states
+    them, with the device's default list capacity."""
+    p = oracle_lib.default_params()
+    p.mnb = DEFAULT_MNB
+    return p
+
+
+def slab_system(*args, **kw):
+    return oracle_lib.slab_system(*args, **kw)
+
+
+def random_ions(*args):
+    return oracle_lib.random_ions(*args)
 
 
 def c1_params(integrator=dml.INTEGRATOR_ERMAK, reservoir=dml.RESERVOIR_PISTON, seed=1234,
               h=1e-3, mnb=1024):
     """Config 1: 35.1 x 35.1 x 60 Å box, piston z0 = 30 Å, skin 10 Å, dt = 1 fs."""
-    p = dml.default_params()
+    p = default_params()
     p.box[:] = [35.1, 35.1, 60.0]
     p.z0, p.zmax = 30.0, 60.0
     p.h = h
@@ -32,12 +59,12 @@ def c1_params(integrator=dml.INTEGRATOR_ERMAK, reservoir=dml.RESERVOIR_PISTON, s
 
 def c1_atoms(seed=7, n_ion=200, dmin=2.5, nz_slab=2):
     """400 frozen electrode atoms (10x10x2 bcc cells) + n_ion Li+ in z in [10, 60)."""
-    return dml.slab_system(10, 10, nz_slab, 60.0, n_ion, 10.0, 60.0, seed, dmin=dmin)
+    return slab_system(10, 10, nz_slab, 60.0, n_ion, 10.0, 60.0, seed, dmin=dmin)
 
 
 def c2_params(seed=1234, mnb=1024):
     """Config 2: 351 x 351 x 320 Å, piston z0 = 160 Å, 1 fs, Ermak."""
-    p = dml.default_params()
+    p = default_params()
     p.box[:] = [351.0, 351.0, 320.0]
     p.z0, p.zmax = 160.0, 320.0
     p.h = 1e-3
@@ -49,12 +76,12 @@ def c2_params(seed=1234, mnb=1024):
 
 def c2_atoms(seed=7, n_ion=200000, dmin=2.5):
     """80 000 electrode atoms (100x100x4 bcc cells) + 200 000 Li+ in z in [15, 300)."""
-    return dml.slab_system(100, 100, 4, 320.0, n_ion, 15.0, 300.0, seed, dmin=dmin)
+    return slab_system(100, 100, 4, 320.0, n_ion, 15.0, 300.0, seed, dmin=dmin)
 
 
 def scaled_params(nx, box_z, z0, seed=1234):
     a = 3.51
-    p = dml.default_params()
+    p = default_params()
     p.box[:] = [nx * a, nx * a, box_z]
     p.z0, p.zmax = z0, box_z
     p.h = 1e-3
@@ -66,7 +93,7 @@ def scaled_params(nx, box_z, z0, seed=1234):
 def gcmc_params(seed=99, integrator=dml.INTEGRATOR_BROWNIAN):
     """The reference's tests/gcmc run: 100^3 Å box, reservoir z in [80, 100],
     act 0.000627, 10 trials per step, dt = 5e-5 ps, skin 2 Å (Brownian)."""
-    p = dml.default_params()
+    p = default_params()
     p.box[:] = [100.0, 100.0, 100.0]
     p.z0, p.zmax = 80.0, 100.0
     p.h = 5e-5
@@ -84,7 +111,7 @@ def gcmc_atoms(seed=5):
     """602 Li+ (1 M in the 100^3 Å box, dana.F90:349-353) at >= 3.2 Å separation."""
     import numpy as np
 
-    ions = dml.random_ions(seed, 602, 100.0, 100.0, 0.0, 100.0, 3.2)
+    ions = random_ions(seed, 602, 100.0, 100.0, 0.0, 100.0, 3.2)
     return {"pos": ions, "z": np.full(len(ions), dml.Z_LI, np.int32)}
 
 
@@ -112,7 +139,7 @@ def c5_params(seed=11, precision=dml.PRECISION_MIXED, nadj=128, cells=C5_CELLS, 
     slab_activity sets the activity that keeps the mean ion count fixed."""
     a = 3.51
     L = cells * a
-    p = dml.default_params()
+    p = default_params()
     p.box[:] = [L, L, 300.0]
     p.z0, p.zmax = 200.0, 300.0
     p.h = 1e-3
@@ -136,8 +163,8 @@ def c5_batch(n_rep, seed=11, precision=dml.PRECISION_MIXED, nadj=128, cells=C5_C
     be moved back forever by overlap_moveback."""
     p = c5_params(seed, precision, nadj, cells, n_ion)
     reps = [dml.replica_of(p, seed=seed * 100003 + r) for r in range(n_rep)]
-    atoms = [dml.slab_system(cells, cells, 2, 300.0, n_ion, 15.0, 300.0,
-                             seed * 7919 + r, dmin=3.2) for r in range(n_rep)]
+    atoms = [slab_system(cells, cells, 2, 300.0, n_ion, 15.0, 300.0, seed * 7919 + r, dmin=3.2)
+             for r in range(n_rep)]
     p.act = slab_activity(p, atoms[0], seed)
     return p, reps, atoms
 
@@ -178,7 +205,7 @@ def c4_batch(n_rep=C4_REPLICAS, seed=13, precision=dml.PRECISION_MIXED):
     import numpy as np
 
     rng = np.random.default_rng(seed)
-    p = dml.default_params()
+    p = default_params()
     p.integrator = dml.INTEGRATOR_BROWNIAN
     p.reservoir = dml.RESERVOIR_PISTON
     p.h = 5e-5
@@ -196,7 +223,7 @@ def c4_batch(n_rep=C4_REPLICAS, seed=13, precision=dml.PRECISION_MIXED):
         lz = 10.0 + height
         rseed = seed * 100003 + r
         reps.append(dml.replica_of(p, box=[L, L, lz], z0=0.5 * lz, zmax=lz, seed=rseed))
-        atoms.append(dml.slab_system(cells, cells, 2, lz, n_ion, 10.0, lz, rseed, dmin=3.2))
+        atoms.append(slab_system(cells, cells, 2, lz, n_ion, 10.0, lz, rseed, dmin=3.2))
     p.box[:] = list(reps[0].box)
     p.z0, p.zmax = reps[0].z0, reps[0].zmax
     return p, reps, atoms

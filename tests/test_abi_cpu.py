@@ -50,17 +50,31 @@ def test_strerror_names_reference_messages():
 
 
 def test_bcc_slab_and_ions():
+    """The product's electrode lattice (host code) equals the oracle's; the
+    oracle's serial ion placement (the checker of the device generator and
+    the source of every test system) keeps the separation."""
+    from tests import oracle_lib
+
     slab = dml.bcc_slab(10, 10, 2)
     assert slab.shape == (400, 3)
     assert slab[:, 2].max() == 1.5 * 3.51
-    ions = dml.random_ions(7, 200, 35.1, 35.1, 10.0, 60.0, 2.5)
+    assert np.array_equal(slab.view(np.uint64), oracle_lib.bcc_slab(10, 10, 2).view(np.uint64))
+    ions = oracle_lib.random_ions(7, 200, 35.1, 35.1, 10.0, 60.0, 2.5)
     d = ions[:, None, :] - ions[None, :, :]
     d[..., :2] -= 35.1 * np.round(d[..., :2] / 35.1)
     r2 = (d ** 2).sum(-1) + np.eye(len(ions)) * 1e9
     assert r2.min() >= 2.5 ** 2
-    assert ions[:, 2].min() >= 10.0 and ions[:, 2].max() < 60.0
-    # a pure function of the seed
-    assert np.array_equal(ions, dml.random_ions(7, 200, 35.1, 35.1, 10.0, 60.0, 2.5))
+    # too many ions for the volume: every try of some ion is rejected
+    _, st = oracle_lib.gen_ions(3, 400, 10.0, 10.0, 0.0, 10.0, 3.2)
+    assert st == dml.E_RSA
+
+
+def test_test_systems_use_the_library_defaults():
+    """tests/systems.py fills parameters without the library; they equal
+    dml_params_default byte for byte."""
+    a = dml.default_params()
+    b = systems.default_params()
+    assert bytes(a) == bytes(b)
 
 
 def test_create_rejects_unsupported_options_without_gpu():
@@ -82,7 +96,8 @@ def test_ctypes_mirrors_match_header_layout(tmp_path):
 
         pytest.skip("no C compiler")
     mirrors = {"dml_params": dml.Params, "dml_replica": dml.Replica, "dml_atoms": dml.Atoms,
-               "dml_counters": dml.Counters, "dml_observables": dml.Observables}
+               "dml_counters": dml.Counters, "dml_observables": dml.Observables,
+               "dml_ion_spec": dml.IonSpec}
     lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "dml.h"', "int main(void) {"]
     for cname, py in mirrors.items():
         lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
@@ -103,13 +118,18 @@ def test_ctypes_mirrors_match_header_layout(tmp_path):
 
 def test_ion_placement_errors():
     """Random sequential addition that cannot place every ion stops with
-    DML_E_RSA (the reference's own stop, src/dana.F90:386-389); malformed
-    boxes are DML_E_ARG."""
+    DML_E_RSA (the reference's own stop, src/dana.F90:386-389), in the
+    oracle's serial generator here and in the device generator on the GPU
+    (tests/test_gpu_rsa.py); malformed boxes are DML_E_ARG before the
+    device is touched."""
     import pytest
 
-    with pytest.raises(dml.DmlError) as e:
-        dml.random_ions(1, 1000, 10.0, 10.0, 0.0, 10.0, 5.0)  # 1000 ions 5 Å apart in 10^3 Å^3
-    assert e.value.code == dml.E_RSA
+    from tests import oracle_lib
+
+    _, st = oracle_lib.gen_ions(1, 1000, 10.0, 10.0, 0.0, 10.0, 5.0)  # 1000 ions 5 Å apart
+    assert st == dml.E_RSA
+    _, st = oracle_lib.gen_ions(1, 10, -1.0, 10.0, 0.0, 10.0, 1.0)
+    assert st == dml.E_ARG
     with pytest.raises(dml.DmlError) as e:
         dml.random_ions(1, 10, -1.0, 10.0, 0.0, 10.0, 1.0)
     assert e.value.code == dml.E_ARG

@@ -72,3 +72,21 @@ def test_reference_arm_under_torchrun_prints_from_rank0_only():
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["warmup"] == 3
     assert d["value"] > 0 and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
+
+
+def test_reference_arm_maps_only_the_oracle_library():
+    """The reference arm builds its workload (parameters, electrode, ion
+    placement) and steps it without the CUDA library: the process maps
+    oracle/_build/liboracle.so and nothing of din-mol-li_gb300/."""
+    code = ("import argparse, sys; sys.path.insert(0, '.'); import bench; "
+            "a = argparse.Namespace(workload='c5', replicas=2, steps=2, warmup=3); "
+            "bench.run_reference(a, 1, 0); "
+            "m = open('/proc/self/maps').read(); "
+            "print('MAPS', int('liboracle.so' in m), int('libdml.so' in m))")
+    p = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
+                       timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    line = [l for l in p.stdout.splitlines() if l.startswith("{")][0]
+    d = json.loads(line)
+    assert d["config"]["replicas"] == 2 and d["config"]["n_ion"] == 40000
+    assert p.stdout.splitlines()[-1] == "MAPS 1 0"

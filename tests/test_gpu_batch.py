@@ -90,10 +90,10 @@ def uneven_replicas(p):
         dml.replica_of(p, box=[35.1, 35.1, 40.0], z0=20.0, zmax=40.0, seed=17),
     ]
     atoms = [
-        dml.slab_system(10, 10, 2, 60.0, 200, 10.0, 60.0, 7),
-        dml.slab_system(10, 10, 2, 60.0, 90, 10.0, 60.0, 8),
-        dml.slab_system(12, 12, 2, 60.0, 320, 10.0, 60.0, 9),
-        dml.slab_system(10, 10, 2, 40.0, 120, 10.0, 40.0, 11),
+        systems.slab_system(10, 10, 2, 60.0, 200, 10.0, 60.0, 7),
+        systems.slab_system(10, 10, 2, 60.0, 90, 10.0, 60.0, 8),
+        systems.slab_system(12, 12, 2, 60.0, 320, 10.0, 60.0, 9),
+        systems.slab_system(10, 10, 2, 40.0, 120, 10.0, 40.0, 11),
     ]
     return reps, atoms
 
@@ -112,7 +112,7 @@ def test_batch_capture_events():
     p = systems.c1_params(integrator=dml.INTEGRATOR_BROWNIAN, reservoir=dml.RESERVOIR_NONE)
     p.h = 1e-2
     reps = [dml.replica_of(p, seed=s) for s in (3, 4, 5)]
-    atoms = [dml.slab_system(10, 10, 2, 60.0, n, 5.0, 20.0, s, dmin=3.2)
+    atoms = [systems.slab_system(10, 10, 2, 60.0, n, 5.0, 20.0, s, dmin=3.2)
              for n, s in ((150, 3), (100, 4), (60, 5))]
     g, orcs = run_batch_vs_oracles(p, reps, atoms, [50, 50])
     for r in range(3):

@@ -91,7 +91,7 @@ def test_config5_shape_gcmc_matches_oracle():
     p.integrator = dml.INTEGRATOR_BROWNIAN
     p.h = 1e-4
     p.mnb = 512
-    atoms = dml.slab_system(15, 15, 2, 100.0, 1500, 15.0, 100.0, 21, dmin=3.2)
+    atoms = systems.slab_system(15, 15, 2, 100.0, 1500, 15.0, 100.0, 21, dmin=3.2)
     p.act = systems.slab_activity(p, atoms, 3)
     g, o = make_pair(p, atoms)
     g.setup()
@@ -125,7 +125,7 @@ def test_dense_gcmc_many_trials_matches_oracle(capacity):
     p.mnb = 256
     if capacity:
         p.capacity = capacity
-    atoms = dml.slab_system(12, 12, 2, 80.0, 900, 15.0, 80.0, 31, dmin=3.2)
+    atoms = systems.slab_system(12, 12, 2, 80.0, 900, 15.0, 80.0, 31, dmin=3.2)
     p.act = 3.0 * systems.slab_activity(p, atoms, 5)
     g, o = make_pair(p, atoms)
     g.setup()
@@ -177,7 +177,7 @@ def config5_shape(n_fill=1500):
     p.integrator = dml.INTEGRATOR_BROWNIAN
     p.h = 1e-4
     p.mnb = 512
-    full = dml.slab_system(15, 15, 2, 100.0, n_fill, 15.0, 100.0, 21, dmin=3.2)
+    full = systems.slab_system(15, 15, 2, 100.0, n_fill, 15.0, 100.0, 21, dmin=3.2)
     p.act = systems.slab_activity(p, full, 3)
     return p
 
@@ -192,7 +192,7 @@ def test_reservoir_filling_from_few_ions_batch():
 
     p = config5_shape()
     reps = [dml.replica_of(p, seed=s) for s in (41, 42, 43)]
-    atoms = [dml.slab_system(15, 15, 2, 100.0, n, 15.0, 100.0, s, dmin=3.2)
+    atoms = [systems.slab_system(15, 15, 2, 100.0, n, 15.0, 100.0, s, dmin=3.2)
              for n, s in ((1, 41), (4, 42), (30, 43))]
     g, orcs = run_batch_vs_oracles(p, reps, atoms, [1, 9, 30])
     for r, o in enumerate(orcs):
@@ -215,12 +215,12 @@ def test_error_parity_empty_gcmc_group(geometry):
     (all-pairs lists)."""
     if geometry == "cells":
         p = config5_shape()
-        full = dml.slab_system(15, 15, 2, 100.0, 1, 15.0, 100.0, 5, dmin=3.2)
+        full = systems.slab_system(15, 15, 2, 100.0, 1, 15.0, 100.0, 5, dmin=3.2)
     else:
         p = systems.c5_small_params(nadj=32)
         p.box[2] = 40.0
         p.z0, p.zmax = 20.0, 40.0
-        full = dml.slab_system(10, 10, 2, 40.0, 1, 10.0, 40.0, 5, dmin=3.2)
+        full = systems.slab_system(10, 10, 2, 40.0, 1, 10.0, 40.0, 5, dmin=3.2)
     keep = full["z"] == dml.Z_CG
     atoms = {k: v[keep] for k, v in full.items()}
     g, o = make_pair(p, atoms)

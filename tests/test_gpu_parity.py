@@ -139,7 +139,7 @@ def test_verlet_path_small_box():
     p.box[2] = 40.0
     p.zmax = 40.0
     p.z0 = 20.0
-    atoms = dml.slab_system(10, 10, 2, 40.0, 120, 10.0, 40.0, 11)
+    atoms = systems.slab_system(10, 10, 2, 40.0, 120, 10.0, 40.0, 11)
     g, o = make_pair(p, atoms)
     g.setup()
     o.setup()
@@ -154,7 +154,7 @@ def test_capture_events_happen_and_match():
     """Ions started next to the electrode are captured; counts match exactly."""
     p = systems.c1_params(integrator=dml.INTEGRATOR_BROWNIAN, reservoir=dml.RESERVOIR_NONE)
     p.h = 1e-2  # sqrt(2*250*0.01) = 2.2 Å per step: reaches the slab quickly
-    atoms = dml.slab_system(10, 10, 2, 60.0, 150, 5.0, 20.0, 3, dmin=3.2)
+    atoms = systems.slab_system(10, 10, 2, 60.0, 150, 5.0, 20.0, 3, dmin=3.2)
     g, o = make_pair(p, atoms)
     g.setup()
     o.setup()
@@ -171,7 +171,7 @@ def test_error_parity_empty_reservoir_piston():
     at the same step (the reference would stop in cgroup_sort, Cells.F90:293)."""
     p = systems.c1_params(integrator=dml.INTEGRATOR_BROWNIAN)
     p.h = 1e-2
-    atoms = dml.slab_system(10, 10, 2, 60.0, 150, 5.0, 20.0, 3, dmin=3.2)
+    atoms = systems.slab_system(10, 10, 2, 60.0, 150, 5.0, 20.0, 3, dmin=3.2)
     g, o = make_pair(p, atoms)
     g.setup()
     o.setup()

@@ -36,7 +36,7 @@ def capture_params():
     few steps, so try and depo are non-zero."""
     p = systems.c1_params(integrator=dml.INTEGRATOR_BROWNIAN, reservoir=dml.RESERVOIR_NONE)
     p.h = 1e-2
-    return p, dml.slab_system(10, 10, 2, 60.0, 150, 5.0, 20.0, 3, dmin=3.2)
+    return p, systems.slab_system(10, 10, 2, 60.0, 150, 5.0, 20.0, 3, dmin=3.2)
 
 
 @pytest.mark.parametrize("case", ["ermak_piston", "brownian_captures"])
