@@ -269,7 +269,7 @@ int set_step(dml_ctx* c, int64_t step) {
 // test_update inside a graph capture: the displacement-test kernel sets the
 // condition of an IF node whose body is the rebuild (update(), Neighbor.F90:
 // 608-633), so steps without a rebuild launch no rebuild kernel at all.
-int capture_test_update(dml_ctx* c, int* n_base, int* n_body, bool near_in_body) {
+int capture_test_update(dml_ctx* c, int* n_base, int* n_body, bool near_in_body, bool second) {
   cudaStream_t s = c->stream;
   cudaStreamCaptureStatus st;
   cudaGraph_t g;
@@ -278,7 +278,7 @@ int capture_test_update(dml_ctx* c, int* n_base, int* n_body, bool near_in_body)
   CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
   cudaGraphConditionalHandle h;
   CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
-  *n_base += k_pbc_dispmax_cond(c->D, c->K, c->D.cap, h, s);
+  *n_base += k_pbc_dispmax_cond(c->D, c->K, c->D.cap, h, s, second);
   CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
   cudaGraphNodeParams cp = {};
   cp.type = cudaGraphNodeTypeConditional;
@@ -323,11 +323,11 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
   };
   const bool ermak_ = c->P.integrator == DML_INTEGRATOR_ERMAK;
   auto test_update = [&](bool first) -> int {
-    if (capture) return capture_test_update(c, &n, &nb, first && ermak_);
+    if (capture) return capture_test_update(c, &n, &nb, first && ermak_, !first);
     if (gaps) {
       // the graph's kernels: the rebuild (and the near search after the
       // first one) only when some replica rebuilds, decided on the host
-      n += k_pbc_dispmax(d, k, cap, s);
+      n += k_pbc_dispmax(d, k, cap, s, !first);
       ProfileGap gp;
       gp.phase = first ? DML_PHASE_TEST_UPDATE1 : DML_PHASE_TEST_UPDATE2;
       CK(cudaEventCreate(&gp.a));
@@ -344,7 +344,7 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
       }
       return 0;
     }
-    n += k_test_update(d, k, cap, cap, cap, s);
+    n += k_test_update(d, k, cap, cap, cap, s, !first);
     return 0;
   };
   mark(DML_PHASE_INTEGRATE);
@@ -711,6 +711,8 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   // only the form in use gets its force accumulators
   const bool mixed = c->P.precision == DML_PRECISION_MIXED;
   AL(d.facc, mixed ? 4 * (size_t)cap : 4);
+  AL(d.ftouch, mixed ? (size_t)cap / 32 + 1 : 1);
+  AL(d.ftlist, mixed ? (size_t)cap : 1);
   AL(d.cand, (size_t)c->K.cand_cap);
   AL(d.ev_count, cap);
   AL(d.ev, mixed ? 1 : (size_t)cap * c->P.event_cap);
@@ -728,6 +730,8 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.pr_cnt, (size_t)nrep * kCntStride);
   d.nblk_part = cap / kBlock + 1;
   AL(d.part, 2 * (size_t)d.nblk_part);
+  AL(d.part1, 2 * (size_t)d.nblk_part);
+  AL(d.dirty, (size_t)d.nblk_part);
   AL(d.sc, nrep);
   AL(d.g, 1);
   AL(d.rc, nrep);
@@ -1225,6 +1229,26 @@ int dml_check_conversions(const double* x, int64_t n, float* f32, double* back) 
   cudaFree(dx);
   cudaFree(db);
   cudaFree(df);
+  return e == cudaSuccess ? 0 : DML_E_CUDA;
+}
+
+int dml_check_normals(const uint32_t* words, int64_t n_pairs, float* out) {
+  if (n_pairs < 0 || (n_pairs > 0 && (!words || !out))) return DML_E_ARG;
+  if (n_pairs == 0) return 0;
+  unsigned* dw = nullptr;
+  float* dout = nullptr;
+  cudaError_t e = cudaMalloc(&dw, sizeof(unsigned) * 2 * n_pairs);
+  if (e == cudaSuccess) e = cudaMalloc(&dout, sizeof(float) * 2 * n_pairs);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(dw, words, sizeof(unsigned) * 2 * n_pairs, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_check_normals(dw, dout, n_pairs, 0);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpy(out, dout, sizeof(float) * 2 * n_pairs, cudaMemcpyDeviceToHost);
+  cudaFree(dw);
+  cudaFree(dout);
   return e == cudaSuccess ? 0 : DML_E_CUDA;
 }
 

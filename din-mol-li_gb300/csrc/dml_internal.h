@@ -119,6 +119,7 @@ struct Global {
   long long list_builds;    // rebuild kernels run (some replica rebuilt)
   int near_stale;           // near lists must be searched in the overlap phase
   int n_big;                // entries of big_cells
+  int n_ftouch;             // entries of ftlist (mixed-form sums)
 };
 
 struct EvRec {            // one interacting list entry seen from one atom
@@ -237,6 +238,10 @@ struct Dev {
   int4* cand;
   // mixed form: per-atom int64 fixed-point force (x, y, z) and energy
   long long* facc;
+  // mixed form: the slots whose accumulators received a pair this call,
+  // one bit per slot (ftouch) and listed once each (ftlist, Global::n_ftouch)
+  unsigned* ftouch;
+  int* ftlist;
   // force events
   int* ev_count;
   EvRec* ev;
@@ -257,6 +262,11 @@ struct Dev {
   // reductions
   unsigned long long* part;  // per-block partials (top-2, as double bits)
   int nblk_part;
+  // The step's second test_update: the FP32 top-2 of every block from the
+  // first one (part1, two float bit patterns per block), and the blocks
+  // where overlap_moveback moved an atom since (dirty)
+  unsigned* part1;
+  int* dirty;
   // replicas
   Scalars* sc;        // [nrep] per-replica state
   Global* g;          // context-wide state
@@ -309,6 +319,7 @@ struct PackOut {
 int k_pack_atoms(const Dev& d, const KParams& p, const PackOut& o, cudaStream_t s);
 int k_salida(const Dev& d, const KParams& p, double kb, dml_observables* out, cudaStream_t s);
 int k_check_conversions(const double* x, float* f32, double* back, long long n, cudaStream_t s);
+int k_check_normals(const unsigned* w, float* out, long long n_pairs, cudaStream_t s);
 int k_check_pick(const unsigned long long* k, const int* n, int* m, long long count, cudaStream_t s);
 int k_step_begin(const Dev& d, int near_stale, cudaStream_t s);
 int k_rank_prefix(const Dev& d, cudaStream_t s);
@@ -319,10 +330,12 @@ int k_force_scan(const Dev& d, const KParams& p, int n_rank, bool near, cudaStre
 int k_reset_candidates(const Dev& d, cudaStream_t s);
 int k_force_sum(const Dev& d, const KParams& p, int n_slots, bool fuse_ermak_b, cudaStream_t s);
 int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
+// second: the step's test_update after overlap_moveback, which recomputes
+// only the blocks where an atom moved since the first one.
 int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
-                  cudaStream_t s);
+                  cudaStream_t s, bool second = false);
 int k_pbc_dispmax_cond(const Dev& d, const KParams& p, int n_slots,
-                       cudaGraphConditionalHandle h, cudaStream_t s);
+                       cudaGraphConditionalHandle h, cudaStream_t s, bool second = false);
 int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, cudaStream_t s);
 // overlap_moveback: standalone (its own delta and near search) or as the
 // second half of a fused step whose first half ran k_overlap_prepare.
@@ -339,7 +352,8 @@ int k_flush(void* buf, size_t bytes, cudaStream_t s);
 int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s);
 int k_gcmc_cells(const Dev& d, const KParams& p, int cap, cudaStream_t s);
 int k_gcmc_trials(const Dev& d, const KParams& p, cudaStream_t s);
-int k_pbc_dispmax(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
+int k_pbc_dispmax(const Dev& d, const KParams& p, int n_slots, cudaStream_t s,
+                  bool second = false);
 
 }  // namespace dml
 

@@ -448,9 +448,13 @@ __device__ __forceinline__ void ermak_a_mixed_atom(const Dev& d, const KParams& 
   int typ = in.typ;
   const long long id = in.id;
   const float rf = p.rfacf[typ - 1], vf = p.vfacf[typ - 1];
-  float nq[8];
-  dml_normal_quadf(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 0), &nq[0]);
-  dml_normal_quadf(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 1), &nq[4]);
+  // six normals: both pairs of the first draw, the first pair of the second
+  float nq[6];
+  const dml_u4 w0 = dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 0);
+  const dml_u4 w1 = dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 1);
+  dml_normal_pair32f(w0.w[0], w0.w[1], &nq[0], &nq[1]);
+  dml_normal_pair32f(w0.w[2], w0.w[3], &nq[2], &nq[3]);
+  dml_normal_pair32f(w1.w[0], w1.w[1], &nq[4], &nq[5]);
   const float vv[3] = {V.x, V.y, V.z}, aa[3] = {A.x, A.y, A.z};
   double pp[3] = {P.x, P.y, P.z};
   float rv[3];
@@ -504,9 +508,10 @@ __device__ __forceinline__ void ermak_a_at(const Dev& d, const KParams& p, int r
   double vv[3] = {V.x, V.y, V.z};
   double aa[3] = {A.x, A.y, A.z};
   double rv[3];
-  double nq[8];
+  double nq[6];
   dml_normal_quad(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 0), &nq[0]);
-  dml_normal_quad(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 1), &nq[4]);
+  const dml_u4 w1 = dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 1);
+  dml_normal_pair32(w1.w[0], w1.w[1], &nq[4], &nq[5]);
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
     double r1 = nq[2 * j], r2 = nq[2 * j + 1];
@@ -1047,6 +1052,13 @@ __device__ __forceinline__ long long to_fixed(const KParams& p, float v, double 
   return __double2ll_rn(x);
 }
 
+// A slot's first pair of the call sets its bit and lists it (once).
+__device__ __forceinline__ void touch_slot(const Dev& d, int h) {
+  const unsigned bit = 1u << (h & 31);
+  if (atomicOr(&d.ftouch[h >> 5], bit) & bit) return;
+  d.ftlist[atomicAdd(&d.g->n_ftouch, 1)] = h;
+}
+
 __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
   int nc = d.g->n_cand;
   if (nc > p.cand_cap) {
@@ -1086,6 +1098,8 @@ __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
       raise_error(d.g, DML_E_FIXEDPOINT_OVERFLOW, h);
       continue;
     }
+    touch_slot(d, h);
+    touch_slot(d, j);
     unsigned long long* ai = (unsigned long long*)(d.facc + 4 * (size_t)h);
     unsigned long long* aj = (unsigned long long*)(d.facc + 4 * (size_t)j);
     atomicAdd(ai + 0, (unsigned long long)fx);
@@ -1100,53 +1114,72 @@ __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
 }
 
 // Fixed point -> double, accumulators cleared, ermak_b fused.
+//
+// The sums are taken without a pass over every slot: forces of the chosen form
+// are sparse (a pair inside r0 is rare between hard-core ions), so only the
+// slots listed by force_exact_mixed_kernel read and clear their fixed-point
+// accumulators (force_touched_kernel), and the hs%ref members (the only
+// atoms whose force fuerza zeroes and ermak_b reads) are walked by rank
+// (force_ref_kernel): a member with no pair gets force 0, epot 0 and
+// ermak_b with a zero force, touching neither the accumulators nor the
+// electrode slots.
 template <bool FUSE_B>
-__device__ __forceinline__ void force_fix_at(Dev d, KParams p, int n_slots, int rep, int pos) {
-  n_slots = d.rc[rep].base + d.sc[rep].n_slots;
-  const int s = pos;
-  if (s == 0) d.g->n_cand = 0;
-  if (s >= n_slots) return;
-  if (d.state[s] != ST_LIVE) return;
-  long long* a = d.facc + 4 * (size_t)s;
-  long long ax = a[0], ay = a[1], az = a[2], ae = a[3];
-  bool inref = d.rank[s] >= 0;
-  bool any = (ax | ay | az | ae) != 0;
-  if (!inref && !any) return;
-  double4 F;
-  double ep;
+__global__ void force_touched_kernel(Dev d, KParams p) {
+  const int nt = d.g->n_ftouch;
   const double inv = p.fix_inv;
-  if (inref && !any) {
-    // no pair inside r0: the sums are zero (no FP64 conversion needed)
-    d.force[s] = make_double4(0.0, 0.0, 0.0, 0.0);
-    d.epot[s] = 0.0;
-    if (FUSE_B) ermak_b_atom_mixed(d, p, s, d.typ[s], 0.0f, 0.0f, 0.0f);
-    return;
-  } else if (inref) {
-    F = make_double4((double)ax * inv, (double)ay * inv, (double)az * inv, 0.0);
-    ep = (double)ae * inv;
-  } else {
-    F = d.force[s];
-    F.x += (double)ax * inv;
-    F.y += (double)ay * inv;
-    F.z += (double)az * inv;
-    ep = d.epot[s] + (double)ae * inv;
-  }
-  if (any) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nt; q += gridDim.x * blockDim.x) {
+    const int s = d.ftlist[q];
+    long long* a = d.facc + 4 * (size_t)s;
+    const long long ax = a[0], ay = a[1], az = a[2], ae = a[3];
     a[0] = 0;
     a[1] = 0;
     a[2] = 0;
     a[3] = 0;
+    double4 F;
+    double ep;
+    const bool inref = d.rank[s] >= 0;
+    if (inref) {
+      F = make_double4((double)ax * inv, (double)ay * inv, (double)az * inv, 0.0);
+      ep = (double)ae * inv;
+    } else {  // fuerza adds to the atoms outside hs%ref
+      F = d.force[s];
+      F.x += (double)ax * inv;
+      F.y += (double)ay * inv;
+      F.z += (double)az * inv;
+      ep = d.epot[s] + (double)ae * inv;
+      atomicAnd(&d.ftouch[s >> 5], ~(1u << (s & 31)));
+    }
+    d.force[s] = F;
+    d.epot[s] = ep;
+    if (FUSE_B && inref) ermak_b_atom_mixed(d, p, s, d.typ[s], (float)F.x, (float)F.y, (float)F.z);
   }
-  d.force[s] = F;
-  d.epot[s] = ep;
-  if (FUSE_B && inref) ermak_b_atom_mixed(d, p, s, d.typ[s], (float)F.x, (float)F.y, (float)F.z);
 }
 
 template <bool FUSE_B>
-__global__ void force_fix_kernel(Dev d, KParams p, int n_slots) {
+__device__ __forceinline__ void force_ref_at(const Dev& d, const KParams& p, int rep, int r) {
+  if (r - d.rc[rep].base >= d.sc[rep].n_rank) return;
+  const int h = d.ref[r];
+  if (h < 0) return;
+  const unsigned bit = 1u << (h & 31);
+  if (d.ftouch[h >> 5] & bit) {  // summed by force_touched_kernel
+    atomicAnd(&d.ftouch[h >> 5], ~bit);
+    return;
+  }
+  d.force[h] = make_double4(0.0, 0.0, 0.0, 0.0);
+  d.epot[h] = 0.0;
+  if (FUSE_B) ermak_b_atom_mixed(d, p, h, d.typ[h], 0.0f, 0.0f, 0.0f);
+}
+
+template <bool FUSE_B>
+__global__ void force_ref_kernel(Dev d, KParams p) {
   const int rep = block_rep(d);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    d.g->n_cand = 0;
+    d.g->n_ftouch = 0;
+  }
+  if ((int)blockIdx.x * kSpan >= d.rc[rep].base + d.sc[rep].n_rank) return;
 #pragma unroll
-  for (int u = 0; u < kSlotU; ++u) force_fix_at<FUSE_B>(d, p, n_slots, rep, span_pos(u));
+  for (int u = 0; u < kSlotU; ++u) force_ref_at<FUSE_B>(d, p, rep, span_pos(u));
 }
 
 // ----------------------------------------------------------- test_update
@@ -1199,7 +1232,14 @@ __device__ __forceinline__ void decide_rebuild(const Dev& d, Scalars* sc, int re
   }
 }
 
-__global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p, int n_slots) {
+// The step's second test_update (second = 1) follows overlap_moveback,
+// which moves atoms back to their step-start positions and nothing else:
+// a block none of whose atoms moved (dirty = 0) has the positions, wraps and
+// displacements of the first test_update, so it reuses that call's FP32
+// top-2 (or, in a replica whose list the first call rebuilt, pos_old = pos
+// and every displacement is 0).  Dirty blocks are recomputed in full.
+__global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p, int n_slots,
+                                                                 int second) {
   // grids are sized by capacity; the block's replica gives the live count
   const int rep = block_rep(d);
   const RepConst& R = d.rc[rep];
@@ -1214,7 +1254,15 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
   // the replica's slots in use only take part in the reduction.
   bool live[kSlotU];
   float4 Pfu[kSlotU], Ofu[kSlotU];
-  const bool used = (int)blockIdx.x * kSpan < n_slots;
+  bool used = (int)blockIdx.x * kSpan < n_slots;
+  if (second && used && d.dirty[blockIdx.x] == 0) {
+    used = false;  // nothing moved here since the first call
+    if (threadIdx.x == 0 && !sc->rebuild) {
+      a1 = __uint_as_float(d.part1[2 * blockIdx.x]);
+      a2 = __uint_as_float(d.part1[2 * blockIdx.x + 1]);
+    }
+  }
+  if (!second && threadIdx.x == 0) d.dirty[blockIdx.x] = 0;
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) {
     const int s = span_pos(u);
@@ -1294,6 +1342,10 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
     for (int w = 0; w < nwarp; ++w) top2f(b1, b2, w1[w], w2[w]);
     d.part[2 * blockIdx.x] = __float_as_uint(b1);
     d.part[2 * blockIdx.x + 1] = __float_as_uint(b2);
+    if (!second) {
+      d.part1[2 * blockIdx.x] = __float_as_uint(b1);
+      d.part1[2 * blockIdx.x + 1] = __float_as_uint(b2);
+    }
     __threadfence();
     unsigned t = atomicAdd(&sc->ticket, 1u);
     last = (t == (unsigned)R.nblk - 1u);
@@ -2355,6 +2407,7 @@ __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, in
         d.pos[x] = O;
         d.posf[x] = to_f4(O, d.typ[x]);
         d.skip[x] = 0;
+        d.dirty[x / kSpan] = 1;
       }
       break;
     }
@@ -2370,6 +2423,7 @@ __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, in
     }
     d.pos[j] = Oj;
     d.posf[j] = to_f4(Oj, d.typ[j]);
+    d.dirty[j / kSpan] = 1;
     d.acel[j] = make_double4(0.0, 0.0, 0.0, 0.0);
     d.vel[j] = make_double4(0.0, 0.0, 0.0, 0.0);
     d.skip[j] = 0;
@@ -5032,11 +5086,16 @@ int k_reset_candidates(const Dev& d, cudaStream_t s) {
 
 int k_force_sum(const Dev& d, const KParams& p, int n_slots, bool fuse_b, cudaStream_t s) {
   if (p.mixed) {
-    if (fuse_b)
-      force_fix_kernel<true><<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
-    else
-      force_fix_kernel<false><<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
-    return 1;
+    // listed slots first: force_ref_kernel skips the members they summed
+    // (and resets the list)
+    if (fuse_b) {
+      force_touched_kernel<true><<<152 * 2, kBlock, 0, s>>>(d, p);
+      force_ref_kernel<true><<<nspan(n_slots), kBlock, 0, s>>>(d, p);
+    } else {
+      force_touched_kernel<false><<<152 * 2, kBlock, 0, s>>>(d, p);
+      force_ref_kernel<false><<<nspan(n_slots), kBlock, 0, s>>>(d, p);
+    }
+    return 2;
   }
   if (fuse_b)
     force_sum_kernel<true><<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
@@ -5050,20 +5109,20 @@ int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   return 1;
 }
 
-int k_pbc_dispmax(const Dev& d, const KParams& p, int n_slots, cudaStream_t s) {
-  pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+int k_pbc_dispmax(const Dev& d, const KParams& p, int n_slots, cudaStream_t s, bool second) {
+  pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots, second ? 1 : 0);
   dispmax_exact_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, 0, 0);
   return 2;
 }
 
 int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank,
-                  cudaStream_t s) {
-  return k_pbc_dispmax(d, p, n_slots, s) + k_rebuild(d, p, n_slots, n_b, n_rank, s);
+                  cudaStream_t s, bool second) {
+  return k_pbc_dispmax(d, p, n_slots, s, second) + k_rebuild(d, p, n_slots, n_b, n_rank, s);
 }
 
 int k_pbc_dispmax_cond(const Dev& d, const KParams& p, int n_slots,
-                       cudaGraphConditionalHandle h, cudaStream_t s) {
-  pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots);
+                       cudaGraphConditionalHandle h, cudaStream_t s, bool second) {
+  pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots, second ? 1 : 0);
   dispmax_exact_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, 1, h);
   return 2;
 }
@@ -5251,6 +5310,17 @@ __global__ void check_pick_kernel(const unsigned long long* k, const int* n, int
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
        i += (long long)gridDim.x * blockDim.x)
     m[i] = gcmc_pick_index(k[i], n[i]);
+}
+
+__global__ void check_normals_kernel(const unsigned* w, float* out, long long n_pairs) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_pairs;
+       i += (long long)gridDim.x * blockDim.x)
+    dml_normal_pair32f(w[2 * i], w[2 * i + 1], &out[2 * i], &out[2 * i + 1]);
+}
+
+int k_check_normals(const unsigned* w, float* out, long long n_pairs, cudaStream_t s) {
+  check_normals_kernel<<<152 * 4, kBlock, 0, s>>>(w, out, n_pairs);
+  return 1;
 }
 
 int k_check_pick(const unsigned long long* k, const int* n, int* m, long long count, cudaStream_t s) {

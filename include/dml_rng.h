@@ -176,6 +176,58 @@ DML_HD float dml_bits_f32(uint32_t u) {
 #endif
 }
 
+/* Integer-to-float conversions written with integer operations on the
+ * device, where GB300 issues conversion instructions on its narrow FP64
+ * pipe (about 1/64 of the FP32 rate); the results are the conversions'
+ * own (round to nearest, ties to even), so host and device still agree.
+ * dml_small_i2f: exact for |e| < 2^22 (1.5 * 2^23 + e is a float whose low
+ * mantissa bits are e; subtracting 1.5 * 2^23 is exact).
+ * dml_u32_to_f32_rn: RN32 of a 32-bit unsigned integer. */
+DML_HD float dml_small_i2f(int e) {
+#if defined(__CUDA_ARCH__)
+  return __fsub_rn(__int_as_float(0x4B400000 + e), 12582912.0f);
+#else
+  return (float)e;
+#endif
+}
+
+DML_HD float dml_u32_to_f32_rn(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  if (x == 0u) return 0.0f;
+  int n = 31 - __clz((int)x); /* position of the leading one */
+  uint32_t m;
+  if (n <= 23) {
+    m = x << (23 - n); /* exact */
+  } else {
+    const int sh = n - 23; /* 1 .. 8 dropped bits */
+    m = x >> sh;
+    const uint32_t rem = x & ((1u << sh) - 1u), half = 1u << (sh - 1);
+    if (rem > half || (rem == half && (m & 1u))) m += 1u;
+    if (m == (1u << 24)) { /* carry into the next binade */
+      m >>= 1;
+      n += 1;
+    }
+  }
+  return __uint_as_float(((uint32_t)(127 + n) << 23) | (m & 0x7FFFFFu));
+#else
+  return (float)x;
+#endif
+}
+
+/* binary32 -> binary64, exact; on the device by rebiasing a normal float's
+ * exponent (1023 - 127 = 896) with its 23 mantissa bits at the top of the
+ * double's 52 (zero, subnormal, inf and NaN take the conversion). */
+DML_HD double dml_f32_to_f64(float f) {
+#if defined(__CUDA_ARCH__)
+  const uint32_t b = __float_as_uint(f), e = (b >> 23) & 0xFFu;
+  if (e == 0u || e == 0xFFu) return (double)f;
+  const uint32_t hi = (b & 0x80000000u) | (((b & 0x7FFFFFFFu) >> 3) + (896u << 20));
+  return __hiloint2double((int)hi, (int)(b << 29));
+#else
+  return (double)f;
+#endif
+}
+
 /* Natural logarithm for normal positive x (the Box-Muller argument lies in
  * [2^-32, 1]).  Exponent split + atanh series, see the header comment. */
 DML_HD float dml_logf(float x) {
@@ -198,7 +250,7 @@ DML_HD float dml_logf(float x) {
   float r = DMLF_MUL(s2, q);
   float two_s = DMLF_MUL(2.0f, s);
   float lm = DMLF_ADD(two_s, DMLF_MUL(two_s, r));
-  return DMLF_ADD(DMLF_MUL((float)e, 0x1.62e430p-1f), lm); /* + e ln2 */
+  return DMLF_ADD(DMLF_MUL(dml_small_i2f(e), 0x1.62e430p-1f), lm); /* + e ln2 */
 }
 
 /* sin and cos of theta in [0, pi/4] by Taylor series (to theta^9 / theta^10). */
@@ -217,12 +269,13 @@ DML_HD void dml_sincosf_small(float th, float* s, float* c) {
   *c = DMLF_ADD(1.0f, DMLF_MUL(pc, t2));
 }
 
-/* sin(2 pi u) and cos(2 pi u) for u in [0,1) that is a multiple of 2^-24. */
-DML_HD void dml_sincosf_2pi(float u, float* sn, float* cs) {
-  float t4 = DMLF_MUL(u, 4.0f); /* exact */
-  float q = floorf(t4);
-  float f = DMLF_SUB(t4, q);    /* exact, [0,1) */
-  int qi = (int)q;
+/* sin(2 pi u) and cos(2 pi u) for u = x * 2^-24, x a 24-bit integer: the
+ * quadrant is floor(4u) = x >> 22 and the fraction 4u - floor(4u) =
+ * (x mod 2^22) * 2^-22, both exact (no rounding or conversion instruction
+ * on the device). */
+DML_HD void dml_sincosf_2pi_bits(uint32_t x, float* sn, float* cs) {
+  const int qi = (int)(x >> 22);
+  float f = DMLF_MUL(dml_u32_to_f32_rn(x & 0x3FFFFFu), 0x1.0p-22f); /* exact, [0,1) */
   int swap = f > 0.5f;
   float g = swap ? DMLF_SUB(1.0f, f) : f; /* exact */
   float th = DMLF_MUL(g, 0x1.921fb6p+0f); /* g * pi/2, in [0, pi/4] */
@@ -238,21 +291,25 @@ DML_HD void dml_sincosf_2pi(float u, float* sn, float* cs) {
   }
 }
 
+/* The same for a float u in [0,1) that is a multiple of 2^-24. */
+DML_HD void dml_sincosf_2pi(float u, float* sn, float* cs) {
+  dml_sincosf_2pi_bits((uint32_t)DMLF_MUL(u, 0x1.0p+24f), sn, cs);
+}
+
 /* Two standard normals from two 32-bit words (Box-Muller): a uniform in
- * (0,1] from the first word, an angle from the top 24 bits of the second.
- * RN32(a + 1) is taken from a 32-bit conversion (a + 1 = 2^32 is exact). */
+ * (0,1] from the first word, u1 = RN32(a + 1) * 2^-32 (a + 1 = 2^32 is
+ * exact), and the angle 2 pi u2 from the top 24 bits of the second,
+ * u2 = (b >> 8) * 2^-24. */
 DML_HD void dml_normal_pair32f(uint32_t a, uint32_t b, float* n0, float* n1) {
 #if defined(__CUDA_ARCH__)
-  float a1 = a == 0xFFFFFFFFu ? 0x1.0p+32f : __uint2float_rn(a + 1u);
+  float a1 = a == 0xFFFFFFFFu ? 0x1.0p+32f : dml_u32_to_f32_rn(a + 1u);
   float u1 = __fmul_rn(a1, 0x1.0p-32f); /* (0,1] */
-  float u2 = __fmul_rn(__uint2float_rn(b >> 8), 0x1.0p-24f);
 #else
   float u1 = (float)((uint64_t)a + 1ull) * 0x1.0p-32f;
-  float u2 = (float)(b >> 8) * 0x1.0p-24f;
 #endif
   float r = DMLF_SQRT(DMLF_MUL(-2.0f, dml_logf(u1)));
   float s, c;
-  dml_sincosf_2pi(u2, &s, &c);
+  dml_sincosf_2pi_bits(b >> 8, &s, &c);
   *n0 = DMLF_MUL(r, c);
   *n1 = DMLF_MUL(r, s);
 }
@@ -260,8 +317,8 @@ DML_HD void dml_normal_pair32f(uint32_t a, uint32_t b, float* n0, float* n1) {
 DML_HD void dml_normal_pair32(uint32_t a, uint32_t b, double* n0, double* n1) {
   float f0, f1;
   dml_normal_pair32f(a, b, &f0, &f1);
-  *n0 = (double)f0;
-  *n1 = (double)f1;
+  *n0 = dml_f32_to_f64(f0);
+  *n1 = dml_f32_to_f64(f1);
 }
 
 /* Four standard normals from one 128-bit draw (FP32 values). */

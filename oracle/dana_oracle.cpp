@@ -1564,6 +1564,10 @@ void orc_rng_draw(uint64_t seed, int64_t step, uint64_t id, uint32_t stream, uin
   for (int k = 0; k < 4; ++k) out4[k] = w.w[k];
 }
 float orc_rng_logf(float x) { return dml_logf(x); }
+void orc_rng_normal_pairs(const uint32_t* w, int64_t n_pairs, float* out) {
+  for (int64_t i = 0; i < n_pairs; ++i)
+    dml_normal_pair32f(w[2 * i], w[2 * i + 1], &out[2 * i], &out[2 * i + 1]);
+}
 void orc_rng_sincosf_2pi(float u, float* s, float* c) { dml_sincosf_2pi(u, s, c); }
 void orc_rng_normal_quad(const uint32_t* w4, double* n4) {
   dml_u4 w;

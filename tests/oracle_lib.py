@@ -69,6 +69,7 @@ def load():
     lib.orc_rng_sincosf_2pi.argtypes = [ctypes.c_float, ctypes.POINTER(ctypes.c_float),
                                         ctypes.POINTER(ctypes.c_float)]
     lib.orc_rng_normal_quad.argtypes = [vp, vp]
+    lib.orc_rng_normal_pairs.argtypes = [vp, i64, vp]
     lib.orc_gen_bcc_slab.argtypes = [i32, i32, i32, ctypes.c_double, vp, i32]
     lib.orc_gen_ions.argtypes = [ctypes.c_uint64, i32, ctypes.c_double, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
