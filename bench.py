@@ -246,8 +246,10 @@ class Workload:
         return {"workload": self.desc, "replicas": self.n_rep, "n_ion": self.n_ion,
                 "n_electrode": self.n_electrode,
                 "parallelism": "replicas" if ws > 1 else "single",
-                "l2": "GPU arm: flushed between timed steps (256 MiB write outside the timed "
-                      "events); CPU reference arm: no flush"}
+                "l2": "GPU arm: not flushed, the K timed steps run as one K-step graph and "
+                      "every step reads and writes more than %.1f GB of per-atom state, far "
+                      "larger than the 129 MB L2; value_l2_flushed flushes before each step); "
+                      "CPU reference arm: no flush" % (state_bytes(self) / 1e9)}
 
     def params(self, precision):
         import ctypes
@@ -288,15 +290,54 @@ class Workload:
 
 
 def timed_steps(sim, args, clocks=None):
-    """W untimed steps, then K steps each bracketed by CUDA events (after setup)."""
+    """W untimed steps, then K steps queued as one K-step CUDA graph (what
+    dml_step does for a run of K steps), bracketed by one pair of CUDA events.
+    No L2 flush: every step reads and writes more per-atom state than the L2
+    holds (state_bytes)."""
+    sim.set_graph_steps(max(1, args.steps))
     sim.step(args.warmup)
     c0 = sim.counters()
     if clocks:
         clocks.start()
-    ms = sim.time_steps(args.steps, flush_l2=True)
+    ms = sim.time_run(args.steps)
     clk = clocks.stop() if clocks else None
     c1 = sim.counters()
     return ms, c0, c1, clk
+
+
+def flushed_steps(sim, args):
+    """K more steps, each its own one-step graph between CUDA events, the L2
+    flushed (256 MiB write) before each, outside the events."""
+    c0 = sim.counters()
+    ms = sim.time_steps(args.steps, flush_l2=True)
+    c1 = sim.counters()
+    return ms, c0, c1
+
+
+def rebuild_window(sim, steps=500):
+    """A longer window in which the replicas' neighbour lists are rebuilt as
+    the atoms move (about every 40-50 steps per config-5 replica, at
+    different steps in different replicas): graphs of 100 steps, one pair of
+    CUDA events around the window."""
+    sim.set_graph_steps(100)
+    c0 = sim.counters()
+    ms = sim.time_run(steps)
+    c1 = sim.counters()
+    n_ion = 0.5 * (c0["n_ref"] + c1["n_ref"])
+    return {"value": n_ion * steps / (ms / 1e3), "unit": UNIT, "steps": steps,
+            "ms_per_step": ms / steps,
+            "list_builds": c1["list_builds"] - c0["list_builds"],
+            "replica_rebuilds": c1["nupd"] - c0["nupd"]}
+
+
+def state_bytes(wl):
+    """A lower bound of the per-atom device state a step reads or writes
+    (bytes): per mobile ion at least 200 B (the integrator alone reads 120 B
+    of position, velocity, acceleration and element and writes position,
+    FP32 copy, old position and noise; the force, displacement and overlap
+    passes add more), per electrode atom 32 B (the displacement test's two
+    FP32 positions)."""
+    return int(wl.n_ion * 200 + wl.n_electrode * 32)
 
 
 def force_error_probe(wl, nrep=4, steps=20):
@@ -314,6 +355,7 @@ def force_error_probe(wl, nrep=4, steps=20):
 
     EV = 96.485 * 100.0  # ui per eV (dana.F90:23)
     rel, rel_all, absd, emix, epl, inter = [], [], [], 0.0, 0.0, 0
+    fmag, unfl = [], []
     for r in range(min(nrep, wl.n_rep)):
         sp = wl.open(dml.PRECISION_FP64, replicas=[r])
         sp.setup()
@@ -341,11 +383,27 @@ def force_error_probe(wl, nrep=4, steps=20):
             frms = float(np.sqrt((fr[hit] ** 2).mean()))
             rel.append(d / np.maximum(fr, frms))
             rel_all.append(d / np.maximum(fr, float(np.sqrt((fr ** 2).mean()))))
+            fmag.append(fr[hit])
+            unfl.append(d[hit] / fr[hit])
         emix += float(em.sum())
         epl += float(ep.sum())
     e = np.concatenate(rel) if rel else np.zeros(1)
     ea = np.concatenate(rel_all) if rel_all else np.zeros(1)
+    # |dF| / |F| with no floor, by decile of |F| over the interacting ions
+    deciles = []
+    if fmag:
+        fm_all, un_all = np.concatenate(fmag), np.concatenate(unfl)
+        order = np.argsort(fm_all)
+        for part in np.array_split(order, 10):
+            if len(part):
+                deciles.append({"f_min_ev_per_A": float(fm_all[part].min() / EV),
+                                "f_max_ev_per_A": float(fm_all[part].max() / EV),
+                                "ions": int(len(part)),
+                                "max_rel": float(un_all[part].max()),
+                                "median_rel": float(np.median(un_all[part]))})
     return {"max_rel": float(e.max()), "rms_rel": float(np.sqrt((e ** 2).mean())),
+            "unfloored": {"max_rel": float(max((x["max_rel"] for x in deciles), default=0.0)),
+                          "by_force_decile": deciles},
             "max_rel_floor_all_ions": float(ea.max()),
             "max_abs_ev_per_A": float(np.concatenate(absd).max() / EV) if absd else 0.0,
             "energy_rel": float(abs(emix - epl) / abs(epl)) if epl else 0.0,
@@ -353,6 +411,40 @@ def force_error_probe(wl, nrep=4, steps=20):
             "state": "after %d FP64 steps and an FP64 ermak_a, fuerza in both forms at those "
                      "positions" % steps,
             "tolerance": 1e-6, "within": bool(e.max() <= 1e-6)}
+
+
+def deposition_probe(n_rep=64, steps=2000):
+    """Deposition statistics of the two forms over seeds: n_rep config-1
+    systems (400-atom bcc electrode, 200 Li+, piston), each its own ion
+    placement and Philox seed, run `steps` Ermak steps in one batch per form.
+    The captures per replica are compared: the chosen form's mean against the
+    plain FP64 form's mean and spread over seeds."""
+    import statistics as st
+
+    import dml
+    from tests import systems
+
+    p = systems.c1_params(seed=500)
+    reps = [dml.replica_of(p, seed=500 + 7919 * r) for r in range(n_rep)]
+    atoms = [systems.c1_atoms(seed=900 + r) for r in range(n_rep)]
+    depo = {}
+    for form, prec in (("fp64", dml.PRECISION_FP64), ("mixed", dml.PRECISION_MIXED)):
+        q = dml.Params()
+        ctypes.memmove(ctypes.byref(q), ctypes.byref(p), ctypes.sizeof(q))
+        q.precision = prec
+        sim = dml.Simulation(q, replicas=reps)
+        sim.set_atoms(atoms)
+        sim.setup()
+        sim.step(steps)
+        depo[form] = [int(sim.counters(replica=r)["depo"]) for r in range(n_rep)]
+        sim.close()
+    mf, mm = st.mean(depo["fp64"]), st.mean(depo["mixed"])
+    sf = st.stdev(depo["fp64"])
+    return {"system": "config 1 (10x10x2-cell electrode, 200 Li+, piston z0=30, Ermak dt=1fs)",
+            "seeds": n_rep, "steps": steps, "fp64_mean": mf, "fp64_sigma": sf,
+            "mixed_mean": mm, "mixed_sigma": st.stdev(depo["mixed"]),
+            "mean_difference_in_fp64_sigma": (mm - mf) / sf if sf else None,
+            "within_1_sigma": bool(sf == 0.0 or abs(mm - mf) <= sf)}
 
 
 def cpu_baseline_sample(wl, budget_s=12.0, max_steps=200, warmup=0):
@@ -644,6 +736,9 @@ def run_gpu(args, ws, rank, local):
     value, ms_max = job_value(dist, n_ion, args.steps, ms)
     # the same rate counting every atom, frozen electrode atoms included
     value_all, _ = job_value(dist, 0.5 * (c0["n_atoms"] + c1["n_atoms"]), args.steps, ms)
+    # the same steps one graph each, the L2 flushed before each
+    ms_f, f0, f1 = flushed_steps(sim, args)
+    value_flushed, _ = job_value(dist, 0.5 * (f0["n_ref"] + f1["n_ref"]), args.steps, ms_f)
     per_step, per_rebuild = sim.launches_per_step()
     tuning = sim.tuning()
     launches = per_step * args.steps + per_rebuild * (c1["list_builds"] - c0["list_builds"])
@@ -651,6 +746,7 @@ def run_gpu(args, ws, rank, local):
     counters = {k: c1[k] - c0[k] for k in ("choques", "depo", "try_", "choques3", "gcmc_ins",
                                            "gcmc_del", "list_builds")}
     counters["n_ref"] = c1["n_ref"]
+    with_rebuilds = rebuild_window(sim) if not args.no_compare else None
     sim.close()
 
     # Comparison arms (chosen form only): the same batch in plain FP64, and
@@ -660,6 +756,7 @@ def run_gpu(args, ws, rank, local):
     if form == "chosen" and not args.no_compare:
         compare = {}
         compare["force_error"] = force_error_probe(wl)
+        compare["deposition"] = deposition_probe()
         sp = wl.open(dml.PRECISION_FP64)
         sp.setup()
         ms_p, p0, p1, _ = timed_steps(sp, args)
@@ -717,6 +814,11 @@ def run_gpu(args, ws, rank, local):
         return 0
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "value_including_electrode": value_all,
+            "value_l2_flushed": {"value": value_flushed, "unit": UNIT,
+                                 "ms_per_step": ms_f / args.steps,
+                                 "how": "the next K steps, one graph launch each, the L2 "
+                                        "flushed before each step outside the events"},
+            "value_with_rebuilds": with_rebuilds,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 pair forces, int64 fixed-point sums, f64 integration" if form == "chosen"

@@ -35,6 +35,8 @@ struct dml_ctx {
   std::vector<dml_replica> reps;  // per-replica geometry and seeds
   std::vector<RepConst> rc;       // per-replica device constants (host copy)
   cudaGraphExec_t step_graph = nullptr;
+  cudaGraphExec_t multi_graph = nullptr;  // graph_steps steps in one graph
+  int graph_steps = 100;
   int launches_per_step = 0;    // kernels of a step without a list rebuild
   int launches_per_rebuild = 0; // extra kernels when the list is rebuilt
   float tune_us[kScanMappings] = {};  // force-scan time per mapping (1, 2, 4, 8, 16, 32 lanes per row)
@@ -464,6 +466,46 @@ int build_step_graph(dml_ctx* c) {
   return 0;
 }
 
+// graph_steps iterations of the loop body captured into one graph (each
+// with its own conditional rebuild nodes), so that a run of many steps is a
+// few graph launches.
+int build_multi_graph(dml_ctx* c) {
+  if (c->multi_graph) return 0;
+  int rc = build_step_graph(c);
+  if (rc) return rc;
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+  for (int i = 0; i < c->graph_steps && rc == 0; ++i) {
+    int nb = 0, nr = 0;
+    rc = enqueue_step(c, nullptr, true, &nb, &nr);
+  }
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (rc) {
+    if (e == cudaSuccess) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture (multi-step graph)");
+  e = cudaGraphInstantiate(&c->multi_graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphInstantiate (multi-step graph)");
+  return 0;
+}
+
+// nsteps iterations: as many graph_steps-step graphs as fit, then one-step
+// graphs.
+int queue_steps(dml_ctx* c, int64_t nsteps) {
+  int rc = build_step_graph(c);
+  if (rc) return rc;
+  int64_t i = 0;
+  if (c->graph_steps > 1 && nsteps >= c->graph_steps) {
+    if ((rc = build_multi_graph(c)) != 0) return rc;
+    for (; i + c->graph_steps <= nsteps; i += c->graph_steps)
+      CK(cudaGraphLaunch(c->multi_graph, c->stream));
+  }
+  for (; i < nsteps; ++i) CK(cudaGraphLaunch(c->step_graph, c->stream));
+  return 0;
+}
+
 constexpr size_t kFlushBytes = 256ull << 20;  // > 2x the 129 MB L2
 
 int ensure_flush(dml_ctx* c) {
@@ -608,6 +650,7 @@ void dml_destroy(dml_ctx* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
+  if (c->multi_graph) cudaGraphExecDestroy(c->multi_graph);
   for (void* p : c->allocs) cudaFree(p);
   if (c->flush_buf) cudaFree(c->flush_buf);
   if (c->h_sc) cudaFreeHost(c->h_sc);
@@ -1125,10 +1168,41 @@ int dml_setup(dml_ctx* c) {
 
 int dml_step_async(dml_ctx* c, int64_t nsteps) {
   if (!c || !c->loaded || !c->setup_done) return DML_E_STATE;
-  int rc = build_step_graph(c);
-  if (rc) return rc;
-  for (int64_t i = 0; i < nsteps; ++i) CK(cudaGraphLaunch(c->step_graph, c->stream));
+  return queue_steps(c, nsteps);
+}
+
+int dml_set_graph_steps(dml_ctx* c, int32_t k) {
+  if (!c || k < 1) return DML_E_ARG;
+  if (k != c->graph_steps && c->multi_graph) {
+    CK(cudaStreamSynchronize(c->stream));
+    cudaGraphExecDestroy(c->multi_graph);
+    c->multi_graph = nullptr;
+  }
+  c->graph_steps = k;
   return 0;
+}
+
+int dml_time_run(dml_ctx* c, int64_t nsteps, double* ms) {
+  if (!c || !ms || nsteps <= 0) return DML_E_ARG;
+  if (!c->loaded || !c->setup_done) return DML_E_STATE;
+  int rc = build_step_graph(c);
+  if (!rc && c->graph_steps > 1 && nsteps >= c->graph_steps) rc = build_multi_graph(c);
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaEventRecord(e0, c->stream));
+  rc = queue_steps(c, nsteps);
+  CK(cudaEventRecord(e1, c->stream));
+  CK(cudaEventSynchronize(e1));
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  *ms = t;
+  return finish(c);
 }
 
 int dml_sync(dml_ctx* c) {

@@ -325,8 +325,10 @@ __global__ void step_begin_kernel(Dev d, int near_stale) {
 // The integrators' share of overlap_moveback in a fused step: the
 // component state of the moving atom, and delta bounded from the FP32
 // positions (|x - RN32(x)| <= 2^-24 |x|; the near radius adds the margin).
-__device__ __forceinline__ void overlap_prepare_atom(const Dev& d, const RepConst& R, int h,
-                                                     float4 before, float4 after) {
+// Returns the squared FP32 move as its bit pattern (non-negative floats
+// order as their bit patterns), for block_max_to.
+__device__ __forceinline__ unsigned overlap_prepare_atom(const Dev& d, const RepConst& R, int h,
+                                                         float4 before, float4 after) {
   d.uf[h] = h;
   d.active[h] = 0;
   d.comp_size[h] = 0;
@@ -335,10 +337,20 @@ __device__ __forceinline__ void overlap_prepare_atom(const Dev& d, const RepCons
   vdist_nint_f(R, after, before, x, y, z);
   float dd = x * x + y * y + z * z;
   if (!(dd == dd)) dd = 0.0f;  // a NaN position takes no part (and stops at test_update)
-  // non-negative floats order as their bit patterns: warp maximum, one atomic
-  const unsigned m = __activemask();
-  const unsigned v = __reduce_max_sync(m, __float_as_uint(dd));
-  if ((int)(threadIdx.x & 31) == __ffs(m) - 1 && v) atomicMax(&d.g->delta2f_bits, v);
+  return __float_as_uint(dd);
+}
+
+// Maximum of v over the block, one atomic per block into *dst (a per-warp
+// atomic on one address serialises some 10^5 operations per launch in the
+// L2).  Every thread of the block must call it.
+__device__ __forceinline__ void block_max_to(unsigned v, unsigned* dst) {
+  __shared__ unsigned s_max;
+  if (threadIdx.x == 0) s_max = 0u;
+  __syncthreads();
+  v = __reduce_max_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0 && v) atomicMax(&s_max, v);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_max) atomicMax(dst, s_max);
 }
 
 // atom_pbc (dana.F90:1187-1250) on registers; returns true when deposited.
@@ -439,10 +451,10 @@ __device__ __forceinline__ void erm_load(const Dev& d, int h, ErmIn& in) {
   in.id = d.id[h];
   in.before = d.posf[h];
 }
-__device__ __forceinline__ void ermak_a_mixed_atom(const Dev& d, const KParams& p,
-                                                   const RepConst& R, Scalars* sc, int h,
-                                                   const ErmIn& in, long long step, double zmax,
-                                                   float zmaxf) {
+__device__ __forceinline__ unsigned ermak_a_mixed_atom(const Dev& d, const KParams& p,
+                                                       const RepConst& R, Scalars* sc, int h,
+                                                       const ErmIn& in, long long step,
+                                                       double zmax, float zmaxf) {
   const double4 P = make_double4(in.Pxy.x, in.Pxy.y, in.Pz, 0.0);
   const float4 V = in.V, A = in.A;
   int typ = in.typ;
@@ -480,7 +492,7 @@ __device__ __forceinline__ void ermak_a_mixed_atom(const Dev& d, const KParams& 
   d.pos[h] = make_double4(pp[0], pp[1], pp[2], 0.0);
   d.posf[h] = after;
   d.ranvf[h] = make_float4(rv[0], rv[1], rv[2], 0.0f);
-  overlap_prepare_atom(d, R, h, before, after);
+  const unsigned mv = overlap_prepare_atom(d, R, h, before, after);
   if (po_changed) {
     d.pos_old[h] = po;
     d.posf_old[h] = to_f4(po, 0);
@@ -488,16 +500,17 @@ __device__ __forceinline__ void ermak_a_mixed_atom(const Dev& d, const KParams& 
   if (v_changed) stv(d.vel, h, V.x, V.y, -V.z);  // the mirror at zmax reverses vz
   if (typ != typ0) d.typ[h] = (int8_t)typ;
   if (!depos) d.skip[h] = 0;
+  return mv;
 }
 
 // ermak_a (dana.F90:974-1028): one thread per hs%ref member; one kernel
 // per form, so that each gets only the registers its own path needs.
 template <bool MIXED>
-__device__ __forceinline__ void ermak_a_at(const Dev& d, const KParams& p, int rep, int h,
-                                           long long step, double zmax, float zmaxf) {
+__device__ __forceinline__ unsigned ermak_a_at(const Dev& d, const KParams& p, int rep, int h,
+                                               long long step, double zmax, float zmaxf) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
-  if (MIXED) return;
+  if (MIXED) return 0u;
   double4 P = d.pos[h];
   double4 V = d.vel[h];
   double4 A = d.acel[h];
@@ -529,7 +542,7 @@ __device__ __forceinline__ void ermak_a_at(const Dev& d, const KParams& p, int r
   d.pos[h] = np;
   d.posf[h] = after;
   d.ranv[h] = make_double4(rv[0], rv[1], rv[2], 0.0);
-  overlap_prepare_atom(d, R, h, before, after);
+  const unsigned mv = overlap_prepare_atom(d, R, h, before, after);
   if (po_changed) {
     d.pos_old[h] = po;
     d.posf_old[h] = to_f4(po, 0);
@@ -537,6 +550,7 @@ __device__ __forceinline__ void ermak_a_at(const Dev& d, const KParams& p, int r
   if (v_changed) d.vel[h] = V;
   if (typ != typ0) d.typ[h] = (int8_t)typ;
   if (!depos) d.skip[h] = 0;
+  return mv;
 }
 
 // The block's hs%ref entries are read first, all four at once, and the
@@ -555,33 +569,35 @@ __global__ void __launch_bounds__(kBlock, 3) ermak_a_kernel(Dev d, KParams p, in
   const long long step = d.g->step;
   const double zmax = d.sc[rep].zmax;
   const float zmaxf = (float)zmax;
+  unsigned mv = 0u;  // largest squared move of the block's atoms (bits)
   if (!MIXED) {
 #pragma unroll 1
     for (int u = 0; u < kSlotU; ++u) {
-      if (h0 >= 0) ermak_a_at<MIXED>(d, p, rep, h0, step, zmax, zmaxf);
+      if (h0 >= 0) mv = max(mv, ermak_a_at<MIXED>(d, p, rep, h0, step, zmax, zmaxf));
       h0 = h1; h1 = h2; h2 = h3;
     }
-    return;
-  }
-  const RepConst& R = d.rc[rep];
-  Scalars* sc = d.sc + rep;
-  ErmIn cur;
-  if (h0 >= 0) erm_load(d, h0, cur);
+  } else {
+    const RepConst& R = d.rc[rep];
+    Scalars* sc = d.sc + rep;
+    ErmIn cur;
+    if (h0 >= 0) erm_load(d, h0, cur);
 #pragma unroll 1
-  for (int u = 0; u < kSlotU; ++u) {
-    ErmIn nxt;
-    if (h1 >= 0) erm_load(d, h1, nxt);
-    if (h0 >= 0) ermak_a_mixed_atom(d, p, R, sc, h0, cur, step, zmax, zmaxf);
-    cur = nxt;
-    h0 = h1; h1 = h2; h2 = h3; h3 = -1;
+    for (int u = 0; u < kSlotU; ++u) {
+      ErmIn nxt;
+      if (h1 >= 0) erm_load(d, h1, nxt);
+      if (h0 >= 0) mv = max(mv, ermak_a_mixed_atom(d, p, R, sc, h0, cur, step, zmax, zmaxf));
+      cur = nxt;
+      h0 = h1; h1 = h2; h2 = h3; h3 = -1;
+    }
   }
+  block_max_to(mv, &d.g->delta2f_bits);
 }
 
 // cbrownian_hs (dana.F90:798-846): one thread per hs%ref member; one kernel
 // per form.
 template <bool MIXED>
-__device__ __forceinline__ void brownian_at(const Dev& d, const KParams& p, int rep, int h,
-                                            long long step, double zmax, float zmaxf) {
+__device__ __forceinline__ unsigned brownian_at(const Dev& d, const KParams& p, int rep, int h,
+                                                long long step, double zmax, float zmaxf) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   double4 P = d.pos[h];
@@ -615,14 +631,14 @@ __device__ __forceinline__ void brownian_at(const Dev& d, const KParams& p, int 
     d.pos[h] = make_double4(pp[0], pp[1], pp[2], 0.0);
     d.posf[h] = after;
     stv(d.vel, h, vf[0], vf[1], vf[2]);
-    overlap_prepare_atom(d, R, h, before, after);
+    const unsigned mv = overlap_prepare_atom(d, R, h, before, after);
     if (po_changed) {
       d.pos_old[h] = po;
       d.posf_old[h] = to_f4(po, 0);
     }
     if (typ != typ0) d.typ[h] = (int8_t)typ;
     if (!depos) d.skip[h] = 0;
-    return;
+    return mv;
   }
   double fac = P.z > p.dif_switch_z ? p.fac_sc : p.fac_sei;
   double nrm[4];
@@ -646,13 +662,14 @@ __device__ __forceinline__ void brownian_at(const Dev& d, const KParams& p, int 
   d.pos[h] = np;
   d.posf[h] = after;
   d.vel[h] = V;
-  overlap_prepare_atom(d, R, h, before, after);
+  const unsigned mv = overlap_prepare_atom(d, R, h, before, after);
   if (po_changed) {
     d.pos_old[h] = po;
     d.posf_old[h] = to_f4(po, 0);
   }
   if (typ != typ0) d.typ[h] = (int8_t)typ;
   if (!depos) d.skip[h] = 0;
+  return mv;
 }
 
 // hs%ref entries and the replica's scalars read first, as in ermak_a.
@@ -669,13 +686,15 @@ __global__ void __launch_bounds__(kBlock, 4) brownian_kernel(Dev d, KParams p, i
   const long long step = d.g->step;
   const double zmax = d.sc[rep].zmax;
   const float zmaxf = (float)zmax;
+  unsigned mv = 0u;
 #pragma unroll 1
   for (int u = 0; u < kSlotU; ++u) {
-    if (h0 >= 0) brownian_at<MIXED>(d, p, rep, h0, step, zmax, zmaxf);
+    if (h0 >= 0) mv = max(mv, brownian_at<MIXED>(d, p, rep, h0, step, zmax, zmaxf));
     h0 = h1;
     h1 = h2;
     h2 = h3;
   }
+  block_max_to(mv, &d.g->delta2f_bits);
 }
 
 // Union-find over hs slots (overlap components): path halving, union by

@@ -82,6 +82,8 @@ def lib():
     L.dml_last_error.restype = ctypes.c_char_p
     L.dml_last_error.argtypes = [vp]
     L.dml_time_steps.argtypes = [vp, i64, i32, P(ctypes.c_double)]
+    L.dml_time_run.argtypes = [vp, i64, P(ctypes.c_double)]
+    L.dml_set_graph_steps.argtypes = [vp, i32]
     L.dml_profile_steps.argtypes = [vp, i64, i32, vp, i32]
     L.dml_launches_per_step.argtypes = [vp, P(i32)]
     L.dml_get_tuning.argtypes = [vp, P(i32), vp]
@@ -349,6 +351,15 @@ class Simulation:
 
     PHASES = ["integrate", "force_pairs", "force_sum", "test_update1", "overlap",
               "test_update2", "commit", "gcmc_cells", "gcmc", "rho_piston"]
+
+    def time_run(self, n):
+        """Device milliseconds of n steps queued as step(n) queues them."""
+        ms = ctypes.c_double()
+        self._check(self.lib.dml_time_run(self.h, n, ctypes.byref(ms)), "dml_time_run")
+        return ms.value
+
+    def set_graph_steps(self, k):
+        self._check(self.lib.dml_set_graph_steps(self.h, k), "dml_set_graph_steps")
 
     def profile_steps(self, n, flush_l2=True):
         """Per-phase device time [ms] summed over n un-graphed steps."""

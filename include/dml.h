@@ -224,6 +224,18 @@ int dml_step(dml_ctx* c, int64_t nsteps);
 int dml_step_async(dml_ctx* c, int64_t nsteps);
 int dml_sync(dml_ctx* c);
 
+/* Steps per graph launch (no counterpart in the reference): dml_step and
+ * dml_step_async queue runs of k steps as one CUDA graph (each step with its
+ * own conditional rebuild nodes, built at the first run of k or more steps)
+ * and the rest one step per launch.  Default 100; 1 launches one graph per
+ * step.  The results do not depend on k. */
+int dml_set_graph_steps(dml_ctx* c, int32_t k);
+
+/* Benchmark support: nsteps steps queued as dml_step queues them (graphs of
+ * graph_steps steps), bracketed by one pair of CUDA events on the context
+ * stream; *ms is their device time.  No L2 flush. */
+int dml_time_run(dml_ctx* c, int64_t nsteps, double* ms);
+
 /* Benchmark support.  dml_time_steps queues nsteps steps like dml_step,
  * each bracketed by CUDA events on the context stream; with flush_l2 a
  * 256 MiB buffer is overwritten between steps, outside the events.  *ms is

@@ -196,3 +196,30 @@ def test_batch_download_equals_per_replica(precision):
             assert same_bits(full[r][k], one[k]), "replica %d member %s" % (r, k)
         assert set(sub[r]) == {"pos", "z"}
         assert same_bits(sub[r]["pos"], one["pos"]) and np.array_equal(sub[r]["z"], one["z"])
+
+
+@pytest.mark.parametrize("precision", [dml.PRECISION_FP64, dml.PRECISION_MIXED])
+def test_steps_per_graph_do_not_change_results(precision):
+    """dml_step queues runs of graph_steps steps as one CUDA graph (each step
+    with its own conditional rebuild nodes): 1, 7 and 100 steps per graph
+    give the same state, bit for bit, after 150 GCMC + Ermak steps."""
+    p = systems.c5_small_params(nadj=64)
+    p.precision = precision
+    p.skin = 1.0  # list rebuilds inside the run
+    reps = [dml.replica_of(p, seed=3), dml.replica_of(p, seed=4)]
+    atoms = [systems.c1_atoms(seed=s, dmin=3.2) for s in (5, 6)]
+    out = []
+    for k in (1, 7, 100):
+        g = dml.Simulation(p, replicas=reps)
+        g.set_atoms(atoms)
+        g.setup()
+        g.set_graph_steps(k)
+        g.step(150)
+        out.append([g.get_atoms(replica=r) for r in range(2)] + [g.counters()])
+        g.close()
+    assert out[0][2]["nupd"] >= 4 and out[0][2]["gcmc_ins"] > 0
+    for other in out[1:]:
+        for r in range(2):
+            for key in FIELDS:
+                assert same_bits(out[0][r][key], other[r][key]), (r, key)
+        assert out[0][2] == other[2]
