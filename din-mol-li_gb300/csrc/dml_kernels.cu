@@ -2348,21 +2348,19 @@ __device__ __forceinline__ void overlap_assign_at(const Dev& d, int end, int i) 
   }
 }
 
+// The listed members are few (atoms with a near contact): one block per
+// replica walks its list segment, instead of a block per 1024 positions.
 __global__ void overlap_assign_kernel(Dev d) {
-  const int rep = block_rep(d);
-  const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntAct];
-  if (blockIdx.x * kSpan >= end) return;  // block-uniform
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) overlap_assign_at(d, end, span_pos(u));
+  const int rep = blockIdx.x;
+  const int base = d.rc[rep].base;
+  const int end = base + d.pr_cnt[rep * kCntStride + kCntAct];
+  for (int i0 = base; i0 < end; i0 += blockDim.x) overlap_assign_at(d, end, i0 + threadIdx.x);
 }
 
 __global__ void overlap_scatter_kernel(Dev d) {
-  const int rep = block_rep(d);
+  const int rep = blockIdx.x;
   const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntAct];
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) {
-    const int i = span_pos(u);
-    if (i >= end) break;
+  for (int i = d.rc[rep].base + threadIdx.x; i < end; i += blockDim.x) {
     const int r = d.act_list[i];
     const int h = d.ref[r];
     const int root = d.uf[h];
@@ -2376,12 +2374,9 @@ __global__ void overlap_scatter_kernel(Dev d) {
 // number of smaller ranks in its component (contiguous loads, all members
 // in parallel).
 __global__ void overlap_order_kernel(Dev d) {
-  const int rep = block_rep(d);
+  const int rep = blockIdx.x;
   const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntAct];
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) {
-    const int i = span_pos(u);
-    if (i >= end) break;
+  for (int i = d.rc[rep].base + threadIdx.x; i < end; i += blockDim.x) {
     const int r = d.act_list[i];
     const int h = d.ref[r];
     const int cid = d.comp_id[d.uf[h]];
@@ -2458,9 +2453,7 @@ __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, in
 // the members with skip = false, in rank order, whatever the other
 // components do.  Otherwise only pass 1 runs here and the later passes run
 // in overlap_passn_kernel with a barrier per pass.
-__global__ void overlap_pass1_kernel(Dev d, KParams p, int all_passes) {
-  int cid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (cid >= d.g->n_comp) return;
+__device__ void overlap_pass1_comp(const Dev& d, const KParams& p, int all_passes, int cid) {
   int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
   const int* mem = d.comp_members + off;
   int pass = 1;
@@ -2488,6 +2481,13 @@ __global__ void overlap_pass1_kernel(Dev d, KParams p, int all_passes) {
   }
   if (sz > 0) atomicMax(&d.sc[d.rep_of[mem[0]]].passes, pass);
   atomicMax(&d.g->passes, pass);
+}
+
+__global__ void overlap_pass1_kernel(Dev d, KParams p, int all_passes) {
+  const int ncomp = d.g->n_comp;
+  for (int cid = blockIdx.x * blockDim.x + threadIdx.x; cid < ncomp;
+       cid += gridDim.x * blockDim.x)
+    overlap_pass1_comp(d, p, all_passes, cid);
 }
 
 // Passes 2.. (the recursion, needed when a capture can fail): one block, a
@@ -5202,11 +5202,11 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
   }
   if (detect) n += k_overlap_detect(d, p, n_rank, detect == 1 ? 1 : 0, s);
   overlap_count_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
-  overlap_assign_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d);
-  overlap_scatter_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d);
-  overlap_order_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d);
+  overlap_assign_kernel<<<d.nrep, kBlock, 0, s>>>(d);
+  overlap_scatter_kernel<<<d.nrep, kBlock, 0, s>>>(d);
+  overlap_order_kernel<<<d.nrep, kBlock, 0, s>>>(d);
   int all_passes = p.prob >= 1.0;
-  overlap_pass1_kernel<<<nblk(n_rank, 128), 128, 0, s>>>(d, p, all_passes);
+  overlap_pass1_kernel<<<152 * 4, 128, 0, s>>>(d, p, all_passes);
   n += 5;
   if (all_passes) return n;
   overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
