@@ -36,6 +36,11 @@ struct dml_ctx {
   std::vector<RepConst> rc;       // per-replica device constants (host copy)
   cudaGraphExec_t step_graph = nullptr;
   cudaGraphExec_t multi_graph = nullptr;  // graph_steps steps in one graph
+  // chunk reservoir template (dml_set_chunk): positions as chunk.xyz gives
+  // them, elements, chunk height
+  std::vector<double> chunk_pos;
+  std::vector<int> chunk_z;
+  double chunk_dist = 0.0;
   int graph_steps = 100;
   int launches_per_step = 0;    // kernels of a step without a list rebuild
   int launches_per_rebuild = 0; // extra kernels when the list is rebuilt
@@ -197,6 +202,10 @@ void make_kparams(const dml_params& P, KParams& K) {
   K.prob = P.prob;
   K.h_over_tau = P.h / P.tau;
   K.ztop_is_z1 = P.reservoir == DML_RESERVOIR_CHUNKS ? 1.0 : 0.0;
+  K.rcut_b = P.rc + P.skin;
+  K.rhomedia = 5.775329e-4;  // dana.F90:445
+  K.chunk_dist = 0.0;
+  K.n_chunk = 0;
   K.integrator = P.integrator;
   K.reservoir = P.reservoir;
   K.mnb = P.mnb;
@@ -300,6 +309,52 @@ int capture_test_update(dml_ctx* c, int* n_base, int* n_body, bool near_in_body,
   return 0;
 }
 
+// bloques (dana.F90:247, 716-773) and the test_update it ends with: the
+// chunk kernel, then the rebuild of the replicas that took a chunk -- a
+// conditional graph node under capture, else decided on the host.  The
+// displacement test runs for every replica; those without a chunk decide
+// what their second test_update of the step decided (nothing has moved since).
+int queue_bloques(dml_ctx* c, bool capture, int* n_base, int* n_body) {
+  cudaStream_t s = c->stream;
+  *n_base += k_bloques(c->D, c->K, s);
+  if (capture) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphConditionalHandle h;
+    CK(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+    *n_base += k_chunk_cond(c->D, h, s);
+    CK(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    CK(cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    CK(cudaStreamBeginCaptureToGraph(c->aux, body, nullptr, nullptr, 0,
+                                     cudaStreamCaptureModeRelaxed));
+    *n_body += k_rank_prefix(c->D, c->aux);
+    *n_body += k_test_update(c->D, c->K, c->D.cap, c->D.cap, c->D.cap, c->aux);
+    cudaGraph_t outg;
+    CK(cudaStreamEndCapture(c->aux, &outg));
+    CK(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1,
+                                           cudaStreamSetCaptureDependencies));
+    return 0;
+  }
+  int ev = 0;
+  CK(cudaMemcpyAsync(&ev, &c->D.g->chunk_event, sizeof ev, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (ev) {
+    *n_body += k_rank_prefix(c->D, s);
+    *n_body += k_test_update(c->D, c->K, c->D.cap, c->D.cap, c->D.cap, s);
+  }
+  return 0;
+}
+
 // One iteration of the loop body of dana.F90:173-265 (without salida,
 // timer_dump and the chunk reservoir), queued on the context stream.  With
 // `ev` (DML_NPHASE + 1 events) the phase boundaries are recorded.  With
@@ -382,6 +437,8 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
   mark(DML_PHASE_RHO_PISTON);
   n += k_calc_rho(d, k, cap, s);
   if (c->P.reservoir == DML_RESERVOIR_PISTON) n += k_piston(d, k, cap, s);
+  if (c->P.reservoir == DML_RESERVOIR_CHUNKS && (rc = queue_bloques(c, capture, &n, &nb)) != 0)
+    return rc;
   mark(DML_NPHASE);
   if (n_base) *n_base = n;
   if (n_body) *n_body = nb;
@@ -593,7 +650,6 @@ int dml_create_batch(const dml_params* p, int32_t n_rep, const dml_replica* reps
   if (!p || !out || n_rep <= 0 || !reps) return DML_E_ARG;
   *out = nullptr;
   if (p->reservoir < 0 || p->reservoir > 3) return DML_E_RESERVOIR;
-  if (p->reservoir == DML_RESERVOIR_CHUNKS) return DML_E_UNSUPPORTED;
   if (p->reservoir == DML_RESERVOIR_GCMC && (p->nadj < 0 || !(p->act > 0))) return DML_E_ARG;
   if (p->precision != DML_PRECISION_FP64 && p->precision != DML_PRECISION_MIXED) return DML_E_ARG;
   if (!(p->h > 0 && p->rc > 0)) return DML_E_ARG;
@@ -677,11 +733,19 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   // kMaxPositions of them (far beyond what HBM holds at this layout)
   constexpr long long kMaxPositions = 1LL << 30;
   int total = 0, ncell = 0, any_cells = 0, any_verlet = 0, n_cch = 0;
+  const bool chunks = c->P.reservoir == DML_RESERVOIR_CHUNKS;
+  const int n_chunk = (int)c->chunk_z.size();
+  if (chunks && n_chunk == 0) {
+    c->last_error = "chunk reservoir: dml_set_chunk must come before the atoms";
+    return DML_E_STATE;
+  }
   for (int r = 0; r < nrep; ++r) {
     const dml_atoms* a = atoms + r;
     if (a->n <= 0 || !a->pos || !a->z) return DML_E_ARG;
+    // room for 16 chunks by default with the chunk reservoir
     const long long want = c->P.capacity > 0 ? c->P.capacity
-                           : (c->P.reservoir == DML_RESERVOIR_GCMC ? 2LL * a->n + 1024 : a->n);
+                           : (c->P.reservoir == DML_RESERVOIR_GCMC ? 2LL * a->n + 1024
+                              : chunks ? a->n + 16LL * n_chunk : a->n);
     const long long capl = (std::max<long long>(a->n, want) + kSpan - 1) / kSpan * kSpan;
     if (total + capl > kMaxPositions) {
       c->last_error = "capacity: more than 2^30 atom positions in one context";
@@ -689,15 +753,33 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     }
     const int cap = (int)capl;
     RepConst& R = c->rc[r];
+    // The chunk reservoir raises the box by the chunk height at each chunk,
+    // at most (cap - n) / n_chunk times: the replica's cells (and its FP32
+    // pre-filter margins) are sized for the tallest box.
+    RepConst M = R;
+    if (chunks) {
+      dml_replica tall = c->reps[r];
+      const long long events = (cap - a->n) / n_chunk;
+      tall.zmax = c->reps[r].zmax + (double)events * c->chunk_dist;
+      tall.box[2] = std::max(c->reps[r].box[2], tall.zmax);
+      make_repconst(c->P, tall, M);
+      R.margin = M.margin;
+      R.rlist_lo2 = M.rlist_lo2;
+      R.rlist_hi2 = M.rlist_hi2;
+      R.rc_lo2 = M.rc_lo2;
+      R.rc_hi2 = M.rc_hi2;
+      std::memcpy(R.r0f_pref2, M.r0f_pref2, sizeof R.r0f_pref2);
+    }
     R.base = total;
     R.cap = cap;
     R.nblk = cap / kSpan;
     R.cell_off = ncell;
     R.cch0 = n_cch;
-    n_cch += (R.ncell + kCellChunk - 1) / kCellChunk;
-    ncell += R.ncell + (R.use_cells ? 1 : 0);  // + the replica's sentinel cell
+    n_cch += (M.ncell + kCellChunk - 1) / kCellChunk;
+    ncell += M.ncell + (M.use_cells ? 1 : 0);  // + the replica's sentinel cell
     total += cap;
-    if (R.use_cells) any_cells = 1; else any_verlet = 1;
+    if (R.use_cells || M.use_cells) any_cells = 1;
+    if (!R.use_cells) any_verlet = 1;
   }
   d.cap = total;
   d.max_rep_cap = 0;
@@ -787,16 +869,21 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.big_cells, ncell + 1);
   AL(d.cch_rep, n_cch > 0 ? n_cch : 1);
   {
+    // every chunk of the replicas' cell ranges (those sized for a taller box
+    // included) belongs to its replica
     std::vector<int> cr(n_cch > 0 ? n_cch : 1, 0);
     for (int r = 0; r < nrep; ++r) {
-      const RepConst& R = c->rc[r];
-      for (int q = 0; q < (R.ncell + kCellChunk - 1) / kCellChunk; ++q) cr[R.cch0 + q] = r;
+      const int end = r + 1 < nrep ? c->rc[r + 1].cch0 : n_cch;
+      for (int q = c->rc[r].cch0; q < end; ++q) cr[q] = r;
     }
     // on the context stream, after the zeroing of the new allocation
     CK(cudaMemcpyAsync(d.cch_rep, cr.data(), sizeof(int) * cr.size(), cudaMemcpyHostToDevice,
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));
   }
+  AL(d.chk_pos, chunks ? (size_t)nrep * n_chunk : 1);
+  AL(d.chk_pold, chunks ? (size_t)nrep * n_chunk : 1);
+  AL(d.chk_typ, chunks ? (size_t)n_chunk : 1);
   if (c->P.reservoir == DML_RESERVOIR_GCMC) {
     const bool par = c->P.nadj <= kGcmcMaxTrials;
     AL(d.grp, nrep);
@@ -978,6 +1065,9 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     S.free_lo = n;  // slots are dense after loading
     S.bfree_lo = n;
     S.next_id = max_id + 1;
+    // config_chunk: the template atoms take the next ids (never keys of a
+    // draw: they do not move)
+    if (c->P.reservoir == DML_RESERVOIR_CHUNKS) S.next_id += (long long)c->chunk_z.size();
     }
   };
   if (e == cudaSuccess) {
@@ -1044,6 +1134,29 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   cudaFree(db);
   if (e != cudaSuccess) return cuda_fail(c, e, what);
   CK(cudaMemcpyAsync(d.sc, c->h_sc, sizeof(Scalars) * nrep, cudaMemcpyHostToDevice, st));
+  if (chunks) {
+    // config_chunk (dana.F90:552-587): the template raised by zmax, its old
+    // position by zmax again (as the reference writes it)
+    std::vector<double4> tp((size_t)nrep * n_chunk), to((size_t)nrep * n_chunk);
+    std::vector<int8_t> tz(n_chunk);
+    for (int r = 0; r < nrep; ++r) {
+      const double zm = c->reps[r].zmax;
+      for (int j = 0; j < n_chunk; ++j) {
+        const double* q = &c->chunk_pos[3 * (size_t)j];
+        const double zr = q[2] + zm;
+        tp[(size_t)r * n_chunk + j] = make_double4(q[0], q[1], zr, 0.0);
+        to[(size_t)r * n_chunk + j] = make_double4(q[0], q[1], zr + zm, 0.0);
+      }
+    }
+    for (int j = 0; j < n_chunk; ++j) tz[j] = (int8_t)c->chunk_z[j];
+    CK(cudaMemcpyAsync(d.chk_pos, tp.data(), sizeof(double4) * tp.size(), cudaMemcpyHostToDevice,
+                       st));
+    CK(cudaMemcpyAsync(d.chk_pold, to.data(), sizeof(double4) * to.size(),
+                       cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d.chk_typ, tz.data(), tz.size(), cudaMemcpyHostToDevice, st));
+    c->K.chunk_dist = c->chunk_dist;
+    c->K.n_chunk = n_chunk;
+  }
   std::memset(c->h_g, 0, sizeof(Global));
   CK(cudaMemcpyAsync(d.g, c->h_g, sizeof(Global), cudaMemcpyHostToDevice, st));
   CK(cudaStreamSynchronize(st));
@@ -1164,6 +1277,28 @@ int dml_setup(dml_ctx* c) {
   if (rc) return rc;
   c->setup_done = true;
   return 0;
+}
+
+int dml_set_chunk(dml_ctx* c, int32_t n, const double* pos, const int32_t* z, double dist) {
+  if (!c || n <= 0 || !pos || !z || !(dist > 0)) return DML_E_ARG;
+  if (c->P.reservoir != DML_RESERVOIR_CHUNKS) return DML_E_RESERVOIR;
+  if (c->loaded) return DML_E_STATE;
+  for (int j = 0; j < n; ++j)
+    if (z[j] < 1 || z[j] > 3) return DML_E_ARG;
+  c->chunk_pos.assign(pos, pos + 3 * (size_t)n);
+  c->chunk_z.assign(z, z + n);
+  c->chunk_dist = dist;
+  return 0;
+}
+
+int dml_bloques(dml_ctx* c) {
+  if (!c || !c->loaded) return DML_E_STATE;
+  if (c->P.reservoir != DML_RESERVOIR_CHUNKS) return DML_E_RESERVOIR;
+  CK(cudaMemsetAsync(&c->D.g->chunk_event, 0, sizeof(int), c->stream));
+  int nb = 0, nbody = 0;
+  int rc = queue_bloques(c, false, &nb, &nbody);
+  if (rc) return rc;
+  return finish(c);
 }
 
 int dml_step_async(dml_ctx* c, int64_t nsteps) {

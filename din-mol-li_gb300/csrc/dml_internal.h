@@ -120,6 +120,7 @@ struct Global {
   int near_stale;           // near lists must be searched in the overlap phase
   int n_big;                // entries of big_cells
   int n_ftouch;             // entries of ftlist (mixed-form sums)
+  int chunk_event;          // some replica added its chunk this step (bloques)
 };
 
 struct EvRec {            // one interacting list entry seen from one atom
@@ -157,6 +158,10 @@ struct KParams {
   double prob;
   double h_over_tau;
   double ztop_is_z1;        // chunks: calc_rho uses z1
+  // chunk reservoir (bloques, dana.F90:716-773): chunk height, the density
+  // it keeps (rhomedia, dana.F90:445) and the cell edge bound rc + skin
+  double chunk_dist, rhomedia, rcut_b;
+  int n_chunk;
   int integrator, reservoir;
   int mnb, ev_cap, max_passes;
   // gcmc_run (dana.F90:590-713)
@@ -286,6 +291,10 @@ struct Dev {
   unsigned* gpm;       // [nrep][kGcmcMaxTrials][kGcmcMaskW] earlier trial points within rc
   GcmcRepPre* grp;     // [nrep]
   unsigned *gw_mem, *gw_slab;  // [cap / 32] membership / in-slab bits of gcmc%alist positions
+  // chunk reservoir: every replica's template atoms (positions and old
+  // positions, [nrep][n_chunk]) and their elements ([n_chunk])
+  double4 *chk_pos, *chk_pold;
+  int8_t* chk_typ;
   int nrep;
   int cap;            // positions over all replicas (sum of the replica caps)
   int max_rep_cap;    // largest replica capacity
@@ -347,6 +356,10 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
 int k_overlap_detect(const Dev& d, const KParams& p, int n_rank, int mode, cudaStream_t s);
 int k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_calc_rho(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
+// bloques: the chunk event of every replica (sets Global::chunk_event); with
+// a conditional handle the kernel after it opens the rebuild subgraph.
+int k_bloques(const Dev& d, const KParams& p, cudaStream_t s);
+int k_chunk_cond(const Dev& d, cudaGraphConditionalHandle h, cudaStream_t s);
 int k_piston(const Dev& d, const KParams& p, int n_slots, cudaStream_t s);
 int k_flush(void* buf, size_t bytes, cudaStream_t s);
 int k_gcmc(const Dev& d, const KParams& p, int cap, cudaStream_t s);

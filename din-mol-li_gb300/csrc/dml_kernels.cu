@@ -308,6 +308,7 @@ __global__ void step_begin_kernel(Dev d, int near_stale) {
   if (threadIdx.x == 0) {
     g->step += 1;
     g->delta2f_bits = 0u;
+    g->chunk_event = 0;
     g->near_stale = near_stale;
     // overlap_moveback's counters (reset per call in the standalone path)
     g->again = 0;
@@ -2660,6 +2661,148 @@ __global__ void piston_kernel(Dev d, KParams p, int n_slots) {
   for (int u = 0; u < kSlotU; ++u) piston_at(d, p, n_slots, rep, span_pos(u));
 }
 
+
+// ------------------------------------------------------------- bloques
+// cgroup_tessellate (Cells.F90:180-265) after the box height changed to bz:
+// a tessellated replica keeps its cell counts while every cell edge stays
+// in (rc + skin, (n + 1)/n (rc + skin)], else the counts are taken again
+// from int(box / (rc + skin)); cells are off while all three counts are
+// below 4.  Only z changes (the chunk reservoir raises the box), so the x
+// and y values are those of the replica's creation.
+__device__ void tessellate_height(RepConst& R, const KParams& p, double bz) {
+  R.box[2] = bz;
+  R.one_box[2] = 1.0 / bz;
+  R.halfbox[2] = bz * .5;
+  R.boxf[2] = __double2float_rn(bz);
+  R.halfboxf[2] = __double2float_rn(bz * .5);
+  bool keep = false;
+  if (R.use_cells) {
+    keep = true;
+    for (int k = 0; k < 3; ++k) {
+      if (!((double)(R.ncells[k] + 1) >= R.box[k] / p.rcut_b)) keep = false;
+      if (!(p.rcut_b < R.box[k] / (double)R.ncells[k])) keep = false;
+    }
+  }
+  if (!keep) {
+    int n[3];
+    for (int k = 0; k < 3; ++k) n[k] = (int)(R.box[k] / p.rcut_b);
+    if (n[0] < 4 && n[1] < 4 && n[2] < 4) return;  // still no cells
+    R.use_cells = 1;
+    for (int k = 0; k < 3; ++k) R.ncells[k] = n[k] < 1 ? 1 : n[k];
+  }
+  for (int k = 0; k < 3; ++k) {
+    R.cell[k] = R.box[k] / (double)R.ncells[k];
+    R.inv_cellf[k] = __double2float_rn(1.0 / R.cell[k]);
+    R.cellf[k] = __double2float_rn(R.cell[k]);
+    R.head_dim[k] = R.ncells[k] + 2;
+  }
+  R.ncell = R.head_dim[0] * R.head_dim[1] * R.head_dim[2];
+  R.tess_hif = __double2float_rn((double)(R.ncells[2] + 1) * R.cell[2]);
+}
+
+// bloques (dana.F90:716-773), one block per replica, one thread: when the
+// sensor density strays from rhomedia by 0.186 rhomedia or more (the
+// literal is single precision), the planes rise by the chunk height, the
+// template atoms are attached in template order (sys%alist appended, first
+// free hs and hs%b slots, hs%ref appended, a new id; atom_asign copies the
+// template's position, old position, velocity, acceleration, force, energy
+// and element), the template rises, the box height becomes zmax and the
+// list is marked stale, so that the test_update after it rebuilds.
+__global__ void bloques_kernel(Dev d, KParams p) {
+  const int rep = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  Scalars* sc = d.sc + rep;
+  RepConst& R = d.rc[rep];
+  const double drho = sc->rho - p.rhomedia;
+  if (fabs(drho) < (p.rhomedia * (double)0.186f)) return;
+  sc->z0 = sc->z0 + p.chunk_dist;
+  sc->z1 = sc->z1 + p.chunk_dist;
+  sc->zmax = sc->zmax + p.chunk_dist;
+  sc->zmax_frame = sc->zmax;
+  sc->listed = 0;
+  const int B = R.base;
+  double4* tp = d.chk_pos + (size_t)rep * p.n_chunk;
+  double4* to = d.chk_pold + (size_t)rep * p.n_chunk;
+  for (int j = 0; j < p.n_chunk; ++j) {
+    // first free hs slot (limbo slots are not free) and hs%b slot
+    const int nat = sc->n_atoms + 1, bnat = sc->b_nat + 1;
+    const int ns = sc->n_slots, nb = sc->n_b;
+    int ls = ns, lb = nb;
+    if (ns >= nat + sc->nlimbo) {
+      ls = INT_MAX;
+      for (int q = sc->free_lo; q < ns; ++q)
+        if (d.state[B + q] == ST_NULL) {
+          ls = q;
+          break;
+        }
+    }
+    if (nb >= bnat) {
+      lb = INT_MAX;
+      for (int q = sc->bfree_lo; q < nb; ++q)
+        if (d.b2hs[B + q] < 0) {
+          lb = q;
+          break;
+        }
+    }
+    if (ls == INT_MAX || lb == INT_MAX) {
+      raise_error(d.g, DML_E_INDEX, j);
+      return;
+    }
+    if (ls >= R.cap || lb >= R.cap || sc->n_rank >= R.cap || sc->n_alist >= R.cap) {
+      raise_error(d.g, DML_E_CAPACITY, j);
+      return;
+    }
+    const int slot = B + ls, bs = B + lb;
+    const int typ = d.chk_typ[j];
+    const double4 P = tp[j], O = to[j];
+    d.pos[slot] = P;
+    d.pos_old[slot] = O;
+    d.posf[slot] = to_f4(P, typ);
+    d.posf_old[slot] = to_f4(O, 0);
+    d.vel[slot] = make_double4(0.0, 0.0, 0.0, 0.0);
+    d.acel[slot] = make_double4(0.0, 0.0, 0.0, 0.0);
+    d.force[slot] = make_double4(0.0, 0.0, 0.0, 0.0);
+    d.epot[slot] = 0.0;
+    d.old_cg[slot] = make_double4(1e8, 1e8, 1e8, 0.0);
+    d.typ[slot] = (int8_t)typ;
+    d.skip[slot] = 0;
+    d.id[slot] = sc->next_id;
+    sc->next_id += 1;
+    d.ev_count[slot] = 0;
+    d.nn[slot] = 0;
+    // sys
+    const int ap = sc->n_alist;
+    d.alist[B + ap] = slot;
+    d.apos[slot] = B + ap;
+    sc->n_alist = ap + 1;
+    // hs%ref
+    const int rk = sc->n_rank;
+    d.ref[B + rk] = slot;
+    d.rank[slot] = B + rk;
+    sc->n_rank = rk + 1;
+    sc->n_ref += 1;
+    // hs%b (not sorted into cells: the list is stale)
+    d.b2hs[bs] = slot;
+    d.bslot[slot] = bs;
+    if (lb == nb) sc->n_b = nb + 1;
+    sc->b_nat = bnat;
+    sc->bfree_lo = lb + 1;
+    // hs
+    d.state[slot] = ST_LIVE;
+    if (ls == ns) sc->n_slots = ns + 1;
+    sc->free_lo = ls + 1;
+    sc->n_atoms = nat;
+    // the template rises (dana.F90:762-763)
+    tp[j].z = P.z + p.chunk_dist;
+    to[j].z = O.z + p.chunk_dist;
+  }
+  tessellate_height(R, p, sc->zmax);
+  atomicOr(&d.g->chunk_event, 1);
+}
+
+__global__ void chunk_cond_kernel(Global* g, cudaGraphConditionalHandle h) {
+  cudaGraphSetConditional(h, g->chunk_event ? 1u : 0u);
+}
 
 // ------------------------------------------------------------------ gcmc_run
 // gcmc_run (dana.F90:590-713): the trials are sequential (each sees the
@@ -5211,6 +5354,16 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
   if (all_passes) return n;
   overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
   return n + 1;
+}
+
+int k_bloques(const Dev& d, const KParams& p, cudaStream_t s) {
+  bloques_kernel<<<d.nrep, 32, 0, s>>>(d, p);
+  return 1;
+}
+
+int k_chunk_cond(const Dev& d, cudaGraphConditionalHandle h, cudaStream_t s) {
+  chunk_cond_kernel<<<1, 1, 0, s>>>(d.g, h);
+  return 1;
 }
 
 int k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {

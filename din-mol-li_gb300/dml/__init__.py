@@ -84,6 +84,8 @@ def lib():
     L.dml_time_steps.argtypes = [vp, i64, i32, P(ctypes.c_double)]
     L.dml_time_run.argtypes = [vp, i64, P(ctypes.c_double)]
     L.dml_set_graph_steps.argtypes = [vp, i32]
+    L.dml_set_chunk.argtypes = [vp, i32, vp, vp, ctypes.c_double]
+    L.dml_bloques.argtypes = [vp]
     L.dml_profile_steps.argtypes = [vp, i64, i32, vp, i32]
     L.dml_launches_per_step.argtypes = [vp, P(i32)]
     L.dml_get_tuning.argtypes = [vp, P(i32), vp]
@@ -351,6 +353,17 @@ class Simulation:
 
     PHASES = ["integrate", "force_pairs", "force_sum", "test_update1", "overlap",
               "test_update2", "commit", "gcmc_cells", "gcmc", "rho_piston"]
+
+    def set_chunk(self, pos, z, dist):
+        """config_chunk: the chunk reservoir's template (positions as
+        chunk.xyz gives them, elements) and chunk height; before set_atoms."""
+        pos = np.ascontiguousarray(pos, np.float64)
+        z = np.ascontiguousarray(z, np.int32)
+        self._check(self.lib.dml_set_chunk(self.h, len(z), pos.ctypes.data, z.ctypes.data,
+                                           float(dist)), "dml_set_chunk")
+
+    def bloques(self):
+        self._check(self.lib.dml_bloques(self.h), "dml_bloques")
 
     def time_run(self, n):
         """Device milliseconds of n steps queued as step(n) queues them."""

@@ -215,9 +215,25 @@ int dml_calc_rho(dml_ctx* c, double* rho);
 /* maxz (src/dana.F90:776-794): piston compression using the last rho. */
 int dml_piston(dml_ctx* c);
 
+/* Chunk reservoir (reservoir DML_RESERVOIR_CHUNKS).  dml_set_chunk replaces
+ * config_chunk (src/dana.F90:552-587): the n template atoms as chunk.xyz
+ * gives them (pos [n][3], elements z [n]), the same for every replica, and
+ * the chunk height dist (entrada.ini's dist plus rc, as config_inic makes it,
+ * :437-441; z0, z1 and zmax come in dml_params / dml_replica as config_inic
+ * leaves them).  It must come before dml_set_atoms_batch: the template is
+ * raised by each replica's zmax there and takes the ids after the
+ * replica's atoms, and each replica's cells are sized for the tallest box
+ * its capacity allows ((capacity - atoms) / n chunks; default capacity:
+ * room for 16 chunks).  dml_bloques replaces bloques (:716-773) with the
+ * test_update it ends with; dml_step runs it after calc_rho, as the
+ * reference's step does (:247). */
+int dml_set_chunk(dml_ctx* c, int32_t n, const double* pos, const int32_t* z, double dist);
+int dml_bloques(dml_ctx* c);
+
 /* One or more iterations of the step loop body (src/dana.F90:173-265,
- * without the output and timer lines), starting at step counter+1.  The
- * steps are queued as one CUDA graph per call shape and replayed. */
+ * without the output and timer lines, with the piston's maxz and the chunk
+ * reservoir's bloques), starting at step counter+1.  The steps are queued
+ * as CUDA graphs (see dml_set_graph_steps) and replayed. */
 int dml_step(dml_ctx* c, int64_t nsteps);
 
 /* Queues nsteps like dml_step and returns without waiting. dml_sync waits. */

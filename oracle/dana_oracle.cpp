@@ -993,6 +993,7 @@ struct Sim {
     z0 = z0 + dist;
     z1 = z1 + dist;
     zmax = zmax + dist;
+    zmax_frame = zmax;  // salida's info line reports the new top
     listed = false;
     std::vector<int> chunk = chunk_list;
     for (int h1 : chunk) {
@@ -1295,6 +1296,38 @@ int orc_gcmc(orc_sim* o, int64_t step) {
   o->s.gcmc_run();
   return o->s.err;
 }
+// config_chunk (dana.F90:552-587) from arrays instead of chunk.xyz: n
+// template atoms at pos (as the file gives them) with elements z, raised by
+// zmax (pos_old by twice zmax, as the reference writes it), outside every
+// group; dist is the chunk height (entrada.ini's dist plus rc, :437-441).
+int orc_set_chunk(orc_sim* o, int32_t n, const double* pos, const int32_t* z, double dist) {
+  Sim& s = o->s;
+  if (n <= 0 || !pos || !z) return DML_E_ARG;
+  s.dist = dist;
+  for (int j = 0; j < n; ++j) {
+    const int h = s.new_atom();
+    Atom& a = s.at[h];
+    for (int k = 0; k < 3; ++k) a.pos[k] = pos[3 * j + k];
+    s.setz(a, z[j]);
+    for (int k = 0; k < 3; ++k) {
+      a.force[k] = 0.0;
+      a.pos_old[k] = a.pos[k];
+    }
+    a.pos[2] = a.pos[2] + s.zmax;
+    a.pos_old[2] = a.pos[2] + s.zmax;
+    a.pbc[0] = a.pbc[1] = true;
+    a.pbc[2] = false;
+    s.chunk_list.push_back(h);
+  }
+  return 0;
+}
+
+// bloques (dana.F90:716-773) on its own.
+int orc_bloques(orc_sim* o) {
+  o->s.bloques();
+  return o->s.err;
+}
+
 int orc_calc_rho(orc_sim* o, double* rho) {
   o->s.calc_rho();
   if (rho) *rho = o->s.rho;

@@ -84,6 +84,8 @@ int orc_overlap_moveback(orc_sim* o, int64_t step);
 int orc_capture_commit(orc_sim* o, int32_t* n_new);
 int orc_gcmc(orc_sim* o, int64_t step);
 int orc_calc_rho(orc_sim* o, double* rho);
+int orc_set_chunk(orc_sim* o, int32_t n, const double* pos, const int32_t* z, double dist);
+int orc_bloques(orc_sim* o);
 int orc_piston(orc_sim* o);
 int orc_get_atoms(orc_sim* o, dml_atoms* a);
 int orc_get_neighbors(orc_sim* o, int32_t* n_ref, int32_t* nn, int32_t* list, int32_t ld);

@@ -70,6 +70,8 @@ def load():
                                         ctypes.POINTER(ctypes.c_float)]
     lib.orc_rng_normal_quad.argtypes = [vp, vp]
     lib.orc_rng_normal_pairs.argtypes = [vp, i64, vp]
+    lib.orc_set_chunk.argtypes = [vp, i32, vp, vp, ctypes.c_double]
+    lib.orc_bloques.argtypes = [vp]
     lib.orc_gen_bcc_slab.argtypes = [i32, i32, i32, ctypes.c_double, vp, i32]
     lib.orc_gen_ions.argtypes = [ctypes.c_uint64, i32, ctypes.c_double, ctypes.c_double,
                                  ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
@@ -204,6 +206,15 @@ class Oracle:
 
     def maxz(self):
         self._check(self.lib.orc_piston(self.h))
+
+    def set_chunk(self, pos, z, dist):
+        """config_chunk: the chunk template (positions as chunk.xyz gives them)."""
+        pos = np.ascontiguousarray(pos, np.float64)
+        z = np.ascontiguousarray(z, np.int32)
+        self._check(self.lib.orc_set_chunk(self.h, len(z), pos.ctypes.data, z.ctypes.data, dist))
+
+    def bloques(self):
+        self._check(self.lib.orc_bloques(self.h))
 
     def set_step(self, step):
         self.lib.orc_set_step(self.h, step)

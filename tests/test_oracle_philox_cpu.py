@@ -101,3 +101,22 @@ def test_deposit_above_z0_stops_the_run():
         o.step(50)
     c = o.counters()
     assert c["depo"] >= 1 and c["try_"] >= c["depo"]
+
+
+def test_chunk_reservoir_adds_chunks():
+    """The oracle's bloques in the keyed-stream mode: the tests/brown geometry
+    takes chunks as the sensor empties (the chunk parity tests on the GPU
+    compare the device with this)."""
+    from tests.test_gpu_chunks import brown_atoms, brown_params, read_chunk
+
+    p, dist = brown_params()
+    pos, z = read_chunk()
+    o = oracle_lib.Oracle(p)
+    o.set_atoms(brown_atoms())
+    o.set_chunk(pos, z, dist)
+    o.setup()
+    z0 = o.counters()["zmax"]
+    o.step(5)
+    c = o.counters()
+    assert c["zmax"] >= z0 + 2 * dist - 1e-9
+    assert c["n_atoms"] == 602 + 301 * round((c["zmax"] - z0) / dist)
