@@ -1441,8 +1441,9 @@ int dml_check_conversions(const double* x, int64_t n, float* f32, double* back) 
   return e == cudaSuccess ? 0 : DML_E_CUDA;
 }
 
-int dml_check_normals(const uint32_t* words, int64_t n_pairs, float* out) {
+int dml_check_normals(const uint32_t* words, int64_t n_pairs, int32_t precision, float* out) {
   if (n_pairs < 0 || (n_pairs > 0 && (!words || !out))) return DML_E_ARG;
+  if (precision != DML_PRECISION_FP64 && precision != DML_PRECISION_MIXED) return DML_E_ARG;
   if (n_pairs == 0) return 0;
   unsigned* dw = nullptr;
   float* dout = nullptr;
@@ -1451,7 +1452,7 @@ int dml_check_normals(const uint32_t* words, int64_t n_pairs, float* out) {
   if (e == cudaSuccess)
     e = cudaMemcpy(dw, words, sizeof(unsigned) * 2 * n_pairs, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) {
-    k_check_normals(dw, dout, n_pairs, 0);
+    k_check_normals(dw, dout, n_pairs, precision == DML_PRECISION_MIXED ? 1 : 0, 0);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess)

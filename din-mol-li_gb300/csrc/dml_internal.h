@@ -328,7 +328,8 @@ struct PackOut {
 int k_pack_atoms(const Dev& d, const KParams& p, const PackOut& o, cudaStream_t s);
 int k_salida(const Dev& d, const KParams& p, double kb, dml_observables* out, cudaStream_t s);
 int k_check_conversions(const double* x, float* f32, double* back, long long n, cudaStream_t s);
-int k_check_normals(const unsigned* w, float* out, long long n_pairs, cudaStream_t s);
+int k_check_normals(const unsigned* w, float* out, long long n_pairs, int fast,
+                    cudaStream_t s);
 int k_check_pick(const unsigned long long* k, const int* n, int* m, long long count, cudaStream_t s);
 int k_step_begin(const Dev& d, int near_stale, cudaStream_t s);
 int k_rank_prefix(const Dev& d, cudaStream_t s);

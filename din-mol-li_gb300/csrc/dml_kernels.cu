@@ -402,6 +402,32 @@ __device__ __forceinline__ bool atom_pbc_dev(const KParams& p, const RepConst& R
   return depos;
 }
 
+// Box-Muller pair of the chosen form: the same two words as
+// dml_normal_pair32f, the transform from the hardware's approximate
+// log2, sin and cos (__log2f, __sinf, __cosf) instead of the exactly
+// rounded series the plain form shares with the oracle.  u1 = (a + 1) 2^-32
+// enters as 2^e m, e = -1 - clz(a + 1) and m in [1, 2) from the next 23
+// bits (truncated), so no conversion instruction is needed and the radius
+// still reaches the plain form's 6.66 sigma; u2 takes the top 23 bits of b.
+// The approximate log2 is good to about 2^-22 absolute, so the normals agree
+// with the plain form's within about 2e-6 (1 + r) for radii r above 0.05
+// (the radius of the smaller ones, a fraction 1e-3 of the pairs, within 1e-3).
+__device__ __forceinline__ void normal_pair_fast(uint32_t a, uint32_t b, float& n0, float& n1) {
+  const uint32_t x = a + 1u;  // 0 stands for 2^32 (u1 = 1)
+  float l2 = 0.0f;            // log2(u1)
+  if (x != 0u) {
+    const int lz = __clz((int)x);
+    const uint32_t m = (x << lz) << 1;  // the bits after the leading one
+    l2 = __log2f(__uint_as_float(0x3F800000u | (m >> 9))) + dml_small_i2f(-1 - lz);
+  }
+  const float r = __fsqrt_rn(-1.3862944f * l2);  // sqrt(-2 ln u1) = sqrt(-2 ln2 log2 u1)
+  const float th = 6.2831853f * (__uint_as_float(0x3F800000u | (b >> 9)) - 1.0f);
+  float sn, cs;
+  __sincosf(th, &sn, &cs);
+  n0 = r * cs;
+  n1 = r * sn;
+}
+
 // The chosen form's FP32 velocity (first half) and acceleration (second
 // half) of an atom's vel slot.
 __device__ __forceinline__ void ldva(const double4* vel, int h, float4& v, float4& a) {
@@ -465,9 +491,9 @@ __device__ __forceinline__ unsigned ermak_a_mixed_atom(const Dev& d, const KPara
   float nq[6];
   const dml_u4 w0 = dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 0);
   const dml_u4 w1 = dml_draw(R.seed, step, (uint64_t)id, DML_RNG_ERMAK, 1);
-  dml_normal_pair32f(w0.w[0], w0.w[1], &nq[0], &nq[1]);
-  dml_normal_pair32f(w0.w[2], w0.w[3], &nq[2], &nq[3]);
-  dml_normal_pair32f(w1.w[0], w1.w[1], &nq[4], &nq[5]);
+  normal_pair_fast(w0.w[0], w0.w[1], nq[0], nq[1]);
+  normal_pair_fast(w0.w[2], w0.w[3], nq[2], nq[3]);
+  normal_pair_fast(w1.w[0], w1.w[1], nq[4], nq[5]);
   const float vv[3] = {V.x, V.y, V.z}, aa[3] = {A.x, A.y, A.z};
   double pp[3] = {P.x, P.y, P.z};
   float rv[3];
@@ -559,7 +585,7 @@ __device__ __forceinline__ unsigned ermak_a_at(const Dev& d, const KParams& p, i
 // while the previous atom is integrated (three blocks per SM leave the
 // registers for the second set).
 template <bool MIXED>
-__global__ void __launch_bounds__(kBlock, 3) ermak_a_kernel(Dev d, KParams p, int n_rank) {
+__global__ void __launch_bounds__(kBlock, MIXED ? 4 : 3) ermak_a_kernel(Dev d, KParams p, int n_rank) {
   const int rep = block_rep(d);
   const int end = d.rc[rep].base + d.sc[rep].n_rank;
   if ((int)blockIdx.x * kSpan >= end) return;
@@ -608,7 +634,9 @@ __device__ __forceinline__ unsigned brownian_at(const Dev& d, const KParams& p, 
     // chosen form: FP32 increments added to the FP64 position, FP32 velocity
     const float facf = P.z > p.dif_switch_z ? p.fac_scf : p.fac_seif;
     float nf[4];
-    dml_normal_quadf(dml_draw(R.seed, step, (uint64_t)id, DML_RNG_BROWN, 0), nf);
+    const dml_u4 w = dml_draw(R.seed, step, (uint64_t)id, DML_RNG_BROWN, 0);
+    normal_pair_fast(w.w[0], w.w[1], nf[0], nf[1]);
+    normal_pair_fast(w.w[2], w.w[3], nf[2], nf[3]);
     double pp[3] = {P.x, P.y, P.z};
     float vf[3];
 #pragma unroll
@@ -5484,14 +5512,20 @@ __global__ void check_pick_kernel(const unsigned long long* k, const int* n, int
     m[i] = gcmc_pick_index(k[i], n[i]);
 }
 
-__global__ void check_normals_kernel(const unsigned* w, float* out, long long n_pairs) {
+__global__ void check_normals_kernel(const unsigned* w, float* out, long long n_pairs,
+                                     int fast) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_pairs;
-       i += (long long)gridDim.x * blockDim.x)
-    dml_normal_pair32f(w[2 * i], w[2 * i + 1], &out[2 * i], &out[2 * i + 1]);
+       i += (long long)gridDim.x * blockDim.x) {
+    if (fast)
+      normal_pair_fast(w[2 * i], w[2 * i + 1], out[2 * i], out[2 * i + 1]);
+    else
+      dml_normal_pair32f(w[2 * i], w[2 * i + 1], &out[2 * i], &out[2 * i + 1]);
+  }
 }
 
-int k_check_normals(const unsigned* w, float* out, long long n_pairs, cudaStream_t s) {
-  check_normals_kernel<<<152 * 4, kBlock, 0, s>>>(w, out, n_pairs);
+int k_check_normals(const unsigned* w, float* out, long long n_pairs, int fast,
+                    cudaStream_t s) {
+  check_normals_kernel<<<152 * 4, kBlock, 0, s>>>(w, out, n_pairs, fast);
   return 1;
 }
 

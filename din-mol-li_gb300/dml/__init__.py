@@ -91,7 +91,7 @@ def lib():
     L.dml_get_tuning.argtypes = [vp, P(i32), vp]
     L.dml_check_conversions.argtypes = [vp, i64, vp, vp]
     L.dml_check_pick.argtypes = [vp, vp, i64, vp]
-    L.dml_check_normals.argtypes = [vp, i64, vp]
+    L.dml_check_normals.argtypes = [vp, i64, i32, vp]
     L.dml_gen_bcc_slab.argtypes = [i32, i32, i32, ctypes.c_double, vp, i32]
     L.dml_gen_ions.argtypes = [ctypes.c_uint64, i32, ctypes.c_double, ctypes.c_double,
                                ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
@@ -119,12 +119,13 @@ def check_conversions(x):
     return f32, back
 
 
-def check_normals(words):
+def check_normals(words, precision=PRECISION_FP64):
     """The device's Box-Muller normals of 32-bit word pairs (uint32 array of
-    even length): float32 array of the same length."""
+    even length): float32 array of the same length.  PRECISION_FP64: the
+    plain form's pair; PRECISION_MIXED: the chosen form's integrators' pair."""
     w = np.ascontiguousarray(words, dtype=np.uint32)
     out = np.zeros(w.shape, np.float32)
-    rc = lib().dml_check_normals(w.ctypes.data, w.size // 2, out.ctypes.data)
+    rc = lib().dml_check_normals(w.ctypes.data, w.size // 2, precision, out.ctypes.data)
     if rc:
         raise DmlError(rc, "dml_check_normals")
     return out

@@ -419,11 +419,14 @@ int dml_gen_ions(uint64_t seed, int32_t n, double box_x, double box_y, double zl
 int dml_check_conversions(const double* x, int64_t n, float* f32, double* back);
 
 /* Diagnostic (no counterpart in the reference): the device's Box-Muller pair
- * of the keyed streams, out[2i], out[2i+1] = the two normals that the
- * integrators and gcmc_run make from the 32-bit words words[2i], words[2i+1]
- * (include/dml_rng.h, dml_normal_pair32f; its integer-to-float steps are
- * integer operations on the device).  Host arrays; returns 0 or DML_E_CUDA. */
-int dml_check_normals(const uint32_t* words, int64_t n_pairs, float* out);
+ * of the keyed streams, out[2i], out[2i+1] = the two normals made from the
+ * 32-bit words words[2i], words[2i+1].  precision DML_PRECISION_FP64: the
+ * pair of the plain form and of gcmc_run (include/dml_rng.h,
+ * dml_normal_pair32f, bit-identical to the host build; its integer-to-float
+ * steps are integer operations on the device).  DML_PRECISION_MIXED: the
+ * chosen form's integrators' pair (approximate hardware log2, sin, cos).
+ * Host arrays; returns 0, DML_E_ARG or DML_E_CUDA. */
+int dml_check_normals(const uint32_t* words, int64_t n_pairs, int32_t precision, float* out);
 
 /* Diagnostic (no counterpart in the reference): the device's deletion pick
  * of gcmc_run, m[i] = int(upick * n[i]) + 1 capped at n[i] with upick =

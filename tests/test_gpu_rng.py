@@ -49,9 +49,35 @@ def test_device_normals_equal_host_normals():
     w = np.empty(2 * len(a), np.uint32)
     w[0::2] = np.array(a, np.uint64).astype(np.uint32)
     w[1::2] = np.array(b, np.uint64).astype(np.uint32)
-    got = dml.check_normals(w)
+    got = dml.check_normals(w, dml.PRECISION_FP64)
     want = host_normals(w)
     bad = np.flatnonzero(got.view(np.uint32) != want.view(np.uint32))
     assert len(bad) == 0, (len(bad), w[2 * (bad[0] // 2)], w[2 * (bad[0] // 2) + 1])
     assert np.isfinite(got).all()
     assert abs(float(got.mean())) < 0.01 and abs(float(got.var()) - 1.0) < 0.01
+
+
+def test_chosen_form_normals_close_to_exact_ones():
+    """The chosen form's integrators take the same words through the
+    hardware's approximate log2, sin and cos.  The log2 error is absolute
+    (about 2^-22), so the radius r = sqrt(-2 ln u1) is within 2e-6 (1 + r)
+    of the exact one where r > 0.05, and within 1e-3 where r is smaller
+    (u1 within 1e-3 of 1); standard moments, tails to 6.6 sigma."""
+    rng = np.random.default_rng(12)
+    n = 400000
+    w = rng.integers(0, 2 ** 32, 2 * n, dtype=np.uint64).astype(np.uint32)
+    w[0], w[2], w[4] = 0xFFFFFFFF, 0, 1  # u1 = 1 and the two smallest u1
+    fast = dml.check_normals(w, dml.PRECISION_MIXED)
+    exact = host_normals(w)
+    assert np.isfinite(fast).all()
+    r = np.hypot(exact[0::2].astype(np.float64), exact[1::2]).repeat(2)
+    diff = np.abs(fast.astype(np.float64) - exact)
+    big = r > 0.05
+    assert (diff[big] / (1.0 + r[big])).max() < 2e-6
+    assert diff.max() < 1e-3
+    assert fast[0] == 0.0 and fast[1] == 0.0
+    assert np.abs(fast[2:6]).max() > 6.0
+    v = fast[6:].astype(np.float64)
+    assert abs(v.mean()) < 0.005 and abs(v.var() - 1.0) < 0.005
+    assert abs((v ** 4).mean() - 3.0) < 0.05
+
