@@ -463,10 +463,12 @@ int autotune_scan(dml_ctx* c) {
   CK(cudaEventCreate(&e1));
   k_rank_prefix(c->D, s);
   KParams k = c->K;
-  float best = 1e30f;
-  int best_l = 32;
-  auto scan = [&]() {
-    if (ermak) {
+  // near: the near-contact search of overlap_moveback (every step with the
+  // Brownian integrator; with Ermak only over the rows of replicas whose
+  // list was just rebuilt, the force scan finding the near entries
+  // otherwise), else the force scan.
+  auto scan = [&](bool near) {
+    if (!near) {
       k_force_scan(c->D, k, c->D.cap, false, s);
       k_reset_candidates(c->D, s);
     } else {
@@ -476,31 +478,41 @@ int autotune_scan(dml_ctx* c) {
   // Mappings in order of lanes; the search stops at the first one that is
   // slower than the previous and than 1.25x the best (times grow with the
   // lanes past the best); untimed mappings keep tune_us 0.
-  float prev = 1e30f;
-  for (int v = 0; v < kScanMappings; ++v) {
-    k.scan_lanes = lanes[v];
-    k.near_lanes = lanes[v];
-    scan();  // warm-up
-    CK(cudaEventRecord(e0, s));
-    for (int rep = 0; rep < 3; ++rep) scan();
-    CK(cudaEventRecord(e1, s));
-    CK(cudaEventSynchronize(e1));
-    float ms = 0;
-    CK(cudaEventElapsedTime(&ms, e0, e1));
-    c->tune_us[v] = ms * 1e3f / 3.0f;
-    if (ms < best) {
-      best = ms;
-      best_l = lanes[v];
+  auto sweep = [&](bool near, float* us) -> int {
+    float best = 1e30f, prev = 1e30f;
+    int best_l = 32;
+    for (int v = 0; v < kScanMappings; ++v) {
+      k.scan_lanes = lanes[v];
+      k.near_lanes = lanes[v];
+      scan(near);  // warm-up
+      float ms = 0;
+      if (cudaEventRecord(e0, s) != cudaSuccess) return -1;
+      for (int rep = 0; rep < 3; ++rep) scan(near);
+      if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+        return -1;
+      if (us) us[v] = ms * 1e3f / 3.0f;
+      if (ms < best) {
+        best = ms;
+        best_l = lanes[v];
+      }
+      if (ms > prev && ms > 1.25f * best) break;
+      prev = ms;
     }
-    if (ms > prev && ms > 1.25f * best) break;
-    prev = ms;
+    return best_l;
+  };
+  int sl = 0, nl = 0;
+  if (ermak) {
+    sl = sweep(false, c->tune_us);
+    nl = sl < 0 ? -1 : sweep(true, nullptr);
+  } else {
+    nl = sweep(true, c->tune_us);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (ermak)
-    c->K.scan_lanes = best_l;
-  else
-    c->K.near_lanes = best_l;
+  if (sl < 0 || nl < 0) return cuda_fail(c, cudaGetLastError(), "autotune timing");
+  if (ermak) c->K.scan_lanes = sl;
+  c->K.near_lanes = nl;
   return finish(c);
 }
 
