@@ -23,6 +23,7 @@
 using namespace dml;
 
 constexpr int kScanMappings = 6;  // lanes per list row tried by the force-scan autotuner
+constexpr double kThreadRowCand = 64.0;  // list build: one thread per row below this
 
 struct dml_ctx {
   dml_params P;
@@ -806,6 +807,18 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   d.n_cch = n_cch;
   d.any_cells = any_cells;
   d.any_verlet = any_verlet;
+  // List build mapping per replica: one thread per row where the 27 cells
+  // around an atom hold few candidates (below kThreadRowCand on average at
+  // loading), a warp per row elsewhere.  Both give the same rows.
+  d.any_list_thread = 0;
+  d.any_list_warp = 0;
+  for (int r = 0; r < nrep; ++r) {
+    RepConst& R = c->rc[r];
+    const double cells = (double)R.ncells[0] * R.ncells[1] * R.ncells[2];
+    const double cand = 27.0 * atoms[r].n / cells;
+    R.list_thread = cand <= kThreadRowCand ? 1 : 0;
+    if (R.list_thread) d.any_list_thread = 1; else d.any_list_warp = 1;
+  }
   const int cap = total;
   c->K.cand_cap = (int)std::min<long long>(16LL * cap, 1LL << 30);  // writes are bounded by it
   int rc = 0;

@@ -51,6 +51,7 @@ struct RepConst {
   int ncells[3];
   int head_dim[3];          // ncells + 2
   int use_cells;
+  int list_thread;          // list build one thread per row (sparse cells), else a warp
   int cell_off, ncell;      // this replica's cells [cell_off, cell_off + ncell), then
                             // one sentinel cell (always empty) whose start is the end
   int cch0;                 // its first chunk of kCellChunk cells (per-cell kernels)
@@ -300,6 +301,7 @@ struct Dev {
   int max_rep_cap;    // largest replica capacity
   int gcmc_rows;      // most cell rows (z layer, y row) of a replica with cells
   int any_cells, any_verlet;  // some replica uses linked cells / the all-pairs build
+  int any_list_thread, any_list_warp;  // the mappings of the cell list builds in use
 };
 
 // Compact per-atom input of dml_set_atoms_batch on the device: the replicas'

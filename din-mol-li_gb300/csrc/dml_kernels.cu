@@ -2000,7 +2000,7 @@ __device__ __forceinline__ void list_cells_row(const Dev& d, const KParams& p, i
   const int rep = d.rep_of[r];
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
-  if (!sc->rebuild || !R.use_cells) return;
+  if (!sc->rebuild || !R.use_cells || R.list_thread) return;
   if (r - R.base >= sc->n_rank) return;
   int h = d.ref[r];
   if (h < 0) return;
@@ -2087,6 +2087,97 @@ __device__ __forceinline__ void list_cells_row(const Dev& d, const KParams& p, i
     }
     d.nn[h] = cnt;
     atomicMax(&sc->max_nn, cnt);
+  }
+}
+
+// The same rows, one thread per row, for replicas whose cells hold few
+// atoms (RepConst::list_thread): a warp per row there spends most of its
+// instructions on the 27-cell set-up of a handful of candidates.  The
+// thread walks the 27 stencil cells in map order and each cell in chain
+// order, with the warp version's inclusion test, so the rows are the same.
+// Returns the row length (or -1 when the thread had no row).
+__device__ __forceinline__ int list_cells_row_thread(const Dev& d, const KParams& p, int r,
+                                                     int rep) {
+  const RepConst& R = d.rc[rep];
+  Scalars* sc = d.sc + rep;
+  if (!sc->rebuild || !R.use_cells || !R.list_thread) return -1;
+  if (r - R.base >= sc->n_rank) return -1;
+  const int h = d.ref[r];
+  if (h < 0) return -1;
+  const double4 P = d.pos[h];
+  const float4 Pf = d.posf[h];
+  int rc[3];
+  cell_index3(R, Pf, d.pos + h, rc[0], rc[1], rc[2]);
+  if (rc[0] == INT_MIN || rc[1] == INT_MIN || rc[2] == INT_MIN) {
+    raise_error(d.g, DML_E_OUT_OF_TESSELLATION, h);
+    return -1;
+  }
+  // the wrapped cell coordinate of offsets -1, 0, +1 along each axis
+  // (cell_pbc), held in registers and selected per stencil cell
+  int wm[3], w0[3], wp[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    wm[k] = (rc[k] - 2 + R.ncells[k]) % R.ncells[k] + 1;
+    w0[k] = (rc[k] - 1 + R.ncells[k]) % R.ncells[k] + 1;
+    wp[k] = (rc[k] + R.ncells[k]) % R.ncells[k] + 1;
+    if (min(wm[k], min(w0[k], wp[k])) < 0 || max(wm[k], max(w0[k], wp[k])) > R.ncells[k] + 1) {
+      raise_error(d.g, DML_E_OUT_OF_TESSELLATION, h);
+      return -1;
+    }
+  }
+  int* row = d.list + (size_t)h * p.mnb;
+  int cnt = 0;
+#pragma unroll 1
+  for (int q = 0; q < 27; ++q) {
+    int nc[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int o = map_off(q, k);
+      nc[k] = o < 0 ? wm[k] : (o == 0 ? w0[k] : wp[k]);
+    }
+    const int c = R.cell_off + (nc[2] * R.head_dim[1] + nc[1]) * R.head_dim[0] + nc[0];
+    const int en = d.cell_start[c + 1];
+#pragma unroll 1
+    for (int i = d.cell_start[c]; i < en; ++i) {
+      const int j = d.cell_atoms[i];  // hs slot
+      if (j == h) continue;
+      const float4 Q = d.posf[j];
+      float fx, fy, fz;
+      vdist_nint_f(R, Q, Pf, fx, fy, fz);
+      const float drf = fx * fx + fy * fy + fz * fz;
+      bool inc = false;
+      if (drf < R.rlist_lo2) {
+        inc = true;
+      } else if (drf <= R.rlist_hi2) {
+        double vx, vy, vz;
+        vdist_nint(R, d.pos[j], P, vx, vy, vz);
+        inc = dot3(vx, vy, vz) < p.rlist2;
+      }
+      if (inc) {
+        if (cnt < p.mnb) row[cnt] = j;
+        ++cnt;
+      }
+    }
+  }
+  if (cnt > p.mnb) {
+    raise_error(d.g, DML_E_NEIGH_OVERFLOW, h);
+    cnt = p.mnb;
+  }
+  d.nn[h] = cnt;
+  return cnt;
+}
+
+__global__ void __launch_bounds__(256) list_cells_thread_kernel(Dev d, KParams p) {
+  const int total = d.reb_pre[d.nrep];  // rows of the replicas that rebuild
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int r = row_rank_in(d, d.reb_pre, i);
+    const int rep = d.rep_of[r];
+    const int cnt = list_cells_row_thread(d, p, r, rep);
+    // the longest row per replica: one atomic per replica present in the warp
+    const unsigned act = __activemask();
+    const unsigned grp = __match_any_sync(act, rep);
+    const int m = __reduce_max_sync(grp, cnt > 0 ? cnt : 0);
+    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1 && m > 0) atomicMax(&d.sc[rep].max_nn, m);
   }
 }
 
@@ -2658,14 +2749,16 @@ __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
   }
 }
 
-// maxz (dana.F90:776-794)
-__device__ __forceinline__ void piston_at(Dev d, KParams p, int n_slots, int rep, int pos) {
+// maxz (dana.F90:776-794).  lohi is formed once per block (an FP64 divide
+// issues on the narrow FP64 pipe; every thread forming it cost more than
+// the compression itself).
+__device__ __forceinline__ void piston_at(Dev d, KParams p, int n_slots, int rep, int pos,
+                                          double lohi) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
   const int s = pos;
   double z0 = sc->z0;
-  double lohi = (p.h_over_tau * ((sc->rho0 - sc->rho) / sc->rho));
   if (s < n_slots && d.state[s] == ST_LIVE) {
     double4 P = d.pos[s];
     if (P.z > z0) {
@@ -2684,8 +2777,15 @@ __device__ __forceinline__ void piston_at(Dev d, KParams p, int n_slots, int rep
 
 __global__ void piston_kernel(Dev d, KParams p, int n_slots) {
   const int rep = block_rep(d);
+  __shared__ double s_lohi;
+  if (threadIdx.x == 0) {
+    const Scalars* sc = d.sc + rep;
+    s_lohi = (p.h_over_tau * ((sc->rho0 - sc->rho) / sc->rho));
+  }
+  __syncthreads();
+  const double lohi = s_lohi;
 #pragma unroll
-  for (int u = 0; u < kSlotU; ++u) piston_at(d, p, n_slots, rep, span_pos(u));
+  for (int u = 0; u < kSlotU; ++u) piston_at(d, p, n_slots, rep, span_pos(u), lohi);
 }
 
 
@@ -5328,8 +5428,16 @@ int k_rebuild(const Dev& d, const KParams& p, int n_slots, int n_b, int n_rank, 
     cell_scatter_kernel<<<nspan(n_b), kBlock, 0, s>>>(d, n_b, 0);
     cell_order_reb_kernel<<<152 * 8, kBlock, 0, s>>>(d);
     cell_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d, 0);
-    list_cells_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, n_rank);
-    n += 7;
+    n += 6;
+    if (d.any_list_warp) {
+      list_cells_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, n_rank);
+      n += 1;
+    }
+    if (d.any_list_thread) {
+      list_cells_thread_kernel<<<nblk(n_rank) < kRowGrid ? nblk(n_rank) : kRowGrid, kBlock, 0,
+                                 s>>>(d, p);
+      n += 1;
+    }
   }
   if (d.any_verlet) {
     list_verlet_kernel<<<nblk_rows(n_rank), kBlock, 0, s>>>(d, p, n_rank, n_b);
