@@ -3069,7 +3069,11 @@ __device__ __forceinline__ bool in_slab(double z, double z0, double zmax) {
 }
 
 // gcmc_run's preparation, one block per replica: the order arrays grow by
-// appends and are compacted before they could overflow; the listing of
+// appends (insertions) and gain holes (deletions, captures); they are
+// compacted, order kept, before they could overflow and whenever holes make
+// up an eighth of them (every per-rank kernel walks the holes too: without
+// this, config 5's hs%ref order doubles in length within a few hundred
+// steps, and so does the time of those kernels); the listing of
 // gcmc_bin_kernel starts empty, the member bounds at their identities, and
 // the bit words past the used gcmc%alist positions (appends set bits there)
 // are cleared.
@@ -3080,17 +3084,17 @@ __global__ void gcmc_prep_kernel(Dev d, KParams p, int par) {
   const int B = R.base, tid = threadIdx.x, nt = blockDim.x;
   if (tid == 0) d.pr_cnt[rep * kCntStride + kCntGlist] = 0;
   if (!sc->listed) return;  // gcmc_kernel reports the state error
-  if (sc->n_rank + p.nadj >= R.cap) {
+  if (sc->n_rank + p.nadj >= R.cap || 8 * (sc->n_rank - sc->n_ref) > sc->n_rank) {
     int n = blk_compact(d.ref, B, sc->n_rank, d.rank);
     if (tid == 0) sc->n_rank = n;
     __syncthreads();
   }
-  if (sc->n_alist + p.nadj >= R.cap) {
+  if (sc->n_alist + p.nadj >= R.cap || 8 * (sc->n_alist - sc->n_atoms) > sc->n_alist) {
     int n = blk_compact(d.alist, B, sc->n_alist, d.apos);
     if (tid == 0) sc->n_alist = n;
     __syncthreads();
   }
-  if (sc->n_gorder + p.nadj >= R.cap) {
+  if (sc->n_gorder + p.nadj >= R.cap || 8 * (sc->n_gorder - sc->n_gcmc) > sc->n_gorder) {
     int n = blk_compact(d.gorder, B, sc->n_gorder, d.gpos);
     if (tid == 0) sc->n_gorder = n;
     __syncthreads();
