@@ -24,6 +24,7 @@ using namespace dml;
 
 constexpr int kScanMappings = 6;  // lanes per list row tried by the force-scan autotuner
 constexpr double kThreadRowCand = 64.0;  // list build: one thread per row below this
+constexpr int kCellFactors = 6;  // cell edge bounds tried by dml_tune_cells: 1.0, 1.1, .. 1.5
 
 struct dml_ctx {
   dml_params P;
@@ -46,6 +47,8 @@ struct dml_ctx {
   int launches_per_step = 0;    // kernels of a step without a list rebuild
   int launches_per_rebuild = 0; // extra kernels when the list is rebuilt
   float tune_us[kScanMappings] = {};  // force-scan time per mapping (1, 2, 4, 8, 16, 32 lanes per row)
+  double cell_factor = 1.0;           // chosen form: cell edge bound / (rc + skin)
+  float cell_us[kCellFactors] = {};   // dml_tune_cells: time per step of each factor
   void* flush_buf = nullptr;
   std::string last_error;
   void* h_stage = nullptr;   // pinned staging of atom downloads, grown on demand
@@ -90,7 +93,9 @@ double pow6h(double x) {
 
 // Per-replica constants: box, cells (cgroup_tessellate, Cells.F90:227-242:
 // ncells = int(box/(rc+skin)), cells off when all three are below 4).
-void make_repconst(const dml_params& P, const dml_replica& r, RepConst& R) {
+// `edge`: the cell edge bound in units of rc + skin (1 as the reference;
+// the chosen form's cell tuning takes larger cells, see dml_set_cell_factor).
+void make_repconst(const dml_params& P, const dml_replica& r, RepConst& R, double edge = 1.0) {
   std::memset(&R, 0, sizeof R);
   for (int k = 0; k < 3; ++k) {
     R.box[k] = r.box[k];
@@ -102,6 +107,13 @@ void make_repconst(const dml_params& P, const dml_replica& r, RepConst& R) {
   double rcut_b = P.rc + P.skin;
   for (int k = 0; k < 3; ++k) R.ncells[k] = (int)(r.box[k] / rcut_b);
   R.use_cells = !(R.ncells[0] < 4 && R.ncells[1] < 4 && R.ncells[2] < 4);
+  if (edge > 1.0 && R.use_cells)
+    for (int k = 0; k < 3; ++k) {
+      // larger cells, but never fewer than 3 along an axis that had 3 (no
+      // stencil duplicates that the reference grid lacks)
+      const int n = (int)(r.box[k] / (rcut_b * edge));
+      R.ncells[k] = std::max(std::min(3, R.ncells[k]), n);
+    }
   for (int k = 0; k < 3; ++k) {
     if (R.ncells[k] < 1) R.ncells[k] = 1;
     R.cell[k] = r.box[k] / (double)R.ncells[k];
@@ -1434,6 +1446,104 @@ int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phas
   }
   for (auto& e : ev) cudaEventDestroy(e);
   return finish(c);
+}
+
+// The chosen form's cells (no counterpart in the reference, whose cells
+// are int(box / (rc + skin)) per axis): cells with an edge bound of
+// factor * (rc + skin).  The lists hold the same atoms in another order (the
+// 27-cell stencil still covers rc + skin), which the order-independent
+// fixed-point sums do not see; overlap_moveback's examination order and
+// gcmc_run's own-list order follow the list, so trajectories differ from
+// factor 1 the way two seeds do.  Every list is rebuilt at the next
+// test_update.  Cells are allocated for factor 1, so any factor >= 1 fits.
+int dml_set_cell_factor(dml_ctx* c, double factor) {
+  if (!c || !(factor >= 1.0 && factor <= 2.0)) return DML_E_ARG;
+  if (!c->loaded) return DML_E_STATE;
+  if (c->P.precision != DML_PRECISION_MIXED || c->P.reservoir == DML_RESERVOIR_CHUNKS)
+    return DML_E_UNSUPPORTED;
+  CK(cudaStreamSynchronize(c->stream));
+  int rc = read_scalars(c);
+  if (rc) return rc;
+  Dev& d = c->D;
+  int any_thread = 0, any_warp = 0;
+  for (int r = 0; r < d.nrep; ++r) {
+    RepConst& R = c->rc[r];
+    RepConst T;
+    make_repconst(c->P, c->reps[r], T, factor);
+    if (!T.use_cells || !R.use_cells) continue;  // the all-pairs build keeps its path
+    // the grid of the new factor; placement, capacity and margins stay
+    for (int k = 0; k < 3; ++k) {
+      R.ncells[k] = T.ncells[k];
+      R.cell[k] = T.cell[k];
+      R.inv_cellf[k] = T.inv_cellf[k];
+      R.cellf[k] = T.cellf[k];
+      R.head_dim[k] = T.head_dim[k];
+    }
+    R.ncell = T.ncell;
+    R.tess_hif = T.tess_hif;
+    R.gl_all = T.gl_all;
+    R.gl_mask = T.gl_mask;
+    R.gl_cmask = T.gl_cmask;
+    const double cells = (double)R.ncells[0] * R.ncells[1] * R.ncells[2];
+    R.list_thread = 27.0 * c->h_sc[r].n_b / cells <= kThreadRowCand ? 1 : 0;
+    c->h_sc[r].listed = 0;
+  }
+  for (int r = 0; r < d.nrep; ++r) {
+    if (!c->rc[r].use_cells) continue;
+    if (c->rc[r].list_thread) any_thread = 1; else any_warp = 1;
+  }
+  if (any_thread != d.any_list_thread || any_warp != d.any_list_warp) {
+    // the step graph launches the list builds in use: capture it again
+    d.any_list_thread |= any_thread;
+    d.any_list_warp |= any_warp;
+    if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
+    if (c->multi_graph) cudaGraphExecDestroy(c->multi_graph);
+    c->step_graph = nullptr;
+    c->multi_graph = nullptr;
+  }
+  CK(cudaMemcpyAsync(d.rc, c->rc.data(), sizeof(RepConst) * d.nrep, cudaMemcpyHostToDevice,
+                     c->stream));
+  rc = write_scalars(c);
+  if (rc) return rc;
+  c->cell_factor = factor;
+  return 0;
+}
+
+// Tries the cell factors 1.0, 1.1, .. 1.5: after each one's rebuild step,
+// `steps` steps are timed, and the fastest factor is kept (its lists are
+// rebuilt once more).  The run advances by kCellFactors * (steps + 1) + 1
+// steps.
+int dml_tune_cells(dml_ctx* c, int32_t steps, double* best) {
+  if (!c || steps < 1) return DML_E_ARG;
+  if (!c->loaded || !c->setup_done) return DML_E_STATE;
+  double best_f = 1.0;
+  float best_t = 1e30f;
+  for (int v = 0; v < kCellFactors; ++v) {
+    const double f = 1.0 + 0.1 * v;
+    int rc = dml_set_cell_factor(c, f);
+    if (rc) return rc;
+    if ((rc = dml_step(c, 1)) != 0) return rc;  // the rebuild
+    double ms = 0.0;
+    if ((rc = dml_time_run(c, steps, &ms)) != 0) return rc;
+    c->cell_us[v] = (float)(1e3 * ms / steps);
+    if (c->cell_us[v] < best_t) {
+      best_t = c->cell_us[v];
+      best_f = f;
+    }
+  }
+  int rc = dml_set_cell_factor(c, best_f);
+  if (rc) return rc;
+  if ((rc = dml_step(c, 1)) != 0) return rc;
+  if (best) *best = best_f;
+  return 0;
+}
+
+int dml_get_cell_tuning(dml_ctx* c, double* factor, float* us) {
+  if (!c) return DML_E_ARG;
+  if (factor) *factor = c->cell_factor;
+  if (us)
+    for (int v = 0; v < kCellFactors; ++v) us[v] = c->cell_us[v];
+  return 0;
 }
 
 int dml_get_tuning(dml_ctx* c, int32_t* scan_lanes, float* scan_us) {

@@ -295,6 +295,17 @@ __device__ __forceinline__ int span_pos(int u) {
   return blockIdx.x * kSpan + u * kBlock + (int)threadIdx.x;
 }
 
+// The per-atom kernels whose result does not depend on the order of
+// hs%ref (the integrators, ermak_b, the force scan, the capture commit and
+// overlap_moveback's member count) walk hs slots instead of ranks: a slot
+// belongs to hs%ref exactly when its rank is set.  Ranks follow the
+// reference's attachment order, which GCMC insertions (appended, into the
+// first free slots) decorrelate from slot order; slot order keeps the
+// per-atom loads coalesced as the run goes on.
+__device__ __forceinline__ int ref_slot(const Dev& d, int s, int end) {
+  return s < end && d.rank[s] >= 0 ? s : -1;
+}
+
 __device__ __forceinline__ int warp_id_global() {
   return (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 }
@@ -587,12 +598,12 @@ __device__ __forceinline__ unsigned ermak_a_at(const Dev& d, const KParams& p, i
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock, MIXED ? 4 : 3) ermak_a_kernel(Dev d, KParams p, int n_rank) {
   const int rep = block_rep(d);
-  const int end = d.rc[rep].base + d.sc[rep].n_rank;
+  const int end = d.rc[rep].base + d.sc[rep].n_slots;
   if ((int)blockIdx.x * kSpan >= end) return;
-  int h0 = span_pos(0) < end ? d.ref[span_pos(0)] : -1;
-  int h1 = span_pos(1) < end ? d.ref[span_pos(1)] : -1;
-  int h2 = span_pos(2) < end ? d.ref[span_pos(2)] : -1;
-  int h3 = span_pos(3) < end ? d.ref[span_pos(3)] : -1;
+  int h0 = ref_slot(d, span_pos(0), end);
+  int h1 = ref_slot(d, span_pos(1), end);
+  int h2 = ref_slot(d, span_pos(2), end);
+  int h3 = ref_slot(d, span_pos(3), end);
   const long long step = d.g->step;
   const double zmax = d.sc[rep].zmax;
   const float zmaxf = (float)zmax;
@@ -704,12 +715,12 @@ __device__ __forceinline__ unsigned brownian_at(const Dev& d, const KParams& p, 
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock, 4) brownian_kernel(Dev d, KParams p, int n_rank) {
   const int rep = block_rep(d);
-  const int end = d.rc[rep].base + d.sc[rep].n_rank;
+  const int end = d.rc[rep].base + d.sc[rep].n_slots;
   if ((int)blockIdx.x * kSpan >= end) return;
-  int h0 = span_pos(0) < end ? d.ref[span_pos(0)] : -1;
-  int h1 = span_pos(1) < end ? d.ref[span_pos(1)] : -1;
-  int h2 = span_pos(2) < end ? d.ref[span_pos(2)] : -1;
-  int h3 = span_pos(3) < end ? d.ref[span_pos(3)] : -1;
+  int h0 = ref_slot(d, span_pos(0), end);
+  int h1 = ref_slot(d, span_pos(1), end);
+  int h2 = ref_slot(d, span_pos(2), end);
+  int h3 = ref_slot(d, span_pos(3), end);
   static_assert(kSlotU == 4, "four hs%ref entries per thread");
   const long long step = d.g->step;
   const double zmax = d.sc[rep].zmax;
@@ -876,18 +887,18 @@ __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p) {
   }
 }
 
-// One lane per row: the rank positions of the replica's span, four per
-// thread, their hs%ref entries, positions and list lengths loaded up front.
+// One lane per row: the hs slots of the replica's span, four per thread,
+// their membership, positions and list lengths loaded up front.
 template <bool NEAR>
 __global__ void __launch_bounds__(kBlock) force_scan_span_kernel(Dev d, KParams p) {
   const int rep = block_rep(d);
-  const int end = d.rc[rep].base + d.sc[rep].n_rank;
+  const int end = d.rc[rep].base + d.sc[rep].n_slots;
   if ((int)blockIdx.x * kSpan >= end) return;  // whole block: warps stay full
   static_assert(kSlotU == 4, "four rows per thread");
-  int h0 = span_pos(0) < end ? d.ref[span_pos(0)] : -1;
-  int h1 = span_pos(1) < end ? d.ref[span_pos(1)] : -1;
-  int h2 = span_pos(2) < end ? d.ref[span_pos(2)] : -1;
-  int h3 = span_pos(3) < end ? d.ref[span_pos(3)] : -1;
+  int h0 = ref_slot(d, span_pos(0), end);
+  int h1 = ref_slot(d, span_pos(1), end);
+  int h2 = ref_slot(d, span_pos(2), end);
+  int h3 = ref_slot(d, span_pos(3), end);
   const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
   float4 P0 = h0 >= 0 ? d.posf[h0] : z4, P1 = h1 >= 0 ? d.posf[h1] : z4;
   float4 P2 = h2 >= 0 ? d.posf[h2] : z4, P3 = h3 >= 0 ? d.posf[h3] : z4;
@@ -896,7 +907,8 @@ __global__ void __launch_bounds__(kBlock) force_scan_span_kernel(Dev d, KParams 
   // one copy of the row body, the rows rotated through registers
 #pragma unroll 1
   for (int u = 0; u < kSlotU; ++u) {
-    force_scan_row<NEAR, 1>(d, p, rep, span_pos(u), h0, P0, n0);
+    // the row's rank keys the reference's summation order of its entries
+    force_scan_row<NEAR, 1>(d, p, rep, h0 >= 0 ? d.rank[h0] : 0, h0, P0, n0);
     h0 = h1; h1 = h2; h2 = h3;
     P0 = P1; P1 = P2; P2 = P3;
     n0 = n1; n1 = n2; n2 = n3;
@@ -1203,9 +1215,8 @@ __global__ void force_touched_kernel(Dev d, KParams p) {
 }
 
 template <bool FUSE_B>
-__device__ __forceinline__ void force_ref_at(const Dev& d, const KParams& p, int rep, int r) {
-  if (r - d.rc[rep].base >= d.sc[rep].n_rank) return;
-  const int h = d.ref[r];
+__device__ __forceinline__ void force_ref_at(const Dev& d, const KParams& p, int rep, int s) {
+  const int h = ref_slot(d, s, d.rc[rep].base + d.sc[rep].n_slots);
   if (h < 0) return;
   const unsigned bit = 1u << (h & 31);
   if (d.ftouch[h >> 5] & bit) {  // summed by force_touched_kernel
@@ -1224,7 +1235,7 @@ __global__ void force_ref_kernel(Dev d, KParams p) {
     d.g->n_cand = 0;
     d.g->n_ftouch = 0;
   }
-  if ((int)blockIdx.x * kSpan >= d.rc[rep].base + d.sc[rep].n_rank) return;
+  if ((int)blockIdx.x * kSpan >= d.rc[rep].base + d.sc[rep].n_slots) return;
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) force_ref_at<FUSE_B>(d, p, rep, span_pos(u));
 }
@@ -2401,15 +2412,16 @@ __global__ void __launch_bounds__(256) overlap_detect_kernel(Dev d, KParams p, i
 // and can never be moved; the others are counted per component root and
 // listed (act_list) for the component passes.  Every lane calls it.
 __device__ __forceinline__ void overlap_count_at(Dev d, int n_rank, int rep, int pos) {
-  const int r = pos;
   const int lane = threadIdx.x & 31;
-  int h = -1;
+  const int h = ref_slot(d, pos, d.rc[rep].base + d.sc[rep].n_slots);
   bool act = false;
-  if (r - d.rc[rep].base < d.sc[rep].n_rank) {
-    h = d.ref[r];
-    if (h >= 0) {
-      if (d.active[h]) act = true;
-      else d.skip[h] = 1;
+  int r = -1;
+  if (h >= 0) {
+    if (d.active[h]) {
+      act = true;
+      r = d.rank[h];
+    } else {
+      d.skip[h] = 1;
     }
   }
   const unsigned m = __ballot_sync(0xffffffffu, act);
@@ -2666,11 +2678,10 @@ __global__ void overlap_passn_kernel(Dev d, KParams p) {
 __device__ __forceinline__ void commit_at(Dev d, int n_rank, int rep, int pos) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
-  const int r = pos;
-  if (r - R.base >= sc->n_rank) return;
-  int h = d.ref[r];
+  const int h = ref_slot(d, pos, R.base + sc->n_slots);
   if (h < 0) return;
   if (d.typ[h] != DML_Z_F) return;
+  const int r = d.rank[h];
   d.typ[h] = DML_Z_CG;
   float4 f = d.posf[h];
   f.w = __int_as_float(DML_Z_CG);

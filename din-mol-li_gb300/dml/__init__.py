@@ -85,6 +85,9 @@ def lib():
     L.dml_time_run.argtypes = [vp, i64, P(ctypes.c_double)]
     L.dml_set_graph_steps.argtypes = [vp, i32]
     L.dml_set_chunk.argtypes = [vp, i32, vp, vp, ctypes.c_double]
+    L.dml_set_cell_factor.argtypes = [vp, ctypes.c_double]
+    L.dml_tune_cells.argtypes = [vp, i32, P(ctypes.c_double)]
+    L.dml_get_cell_tuning.argtypes = [vp, P(ctypes.c_double), vp]
     L.dml_bloques.argtypes = [vp]
     L.dml_profile_steps.argtypes = [vp, i64, i32, vp, i32]
     L.dml_launches_per_step.argtypes = [vp, P(i32)]
@@ -362,6 +365,24 @@ class Simulation:
         z = np.ascontiguousarray(z, np.int32)
         self._check(self.lib.dml_set_chunk(self.h, len(z), pos.ctypes.data, z.ctypes.data,
                                            float(dist)), "dml_set_chunk")
+
+    def set_cell_factor(self, f):
+        """Chosen form: cells of edge bound f * (rc + skin) (lists rebuilt)."""
+        self._check(self.lib.dml_set_cell_factor(self.h, float(f)), "dml_set_cell_factor")
+
+    def tune_cells(self, steps=10):
+        """Chosen form: time the cell factors 1.0 .. 1.5 and keep the fastest."""
+        b = ctypes.c_double()
+        self._check(self.lib.dml_tune_cells(self.h, steps, ctypes.byref(b)), "dml_tune_cells")
+        return b.value
+
+    def cell_tuning(self):
+        f = ctypes.c_double()
+        us = np.zeros(6, np.float32)
+        self._check(self.lib.dml_get_cell_tuning(self.h, ctypes.byref(f), us.ctypes.data),
+                    "dml_get_cell_tuning")
+        return {"factor": f.value,
+                "us_per_step": {"%.1f" % (1.0 + 0.1 * v): float(us[v]) for v in range(6)}}
 
     def bloques(self):
         self._check(self.lib.dml_bloques(self.h), "dml_bloques")

@@ -328,6 +328,22 @@ int dml_get_counters(dml_ctx* c, dml_counters* out);
  * measured time of each mapping in microseconds (scan_us[6], in that order,
  * zero before tuning).  Either pointer may be NULL. */
 int dml_get_tuning(dml_ctx* c, int32_t* scan_lanes, float* scan_us);
+
+/* Cell size of the chosen form (no counterpart in the reference, whose
+ * cells are int(box / (rc + skin)) per axis; DML_PRECISION_MIXED only, not
+ * with the chunk reservoir, after dml_set_atoms).  dml_set_cell_factor takes
+ * cells with an edge bound of factor * (rc + skin), factor in [1, 2] (never
+ * fewer than 3 cells along an axis that had 3): the lists hold the same
+ * atoms in another order, which the fixed-point force sums do not see, and
+ * every list is rebuilt at the next test_update.  dml_tune_cells times
+ * `steps` steps with each factor 1.0, 1.1, .. 1.5 (after its rebuild step)
+ * and keeps the fastest, *best (may be NULL); the run advances by
+ * 6 * (steps + 1) + 1 steps.  dml_get_cell_tuning reports the factor in use
+ * and the microseconds per step of each factor tried (us[6], zero if not
+ * tuned).  Either pointer may be NULL. */
+int dml_set_cell_factor(dml_ctx* c, double factor);
+int dml_tune_cells(dml_ctx* c, int32_t steps, double* best);
+int dml_get_cell_tuning(dml_ctx* c, double* factor, float* us);
 int dml_get_counters_replica(dml_ctx* c, int32_t rep, dml_counters* out);
 
 /* Diagnostic (no counterpart in the reference): how many gcmc_run calls of

@@ -103,3 +103,63 @@ def test_device_conversions_match_ieee():
     wb = f32.astype(np.float64)
     assert np.array_equal(np.isnan(back), nan)
     assert np.array_equal(back[~nan].view(np.uint64), wb[~nan].view(np.uint64))
+
+
+def _sorted_rows(nn, lst):
+    return [np.sort(lst[k, : nn[k]]) for k in range(len(nn))]
+
+
+@pytest.mark.parametrize("factor", [1.2, 1.5])
+def test_cell_factor_keeps_list_sets_and_forces(factor):
+    """The chosen form's larger cells: after the rebuild each row holds the
+    same atoms as with the reference grid (in another order), and the
+    fixed-point forces at those positions are the same bits."""
+    import copy
+
+    p = systems.c5_small_params(nadj=32)
+    p.precision = dml.PRECISION_MIXED
+    p.skin = 2.0
+    atoms = systems.c1_atoms(seed=21, dmin=2.2, n_ion=300)
+    sims = []
+    for f in (1.0, factor):
+        g = dml.Simulation(copy.copy(p))
+        g.set_atoms(atoms)
+        g.setup()
+        if f != 1.0:
+            g.set_cell_factor(f)
+        assert g.test_update() == (1 if f != 1.0 else 0)
+        g.fuerza()
+        sims.append(g)
+    (n1, l1), (n2, l2) = [g.get_neighbors(p.mnb) for g in sims]
+    assert np.array_equal(n1, n2)
+    for a, b in zip(_sorted_rows(n1, l1), _sorted_rows(n2, l2)):
+        assert np.array_equal(a, b)
+    a, b = sims[0].get_atoms(), sims[1].get_atoms()
+    assert np.array_equal(a["force"].view(np.uint64), b["force"].view(np.uint64))
+    assert np.abs(a["force"]).max() > 0
+    sims[1].step(60)  # GCMC and rebuilds on the coarser grid
+    for g in sims:
+        g.close()
+
+
+def test_cell_tuning_picks_a_factor():
+    p, reps, atoms = systems.c4_batch(n_rep=24, seed=5)
+    g = dml.Simulation(p, replicas=reps)
+    g.set_atoms(atoms)
+    g.setup()
+    best = g.tune_cells(steps=3)
+    t = g.cell_tuning()
+    assert 1.0 <= best <= 1.5 and t["factor"] == best
+    assert all(v > 0 for v in t["us_per_step"].values())
+    g.step(10)
+    g.close()
+
+
+def test_cell_factor_refused_for_the_plain_form():
+    p = systems.c1_params()
+    g = dml.Simulation(p)
+    g.set_atoms(systems.c1_atoms())
+    with pytest.raises(dml.DmlError) as e:
+        g.set_cell_factor(1.3)
+    assert e.value.code == dml.E_UNSUPPORTED
+    g.close()
