@@ -137,9 +137,18 @@ def test_cell_factor_keeps_list_sets_and_forces(factor):
     a, b = sims[0].get_atoms(), sims[1].get_atoms()
     assert np.array_equal(a["force"].view(np.uint64), b["force"].view(np.uint64))
     assert np.abs(a["force"]).max() > 0
-    sims[1].step(60)  # GCMC and rebuilds on the coarser grid
     for g in sims:
         g.close()
+    # GCMC steps and rebuilds on the coarser grid (ions start rc apart: closer
+    # ones would be moved back forever without a piston, as in the reference)
+    g = dml.Simulation(copy.copy(p))
+    g.set_atoms(systems.c1_atoms(seed=22, dmin=3.2))
+    g.setup()
+    g.set_cell_factor(factor)
+    g.step(60)
+    c = g.counters()
+    assert c["nupd"] >= 2 and c["gcmc_ins"] > 0
+    g.close()
 
 
 def test_cell_tuning_picks_a_factor():
