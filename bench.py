@@ -726,13 +726,22 @@ def run_gpu(args, ws, rank, local):
     prec = dml.PRECISION_MIXED if form == "chosen" else dml.PRECISION_FP64
     clocks = Clocks(local)
 
-    # Main arm: the whole workload in one context.  The chosen form's cell
-    # size is picked by the autotuner (edge bound 1.0 .. 1.5 x (rc + skin),
-    # timed over 10 steps each) before the warm-up.
+    # The chosen form's cell size is picked by the autotuner (edge bound
+    # 1.0 .. 1.5 x (rc + skin), timed over 10 steps each) on a context of its
+    # own, so that the measured run starts from the same state as the others.
+    cell_tuning = None
+    if form == "chosen" and wl.batched:
+        tune = wl.open(prec)
+        tune.setup()
+        tune.tune_cells(steps=10)
+        cell_tuning = tune.cell_tuning()
+        tune.close()
+
+    # Main arm: the whole workload in one context.
     sim = wl.open(prec)
     sim.setup()
-    if form == "chosen" and wl.batched:
-        sim.tune_cells(steps=10)
+    if cell_tuning and cell_tuning["factor"] != 1.0:
+        sim.set_cell_factor(cell_tuning["factor"])
     dist.barrier()
     ms, c0, c1, clk = timed_steps(sim, args, clocks)
     dist.barrier()
@@ -745,8 +754,8 @@ def run_gpu(args, ws, rank, local):
     value_flushed, _ = job_value(dist, 0.5 * (f0["n_ref"] + f1["n_ref"]), args.steps, ms_f)
     per_step, per_rebuild = sim.launches_per_step()
     tuning = sim.tuning()
-    if form == "chosen" and wl.batched:
-        tuning["cells"] = sim.cell_tuning()
+    if cell_tuning:
+        tuning["cells"] = cell_tuning
     launches = per_step * args.steps + per_rebuild * (c1["list_builds"] - c0["list_builds"])
     roofline = roofline_of(sim, wl, max(3, min(args.steps, 10)))
     counters = {k: c1[k] - c0[k] for k in ("choques", "depo", "try_", "choques3", "gcmc_ins",
@@ -794,8 +803,8 @@ def run_gpu(args, ws, rank, local):
         t0 = time.perf_counter()
         s2 = wl.open(prec)
         s2.setup()
-        if form == "chosen" and wl.batched:  # the cell size the tuner picked
-            s2.set_cell_factor(tuning["cells"]["factor"])
+        if cell_tuning and cell_tuning["factor"] != 1.0:  # the cell size the tuner picked
+            s2.set_cell_factor(cell_tuning["factor"])
         done, d2h = 0, 0
         while done < args.steps:
             k = min(NWR, args.steps - done)
