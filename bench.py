@@ -74,7 +74,7 @@ PHASE_KERNEL = {"integrate": ("ermak_a_kernel", "ion", 120.0),
                 "force_pairs": ("force_scan_span_kernel + force_exact_mixed_kernel", "ion", 24.0),
                 "force_sum": ("force_touched_kernel + force_ref_kernel", "ion", 105.0),
                 "test_update1": ("pbc_dispmax_kernel + dispmax_exact_kernel", "ion", 48.0),
-                "overlap": ("overlap_* (6 kernels)", "ion", 48.0),
+                "overlap": ("overlap_count_kernel + overlap_comp_kernel", "ion", 48.0),
                 "test_update2": ("pbc_dispmax_kernel + dispmax_exact_kernel", "ion", 48.0),
                 "commit": ("commit_kernel", "ion", 1.0),
                 "gcmc_cells": ("gcmc_prep_kernel + gcmc_bin_kernel", "slot", 32.0),

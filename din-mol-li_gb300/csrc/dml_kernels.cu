@@ -2479,45 +2479,8 @@ __device__ __forceinline__ void overlap_assign_at(const Dev& d, int end, int i) 
   }
 }
 
-// The listed members are few (atoms with a near contact): one block per
-// replica walks its list segment, instead of a block per 1024 positions.
-__global__ void overlap_assign_kernel(Dev d) {
-  const int rep = blockIdx.x;
-  const int base = d.rc[rep].base;
-  const int end = base + d.pr_cnt[rep * kCntStride + kCntAct];
-  for (int i0 = base; i0 < end; i0 += blockDim.x) overlap_assign_at(d, end, i0 + threadIdx.x);
-}
-
-__global__ void overlap_scatter_kernel(Dev d) {
-  const int rep = blockIdx.x;
-  const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntAct];
-  for (int i = d.rc[rep].base + threadIdx.x; i < end; i += blockDim.x) {
-    const int r = d.act_list[i];
-    const int h = d.ref[r];
-    const int root = d.uf[h];
-    const int cid = d.comp_id[root];
-    const int idx = d.comp_list[2 * cid] + atomicAdd(&d.comp_fill[root], 1);
-    d.comp_rank[idx] = r;  // the component's ranks, in no particular order
-  }
-}
-
-// Members of every component in rank order: each member's place is the
-// number of smaller ranks in its component (contiguous loads, all members
-// in parallel).
-__global__ void overlap_order_kernel(Dev d) {
-  const int rep = blockIdx.x;
-  const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntAct];
-  for (int i = d.rc[rep].base + threadIdx.x; i < end; i += blockDim.x) {
-    const int r = d.act_list[i];
-    const int h = d.ref[r];
-    const int cid = d.comp_id[d.uf[h]];
-    const int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
-    const int* rk = d.comp_rank + off;
-    int before = 0;
-    for (int q = 0; q < sz; ++q) before += rk[q] < r;
-    d.comp_members[off + before] = h;
-  }
-}
+// Members of every component in rank order (overlap_comp_kernel): each
+// member's place is the number of smaller ranks in its component.
 
 // Examination of o1 = x in pass `pass` (dana.F90:871-935).
 __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, int* again) {
@@ -2612,6 +2575,45 @@ __device__ void overlap_pass1_comp(const Dev& d, const KParams& p, int all_passe
   }
   if (sz > 0) atomicMax(&d.sc[d.rep_of[mem[0]]].passes, pass);
   atomicMax(&d.g->passes, pass);
+}
+
+// The bookkeeping of one replica's listed members (component numbers and
+// ranges, members scattered, members in rank order), then, when every pass
+// can run inside a component (prob >= 1), the component passes: one block per
+// replica, the stages separated by block barriers (a component lies inside
+// one replica).  The same work as overlap_assign, _scatter, _order and _pass1
+// in one launch.
+__global__ void overlap_comp_kernel(Dev d, KParams p, int passes) {
+  const int rep = blockIdx.x;
+  const int base = d.rc[rep].base;
+  const int end = base + d.pr_cnt[rep * kCntStride + kCntAct];
+  if (end == base) return;  // no member with a near contact
+  for (int i0 = base; i0 < end; i0 += blockDim.x) overlap_assign_at(d, end, i0 + threadIdx.x);
+  __syncthreads();
+  for (int i = base + threadIdx.x; i < end; i += blockDim.x) {
+    const int h = d.ref[d.act_list[i]];
+    const int root = d.uf[h];
+    const int cid = d.comp_id[root];
+    d.comp_rank[d.comp_list[2 * cid] + atomicAdd(&d.comp_fill[root], 1)] = d.act_list[i];
+  }
+  __syncthreads();
+  for (int i = base + threadIdx.x; i < end; i += blockDim.x) {
+    const int r = d.act_list[i];
+    const int h = d.ref[r];
+    const int cid = d.comp_id[d.uf[h]];
+    const int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
+    const int* rk = d.comp_rank + off;
+    int before = 0;
+    for (int q = 0; q < sz; ++q) before += rk[q] < r;
+    d.comp_members[off + before] = h;
+  }
+  if (!passes) return;
+  __syncthreads();
+  // every component of the replica once: through its root's listed member
+  for (int i = base + threadIdx.x; i < end; i += blockDim.x) {
+    const int h = d.ref[d.act_list[i]];
+    if (d.uf[h] == h) overlap_pass1_comp(d, p, 1, d.comp_id[h]);
+  }
 }
 
 __global__ void overlap_pass1_kernel(Dev d, KParams p, int all_passes) {
@@ -5495,15 +5497,14 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
   }
   if (detect) n += k_overlap_detect(d, p, n_rank, detect == 1 ? 1 : 0, s);
   overlap_count_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
-  overlap_assign_kernel<<<d.nrep, kBlock, 0, s>>>(d);
-  overlap_scatter_kernel<<<d.nrep, kBlock, 0, s>>>(d);
-  overlap_order_kernel<<<d.nrep, kBlock, 0, s>>>(d);
-  int all_passes = p.prob >= 1.0;
-  overlap_pass1_kernel<<<152 * 4, 128, 0, s>>>(d, p, all_passes);
-  n += 5;
+  const int all_passes = p.prob >= 1.0;
+  // with prob >= 1 the passes run inside the per-replica kernel
+  overlap_comp_kernel<<<d.nrep, kBlock, 0, s>>>(d, p, all_passes);
+  n += 2;
   if (all_passes) return n;
+  overlap_pass1_kernel<<<152 * 4, 128, 0, s>>>(d, p, 0);
   overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
-  return n + 1;
+  return n + 2;
 }
 
 int k_bloques(const Dev& d, const KParams& p, cudaStream_t s) {
