@@ -875,6 +875,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.facc, mixed ? 4 * (size_t)cap : 4);
   AL(d.ftouch, mixed ? (size_t)cap / 32 + 1 : 1);
   AL(d.ftlist, mixed ? (size_t)cap : 1);
+  AL(d.flist, cap);
   AL(d.cand, (size_t)c->K.cand_cap);
   AL(d.ev_count, cap);
   AL(d.ev, mixed ? 1 : (size_t)cap * c->P.event_cap);
@@ -1194,7 +1195,13 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     c->K.chunk_dist = c->chunk_dist;
     c->K.n_chunk = n_chunk;
   }
+  // the context-wide state starts at zero but for the F members the load
+  // listed for the first capture commit
+  int n_f = 0;
+  CK(cudaMemcpyAsync(&n_f, &d.g->n_f, sizeof n_f, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
   std::memset(c->h_g, 0, sizeof(Global));
+  c->h_g->n_f = n_f;
   CK(cudaMemcpyAsync(d.g, c->h_g, sizeof(Global), cudaMemcpyHostToDevice, st));
   CK(cudaStreamSynchronize(st));
   c->loaded = true;

@@ -122,6 +122,7 @@ struct Global {
   int n_big;                // entries of big_cells
   int n_ftouch;             // entries of ftlist (mixed-form sums)
   int chunk_event;          // some replica added its chunk this step (bloques)
+  int n_f;                  // entries of Dev::flist
 };
 
 struct EvRec {            // one interacting list entry seen from one atom
@@ -248,6 +249,8 @@ struct Dev {
   // one bit per slot (ftouch) and listed once each (ftlist, Global::n_ftouch)
   unsigned* ftouch;
   int* ftlist;
+  // hs slots whose element became F (captured) since the last capture commit
+  int* flist;
   // force events
   int* ev_count;
   EvRec* ev;

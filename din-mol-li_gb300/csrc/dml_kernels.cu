@@ -365,6 +365,12 @@ __device__ __forceinline__ void block_max_to(unsigned v, unsigned* dst) {
   if (threadIdx.x == 0 && s_max) atomicMax(dst, s_max);
 }
 
+// An atom whose element became F: listed for the capture commit.
+__device__ __forceinline__ void note_f(const Dev& d, int h) {
+  const int q = atomicAdd(&d.g->n_f, 1);
+  if (q < d.cap) d.flist[q] = h;
+}
+
 // atom_pbc (dana.F90:1187-1250) on registers; returns true when deposited.
 __device__ __forceinline__ bool atom_pbc_dev(const KParams& p, const RepConst& R, Scalars* sc,
                                              long long step,
@@ -534,7 +540,10 @@ __device__ __forceinline__ unsigned ermak_a_mixed_atom(const Dev& d, const KPara
     d.posf_old[h] = to_f4(po, 0);
   }
   if (v_changed) stv(d.vel, h, V.x, V.y, -V.z);  // the mirror at zmax reverses vz
-  if (typ != typ0) d.typ[h] = (int8_t)typ;
+  if (typ != typ0) {
+    d.typ[h] = (int8_t)typ;
+    if (typ == DML_Z_F) note_f(d, h);
+  }
   if (!depos) d.skip[h] = 0;
   return mv;
 }
@@ -584,7 +593,10 @@ __device__ __forceinline__ unsigned ermak_a_at(const Dev& d, const KParams& p, i
     d.posf_old[h] = to_f4(po, 0);
   }
   if (v_changed) d.vel[h] = V;
-  if (typ != typ0) d.typ[h] = (int8_t)typ;
+  if (typ != typ0) {
+    d.typ[h] = (int8_t)typ;
+    if (typ == DML_Z_F) note_f(d, h);
+  }
   if (!depos) d.skip[h] = 0;
   return mv;
 }
@@ -675,7 +687,10 @@ __device__ __forceinline__ unsigned brownian_at(const Dev& d, const KParams& p, 
       d.pos_old[h] = po;
       d.posf_old[h] = to_f4(po, 0);
     }
-    if (typ != typ0) d.typ[h] = (int8_t)typ;
+    if (typ != typ0) {
+    d.typ[h] = (int8_t)typ;
+    if (typ == DML_Z_F) note_f(d, h);
+  }
     if (!depos) d.skip[h] = 0;
     return mv;
   }
@@ -706,7 +721,10 @@ __device__ __forceinline__ unsigned brownian_at(const Dev& d, const KParams& p, 
     d.pos_old[h] = po;
     d.posf_old[h] = to_f4(po, 0);
   }
-  if (typ != typ0) d.typ[h] = (int8_t)typ;
+  if (typ != typ0) {
+    d.typ[h] = (int8_t)typ;
+    if (typ == DML_Z_F) note_f(d, h);
+  }
   if (!depos) d.skip[h] = 0;
   return mv;
 }
@@ -2506,6 +2524,7 @@ __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, in
       if (ne < p.prob) {
         count_add(&sc->depo, 1ull);
         d.typ[x] = DML_Z_F;
+        note_f(d, x);
         float4 f = d.posf[x];
         f.w = __int_as_float(DML_Z_F);
         d.posf[x] = f;
@@ -2677,18 +2696,16 @@ __global__ void overlap_passn_kernel(Dev d, KParams p) {
 // ------------------------------------------------- capture commit, rho, piston
 // dana.F90:228-236: every F member of hs%ref becomes CG and leaves hs%ref
 // (its rank becomes a hole; the order of the remaining members is kept).
-__device__ __forceinline__ void commit_at(Dev d, int n_rank, int rep, int pos) {
-  const RepConst& R = d.rc[rep];
+__device__ __forceinline__ void commit_at(Dev d, int h) {
+  const int rep = d.rep_of[h];
   Scalars* sc = d.sc + rep;
-  const int h = ref_slot(d, pos, R.base + sc->n_slots);
-  if (h < 0) return;
-  if (d.typ[h] != DML_Z_F) return;
   const int r = d.rank[h];
+  if (r < 0 || d.typ[h] != DML_Z_F) return;
+  if (atomicCAS(&d.rank[h], r, -1) != r) return;  // listed twice: once only
   d.typ[h] = DML_Z_CG;
   float4 f = d.posf[h];
   f.w = __int_as_float(DML_Z_CG);
   d.posf[h] = f;
-  d.rank[h] = -1;
   d.ref[r] = -1;
   atomicSub(&sc->n_ref, 1);
   atomicAdd(&sc->n_new_cg, 1);
@@ -2699,10 +2716,15 @@ __device__ __forceinline__ void commit_at(Dev d, int n_rank, int rep, int pos) {
   }
 }
 
-__global__ void commit_kernel(Dev d, int n_rank) {
-  const int rep = block_rep(d);
-#pragma unroll
-  for (int u = 0; u < kSlotU; ++u) commit_at(d, n_rank, rep, span_pos(u));
+// Over the atoms that became F since the last commit (listed where the
+// element is set: atom_pbc, overlap_moveback's contact capture, loading and
+// chunk attachment), one block: captures are few, and the block empties
+// the list when it is done.
+__global__ void commit_kernel(Dev d) {
+  const int n = min(d.g->n_f, d.cap);
+  for (int q = threadIdx.x; q < n; q += blockDim.x) commit_at(d, d.flist[q]);
+  __syncthreads();
+  if (threadIdx.x == 0) d.g->n_f = 0;
 }
 
 // calc_rho (dana.F90:521-549): integer count, so any reduction order is exact.
@@ -2910,6 +2932,7 @@ __global__ void bloques_kernel(Dev d, KParams p) {
     sc->next_id += 1;
     d.ev_count[slot] = 0;
     d.nn[slot] = 0;
+    if (typ == DML_Z_F) note_f(d, slot);
     // sys
     const int ap = sc->n_alist;
     d.alist[B + ap] = slot;
@@ -5301,6 +5324,7 @@ __global__ void load_atoms_kernel(Dev d, KParams p, LoadIn in) {
     d.b2hs[h] = h;
     const int rk = in.rk[i], gk = in.gk[i];
     if (rk >= 0) {
+      if (z == DML_Z_F) note_f(d, h);  // committed at the first capture commit
       d.rank[h] = B + rk;
       d.ref[B + rk] = h;
     }
@@ -5519,7 +5543,8 @@ int k_chunk_cond(const Dev& d, cudaGraphConditionalHandle h, cudaStream_t s) {
 
 int k_capture_commit(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
   (void)p;
-  commit_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
+  (void)n_rank;
+  commit_kernel<<<1, 1024, 0, s>>>(d);
   return 1;
 }
 
