@@ -413,12 +413,14 @@ def force_error_probe(wl, nrep=4, steps=20):
             "tolerance": 1e-6, "within": bool(e.max() <= 1e-6)}
 
 
-def deposition_probe(n_rep=64, steps=2000):
+def deposition_probe(n_rep=64, steps=2000, cell_factor=1.0):
     """Deposition statistics of the two forms over seeds: n_rep config-1
     systems (400-atom bcc electrode, 200 Li+, piston), each its own ion
     placement and Philox seed, run `steps` Ermak steps in one batch per form.
     The captures per replica are compared: the chosen form's mean against the
-    plain FP64 form's mean and spread over seeds."""
+    plain FP64 form's mean and spread over seeds.  The chosen form runs with
+    cell edges of cell_factor x (rc + skin) (the cell size the autotuner
+    picked for the timed workload); the plain form keeps the reference's."""
     import statistics as st
 
     import dml
@@ -435,13 +437,16 @@ def deposition_probe(n_rep=64, steps=2000):
         sim = dml.Simulation(q, replicas=reps)
         sim.set_atoms(atoms)
         sim.setup()
+        if form == "mixed" and cell_factor != 1.0:
+            sim.set_cell_factor(cell_factor)
         sim.step(steps)
         depo[form] = [int(sim.counters(replica=r)["depo"]) for r in range(n_rep)]
         sim.close()
     mf, mm = st.mean(depo["fp64"]), st.mean(depo["mixed"])
     sf = st.stdev(depo["fp64"])
     return {"system": "config 1 (10x10x2-cell electrode, 200 Li+, piston z0=30, Ermak dt=1fs)",
-            "seeds": n_rep, "steps": steps, "fp64_mean": mf, "fp64_sigma": sf,
+            "seeds": n_rep, "steps": steps, "mixed_cell_factor": cell_factor,
+            "fp64_mean": mf, "fp64_sigma": sf,
             "mixed_mean": mm, "mixed_sigma": st.stdev(depo["mixed"]),
             "mean_difference_in_fp64_sigma": (mm - mf) / sf if sf else None,
             "within_1_sigma": bool(sf == 0.0 or abs(mm - mf) <= sf)}
@@ -771,7 +776,8 @@ def run_gpu(args, ws, rank, local):
     if form == "chosen" and not args.no_compare:
         compare = {}
         compare["force_error"] = force_error_probe(wl)
-        compare["deposition"] = deposition_probe()
+        compare["deposition"] = deposition_probe(
+            cell_factor=cell_tuning["factor"] if cell_tuning else 1.0)
         sp = wl.open(dml.PRECISION_FP64)
         sp.setup()
         ms_p, p0, p1, _ = timed_steps(sp, args)

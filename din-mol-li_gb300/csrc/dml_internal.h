@@ -85,6 +85,7 @@ struct Scalars {
   int max_nn;
   int passes;      // passes of the last overlap_moveback
   int again, again2;     // overlap pass flags (pass p-1, pass p) when captures can fail
+  int comp_defer;        // prob >= 1: this call's components run in overlap_pass1_kernel
   unsigned int ticket;   // last-block-done counters of this replica
   unsigned int ticket2;
   int rho_count;

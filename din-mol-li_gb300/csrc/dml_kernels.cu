@@ -2465,7 +2465,8 @@ __global__ void overlap_count_kernel(Dev d, int n_rank) {
 // members, one atomic per warp on each counter (the components are
 // independent, so their numbering is free).  Per position of each replica's
 // list segment; every lane calls it.
-__device__ __forceinline__ void overlap_assign_at(const Dev& d, int end, int i) {
+__device__ __forceinline__ void overlap_assign_at(const Dev& d, int end, int i,
+                                                  int* n_rep_comp = nullptr) {
   const int lane = threadIdx.x & 31;
   int h = -1, sz = 0;
   if (i < end) {
@@ -2486,6 +2487,7 @@ __device__ __forceinline__ void overlap_assign_at(const Dev& d, int end, int i) 
   if (lane == leader) {
     bc = atomicAdd(&d.g->n_comp, __popc(m));
     bt = atomicAdd(&d.g->comp_total, total);
+    if (n_rep_comp) atomicAdd(n_rep_comp, __popc(m));
   }
   bc = __shfl_sync(0xffffffffu, bc, leader);
   bt = __shfl_sync(0xffffffffu, bt, leader);
@@ -2598,17 +2600,24 @@ __device__ void overlap_pass1_comp(const Dev& d, const KParams& p, int all_passe
 
 // The bookkeeping of one replica's listed members (component numbers and
 // ranges, members scattered, members in rank order), then, when every pass
-// can run inside a component (prob >= 1), the component passes: one block per
-// replica, the stages separated by block barriers (a component lies inside
-// one replica).  The same work as overlap_assign, _scatter, _order and _pass1
-// in one launch.
+// can run inside a component (prob >= 1) and the replica has at most one
+// component per thread, the component passes: one block per replica, the
+// stages separated by block barriers (a component lies inside one replica).
+// A replica with more components leaves its passes to overlap_pass1_kernel,
+// whose grid spreads them over every SM (comp_defer).
 __global__ void overlap_comp_kernel(Dev d, KParams p, int passes) {
   const int rep = blockIdx.x;
   const int base = d.rc[rep].base;
   const int end = base + d.pr_cnt[rep * kCntStride + kCntAct];
   if (end == base) return;  // no member with a near contact
-  for (int i0 = base; i0 < end; i0 += blockDim.x) overlap_assign_at(d, end, i0 + threadIdx.x);
+  __shared__ int s_ncomp;
+  if (threadIdx.x == 0) s_ncomp = 0;
   __syncthreads();
+  for (int i0 = base; i0 < end; i0 += blockDim.x)
+    overlap_assign_at(d, end, i0 + threadIdx.x, &s_ncomp);
+  __syncthreads();
+  const bool here = passes && s_ncomp <= (int)blockDim.x;
+  if (threadIdx.x == 0) d.sc[rep].comp_defer = passes && !here;
   for (int i = base + threadIdx.x; i < end; i += blockDim.x) {
     const int h = d.ref[d.act_list[i]];
     const int root = d.uf[h];
@@ -2626,7 +2635,7 @@ __global__ void overlap_comp_kernel(Dev d, KParams p, int passes) {
     for (int q = 0; q < sz; ++q) before += rk[q] < r;
     d.comp_members[off + before] = h;
   }
-  if (!passes) return;
+  if (!here) return;
   __syncthreads();
   // every component of the replica once: through its root's listed member
   for (int i = base + threadIdx.x; i < end; i += blockDim.x) {
@@ -2635,11 +2644,19 @@ __global__ void overlap_comp_kernel(Dev d, KParams p, int passes) {
   }
 }
 
+// Pass 1 of every component on a fixed grid; with all_passes (prob >= 1)
+// every pass, and only the components of replicas that overlap_comp_kernel
+// left to this kernel.
 __global__ void overlap_pass1_kernel(Dev d, KParams p, int all_passes) {
   const int ncomp = d.g->n_comp;
   for (int cid = blockIdx.x * blockDim.x + threadIdx.x; cid < ncomp;
-       cid += gridDim.x * blockDim.x)
+       cid += gridDim.x * blockDim.x) {
+    if (all_passes) {
+      const int sz = d.comp_list[2 * cid + 1];
+      if (sz == 0 || !d.sc[d.rep_of[d.comp_members[d.comp_list[2 * cid]]]].comp_defer) continue;
+    }
     overlap_pass1_comp(d, p, all_passes, cid);
+  }
 }
 
 // Passes 2.. (the recursion, needed when a capture can fail): one block, a
@@ -5522,13 +5539,14 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
   if (detect) n += k_overlap_detect(d, p, n_rank, detect == 1 ? 1 : 0, s);
   overlap_count_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
   const int all_passes = p.prob >= 1.0;
-  // with prob >= 1 the passes run inside the per-replica kernel
+  // with prob >= 1 the passes of a replica with few components run inside
+  // the per-replica kernel, the others in overlap_pass1_kernel
   overlap_comp_kernel<<<d.nrep, kBlock, 0, s>>>(d, p, all_passes);
-  n += 2;
+  overlap_pass1_kernel<<<152 * 4, 128, 0, s>>>(d, p, all_passes);
+  n += 3;
   if (all_passes) return n;
-  overlap_pass1_kernel<<<152 * 4, 128, 0, s>>>(d, p, 0);
   overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
-  return n + 2;
+  return n + 1;
 }
 
 int k_bloques(const Dev& d, const KParams& p, cudaStream_t s) {
