@@ -889,6 +889,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.comp_members, cap);
   AL(d.comp_list, 2 * (size_t)cap);
   AL(d.act_list, cap);
+  AL(d.act_big_pre, nrep + 1);
   AL(d.glist, c->P.reservoir == DML_RESERVOIR_GCMC ? (size_t)cap : 1);
   AL(d.pr_cnt, (size_t)nrep * kCntStride);
   d.nblk_part = cap / kBlock + 1;

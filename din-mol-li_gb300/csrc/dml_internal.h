@@ -32,6 +32,10 @@ constexpr int kSlotU = 4;                 // positions per thread of the per-pos
 constexpr int kSpan = kBlock * kSlotU;    // positions per block; replica capacities are multiples
 constexpr int kCellChunk = kBlock * 4;    // cells per block of the per-cell kernels
 constexpr int kCntStride = 32, kCntGlist = 0, kCntAct = 1;  // pr_cnt layout
+// overlap_moveback's bookkeeping: a replica with at most this many listed
+// members is handled by one block (overlap_comp_kernel), a larger one by
+// grid kernels over all its listed members
+constexpr int kCompBlockMax = 2048;
 constexpr int kCntGcmcPar = 2, kCntGcmcSeq = 3;  // gcmc_run calls per path (diagnostic)
 
 // Replicas.  A context holds one or more independent systems ("replicas",
@@ -124,6 +128,7 @@ struct Global {
   int n_ftouch;             // entries of ftlist (mixed-form sums)
   int chunk_event;          // some replica added its chunk this step (bloques)
   int n_f;                  // entries of Dev::flist
+  unsigned int ticket_act;  // overlap_count blocks done (the last forms act_big_pre)
 };
 
 struct EvRec {            // one interacting list entry seen from one atom
@@ -263,6 +268,8 @@ struct Dev {
   int *near_count, *near, *uf, *comp_size, *comp_id, *comp_rank, *comp_fill, *comp_members, *comp_list;
   int* act_list;      // ranks of the hs%ref members with a near contact this step, replica
                       // r's at [base, base + pr_cnt[r * kCntStride + kCntAct])
+  int* act_big_pre;   // nrep + 1: prefix of the listed members of the replicas with more
+                      // than kCompBlockMax of them (0 for the others)
   int2* glist;        // gcmc_run's cell sort: (hs slot, cell) of the atoms within reach,
                       // replica r's entries at [base, base + pr_cnt[r * kCntStride + kCntGlist])
   float4* glp;        // the same entries' FP32 positions, w = hs slot (integer bits)

@@ -2455,10 +2455,52 @@ __device__ __forceinline__ void overlap_count_at(Dev d, int n_rank, int rep, int
   atomicAdd(&d.comp_size[root], 1);
 }
 
+// The last block to finish forms the prefix of the listed members of the
+// replicas with more than kCompBlockMax of them (act_big_pre).
 __global__ void overlap_count_kernel(Dev d, int n_rank) {
   const int rep = block_rep(d);
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) overlap_count_at(d, n_rank, rep, span_pos(u));
+  __shared__ int s_last, s_carry;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&d.g->ticket_act, 1u) == gridDim.x - 1u;
+    s_carry = 0;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int r0 = 0; r0 < d.nrep; r0 += blockDim.x) {
+    const int r = r0 + threadIdx.x;
+    int v = 0;
+    if (r < d.nrep) {
+      v = __ldcg(d.pr_cnt + r * kCntStride + kCntAct);
+      if (v <= kCompBlockMax) v = 0;
+    }
+    int tot;
+    const int e = blk_scan_excl(v, &tot);
+    if (r < d.nrep) d.act_big_pre[r] = s_carry + e;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    d.act_big_pre[d.nrep] = s_carry;
+    d.g->ticket_act = 0;
+  }
+}
+
+// The replica of position g of the big replicas' listed members: the last
+// replica r with act_big_pre[r] <= g (then act_big_pre[r + 1] > g, so r has
+// listed members).
+__device__ __forceinline__ int big_rep_of(const Dev& d, int g) {
+  int lo = 0, hi = d.nrep - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (d.act_big_pre[mid] <= g) lo = mid; else hi = mid - 1;
+  }
+  return lo;
 }
 
 // Component numbers and member ranges for the roots among the listed
@@ -2499,8 +2541,54 @@ __device__ __forceinline__ void overlap_assign_at(const Dev& d, int end, int i,
   }
 }
 
-// Members of every component in rank order (overlap_comp_kernel): each
-// member's place is the number of smaller ranks in its component.
+// The same bookkeeping for the replicas with more than kCompBlockMax listed
+// members, three grid kernels over all of their listed members (the stages
+// need every block's results): component numbers and ranges, the members
+// scattered, the members in rank order (each member's place is the number
+// of smaller ranks in its component).
+__global__ void overlap_assign_big_kernel(Dev d) {
+  const int total = d.act_big_pre[d.nrep];
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int w = warp_id_global(); 32 * w < total; w += nw) {
+    const int g = 32 * w + (threadIdx.x & 31);
+    int end = 0, i = 1;  // past the total: no entry
+    if (g < total) {
+      const int rep = big_rep_of(d, g);
+      const int base = d.rc[rep].base;
+      end = base + d.pr_cnt[rep * kCntStride + kCntAct];
+      i = base + g - d.act_big_pre[rep];
+    }
+    overlap_assign_at(d, end, i);
+  }
+}
+
+__device__ __forceinline__ int big_act_entry(const Dev& d, int g) {
+  const int rep = big_rep_of(d, g);
+  return d.act_list[d.rc[rep].base + g - d.act_big_pre[rep]];
+}
+
+__global__ void overlap_scatter_big_kernel(Dev d) {
+  const int total = d.act_big_pre[d.nrep];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    const int r = big_act_entry(d, g);
+    const int root = d.uf[d.ref[r]];
+    d.comp_rank[d.comp_list[2 * d.comp_id[root]] + atomicAdd(&d.comp_fill[root], 1)] = r;
+  }
+}
+
+__global__ void overlap_order_big_kernel(Dev d) {
+  const int total = d.act_big_pre[d.nrep];
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    const int r = big_act_entry(d, g);
+    const int h = d.ref[r];
+    const int cid = d.comp_id[d.uf[h]];
+    const int off = d.comp_list[2 * cid], sz = d.comp_list[2 * cid + 1];
+    const int* rk = d.comp_rank + off;
+    int before = 0;
+    for (int q = 0; q < sz; ++q) before += rk[q] < r;
+    d.comp_members[off + before] = h;
+  }
+}
 
 // Examination of o1 = x in pass `pass` (dana.F90:871-935).
 __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, int* again) {
@@ -2604,12 +2692,17 @@ __device__ void overlap_pass1_comp(const Dev& d, const KParams& p, int all_passe
 // component per thread, the component passes: one block per replica, the
 // stages separated by block barriers (a component lies inside one replica).
 // A replica with more components leaves its passes to overlap_pass1_kernel,
-// whose grid spreads them over every SM (comp_defer).
+// whose grid spreads them over every SM (comp_defer); one with more than
+// kCompBlockMax listed members was handled by the _big kernels.
 __global__ void overlap_comp_kernel(Dev d, KParams p, int passes) {
   const int rep = blockIdx.x;
   const int base = d.rc[rep].base;
   const int end = base + d.pr_cnt[rep * kCntStride + kCntAct];
   if (end == base) return;  // no member with a near contact
+  if (end - base > kCompBlockMax) {
+    if (threadIdx.x == 0) d.sc[rep].comp_defer = passes;
+    return;
+  }
   __shared__ int s_ncomp;
   if (threadIdx.x == 0) s_ncomp = 0;
   __syncthreads();
@@ -5538,12 +5631,16 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
   }
   if (detect) n += k_overlap_detect(d, p, n_rank, detect == 1 ? 1 : 0, s);
   overlap_count_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
+  // replicas with many listed members: their bookkeeping on the whole grid
+  overlap_assign_big_kernel<<<152 * 4, kBlock, 0, s>>>(d);
+  overlap_scatter_big_kernel<<<152 * 4, kBlock, 0, s>>>(d);
+  overlap_order_big_kernel<<<152 * 4, kBlock, 0, s>>>(d);
   const int all_passes = p.prob >= 1.0;
   // with prob >= 1 the passes of a replica with few components run inside
   // the per-replica kernel, the others in overlap_pass1_kernel
   overlap_comp_kernel<<<d.nrep, kBlock, 0, s>>>(d, p, all_passes);
   overlap_pass1_kernel<<<152 * 4, 128, 0, s>>>(d, p, all_passes);
-  n += 3;
+  n += 6;
   if (all_passes) return n;
   overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
   return n + 1;
