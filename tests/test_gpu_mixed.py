@@ -76,7 +76,7 @@ def test_mixed_is_deterministic():
 
 
 def test_device_conversions_match_ieee():
-    """The integer-pipe conversions behind the FP32 position copies and the
+    """The device conversions behind the FP32 position copies and the
     integrators' FP32 increments equal IEEE 754 round-to-nearest-even (numpy)
     over random bit patterns, positions in the box range, halfway cases,
     mantissa carries and the subnormal, overflow, zero, inf and NaN edges."""
