@@ -44,6 +44,8 @@ struct dml_ctx {
   std::vector<int> chunk_z;
   double chunk_dist = 0.0;
   int graph_steps = 100;
+  bool scan_stale = true;  // the host changed the state: the next force scan is full
+  int forced_lanes = 0;    // dml_set_scan_lanes (0: tuned)
   int launches_per_step = 0;    // kernels of a step without a list rebuild
   int launches_per_rebuild = 0; // extra kernels when the list is rebuilt
   float tune_us[kScanMappings] = {};  // force-scan time per mapping (1, 2, 4, 8, 16, 32 lanes per row)
@@ -226,6 +228,8 @@ void make_kparams(const dml_params& P, KParams& K) {
   K.max_passes = P.max_passes;
   K.mixed = P.precision == DML_PRECISION_MIXED;
   K.scan_lanes = 16;  // until the step graph is tuned
+  K.short_scan = 0;   // set with the tuned mapping (one lane per row)
+  K.short_skin = 0.5f;
   K.near_lanes = 32;
   K.rcf = (float)P.rc;
   // 2^32 per eV/Å; 1 eV = 96.485 * 100 ui (dana.F90:23)
@@ -270,6 +274,7 @@ int write_scalars(dml_ctx* c) {
 }
 
 int finish(dml_ctx* c) {
+  c->scan_stale = true;  // whatever the call did, the next step's force scan is full
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(c, e, "kernel launch");
   int rc = read_scalars(c);
@@ -516,7 +521,7 @@ int autotune_scan(dml_ctx* c) {
   };
   int sl = 0, nl = 0;
   if (ermak) {
-    sl = sweep(false, c->tune_us);
+    sl = c->forced_lanes > 0 ? c->forced_lanes : sweep(false, c->tune_us);
     nl = sl < 0 ? -1 : sweep(true, nullptr);
   } else {
     nl = sweep(true, c->tune_us);
@@ -526,6 +531,11 @@ int autotune_scan(dml_ctx* c) {
   if (sl < 0 || nl < 0) return cuda_fail(c, cudaGetLastError(), "autotune timing");
   if (ermak) c->K.scan_lanes = sl;
   c->K.near_lanes = nl;
+  // The force scan walks only flagged rows between full scans when a step
+  // moves atoms by their integrator alone (no piston, no chunk shifts) and
+  // the scan runs one lane per row.
+  c->K.short_scan = ermak && sl == 1 && c->P.reservoir != DML_RESERVOIR_PISTON &&
+                    c->P.reservoir != DML_RESERVOIR_CHUNKS;
   return finish(c);
 }
 
@@ -575,9 +585,18 @@ int build_multi_graph(dml_ctx* c) {
 
 // nsteps iterations: as many graph_steps-step graphs as fit, then one-step
 // graphs.
+// Before steps queued after any other call: every replica's next force scan
+// is full (the flags of the partial scans belong to the state the steps left).
+void scan_refresh(dml_ctx* c) {
+  if (!c->scan_stale) return;
+  k_scan_invalidate(c->D, c->stream);
+  c->scan_stale = false;
+}
+
 int queue_steps(dml_ctx* c, int64_t nsteps) {
   int rc = build_step_graph(c);
   if (rc) return rc;
+  scan_refresh(c);
   int64_t i = 0;
   if (c->graph_steps > 1 && nsteps >= c->graph_steps) {
     if ((rc = build_multi_graph(c)) != 0) return rc;
@@ -890,6 +909,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.comp_list, 2 * (size_t)cap);
   AL(d.act_list, cap);
   AL(d.act_big_pre, nrep + 1);
+  AL(d.rowflag, cap);
   AL(d.glist, c->P.reservoir == DML_RESERVOIR_GCMC ? (size_t)cap : 1);
   AL(d.pr_cnt, (size_t)nrep * kCntStride);
   d.nblk_part = cap / kBlock + 1;
@@ -1401,6 +1421,7 @@ int dml_time_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* ms) {
   if (!c->loaded || !c->setup_done) return DML_E_STATE;
   int rc = build_step_graph(c);
   if (rc) return rc;
+  scan_refresh(c);
   if (flush_l2 && (rc = ensure_flush(c)) != 0) return rc;
   std::vector<cudaEvent_t> ev(2 * nsteps);
   for (auto& e : ev) CK(cudaEventCreate(&e));
@@ -1432,6 +1453,7 @@ int dml_profile_steps(dml_ctx* c, int64_t nsteps, int32_t flush_l2, double* phas
   std::vector<cudaEvent_t> ev(ne * nsteps);
   for (auto& e : ev) CK(cudaEventCreate(&e));
   std::vector<ProfileGap> gaps;
+  scan_refresh(c);
   for (int64_t i = 0; i < nsteps; ++i) {
     if (flush_l2) k_flush(c->flush_buf, kFlushBytes, c->stream);
     rc = enqueue_step(c, &ev[ne * i], false, nullptr, nullptr, &gaps);
@@ -1660,6 +1682,34 @@ int dml_get_counters_replica(dml_ctx* c, int32_t rep, dml_counters* o) {
   o->z0 = s.z0;
   o->rho = s.rho;
   o->rho0 = s.rho0;
+  return 0;
+}
+
+int dml_get_scan_counts(dml_ctx* c, int32_t rep, int64_t* full, int64_t* partial) {
+  if (!c || rep < 0 || rep >= c->D.nrep) return DML_E_ARG;
+  Scalars v;
+  std::memset(&v, 0, sizeof v);
+  if (c->loaded) {
+    CK(cudaMemcpyAsync(&v, c->D.sc + rep, sizeof v, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  if (full) *full = (int64_t)v.sl_nfull;
+  if (partial) *partial = (int64_t)v.sl_npartial;
+  return 0;
+}
+
+int dml_set_scan_lanes(dml_ctx* c, int32_t lanes) {
+  if (!c || !(lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8 ||
+              lanes == 16 || lanes == 32))
+    return DML_E_ARG;
+  c->forced_lanes = lanes;
+  if (c->step_graph || c->multi_graph) {
+    CK(cudaStreamSynchronize(c->stream));
+    if (c->step_graph) cudaGraphExecDestroy(c->step_graph);
+    if (c->multi_graph) cudaGraphExecDestroy(c->multi_graph);
+    c->step_graph = nullptr;
+    c->multi_graph = nullptr;
+  }
   return 0;
 }
 

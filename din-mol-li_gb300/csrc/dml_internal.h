@@ -90,6 +90,15 @@ struct Scalars {
   int passes;      // passes of the last overlap_moveback
   int again, again2;     // overlap pass flags (pass p-1, pass p) when captures can fail
   int comp_defer;        // prob >= 1: this call's components run in overlap_pass1_kernel
+  // The force scan between full scans (KParams::short_scan): the rows it
+  // walks are those flagged at the replica's last full scan (an entry
+  // within sl_rs) or written since; valid while every list entry's
+  // displacement since then stays under sl_disp.
+  float sl_disp;         // bound on any atom's displacement since the last full scan (A)
+  float sl_rs;           // the flag radius of the last full scan (A)
+  int sl_mode;           // this step's scan: 1 full (flags rewritten), 0 flagged rows only
+  int sl_full;           // the next scan must be full (lists rebuilt, state changed by the host)
+  unsigned long long sl_nfull, sl_npartial;  // steps of each mode so far
   unsigned int ticket;   // last-block-done counters of this replica
   unsigned int ticket2;
   int rho_count;
@@ -151,6 +160,8 @@ struct KParams {
   int mixed;
   int scan_lanes;           // lanes per list row in the force scan (1 .. 32; tuned)
   int near_lanes;           // lanes per list row in the near search (1 .. 32; tuned)
+  int short_scan;           // Ermak force scan of flagged rows between full scans (no piston/chunks)
+  float short_skin;         // flag radius beyond the scan's own radii (A)
   double c12[3][3];         // 12 eps / r0^2 (scalar pair force of the mixed form)
   int cand_cap;
   float rcf;                // rc (FP32, pre-filters)
@@ -268,6 +279,7 @@ struct Dev {
   int *near_count, *near, *uf, *comp_size, *comp_id, *comp_rank, *comp_fill, *comp_members, *comp_list;
   int* act_list;      // ranks of the hs%ref members with a near contact this step, replica
                       // r's at [base, base + pr_cnt[r * kCntStride + kCntAct])
+  uint8_t* rowflag;   // cap: the row takes part in the force scans between full scans
   int* act_big_pre;   // nrep + 1: prefix of the listed members of the replicas with more
                       // than kCompBlockMax of them (0 for the others)
   int2* glist;        // gcmc_run's cell sort: (hs slot, cell) of the atoms within reach,
@@ -351,6 +363,7 @@ int k_brownian(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 int k_force_pairs(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s);
 int k_force_scan(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s);
 int k_reset_candidates(const Dev& d, cudaStream_t s);
+int k_scan_invalidate(const Dev& d, cudaStream_t s);
 int k_force_sum(const Dev& d, const KParams& p, int n_slots, bool fuse_ermak_b, cudaStream_t s);
 int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s);
 // second: the step's test_update after overlap_moveback, which recomputes

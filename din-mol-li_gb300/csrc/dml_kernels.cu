@@ -782,8 +782,8 @@ __device__ __forceinline__ float near_radius2(const Dev& d, const KParams& p, co
 // agree on rep, r, h; h < 0 for no row).  Every lane of the warp takes part.
 // Pf and n are the row owner's FP32 position and list length.
 template <bool NEAR, int L>
-__device__ __forceinline__ void force_scan_row(const Dev& d, const KParams& p, int rep, int r,
-                                               int h, float4 Pf, int n) {
+__device__ __forceinline__ bool force_scan_row(const Dev& d, const KParams& p, int rep, int r,
+                                               int h, float4 Pf, int n, float flag_r2 = -1.0f) {
   // each lane keeps 4 entries in flight
   constexpr int U = 4, STEP = L * U;
   const unsigned FULL = 0xffffffffu;
@@ -796,14 +796,14 @@ __device__ __forceinline__ void force_scan_row(const Dev& d, const KParams& p, i
   int nmax = n;
 #pragma unroll
   for (int o = L; o < 32; o <<= 1) nmax = max(nmax, __shfl_xor_sync(FULL, nmax, o));
-  if (nmax == 0) return;  // every row of the warp is empty
+  if (nmax == 0) return false;  // every row of the warp is empty
   const int* row = d.list + (size_t)(h >= 0 ? h : 0) * p.mnb;
   // With NEAR the same pass records overlap_moveback's near entries (list
   // entries within rc + 2 delta, in list order) and unites their components.
   const float rn2 = NEAR ? near_radius2(d, p, R) : 0.0f;
   int* near = d.near + (size_t)(h >= 0 ? h : 0) * kNearCap;
   int ncnt = 0;
-  bool any = false;
+  bool any = false, flag = false;
   const unsigned lt = (1u << lane) - 1u;
   for (int base = 0; base < nmax; base += STEP) {
     int j[U];
@@ -828,6 +828,7 @@ __device__ __forceinline__ void force_scan_row(const Dev& d, const KParams& p, i
         if (fy > R.halfboxf[1]) fy -= R.boxf[1]; else if (fy < -R.halfboxf[1]) fy += R.boxf[1];
         df = fx * fx + fy * fy + fz * fz;
       }
+      flag = flag || (live && df <= flag_r2);
       // fuerza: r <= r0 + margin, eps != 0, not CG-CG (signed zeros only)
       const bool cand = live && !(k == DML_Z_CG && m == DML_Z_CG) && p.pair_on[k - 1][m - 1] &&
                         df <= R.r0f_pref2[k - 1][m - 1];
@@ -861,6 +862,7 @@ __device__ __forceinline__ void force_scan_row(const Dev& d, const KParams& p, i
     d.near_count[h] = ncnt > kNearCap ? -1 : ncnt;
     if (any) d.active[h] = 1;
   }
+  return flag;
 }
 
 // The rows in use, 32 / L per warp (L lanes each, so that the dependent
@@ -893,10 +895,24 @@ __global__ void __launch_bounds__(kBlock) force_scan_span_kernel(Dev d, KParams 
   const int end = d.rc[rep].base + d.sc[rep].n_slots;
   if ((int)blockIdx.x * kSpan >= end) return;  // whole block: warps stay full
   static_assert(kSlotU == 4, "four rows per thread");
+  // Between full scans (short_scan) only the flagged rows are walked: an
+  // unflagged row had no entry within sl_rs at the last full scan, and no
+  // atom has moved by more than sl_disp since, so none of its entries can
+  // lie within the force pre-filter or the near radius now (its near count
+  // is still the 0 of that scan).  A full scan rewrites the flags.
+  const bool short_mode = NEAR && p.short_scan;
+  const int full = short_mode ? d.sc[rep].sl_mode : 1;
+  const float flag_r2 = short_mode && full ? d.sc[rep].sl_rs * d.sc[rep].sl_rs : -1.0f;
   int h0 = ref_slot(d, span_pos(0), end);
   int h1 = ref_slot(d, span_pos(1), end);
   int h2 = ref_slot(d, span_pos(2), end);
   int h3 = ref_slot(d, span_pos(3), end);
+  if (!full) {  // a member's row is its own slot's: flags load with the ranks
+    if (h0 >= 0 && !d.rowflag[h0]) h0 = -1;
+    if (h1 >= 0 && !d.rowflag[h1]) h1 = -1;
+    if (h2 >= 0 && !d.rowflag[h2]) h2 = -1;
+    if (h3 >= 0 && !d.rowflag[h3]) h3 = -1;
+  }
   const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
   float4 P0 = h0 >= 0 ? d.posf[h0] : z4, P1 = h1 >= 0 ? d.posf[h1] : z4;
   float4 P2 = h2 >= 0 ? d.posf[h2] : z4, P3 = h3 >= 0 ? d.posf[h3] : z4;
@@ -906,11 +922,53 @@ __global__ void __launch_bounds__(kBlock) force_scan_span_kernel(Dev d, KParams 
 #pragma unroll 1
   for (int u = 0; u < kSlotU; ++u) {
     // the row's rank keys the reference's summation order of its entries
-    force_scan_row<NEAR, 1>(d, p, rep, h0 >= 0 ? d.rank[h0] : 0, h0, P0, n0);
+    const bool fl = force_scan_row<NEAR, 1>(d, p, rep, h0 >= 0 ? d.rank[h0] : 0, h0, P0, n0,
+                                            flag_r2);
+    if (short_mode && full && h0 >= 0) d.rowflag[h0] = fl ? 1 : 0;
     h0 = h1; h1 = h2; h2 = h3;
     P0 = P1; P1 = P2; P2 = P3;
     n0 = n1; n1 = n2; n2 = n3;
   }
+}
+
+// Each replica's force scan mode for this step (KParams::short_scan), after
+// the integrator: full when its lists changed or were loaded (sl_full), or
+// when the displacement bound since its last full scan could bring an
+// unflagged entry inside the larger of the force pre-filter and the near
+// radius; otherwise flagged rows only.  delta is this step's largest move
+// (the FP32 bound of ermak_a, plus margins); a full scan's flags are taken
+// at this step's positions, which overlap_moveback may still move back by
+// delta, so the bound restarts at delta.
+__global__ void scan_mode_kernel(Dev d, KParams p) {
+  const float delta = sqrtf(__uint_as_float(d.g->delta2f_bits));
+  for (int r = threadIdx.x; r < d.nrep; r += blockDim.x) {
+    Scalars* sc = d.sc + r;
+    const RepConst& R = d.rc[r];
+    float f2 = 0.0f;
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 3; ++b)
+        if (p.pair_on[a][b]) f2 = fmaxf(f2, R.r0f_pref2[a][b]);
+    const float need = fmaxf(sqrtf(near_radius2(d, p, R)), sqrtf(f2)) * 1.000001f;
+    const float dlt = (delta + 4.0f * R.margin) * 1.000001f;
+    const float D = sc->sl_disp + dlt;
+    if (sc->sl_full || need + 2.0f * D > sc->sl_rs) {
+      sc->sl_mode = 1;
+      sc->sl_full = 0;
+      sc->sl_disp = dlt;
+      sc->sl_rs = need + p.short_skin;
+      sc->sl_nfull += 1;
+    } else {
+      sc->sl_mode = 0;
+      sc->sl_disp = D;
+      sc->sl_npartial += 1;
+    }
+  }
+}
+
+// Every replica's next force scan is full (lists or positions changed outside
+// the step sequence).
+__global__ void scan_invalidate_kernel(Dev d) {
+  for (int r = threadIdx.x; r < d.nrep; r += blockDim.x) d.sc[r].sl_full = 1;
 }
 
 // Exact FP64 evaluation of the queued entries (dana.F90:1095-1134), one
@@ -1282,6 +1340,7 @@ __device__ __forceinline__ float disp2f(float4 P, float4 O) {
 __device__ __forceinline__ void decide_rebuild(const Dev& d, Scalars* sc, int rebuild) {
   sc->rebuild = rebuild;
   if (rebuild) {
+    sc->sl_full = 1;  // new lists: the next force scan sets the row flags again
     sc->nupd += 1;
     sc->max_nn = 0;
     atomicOr(&d.g->any_rebuild, 1);
@@ -3184,6 +3243,7 @@ __device__ void gcmc_own_list(const Dev& d, const KParams& p, const RepConst& R,
   if (lane == 0) {
     if (cnt > p.mnb) raise_error(d.g, DML_E_NEIGH_OVERFLOW, i);
     d.nn[i] = cnt > p.mnb ? p.mnb : cnt;
+    d.rowflag[i] = 1;  // a row written between full force scans
   }
 }
 
@@ -3837,6 +3897,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
         }
         d.list[(size_t)j * p.mnb + m] = slot;
         d.nn[j] = m + 1;
+        d.rowflag[j] = 1;
       };
       if (flat) {
         // Own list in stencil order: per cell, this run's insertions (chain,
@@ -3871,6 +3932,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
           }
           if (acc > p.mnb) raise_error(d.g, DML_E_NEIGH_OVERFLOW, slot);
           d.nn[slot] = acc > p.mnb ? p.mnb : acc;
+          d.rowflag[slot] = 1;
         }
         __syncthreads();
         int* row = d.list + (size_t)slot * p.mnb;
@@ -3990,6 +4052,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
         d.gorder[gp] = -1;
         sc->n_gcmc -= 1;
         d.nn[h] = 0;
+        d.rowflag[h] = 1;
         if (rk >= 0) {
           d.ref[rk] = -1;
           d.rank[h] = -1;
@@ -5240,6 +5303,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
       if (lane == 0) {
         if (cnt > p.mnb) raise_error(d.g, DML_E_NEIGH_OVERFLOW, slot);
         d.nn[slot] = cnt > p.mnb ? p.mnb : cnt;
+        d.rowflag[slot] = 1;  // a row written between full force scans
       }
     }
   }
@@ -5298,6 +5362,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
     d.in_gcmc[h] = 0;
     d.gorder[B + S.del_pos[q]] = -1;
     d.nn[h] = 0;
+    d.rowflag[h] = 1;
     if (rk >= 0) {
       d.ref[rk] = -1;
       d.rank[h] = -1;
@@ -5338,7 +5403,10 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
       const int m = S.app_base[e] + before;
       if (m < p.mnb) d.list[(size_t)j * p.mnb + m] = B + S.ins_slot[k];
       else raise_error(d.g, DML_E_NEIGH_OVERFLOW, j);
-      if (before == cnt - 1) d.nn[j] = min(S.app_base[e] + cnt, p.mnb);
+      if (before == cnt - 1) {
+        d.nn[j] = min(S.app_base[e] + cnt, p.mnb);
+        d.rowflag[j] = 1;
+      }
     }
   } else if (wid == 0) {
     // more appends than the shared table holds: one insertion at a time
@@ -5351,6 +5419,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
         }
         d.list[(size_t)j * p.mnb + m] = B + S.ins_slot[k];
         d.nn[j] = m + 1;
+        d.rowflag[j] = 1;
       });
       __syncwarp();
     }
@@ -5492,12 +5561,22 @@ int k_force_scan(const Dev& d, const KParams& p, int n_rank, bool near, cudaStre
 }
 
 int k_force_pairs(const Dev& d, const KParams& p, int n_rank, bool near, cudaStream_t s) {
+  int n = 2;
+  if (near && p.short_scan) {
+    scan_mode_kernel<<<1, 256, 0, s>>>(d, p);
+    n += 1;
+  }
   k_force_scan(d, p, n_rank, near, s);
   if (p.mixed)
     force_exact_mixed_kernel<<<152 * 4, kBlock, 0, s>>>(d, p);
   else
     force_exact_kernel<<<152 * 4, kBlock, 0, s>>>(d, p);
-  return 2;
+  return n;
+}
+
+int k_scan_invalidate(const Dev& d, cudaStream_t s) {
+  scan_invalidate_kernel<<<1, 256, 0, s>>>(d);
+  return 1;
 }
 
 int k_reset_candidates(const Dev& d, cudaStream_t s) {

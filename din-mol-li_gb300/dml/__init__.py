@@ -100,6 +100,8 @@ def lib():
                                ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
     L.dml_gen_ions_batch.argtypes = [i32, P(_abi.IonSpec), vp, vp]
     L.dml_get_gcmc_paths.argtypes = [vp, i32, P(i64), P(i64)]
+    L.dml_get_scan_counts.argtypes = [vp, i32, P(i64), P(i64)]
+    L.dml_set_scan_lanes.argtypes = [vp, i32]
     _lib = L
     return L
 
@@ -426,6 +428,17 @@ class Simulation:
         self._check(self.lib.dml_get_gcmc_paths(self.h, replica, ctypes.byref(a),
                                                  ctypes.byref(b)), "dml_get_gcmc_paths")
         return a.value, b.value
+
+    def scan_counts(self, replica=0):
+        """(full, flagged-rows-only) force scans of a replica so far."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.dml_get_scan_counts(self.h, replica, ctypes.byref(a),
+                                                  ctypes.byref(b)), "dml_get_scan_counts")
+        return a.value, b.value
+
+    def set_scan_lanes(self, lanes):
+        """Pin the force scan's lanes per row (0: autotuned)."""
+        self._check(self.lib.dml_set_scan_lanes(self.h, int(lanes)), "dml_set_scan_lanes")
 
     def get_neighbors(self, ld, replica=None):
         n_ref = self.counters(replica)["n_ref"]

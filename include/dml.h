@@ -353,6 +353,20 @@ int dml_get_counters_replica(dml_ctx* c, int32_t rep, dml_counters* out);
  * path's bounds).  Either pointer may be NULL. */
 int dml_get_gcmc_paths(dml_ctx* c, int32_t rep, int64_t* parallel, int64_t* sequential);
 
+/* Diagnostic (no counterpart in the reference): how many steps of replica
+ * `rep` ran the force scan over all rows (a full scan, which also flags the
+ * rows with an entry near enough to matter until atoms have moved by the
+ * flag margin) and how many over the flagged rows only.  The second count
+ * stays 0 unless the scan runs one lane per row with the Ermak integrator and
+ * a GCMC or fixed reservoir.  Either pointer may be NULL. */
+int dml_get_scan_counts(dml_ctx* c, int32_t rep, int64_t* full, int64_t* partial);
+
+/* Lanes per neighbour-list row of the force scan (1, 2, 4, 8, 16 or 32), or
+ * 0 to let the autotuner choose when the step graph is next built (the
+ * default).  The step graph is built again at the next step.  Returns 0 or
+ * DML_E_ARG. */
+int dml_set_scan_lanes(dml_ctx* c, int32_t lanes);
+
 /* One replica's atoms and neighbour lists (same layout as dml_get_atoms and
  * dml_get_neighbors, which take a one-replica context). */
 int dml_get_atoms_replica(dml_ctx* c, int32_t rep, dml_atoms* a);

@@ -10,7 +10,8 @@ run of the same replica, fed the same keyed Philox streams:
 
   config 5  two full replicas of the GCMC batch (40 x 40 x 2-cell electrode,
             20 000 Li+, 128 trials per step, Ermak, skin 2 Å), 100 steps with
-            list rebuilds, both replicas on the parallel GCMC path;
+            list rebuilds, both replicas on the parallel GCMC path and the
+            force scan walking flagged rows between full scans;
   config 2  the 280 000-atom system: the set-up list build and 20 steps,
             forces also checked within 1e-12 relative (src/dana.F90:173-265);
   config 1  the full 10 000-step run, captures compared every 1000 steps;
@@ -66,6 +67,7 @@ def test_config5_replicas_full_size():
     p, reps, atoms = systems.c5_batch(2, precision=dml.PRECISION_FP64)
     g = dml.Simulation(p, replicas=reps)
     g.set_atoms(atoms)
+    g.set_scan_lanes(1)  # the benchmark's mapping: flagged-row scans between full ones
     orcs = []
     for rep, at in zip(reps, atoms):
         o = oracle_lib.Oracle(replica_params(p, rep))
@@ -93,6 +95,8 @@ def test_config5_replicas_full_size():
         assert c["gcmc_ins"] > 0 and c["gcmc_del"] > 0 and c["choques"] > 0
         par, seq = g.gcmc_paths(replica=r)
         assert par == done and seq == 0, (r, par, seq)
+        full, partial = g.scan_counts(replica=r)
+        assert full + partial == done and partial > 0, (r, full, partial)
     g.close()
 
 

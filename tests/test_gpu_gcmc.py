@@ -60,10 +60,16 @@ def test_reference_gcmc_case_fused_steps():
     assert c["gcmc_ins"] > 0 and c["gcmc_del"] > 0
 
 
-def test_ermak_gcmc_with_electrode():
-    """Electrode + Ermak forces + GCMC reservoir (config 5 at test size)."""
+@pytest.mark.parametrize("lanes", [0, 1])
+def test_ermak_gcmc_with_electrode(lanes):
+    """Electrode + Ermak forces + GCMC reservoir (config 5 at test size).
+    With one lane per list row the force scan walks only the rows flagged at
+    its last full scan (or written by GCMC since) until the atoms have moved
+    by the flag margin: the run must still equal the oracle bit for bit, and
+    most scans must have been of that kind."""
     p = systems.c5_small_params()
     g, o = make_pair(p, systems.c1_atoms(dmin=3.2))
+    g.set_scan_lanes(lanes)
     g.setup()
     o.setup()
     done = 0
@@ -76,6 +82,9 @@ def test_ermak_gcmc_with_electrode():
     assert_same_lists(g, o, "ermak+gcmc end")
     c = g.counters()
     assert c["gcmc_ins"] > 0 and c["gcmc_del"] > 0
+    if lanes == 1:
+        full, partial = g.scan_counts()
+        assert full + partial == done and partial > full, (full, partial)
 
 
 def test_config5_shape_gcmc_matches_oracle():
