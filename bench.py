@@ -270,6 +270,8 @@ class Workload:
             p.z0, p.zmax, p.z1, p.seed = q.z0, q.zmax, q.z1, q.seed
         return p
 
+    scan_lanes = 0  # force scan lanes per row (0: autotuned)
+
     def open(self, precision, replicas=None):
         """A loaded context (all replicas, or the listed ones one by one)."""
         import dml
@@ -278,14 +280,16 @@ class Workload:
         if not self.batched:
             sim = dml.Simulation(p)
             sim.set_atoms(self.atoms[0])
-            return sim
-        idx = list(range(self.n_rep)) if replicas is None else replicas
-        if len(idx) == 1:
-            sim = dml.Simulation(self.replica_params(idx[0], precision))
-            sim.set_atoms(self.atoms[idx[0]])
-            return sim
-        sim = dml.Simulation(p, replicas=[self.reps[i] for i in idx])
-        sim.set_atoms([self.atoms[i] for i in idx])
+        else:
+            idx = list(range(self.n_rep)) if replicas is None else replicas
+            if len(idx) == 1:
+                sim = dml.Simulation(self.replica_params(idx[0], precision))
+                sim.set_atoms(self.atoms[idx[0]])
+            else:
+                sim = dml.Simulation(p, replicas=[self.reps[i] for i in idx])
+                sim.set_atoms([self.atoms[i] for i in idx])
+        if self.scan_lanes:
+            sim.set_scan_lanes(self.scan_lanes)
         return sim
 
 
@@ -727,6 +731,7 @@ def run_gpu(args, ws, rank, local):
     dml.build()
     dist = Dist(ws)
     wl = Workload(args.workload, rank, args.replicas)
+    wl.scan_lanes = args.scan_lanes
     form = args.form or ("chosen" if wl.batched else "plain")
     prec = dml.PRECISION_MIXED if form == "chosen" else dml.PRECISION_FP64
     clocks = Clocks(local)
@@ -870,6 +875,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-compare", action="store_true")
+    ap.add_argument("--scan-lanes", type=int, default=0,
+                    help="pin the force scan's lanes per list row (profiling a reduced "
+                         "workload with the full workload's mapping); 0: autotuned")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 10000 if args.workload == "c3" else 100
