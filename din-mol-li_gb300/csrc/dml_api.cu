@@ -910,6 +910,9 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   AL(d.act_list, cap);
   AL(d.act_big_pre, nrep + 1);
   AL(d.rowflag, cap);
+  AL(d.sl_rows, cap);
+  AL(d.sl_pre, nrep + 1);
+  AL(d.sl_nrows, nrep);
   AL(d.glist, c->P.reservoir == DML_RESERVOIR_GCMC ? (size_t)cap : 1);
   AL(d.pr_cnt, (size_t)nrep * kCntStride);
   d.nblk_part = cap / kBlock + 1;

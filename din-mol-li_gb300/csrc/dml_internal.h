@@ -279,7 +279,12 @@ struct Dev {
   int *near_count, *near, *uf, *comp_size, *comp_id, *comp_rank, *comp_fill, *comp_members, *comp_list;
   int* act_list;      // ranks of the hs%ref members with a near contact this step, replica
                       // r's at [base, base + pr_cnt[r * kCntStride + kCntAct])
-  uint8_t* rowflag;   // cap: the row takes part in the force scans between full scans
+  int* rowflag;       // cap: the row takes part in the force scans between full scans
+  int* sl_rows;       // cap: the flagged rows (hs slots), replica r's from its base
+  int* sl_pre;        // nrep + 1: prefix of the flagged rows of the replicas scanned partially
+  int* sl_nrows;      // nrep: entries of each replica's flagged-row list (not in Scalars:
+                      // gcmc_run's kernels keep the scalars in shared memory and write them
+                      // back, while their appends list rows)
   int* act_big_pre;   // nrep + 1: prefix of the listed members of the replicas with more
                       // than kCompBlockMax of them (0 for the others)
   int2* glist;        // gcmc_run's cell sort: (hs slot, cell) of the atoms within reach,

@@ -895,40 +895,91 @@ __global__ void __launch_bounds__(kBlock) force_scan_span_kernel(Dev d, KParams 
   const int end = d.rc[rep].base + d.sc[rep].n_slots;
   if ((int)blockIdx.x * kSpan >= end) return;  // whole block: warps stay full
   static_assert(kSlotU == 4, "four rows per thread");
-  // Between full scans (short_scan) only the flagged rows are walked: an
-  // unflagged row had no entry within sl_rs at the last full scan, and no
-  // atom has moved by more than sl_disp since, so none of its entries can
-  // lie within the force pre-filter or the near radius now (its near count
-  // is still the 0 of that scan).  A full scan rewrites the flags.
+  // With short_scan a replica scans all its rows only at a full scan, which
+  // flags the rows with an entry within sl_rs and lists them; between full
+  // scans force_scan_listed_kernel walks the list instead.
   const bool short_mode = NEAR && p.short_scan;
-  const int full = short_mode ? d.sc[rep].sl_mode : 1;
-  const float flag_r2 = short_mode && full ? d.sc[rep].sl_rs * d.sc[rep].sl_rs : -1.0f;
+  if (short_mode && !d.sc[rep].sl_mode) return;
+  const float flag_r2 = short_mode ? d.sc[rep].sl_rs * d.sc[rep].sl_rs : -1.0f;
   int h0 = ref_slot(d, span_pos(0), end);
   int h1 = ref_slot(d, span_pos(1), end);
   int h2 = ref_slot(d, span_pos(2), end);
   int h3 = ref_slot(d, span_pos(3), end);
-  if (!full) {  // a member's row is its own slot's: flags load with the ranks
-    if (h0 >= 0 && !d.rowflag[h0]) h0 = -1;
-    if (h1 >= 0 && !d.rowflag[h1]) h1 = -1;
-    if (h2 >= 0 && !d.rowflag[h2]) h2 = -1;
-    if (h3 >= 0 && !d.rowflag[h3]) h3 = -1;
-  }
   const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
   float4 P0 = h0 >= 0 ? d.posf[h0] : z4, P1 = h1 >= 0 ? d.posf[h1] : z4;
   float4 P2 = h2 >= 0 ? d.posf[h2] : z4, P3 = h3 >= 0 ? d.posf[h3] : z4;
   int n0 = h0 >= 0 ? d.nn[h0] : 0, n1 = h1 >= 0 ? d.nn[h1] : 0;
   int n2 = h2 >= 0 ? d.nn[h2] : 0, n3 = h3 >= 0 ? d.nn[h3] : 0;
+  const int lane = threadIdx.x & 31;
   // one copy of the row body, the rows rotated through registers
 #pragma unroll 1
   for (int u = 0; u < kSlotU; ++u) {
     // the row's rank keys the reference's summation order of its entries
     const bool fl = force_scan_row<NEAR, 1>(d, p, rep, h0 >= 0 ? d.rank[h0] : 0, h0, P0, n0,
                                             flag_r2);
-    if (short_mode && full && h0 >= 0) d.rowflag[h0] = fl ? 1 : 0;
+    if (short_mode) {
+      if (h0 >= 0) d.rowflag[h0] = fl ? 1 : 0;
+      const unsigned m = __ballot_sync(0xffffffffu, fl && h0 >= 0);
+      if (m) {
+        int b = 0;
+        if (lane == __ffs(m) - 1) b = atomicAdd(&d.sl_nrows[rep], __popc(m));
+        b = __shfl_sync(0xffffffffu, b, __ffs(m) - 1);
+        if (fl && h0 >= 0)
+          d.sl_rows[d.rc[rep].base + b + __popc(m & ((1u << lane) - 1u))] = h0;
+      }
+    }
     h0 = h1; h1 = h2; h2 = h3;
     P0 = P1; P1 = P2; P2 = P3;
     n0 = n1; n1 = n2; n2 = n3;
   }
+}
+
+// Between full scans (short_scan): the listed rows of the replicas scanned
+// partially, each walked whole as the full scan walks it.  An unlisted row
+// had no entry within sl_rs at the last full scan and no atom has moved by
+// sl_disp since, so none of its entries can lie within the force pre-filter
+// or the near radius now (its near count is still the 0 of that scan).
+// Rows whose atom left hs%ref since (captures, deletions) are skipped.
+template <bool NEAR>
+__global__ void __launch_bounds__(kBlock) force_scan_listed_kernel(Dev d, KParams p) {
+  const int total = d.sl_pre[d.nrep];
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  const int lane = threadIdx.x & 31;
+  for (int w = warp_id_global(); 32 * w < total; w += nw) {
+    const int g = 32 * w + lane;
+    int rep = 0, h = -1;
+    if (g < total) {
+      int lo = 0, hi = d.nrep - 1;  // the last replica whose prefix is <= g
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (d.sl_pre[mid] <= g) lo = mid; else hi = mid - 1;
+      }
+      rep = lo;
+      h = d.sl_rows[d.rc[rep].base + g - d.sl_pre[rep]];
+    }
+    const int r = h >= 0 ? d.rank[h] : -1;
+    if (r < 0) h = -1;
+    const float4 P = h >= 0 ? d.posf[h] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int n = h >= 0 ? d.nn[h] : 0;
+    force_scan_row<NEAR, 1>(d, p, rep, r >= 0 ? r : 0, h, P, n);
+  }
+}
+
+// A member's row that GCMC appends to between full force scans joins its
+// replica's flagged-row list, once (the flag says it is listed).
+__device__ __forceinline__ void flag_row(const Dev& d, int h) {
+  if (atomicExch(&d.rowflag[h], 1) != 0) return;
+  const int rep = d.rep_of[h];
+  d.sl_rows[d.rc[rep].base + atomicAdd(&d.sl_nrows[rep], 1)] = h;
+}
+
+// An inserted atom's row: its slot was free, so no list holds it (slots are
+// freed only by the list rebuilds, which make the next scan full) and it is
+// listed whatever its stale flag says.
+__device__ __forceinline__ void list_new_row(const Dev& d, int h) {
+  atomicExch(&d.rowflag[h], 1);
+  const int rep = d.rep_of[h];
+  d.sl_rows[d.rc[rep].base + atomicAdd(&d.sl_nrows[rep], 1)] = h;
 }
 
 // Each replica's force scan mode for this step (KParams::short_scan), after
@@ -939,30 +990,50 @@ __global__ void __launch_bounds__(kBlock) force_scan_span_kernel(Dev d, KParams 
 // (the FP32 bound of ermak_a, plus margins); a full scan's flags are taken
 // at this step's positions, which overlap_moveback may still move back by
 // delta, so the bound restarts at delta.
+__device__ int blk_scan_excl(int v, int* total);
+
 __global__ void scan_mode_kernel(Dev d, KParams p) {
   const float delta = sqrtf(__uint_as_float(d.g->delta2f_bits));
-  for (int r = threadIdx.x; r < d.nrep; r += blockDim.x) {
-    Scalars* sc = d.sc + r;
-    const RepConst& R = d.rc[r];
-    float f2 = 0.0f;
-    for (int a = 0; a < 3; ++a)
-      for (int b = 0; b < 3; ++b)
-        if (p.pair_on[a][b]) f2 = fmaxf(f2, R.r0f_pref2[a][b]);
-    const float need = fmaxf(sqrtf(near_radius2(d, p, R)), sqrtf(f2)) * 1.000001f;
-    const float dlt = (delta + 4.0f * R.margin) * 1.000001f;
-    const float D = sc->sl_disp + dlt;
-    if (sc->sl_full || need + 2.0f * D > sc->sl_rs) {
-      sc->sl_mode = 1;
-      sc->sl_full = 0;
-      sc->sl_disp = dlt;
-      sc->sl_rs = need + p.short_skin;
-      sc->sl_nfull += 1;
-    } else {
-      sc->sl_mode = 0;
-      sc->sl_disp = D;
-      sc->sl_npartial += 1;
+  __shared__ int s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int r0 = 0; r0 < d.nrep; r0 += blockDim.x) {
+    const int r = r0 + threadIdx.x;
+    int rows = 0;  // the listed rows this step walks (replicas scanned partially)
+    if (r < d.nrep) {
+      Scalars* sc = d.sc + r;
+      const RepConst& R = d.rc[r];
+      float f2 = 0.0f;
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b)
+          if (p.pair_on[a][b]) f2 = fmaxf(f2, R.r0f_pref2[a][b]);
+      const float need = fmaxf(sqrtf(near_radius2(d, p, R)), sqrtf(f2)) * 1.000001f;
+      // delta comes from FP32 copies of the positions, each within half an
+      // ulp of the coordinate (R.margin is 64 ulps of the largest one)
+      const float dlt = (delta + 0.125f * R.margin) * 1.000001f;
+      const float D = sc->sl_disp + dlt;
+      if (sc->sl_full || need + 2.0f * D > sc->sl_rs) {
+        sc->sl_mode = 1;
+        sc->sl_full = 0;
+        sc->sl_disp = dlt;
+        sc->sl_rs = need + p.short_skin;
+        d.sl_nrows[r] = 0;  // the full scan lists the flagged rows again
+        sc->sl_nfull += 1;
+      } else {
+        sc->sl_mode = 0;
+        sc->sl_disp = D;
+        sc->sl_npartial += 1;
+        rows = d.sl_nrows[r];
+      }
     }
+    int tot;
+    const int e = blk_scan_excl(rows, &tot);
+    if (r < d.nrep) d.sl_pre[r] = s_carry + e;
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += tot;
+    __syncthreads();
   }
+  if (threadIdx.x == 0) d.sl_pre[d.nrep] = s_carry;
 }
 
 // Every replica's next force scan is full (lists or positions changed outside
@@ -3243,7 +3314,7 @@ __device__ void gcmc_own_list(const Dev& d, const KParams& p, const RepConst& R,
   if (lane == 0) {
     if (cnt > p.mnb) raise_error(d.g, DML_E_NEIGH_OVERFLOW, i);
     d.nn[i] = cnt > p.mnb ? p.mnb : cnt;
-    d.rowflag[i] = 1;  // a row written between full force scans
+    list_new_row(d, i);  // an inserted atom's row, written between full force scans
   }
 }
 
@@ -3897,7 +3968,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
         }
         d.list[(size_t)j * p.mnb + m] = slot;
         d.nn[j] = m + 1;
-        d.rowflag[j] = 1;
+        flag_row(d, j);
       };
       if (flat) {
         // Own list in stencil order: per cell, this run's insertions (chain,
@@ -3932,7 +4003,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
           }
           if (acc > p.mnb) raise_error(d.g, DML_E_NEIGH_OVERFLOW, slot);
           d.nn[slot] = acc > p.mnb ? p.mnb : acc;
-          d.rowflag[slot] = 1;
+          list_new_row(d, slot);
         }
         __syncthreads();
         int* row = d.list + (size_t)slot * p.mnb;
@@ -4052,7 +4123,6 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
         d.gorder[gp] = -1;
         sc->n_gcmc -= 1;
         d.nn[h] = 0;
-        d.rowflag[h] = 1;
         if (rk >= 0) {
           d.ref[rk] = -1;
           d.rank[h] = -1;
@@ -5303,7 +5373,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
       if (lane == 0) {
         if (cnt > p.mnb) raise_error(d.g, DML_E_NEIGH_OVERFLOW, slot);
         d.nn[slot] = cnt > p.mnb ? p.mnb : cnt;
-        d.rowflag[slot] = 1;  // a row written between full force scans
+        list_new_row(d, slot);  // an inserted atom's row, written between full force scans
       }
     }
   }
@@ -5362,7 +5432,6 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
     d.in_gcmc[h] = 0;
     d.gorder[B + S.del_pos[q]] = -1;
     d.nn[h] = 0;
-    d.rowflag[h] = 1;
     if (rk >= 0) {
       d.ref[rk] = -1;
       d.rank[h] = -1;
@@ -5405,7 +5474,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
       else raise_error(d.g, DML_E_NEIGH_OVERFLOW, j);
       if (before == cnt - 1) {
         d.nn[j] = min(S.app_base[e] + cnt, p.mnb);
-        d.rowflag[j] = 1;
+        flag_row(d, j);
       }
     }
   } else if (wid == 0) {
@@ -5419,7 +5488,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
         }
         d.list[(size_t)j * p.mnb + m] = B + S.ins_slot[k];
         d.nn[j] = m + 1;
-        d.rowflag[j] = 1;
+        flag_row(d, j);
       });
       __syncwarp();
     }
@@ -5564,7 +5633,8 @@ int k_force_pairs(const Dev& d, const KParams& p, int n_rank, bool near, cudaStr
   int n = 2;
   if (near && p.short_scan) {
     scan_mode_kernel<<<1, 256, 0, s>>>(d, p);
-    n += 1;
+    force_scan_listed_kernel<true><<<152 * 8, kBlock, 0, s>>>(d, p);
+    n += 2;
   }
   k_force_scan(d, p, n_rank, near, s);
   if (p.mixed)
