@@ -71,7 +71,8 @@ NWR = 100  # output cadence of the reference's tests (entrada.ini nwr)
 # around its point (24 B each; the cell volume is bounded below by
 # (rc + skin)^3, so the count is a lower bound).
 PHASE_KERNEL = {"integrate": ("ermak_a_kernel", "ion", 120.0),
-                "force_pairs": ("force_scan_span_kernel + force_exact_mixed_kernel", "ion", 24.0),
+                "force_pairs": ("scan_mode_kernel + force_scan_span_kernel / "
+                                "force_scan_listed_kernel + force_exact_mixed_kernel", "ion", 24.0),
                 "force_sum": ("force_touched_kernel + force_ref_kernel", "ion", 105.0),
                 "test_update1": ("pbc_dispmax_kernel + dispmax_exact_kernel", "ion", 48.0),
                 "overlap": ("overlap_count_kernel + overlap_comp_kernel", "ion", 48.0),

@@ -137,7 +137,6 @@ struct Global {
   int n_ftouch;             // entries of ftlist (mixed-form sums)
   int chunk_event;          // some replica added its chunk this step (bloques)
   int n_f;                  // entries of Dev::flist
-  unsigned int ticket_act;  // overlap_count blocks done (the last forms act_big_pre)
 };
 
 struct EvRec {            // one interacting list entry seen from one atom

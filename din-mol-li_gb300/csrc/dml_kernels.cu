@@ -2565,27 +2565,23 @@ __device__ __forceinline__ void overlap_count_at(Dev d, int n_rank, int rep, int
   atomicAdd(&d.comp_size[root], 1);
 }
 
-// The last block to finish forms the prefix of the listed members of the
-// replicas with more than kCompBlockMax of them (act_big_pre).
 __global__ void overlap_count_kernel(Dev d, int n_rank) {
   const int rep = block_rep(d);
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) overlap_count_at(d, n_rank, rep, span_pos(u));
-  __shared__ int s_last, s_carry;
+}
+
+// The prefix of the listed members of the replicas with more than
+// kCompBlockMax of them (act_big_pre), one block.
+__global__ void overlap_big_prefix_kernel(Dev d) {
+  __shared__ int s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd(&d.g->ticket_act, 1u) == gridDim.x - 1u;
-    s_carry = 0;
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
   for (int r0 = 0; r0 < d.nrep; r0 += blockDim.x) {
     const int r = r0 + threadIdx.x;
     int v = 0;
     if (r < d.nrep) {
-      v = __ldcg(d.pr_cnt + r * kCntStride + kCntAct);
+      v = d.pr_cnt[r * kCntStride + kCntAct];
       if (v <= kCompBlockMax) v = 0;
     }
     int tot;
@@ -2595,10 +2591,7 @@ __global__ void overlap_count_kernel(Dev d, int n_rank) {
     if (threadIdx.x == 0) s_carry += tot;
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    d.act_big_pre[d.nrep] = s_carry;
-    d.g->ticket_act = 0;
-  }
+  if (threadIdx.x == 0) d.act_big_pre[d.nrep] = s_carry;
 }
 
 // The replica of position g of the big replicas' listed members: the last
@@ -5760,6 +5753,7 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
   }
   if (detect) n += k_overlap_detect(d, p, n_rank, detect == 1 ? 1 : 0, s);
   overlap_count_kernel<<<nspan(n_rank), kBlock, 0, s>>>(d, n_rank);
+  overlap_big_prefix_kernel<<<1, 256, 0, s>>>(d);
   // replicas with many listed members: their bookkeeping on the whole grid
   overlap_assign_big_kernel<<<152 * 4, kBlock, 0, s>>>(d);
   overlap_scatter_big_kernel<<<152 * 4, kBlock, 0, s>>>(d);
@@ -5769,7 +5763,7 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
   // the per-replica kernel, the others in overlap_pass1_kernel
   overlap_comp_kernel<<<d.nrep, kBlock, 0, s>>>(d, p, all_passes);
   overlap_pass1_kernel<<<152 * 4, 128, 0, s>>>(d, p, all_passes);
-  n += 6;
+  n += 7;
   if (all_passes) return n;
   overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
   return n + 1;
