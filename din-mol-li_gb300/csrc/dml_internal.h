@@ -35,7 +35,8 @@ constexpr int kCntStride = 32, kCntGlist = 0, kCntAct = 1;  // pr_cnt layout
 // overlap_moveback's bookkeeping: a replica with at most this many listed
 // members is handled by one block (overlap_comp_kernel), a larger one by
 // grid kernels over all its listed members
-constexpr int kCompBlockMax = 2048;
+constexpr int kCompBlockMax = 4096;
+constexpr int kCompThreads = 512;   // overlap_comp_kernel's block
 constexpr int kCntGcmcPar = 2, kCntGcmcSeq = 3;  // gcmc_run calls per path (diagnostic)
 
 // Replicas.  A context holds one or more independent systems ("replicas",

@@ -5761,8 +5761,8 @@ int k_overlap(const Dev& d, const KParams& p, int n_rank, int n_slots, bool stan
   const int all_passes = p.prob >= 1.0;
   // with prob >= 1 the passes of a replica with few components run inside
   // the per-replica kernel, the others in overlap_pass1_kernel
-  overlap_comp_kernel<<<d.nrep, kBlock, 0, s>>>(d, p, all_passes);
-  overlap_pass1_kernel<<<152 * 4, 128, 0, s>>>(d, p, all_passes);
+  overlap_comp_kernel<<<d.nrep, kCompThreads, 0, s>>>(d, p, all_passes);
+  overlap_pass1_kernel<<<152 * 16, 128, 0, s>>>(d, p, all_passes);
   n += 7;
   if (all_passes) return n;
   overlap_passn_kernel<<<1, 1024, 0, s>>>(d, p);
