@@ -3006,13 +3006,22 @@ __device__ __forceinline__ void piston_at(Dev d, KParams p, int n_slots, int rep
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
   const int s = pos;
-  double z0 = sc->z0;
-  if (s < n_slots && d.state[s] == ST_LIVE) {
-    double4 P = d.pos[s];
-    if (P.z > z0) {
-      P.z = P.z - lohi * (P.z - z0);
-      d.pos[s] = P;
-      d.posf[s] = to_f4(P, d.typ[s]);
+  const double z0 = sc->z0;
+  // A slot is live exactly when its FP32 copy carries an element, and
+  // RN32(z) < RN32(z0) implies z < z0 (monotone rounding): only atoms at or
+  // above RN32(z0) read their FP64 z.  Only z changes, so the copy keeps its
+  // x, y and element.
+  if (s < n_slots) {
+    float4 f = d.posf[s];
+    if (elem_of(f) != 0 && !(f.z < (float)z0)) {
+      double* const pz = reinterpret_cast<double*>(d.pos + s) + 2;
+      const double z = *pz;
+      if (z > z0) {
+        const double zn = z - lohi * (z - z0);
+        *pz = zn;
+        f.z = f64_to_f32_rn(zn);
+        d.posf[s] = f;
+      }
     }
   }
   if (s == R.base) {
