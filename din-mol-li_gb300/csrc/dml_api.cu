@@ -217,6 +217,8 @@ void make_kparams(const dml_params& P, KParams& K) {
   K.prob = P.prob;
   K.h_over_tau = P.h / P.tau;
   K.ztop_is_z1 = P.reservoir == DML_RESERVOIR_CHUNKS ? 1.0 : 0.0;
+  // piston: the step's second pbc_dispmax takes calc_rho's slab count
+  K.rho_fused = P.reservoir == DML_RESERVOIR_PISTON;
   K.rcut_b = P.rc + P.skin;
   K.rhomedia = 5.775329e-4;  // dana.F90:445
   K.chunk_dist = 0.0;
@@ -453,7 +455,7 @@ int enqueue_step(dml_ctx* c, cudaEvent_t* ev, bool capture, int* n_base, int* n_
   mark(DML_PHASE_GCMC);
   if (c->P.reservoir == DML_RESERVOIR_GCMC) n += k_gcmc_trials(d, k, s);
   mark(DML_PHASE_RHO_PISTON);
-  n += k_calc_rho(d, k, cap, s);
+  if (!k.rho_fused) n += k_calc_rho(d, k, cap, s);  // else taken by the second test_update
   if (c->P.reservoir == DML_RESERVOIR_PISTON) n += k_piston(d, k, cap, s);
   if (c->P.reservoir == DML_RESERVOIR_CHUNKS && (rc = queue_bloques(c, capture, &n, &nb)) != 0)
     return rc;
@@ -918,6 +920,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   d.nblk_part = cap / kBlock + 1;
   AL(d.part, 2 * (size_t)d.nblk_part);
   AL(d.part1, 2 * (size_t)d.nblk_part);
+  AL(d.part_cnt, 2 * (size_t)d.nblk_part);
   AL(d.dirty, (size_t)d.nblk_part);
   AL(d.sc, nrep);
   AL(d.g, 1);

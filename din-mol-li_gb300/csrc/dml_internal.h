@@ -177,6 +177,7 @@ struct KParams {
   double prob;
   double h_over_tau;
   double ztop_is_z1;        // chunks: calc_rho uses z1
+  int rho_fused;            // piston: calc_rho's count taken by the step's second pbc_dispmax
   // chunk reservoir (bloques, dana.F90:716-773): chunk height, the density
   // it keeps (rhomedia, dana.F90:445) and the cell edge bound rc + skin
   double chunk_dist, rhomedia, rcut_b;
@@ -300,6 +301,7 @@ struct Dev {
   // first one (part1, two float bit patterns per block), and the blocks
   // where overlap_moveback moved an atom since (dirty)
   unsigned* part1;
+  int* part_cnt;       // 2 per block: the reservoir-slab count of the first pass, of the current one
   int* dirty;
   // replicas
   Scalars* sc;        // [nrep] per-replica state

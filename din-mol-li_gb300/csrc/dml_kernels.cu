@@ -1457,6 +1457,26 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
     Ofu[u] = in ? d.posf_old[s] : make_float4(0.f, 0.f, 0.f, 0.f);
     live[u] = in && elem_of(Pfu[u]) != 0;
   }
+  // With rho_fused (piston), calc_rho's count of live atoms in (z0, zt) is
+  // taken here: z changes only by the integrator, overlap_moveback (dirty
+  // blocks) and the piston, which follows calc_rho, so the step's second call
+  // has calc_rho's positions and a clean block keeps the first call's count.
+  int cnt = 0;
+  const double cz0 = sc->z0, czt = sc->zmax;
+  if (p.rho_fused) {
+    const float z0f = (float)cz0, ztf = (float)czt;
+#pragma unroll
+    for (int u = 0; u < kSlotU; ++u) {
+      if (!live[u]) continue;
+      const float zf = Pfu[u].z;  // z in (z0, zt) from the FP32 copy (monotone rounding)
+      if (zf > z0f && zf < ztf) {
+        cnt += 1;
+      } else if (!(zf < z0f || zf > ztf)) {
+        const double z = d.pos[span_pos(u)].z;
+        cnt += (z > cz0 && z < czt) ? 1 : 0;
+      }
+    }
+  }
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) {
   const int s = span_pos(u);
@@ -1512,25 +1532,39 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
     float b1 = __shfl_down_sync(0xffffffffu, a1, off);
     float b2 = __shfl_down_sync(0xffffffffu, a2, off);
     top2f(a1, a2, b1, b2);
+    cnt += __shfl_down_sync(0xffffffffu, cnt, off);
   }
   __shared__ float w1[32], w2[32];
+  __shared__ int wc[32];
   __shared__ unsigned long long x1[32], x2[32];
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nwarp = blockDim.x >> 5;
   if (lane == 0) {
     w1[wid] = a1;
     w2[wid] = a2;
+    wc[wid] = cnt;
   }
   __syncthreads();
   __shared__ bool last;
   if (threadIdx.x == 0) {
     float b1 = tinyf, b2 = tinyf;
-    for (int w = 0; w < nwarp; ++w) top2f(b1, b2, w1[w], w2[w]);
+    int c = 0;
+    for (int w = 0; w < nwarp; ++w) {
+      top2f(b1, b2, w1[w], w2[w]);
+      c += wc[w];
+    }
     d.part[2 * blockIdx.x] = __float_as_uint(b1);
     d.part[2 * blockIdx.x + 1] = __float_as_uint(b2);
     if (!second) {
       d.part1[2 * blockIdx.x] = __float_as_uint(b1);
       d.part1[2 * blockIdx.x + 1] = __float_as_uint(b2);
+    }
+    if (p.rho_fused) {
+      // a clean block of the second call: the first call's count
+      if (second && (int)blockIdx.x * kSpan < n_slots && d.dirty[blockIdx.x] == 0)
+        c = d.part_cnt[2 * blockIdx.x];
+      if (!second) d.part_cnt[2 * blockIdx.x] = c;
+      d.part_cnt[2 * blockIdx.x + 1] = c;
     }
     __threadfence();
     unsigned t = atomicAdd(&sc->ticket, 1u);
@@ -1556,6 +1590,20 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
     w2[wid] = b2;
   }
   __syncthreads();
+  if (p.rho_fused && second) {  // calc_rho (dana.F90:521-549) of the replica
+    __shared__ int s_c;
+    if (threadIdx.x == 0) s_c = 0;
+    __syncthreads();
+    int c = 0;
+    for (int b = b0 + threadIdx.x; b < b0 + R.nblk; b += blockDim.x)
+      c += __ldcg(d.part_cnt + 2 * b + 1);
+    if (c) atomicAdd(&s_c, c);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const double vol = R.box[0] * R.box[1] * (czt - cz0);
+      sc->rho = (double)s_c / vol;
+    }
+  }
   if (threadIdx.x == 0) {
     float F1 = tinyf, F2 = tinyf;
     for (int w = 0; w < nwarp; ++w) top2f(F1, F2, w1[w], w2[w]);
