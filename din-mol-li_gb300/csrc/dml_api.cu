@@ -895,6 +895,7 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   const bool mixed = c->P.precision == DML_PRECISION_MIXED;
   AL(d.facc, mixed ? 4 * (size_t)cap : 4);
   AL(d.ftouch, mixed ? (size_t)cap / 32 + 1 : 1);
+  AL(d.fnz, mixed ? (size_t)cap / 32 + 1 : 1);
   AL(d.ftlist, mixed ? (size_t)cap : 1);
   AL(d.flist, cap);
   AL(d.cand, (size_t)c->K.cand_cap);
@@ -1191,6 +1192,10 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
     what = "load_atoms_kernel launch";
     k_load_atoms(d, c->K, in, st);
     e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && c->K.mixed) {  // loaded forces may be nonzero anywhere
+    what = "cudaMemsetAsync (force bits)";
+    e = cudaMemsetAsync(d.fnz, 0xFF, sizeof(unsigned) * ((size_t)d.cap / 32 + 1), st);
   }
   if (e == cudaSuccess) {
     what = "load_atoms_kernel";

@@ -266,6 +266,10 @@ struct Dev {
   // mixed form: the slots whose accumulators received a pair this call,
   // one bit per slot (ftouch) and listed once each (ftlist, Global::n_ftouch)
   unsigned* ftouch;
+  // chosen form: one bit per slot, set where force/epot may be nonzero (written
+  // by a sum, an insertion or a load); force_ref writes the zeros of a member
+  // with no pair only where the bit is set
+  unsigned* fnz;
   int* ftlist;
   // hs slots whose element became F (captured) since the last capture commit
   int* flist;

@@ -1337,6 +1337,7 @@ __global__ void force_touched_kernel(Dev d, KParams p) {
     }
     d.force[s] = F;
     d.epot[s] = ep;
+    if (inref) atomicOr(&d.fnz[s >> 5], 1u << (s & 31));
     if (FUSE_B && inref) ermak_b_atom_mixed(d, p, s, d.typ[s], (float)F.x, (float)F.y, (float)F.z);
   }
 }
@@ -1350,8 +1351,11 @@ __device__ __forceinline__ void force_ref_at(const Dev& d, const KParams& p, int
     atomicAnd(&d.ftouch[h >> 5], ~bit);
     return;
   }
-  d.force[h] = make_double4(0.0, 0.0, 0.0, 0.0);
-  d.epot[h] = 0.0;
+  if (d.fnz[h >> 5] & bit) {  // zero where a force may stand; elsewhere it is zero already
+    d.force[h] = make_double4(0.0, 0.0, 0.0, 0.0);
+    d.epot[h] = 0.0;
+    atomicAnd(&d.fnz[h >> 5], ~bit);
+  }
   if (FUSE_B) ermak_b_atom_mixed(d, p, h, d.typ[h], 0.0f, 0.0f, 0.0f);
 }
 
@@ -3938,6 +3942,7 @@ __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, in
         const double te = d.epot[href];
         d.vel[slot] = tv;
         d.force[slot] = tf;
+        if (p.mixed) atomicOr(&d.fnz[slot >> 5], 1u << (slot & 31));
         d.acel[slot] = ta;
         d.epot[slot] = te;
         d.typ[slot] = (int8_t)typ;
@@ -5442,6 +5447,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
       d.vel[slot] = make_double4(S.fvel[k].x, S.fvel[k].y, S.fvel[k].z, 0.0);
     }
     d.force[slot] = tf;
+    if (p.mixed) atomicOr(&d.fnz[slot >> 5], 1u << (slot & 31));
     d.acel[slot] = ta;
     d.epot[slot] = te;
     d.typ[slot] = (int8_t)typ;
