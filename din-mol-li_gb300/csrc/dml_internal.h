@@ -26,6 +26,17 @@ namespace dml {
 
 enum { ST_NULL = 0, ST_LIVE = 1, ST_LIMBO = 2 };
 
+// The first statement of every kernel.  In the step graphs the edges between
+// kernels are programmatic (dml_api.cu, programmatic_edges): a kernel may be
+// launched before the kernel it follows has completed, and waits here until
+// that kernel's writes are visible.  Without such an edge (eager launches)
+// the wait returns at once.
+#if defined(__CUDA_ARCH__)
+#define DML_GRID_WAIT() asm volatile("griddepcontrol.wait;" ::: "memory")
+#else
+#define DML_GRID_WAIT() ((void)0)
+#endif
+
 constexpr int kNearCap = 32;   // near-contact entries per atom (overlap)
 constexpr int kBlock = 256;
 constexpr int kSlotU = 4;                 // positions per thread of the per-position kernels

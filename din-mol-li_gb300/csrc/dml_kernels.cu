@@ -218,6 +218,7 @@ __device__ __forceinline__ bool in_tessellation(const RepConst& R, double4 P) {
 // Prefix of the replicas' rows in use (one block): the warp-per-row kernels
 // walk only the rows in use, the capacity headroom of every replica skipped.
 __global__ void rank_prefix_kernel(Dev d) {
+  DML_GRID_WAIT();
   __shared__ int ws[32];
   __shared__ int carry;
   if (threadIdx.x == 0) carry = 0;
@@ -295,6 +296,7 @@ __device__ __forceinline__ int warp_id_global() {
 // overlap search, and whether its near lists still need a search of their
 // own (always with the Brownian integrator, which has no force scan).
 __global__ void step_begin_kernel(Dev d, int near_stale) {
+  DML_GRID_WAIT();
   Global* g = d.g;
   if (threadIdx.x == 0) {
     g->step += 1;
@@ -589,6 +591,7 @@ __device__ __forceinline__ unsigned ermak_a_at(const Dev& d, const KParams& p, i
 // with both at four blocks per SM (spills).
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock, MIXED ? 4 : 3) ermak_a_kernel(Dev d, KParams p, int n_rank) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
   const int end = d.rc[rep].base + d.sc[rep].n_slots;
   if ((int)blockIdx.x * kSpan >= end) return;
@@ -712,6 +715,7 @@ __device__ __forceinline__ unsigned brownian_at(const Dev& d, const KParams& p, 
 // hs%ref entries and the replica's scalars read first, as in ermak_a.
 template <bool MIXED>
 __global__ void __launch_bounds__(kBlock, 4) brownian_kernel(Dev d, KParams p, int n_rank) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
   const int end = d.rc[rep].base + d.sc[rep].n_slots;
   if ((int)blockIdx.x * kSpan >= end) return;
@@ -870,6 +874,7 @@ __device__ __forceinline__ bool force_scan_row(const Dev& d, const KParams& p, i
 // comes from the replicas' prefix of rows in use.
 template <bool NEAR, int L>
 __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   const int nw = gridDim.x * (blockDim.x >> 5);
   const int total = d.rank_pre[d.nrep];
   const int sub = (threadIdx.x & 31) / L;
@@ -891,6 +896,7 @@ __global__ void __launch_bounds__(256) force_scan_kernel(Dev d, KParams p) {
 // their membership, positions and list lengths loaded up front.
 template <bool NEAR>
 __global__ void __launch_bounds__(kBlock) force_scan_span_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
   const int end = d.rc[rep].base + d.sc[rep].n_slots;
   if ((int)blockIdx.x * kSpan >= end) return;  // whole block: warps stay full
@@ -942,6 +948,7 @@ __global__ void __launch_bounds__(kBlock) force_scan_span_kernel(Dev d, KParams 
 // Rows whose atom left hs%ref since (captures, deletions) are skipped.
 template <bool NEAR>
 __global__ void __launch_bounds__(kBlock) force_scan_listed_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   const int total = d.sl_pre[d.nrep];
   const int nw = gridDim.x * (blockDim.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -993,6 +1000,7 @@ __device__ __forceinline__ void list_new_row(const Dev& d, int h) {
 __device__ int blk_scan_excl(int v, int* total);
 
 __global__ void scan_mode_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   const float delta = sqrtf(__uint_as_float(d.g->delta2f_bits));
   __shared__ int s_carry;
   if (threadIdx.x == 0) s_carry = 0;
@@ -1039,6 +1047,7 @@ __global__ void scan_mode_kernel(Dev d, KParams p) {
 // Every replica's next force scan is full (lists or positions changed outside
 // the step sequence).
 __global__ void scan_invalidate_kernel(Dev d) {
+  DML_GRID_WAIT();
   for (int r = threadIdx.x; r < d.nrep; r += blockDim.x) d.sc[r].sl_full = 1;
 }
 
@@ -1046,6 +1055,7 @@ __global__ void scan_invalidate_kernel(Dev d) {
 // thread per entry, recording each interacting entry for both atoms with the
 // key (rank, jj) that orders the reference's accumulation.
 __global__ void force_exact_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   int nc = d.g->n_cand;
   if (nc > p.cand_cap) {
     if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(d.g, DML_E_EVENT_OVERFLOW, nc);
@@ -1200,6 +1210,7 @@ __device__ __forceinline__ void force_sum_at(Dev d, KParams p, int n_slots, int 
 
 template <bool FUSE_B>
 __global__ void force_sum_kernel(Dev d, KParams p, int n_slots) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) force_sum_at<FUSE_B>(d, p, n_slots, rep, span_pos(u));
@@ -1220,6 +1231,7 @@ __device__ __forceinline__ void ermak_b_at(Dev d, KParams p, int n_rank, int rep
 }
 
 __global__ void ermak_b_kernel(Dev d, KParams p, int n_rank) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) ermak_b_at(d, p, n_rank, rep, span_pos(u));
@@ -1246,6 +1258,7 @@ __device__ __forceinline__ void touch_slot(const Dev& d, int h) {
 }
 
 __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   int nc = d.g->n_cand;
   if (nc > p.cand_cap) {
     if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(d.g, DML_E_EVENT_OVERFLOW, nc);
@@ -1311,6 +1324,7 @@ __global__ void force_exact_mixed_kernel(Dev d, KParams p) {
 // electrode slots.
 template <bool FUSE_B>
 __global__ void force_touched_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   const int nt = d.g->n_ftouch;
   const double inv = p.fix_inv;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nt; q += gridDim.x * blockDim.x) {
@@ -1361,6 +1375,7 @@ __device__ __forceinline__ void force_ref_at(const Dev& d, const KParams& p, int
 
 template <bool FUSE_B>
 __global__ void force_ref_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     d.g->n_cand = 0;
@@ -1430,6 +1445,7 @@ __device__ __forceinline__ void decide_rebuild(const Dev& d, Scalars* sc, int re
 // and every displacement is 0).  Dirty blocks are recomputed in full.
 __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p, int n_slots,
                                                                  int second) {
+  DML_GRID_WAIT();
   // grids are sized by capacity; the block's replica gives the live count
   const int rep = block_rep(d);
   const RepConst& R = d.rc[rep];
@@ -1632,6 +1648,7 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
 // opens the rebuild subgraph if any.
 __global__ void dispmax_exact_kernel(Dev d, KParams p, int cond,
                                      cudaGraphConditionalHandle cond_handle) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
@@ -1837,6 +1854,7 @@ __device__ __forceinline__ void rebuild_prep_at(Dev d, KParams p, int n_slots, i
 }
 
 __global__ void rebuild_prep_kernel(Dev d, KParams p, int n_slots, int n_b, int cells_only) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) rebuild_prep_at(d, p, n_slots, n_b, cells_only, rep, span_pos(u));
@@ -1890,6 +1908,7 @@ __device__ __forceinline__ bool gcmc_sorts(const Dev& d, int rep, int par) {
 // every cell and the sentinel after the last; the sort for gcmc_run covers
 // the runs of z layers its searches reach, each followed by its end.
 __global__ void cell_scan_kernel(Dev d, int force, int par) {
+  DML_GRID_WAIT();
   const RepConst& R = d.rc[blockIdx.x];
   const Scalars* sc = d.sc + blockIdx.x;
   if (!R.use_cells) return;
@@ -1927,6 +1946,7 @@ __device__ __forceinline__ void cell_scatter_at(Dev d, int n_b, int force, int r
 }
 
 __global__ void cell_scatter_kernel(Dev d, int n_b, int force) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) cell_scatter_at(d, n_b, force, rep, span_pos(u));
@@ -2028,6 +2048,7 @@ __device__ void cell_order_chunk(const Dev& d, const RepConst& R, int force, int
 }
 
 __global__ void cell_order_small_kernel(Dev d, int force, int par) {
+  DML_GRID_WAIT();
   if (!force && !d.g->any_rebuild) return;
   const int rep = d.cch_rep[blockIdx.x];
   const RepConst& R = d.rc[rep];
@@ -2082,6 +2103,7 @@ __device__ __forceinline__ void reb_chunk(const Dev& d, int g, int& rep, int& q)
 // replica's chunks (from its first cell_atoms place, with the sentinel
 // cell's start), and each chunk's own prefix.
 __global__ void cell_chunk_sum_kernel(Dev d) {
+  DML_GRID_WAIT();
   __shared__ int ws[kBlock / 32];
   const int total = d.rebc_pre[d.nrep];
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
@@ -2107,6 +2129,7 @@ __global__ void cell_chunk_sum_kernel(Dev d) {
 }
 
 __global__ void cell_chunk_scan_kernel(Dev d) {
+  DML_GRID_WAIT();
   const int rep = blockIdx.x;
   const RepConst& R = d.rc[rep];
   if (!R.use_cells || !d.sc[rep].rebuild) return;
@@ -2128,6 +2151,7 @@ __global__ void cell_chunk_scan_kernel(Dev d) {
 }
 
 __global__ void cell_chunk_fill_kernel(Dev d) {
+  DML_GRID_WAIT();
   const int total = d.rebc_pre[d.nrep];
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
     int rep, q;
@@ -2156,6 +2180,7 @@ __global__ void cell_chunk_fill_kernel(Dev d) {
 
 // The rebuild's in-cell order over the same chunks.
 __global__ void cell_order_reb_kernel(Dev d) {
+  DML_GRID_WAIT();
   const int total = d.rebc_pre[d.nrep];
   for (int g = blockIdx.x; g < total; g += gridDim.x) {
     int rep, q;
@@ -2169,6 +2194,7 @@ __global__ void cell_order_reb_kernel(Dev d) {
 // leaves at once unless the replica's trials run sequentially (the rare
 // case, where its chunks are ordered one after another).
 __global__ void gcmc_order_kernel(Dev d) {
+  DML_GRID_WAIT();
   const int rep = blockIdx.x;
   const RepConst& R = d.rc[rep];
   if (!R.use_cells || !gcmc_sorts(d, rep, 1)) return;
@@ -2176,6 +2202,7 @@ __global__ void gcmc_order_kernel(Dev d) {
 }
 
 __global__ void cell_order_big_kernel(Dev d, int force) {
+  DML_GRID_WAIT();
   if (!force && !d.g->any_rebuild) return;
   const int nw = gridDim.x * (blockDim.x >> 5);
   const int nb = d.g->n_big;
@@ -2359,6 +2386,7 @@ __device__ __forceinline__ int list_cells_row_thread(const Dev& d, const KParams
 }
 
 __global__ void __launch_bounds__(256) list_cells_thread_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   const int total = d.reb_pre[d.nrep];  // rows of the replicas that rebuild
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
     const int r = row_rank_in(d, d.reb_pre, i);
@@ -2373,6 +2401,7 @@ __global__ void __launch_bounds__(256) list_cells_thread_kernel(Dev d, KParams p
 }
 
 __global__ void __launch_bounds__(256) list_cells_kernel(Dev d, KParams p, int n_rank) {
+  DML_GRID_WAIT();
   __shared__ int tab[8][56];  // per warp: the stencil cells' starts and prefixes
   const int nw = gridDim.x * (blockDim.x >> 5);
   const int total = d.reb_pre[d.nrep];  // rows of the replicas that rebuild
@@ -2433,6 +2462,7 @@ __device__ __forceinline__ void list_verlet_row(const Dev& d, const KParams& p, 
 }
 
 __global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
+  DML_GRID_WAIT();
   const int nw = gridDim.x * (blockDim.x >> 5);
   const int total = d.reb_pre[d.nrep];  // rows of the replicas that rebuild
   for (int i = warp_id_global(); i < total; i += nw)
@@ -2440,6 +2470,7 @@ __global__ void list_verlet_kernel(Dev d, KParams p, int n_rank, int n_b) {
 }
 
 __global__ void rebuild_done_kernel(Dev d) {
+  DML_GRID_WAIT();
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r == 0) {
     if (d.g->any_rebuild) d.g->list_builds += 1;
@@ -2459,7 +2490,10 @@ __global__ void rebuild_done_kernel(Dev d) {
 // commute, so each component is replayed in rank order by one thread and
 // gives exactly the reference's result.
 
-__global__ void delta_reset_kernel(Global* g) { g->delta2f_bits = 0u; }
+__global__ void delta_reset_kernel(Global* g) {
+  DML_GRID_WAIT();
+  g->delta2f_bits = 0u;
+}
 
 // Resets the component state and takes delta = max |pos - old_cg| over the
 // moving atoms (positions after the integrator; they do not change until
@@ -2499,6 +2533,7 @@ __device__ __forceinline__ void overlap_init_at(Dev d, KParams p, int n_slots, i
 }
 
 __global__ void overlap_init_kernel(Dev d, KParams p, int n_slots) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) overlap_init_at(d, p, n_slots, rep, span_pos(u));
@@ -2579,6 +2614,7 @@ __device__ __forceinline__ void overlap_detect_rows(const Dev& d, const KParams&
 // scan, for the replicas that rebuilt; 2: the replicas that rebuilt.
 template <int L>
 __global__ void __launch_bounds__(256) overlap_detect_kernel(Dev d, KParams p, int mode) {
+  DML_GRID_WAIT();
   if (mode == 1 && !d.g->near_stale) return;  // the force scan found them
   const int nw = gridDim.x * (blockDim.x >> 5);
   // modes 1 and 2 walk only the rows of the replicas that rebuilt
@@ -2618,6 +2654,7 @@ __device__ __forceinline__ void overlap_count_at(Dev d, int n_rank, int rep, int
 }
 
 __global__ void overlap_count_kernel(Dev d, int n_rank) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) overlap_count_at(d, n_rank, rep, span_pos(u));
@@ -2626,6 +2663,7 @@ __global__ void overlap_count_kernel(Dev d, int n_rank) {
 // The prefix of the listed members of the replicas with more than
 // kCompBlockMax of them (act_big_pre), one block.
 __global__ void overlap_big_prefix_kernel(Dev d) {
+  DML_GRID_WAIT();
   __shared__ int s_carry;
   if (threadIdx.x == 0) s_carry = 0;
   __syncthreads();
@@ -2702,6 +2740,7 @@ __device__ __forceinline__ void overlap_assign_at(const Dev& d, int end, int i,
 // scattered, the members in rank order (each member's place is the number
 // of smaller ranks in its component).
 __global__ void overlap_assign_big_kernel(Dev d) {
+  DML_GRID_WAIT();
   const int total = d.act_big_pre[d.nrep];
   const int nw = gridDim.x * (blockDim.x >> 5);
   for (int w = warp_id_global(); 32 * w < total; w += nw) {
@@ -2723,6 +2762,7 @@ __device__ __forceinline__ int big_act_entry(const Dev& d, int g) {
 }
 
 __global__ void overlap_scatter_big_kernel(Dev d) {
+  DML_GRID_WAIT();
   const int total = d.act_big_pre[d.nrep];
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
     const int r = big_act_entry(d, g);
@@ -2732,6 +2772,7 @@ __global__ void overlap_scatter_big_kernel(Dev d) {
 }
 
 __global__ void overlap_order_big_kernel(Dev d) {
+  DML_GRID_WAIT();
   const int total = d.act_big_pre[d.nrep];
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
     const int r = big_act_entry(d, g);
@@ -2850,6 +2891,7 @@ __device__ void overlap_pass1_comp(const Dev& d, const KParams& p, int all_passe
 // whose grid spreads them over every SM (comp_defer); one with more than
 // kCompBlockMax listed members was handled by the _big kernels.
 __global__ void overlap_comp_kernel(Dev d, KParams p, int passes) {
+  DML_GRID_WAIT();
   const int rep = blockIdx.x;
   const int base = d.rc[rep].base;
   const int end = base + d.pr_cnt[rep * kCntStride + kCntAct];
@@ -2896,6 +2938,7 @@ __global__ void overlap_comp_kernel(Dev d, KParams p, int passes) {
 // every pass, and only the components of replicas that overlap_comp_kernel
 // left to this kernel.
 __global__ void overlap_pass1_kernel(Dev d, KParams p, int all_passes) {
+  DML_GRID_WAIT();
   const int ncomp = d.g->n_comp;
   for (int cid = blockIdx.x * blockDim.x + threadIdx.x; cid < ncomp;
        cid += gridDim.x * blockDim.x) {
@@ -2912,6 +2955,7 @@ __global__ void overlap_pass1_kernel(Dev d, KParams p, int all_passes) {
 // alone: a component is examined in pass p only if its replica's pass p-1
 // moved an atom.
 __global__ void overlap_passn_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   __shared__ int again_s;
   __shared__ int go;
   int ncomp = d.g->n_comp;
@@ -2986,6 +3030,7 @@ __device__ __forceinline__ void commit_at(Dev d, int h) {
 // chunk attachment), one block: captures are few, and the block empties
 // the list when it is done.
 __global__ void commit_kernel(Dev d) {
+  DML_GRID_WAIT();
   const int n = min(d.g->n_f, d.cap);
   for (int q = threadIdx.x; q < n; q += blockDim.x) commit_at(d, d.flist[q]);
   __syncthreads();
@@ -2994,6 +3039,7 @@ __global__ void commit_kernel(Dev d) {
 
 // calc_rho (dana.F90:521-549): integer count, so any reduction order is exact.
 __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
+  DML_GRID_WAIT();
   // grids are sized by capacity; the block's replica gives the live count
   const int rep = block_rep(d);
   const RepConst& R = d.rc[rep];
@@ -3085,6 +3131,7 @@ __device__ __forceinline__ void piston_at(Dev d, KParams p, int n_slots, int rep
 }
 
 __global__ void piston_kernel(Dev d, KParams p, int n_slots) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
   __shared__ double s_lohi;
   if (threadIdx.x == 0) {
@@ -3145,6 +3192,7 @@ __device__ void tessellate_height(RepConst& R, const KParams& p, double bz) {
 // and element), the template rises, the box height becomes zmax and the
 // list is marked stale, so that the test_update after it rebuilds.
 __global__ void bloques_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   const int rep = blockIdx.x;
   if (threadIdx.x != 0) return;
   Scalars* sc = d.sc + rep;
@@ -3238,6 +3286,7 @@ __global__ void bloques_kernel(Dev d, KParams p) {
 }
 
 __global__ void chunk_cond_kernel(Global* g, cudaGraphConditionalHandle h) {
+  DML_GRID_WAIT();
   cudaGraphSetConditional(h, g->chunk_event ? 1u : 0u);
 }
 
@@ -3389,6 +3438,7 @@ __device__ __forceinline__ bool in_slab(double z, double z0, double zmax) {
 // the bit words past the used gcmc%alist positions (appends set bits there)
 // are cleared.
 __global__ void gcmc_prep_kernel(Dev d, KParams p, int par) {
+  DML_GRID_WAIT();
   const int rep = blockIdx.x;
   const RepConst& R = d.rc[rep];
   Scalars* const sc = d.sc + rep;
@@ -3542,6 +3592,7 @@ __device__ __forceinline__ void gcmc_member_words(const Dev& d, int rep) {
 }
 
 __global__ void gcmc_bin_kernel(Dev d, int par) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
   if (blockIdx.x == 0 && threadIdx.x == 0) d.g->n_big = 0;  // cell_order's list
 #pragma unroll
@@ -3552,6 +3603,7 @@ __global__ void gcmc_bin_kernel(Dev d, int par) {
 // The same two passes, one block per replica (the parallel trials: most
 // replicas leave at once).
 __global__ void gcmc_count_rep_kernel(Dev d) {
+  DML_GRID_WAIT();
   const int rep = blockIdx.x;
   if (!gcmc_sorts(d, rep, 1)) return;
   const int B = d.rc[rep].base, end = B + d.pr_cnt[rep * kCntStride + kCntGlist];
@@ -3559,6 +3611,7 @@ __global__ void gcmc_count_rep_kernel(Dev d) {
 }
 
 __global__ void gcmc_scatter_rep_kernel(Dev d) {
+  DML_GRID_WAIT();
   const int rep = blockIdx.x;
   if (!gcmc_sorts(d, rep, 1)) return;
   const int B = d.rc[rep].base, end = B + d.pr_cnt[rep * kCntStride + kCntGlist];
@@ -3570,6 +3623,7 @@ __global__ void gcmc_scatter_rep_kernel(Dev d) {
 
 // The cell counts of the sequentially run replicas' listed atoms.
 __global__ void gcmc_count_kernel(Dev d, int par) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
   if (!gcmc_sorts(d, rep, par)) return;
   const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntGlist];
@@ -3583,6 +3637,7 @@ __global__ void gcmc_count_kernel(Dev d, int par) {
 // Scatter pass over each sorting replica's listed atoms (cell_atoms holds
 // hs%b slots until cell_order turns them into hs slots).
 __global__ void gcmc_scatter_kernel(Dev d, int par) {
+  DML_GRID_WAIT();
   const int rep = block_rep(d);
   if (!gcmc_sorts(d, rep, par)) return;
   const int end = d.rc[rep].base + d.pr_cnt[rep * kCntStride + kCntGlist];
@@ -3665,6 +3720,7 @@ __device__ __forceinline__ int stencil_cell(const RepConst& R, float4 Pf, const 
 // velocity) are tracked across trials.  Replicas without cells, or with an
 // atom in a halo cell, scan the whole group as the reference does.
 __global__ void __launch_bounds__(kGcmcThreads) gcmc_kernel(Dev d, KParams p, int par) {
+  DML_GRID_WAIT();
   if (par && d.grp[blockIdx.x].fast) return;  // decided by gcmc_fast_kernel
   if (threadIdx.x == 0) d.pr_cnt[blockIdx.x * kCntStride + kCntGcmcSeq] += 1;
   // dynamic shared memory: the trials, then in-slab members per gorder chunk
@@ -4305,6 +4361,7 @@ __device__ int blk_collect(int lo, int hi, int want, Pred free_at, int* out, int
 }
 
 __global__ void __launch_bounds__(kGcmcPreThreads) gcmc_pre_kernel(Dev d, KParams p) {
+  DML_GRID_WAIT();
   const int rep = blockIdx.x;
   const RepConst& R = d.rc[rep];
   Scalars* const sc = d.sc + rep;
@@ -4912,6 +4969,7 @@ __device__ void gcmc_append_targets(const Dev& d, const KParams& p, const RepCon
 
 __global__ void __launch_bounds__(kGcmcFastThreads)
     gcmc_fast_kernel(Dev d, KParams p, int wmax, int gmax, int words_smem) {
+  DML_GRID_WAIT();
   const int rep = blockIdx.x;
   const GcmcRepPre* const gr = d.grp + rep;
   if (!gr->fast) return;
@@ -5557,6 +5615,7 @@ __global__ void __launch_bounds__(kGcmcFastThreads)
 // every loaded atom's slot (hs slot = hs%b slot = sys%alist position) from
 // the compact input.  Positions left unused keep the -1 / zero fill.
 __global__ void load_rep_kernel(Dev d) {
+  DML_GRID_WAIT();
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < d.cap; q += gridDim.x * blockDim.x) {
     int lo = 0, hi = d.nrep - 1;  // largest replica whose base is <= q
     while (lo < hi) {
@@ -5568,6 +5627,7 @@ __global__ void load_rep_kernel(Dev d) {
 }
 
 __global__ void load_atoms_kernel(Dev d, KParams p, LoadIn in) {
+  DML_GRID_WAIT();
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < in.n_tot; i += gridDim.x * blockDim.x) {
     int lo = 0, hi = d.nrep - 1;  // replica of compact atom i
     while (lo < hi) {
@@ -5631,6 +5691,7 @@ inline int nblk_rows(int rows) { int b = nblk_warps(rows); return b < kRowGrid ?
 
 // Overwrites a buffer larger than L2 (benchmark L2 flush between steps).
 __global__ void flush_kernel(uint4* buf, size_t n) {
+  DML_GRID_WAIT();
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   size_t stride = (size_t)gridDim.x * blockDim.x;
   for (; i < n; i += stride) buf[i] = make_uint4((unsigned)i, 0u, 0u, 0u);
@@ -5946,6 +6007,7 @@ int k_flush(void* buf, size_t bytes, cudaStream_t s) {
 namespace dml {
 __global__ void check_conversions_kernel(const double* x, float* f32, double* back,
                                          long long n) {
+  DML_GRID_WAIT();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
     const float f = f64_to_f32_rn(x[i]);
@@ -5956,6 +6018,7 @@ __global__ void check_conversions_kernel(const double* x, float* f32, double* ba
 
 __global__ void check_pick_kernel(const unsigned long long* k, const int* n, int* m,
                                   long long count) {
+  DML_GRID_WAIT();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count;
        i += (long long)gridDim.x * blockDim.x)
     m[i] = gcmc_pick_index(k[i], n[i]);
@@ -5963,6 +6026,7 @@ __global__ void check_pick_kernel(const unsigned long long* k, const int* n, int
 
 __global__ void check_normals_kernel(const unsigned* w, float* out, long long n_pairs,
                                      int fast) {
+  DML_GRID_WAIT();
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_pairs;
        i += (long long)gridDim.x * blockDim.x) {
     if (fast)
@@ -5987,6 +6051,7 @@ int k_check_pick(const unsigned long long* k, const int* n, int* m, long long co
 // rounds of the block, numbering the live entries by a block scan, and
 // writes each live atom's requested members at its place in the output.
 __global__ void pack_atoms_kernel(Dev d, KParams p, PackOut o) {
+  DML_GRID_WAIT();
   const int rep = blockIdx.x;
   const int B = d.rc[rep].base, nal = d.sc[rep].n_alist;
   const long long base = o.off[rep];
@@ -6063,6 +6128,7 @@ int k_pack_atoms(const Dev& d, const KParams& p, const PackOut& o, cudaStream_t 
 // the non-CG ones.  Thread 0 writes the record and resets try and depo.
 __global__ void __launch_bounds__(1024) salida_kernel(Dev d, KParams p, double kb,
                                                       dml_observables* out) {
+  DML_GRID_WAIT();
   const int rep = blockIdx.x;
   const int B = d.rc[rep].base, nal = d.sc[rep].n_alist;
   __shared__ double s_e[1024], s_v[1024];

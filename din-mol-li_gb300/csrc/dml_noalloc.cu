@@ -77,6 +77,7 @@ struct NoallocParams {
 };
 
 __global__ void noalloc_clear_kernel(NoallocScratch* sc, int n) {
+  DML_GRID_WAIT();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) {
     sc->error = 0;
@@ -97,6 +98,7 @@ __device__ __forceinline__ void noalloc_fail(NoallocScratch* sc, int code, int i
 __global__ void noalloc_pairs_kernel(NoallocScratch* sc, NoallocParams p, int n_atoms, int n_ref,
                                      const double* pos, const int32_t* z, const int32_t* ref,
                                      const int32_t* nn, const int32_t* list, int ld) {
+  DML_GRID_WAIT();
   int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (r >= n_ref) return;
@@ -175,6 +177,7 @@ __global__ void noalloc_pairs_kernel(NoallocScratch* sc, NoallocParams p, int n_
 // caller's values (fuerza zeroes only hs%ref, dana.F90:1067-1073).
 // A call whose pair kernel or member marks raised an error writes nothing.
 __global__ void noalloc_sum_kernel(NoallocScratch* sc, int n_atoms, double* force, double* epot) {
+  DML_GRID_WAIT();
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n_atoms) return;
   if (*(volatile int*)&sc->error != 0) return;
@@ -226,6 +229,7 @@ __global__ void noalloc_sum_kernel(NoallocScratch* sc, int n_atoms, double* forc
 
 __global__ void noalloc_ref_mark_kernel(NoallocScratch* sc, const int32_t* ref, int n_ref,
                                         int n_atoms) {
+  DML_GRID_WAIT();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_ref) return;
   int h = ref[i];

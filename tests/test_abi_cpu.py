@@ -134,3 +134,38 @@ def test_ion_placement_errors():
         dml.random_ions(1, 10, -1.0, 10.0, 0.0, 10.0, 1.0)
     assert e.value.code == dml.E_ARG
     assert dml.random_ions(1, 0, 10.0, 10.0, 0.0, 10.0, 1.0).shape == (0, 3)
+
+
+def kernel_bodies(src):
+    """(name, first statement) of every __global__ definition in a source."""
+    out = []
+    for m in re.finditer(r"__global__", src):
+        k, depth, seen = m.end(), 0, False
+        while True:
+            c = src[k]
+            if c == "(":
+                depth, seen = depth + 1, True
+            elif c == ")":
+                depth -= 1
+            elif depth == 0 and seen and c in ";{":
+                break
+            k += 1
+        if src[k] == ";":
+            continue  # a declaration
+        head = src[m.end():k]
+        name = re.findall(r"(\w+)\s*\(", re.sub(r"__launch_bounds__\s*\([^)]*\)", "", head))[0]
+        out.append((name, src[k + 1:].lstrip().split(";", 1)[0]))
+    return out
+
+
+def test_every_graph_kernel_waits_for_its_predecessor():
+    """The step graphs' kernel-to-kernel edges are programmatic, so a kernel
+    may be launched before the one it follows has completed; each kernel
+    must begin with the grid-dependency wait before it touches memory."""
+    csrc = os.path.join(ROOT, "din-mol-li_gb300", "csrc")
+    seen = 0
+    for f in ("dml_kernels.cu", "dml_noalloc.cu"):
+        for name, first in kernel_bodies(open(os.path.join(csrc, f)).read()):
+            seen += 1
+            assert first == "DML_GRID_WAIT()", (f, name, first)
+    assert seen >= 60
