@@ -975,6 +975,8 @@ int dml_set_atoms_batch(dml_ctx* c, const dml_atoms* atoms) {
   d.nblk_part = cap / kBlock + 1;
   AL(d.part, 2 * (size_t)d.nblk_part);
   AL(d.part1, 2 * (size_t)d.nblk_part);
+  AL(d.xspan, (size_t)cap / kSpan + 1);
+  AL(d.xpart, 2 * ((size_t)cap / kSpan + 1));
   AL(d.part_cnt, 2 * (size_t)d.nblk_part);
   AL(d.dirty, (size_t)d.nblk_part);
   AL(d.sc, nrep);
@@ -1760,6 +1762,19 @@ int dml_get_scan_counts(dml_ctx* c, int32_t rep, int64_t* full, int64_t* partial
   }
   if (full) *full = (int64_t)v.sl_nfull;
   if (partial) *partial = (int64_t)v.sl_npartial;
+  return 0;
+}
+
+int dml_get_test_counts(dml_ctx* c, int32_t rep, int64_t* tests, int64_t* exact) {
+  if (!c || rep < 0 || rep >= c->D.nrep) return DML_E_ARG;
+  Scalars v;
+  std::memset(&v, 0, sizeof v);
+  if (c->loaded) {
+    CK(cudaMemcpyAsync(&v, c->D.sc + rep, sizeof v, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  if (tests) *tests = (int64_t)v.dt_tests;
+  if (exact) *exact = (int64_t)v.dt_exact;
   return 0;
 }
 

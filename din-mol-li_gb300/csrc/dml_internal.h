@@ -111,6 +111,7 @@ struct Scalars {
   int sl_mode;           // this step's scan: 1 full (flags rewritten), 0 flagged rows only
   int sl_full;           // the next scan must be full (lists rebuilt, state changed by the host)
   unsigned long long sl_nfull, sl_npartial;  // steps of each mode so far
+  unsigned long long dt_tests, dt_exact;     // displacement tests, those decided in FP64
   unsigned int ticket;   // last-block-done counters of this replica
   unsigned int ticket2;
   int rho_count;
@@ -126,6 +127,7 @@ struct Scalars {
   int halo;        // an atom sat in a halo cell at the last cell sort
   int dec;         // displacement test: 0 keep, 1 rebuild, 2 decided in FP64
   float thr;       // its FP32 candidate threshold for the FP64 top-2
+  int xbeg, xcnt;  // dec 2: its spans listed for the exact pass (Dev::xspan)
   long long next_id;
 };
 
@@ -143,6 +145,7 @@ struct Global {
   int n_cand;      // entries in the force candidate queue
   int any_rebuild; // some replica rebuilds its list this test_update
   unsigned int ticket_rep;  // replicas finished with the displacement test
+  int n_xspan;               // spans listed for the exact displacement pass
   long long list_builds;    // rebuild kernels run (some replica rebuilt)
   int near_stale;           // near lists must be searched in the overlap phase
   int n_big;                // entries of big_cells
@@ -312,6 +315,11 @@ struct Dev {
   // reductions
   unsigned long long* part;  // per-block partials (top-2, as double bits)
   int nblk_part;
+  // The displacement test's exact pass: the spans it walks (global span
+  // indices, each undecided replica's contiguous from Scalars::xbeg) and
+  // their partial top-2 (2 per listed span)
+  int* xspan;
+  unsigned long long* xpart;
   // The step's second test_update: the FP32 top-2 of every block from the
   // first one (part1, two float bit patterns per block), and the blocks
   // where overlap_moveback moved an atom since (dirty)

@@ -1624,6 +1624,8 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
       sc->rho = (double)s_c / vol;
     }
   }
+  __shared__ int s_dec;
+  __shared__ float s_thr;
   if (threadIdx.x == 0) {
     float F1 = tinyf, F2 = tinyf;
     for (int w = 0; w < nwarp; ++w) top2f(F1, F2, w1[w], w2[w]);
@@ -1635,35 +1637,72 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
     else dec = 2;
     sc->dec = dec;
     sc->thr = sqrtf(F2) - 3.0f * e;
+    sc->dt_tests += 1;
+    if (dec == 2) sc->dt_exact += 1;
     sc->ticket = 0;
     if (dec != 2) decide_rebuild(d, sc, dec);
+    s_dec = dec;
+    s_thr = sc->thr;
   }
+  __syncthreads();
+  if (s_dec != 2) return;
+  // Undecided: the exact pass walks the spans in use whose FP32 maximum
+  // reaches the threshold (an atom's rdf is at most its span's maximum, and
+  // sqrtf is correctly rounded, hence monotone), listed here contiguously.
+  const int nu = (n_slots - R.base + kSpan - 1) / kSpan;
+  int nsp = 0;
+  for (int b = threadIdx.x; b < nu; b += blockDim.x)
+    nsp += sqrtf(__uint_as_float((unsigned)__ldcg(d.part + 2 * (b0 + b)))) >= s_thr;
+  int tot;
+  const int pre = blk_scan_excl(nsp, &tot);
+  __shared__ int s_beg;
+  if (threadIdx.x == 0) {
+    s_beg = tot ? atomicAdd(&d.g->n_xspan, tot) : 0;
+    sc->xbeg = s_beg;
+    sc->xcnt = tot;
+  }
+  __syncthreads();
+  int at = s_beg + pre;
+  for (int b = threadIdx.x; b < nu; b += blockDim.x)
+    if (sqrtf(__uint_as_float((unsigned)__ldcg(d.part + 2 * (b0 + b)))) >= s_thr)
+      d.xspan[at++] = b0 + b;
 }
 
 // The replicas whose FP32 top-2 lies within the margins of the skin: the
 // exact FP64 top-2 over the candidates (sqrt(rdf) >= sqrt(F2) - 3e, which
-// holds for every atom of the exact top-2), spread over the replica's blocks
-// and merged by its last one.  Then the last replica to decide prefixes the
-// rows of the replicas that rebuild (the list build walks only those) and
-// opens the rebuild subgraph if any.
-__global__ void dispmax_exact_kernel(Dev d, KParams p, int cond,
-                                     cudaGraphConditionalHandle cond_handle) {
+// holds for every atom of the exact top-2), on a fixed grid.  First the spans
+// pbc_dispmax listed (one block per span in turn; the last span of a replica
+// merges its partials and decides), then each block counts the replicas of
+// its share that were decided without the pass.  The replica count that
+// reaches nrep makes its block the last: it prefixes the rows of the replicas
+// that rebuild (the list build walks only those) and opens the rebuild
+// subgraph if any.  With no replica undecided the launch is one short wave.
+constexpr int kExactGrid = 152 * 4;
+__global__ void __launch_bounds__(kBlock) dispmax_exact_kernel(
+    Dev d, KParams p, int cond, cudaGraphConditionalHandle cond_handle) {
   DML_GRID_WAIT();
-  const int rep = block_rep(d);
-  const RepConst& R = d.rc[rep];
-  Scalars* sc = d.sc + rep;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nwarp = blockDim.x >> 5;
-  __shared__ int s_close;  // this block closes its replica's decision
+  const unsigned long long tiny = (unsigned long long)__double_as_longlong(1.e-16);
   __shared__ unsigned long long x1[32], x2[32];
-  if (sc->dec == 2) {
+  __shared__ int s_close, s_lastrep;
+  __shared__ int s_cnt;
+  if (threadIdx.x == 0) {
+    s_lastrep = 0;
+    s_cnt = 0;
+  }
+  const int nx = d.g->n_xspan;
+  for (int t = blockIdx.x; t < nx; t += gridDim.x) {
+    const int sp = d.xspan[t];
+    const int rep = d.rep_of[sp * kSpan];
+    const RepConst& R = d.rc[rep];
+    Scalars* sc = d.sc + rep;
     const int n_slots = R.base + sc->n_slots;
     const float thr = sc->thr;
-    const unsigned long long tiny = (unsigned long long)__double_as_longlong(1.e-16);
     unsigned long long e1 = tiny, e2 = tiny;
 #pragma unroll
     for (int u = 0; u < kSlotU; ++u) {
-      const int q = span_pos(u);
+      const int q = sp * kSpan + u * kBlock + (int)threadIdx.x;
       if (q < n_slots && d.state[q] == ST_LIVE) {
         const float rdf = disp2f(d.posf[q], d.posf_old[q]);
         if (rdf == rdf && sqrtf(rdf) >= thr) {
@@ -1686,19 +1725,20 @@ __global__ void dispmax_exact_kernel(Dev d, KParams p, int cond,
     if (threadIdx.x == 0) {
       unsigned long long f1 = tiny, f2 = tiny;
       for (int w = 0; w < nwarp; ++w) top2_merge(f1, f2, x1[w], x2[w]);
-      d.part[2 * blockIdx.x] = f1;
-      d.part[2 * blockIdx.x + 1] = f2;
+      d.xpart[2 * t] = f1;
+      d.xpart[2 * t + 1] = f2;
       __threadfence();
-      const unsigned t = atomicAdd(&sc->ticket, 1u);
-      s_close = t == (unsigned)R.nblk - 1u;
+      const unsigned tk = atomicAdd(&sc->ticket, 1u);
+      s_close = tk == (unsigned)sc->xcnt - 1u;
     }
     __syncthreads();
     if (s_close) {
+      // the replica's last listed span: its partials merged, the decision
       __threadfence();
       unsigned long long f1 = tiny, f2 = tiny;
-      const int b0 = R.base / kSpan;
-      for (int b = b0 + threadIdx.x; b < b0 + R.nblk; b += blockDim.x)
-        top2_merge(f1, f2, __ldcg(d.part + 2 * b), __ldcg(d.part + 2 * b + 1));
+      const int xb = sc->xbeg, xc = sc->xcnt;
+      for (int b = xb + threadIdx.x; b < xb + xc; b += blockDim.x)
+        top2_merge(f1, f2, __ldcg(d.xpart + 2 * b), __ldcg(d.xpart + 2 * b + 1));
       for (int off = 16; off > 0; off >>= 1) {
         unsigned long long c1 = __shfl_down_sync(0xffffffffu, f1, off);
         unsigned long long c2 = __shfl_down_sync(0xffffffffu, f2, off);
@@ -1717,18 +1757,33 @@ __global__ void dispmax_exact_kernel(Dev d, KParams p, int cond,
         const double d2 = __longlong_as_double((long long)g2);
         decide_rebuild(d, sc, sqrt(d1) + sqrt(d2) > p.skin ? 1 : 0);
         sc->ticket = 0;
+        s_cnt += 1;
       }
     }
-  } else {
-    if (threadIdx.x == 0) s_close = blockIdx.x * kSpan == R.base;  // the replica's first block
     __syncthreads();
   }
-  if (!s_close) return;
-  __shared__ int s_lastrep;
-  if (threadIdx.x == 0) {
+  // the replicas of this block's share decided without the exact pass (an
+  // undecided replica with no listed span has no candidate: its exact top-2
+  // is empty)
+  int cnt = 0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < d.nrep; r += gridDim.x * blockDim.x) {
+    Scalars* sc = d.sc + r;
+    if (sc->dec != 2) {
+      ++cnt;
+    } else if (sc->xcnt == 0) {
+      const double t1 = __longlong_as_double((long long)tiny);
+      decide_rebuild(d, sc, sqrt(t1) + sqrt(t1) > p.skin ? 1 : 0);
+      ++cnt;
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, off);
+  __syncthreads();
+  if (lane == 0 && cnt) atomicAdd(&s_cnt, cnt);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_cnt) {
     __threadfence();
-    unsigned t2 = atomicAdd(&d.g->ticket_rep, 1u);
-    s_lastrep = t2 == (unsigned)d.nrep - 1u;
+    const unsigned t2 = atomicAdd(&d.g->ticket_rep, (unsigned)s_cnt);
+    s_lastrep = t2 + (unsigned)s_cnt == (unsigned)d.nrep;
   }
   __syncthreads();
   if (!s_lastrep) return;
@@ -1796,6 +1851,7 @@ __global__ void dispmax_exact_kernel(Dev d, KParams p, int cond,
     d.rebc_pre[d.nrep] = carry2;
     int any = atomicAdd(&d.g->any_rebuild, 0);
     d.g->ticket_rep = 0;
+    d.g->n_xspan = 0;  // every listed span has been walked
     if (any) d.g->near_stale = 1;  // lists change: the near entries too
     if (cond) cudaGraphSetConditional(cond_handle, any ? 1u : 0u);
   }
@@ -5797,7 +5853,7 @@ int k_ermak_b(const Dev& d, const KParams& p, int n_rank, cudaStream_t s) {
 
 int k_pbc_dispmax(const Dev& d, const KParams& p, int n_slots, cudaStream_t s, bool second) {
   pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots, second ? 1 : 0);
-  dispmax_exact_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, 0, 0);
+  dispmax_exact_kernel<<<kExactGrid, kBlock, 0, s>>>(d, p, 0, 0);
   return 2;
 }
 
@@ -5809,7 +5865,7 @@ int k_test_update(const Dev& d, const KParams& p, int n_slots, int n_b, int n_ra
 int k_pbc_dispmax_cond(const Dev& d, const KParams& p, int n_slots,
                        cudaGraphConditionalHandle h, cudaStream_t s, bool second) {
   pbc_dispmax_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, n_slots, second ? 1 : 0);
-  dispmax_exact_kernel<<<nspan(n_slots), kBlock, 0, s>>>(d, p, 1, h);
+  dispmax_exact_kernel<<<kExactGrid, kBlock, 0, s>>>(d, p, 1, h);
   return 2;
 }
 

@@ -102,6 +102,7 @@ def lib():
     L.dml_get_gcmc_paths.argtypes = [vp, i32, P(i64), P(i64)]
     L.dml_get_scan_counts.argtypes = [vp, i32, P(i64), P(i64)]
     L.dml_set_scan_lanes.argtypes = [vp, i32]
+    L.dml_get_test_counts.argtypes = [vp, i32, P(i64), P(i64)]
     _lib = L
     return L
 
@@ -434,6 +435,13 @@ class Simulation:
         a, b = ctypes.c_int64(), ctypes.c_int64()
         self._check(self.lib.dml_get_scan_counts(self.h, replica, ctypes.byref(a),
                                                   ctypes.byref(b)), "dml_get_scan_counts")
+        return a.value, b.value
+
+    def test_counts(self, replica=0):
+        """(displacement tests, those decided by the exact FP64 pass) of a replica."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        self._check(self.lib.dml_get_test_counts(self.h, replica, ctypes.byref(a),
+                                                  ctypes.byref(b)), "dml_get_test_counts")
         return a.value, b.value
 
     def set_scan_lanes(self, lanes):

@@ -361,6 +361,12 @@ int dml_get_gcmc_paths(dml_ctx* c, int32_t rep, int64_t* parallel, int64_t* sequ
  * a GCMC or fixed reservoir.  Either pointer may be NULL. */
 int dml_get_scan_counts(dml_ctx* c, int32_t rep, int64_t* full, int64_t* partial);
 
+/* Diagnostic (no counterpart in the reference): how many displacement tests
+ * (test_update's inq_dispmax, src/Neighbor.F90:635-666) replica `rep` ran
+ * and how many of them the FP32 top-2 left within its error margin of the
+ * skin, so that the exact FP64 pass decided.  Either pointer may be NULL. */
+int dml_get_test_counts(dml_ctx* c, int32_t rep, int64_t* tests, int64_t* exact);
+
 /* Lanes per neighbour-list row of the force scan (1, 2, 4, 8, 16 or 32), or
  * 0 to let the autotuner choose when the step graph is next built (the
  * default).  The step graph is built again at the next step.  Returns 0 or

@@ -106,6 +106,26 @@ def test_uneven_batch_matches_oracle_per_replica(integrator):
     assert g.counters()["nupd"] >= 4  # every replica built its list
 
 
+def test_many_replicas_exact_displacement_pass():
+    """160 replicas: the displacement test's exact FP64 pass runs one block
+    per replica (more than 152 replicas), and every replica whose FP32 top-2
+    lands within the margin of the skin must decide as the oracle does.
+    Skin 1 A, so lists are rebuilt several times in 150 steps."""
+    p = systems.c1_params(reservoir=dml.RESERVOIR_NONE)
+    p.skin = 1.0
+    reps = [dml.replica_of(p, box=[21.06, 21.06, 60.0], seed=500 + r) for r in range(160)]
+    atoms = [systems.slab_system(6, 6, 2, 60.0, 60, 10.0, 60.0, 300 + r, dmin=3.2)
+             for r in range(160)]
+    g, orcs = run_batch_vs_oracles(p, reps, atoms, [1, 49, 100])
+    tests = exact = 0
+    for r in range(160):
+        t, e = g.test_counts(replica=r)
+        tests += t
+        exact += e
+        assert g.counters(replica=r)["nupd"] == orcs[r].counters()["nupd"]
+    assert tests >= 160 * 300 and exact > 0, (tests, exact)
+
+
 def test_batch_capture_events():
     """Ions next to the electrode, Brownian, no reservoir: captures happen in
     every replica and match the oracle per replica."""

@@ -97,6 +97,8 @@ def test_config5_replicas_full_size():
         assert par == done and seq == 0, (r, par, seq)
         full, partial = g.scan_counts(replica=r)
         assert full + partial == done and partial > 0, (r, full, partial)
+    # the exact displacement pass, several blocks per replica (two replicas)
+    assert sum(g.test_counts(replica=r)[1] for r in range(2)) > 0
     g.close()
 
 
@@ -144,6 +146,9 @@ def test_config1_full_run():
         _, c = check_state(g, o, "c1 after %d steps" % (1000 * (k + 1)))
     check_lists(g, o, "c1 end", p.mnb)
     assert c["step"] == 10000 and c["depo"] > 0 and c["nupd"] > 1
+    # the exact displacement pass, one replica spread over many blocks
+    tests, exact = g.test_counts()
+    assert tests >= 20000 and exact > 0, (tests, exact)
     g.close()
 
 
