@@ -1451,13 +1451,17 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
+  // the spans in use take part (the first one always, so that every replica
+  // decides); a block past them leaves at once
+  const int b0 = R.base / kSpan;
+  const int nu = max(1, (n_slots - R.base + kSpan - 1) / kSpan);
+  if ((int)blockIdx.x - b0 >= nu) return;
   const float tinyf = 1e-16f;
   const float e = R.margin;
   float a1 = tinyf, a2 = tinyf;
   // The loads of all the thread's positions are issued together: a slot is
   // live exactly when its FP32 copy carries an element (w != 0; limbo and
-  // free slots hold 0), so no state load has to come first.  Blocks past
-  // the replica's slots in use only take part in the reduction.
+  // free slots hold 0), so no state load has to come first.
   bool live[kSlotU];
   float4 Pfu[kSlotU], Ofu[kSlotU];
   bool used = (int)blockIdx.x * kSpan < n_slots;
@@ -1588,15 +1592,14 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
     }
     __threadfence();
     unsigned t = atomicAdd(&sc->ticket, 1u);
-    last = (t == (unsigned)R.nblk - 1u);
+    last = (t == (unsigned)nu - 1u);
   }
   __syncthreads();
   if (!last) return;
   __threadfence();
   // last block of this replica: FP32 top-2 over the replica's partials
   float b1 = tinyf, b2 = tinyf;
-  const int b0 = R.base / kSpan;
-  for (int b = b0 + threadIdx.x; b < b0 + R.nblk; b += blockDim.x)
+  for (int b = b0 + threadIdx.x; b < b0 + nu; b += blockDim.x)
     top2f(b1, b2, __uint_as_float((unsigned)__ldcg(d.part + 2 * b)),
           __uint_as_float((unsigned)__ldcg(d.part + 2 * b + 1)));
   for (int off = 16; off > 0; off >>= 1) {
@@ -1615,7 +1618,7 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
     if (threadIdx.x == 0) s_c = 0;
     __syncthreads();
     int c = 0;
-    for (int b = b0 + threadIdx.x; b < b0 + R.nblk; b += blockDim.x)
+    for (int b = b0 + threadIdx.x; b < b0 + nu; b += blockDim.x)
       c += __ldcg(d.part_cnt + 2 * b + 1);
     if (c) atomicAdd(&s_c, c);
     __syncthreads();
@@ -1649,7 +1652,6 @@ __global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p
   // Undecided: the exact pass walks the spans in use whose FP32 maximum
   // reaches the threshold (an atom's rdf is at most its span's maximum, and
   // sqrtf is correctly rounded, hence monotone), listed here contiguously.
-  const int nu = (n_slots - R.base + kSpan - 1) / kSpan;
   int nsp = 0;
   for (int b = threadIdx.x; b < nu; b += blockDim.x)
     nsp += sqrtf(__uint_as_float((unsigned)__ldcg(d.part + 2 * (b0 + b)))) >= s_thr;
@@ -2712,6 +2714,7 @@ __device__ __forceinline__ void overlap_count_at(Dev d, int n_rank, int rep, int
 __global__ void overlap_count_kernel(Dev d, int n_rank) {
   DML_GRID_WAIT();
   const int rep = block_rep(d);
+  if ((int)blockIdx.x * kSpan >= d.rc[rep].base + d.sc[rep].n_slots) return;
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) overlap_count_at(d, n_rank, rep, span_pos(u));
 }
@@ -3101,12 +3104,24 @@ __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
   const RepConst& R = d.rc[rep];
   Scalars* sc = d.sc + rep;
   n_slots = R.base + sc->n_slots;  // positions in use end here
+  // the spans in use take part (the first one always); a block past them
+  // leaves at once
+  const int nu = max(1, (n_slots - R.base + kSpan - 1) / kSpan);
+  if ((int)blockIdx.x - R.base / kSpan >= nu) return;
   double z0 = sc->z0;
   double zt = p.ztop_is_z1 != 0.0 ? sc->z1 : sc->zmax;
   // z > z0 && z < zt from the FP32 copy zf = RN32(z) (monotone rounding:
   // zf beyond RN32 of a bound decides), FP64 when zf equals one (or NaN);
-  // a slot is live exactly when its FP32 copy carries an element
-  const float z0f = (float)z0, ztf = (float)zt;
+  // a slot is live exactly when its FP32 copy carries an element.  The
+  // bounds' FP32 copies are formed once per block (conversions issue on the
+  // narrow FP64 pipe).
+  __shared__ float s_z0f, s_ztf;
+  if (threadIdx.x == 0) {
+    s_z0f = (float)z0;
+    s_ztf = (float)zt;
+  }
+  __syncthreads();
+  const float z0f = s_z0f, ztf = s_ztf;
   const bool used = (int)blockIdx.x * kSpan < n_slots;
   float4 Pf[kSlotU];
 #pragma unroll
@@ -3138,7 +3153,7 @@ __global__ void calc_rho_kernel(Dev d, KParams p, int n_slots) {
     if (c) atomicAdd(&sc->rho_count, c);
     __threadfence();
     unsigned t = atomicAdd(&sc->ticket2, 1u);
-    last = (t == (unsigned)R.nblk - 1u);  // the replica's last block
+    last = (t == (unsigned)nu - 1u);  // the replica's last block
   }
   __syncthreads();
   if (last && threadIdx.x == 0) {
