@@ -3666,6 +3666,10 @@ __global__ void gcmc_bin_kernel(Dev d, int par) {
   DML_GRID_WAIT();
   const int rep = block_rep(d);
   if (blockIdx.x == 0 && threadIdx.x == 0) d.g->n_big = 0;  // cell_order's list
+  // a block past the slots in use (and, with the parallel trials, past the
+  // gcmc%alist positions in use) has nothing to bin or to mark
+  const int lim = max(d.sc[rep].n_slots, par ? d.grp[rep].ng : 0);
+  if ((int)blockIdx.x * kSpan - d.rc[rep].base >= lim) return;
 #pragma unroll
   for (int u = 0; u < kSlotU; ++u) gcmc_bin_at(d, rep, span_pos(u), par);
   if (par) gcmc_member_words(d, rep);
