@@ -2403,15 +2403,28 @@ __device__ __forceinline__ int list_cells_row_thread(const Dev& d, const KParams
   }
   int* row = d.list + (size_t)h * p.mnb;
   int cnt = 0;
-#pragma unroll 1
-  for (int q = 0; q < 27; ++q) {
+  // The bounds of all 27 stencil cells first, their loads issued together
+  // (a bit per non-empty cell), then the non-empty cells in map order: most
+  // cells of a sparse replica are empty, and walking them one by one put a
+  // load latency per cell on the row's chain.
+  auto stencil_cell = [&](int q) {
     int nc[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const int o = map_off(q, k);
       nc[k] = o < 0 ? wm[k] : (o == 0 ? w0[k] : wp[k]);
     }
-    const int c = R.cell_off + (nc[2] * R.head_dim[1] + nc[1]) * R.head_dim[0] + nc[0];
+    return R.cell_off + (nc[2] * R.head_dim[1] + nc[1]) * R.head_dim[0] + nc[0];
+  };
+  unsigned ne = 0u;
+#pragma unroll
+  for (int q = 0; q < 27; ++q) {
+    const int c = stencil_cell(q);
+    if (d.cell_start[c + 1] > d.cell_start[c]) ne |= 1u << q;
+  }
+#pragma unroll 1
+  for (; ne != 0u; ne &= ne - 1u) {
+    const int c = stencil_cell(__ffs(ne) - 1);
     const int en = d.cell_start[c + 1];
 #pragma unroll 1
     for (int i = d.cell_start[c]; i < en; ++i) {
