@@ -2866,15 +2866,27 @@ __device__ void overlap_exam(const Dev& d, const KParams& p, int x, int pass, in
   int nc = d.near_count[x];
   int n = nc >= 0 ? nc : d.nn[x];
   const int* src = nc >= 0 ? d.near + (size_t)x * kNearCap : d.list + (size_t)x * p.mnb;
+  // x's own position changes only where the walk ends (its near entries
+  // never hold x), so it is read once
+  const double4 P = d.pos[x];
+  const float4 Pf = d.posf[x];
   for (int q = 0; q < n; ++q) {
     int j = src[q];
     if (d.state[j] != ST_LIVE) continue;
-    double4 P = d.pos[x];
+    // |P - Q|^2 > rc^2 decided from the FP32 copies outside the margins
+    // (a NaN distance takes the FP64 test, as in the reference it passes)
+    const float4 Qf = d.posf[j];
+    float fx, fy, fz;
+    vdist_nint_f(R, Pf, Qf, fx, fy, fz);
+    const float df = fx * fx + fy * fy + fz * fz;
+    if (df > R.rc_hi2) continue;
     double4 Q = d.pos[j];
-    double vx, vy, vz;
-    vdist_nint(R, P, Q, vx, vy, vz);
-    double dr = dot3(vx, vy, vz);
-    if (dr > p.rc2) continue;
+    if (!(df < R.rc_lo2)) {
+      double vx, vy, vz;
+      vdist_nint(R, P, Q, vx, vy, vz);
+      double dr = dot3(vx, vy, vz);
+      if (dr > p.rc2) continue;
+    }
     if (d.typ[j] == DML_Z_CG) {
       count_add(&sc->try_, 1ull);
       double ne = dml_uniform(dml_draw(R.seed, d.g->step, (uint64_t)d.id[x], DML_RNG_OVERLAP,
