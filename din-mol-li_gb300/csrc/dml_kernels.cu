@@ -2422,31 +2422,48 @@ __device__ __forceinline__ int list_cells_row_thread(const Dev& d, const KParams
     const int c = stencil_cell(q);
     if (d.cell_start[c + 1] > d.cell_start[c]) ne |= 1u << q;
   }
+  // The candidates of the non-empty cells (map order, chain order within a
+  // cell) as one stream: while candidate k is tested, the FP32 position of
+  // k + 1 and the hs slot of k + 2 are loaded, so that the stream waits on
+  // one load latency per candidate instead of two.
+  int fi = 0, fe = 0;  // the next stream position to fetch: cell_atoms[fi], fi < fe
+  auto fetch = [&]() -> int {
+    if (fi >= fe) {
+      if (ne == 0u) return -1;
+      const int c = stencil_cell(__ffs(ne) - 1);
+      ne &= ne - 1u;
+      fi = d.cell_start[c];
+      fe = d.cell_start[c + 1];
+    }
+    return d.cell_atoms[fi++];  // hs slot
+  };
+  int j1 = fetch();
+  int j2 = j1 >= 0 ? fetch() : -1;
+  float4 Q1 = j1 >= 0 ? d.posf[j1] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
-  for (; ne != 0u; ne &= ne - 1u) {
-    const int c = stencil_cell(__ffs(ne) - 1);
-    const int en = d.cell_start[c + 1];
-#pragma unroll 1
-    for (int i = d.cell_start[c]; i < en; ++i) {
-      const int j = d.cell_atoms[i];  // hs slot
-      if (j == h) continue;
-      const float4 Q = d.posf[j];
+  while (j1 >= 0) {
+    const int j3 = j2 >= 0 ? fetch() : -1;
+    const float4 Q2 = j2 >= 0 ? d.posf[j2] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (j1 != h) {
       float fx, fy, fz;
-      vdist_nint_f(R, Q, Pf, fx, fy, fz);
+      vdist_nint_f(R, Q1, Pf, fx, fy, fz);
       const float drf = fx * fx + fy * fy + fz * fz;
       bool inc = false;
       if (drf < R.rlist_lo2) {
         inc = true;
       } else if (drf <= R.rlist_hi2) {
         double vx, vy, vz;
-        vdist_nint(R, d.pos[j], P, vx, vy, vz);
+        vdist_nint(R, d.pos[j1], P, vx, vy, vz);
         inc = dot3(vx, vy, vz) < p.rlist2;
       }
       if (inc) {
-        if (cnt < p.mnb) row[cnt] = j;
+        if (cnt < p.mnb) row[cnt] = j1;
         ++cnt;
       }
     }
+    j1 = j2;
+    Q1 = Q2;
+    j2 = j3;
   }
   if (cnt > p.mnb) {
     raise_error(d.g, DML_E_NEIGH_OVERFLOW, h);
