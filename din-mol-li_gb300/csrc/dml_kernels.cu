@@ -809,16 +809,26 @@ __device__ __forceinline__ bool force_scan_row(const Dev& d, const KParams& p, i
   int ncnt = 0;
   bool any = false, flag = false;
   const unsigned lt = (1u << lane) - 1u;
+  // The entries of the next batch are loaded while this batch's positions
+  // are, so that a batch waits on one load latency instead of two.
+  int jn[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int jj = L * u + sl;
+    jn[u] = jj < n ? __ldg(row + jj) : -1;
+  }
   for (int base = 0; base < nmax; base += STEP) {
     int j[U];
     float4 Q[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      int jj = base + L * u + sl;
-      j[u] = jj < n ? __ldg(row + jj) : -1;
-    }
+    for (int u = 0; u < U; ++u) j[u] = jn[u];
 #pragma unroll
     for (int u = 0; u < U; ++u) Q[u] = j[u] >= 0 ? d.posf[j[u]] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int jj = base + STEP + L * u + sl;
+      jn[u] = jj < n ? __ldg(row + jj) : -1;
+    }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       // one FP32 minimum-image distance serves both tests; the element of
