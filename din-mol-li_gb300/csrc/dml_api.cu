@@ -578,7 +578,7 @@ int autotune_scan(dml_ctx* c) {
     sl = c->forced_lanes > 0 ? c->forced_lanes : sweep(false, c->tune_us);
     nl = sl < 0 ? -1 : sweep(true, nullptr);
   } else {
-    nl = sweep(true, c->tune_us);
+    nl = c->forced_lanes > 0 ? c->forced_lanes : sweep(true, c->tune_us);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

@@ -367,10 +367,11 @@ int dml_get_scan_counts(dml_ctx* c, int32_t rep, int64_t* full, int64_t* partial
  * skin, so that the exact FP64 pass decided.  Either pointer may be NULL. */
 int dml_get_test_counts(dml_ctx* c, int32_t rep, int64_t* tests, int64_t* exact);
 
-/* Lanes per neighbour-list row of the force scan (1, 2, 4, 8, 16 or 32), or
- * 0 to let the autotuner choose when the step graph is next built (the
- * default).  The step graph is built again at the next step.  Returns 0 or
- * DML_E_ARG. */
+/* Lanes per neighbour-list row of the force scan (1, 2, 4, 8, 16 or 32;
+ * with the Brownian integrator, which has no force scan, of overlap_moveback's
+ * near-contact search), or 0 to let the autotuner choose when the step graph
+ * is next built (the default).  The step graph is built again at the next
+ * step.  Returns 0 or DML_E_ARG. */
 int dml_set_scan_lanes(dml_ctx* c, int32_t lanes);
 
 /* One replica's atoms and neighbour lists (same layout as dml_get_atoms and
