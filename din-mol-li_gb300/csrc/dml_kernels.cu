@@ -2483,7 +2483,7 @@ __device__ __forceinline__ int list_cells_row_thread(const Dev& d, const KParams
   return cnt;
 }
 
-__global__ void __launch_bounds__(256) list_cells_thread_kernel(Dev d, KParams p) {
+__global__ void __launch_bounds__(256, 5) list_cells_thread_kernel(Dev d, KParams p) {
   DML_GRID_WAIT();
   const int total = d.reb_pre[d.nrep];  // rows of the replicas that rebuild
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
