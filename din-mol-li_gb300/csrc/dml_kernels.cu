@@ -1453,7 +1453,7 @@ __device__ __forceinline__ void decide_rebuild(const Dev& d, Scalars* sc, int re
 // displacements of the first test_update, so it reuses that call's FP32
 // top-2 (or, in a replica whose list the first call rebuilt, pos_old = pos
 // and every displacement is 0).  Dirty blocks are recomputed in full.
-__global__ void __launch_bounds__(kBlock, 4) pbc_dispmax_kernel(Dev d, KParams p, int n_slots,
+__global__ void __launch_bounds__(kBlock, 6) pbc_dispmax_kernel(Dev d, KParams p, int n_slots,
                                                                  int second) {
   DML_GRID_WAIT();
   // grids are sized by capacity; the block's replica gives the live count
@@ -3714,7 +3714,7 @@ __device__ __forceinline__ void gcmc_member_words(const Dev& d, int rep) {
   }
 }
 
-__global__ void gcmc_bin_kernel(Dev d, int par) {
+__global__ void __launch_bounds__(kBlock, 6) gcmc_bin_kernel(Dev d, int par) {
   DML_GRID_WAIT();
   const int rep = block_rep(d);
   if (blockIdx.x == 0 && threadIdx.x == 0) d.g->n_big = 0;  // cell_order's list
