@@ -2711,7 +2711,7 @@ __device__ __forceinline__ void overlap_detect_rows(const Dev& d, const KParams&
 // mode 0: every replica; 1: only if some list was rebuilt since the force
 // scan, for the replicas that rebuilt; 2: the replicas that rebuilt.
 template <int L>
-__global__ void __launch_bounds__(256) overlap_detect_kernel(Dev d, KParams p, int mode) {
+__global__ void __launch_bounds__(256, 8) overlap_detect_kernel(Dev d, KParams p, int mode) {
   DML_GRID_WAIT();
   if (mode == 1 && !d.g->near_stale) return;  // the force scan found them
   const int nw = gridDim.x * (blockDim.x >> 5);
